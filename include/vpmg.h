@@ -1,0 +1,159 @@
+/*
+ * vpmg.h -- C-ABI of the GB300 (sm_103a) particle-mesh step library.
+ *
+ * Drop-in boundary for vpm_free's hot path: the Fortran host keeps its
+ * `vpm(...)` driver call, pm.inp and particle arrays, and binds these entry
+ * points through iso_c_binding (see vpm_free_gb300/fortran/).  Plain C
+ * types only; every call returns an int status (0 = OK, < 0 = error, see
+ * vpmg_status) and never aborts the process.  All arithmetic is FP64.
+ *
+ * Array conventions follow the reference (Fortran column-major):
+ *   XP(3,NVRM)  positions            -> double xp[ld*3], xp[3*p + d]
+ *   QP(4,NVRM)  -omega*vol, volume   -> double qp[ld*4], qp[4*p + c]
+ *   UP(3,NVRM), GP(3,NVRM) outputs
+ *   fields (neq, NX, NY, NZ)         -> here one array per component,
+ *                                       x fastest: f[c][i + NX*(j + NY*k)]
+ * A handle owns one CUDA stream and its device memory; calls on one handle
+ * must not overlap, calls on different handles may.
+ */
+#ifndef VPMG_H
+#define VPMG_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum vpmg_status {
+  VPMG_OK = 0,
+  VPMG_ERR_ARG = -1,          /* bad argument / size                              */
+  VPMG_ERR_CUDA = -2,         /* CUDA runtime error (message via vpmg_last_error) */
+  VPMG_ERR_NOMEM = -3,        /* device allocation failed                          */
+  VPMG_ERR_OUTSIDE = -4,      /* a particle stencil leaves the mesh                */
+  VPMG_ERR_CAPACITY = -5,     /* remesh produced more particles than capacity      */
+  VPMG_ERR_UNSUPPORTED = -6,  /* option outside the single-block 3-D path          */
+  VPMG_ERR_STATE = -7,        /* call order (e.g. step before define_sizes)        */
+  VPMG_ERR_TREE = -8          /* quadtree inconsistency (pinfdomain.f90:1516)      */
+} vpmg_status;
+
+/* pm.inp (source/vpm.f90:132-152 reads it positionally) + explicit box. */
+typedef struct vpmg_config {
+  double dpm[3];        /* DXpm DYpm DZpm                         pm.inp:1  */
+  int interf_iproj;     /* projection function (2,3,4,5,6; 4=M4') pm.inp:2  */
+  int ibctyp;           /* 2: infinite-domain sources             pm.inp:3  */
+  int idvpm;            /* 1: constant volume                     pm.inp:4  */
+  double epsvol;        /*                                        pm.inp:5  */
+  int ncoarse;          /* coarse/fine ratio of YAPS              pm.inp:6  */
+  int nbi, nbj, nbk;    /* blocks (1 1 1 on one GPU)              pm.inp:7  */
+  int nremesh, ncell_rem; /*                                      pm.inp:8  */
+  int iyntree, ilevmax; /* quadtree on/off, levels                pm.inp:9  */
+  int ompthreads;       /* ignored (host threads)                 pm.inp:10 */
+  int idefine;          /* 1: box frozen after step 0             pm.inp:11 */
+  int iynslice;         /* writer option (ignored)                pm.inp:12 */
+  int use_box;          /* 1: box[] is the global mesh (no shrink-wrap)     */
+  double box[6];        /* XMIN YMIN ZMIN XMAX YMAX ZMAX                    */
+} vpmg_config;
+
+/* Mesh descriptors of define_sizes (source/vpm.f90:477-660), one block. */
+typedef struct vpmg_sizes {
+  double xbound[6], dpm[3];
+  int nn[3], nn_bl[6];
+  double xbound_bl[6];
+  int nnbl[3], nnbl_bl[6];
+  double xbound_coarse[6], dpm_coarse[3];
+  int nn_coarse[3], nn_bl_coarse[6];
+  int ilevmax;
+  double dvpm;
+  int defined;
+} vpmg_sizes;
+
+typedef struct vpmg_handle vpmg_handle;
+
+/* ---- configuration ------------------------------------------------------ */
+/* Parses pm.inp with the reference's positional reads (vpm.f90:132-152).   */
+int vpmg_read_pm_inp(const char* path, vpmg_config* cfg);
+
+/* ---- handle ------------------------------------------------------------- */
+/* device < 0 keeps the current device.  Replaces the module state of
+ * vpm_lib (source/vpm.f90:1-32) with an explicit handle.                   */
+int vpmg_create(const vpmg_config* cfg, int device, vpmg_handle** out);
+int vpmg_destroy(vpmg_handle* h);
+const char* vpmg_last_error(const vpmg_handle* h);
+const char* vpmg_status_string(int status);
+
+/* ---- the reference's driver call --------------------------------------- */
+/* vpm(XP,QP,UP,GP,NVR,neqpm,WhatToDo,RHS_pm,velx,vely,velz,NTIME,NI,NVRM)
+ * (source/vpm.f90:54-475).  WhatToDo 0 = read sizes (define_sizes, with
+ * the pm.inp already given to vpmg_create), 2 = field step: UP is
+ * overwritten with the interpolated velocity and GP with the stretching
+ * term times the particle volume (vpm_time.f90:62-107).  neqpm must be 3.
+ * Host pointers; the copies to and from the device happen inside.          */
+int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int* nvr, int neqpm,
+             int whattodo, int ntime, double ni, int nvrm);
+
+/* remesh_particles_3d(1) (source/vpm_remesh.f90:5-225), ncell_rem = 1.
+ * Reads *nvr particles from xp/qp (leading dimension = capacity) and
+ * overwrites them with the new set; *nvr = new count.  If the new count
+ * exceeds capacity nothing is written, *nvr holds the required count and
+ * VPMG_ERR_CAPACITY is returned (the reference reallocates XPR/QPR).       */
+int vpmg_remesh_particles_3d(vpmg_handle* h, int iflag, double* xp, double* qp, int* nvr, int capacity);
+
+/* ---- the reference's single-block library calls ------------------------ */
+/* pmesh(SOL,RHS,...,Xbound,Dpm,NN,NN_bl,...,ibctyp,neqs,neqf,iynbc,NVR,itree,levmax)
+ * (source/pmlib.f90:69-192), 3-D, ibctyp = 2, neqs = 1, neqf = 3.
+ * sol/rhs: 3 host arrays of NN[0]*NN[1]*NN[2] doubles each.              */
+int vpmg_pmesh(vpmg_handle* h, double* const sol[3], const double* const rhs[3], const double xbound[6],
+               const double dpm[3], const int nn[3], const int nn_bl[6], int iynbc, int itree, int levmax);
+
+/* project_particles_3D + project_vol3d(IDVPM=1) (source/pmproject.f90:43-153)
+ * on the mesh of the last define_sizes: rhs[c] = sum_p W(x)W(y)W(z) QP(c,p) / DVpm. */
+int vpmg_project_particles_3d(vpmg_handle* h, const double* xp, const double* qp, int nvr,
+                              double* const rhs[3]);
+
+/* ---- device-resident loop (test.f90:83-150 without the AVATAR inflow) -- */
+int vpmg_define_sizes(vpmg_handle* h, const double* xp, int nvr, int ntime);
+int vpmg_get_sizes(const vpmg_handle* h, vpmg_sizes* out);
+/* Upload particles to the handle's device arrays (capacity particles).    */
+int vpmg_set_particles(vpmg_handle* h, const double* xp, const double* qp, int nvr, int capacity);
+int vpmg_get_particles(vpmg_handle* h, double* xp, double* qp, int* nvr, int capacity);
+int vpmg_get_particle_velocity(vpmg_handle* h, double* up, double* gp, int nvr);
+/* One device-resident step on the uploaded particles: field step
+ * (WhatToDo = 2), forward Euler (test.f90:104-117) and, if remesh != 0,
+ * remesh_particles_3d(1).  No host copies of particle data.             */
+int vpmg_step(vpmg_handle* h, double dt, const double uinf[3], int remesh);
+int vpmg_remesh_device(vpmg_handle* h);
+int vpmg_num_particles(const vpmg_handle* h, int* nvr);
+
+/* Field ids for vpmg_get_field. */
+enum {
+  VPMG_F_RHS = 0,      /* RHS_pm(1:3) after project_vol3d            3 x N  */
+  VPMG_F_SOL = 1,      /* SOL_pm (vector potential) after solget_3d  3 x N  */
+  VPMG_F_VEL = 2,      /* velvr[xyz]_pm                             3 x N  */
+  VPMG_F_DEF = 3,      /* stretching (SOL_pm after calc_velocity)   3 x N  */
+  VPMG_F_BL_SOL1 = 4,  /* block after the infinite-domain solve     3 x Nb */
+  VPMG_F_COARSE_RHS = 5,
+  VPMG_F_COARSE_SOL = 6,
+  VPMG_F_BL_FINAL = 7  /* block after the final Dirichlet solve     3 x Nb */
+};
+/* Copies 3 components (back to back) of a resident field into out.
+ * *count = elements per component.                                      */
+int vpmg_get_field(vpmg_handle* h, int which, double* out, size_t capacity, size_t* count);
+
+/* ---- instrumentation --------------------------------------------------- */
+/* Number of kernels launched by this handle since creation.              */
+long long vpmg_kernel_launches(const vpmg_handle* h);
+/* Per-phase device milliseconds of the last vpmg_step (CUDA events):
+ * [0] deposit, [1] fine zero-BC solve, [2] boundary values, [3] fine BC
+ * solve, [4] coarse, [5] final solve, [6] FD, [7] M2P+Euler, [8] remesh. */
+int vpmg_phase_times(const vpmg_handle* h, double ms[9]);
+/* Boundary-operator statistics: interactions per fine solve, bytes held. */
+int vpmg_tree_stats(const vpmg_handle* h, long long* interactions, long long* bytes, int* precomputed);
+/* Turns per-phase event timing on/off (default off). */
+int vpmg_set_profiling(vpmg_handle* h, int on);
+/* Memory limit (bytes) for the precomputed boundary operator; 0 = never
+ * precompute (walk the tree every step).  Default: 100 GiB.              */
+int vpmg_set_operator_budget(vpmg_handle* h, long long bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,96 @@
+"""Whole-step parity (vpm WhatToDo = 2, Euler, remesh) vs the oracle.
+
+Fields: relative L2 <= 1e-10 (vorticity/RHS, vector potential, velocity,
+stretching); particles: relative L2 <= 1e-9 (positions, strengths).
+"""
+import numpy as np
+import pytest
+
+from helpers import configs_for, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-10
+PART_TOL = 1e-9
+
+
+def _pairs(V, O):
+    return [("rhs", O.F_RHS), ("sol", O.F_SOL), ("vel", O.F_VEL), ("def", O.F_DEF)]
+
+
+@pytest.mark.parametrize("ncell", [32, 48])
+def test_step_fields_match_oracle(gpulib, oracle, ncell):
+    from vpm_free_gb300 import workloads as W
+    V, O = gpulib, oracle
+    xp, qp, w = W.scaled_ring(ncell)
+    ocfg, gcfg = configs_for(w)
+    s = O.define_sizes(ocfg, xp)
+    up_o, gp_o = O.step_fields(ocfg, s, xp, qp)
+    with V.VPM(gcfg) as h:
+        h.vpm(xp, qp, None, None, xp.shape[0], WhatToDo=0)
+        up = np.zeros_like(up_o)
+        gp = np.zeros_like(gp_o)
+        h.vpm(np.ascontiguousarray(xp), np.ascontiguousarray(qp), up, gp, xp.shape[0], WhatToDo=2)
+        for name, fid in _pairs(V, O):
+            ref = O.get_field(fid)
+            got = h.field(name).ravel()
+            assert rel_l2(got, ref) <= FIELD_TOL, name
+    assert rel_l2(up, up_o) <= PART_TOL
+    assert rel_l2(gp, gp_o) <= PART_TOL
+
+
+def test_ring64_ten_steps_match_oracle(gpulib, oracle):
+    """The 64^3 single-ring case: remesh, then 10 x (step, Euler, remesh)."""
+    from vpm_free_gb300 import workloads as W
+    V, O = gpulib, oracle
+    xp, qp, w = W.ring64()
+    ocfg, gcfg = configs_for(w)
+    s = O.define_sizes(ocfg, xp)
+    xo, qo = O.remesh(ocfg, s, xp, qp)
+    with V.VPM(gcfg) as h:
+        h.define_sizes(xp)
+        xg, qg = h.remesh_particles_3d(1, xp, qp)
+        assert xg.shape == xo.shape
+        h.set_particles(xg, qg)
+        for step in range(w["steps"]):
+            up, gp = O.step_fields(ocfg, s, xo, qo)
+            O.euler(xo, qo, up, gp, w["dt"])
+            xo, qo = O.remesh(ocfg, s, xo, qo)
+            h.step(w["dt"])
+            xg, qg = h.get_particles()
+            assert xg.shape[0] == xo.shape[0], step
+            assert rel_l2(xg, xo) <= PART_TOL, step
+            assert rel_l2(qg, qo) <= PART_TOL, step
+
+
+def test_deposition_deterministic(gpulib):
+    from vpm_free_gb300 import workloads as W
+    V = gpulib
+    xp, qp, w = W.scaled_ring(32)
+    _, gcfg = configs_for(w)
+    with V.VPM(gcfg) as h:
+        h.define_sizes(xp)
+        a = h.project_particles_3D(xp, qp)
+        perm = np.random.default_rng(3).permutation(xp.shape[0])
+        b = h.project_particles_3D(xp[perm], qp[perm])
+        c = h.project_particles_3D(xp, qp)
+    for x, y in zip(a, c):
+        assert np.array_equal(x, y)          # run to run: bitwise
+    for x, y in zip(a, b):
+        assert rel_l2(x, y) <= 1e-14         # input order only changes rounding
+
+
+def test_deposition_matches_oracle(gpulib, oracle):
+    from vpm_free_gb300 import workloads as W
+    V, O = gpulib, oracle
+    xp, qp, w = W.scaled_ring(48)
+    ocfg, gcfg = configs_for(w)
+    s = O.define_sizes(ocfg, xp)
+    nx, ny, nz = list(s.nn)
+    ref = [np.zeros(nx * ny * nz) for _ in range(3)]
+    O.lib().vpmo_project_particles(s, 4, np.ascontiguousarray(xp), np.ascontiguousarray(qp), xp.shape[0], *ref, 0)
+    with V.VPM(gcfg) as h:
+        h.define_sizes(xp)
+        got = h.project_particles_3D(xp, qp)
+    for c in range(3):
+        assert rel_l2(got[c], ref[c]) <= 1e-13

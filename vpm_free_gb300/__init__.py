@@ -1,0 +1,309 @@
+"""vpm_free_gb300 -- GB300 (sm_103a) particle-mesh time step of vpm_free.
+
+Host-side mirror of the reference's Fortran interface for this path, over
+the C-ABI of libvpmg.so (include/vpmg.h):
+
+  * ``read_pm_inp(path)``          -- pm.inp, positional (source/vpm.f90:132-152)
+  * ``VPM(cfg)``                   -- the vpm_lib module state as an object:
+      ``.vpm(XP, QP, UP, GP, NVR, neqpm, WhatToDo, NTIME, NI, NVRM)``
+                                      (source/vpm.f90:54-475, WhatToDo 0 and 2)
+      ``.remesh_particles_3d(iflag, XP, QP)``  (source/vpm_remesh.f90:5-225)
+      ``.pmesh(...)``, ``.project_particles_3D(...)`` (pmlib / projlib calls)
+      plus a device-resident loop (``set_particles``/``step``) for
+      test.f90-style time stepping without host copies.
+
+Particle arrays use the reference's layout in C order: XP(3,NVR) is a
+(NVR, 3) float64 array, QP(4,NVR) a (NVR, 4) array with QP(:,1:3) =
+-omega*vol and QP(:,4) = vol.  Everything computes in FP64 on the GPU;
+there is no CPU fallback: without the compiled library or a GPU every call
+raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = ["VPMConfig", "VPM", "VPMError", "read_pm_inp", "load_library", "library_path", "FIELDS"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+FIELDS = {"rhs": 0, "sol": 1, "vel": 2, "def": 3, "bl_sol1": 4, "coarse_rhs": 5, "coarse_sol": 6, "bl_final": 7}
+
+EXPORTS = [
+    "vpmg_read_pm_inp", "vpmg_create", "vpmg_destroy", "vpmg_last_error", "vpmg_status_string", "vpmg_vpm",
+    "vpmg_remesh_particles_3d", "vpmg_pmesh", "vpmg_project_particles_3d", "vpmg_define_sizes", "vpmg_get_sizes",
+    "vpmg_set_particles", "vpmg_get_particles", "vpmg_get_particle_velocity", "vpmg_step", "vpmg_remesh_device",
+    "vpmg_num_particles", "vpmg_get_field", "vpmg_kernel_launches", "vpmg_phase_times", "vpmg_tree_stats",
+    "vpmg_set_profiling", "vpmg_set_operator_budget",
+]
+
+
+class VPMError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"vpmg status {status}: {msg}")
+        self.status = status
+
+
+class VPMConfig(C.Structure):
+    """vpmg_config: pm.inp plus an explicit mesh box."""
+    _fields_ = [
+        ("dpm", C.c_double * 3), ("interf_iproj", C.c_int), ("ibctyp", C.c_int), ("idvpm", C.c_int),
+        ("epsvol", C.c_double), ("ncoarse", C.c_int), ("nbi", C.c_int), ("nbj", C.c_int), ("nbk", C.c_int),
+        ("nremesh", C.c_int), ("ncell_rem", C.c_int), ("iyntree", C.c_int), ("ilevmax", C.c_int),
+        ("ompthreads", C.c_int), ("idefine", C.c_int), ("iynslice", C.c_int), ("use_box", C.c_int),
+        ("box", C.c_double * 6),
+    ]
+
+    @classmethod
+    def make(cls, dpm=(0.05, 0.05, 0.05), interf_iproj=4, ibctyp=2, idvpm=1, epsvol=0.0, ncoarse=8, nb=(1, 1, 1),
+             nremesh=1, ncell_rem=1, iyntree=1, ilevmax=3, ompthreads=1, idefine=1, iynslice=0, box=None):
+        c = cls()
+        c.dpm[:] = list(dpm)
+        c.interf_iproj, c.ibctyp, c.idvpm, c.epsvol, c.ncoarse = interf_iproj, ibctyp, idvpm, epsvol, ncoarse
+        c.nbi, c.nbj, c.nbk = nb
+        c.nremesh, c.ncell_rem, c.iyntree, c.ilevmax = nremesh, ncell_rem, iyntree, ilevmax
+        c.ompthreads, c.idefine, c.iynslice = ompthreads, idefine, iynslice
+        if box is not None:
+            c.use_box = 1
+            c.box[:] = list(box)
+        return c
+
+
+class VPMSizes(C.Structure):
+    _fields_ = [
+        ("xbound", C.c_double * 6), ("dpm", C.c_double * 3), ("nn", C.c_int * 3), ("nn_bl", C.c_int * 6),
+        ("xbound_bl", C.c_double * 6), ("nnbl", C.c_int * 3), ("nnbl_bl", C.c_int * 6),
+        ("xbound_coarse", C.c_double * 6), ("dpm_coarse", C.c_double * 3), ("nn_coarse", C.c_int * 3),
+        ("nn_bl_coarse", C.c_int * 6), ("ilevmax", C.c_int), ("dvpm", C.c_double), ("defined", C.c_int),
+    ]
+
+
+_dp = C.POINTER(C.c_double)
+_PP = _dp * 3
+
+
+def library_path():
+    return os.path.join(_HERE, "libvpmg.so")
+
+
+def load_library():
+    """Loads libvpmg.so (built in tree by vpm_free_gb300/build.py)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise VPMError(-2, f"{path} is missing: run vpm_free_gb300/build.py (there is no CPU fallback)")
+    L = C.CDLL(path)
+    L.vpmg_read_pm_inp.argtypes = [C.c_char_p, C.POINTER(VPMConfig)]
+    L.vpmg_create.argtypes = [C.POINTER(VPMConfig), C.c_int, C.POINTER(C.c_void_p)]
+    L.vpmg_destroy.argtypes = [C.c_void_p]
+    L.vpmg_last_error.argtypes = [C.c_void_p]
+    L.vpmg_last_error.restype = C.c_char_p
+    L.vpmg_status_string.argtypes = [C.c_int]
+    L.vpmg_status_string.restype = C.c_char_p
+    L.vpmg_vpm.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int, C.c_double,
+                           C.c_int]
+    L.vpmg_remesh_particles_3d.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.POINTER(C.c_int), C.c_int]
+    L.vpmg_pmesh.argtypes = [C.c_void_p, _PP, _PP, _dp, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
+                             C.c_int]
+    L.vpmg_project_particles_3d.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _PP]
+    L.vpmg_define_sizes.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int]
+    L.vpmg_get_sizes.argtypes = [C.c_void_p, C.POINTER(VPMSizes)]
+    L.vpmg_set_particles.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int]
+    L.vpmg_get_particles.argtypes = [C.c_void_p, _dp, _dp, C.POINTER(C.c_int), C.c_int]
+    L.vpmg_get_particle_velocity.argtypes = [C.c_void_p, _dp, _dp, C.c_int]
+    L.vpmg_step.argtypes = [C.c_void_p, C.c_double, _dp, C.c_int]
+    L.vpmg_remesh_device.argtypes = [C.c_void_p]
+    L.vpmg_num_particles.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+    L.vpmg_get_field.argtypes = [C.c_void_p, C.c_int, _dp, C.c_size_t, C.POINTER(C.c_size_t)]
+    L.vpmg_kernel_launches.argtypes = [C.c_void_p]
+    L.vpmg_kernel_launches.restype = C.c_longlong
+    L.vpmg_phase_times.argtypes = [C.c_void_p, _dp]
+    L.vpmg_tree_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]
+    L.vpmg_set_profiling.argtypes = [C.c_void_p, C.c_int]
+    L.vpmg_set_operator_budget.argtypes = [C.c_void_p, C.c_longlong]
+    _LIB = L
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return a
+
+
+def read_pm_inp(path):
+    """pm.inp -> VPMConfig (positional list-directed reads of source/vpm.f90:132-152)."""
+    L = load_library()
+    cfg = VPMConfig()
+    rc = L.vpmg_read_pm_inp(os.fsencode(path), C.byref(cfg))
+    if rc != 0:
+        raise VPMError(rc, f"cannot parse {path}")
+    return cfg
+
+
+class VPM:
+    """The vpm_lib module state (source/vpm.f90:1-32) on one GPU."""
+
+    def __init__(self, cfg, device=-1):
+        self._L = load_library()
+        self.cfg = cfg
+        h = C.c_void_p()
+        rc = self._L.vpmg_create(C.byref(cfg), device, C.byref(h))
+        if rc != 0:
+            raise VPMError(rc, self._L.vpmg_status_string(rc).decode())
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.vpmg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _chk(self, rc):
+        if rc != 0:
+            msg = self._L.vpmg_last_error(self._h)
+            raise VPMError(rc, (msg or b"").decode() or self._L.vpmg_status_string(rc).decode())
+
+    # ---- the reference's calls ------------------------------------------
+    def vpm(self, XP, QP, UP, GP, NVR, neqpm=3, WhatToDo=2, NTIME=0, NI=0.0, NVRM=None):
+        """vpm(XP,QP,UP,GP,NVR,neqpm,WhatToDo,...,NTIME,NI,NVRM).  UP/GP are
+        overwritten (WhatToDo = 2).  Returns NVR."""
+        nvrm = XP.shape[0] if NVRM is None else NVRM
+        for a, w in ((XP, 3), (QP, 4), (UP, 3), (GP, 3)):
+            if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous or a.shape[1] != w):
+                raise ValueError("particle arrays must be C-contiguous float64 (NVRM, 3|4)")
+        n = C.c_int(int(NVR))
+        self._chk(self._L.vpmg_vpm(self._h, _p(XP), _p(QP), _p(UP), _p(GP), C.byref(n), neqpm, WhatToDo, NTIME,
+                                   float(NI), int(nvrm)))
+        return n.value
+
+    def define_sizes(self, XP, NTIME=0):
+        XP = _f64(XP)
+        self._chk(self._L.vpmg_define_sizes(self._h, _p(XP), XP.shape[0], NTIME))
+        return self.sizes()
+
+    def sizes(self):
+        s = VPMSizes()
+        self._chk(self._L.vpmg_get_sizes(self._h, C.byref(s)))
+        return s
+
+    def remesh_particles_3d(self, iflag, XP, QP, capacity=None):
+        """remesh_particles_3d(iflag) on (XP, QP); returns new (XP, QP) arrays."""
+        nn = list(self.sizes().nn)
+        cap = int(capacity or max(int(np.prod(nn)), XP.shape[0]))
+        xb = np.zeros((cap, 3))
+        qb = np.zeros((cap, 4))
+        xb[:XP.shape[0]] = XP
+        qb[:QP.shape[0]] = QP
+        n = C.c_int(XP.shape[0])
+        self._chk(self._L.vpmg_remesh_particles_3d(self._h, iflag, _p(xb), _p(qb), C.byref(n), cap))
+        return xb[:n.value].copy(), qb[:n.value].copy()
+
+    def pmesh(self, SOL, RHS, Xbound, Dpm, iynbc, itree=1, levmax=3, NN_bl=None):
+        """pmesh (source/pmlib.f90:69-192), 3 components, ibctyp = 2.
+        SOL, RHS: lists of 3 arrays shaped (NZ, NY, NX); SOL updated in place."""
+        nz, ny, nx = RHS[0].shape
+        sol = [_f64(s) for s in SOL]
+        rhs = [_f64(r) for r in RHS]
+        nn = (C.c_int * 3)(nx, ny, nz)
+        nnbl = (C.c_int * 6)(*(NN_bl if NN_bl is not None else (1, 1, 1, nx, ny, nz)))
+        self._chk(self._L.vpmg_pmesh(self._h, _PP(*[_p(s) for s in sol]), _PP(*[_p(r) for r in rhs]),
+                                     _p(_f64(Xbound)), _p(_f64(Dpm)), nn, nnbl, iynbc, itree, levmax))
+        for dst, src in zip(SOL, sol):
+            if dst is not src:
+                dst[...] = src
+        return SOL
+
+    def project_particles_3D(self, XP, QP):
+        """project_particles_3D + project_vol3d(IDVPM=1) on the current mesh;
+        returns RHS(1:3) as 3 arrays (NZ, NY, NX)."""
+        nx, ny, nz = list(self.sizes().nn)
+        XP, QP = _f64(XP), _f64(QP)
+        out = [np.empty((nz, ny, nx)) for _ in range(3)]
+        self._chk(self._L.vpmg_project_particles_3d(self._h, _p(XP), _p(QP), XP.shape[0], _PP(*[_p(o) for o in out])))
+        return out
+
+    # ---- device-resident loop -------------------------------------------
+    def set_particles(self, XP, QP):
+        XP, QP = _f64(XP), _f64(QP)
+        self._chk(self._L.vpmg_set_particles(self._h, _p(XP), _p(QP), XP.shape[0], XP.shape[0]))
+
+    def get_particles(self):
+        n = self.num_particles()
+        xp, qp = np.empty((max(n, 1), 3)), np.empty((max(n, 1), 4))
+        m = C.c_int(0)
+        self._chk(self._L.vpmg_get_particles(self._h, _p(xp), _p(qp), C.byref(m), max(n, 1)))
+        return xp[:m.value], qp[:m.value]
+
+    def get_particle_velocity(self, n=None):
+        n = self.num_particles() if n is None else n
+        up, gp = np.empty((max(n, 1), 3)), np.empty((max(n, 1), 3))
+        self._chk(self._L.vpmg_get_particle_velocity(self._h, _p(up), _p(gp), n))
+        return up[:n], gp[:n]
+
+    def num_particles(self):
+        n = C.c_int(0)
+        self._chk(self._L.vpmg_num_particles(self._h, C.byref(n)))
+        return n.value
+
+    def step(self, dt, uinf=(0.0, 0.0, 0.0), remesh=True):
+        u = np.asarray(uinf, dtype=np.float64)
+        self._chk(self._L.vpmg_step(self._h, float(dt), _p(u), 1 if remesh else 0))
+
+    def remesh(self):
+        self._chk(self._L.vpmg_remesh_device(self._h))
+
+    def field(self, name):
+        """Resident field (3, NZ, NY, NX) of the last step."""
+        which = FIELDS[name]
+        cnt = C.c_size_t(0)
+        self._chk(self._L.vpmg_get_field(self._h, which, None, 0, C.byref(cnt)))
+        out = np.empty(3 * cnt.value)
+        self._chk(self._L.vpmg_get_field(self._h, which, _p(out), out.size, C.byref(cnt)))
+        s = self.sizes()
+        if which in (0, 1, 2, 3):
+            dims = list(s.nn)
+        elif which in (4, 7):
+            dims = list(s.nnbl)
+        else:
+            dims = list(s.nn_coarse)
+        return out.reshape(3, dims[2], dims[1], dims[0])
+
+    # ---- instrumentation --------------------------------------------------
+    def kernel_launches(self):
+        return int(self._L.vpmg_kernel_launches(self._h))
+
+    def phase_times(self):
+        ms = (C.c_double * 9)()
+        self._chk(self._L.vpmg_phase_times(self._h, ms))
+        return list(ms)
+
+    def tree_stats(self):
+        a, b, c = C.c_longlong(0), C.c_longlong(0), C.c_int(0)
+        self._chk(self._L.vpmg_tree_stats(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"interactions": a.value, "bytes": b.value, "precomputed": bool(c.value)}
+
+    def set_profiling(self, level):
+        self._chk(self._L.vpmg_set_profiling(self._h, int(level)))
+
+    def set_operator_budget(self, nbytes):
+        self._chk(self._L.vpmg_set_operator_budget(self._h, int(nbytes)))

@@ -1,0 +1,730 @@
+// api.cu -- the C-ABI (include/vpmg.h): handle, sizing, step orchestration.
+//
+// One handle = one CUDA stream + the device state that the reference keeps
+// in module variables (vpm_vars / vpm_size / pmgrid / parvar,
+// source/vpm.f90:1-32, source/main_pm.f90:2-45).  Fields stay resident in
+// HBM between calls; the Fortran-facing vpm() copies particles in and out.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+
+#include "fields.h"
+#include "particles.h"
+#include "vpmg_internal.h"
+
+using namespace vpmg;
+
+struct vpmg_handle {
+  vpmg_config cfg{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  long long launches = 0;
+  vpmg_sizes sz{};
+  bool sized = false, prepared = false;
+  long long op_budget = 100LL << 30;
+  // grids
+  Grid gglob{}, gbl{}, gco{};
+  int inner_lo[3] = {0, 0, 0}, inner_ext[3] = {0, 0, 0};  // block inner box (0-based) and extent
+  // fields (3 components back to back)
+  DBuf<double> rhs, sol, vel, def;
+  DBuf<double> rhs_bl, sol_bl, sol0, work, bl_sol1_copy;
+  DBuf<double> samp, crhs, csol, csol0;
+  DirichletPlan dp_bl, dp_inner, dp_c;
+  BoundaryOp bo_bl, bo_c;
+  YapsDev yaps;
+  bool keep_intermediates = false;
+  // particles
+  Particles parts;
+  Binning bins;
+  int np = 0;
+  DBuf<double> stage;  // AoS staging for host copies
+  // timing
+  bool profile = false;
+  cudaEvent_t ev[10] = {};
+  double phase_ms[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+namespace {
+
+struct LaunchScope {  // routes VPMG_LAUNCHED() to the handle's counter
+  long long* prev;
+  explicit LaunchScope(vpmg_handle* h) : prev(g_launch_counter) { g_launch_counter = &h->launches; }
+  ~LaunchScope() { g_launch_counter = prev; }
+};
+
+template <class F>
+int guarded(vpmg_handle* h, F&& f) {
+  if (!h) return VPMG_ERR_ARG;
+  try {
+    LaunchScope ls(h);
+    VPMG_CUDA(cudaSetDevice(h->device));
+    f();
+    return VPMG_OK;
+  } catch (const Error& e) {
+    h->err = e.msg;
+    return e.status;
+  } catch (const std::exception& e) {
+    h->err = e.what();
+    return VPMG_ERR_ARG;
+  }
+}
+
+inline int fnint(double x) { return (int)std::lround(x); }
+
+// definepm (source/pmlib.f90:216-432), itype 1 and 3, ND = 3.
+void definepm(int itype, double Xb[6], const double D[3], int ndum, const int nsize[3], int NN[3], int NN_bl[6]) {
+  for (int d = 0; d < 3; ++d) {
+    Xb[d] = Xb[d] - ((double)ndum * D[d]);
+    Xb[d + 3] = Xb[d + 3] + ((double)ndum * D[d]);
+    NN[d] = fnint(std::fabs(Xb[d + 3] - Xb[d]) / D[d]) + 1;
+  }
+  if (itype == 1) {
+    for (int d = 0; d < 3; ++d) { NN_bl[d] = ndum + 1; NN_bl[d + 3] = NN[d] - ndum; }
+    return;
+  }
+  // itype 3: pad symmetrically so that NN-1 divides by nsize (odd remainder on the min side)
+  for (int d = 0; d < 3; ++d) {
+    const int nd = nsize[d] - ((NN[d] - 1) % nsize[d]);
+    if (nd % 2 == 0) {
+      Xb[d] = Xb[d] - ((double)(nd / 2) * D[d]);
+      Xb[d + 3] = Xb[d + 3] + ((double)(nd / 2) * D[d]);
+    } else {
+      Xb[d] = Xb[d] - ((double)(nd % 2 + nd / 2) * D[d]);
+      Xb[d + 3] = Xb[d + 3] + ((double)(nd / 2) * D[d]);
+    }
+    NN[d] = fnint(std::fabs(Xb[d + 3] - Xb[d]) / D[d]) + 1;
+    NN_bl[d] = ndum + 1;
+    NN_bl[d + 3] = NN[d] - ndum;
+  }
+}
+
+// define_sizes (source/vpm.f90:477-660), one block.  xp: XP(3,nvr).
+void define_sizes(vpmg_handle* h, const double* xp, int nvr, int ntime, vpmg_sizes& s) {
+  const vpmg_config& cfg = h->cfg;
+  VPMG_CHECK(cfg.nbi == 1 && cfg.nbj == 1 && cfg.nbk == 1, VPMG_ERR_UNSUPPORTED,
+             "one GPU runs one YAPS block: NBI = NBJ = NBK = 1");
+  const bool recompute = (ntime == 0 && cfg.idefine == 1) || cfg.idefine == 0 || !h->sized;
+  if (recompute) {
+    double Xb[6], Dpm[3] = {cfg.dpm[0], cfg.dpm[1], cfg.dpm[2]};
+    int NN[3], NN_bl[6];
+    if (cfg.use_box) {
+      for (int d = 0; d < 6; ++d) Xb[d] = cfg.box[d];
+      for (int d = 0; d < 3; ++d) {
+        NN[d] = fnint(std::fabs(Xb[d + 3] - Xb[d]) / Dpm[d]) + 1;
+        NN_bl[d] = 1;
+        NN_bl[d + 3] = NN[d];
+        VPMG_CHECK((NN[d] - 1) % cfg.ncoarse == 0, VPMG_ERR_ARG, "explicit box: cells must divide by ncoarse");
+      }
+    } else {
+      VPMG_CHECK(nvr > 0 && xp, VPMG_ERR_ARG, "define_sizes needs particles to size the box");
+      double mn[3] = {xp[0], xp[1], xp[2]}, mx[3] = {xp[0], xp[1], xp[2]};
+      for (int p = 1; p < nvr; ++p)
+        for (int d = 0; d < 3; ++d) {
+          mn[d] = std::min(mn[d], xp[3 * (size_t)p + d]);
+          mx[d] = std::max(mx[d], xp[3 * (size_t)p + d]);
+        }
+      for (int d = 0; d < 3; ++d) {
+        Xb[d] = mn[d] - (double)cfg.interf_iproj * cfg.dpm[d];
+        Xb[d + 3] = mx[d] + (double)cfg.interf_iproj * cfg.dpm[d];
+      }
+      const int nsiz[3] = {cfg.nbi * cfg.ncoarse, cfg.nbj * cfg.ncoarse, cfg.nbk * cfg.ncoarse};
+      definepm(3, Xb, Dpm, 0, nsiz, NN, NN_bl);
+    }
+    for (int d = 0; d < 6; ++d) { s.xbound[d] = Xb[d]; s.nn_bl[d] = NN_bl[d]; }
+    for (int d = 0; d < 3; ++d) { s.dpm[d] = Dpm[d]; s.nn[d] = NN[d]; }
+  }
+  const double* Xb = s.xbound;
+  const double* D = s.dpm;
+  const int NXbl = fnint((Xb[3] - Xb[0]) / D[0]) / cfg.nbi;
+  const int NYbl = fnint((Xb[4] - Xb[1]) / D[1]) / cfg.nbj;
+  const int NZbl = fnint((Xb[5] - Xb[2]) / D[2]) / cfg.nbk;
+  double Xt[6] = {Xb[0] + (double)(0 * NXbl) * D[0], Xb[1] + (double)(0 * NYbl) * D[1], Xb[2] + (double)(0 * NZbl) * D[2],
+                  Xb[0] + (double)(1 * NXbl) * D[0], Xb[1] + (double)(1 * NYbl) * D[1], Xb[2] + (double)(1 * NZbl) * D[2]};
+  const int nsb[3] = {cfg.ncoarse, cfg.ncoarse, cfg.ncoarse};
+  definepm(1, Xt, D, cfg.ncoarse, nsb, s.nnbl, s.nnbl_bl);
+  for (int d = 0; d < 6; ++d) { s.xbound_bl[d] = Xt[d]; s.xbound_coarse[d] = Xb[d]; }
+  for (int d = 0; d < 3; ++d) s.dpm_coarse[d] = (double)cfg.ncoarse * D[d];
+  const int ns2 = 1 << std::max(cfg.ilevmax, 0);
+  const int nsc[3] = {ns2, ns2, ns2};
+  definepm(1, s.xbound_coarse, s.dpm_coarse, 4, nsc, s.nn_coarse, s.nn_bl_coarse);
+  int ilev = cfg.ilevmax;
+  for (int lev = 0; lev <= ilev; ++lev) {
+    const int istep = 1 << lev;
+    if ((s.nnbl_bl[3] - s.nnbl_bl[0]) / istep == 0 || (s.nnbl_bl[4] - s.nnbl_bl[1]) / istep == 0 ||
+        (s.nnbl_bl[5] - s.nnbl_bl[2]) / istep == 0) {
+      ilev = lev - 1;
+      break;
+    }
+  }
+  s.ilevmax = ilev;
+  s.dvpm = D[0] * D[1] * D[2];
+  s.defined = 1;
+}
+
+bool same_sizes(const vpmg_sizes& a, const vpmg_sizes& b) {
+  return std::memcmp(&a, &b, sizeof(vpmg_sizes)) == 0;
+}
+
+Grid make_grid(const double xb[6], const double d[3], const int n[3]) {
+  Grid g;
+  for (int k = 0; k < 3; ++k) { g.xmin[k] = xb[k]; g.d[k] = d[k]; g.n[k] = n[k]; }
+  return g;
+}
+
+double* comp(DBuf<double>& b, size_t n, int c) { return b.p + (size_t)c * n; }
+
+void prepare(vpmg_handle* h) {
+  const vpmg_sizes& s = h->sz;
+  cudaStream_t st = h->stream;
+  h->gglob = make_grid(s.xbound, s.dpm, s.nn);
+  h->gbl = make_grid(s.xbound_bl, s.dpm, s.nnbl);
+  h->gco = make_grid(s.xbound_coarse, s.dpm_coarse, s.nn_coarse);
+  const size_t N = h->gglob.count(), NB = h->gbl.count(), NC = h->gco.count();
+  h->rhs.ensure(3 * N); h->sol.ensure(3 * N); h->vel.ensure(3 * N); h->def.ensure(3 * N);
+  h->rhs_bl.ensure(3 * NB); h->sol_bl.ensure(3 * NB); h->sol0.ensure(NB);
+  h->samp.ensure(3 * NC); h->crhs.ensure(3 * NC); h->csol.ensure(3 * NC); h->csol0.ensure(NC);
+  for (DBuf<double>* b : {&h->rhs, &h->sol, &h->vel, &h->def, &h->rhs_bl, &h->sol_bl, &h->sol0, &h->samp, &h->crhs,
+                          &h->csol, &h->csol0})
+    fill_zero(b->p, b->n, st);
+  // Dirichlet plans: whole block, inner block box, whole coarse grid
+  const int bl_full[6] = {0, 0, 0, s.nnbl[0] - 1, s.nnbl[1] - 1, s.nnbl[2] - 1};
+  const int bl_inner[6] = {s.nnbl_bl[0] - 1, s.nnbl_bl[1] - 1, s.nnbl_bl[2] - 1,
+                           s.nnbl_bl[3] - 1, s.nnbl_bl[4] - 1, s.nnbl_bl[5] - 1};
+  const int c_full[6] = {0, 0, 0, s.nn_coarse[0] - 1, s.nn_coarse[1] - 1, s.nn_coarse[2] - 1};
+  dirichlet_prepare(h->dp_bl, s.nnbl, bl_full, s.dpm, st);
+  dirichlet_prepare(h->dp_inner, s.nnbl, bl_inner, s.dpm, st);
+  dirichlet_prepare(h->dp_c, s.nn_coarse, c_full, s.dpm_coarse, st);
+  size_t wmax = 0;
+  for (DirichletPlan* p : {&h->dp_bl, &h->dp_inner, &h->dp_c}) wmax = std::max(wmax, (size_t)p->m[0] * p->m[1] * p->m[2]);
+  h->work.ensure(wmax);
+  for (int d = 0; d < 3; ++d) {
+    h->inner_lo[d] = s.nnbl_bl[d] - 1;
+    h->inner_ext[d] = s.nnbl_bl[d + 3] - s.nnbl_bl[d] + 1;
+  }
+  // boundary operators: fine block (levels ilevmax), coarse (ilevmax-1); iyntree = 0 -> untreed sum
+  const bool tree = h->cfg.iyntree == 1;
+  boundary_prepare(h->bo_bl, h->gbl, tree ? std::max(s.ilevmax, 0) : 0, h->op_budget, st);
+  boundary_prepare(h->bo_c, h->gco, tree ? std::max(s.ilevmax - 1, 0) : 0, h->op_budget, st);
+  // YAPS maps
+  YapsGeom Y;
+  try {
+    build_yaps_geometry(s.xbound_bl, s.dpm, s.nnbl, s.nnbl_bl, s.xbound_coarse, s.dpm_coarse, s.nn_coarse,
+                        h->cfg.ncoarse, Y);
+  } catch (const std::exception& e) {
+    throw Error{VPMG_ERR_UNSUPPORTED, e.what()};
+  }
+  h->yaps.prepare(Y);
+  // particles: capacity for a full remesh of the global mesh
+  h->parts.ensure((int)std::min<size_t>(N, (size_t)INT32_MAX / 16));
+  h->bins.ensure(N);
+  VPMG_CUDA(cudaStreamSynchronize(st));
+  h->prepared = true;
+}
+
+MeshDev mesh_dev(const Grid& g, int itype) {
+  MeshDev m;
+  for (int k = 0; k < 3; ++k) { m.xmin[k] = g.xmin[k]; m.d[k] = g.d[k]; m.n[k] = g.n[k]; }
+  m.itype = itype;
+  m.ips = (itype == 2) ? 0 : 1;
+  m.ipf = (itype == 2) ? 1 : 2;
+  return m;
+}
+
+void ev_mark(vpmg_handle* h, int i) {
+  if (h->profile) VPMG_CUDA(cudaEventRecord(h->ev[i], h->stream));
+}
+
+// pmesh(iynbc = 1) on a grid: zero-BC solve, panels, boundary values, BC solve.
+void infinite_domain(vpmg_handle* h, DirichletPlan& dp, BoundaryOp& bo, const Grid& g, double* rhs3, double* sol3,
+                     double* sol0, size_t n) {
+  cudaStream_t st = h->stream;
+  for (int c = 0; c < 3; ++c) {
+    dirichlet_solve(dp, rhs3 + c * n, sol0, true, h->work.p, st);
+    boundary_panels(bo, g, sol0, c, st);
+  }
+  double* sp[3] = {sol3, sol3 + n, sol3 + 2 * n};
+  boundary_apply(bo, g, sp, st);
+  for (int c = 0; c < 3; ++c) dirichlet_solve(dp, rhs3 + c * n, sol3 + c * n, false, h->work.p, st);
+}
+
+// Field part of vpm(WhatToDo = 2) on binned particles (vpm.f90:171-314 + yaps3d).
+void field_step(vpmg_handle* h) {
+  cudaStream_t st = h->stream;
+  const vpmg_sizes& s = h->sz;
+  const size_t N = h->gglob.count(), NB = h->gbl.count(), NC = h->gco.count();
+  const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
+  double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
+  deposit(h->parts, mg, h->bins, R, st);
+  // rhsscat_3d: global interior -> block inner box; the block padding stays zero
+  const int go[3] = {s.nn_bl[0] - 1, s.nn_bl[1] - 1, s.nn_bl[2] - 1};
+  for (int c = 0; c < 3; ++c) box_copy(R[c], s.nn, go, comp(h->rhs_bl, NB, c), s.nnbl, h->inner_lo, h->inner_ext, st);
+  fill_zero(h->sol_bl.p, 3 * NB, st);
+  ev_mark(h, 1);
+  // yaps3d (a): fine infinite-domain solve on the padded block
+  for (int c = 0; c < 3; ++c) {
+    dirichlet_solve(h->dp_bl, comp(h->rhs_bl, NB, c), h->sol0.p, true, h->work.p, st);
+    boundary_panels(h->bo_bl, h->gbl, h->sol0.p, c, st);
+  }
+  ev_mark(h, 2);
+  double* SB[3] = {comp(h->sol_bl, NB, 0), comp(h->sol_bl, NB, 1), comp(h->sol_bl, NB, 2)};
+  boundary_apply(h->bo_bl, h->gbl, SB, st);
+  ev_mark(h, 3);
+  for (int c = 0; c < 3; ++c) dirichlet_solve(h->dp_bl, comp(h->rhs_bl, NB, c), SB[c], false, h->work.p, st);
+  if (h->keep_intermediates) {
+    h->bl_sol1_copy.ensure(3 * NB);
+    VPMG_CUDA(cudaMemcpyAsync(h->bl_sol1_copy.p, h->sol_bl.p, sizeof(double) * 3 * NB, cudaMemcpyDeviceToDevice, st));
+  }
+  ev_mark(h, 4);
+  // (b)-(d): sample, coarse Laplacian, coarse infinite-domain solve, face interpolation
+  fill_zero(h->samp.p, 3 * NC, st);
+  fill_zero(h->crhs.p, 3 * NC, st);
+  fill_zero(h->csol.p, 3 * NC, st);
+  double* SM[3] = {comp(h->samp, NC, 0), comp(h->samp, NC, 1), comp(h->samp, NC, 2)};
+  double* CR[3] = {comp(h->crhs, NC, 0), comp(h->crhs, NC, 1), comp(h->crhs, NC, 2)};
+  double* CS[3] = {comp(h->csol, NC, 0), comp(h->csol, NC, 1), comp(h->csol, NC, 2)};
+  yaps_sample(h->yaps, SB, SM, st);
+  yaps_coarse_rhs(h->yaps, s.nn_coarse, s.dpm_coarse, SM, CR, st);
+  infinite_domain(h, h->dp_c, h->bo_c, h->gco, h->crhs.p, h->csol.p, h->csol0.p, NC);
+  yaps_face_interp(h->yaps, s.nn_coarse, CS, SM, SB, st);
+  ev_mark(h, 5);
+  // (e): final Dirichlet solve on the inner block box
+  for (int c = 0; c < 3; ++c) dirichlet_solve(h->dp_inner, comp(h->rhs_bl, NB, c), SB[c], false, h->work.p, st);
+  // solget_3d
+  double* S[3] = {comp(h->sol, N, 0), comp(h->sol, N, 1), comp(h->sol, N, 2)};
+  for (int c = 0; c < 3; ++c) box_copy(SB[c], s.nnbl, h->inner_lo, S[c], s.nn, go, h->inner_ext, st);
+  ev_mark(h, 6);
+  // calc_velocity_serial_3d(1)
+  double* V[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
+  double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
+  velocity_and_stretching(s.nn, s.dpm, S, R, V, G, st);
+  ev_mark(h, 7);
+}
+
+void m2p_step(vpmg_handle* h, bool write_up, bool euler, double dt, const double uinf[3]) {
+  const size_t N = h->gglob.count();
+  const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
+  const double* V[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
+  const double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
+  m2p(h->parts, mg, h->bins, V, G, write_up, euler, dt, uinf, h->stream);
+  ev_mark(h, 8);
+}
+
+// remesh_particles_3d(1): deposit on the mesh with the recomputed spacing,
+// emit one particle per node with |w| >= (REAL)1e-9 (vpm_remesh.f90:50-195).
+void remesh(vpmg_handle* h) {
+  cudaStream_t st = h->stream;
+  const vpmg_sizes& s = h->sz;
+  Grid gr = h->gglob;
+  for (int d = 0; d < 3; ++d) gr.d[d] = (s.xbound[d + 3] - s.xbound[d]) / (double)(s.nn[d] - 1);
+  const MeshDev mr = mesh_dev(gr, h->cfg.interf_iproj);
+  const size_t N = gr.count();
+  bin_particles(h->parts, h->np, mr, h->bins, st);
+  double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
+  deposit(h->parts, mr, h->bins, R, st);
+  const int hh = h->cfg.interf_iproj / 2;
+  const int lo[3] = {s.nn_bl[0] - 1 + hh, s.nn_bl[1] - 1 + hh, s.nn_bl[2] - 1 + hh};
+  const int hi[3] = {s.nn_bl[3] - 1 - hh, s.nn_bl[4] - 1 - hh, s.nn_bl[5] - 1 - hh};
+  const double thr = (double)1e-09f;  // default-REAL literal of vpm_remesh.f90:184
+  const int n = remesh_emit(h->parts, mr, h->bins, R, lo, hi, thr, h->parts.capacity, st);
+  VPMG_CHECK(n <= h->parts.capacity, VPMG_ERR_CAPACITY, "remesh exceeds the particle capacity");
+  h->np = n;
+  ev_mark(h, 9);
+}
+
+__global__ void k_aos_to_soa(const double* __restrict__ xa, const double* __restrict__ qa, int n, double* x, double* y,
+                             double* z, double* q0, double* q1, double* q2, double* vol) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  x[p] = xa[3 * (size_t)p]; y[p] = xa[3 * (size_t)p + 1]; z[p] = xa[3 * (size_t)p + 2];
+  q0[p] = qa[4 * (size_t)p]; q1[p] = qa[4 * (size_t)p + 1]; q2[p] = qa[4 * (size_t)p + 2]; vol[p] = qa[4 * (size_t)p + 3];
+}
+
+__global__ void k_soa_to_aos(int n, const double* x, const double* y, const double* z, const double* q0,
+                             const double* q1, const double* q2, const double* vol, double* __restrict__ xa,
+                             double* __restrict__ qa) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  xa[3 * (size_t)p] = x[p]; xa[3 * (size_t)p + 1] = y[p]; xa[3 * (size_t)p + 2] = z[p];
+  qa[4 * (size_t)p] = q0[p]; qa[4 * (size_t)p + 1] = q1[p]; qa[4 * (size_t)p + 2] = q2[p]; qa[4 * (size_t)p + 3] = vol[p];
+}
+
+void upload_particles(vpmg_handle* h, const double* xp, const double* qp, int n) {
+  VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes (WhatToDo = 0) must come first");
+  VPMG_CHECK(n >= 0 && n <= h->parts.capacity, VPMG_ERR_CAPACITY, "more particles than mesh nodes");
+  h->stage.ensure(7 * (size_t)std::max(n, 1));
+  if (n > 0) {
+    VPMG_CUDA(cudaMemcpyAsync(h->stage.p, xp, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+    VPMG_CUDA(cudaMemcpyAsync(h->stage.p + 3 * (size_t)n, qp, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, h->stream));
+    Particles& P = h->parts;
+    k_aos_to_soa<<<(n + 255) / 256, 256, 0, h->stream>>>(h->stage.p, h->stage.p + 3 * (size_t)n, n, P.x.p, P.y.p, P.z.p,
+                                                        P.q0.p, P.q1.p, P.q2.p, P.vol.p);
+    VPMG_LAUNCHED();
+    VPMG_CUDA(cudaGetLastError());
+  }
+  h->np = n;
+}
+
+void download_particles(vpmg_handle* h, double* xp, double* qp, int n) {
+  if (n <= 0) return;
+  h->stage.ensure(7 * (size_t)n);
+  Particles& P = h->parts;
+  k_soa_to_aos<<<(n + 255) / 256, 256, 0, h->stream>>>(n, P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.vol.p,
+                                                      h->stage.p, h->stage.p + 3 * (size_t)n);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaMemcpyAsync(xp, h->stage.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
+  VPMG_CUDA(cudaMemcpyAsync(qp, h->stage.p + 3 * (size_t)n, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, h->stream));
+  VPMG_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+void finish_phase_times(vpmg_handle* h) {
+  if (!h->profile) return;
+  VPMG_CUDA(cudaEventSynchronize(h->ev[9]));
+  for (int i = 0; i < 9; ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]) != cudaSuccess) { cudaGetLastError(); ms = 0.f; }
+    h->phase_ms[i] = ms;
+  }
+}
+
+std::string trim_tokens(const std::string& line, int n, std::vector<std::string>& out) {
+  std::string t = line;
+  for (char& ch : t)
+    if (ch == ',') ch = ' ';
+  std::istringstream is(t);
+  std::string w;
+  for (int i = 0; i < n && (is >> w); ++i) out.push_back(w);
+  return t;
+}
+
+}  // namespace
+
+// ======================================================================
+extern "C" {
+
+const char* vpmg_status_string(int st) {
+  switch (st) {
+    case VPMG_OK: return "ok";
+    case VPMG_ERR_ARG: return "bad argument";
+    case VPMG_ERR_CUDA: return "CUDA error";
+    case VPMG_ERR_NOMEM: return "device out of memory";
+    case VPMG_ERR_OUTSIDE: return "particle stencil outside the mesh";
+    case VPMG_ERR_CAPACITY: return "particle capacity exceeded";
+    case VPMG_ERR_UNSUPPORTED: return "unsupported option";
+    case VPMG_ERR_STATE: return "call out of order";
+    case VPMG_ERR_TREE: return "quadtree inconsistency";
+    default: return "unknown status";
+  }
+}
+
+const char* vpmg_last_error(const vpmg_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int vpmg_read_pm_inp(const char* path, vpmg_config* c) {
+  // Positional list-directed reads of source/vpm.f90:132-152: each READ
+  // takes the leading values of its record and skips the rest.
+  if (!path || !c) return VPMG_ERR_ARG;
+  std::ifstream f(path);
+  if (!f) return VPMG_ERR_ARG;
+  std::memset(c, 0, sizeof(*c));
+  std::string line;
+  auto rec = [&](int n, std::vector<std::string>& v) -> bool {
+    v.clear();
+    while ((int)v.size() < n) {
+      if (!std::getline(f, line)) return false;
+      trim_tokens(line, n - (int)v.size(), v);
+    }
+    return true;
+  };
+  std::vector<std::string> v;
+  try {
+    if (!rec(3, v)) return VPMG_ERR_ARG;
+    for (int d = 0; d < 3; ++d) c->dpm[d] = std::stod(v[d]);
+    if (!rec(1, v)) return VPMG_ERR_ARG; c->interf_iproj = std::stoi(v[0]);
+    if (!rec(1, v)) return VPMG_ERR_ARG; c->ibctyp = std::stoi(v[0]);
+    if (!rec(1, v)) return VPMG_ERR_ARG; c->idvpm = std::stoi(v[0]);
+    if (!rec(1, v)) return VPMG_ERR_ARG; c->epsvol = std::stod(v[0]);
+    if (!rec(1, v)) return VPMG_ERR_ARG; c->ncoarse = std::stoi(v[0]);
+    if (!rec(3, v)) return VPMG_ERR_ARG; c->nbi = std::stoi(v[0]); c->nbj = std::stoi(v[1]); c->nbk = std::stoi(v[2]);
+    if (!rec(2, v)) return VPMG_ERR_ARG; c->nremesh = std::stoi(v[0]); c->ncell_rem = std::stoi(v[1]);
+    if (!rec(2, v)) return VPMG_ERR_ARG; c->iyntree = std::stoi(v[0]); c->ilevmax = std::stoi(v[1]);
+    if (!rec(1, v)) return VPMG_ERR_ARG; c->ompthreads = std::stoi(v[0]);
+    if (!rec(1, v)) return VPMG_ERR_ARG; c->idefine = std::stoi(v[0]);
+    if (!rec(1, v)) return VPMG_ERR_ARG; c->iynslice = std::stoi(v[0]);
+    if (!rec(1, v)) return VPMG_ERR_ARG;
+    if (std::stoi(v[0]) > 10) return VPMG_ERR_ARG;  // IPMWRITE > 10 stops the reference (vpm.f90:146)
+  } catch (...) {
+    return VPMG_ERR_ARG;
+  }
+  return VPMG_OK;
+}
+
+int vpmg_create(const vpmg_config* cfg, int device, vpmg_handle** out) {
+  if (!cfg || !out) return VPMG_ERR_ARG;
+  *out = nullptr;
+  if (cfg->interf_iproj < 2 || cfg->interf_iproj > 6) return VPMG_ERR_ARG;
+  if (cfg->ibctyp != 2) return VPMG_ERR_UNSUPPORTED;
+  if (cfg->idvpm != 1) return VPMG_ERR_UNSUPPORTED;
+  if (cfg->ncell_rem != 1) return VPMG_ERR_UNSUPPORTED;
+  if (cfg->ncoarse < 1 || cfg->dpm[0] <= 0 || cfg->dpm[1] <= 0 || cfg->dpm[2] <= 0) return VPMG_ERR_ARG;
+  vpmg_handle* h = new vpmg_handle();
+  h->cfg = *cfg;
+  if (device < 0) {
+    if (cudaGetDevice(&h->device) != cudaSuccess) { cudaGetLastError(); delete h; return VPMG_ERR_CUDA; }
+  } else {
+    h->device = device;
+  }
+  int rc = guarded(h, [&] {
+    VPMG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 10; ++i) VPMG_CUDA(cudaEventCreate(&h->ev[i]));
+    size_t fr = 0, tot = 0;
+    VPMG_CUDA(cudaMemGetInfo(&fr, &tot));
+    h->op_budget = std::min<long long>(100LL << 30, (long long)(0.6 * (double)fr));
+  });
+  if (rc != VPMG_OK) { delete h; return rc; }
+  *out = h;
+  return VPMG_OK;
+}
+
+int vpmg_destroy(vpmg_handle* h) {
+  if (!h) return VPMG_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (int i = 0; i < 10; ++i)
+    if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return VPMG_OK;
+}
+
+int vpmg_define_sizes(vpmg_handle* h, const double* xp, int nvr, int ntime) {
+  return guarded(h, [&] {
+    vpmg_sizes s = h->sz;
+    define_sizes(h, xp, nvr, ntime, s);
+    if (!h->prepared || !same_sizes(s, h->sz)) {
+      h->sz = s;
+      h->sized = true;
+      prepare(h);
+    }
+  });
+}
+
+int vpmg_get_sizes(const vpmg_handle* h, vpmg_sizes* out) {
+  if (!h || !out) return VPMG_ERR_ARG;
+  if (!h->sized) return VPMG_ERR_STATE;
+  *out = h->sz;
+  return VPMG_OK;
+}
+
+int vpmg_set_particles(vpmg_handle* h, const double* xp, const double* qp, int nvr, int capacity) {
+  (void)capacity;
+  return guarded(h, [&] {
+    upload_particles(h, xp, qp, nvr);
+    VPMG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int vpmg_get_particles(vpmg_handle* h, double* xp, double* qp, int* nvr, int capacity) {
+  return guarded(h, [&] {
+    VPMG_CHECK(nvr, VPMG_ERR_ARG, "nvr is null");
+    *nvr = h->np;
+    VPMG_CHECK(h->np <= capacity, VPMG_ERR_CAPACITY, "caller arrays too small");
+    download_particles(h, xp, qp, h->np);
+  });
+}
+
+int vpmg_get_particle_velocity(vpmg_handle* h, double* up, double* gp, int nvr) {
+  return guarded(h, [&] {
+    VPMG_CHECK(nvr <= h->parts.capacity && nvr >= 0, VPMG_ERR_ARG, "nvr out of range");
+    if (nvr == 0) return;
+    VPMG_CUDA(cudaMemcpyAsync(up, h->parts.up.p, sizeof(double) * 3 * nvr, cudaMemcpyDeviceToHost, h->stream));
+    VPMG_CUDA(cudaMemcpyAsync(gp, h->parts.gp.p, sizeof(double) * 3 * nvr, cudaMemcpyDeviceToHost, h->stream));
+    VPMG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int vpmg_num_particles(const vpmg_handle* h, int* nvr) {
+  if (!h || !nvr) return VPMG_ERR_ARG;
+  *nvr = h->np;
+  return VPMG_OK;
+}
+
+int vpmg_step(vpmg_handle* h, double dt, const double uinf[3], int do_remesh) {
+  return guarded(h, [&] {
+    VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
+    const double u0[3] = {uinf ? uinf[0] : 0.0, uinf ? uinf[1] : 0.0, uinf ? uinf[2] : 0.0};
+    ev_mark(h, 0);
+    bin_particles(h->parts, h->np, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
+    field_step(h);
+    m2p_step(h, true, true, dt, u0);
+    if (do_remesh) remesh(h);
+    else ev_mark(h, 9);
+    VPMG_CUDA(cudaStreamSynchronize(h->stream));
+    finish_phase_times(h);
+  });
+}
+
+int vpmg_remesh_device(vpmg_handle* h) {
+  return guarded(h, [&] {
+    VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
+    remesh(h);
+    VPMG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int* nvr, int neqpm, int whattodo,
+             int ntime, double ni, int nvrm) {
+  (void)ni;
+  return guarded(h, [&] {
+    VPMG_CHECK(nvr, VPMG_ERR_ARG, "NVR is null");
+    VPMG_CHECK(neqpm == 3, VPMG_ERR_UNSUPPORTED, "neqpm must be 3");
+    VPMG_CHECK(*nvr <= nvrm, VPMG_ERR_ARG, "NVR > NVRM");
+    if (whattodo == 0) {
+      vpmg_sizes s = h->sz;
+      define_sizes(h, xp, *nvr, ntime, s);
+      if (!h->prepared || !same_sizes(s, h->sz)) {
+        h->sz = s;
+        h->sized = true;
+        prepare(h);
+      }
+      return;
+    }
+    VPMG_CHECK(whattodo == 2, VPMG_ERR_UNSUPPORTED, "WhatToDo 1, 4, 5 are outside the single-block step");
+    if (*nvr == 0) return;  // vpm.f90:171
+    upload_particles(h, xp, qp, *nvr);
+    const double u0[3] = {0, 0, 0};
+    bin_particles(h->parts, h->np, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
+    field_step(h);
+    m2p_step(h, true, false, 0.0, u0);
+    VPMG_CUDA(cudaMemcpyAsync(up, h->parts.up.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost, h->stream));
+    VPMG_CUDA(cudaMemcpyAsync(gp, h->parts.gp.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost, h->stream));
+    VPMG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int vpmg_remesh_particles_3d(vpmg_handle* h, int iflag, double* xp, double* qp, int* nvr, int capacity) {
+  return guarded(h, [&] {
+    VPMG_CHECK(iflag == 1, VPMG_ERR_UNSUPPORTED, "remesh_particles_3d(iflag /= 1)");
+    VPMG_CHECK(nvr, VPMG_ERR_ARG, "NVR is null");
+    upload_particles(h, xp, qp, *nvr);
+    remesh(h);
+    *nvr = h->np;
+    VPMG_CHECK(h->np <= capacity, VPMG_ERR_CAPACITY, "remesh produced more particles than the caller's capacity");
+    download_particles(h, xp, qp, h->np);
+  });
+}
+
+int vpmg_pmesh(vpmg_handle* h, double* const sol[3], const double* const rhs[3], const double xbound[6],
+               const double dpm[3], const int nn[3], const int nn_bl[6], int iynbc, int itree, int levmax) {
+  return guarded(h, [&] {
+    VPMG_CHECK(sol && rhs && xbound && dpm && nn && nn_bl, VPMG_ERR_ARG, "null argument");
+    const Grid g = make_grid(xbound, dpm, nn);
+    const size_t n = g.count();
+    DBuf<double> r, s, s0, w;
+    r.ensure(3 * n); s.ensure(3 * n); s0.ensure(n);
+    for (int c = 0; c < 3; ++c) {
+      VPMG_CUDA(cudaMemcpyAsync(r.p + c * n, rhs[c], sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+      VPMG_CUDA(cudaMemcpyAsync(s.p + c * n, sol[c], sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    }
+    DirichletPlan dp;
+    if (iynbc == 1) {
+      const int full[6] = {0, 0, 0, nn[0] - 1, nn[1] - 1, nn[2] - 1};
+      dirichlet_prepare(dp, nn, full, dpm, h->stream);
+      w.ensure((size_t)dp.m[0] * dp.m[1] * dp.m[2]);
+      fill_zero(s0.p, n, h->stream);
+      BoundaryOp bo;
+      boundary_prepare(bo, g, itree == 1 ? levmax : 0, h->op_budget, h->stream);
+      for (int c = 0; c < 3; ++c) {
+        dirichlet_solve(dp, r.p + c * n, s0.p, true, w.p, h->stream);
+        boundary_panels(bo, g, s0.p, c, h->stream);
+      }
+      double* sp[3] = {s.p, s.p + n, s.p + 2 * n};
+      boundary_apply(bo, g, sp, h->stream);
+      for (int c = 0; c < 3; ++c) dirichlet_solve(dp, r.p + c * n, s.p + c * n, false, w.p, h->stream);
+      VPMG_CUDA(cudaStreamSynchronize(h->stream));
+    } else {
+      const int box[6] = {nn_bl[0] - 1, nn_bl[1] - 1, nn_bl[2] - 1, nn_bl[3] - 1, nn_bl[4] - 1, nn_bl[5] - 1};
+      dirichlet_prepare(dp, nn, box, dpm, h->stream);
+      w.ensure((size_t)dp.m[0] * dp.m[1] * dp.m[2]);
+      for (int c = 0; c < 3; ++c) dirichlet_solve(dp, r.p + c * n, s.p + c * n, false, w.p, h->stream);
+    }
+    for (int c = 0; c < 3; ++c)
+      VPMG_CUDA(cudaMemcpyAsync(sol[c], s.p + c * n, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+    VPMG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int vpmg_project_particles_3d(vpmg_handle* h, const double* xp, const double* qp, int nvr, double* const rhs[3]) {
+  return guarded(h, [&] {
+    upload_particles(h, xp, qp, nvr);
+    const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
+    bin_particles(h->parts, h->np, mg, h->bins, h->stream);
+    const size_t N = h->gglob.count();
+    double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
+    deposit(h->parts, mg, h->bins, R, h->stream);
+    for (int c = 0; c < 3; ++c)
+      VPMG_CUDA(cudaMemcpyAsync(rhs[c], R[c], sizeof(double) * N, cudaMemcpyDeviceToHost, h->stream));
+    VPMG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int vpmg_get_field(vpmg_handle* h, int which, double* out, size_t capacity, size_t* count) {
+  return guarded(h, [&] {
+    VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "no mesh yet");
+    const size_t N = h->gglob.count(), NB = h->gbl.count(), NC = h->gco.count();
+    const double* src = nullptr;
+    size_t n = 0;
+    switch (which) {
+      case VPMG_F_RHS: src = h->rhs.p; n = N; break;
+      case VPMG_F_SOL: src = h->sol.p; n = N; break;
+      case VPMG_F_VEL: src = h->vel.p; n = N; break;
+      case VPMG_F_DEF: src = h->def.p; n = N; break;
+      case VPMG_F_BL_SOL1:
+        VPMG_CHECK(h->bl_sol1_copy.p, VPMG_ERR_STATE, "intermediates are kept only after vpmg_set_profiling(h, 2)");
+        src = h->bl_sol1_copy.p; n = NB; break;
+      case VPMG_F_COARSE_RHS: src = h->crhs.p; n = NC; break;
+      case VPMG_F_COARSE_SOL: src = h->csol.p; n = NC; break;
+      case VPMG_F_BL_FINAL: src = h->sol_bl.p; n = NB; break;
+      default: throw Error{VPMG_ERR_ARG, "unknown field id"};
+    }
+    if (count) *count = n;
+    if (!out) return;
+    VPMG_CHECK(capacity >= 3 * n, VPMG_ERR_ARG, "output too small");
+    VPMG_CUDA(cudaMemcpyAsync(out, src, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
+    VPMG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+long long vpmg_kernel_launches(const vpmg_handle* h) { return h ? h->launches : -1; }
+
+int vpmg_phase_times(const vpmg_handle* h, double ms[9]) {
+  if (!h || !ms) return VPMG_ERR_ARG;
+  for (int i = 0; i < 9; ++i) ms[i] = h->phase_ms[i];
+  return VPMG_OK;
+}
+
+int vpmg_tree_stats(const vpmg_handle* h, long long* interactions, long long* bytes, int* precomputed) {
+  if (!h) return VPMG_ERR_ARG;
+  if (interactions) *interactions = h->bo_bl.nnz;
+  if (bytes) *bytes = h->bo_bl.bytes();
+  if (precomputed) *precomputed = h->bo_bl.precomputed ? 1 : 0;
+  return VPMG_OK;
+}
+
+int vpmg_set_profiling(vpmg_handle* h, int on) {
+  if (!h) return VPMG_ERR_ARG;
+  h->profile = on != 0;
+  h->keep_intermediates = on >= 2;
+  return VPMG_OK;
+}
+
+int vpmg_set_operator_budget(vpmg_handle* h, long long bytes) {
+  if (!h) return VPMG_ERR_ARG;
+  h->op_budget = bytes;
+  return VPMG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,346 @@
+// boundary.cu -- infinite-domain boundary values on the GPU.
+//
+// Replaces infdomain_3d after its zero-BC solve (source/pinfdomain.f90:86-158):
+//   * calc_normalderiv_3d (pinfdomain.f90:294-547): 4th-order one-sided
+//     normal derivative at the 4 corners of every boundary cell -> panel
+//     source strengths;
+//   * build_level_nbound_3d (pinfdomain.f90:875-1530): area-weighted source
+//     of every quadtree cell (topology and geometry come from the host);
+//   * Bounds3d_lev / tree_calc_3d (pmbound.f90:980-1249): for every
+//     boundary node, sum of -s dS / r over the tree with the opening test
+//     r < 10 sqrt(dS), then SOL += sum / (4 pi).
+// The walk is evaluated with explicitly rounded operations so its opening
+// decisions are those of the reference's expressions.  Because the mesh is
+// frozen after the first step, the walk's interaction list (cell, dS/r) is
+// the same every step: when it fits the memory budget it is recorded once
+// (count + fill passes) and each step is a CSR product with the three
+// source components (3 FP64 FMAs per interaction instead of ~30 FP64
+// operations for sqrt + division + geometry).
+#include <cmath>
+
+#include "tree_host.h"
+#include "vpmg_internal.h"
+
+namespace vpmg {
+
+namespace {
+
+constexpr int kMaxLev = 16;
+
+struct WalkDev {
+  const double *cx, *cy, *cz, *cds, *cthr;
+  const int* child;
+  const int* flags;
+  const double* s0;
+  const double* s1;
+  const double* s2;
+  const int* tgt_node;
+  const double *tx, *ty, *tz;
+  int top0, ntop, levmax, ntarget;
+  double lg;      // log((sqrt2-1)/(sqrt2+1))
+  double inv_pi4;
+};
+
+enum { kAccum = 0, kCount = 1, kFill = 2 };
+
+template <int MODE>
+__global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ o1, double* __restrict__ o2,
+                       int* __restrict__ counts, const long long* __restrict__ rowptr, int* __restrict__ col,
+                       double* __restrict__ wgt) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= W.ntarget) return;
+  const double X = W.tx[t], Y = W.ty[t], Z = W.tz[t];
+  int parent[kMaxLev], pos[kMaxLev], cnt[kMaxLev];
+  int L = W.levmax;
+  pos[L] = 0;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  int ni = 0;
+  long long out = 0;
+  if (MODE == kFill) out = rowptr[t];
+  while (true) {
+    int c;
+    if (L == W.levmax) {
+      if (pos[L] >= W.ntop) break;
+      c = W.top0 + pos[L]++;
+    } else {
+      if (pos[L] >= cnt[L]) {
+        ++L;
+        continue;
+      }
+      c = W.child[4 * parent[L] + pos[L]++];
+    }
+    const double XR = __dsub_rn(W.cx[c], X), YR = __dsub_rn(W.cy[c], Y), ZR = __dsub_rn(W.cz[c], Z);
+    const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(XR, XR), __dmul_rn(YR, YR)), __dmul_rn(ZR, ZR)));
+    const int fl = W.flags[c];
+    if ((r < W.cthr[c] && L > 0) || fl < 0) {
+      parent[L - 1] = c;
+      cnt[L - 1] = (fl < 0) ? 2 : 4;
+      pos[L - 1] = 0;
+      --L;
+      continue;
+    }
+    if (MODE == kCount) {
+      ++ni;
+      continue;
+    }
+    const double DS = W.cds[c];
+    const double w = (r > 1e-05) ? __ddiv_rn(DS, r) : -2.0 * __dsqrt_rn(DS) * W.lg;
+    if (MODE == kFill) {
+      col[out] = c;
+      wgt[out] = w;
+      ++out;
+    } else {
+      a0 = fma(-W.s0[c], w, a0);
+      a1 = fma(-W.s1[c], w, a1);
+      a2 = fma(-W.s2[c], w, a2);
+    }
+  }
+  if (MODE == kCount) {
+    counts[t] = ni;
+  } else if (MODE == kAccum) {
+    const int node = W.tgt_node[t];
+    o0[node] += a0 * W.inv_pi4;
+    o1[node] += a1 * W.inv_pi4;
+    o2[node] += a2 * W.inv_pi4;
+  }
+}
+
+// One warp per boundary node: lanes stride over the node's interaction
+// list (coalesced), fixed-shape shuffle reduction (deterministic).
+__global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__ rowptr, const int* __restrict__ col,
+                                                   const double* __restrict__ wgt, const double* __restrict__ s0,
+                                                   const double* __restrict__ s1, const double* __restrict__ s2,
+                                                   const int* __restrict__ tgt_node, int ntarget, double inv_pi4,
+                                                   double* __restrict__ o0, double* __restrict__ o1,
+                                                   double* __restrict__ o2) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ntarget) return;
+  const long long b = rowptr[warp], e = rowptr[warp + 1];
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (long long k = b + lane; k < e; k += 32) {
+    const int c = __ldg(&col[k]);
+    const double w = __ldg(&wgt[k]);
+    a0 = fma(__ldg(&s0[c]), w, a0);
+    a1 = fma(__ldg(&s1[c]), w, a1);
+    a2 = fma(__ldg(&s2[c]), w, a2);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+  }
+  if (lane == 0) {
+    const int node = tgt_node[warp];
+    o0[node] += -a0 * inv_pi4;
+    o1[node] += -a1 * inv_pi4;
+    o2[node] += -a2 * inv_pi4;
+  }
+}
+
+// calc_normalderiv_3d: one thread per panel.
+__global__ void k_normal_deriv(const double* __restrict__ sol0, int NX, int NY, int NZ, const int* __restrict__ face,
+                               const int* __restrict__ pi, const int* __restrict__ pj, const int* __restrict__ pk,
+                               int nbound, double invx, double invy, double invz, double* __restrict__ src) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nbound) return;
+  const double a1 = 25.0 / 12.0, a2 = -4.0, a3 = 3.0, a4 = -4.0 / 3.0, a5 = 0.25;
+  const int f = face[p];
+  const int i = pi[p] - 1, j = pj[p] - 1, k = pk[p] - 1;  // 0-based
+  const long long sx = 1, sy = NX, sz = (long long)NX * NY;
+  long long step, e1, e2;
+  double inv;
+  if (f < 2) { step = (f == 0) ? sx : -sx; e1 = sy; e2 = sz; inv = invx; }
+  else if (f < 4) { step = (f == 2) ? sy : -sy; e1 = sx; e2 = sz; inv = invy; }
+  else { step = (f == 4) ? sz : -sz; e1 = sx; e2 = sy; inv = invz; }
+  const long long base = i * sx + j * sy + k * sz;
+  // corner order of the reference: (0,0), (1,0), (1,1), (0,1) in the face's (fast, slow) axes
+  const long long corner[4] = {base, base + e1, base + e1 + e2, base + e2};
+  double ps[4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const long long n0 = corner[m];
+    const double v0 = sol0[n0], v1 = sol0[n0 + step], v2 = sol0[n0 + 2 * step], v3 = sol0[n0 + 3 * step],
+                 v4 = sol0[n0 + 4 * step];
+    ps[m] = inv * ((((a1 * v0 + a2 * v1) + a3 * v2) + a4 * v3) + a5 * v4);
+  }
+  src[p] = 0.25 * (((ps[0] + ps[1]) + ps[2]) + ps[3]);
+}
+
+// build_level_nbound_3d sources: area-weighted mean over the istep^2 leaves.
+__global__ void k_aggregate(const int* __restrict__ leaf0, const int* __restrict__ rowlen, const int* __restrict__ istep,
+                            const double* __restrict__ cds, int first, int ncell, double* __restrict__ s0,
+                            double* __restrict__ s1, double* __restrict__ s2) {
+  const int c = first + blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= first + ncell) return;
+  const int l0 = leaf0[c];
+  if (l0 < 0) return;
+  const int n1 = rowlen[c], st = istep[c];
+  double w0 = 0.0, w1 = 0.0, w2 = 0.0;
+  for (int mm = 0; mm < st; ++mm)
+    for (int nn = 0; nn < st; ++nn) {
+      const int leaf = l0 + mm * n1 + nn;
+      const double s = cds[leaf];
+      w0 = s0[leaf] * s + w0;
+      w1 = s1[leaf] * s + w1;
+      w2 = s2[leaf] * s + w2;
+    }
+  const double sc = cds[c];
+  s0[c] = w0 / sc;
+  s1[c] = w1 / sc;
+  s2[c] = w2 / sc;
+}
+
+template <class T>
+void upload(DBuf<T>& b, const std::vector<T>& h) {
+  b.ensure(h.size());
+  if (!h.empty()) VPMG_CUDA(cudaMemcpy(b.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+}
+
+WalkDev walk_dev(const BoundaryOp& B) {
+  WalkDev W;
+  W.cx = B.cx.p; W.cy = B.cy.p; W.cz = B.cz.p; W.cds = B.cds.p; W.cthr = B.cthr.p;
+  W.child = B.child.p; W.flags = B.flags.p;
+  W.s0 = B.csrc.p; W.s1 = B.csrc.p + B.ncell_total; W.s2 = B.csrc.p + 2 * (size_t)B.ncell_total;
+  W.tgt_node = B.tgt_node.p; W.tx = B.tx.p; W.ty = B.ty.p; W.tz = B.tz.p;
+  W.top0 = B.lev_off[B.levmax];
+  W.ntop = B.nbound_lev[B.levmax];
+  W.levmax = B.levmax;
+  W.ntarget = B.ntarget;
+  W.lg = std::log((std::sqrt(2.0) - 1.0) / (std::sqrt(2.0) + 1.0));
+  W.inv_pi4 = 1.0 / (4.0 * kPI);
+  return W;
+}
+
+}  // namespace
+
+long long BoundaryOp::bytes() const {
+  return (long long)(rowptr.bytes() + col.bytes() + w.bytes() + cx.bytes() * 5 + child.bytes() + csrc.bytes());
+}
+
+void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s) {
+  VPMG_CHECK(levmax >= 0 && levmax < kMaxLev - 1, VPMG_ERR_ARG, "levmax out of range");
+  TreeGeom T;
+  try {
+    build_tree_geometry(g.xmin, g.d, g.n, levmax, T);
+  } catch (const std::exception& e) {
+    throw Error{VPMG_ERR_TREE, e.what()};
+  }
+  B.levmax = levmax;
+  B.nbound = T.nbound;
+  B.nbound_lev = T.nbound_lev;
+  B.lev_off.assign(levmax + 2, 0);
+  for (int l = 0; l <= levmax; ++l) B.lev_off[l + 1] = B.lev_off[l] + T.nbound_lev[l];
+  B.ncell_total = B.lev_off[levmax + 1];
+  const int NC = B.ncell_total;
+  std::vector<double> cx(NC), cy(NC), cz(NC), cds(NC), thr(NC);
+  std::vector<int> child(4 * (size_t)NC, -1), flags(NC), leaf0(NC), rowlen(NC), istep(NC);
+  for (int l = 0; l <= levmax; ++l)
+    for (int ic = 0; ic < T.nbound_lev[l]; ++ic) {
+      const Cell& c = T.cells[(size_t)l * T.nbound + ic];
+      const int f = B.lev_off[l] + ic;
+      cx[f] = c.x; cy[f] = c.y; cz[f] = c.z; cds[f] = c.ds; thr[f] = c.thr;
+      flags[f] = c.ilev[5];
+      VPMG_CHECK(c.ilev[5] != 0, VPMG_ERR_TREE, "Something is wrong with the tree (ilev_t(.,.,6) == 0)");
+      leaf0[f] = (l > 0) ? c.leaf0 : -1;
+      rowlen[f] = c.rowlen;
+      istep[f] = c.istep;
+      if (l > 0) {
+        const int nch = (c.ilev[5] < 0) ? 2 : 4;
+        for (int m = 0; m < nch; ++m) {
+          const int ch = c.ilev[m];
+          VPMG_CHECK(ch >= 1 && ch <= T.nbound_lev[l - 1], VPMG_ERR_TREE, "tree child index out of range");
+          child[4 * (size_t)f + m] = B.lev_off[l - 1] + ch - 1;
+        }
+      }
+    }
+  upload(B.cx, cx); upload(B.cy, cy); upload(B.cz, cz); upload(B.cds, cds); upload(B.cthr, thr);
+  upload(B.child, child); upload(B.flags, flags); upload(B.agg_leaf0, leaf0); upload(B.agg_rowlen, rowlen);
+  upload(B.agg_istep, istep);
+  B.csrc.ensure(3 * (size_t)NC);
+  std::vector<int> pf(B.nbound), pi(B.nbound), pj(B.nbound), pk(B.nbound);
+  for (int p = 0; p < B.nbound; ++p) {
+    pf[p] = T.panels[p].face; pi[p] = T.panels[p].i; pj[p] = T.panels[p].j; pk[p] = T.panels[p].k;
+  }
+  upload(B.pan_face, pf); upload(B.pan_i, pi); upload(B.pan_j, pj); upload(B.pan_k, pk);
+  B.ntarget = (int)T.targets.size();
+  std::vector<int> tn(B.ntarget);
+  std::vector<double> tx(B.ntarget), ty(B.ntarget), tz(B.ntarget);
+  for (int t = 0; t < B.ntarget; ++t) {
+    tn[t] = (int)T.targets[t].node; tx[t] = T.targets[t].x; ty[t] = T.targets[t].y; tz[t] = T.targets[t].z;
+  }
+  upload(B.tgt_node, tn); upload(B.tx, tx); upload(B.ty, ty); upload(B.tz, tz);
+  // ---- record the interaction lists if they fit --------------------------
+  B.precomputed = false;
+  B.nnz = 0;
+  B.rowptr.release(); B.col.release(); B.w.release();
+  const WalkDev W = walk_dev(B);
+  const int blocks = (B.ntarget + 127) / 128;
+  DBuf<int> counts;
+  counts.ensure(B.ntarget);
+  k_walk<kCount><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, counts.p, nullptr, nullptr, nullptr);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+  std::vector<int> hc(B.ntarget);
+  VPMG_CUDA(cudaMemcpyAsync(hc.data(), counts.p, sizeof(int) * B.ntarget, cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  std::vector<long long> rp(B.ntarget + 1, 0);
+  for (int t = 0; t < B.ntarget; ++t) rp[t + 1] = rp[t] + hc[t];
+  B.nnz = rp[B.ntarget];
+  const long long need = B.nnz * (long long)(sizeof(int) + sizeof(double)) + (long long)sizeof(long long) * (B.ntarget + 1);
+  size_t free_b = 0, total_b = 0;
+  VPMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  if (budget_bytes > 0 && need <= budget_bytes && need < (long long)(0.8 * (double)free_b)) {
+    try {
+      upload(B.rowptr, rp);
+      B.col.ensure((size_t)B.nnz);
+      B.w.ensure((size_t)B.nnz);
+      k_walk<kFill><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, nullptr, B.rowptr.p, B.col.p, B.w.p);
+      VPMG_LAUNCHED();
+      VPMG_CUDA(cudaGetLastError());
+      VPMG_CUDA(cudaStreamSynchronize(s));
+      B.precomputed = true;
+    } catch (const Error& e) {
+      if (e.status != VPMG_ERR_NOMEM) throw;
+      B.rowptr.release(); B.col.release(); B.w.release();
+      B.precomputed = false;
+    }
+  }
+}
+
+void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp, cudaStream_t s) {
+  double* dst = B.csrc.p + (size_t)comp * B.ncell_total;  // level-0 part = panels
+  k_normal_deriv<<<(B.nbound + 255) / 256, 256, 0, s>>>(sol0, g.n[0], g.n[1], g.n[2], B.pan_face.p, B.pan_i.p,
+                                                        B.pan_j.p, B.pan_k.p, B.nbound, 1.0 / g.d[0], 1.0 / g.d[1],
+                                                        1.0 / g.d[2], dst);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStream_t s) {
+  (void)g;
+  double* s0 = B.csrc.p;
+  double* s1 = B.csrc.p + B.ncell_total;
+  double* s2 = B.csrc.p + 2 * (size_t)B.ncell_total;
+  // levels 1..levmax aggregate level-0 panels (source_bound_lev)
+  for (int l = 1; l <= B.levmax; ++l) {
+    const int n = B.nbound_lev[l];
+    if (n <= 0) continue;
+    k_aggregate<<<(n + 255) / 256, 256, 0, s>>>(B.agg_leaf0.p, B.agg_rowlen.p, B.agg_istep.p, B.cds.p, B.lev_off[l], n,
+                                                s0, s1, s2);
+    VPMG_LAUNCHED();
+  }
+  if (B.precomputed) {
+    const long long threads = (long long)B.ntarget * 32;
+    k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, s0, s1, s2, B.tgt_node.p,
+                                                                  B.ntarget, 1.0 / (4.0 * kPI), sol[0], sol[1], sol[2]);
+  } else {
+    const WalkDev W = walk_dev(B);
+    k_walk<kAccum><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, sol[0], sol[1], sol[2], nullptr, nullptr, nullptr, nullptr);
+  }
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+}  // namespace vpmg

@@ -1,0 +1,211 @@
+// fields.cu -- mesh-to-mesh kernels of the step.
+//
+//  * rhsscat_3d / solget_3d for one block (source/vpm_mpi.f90:199-328):
+//    box copies between the global mesh and the padded block;
+//  * YAPS sampling, coarse Laplacian and face interpolation
+//    (source/yaps3d.f90:104-138, 1914-2016) driven by host-built maps;
+//  * calc_velocity_serial_3d(1) (source/vpm_gcalc.f90:1-136): central-
+//    difference curl and the conservative stretching term.
+#include "fields.h"
+
+namespace vpmg {
+
+namespace {
+
+__global__ void k_box_copy(const double* __restrict__ src, int sx, int sy, int so0, int so1, int so2,
+                           double* __restrict__ dst, int dx, int dy, int do0, int do1, int do2, int e0, int e1, int e2) {
+  const size_t n = (size_t)e0 * e1 * e2;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % e0);
+    const int j = (int)((t / e0) % e1);
+    const int k = (int)(t / ((size_t)e0 * e1));
+    dst[(size_t)(do0 + i) + (size_t)dx * ((do1 + j) + (size_t)dy * (do2 + k))] =
+        src[(size_t)(so0 + i) + (size_t)sx * ((so1 + j) + (size_t)sy * (so2 + k))];
+  }
+}
+
+__global__ void k_sample(const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
+                         const long long* __restrict__ src, const long long* __restrict__ dst, int n,
+                         double* __restrict__ c0, double* __restrict__ c1, double* __restrict__ c2) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  c0[dst[t]] = a0[src[t]];
+  c1[dst[t]] = a1[src[t]];
+  c2[dst[t]] = a2[src[t]];
+}
+
+__global__ void k_coarse_lap(const double* __restrict__ s, double* __restrict__ r, int CX, int CY, int lo0, int lo1,
+                             int lo2, int e0, int e1, int e2, double ih0, double ih1, double ih2) {
+  const size_t n = (size_t)e0 * e1 * e2;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = lo0 + (int)(t % e0);
+  const int j = lo1 + (int)((t / e0) % e1);
+  const int k = lo2 + (int)(t / ((size_t)e0 * e1));
+  const size_t sy = CX, sz = (size_t)CX * CY;
+  const size_t id = (size_t)i + sy * j + sz * k;
+  const double c = s[id];
+  r[id] = ((s[id + 1] - 2.0 * c) + s[id - 1]) * ih0 + ((s[id + sy] - 2.0 * c) + s[id - sy]) * ih1 +
+          ((s[id + sz] - 2.0 * c) + s[id - sz]) * ih2;
+}
+
+__global__ void k_face_interp(const long long* __restrict__ node, const long long* __restrict__ cbase,
+                              const double* __restrict__ w, const int* __restrict__ flagged, int n,
+                              const double* __restrict__ csol, const double* __restrict__ samp, int CX, int CY,
+                              double* __restrict__ sol) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const double* wt = w + 9 * (size_t)t;
+  const size_t b = cbase[t];
+  const size_t sy = CX, sz = (size_t)CX * CY;
+  const bool fl = flagged[t] != 0;
+  double v = sol[node[t]];
+  for (int kc = 0; kc < 3; ++kc)
+    for (int jc = 0; jc < 3; ++jc)
+      for (int ic = 0; ic < 3; ++ic) {
+        const double f = (wt[ic] * wt[3 + jc]) * wt[6 + kc];
+        const size_t cid = b + ic + sy * jc + sz * kc;
+        const double sm = samp[cid];
+        const double add = fl ? sm : 0.0;
+        v = v + f * ((csol[cid] - sm) + add);
+      }
+  sol[node[t]] = v;
+}
+
+// u = curl psi on nodes 1..N-2 (0-based); other nodes keep zero.
+__global__ void k_velocity(const double* __restrict__ p0, const double* __restrict__ p1, const double* __restrict__ p2,
+                           int NX, int NY, int NZ, double i2x, double i2y, double i2z, double* __restrict__ u0,
+                           double* __restrict__ u1, double* __restrict__ u2) {
+  const int ex = NX - 2, ey = NY - 2, ez = NZ - 2;
+  const size_t n = (size_t)ex * ey * ez;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = 1 + (int)(t % ex), j = 1 + (int)((t / ex) % ey), k = 1 + (int)(t / ((size_t)ex * ey));
+  const size_t sy = NX, sz = (size_t)NX * NY;
+  const size_t id = i + sy * j + sz * k;
+  const double dx1 = (p1[id + 1] - p1[id - 1]) * i2x, dx2 = (p2[id + 1] - p2[id - 1]) * i2x;
+  const double dy0 = (p0[id + sy] - p0[id - sy]) * i2y, dy2 = (p2[id + sy] - p2[id - sy]) * i2y;
+  const double dz0 = (p0[id + sz] - p0[id - sz]) * i2z, dz1 = (p1[id + sz] - p1[id - sz]) * i2z;
+  u0[id] = dy2 - dz1;
+  u1[id] = -(dx2 - dz0);
+  u2[id] = dx1 - dy0;
+}
+
+// Stretching  SOL(m) = -sum_j d(RHS_j u_m)/dx_j  on nodes 2..N-3 (0-based).
+__global__ void k_deformation(const double* __restrict__ r0, const double* __restrict__ r1, const double* __restrict__ r2,
+                              const double* __restrict__ u0, const double* __restrict__ u1,
+                              const double* __restrict__ u2, int NX, int NY, int NZ, double i2x, double i2y, double i2z,
+                              double* __restrict__ g0, double* __restrict__ g1, double* __restrict__ g2) {
+  const int ex = NX - 4, ey = NY - 4, ez = NZ - 4;
+  const size_t n = (size_t)ex * ey * ez;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = 2 + (int)(t % ex), j = 2 + (int)((t / ex) % ey), k = 2 + (int)(t / ((size_t)ex * ey));
+  const size_t sy = NX, sz = (size_t)NX * NY;
+  const size_t id = i + sy * j + sz * k;
+  const double rxp = r0[id + 1], rxm = r0[id - 1], ryp = r1[id + sy], rym = r1[id - sy], rzp = r2[id + sz],
+               rzm = r2[id - sz];
+  const double* U[3] = {u0, u1, u2};
+  double* G[3] = {g0, g1, g2};
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const double* u = U[m];
+    const double a = -(rxp * u[id + 1] - rxm * u[id - 1]) * i2x;
+    const double b = -(ryp * u[id + sy] - rym * u[id - sy]) * i2y;
+    const double c = -(rzp * u[id + sz] - rzm * u[id - sz]) * i2z;
+    G[m][id] = (a + b) + c;
+  }
+}
+
+template <class T>
+void upload(DBuf<T>& b, const std::vector<T>& h) {
+  b.ensure(h.size());
+  if (!h.empty()) VPMG_CUDA(cudaMemcpy(b.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+}
+
+unsigned grid_for(size_t n, int threads) { return (unsigned)std::max<size_t>(1, (n + threads - 1) / threads); }
+
+}  // namespace
+
+void box_copy(const double* src, const int sdims[3], const int so[3], double* dst, const int ddims[3], const int dof[3],
+              const int ext[3], cudaStream_t s) {
+  const size_t n = (size_t)ext[0] * ext[1] * ext[2];
+  if (!n) return;
+  k_box_copy<<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 32), 256, 0, s>>>(
+      src, sdims[0], sdims[1], so[0], so[1], so[2], dst, ddims[0], ddims[1], dof[0], dof[1], dof[2], ext[0], ext[1], ext[2]);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void YapsDev::prepare(const YapsGeom& Y) {
+  std::vector<long long> fnode(Y.faces.size()), fcb(Y.faces.size());
+  std::vector<double> fw(9 * Y.faces.size());
+  std::vector<int> ffl(Y.faces.size());
+  for (size_t t = 0; t < Y.faces.size(); ++t) {
+    fnode[t] = Y.faces[t].node;
+    fcb[t] = Y.faces[t].cbase;
+    for (int m = 0; m < 9; ++m) fw[9 * t + m] = Y.faces[t].w[m];
+    ffl[t] = Y.faces[t].flagged;
+  }
+  upload(samp_src, Y.samp_src);
+  upload(samp_dst, Y.samp_dst);
+  upload(face_node, fnode);
+  upload(face_cbase, fcb);
+  upload(face_w, fw);
+  upload(face_flag, ffl);
+  nsamp = (int)Y.samp_src.size();
+  nface = (int)Y.faces.size();
+  for (int d = 0; d < 6; ++d) map[d] = Y.map[d];
+}
+
+void yaps_sample(const YapsDev& Y, const double* const sbl[3], double* const samp[3], cudaStream_t s) {
+  k_sample<<<grid_for(Y.nsamp, 256), 256, 0, s>>>(sbl[0], sbl[1], sbl[2], Y.samp_src.p, Y.samp_dst.p, Y.nsamp, samp[0],
+                                                  samp[1], samp[2]);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void yaps_coarse_rhs(const YapsDev& Y, const int cdims[3], const double dc[3], const double* const samp[3],
+                     double* const crhs[3], cudaStream_t s) {
+  const int lo[3] = {Y.map[0], Y.map[1], Y.map[2]};  // 1-based map(1:3)+1  ->  0-based map(1:3)
+  const int e[3] = {Y.map[3] - Y.map[0] - 1, Y.map[4] - Y.map[1] - 1, Y.map[5] - Y.map[2] - 1};
+  if (e[0] <= 0 || e[1] <= 0 || e[2] <= 0) return;
+  const size_t n = (size_t)e[0] * e[1] * e[2];
+  for (int c = 0; c < 3; ++c) {
+    k_coarse_lap<<<grid_for(n, 256), 256, 0, s>>>(samp[c], crhs[c], cdims[0], cdims[1], lo[0], lo[1], lo[2], e[0], e[1],
+                                                  e[2], 1.0 / (dc[0] * dc[0]), 1.0 / (dc[1] * dc[1]),
+                                                  1.0 / (dc[2] * dc[2]));
+    VPMG_LAUNCHED();
+  }
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void yaps_face_interp(const YapsDev& Y, const int cdims[3], const double* const csol[3], const double* const samp[3],
+                      double* const sbl[3], cudaStream_t s) {
+  for (int c = 0; c < 3; ++c) {
+    k_face_interp<<<grid_for(Y.nface, 128), 128, 0, s>>>(Y.face_node.p, Y.face_cbase.p, Y.face_w.p, Y.face_flag.p,
+                                                         Y.nface, csol[c], samp[c], cdims[0], cdims[1], sbl[c]);
+    VPMG_LAUNCHED();
+  }
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void velocity_and_stretching(const int dims[3], const double h[3], const double* const psi[3], const double* const rhs[3],
+                             double* const vel[3], double* const def[3], cudaStream_t s) {
+  const int NX = dims[0], NY = dims[1], NZ = dims[2];
+  const double i2x = 1.0 / (2 * h[0]), i2y = 1.0 / (2 * h[1]), i2z = 1.0 / (2 * h[2]);
+  if (NX > 2 && NY > 2 && NZ > 2) {
+    const size_t n = (size_t)(NX - 2) * (NY - 2) * (NZ - 2);
+    k_velocity<<<grid_for(n, 256), 256, 0, s>>>(psi[0], psi[1], psi[2], NX, NY, NZ, i2x, i2y, i2z, vel[0], vel[1], vel[2]);
+    VPMG_LAUNCHED();
+  }
+  if (NX > 4 && NY > 4 && NZ > 4) {
+    const size_t n = (size_t)(NX - 4) * (NY - 4) * (NZ - 4);
+    k_deformation<<<grid_for(n, 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], vel[0], vel[1], vel[2], NX, NY, NZ, i2x, i2y,
+                                                   i2z, def[0], def[1], def[2]);
+    VPMG_LAUNCHED();
+  }
+  VPMG_CUDA(cudaGetLastError());
+}
+
+}  // namespace vpmg

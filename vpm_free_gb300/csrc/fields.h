@@ -1,0 +1,27 @@
+// fields.h -- mesh-to-mesh kernels (fields.cu).
+#pragma once
+#include "vpmg_internal.h"
+#include "yaps_host.h"
+
+namespace vpmg {
+
+struct YapsDev {
+  DBuf<long long> samp_src, samp_dst, face_node, face_cbase;
+  DBuf<double> face_w;
+  DBuf<int> face_flag;
+  int nsamp = 0, nface = 0;
+  int map[6] = {0, 0, 0, 0, 0, 0};
+  void prepare(const YapsGeom& Y);
+};
+
+void box_copy(const double* src, const int sdims[3], const int so[3], double* dst, const int ddims[3], const int dof[3],
+              const int ext[3], cudaStream_t s);
+void yaps_sample(const YapsDev& Y, const double* const sbl[3], double* const samp[3], cudaStream_t s);
+void yaps_coarse_rhs(const YapsDev& Y, const int cdims[3], const double dc[3], const double* const samp[3],
+                     double* const crhs[3], cudaStream_t s);
+void yaps_face_interp(const YapsDev& Y, const int cdims[3], const double* const csol[3], const double* const samp[3],
+                      double* const sbl[3], cudaStream_t s);
+void velocity_and_stretching(const int dims[3], const double h[3], const double* const psi[3], const double* const rhs[3],
+                             double* const vel[3], double* const def[3], cudaStream_t s);
+
+}  // namespace vpmg

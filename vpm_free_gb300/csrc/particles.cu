@@ -1,0 +1,356 @@
+// particles.cu -- particle <-> mesh kernels.
+//
+//  * deposition: project_particles_3D + project_vol3d(IDVPM=1)
+//    (source/pmproject.f90:43-153) as sort-by-cell plus a per-node gather:
+//    run-to-run deterministic, no floating-point atomics;
+//  * back_to_particles_3D(itype=1) (source/vpm_time.f90:62-107) fused with
+//    the forward Euler update of source/test.f90:104-117;
+//  * remesh_particles_3d(1) emission (source/vpm_remesh.f90:137-195) as an
+//    ordered stream compaction in (k,j,i) node order.
+#include <cmath>
+
+#include "particles.h"
+
+namespace vpmg {
+
+namespace {
+
+// M4' and the other projection kernels of source/pmproject.f90:391-431.
+__device__ __forceinline__ double proj_fun(int itype, double x) {
+  const double xa = fabs(x);
+  if (itype == 4) {
+    if (xa > 2.0) return 0.0;
+    if (xa >= 1.0) return 0.5 * ((2.0 - xa) * (2.0 - xa)) * (1.0 - xa);
+    return 1.0 - 2.5 * (xa * xa) + 1.5 * (xa * xa * xa);
+  }
+  if (itype == 3) {
+    if (xa > 1.5) return 0.0;
+    if (xa >= 0.5) return 0.5 * (-xa + 1.5) * (-xa + 1.5);
+    return 0.5 * (xa + 1.5) * (xa + 1.5) - 1.5 * (xa + 0.5) * (xa + 0.5);
+  }
+  if (itype == 2) return xa > 1.0 ? 0.0 : 1.0 - xa;
+  if (itype == 5) {
+    if (xa <= 0.5) return 1.0 - xa * xa;
+    if (xa <= 1.5) return 0.5 * (1.0 - xa) * (2.0 - xa);
+    return 0.0;
+  }
+  if (itype == 6) {
+    if (xa <= 1.0) return 1.0 - xa * xa;
+    if (xa <= 2.0) return 0.5 * (1.0 - xa) * (2.0 - xa);
+    return 0.0;
+  }
+  return 0.0;
+}
+
+// Cell index exactly as int((x - XMIN)/DX) (IEEE division, truncation).
+__device__ __forceinline__ int cell_of(double x, double xmin, double d) { return (int)__ddiv_rn(__dsub_rn(x, xmin), d); }
+
+__global__ void k_keys(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z, int np,
+                       MeshDev m, int* __restrict__ key, int* __restrict__ counts, int* __restrict__ err) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const int i0 = cell_of(x[p], m.xmin[0], m.d[0]);
+  const int j0 = cell_of(y[p], m.xmin[1], m.d[1]);
+  const int k0 = cell_of(z[p], m.xmin[2], m.d[2]);
+  // stencil nodes (0-based) c - ips .. c + ipf must lie on the mesh
+  const bool ok = (x[p] - m.xmin[0] >= 0.0) && (y[p] - m.xmin[1] >= 0.0) && (z[p] - m.xmin[2] >= 0.0) &&
+                  i0 - m.ips >= 0 && j0 - m.ips >= 0 && k0 - m.ips >= 0 && i0 + m.ipf < m.n[0] &&
+                  j0 + m.ipf < m.n[1] && k0 + m.ipf < m.n[2];
+  if (!ok) {
+    key[p] = -1;
+    atomicExch(err, 1);
+    return;
+  }
+  const int kk = i0 + m.n[0] * (j0 + m.n[1] * k0);
+  key[p] = kk;
+  atomicAdd(&counts[kk], 1);
+}
+
+__global__ void k_scatter(const int* __restrict__ key, int np, const int* __restrict__ starts, int* __restrict__ cursor,
+                          int* __restrict__ perm) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const int kk = key[p];
+  if (kk < 0) return;
+  const int slot = starts[kk] + atomicAdd(&cursor[kk], 1);
+  perm[slot] = p;
+}
+
+// Restores particle-index order inside each cell (determinism).
+__global__ void k_cell_order(const int* __restrict__ starts, int ncell, int* __restrict__ perm) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int s = starts[c], e = starts[c + 1];
+  if (e - s < 2) return;
+  for (int a = s + 1; a < e; ++a) {
+    const int v = perm[a];
+    int b = a - 1;
+    while (b >= s && perm[b] > v) {
+      perm[b + 1] = perm[b];
+      --b;
+    }
+    perm[b + 1] = v;
+  }
+}
+
+// Sorted records: per slot 4+4+4 stencil weights, 3 strengths, base cell x.
+__global__ void k_records(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
+                          const double* __restrict__ q0, const double* __restrict__ q1, const double* __restrict__ q2,
+                          const int* __restrict__ perm, int nsorted, MeshDev m, double* __restrict__ rec) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsorted) return;
+  const int p = perm[s];
+  const double pos[3] = {x[p], y[p], z[p]};
+  double* r = rec + (size_t)s * kRecLen;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int c0 = cell_of(pos[d], m.xmin[d], m.d[d]);
+    const double inv = 1.0 / m.d[d];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int node = c0 - m.ips + a;  // 0-based node = (i-1) of the reference
+      const double t = (pos[d] - m.xmin[d] - (double)node * m.d[d]) * inv;
+      r[4 * d + a] = (a <= m.ips + m.ipf) ? proj_fun(m.itype, t) : 0.0;
+    }
+    if (d == 0) r[15] = (double)c0;
+  }
+  r[12] = q0[p];
+  r[13] = q1[p];
+  r[14] = q2[p];
+}
+
+// One thread per node: gathers the particles of the (ips+ipf+1)^3 cells
+// whose stencil covers the node, in fixed cell and slot order.
+__global__ void k_deposit(const int* __restrict__ starts, const double* __restrict__ rec, MeshDev m, double inv_dv,
+                          double* __restrict__ r0, double* __restrict__ r1, double* __restrict__ r2) {
+  const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
+  const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (id >= N) return;
+  const int i = (int)(id % m.n[0]);
+  const int j = (int)((id / m.n[0]) % m.n[1]);
+  const int k = (int)(id / ((size_t)m.n[0] * m.n[1]));
+  const int w = m.ips + m.ipf;  // stencil width - 1
+  // particle base cell c covers nodes c-ips .. c+ipf  =>  c in [node-ipf, node+ips]
+  const int xlo = max(i - m.ipf, 0), xhi = min(i + m.ips, m.n[0] - 1);
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int ck = max(k - m.ipf, 0); ck <= min(k + m.ips, m.n[2] - 1); ++ck) {
+    const int iz = k - ck + m.ips;
+    for (int cj = max(j - m.ipf, 0); cj <= min(j + m.ips, m.n[1] - 1); ++cj) {
+      const int iy = j - cj + m.ips;
+      const size_t row = (size_t)m.n[0] * (cj + (size_t)m.n[1] * ck);
+      const int s = starts[row + xlo], e = starts[row + xhi + 1];
+      for (int t = s; t < e; ++t) {
+        const double* r = rec + (size_t)t * kRecLen;
+        const int ix = i - (int)r[15] + m.ips;
+        const double f = (r[ix] * r[4 + iy]) * r[8 + iz];
+        a0 = fma(f, r[12], a0);
+        a1 = fma(f, r[13], a1);
+        a2 = fma(f, r[14], a2);
+      }
+    }
+  }
+  (void)w;
+  r0[id] = a0 * inv_dv;
+  r1[id] = a1 * inv_dv;
+  r2[id] = a2 * inv_dv;
+}
+
+// M2P over sorted slots: UP = sum W vel, GP = (sum W def) * vol; optionally
+// the forward Euler push.
+__global__ void k_m2p(const int* __restrict__ perm, int nsorted, const double* __restrict__ rec, MeshDev m,
+                      const double* __restrict__ v0, const double* __restrict__ v1, const double* __restrict__ v2,
+                      const double* __restrict__ g0, const double* __restrict__ g1, const double* __restrict__ g2,
+                      double* __restrict__ up, double* __restrict__ gp, double* __restrict__ x, double* __restrict__ y,
+                      double* __restrict__ z, double* __restrict__ q0, double* __restrict__ q1, double* __restrict__ q2,
+                      const double* __restrict__ vol, int do_euler, double dt, double ux, double uy, double uz) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsorted) return;
+  const int p = perm[s];
+  const double* r = rec + (size_t)s * kRecLen;
+  double w[12];
+#pragma unroll
+  for (int a = 0; a < 12; ++a) w[a] = r[a];
+  const int c0 = (int)r[15];
+  const int cj = cell_of(y[p], m.xmin[1], m.d[1]), ck = cell_of(z[p], m.xmin[2], m.d[2]);
+  const int nw = m.ips + m.ipf + 1;
+  double u[3] = {0, 0, 0}, gl[3] = {0, 0, 0};
+  for (int c = 0; c < nw; ++c) {
+    const int kk = ck - m.ips + c;
+    for (int b = 0; b < nw; ++b) {
+      const int jj = cj - m.ips + b;
+      const double wyz = w[4 + b] * w[8 + c];
+      const size_t row = (size_t)m.n[0] * (jj + (size_t)m.n[1] * kk) + (c0 - m.ips);
+#pragma unroll 4
+      for (int a = 0; a < nw; ++a) {
+        const double f = w[a] * wyz;
+        const size_t id = row + a;
+        u[0] = fma(f, v0[id], u[0]);
+        u[1] = fma(f, v1[id], u[1]);
+        u[2] = fma(f, v2[id], u[2]);
+        gl[0] = fma(f, g0[id], gl[0]);
+        gl[1] = fma(f, g1[id], gl[1]);
+        gl[2] = fma(f, g2[id], gl[2]);
+      }
+    }
+  }
+  const double vp = vol[p];
+  const double gg0 = gl[0] * vp, gg1 = gl[1] * vp, gg2 = gl[2] * vp;
+  if (up) {
+    up[3 * (size_t)p] = u[0];
+    up[3 * (size_t)p + 1] = u[1];
+    up[3 * (size_t)p + 2] = u[2];
+    gp[3 * (size_t)p] = gg0;
+    gp[3 * (size_t)p + 1] = gg1;
+    gp[3 * (size_t)p + 2] = gg2;
+  }
+  if (do_euler) {
+    x[p] = x[p] + (u[0] + ux) * dt;
+    y[p] = y[p] + (u[1] + uy) * dt;
+    z[p] = z[p] + (u[2] + uz) * dt;
+    q0[p] = q0[p] - gg0 * dt;
+    q1[p] = q1[p] - gg1 * dt;
+    q2[p] = q2[p] - gg2 * dt;
+  }
+}
+
+// Remesh: flag nodes inside [lo, hi] (0-based, per axis) with |w| >= thr.
+__global__ void k_remesh_flags(const double* __restrict__ r0, const double* __restrict__ r1, const double* __restrict__ r2,
+                               MeshDev m, int lo0, int lo1, int lo2, int hi0, int hi1, int hi2, double thr,
+                               int* __restrict__ flag) {
+  const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
+  const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (id >= N) return;
+  const int i = (int)(id % m.n[0]);
+  const int j = (int)((id / m.n[0]) % m.n[1]);
+  const int k = (int)(id / ((size_t)m.n[0] * m.n[1]));
+  int f = 0;
+  if (i >= lo0 && i <= hi0 && j >= lo1 && j <= hi1 && k >= lo2 && k <= hi2) {
+    const double a = r0[id], b = r1[id], c = r2[id];
+    const double wmag = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c)));
+    f = (wmag < thr) ? 0 : 1;
+  }
+  flag[id] = f;
+}
+
+__global__ void k_remesh_emit(const double* __restrict__ r0, const double* __restrict__ r1, const double* __restrict__ r2,
+                              const int* __restrict__ flag, const int* __restrict__ pos, MeshDev m, double dv,
+                              int capacity, double* __restrict__ x, double* __restrict__ y, double* __restrict__ z,
+                              double* __restrict__ q0, double* __restrict__ q1, double* __restrict__ q2,
+                              double* __restrict__ vol) {
+  const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
+  const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (id >= N || !flag[id]) return;
+  const int s = pos[id];
+  if (s >= capacity) return;
+  const int i = (int)(id % m.n[0]);
+  const int j = (int)((id / m.n[0]) % m.n[1]);
+  const int k = (int)(id / ((size_t)m.n[0] * m.n[1]));
+  x[s] = m.xmin[0] + m.d[0] * (double)i;
+  y[s] = m.xmin[1] + m.d[1] * (double)j;
+  z[s] = m.xmin[2] + m.d[2] * (double)k;
+  q0[s] = r0[id] * dv;
+  q1[s] = r1[id] * dv;
+  q2[s] = r2[id] * dv;
+  vol[s] = dv;
+}
+
+__global__ void k_set_total(int* __restrict__ dst, const int* __restrict__ src) { *dst = *src; }
+
+}  // namespace
+
+void Particles::ensure(int cap) {
+  if (cap <= capacity) return;
+  x.ensure(cap); y.ensure(cap); z.ensure(cap);
+  q0.ensure(cap); q1.ensure(cap); q2.ensure(cap); vol.ensure(cap);
+  up.ensure(3 * (size_t)cap); gp.ensure(3 * (size_t)cap);
+  key.ensure(cap); perm.ensure(cap);
+  rec.ensure((size_t)kRecLen * cap);
+  capacity = cap;
+}
+
+void Binning::ensure(size_t ncell) {
+  if (ncell <= ncells) return;
+  starts.ensure(ncell + 1);
+  cursor.ensure(ncell);
+  sums.ensure(scan_block_sums_needed(ncell) + 1);
+  err.ensure(1);
+  ncells = ncell;
+}
+
+// Sort + records.  Returns the number of sorted (in-mesh) particles.
+void bin_particles(Particles& P, int np, const MeshDev& m, Binning& B, cudaStream_t s) {
+  const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
+  B.ensure(N);
+  VPMG_CUDA(cudaMemsetAsync(B.cursor.p, 0, sizeof(int) * N, s));
+  VPMG_CUDA(cudaMemsetAsync(B.err.p, 0, sizeof(int), s));
+  if (np > 0) {
+    k_keys<<<(np + 255) / 256, 256, 0, s>>>(P.x.p, P.y.p, P.z.p, np, m, P.key.p, B.cursor.p, B.err.p);
+    VPMG_LAUNCHED();
+  }
+  VPMG_CUDA(cudaMemsetAsync(B.sums.p, 0, sizeof(int) * B.sums.n, s));
+  exclusive_scan_int(B.cursor.p, B.starts.p, N, B.sums.p, s);
+  const int nt = (int)scan_block_sums_needed(N) - 1;
+  k_set_total<<<1, 1, 0, s>>>(B.starts.p + N, B.sums.p + nt);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaMemsetAsync(B.cursor.p, 0, sizeof(int) * N, s));
+  if (np > 0) {
+    k_scatter<<<(np + 255) / 256, 256, 0, s>>>(P.key.p, np, B.starts.p, B.cursor.p, P.perm.p);
+    VPMG_LAUNCHED();
+  }
+  k_cell_order<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(B.starts.p, (int)N, P.perm.p);
+  VPMG_LAUNCHED();
+  int h[2] = {0, 0};
+  VPMG_CUDA(cudaMemcpyAsync(&h[0], B.starts.p + N, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaMemcpyAsync(&h[1], B.err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  B.nsorted = h[0];
+  VPMG_CHECK(h[1] == 0, VPMG_ERR_OUTSIDE, "a particle's projection stencil leaves the mesh");
+  if (B.nsorted > 0) {
+    k_records<<<(B.nsorted + 255) / 256, 256, 0, s>>>(P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.perm.p, B.nsorted,
+                                                     m, P.rec.p);
+    VPMG_LAUNCHED();
+  }
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void deposit(const Particles& P, const MeshDev& m, const Binning& B, double* const rhs[3], cudaStream_t s) {
+  const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
+  const double dv = m.d[0] * m.d[1] * m.d[2];
+  k_deposit<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(B.starts.p, P.rec.p, m, 1.0 / dv, rhs[0], rhs[1], rhs[2]);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const vel[3], const double* const def[3],
+         bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s) {
+  if (B.nsorted <= 0) return;
+  k_m2p<<<(B.nsorted + 127) / 128, 128, 0, s>>>(P.perm.p, B.nsorted, P.rec.p, m, vel[0], vel[1], vel[2], def[0], def[1],
+                                               def[2], write_up ? P.up.p : nullptr, P.gp.p, P.x.p, P.y.p, P.z.p, P.q0.p,
+                                               P.q1.p, P.q2.p, P.vol.p, euler ? 1 : 0, dt, uinf[0], uinf[1], uinf[2]);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+int remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3], const int hi[3],
+                double thr, int capacity, cudaStream_t s) {
+  const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
+  B.ensure(N);
+  const double dv = m.d[0] * m.d[1] * m.d[2];
+  k_remesh_flags<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], m, lo[0], lo[1], lo[2], hi[0], hi[1],
+                                                              hi[2], thr, B.cursor.p);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaMemsetAsync(B.sums.p, 0, sizeof(int) * B.sums.n, s));
+  exclusive_scan_int(B.cursor.p, B.starts.p, N, B.sums.p, s);
+  const int nt = (int)scan_block_sums_needed(N) - 1;
+  int total = 0;
+  VPMG_CUDA(cudaMemcpyAsync(&total, B.sums.p + nt, sizeof(int), cudaMemcpyDeviceToHost, s));
+  k_remesh_emit<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], B.cursor.p, B.starts.p, m, dv,
+                                                             capacity, P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p,
+                                                             P.vol.p);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  VPMG_CUDA(cudaGetLastError());
+  return total;
+}
+
+}  // namespace vpmg

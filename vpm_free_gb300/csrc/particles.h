@@ -1,0 +1,39 @@
+// particles.h -- device particle storage and the particle/mesh kernels.
+#pragma once
+#include "vpmg_internal.h"
+
+namespace vpmg {
+
+constexpr int kRecLen = 16;  // doubles per sorted particle record
+
+// Mesh parameters as the kernels see them (0-based nodes).
+struct MeshDev {
+  double xmin[3], d[3];
+  int n[3];
+  int itype, ips, ipf;  // projection function and stencil extents
+};
+
+struct Particles {
+  int capacity = 0;
+  DBuf<double> x, y, z, q0, q1, q2, vol;  // SoA, QP(1:3) and QP(4)
+  DBuf<double> up, gp;                    // (3, cap) AoS like UP/GP
+  DBuf<int> key, perm;
+  DBuf<double> rec;                       // kRecLen per sorted slot
+  void ensure(int cap);
+};
+
+struct Binning {
+  size_t ncells = 0;
+  DBuf<int> starts, cursor, sums, err;
+  int nsorted = 0;
+  void ensure(size_t ncell);
+};
+
+void bin_particles(Particles& P, int np, const MeshDev& m, Binning& B, cudaStream_t s);
+void deposit(const Particles& P, const MeshDev& m, const Binning& B, double* const rhs[3], cudaStream_t s);
+void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const vel[3], const double* const def[3],
+         bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s);
+int remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3], const int hi[3],
+                double thr, int capacity, cudaStream_t s);
+
+}  // namespace vpmg

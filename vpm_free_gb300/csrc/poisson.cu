@@ -1,0 +1,505 @@
+// poisson.cu -- batched FP64 Dirichlet solver for the 7-point Laplacian.
+//
+// Replaces the MKL Poisson Library calls of source/pmsolve.f90:284-432
+// (d_Helmholtz_3D with 'DDDDDD' boundaries, q = 0, f = -RHS): the exact
+// discrete solution of  Lap_h u = RHS  on a node box with Dirichlet values.
+//
+// Method (GB300-first: FP64 is the scarce resource, ~1.2 TFLOP/s):
+//   1. x pass: fold the boundary values into the RHS of the first/last
+//      interior layers, DST-I along x (two real lines packed in one complex
+//      FFT of the odd extension, length 2N), scaled for the later inverse;
+//   2. y pass: the same DST-I along y, in place;
+//   3. z pass: per (p,q) mode the constant-coefficient tridiagonal system
+//      -u[k-1] + d_pq u[k] - u[k+1] = r[k] by a Thomas sweep whose
+//      reciprocal pivots come from a table built once per grid (no FP64
+//      divisions per step);
+//   4. inverse y and x passes (DST-I is its own inverse up to 2/N).
+// FFTs run in shared memory as mixed-radix Stockham stages (radix 2,4,8
+// and odd primes up to 31 through the symmetric direct DFT).
+#include <algorithm>
+#include <cmath>
+
+#include "vpmg_internal.h"
+
+namespace vpmg {
+
+namespace {
+
+constexpr int kPairs = 4;         // line pairs (8 real lines) per CTA
+constexpr int kThreads = 128;
+constexpr int kMaxOddRadix = 31;
+
+__constant__ double c_rcos[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
+__constant__ double c_rsin[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
+bool g_tables_ready = false;
+
+struct FFTDev {
+  int n, N, M, nst;
+  int radix[24];
+  const double2* tw;
+};
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+
+template <int R>
+struct DFT;
+
+template <>
+struct DFT<2> {
+  __device__ __forceinline__ static void run(double2 (&v)[2]) {
+    const double2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+
+__device__ __forceinline__ void dft4(double2& v0, double2& v1, double2& v2, double2& v3) {
+  const double2 t0 = cadd(v0, v2), t1 = csub(v0, v2), t2 = cadd(v1, v3), t3 = csub(v1, v3);
+  v0 = cadd(t0, t2);
+  v2 = csub(t0, t2);
+  v1 = make_double2(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
+  v3 = make_double2(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
+}
+
+template <>
+struct DFT<4> {
+  __device__ __forceinline__ static void run(double2 (&v)[4]) { dft4(v[0], v[1], v[2], v[3]); }
+};
+
+template <>
+struct DFT<8> {
+  __device__ __forceinline__ static void run(double2 (&v)[8]) {
+    double2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    double2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4(e0, e1, e2, e3);
+    dft4(o0, o1, o2, o3);
+    const double r = 0.70710678118654752440084436210484904;
+    // W8^1 o1 = ((x+y) + i(y-x))/sqrt2 ; W8^2 o2 = -i o2 ; W8^3 o3 = ((y-x) - i(x+y))/sqrt2
+    const double2 w1 = make_double2((o1.x + o1.y) * r, (o1.y - o1.x) * r);
+    const double2 w2 = make_double2(o2.y, -o2.x);
+    const double2 w3 = make_double2((o3.y - o3.x) * r, -(o3.x + o3.y) * r);
+    v[0] = cadd(e0, o0);
+    v[4] = csub(e0, o0);
+    v[1] = cadd(e1, w1);
+    v[5] = csub(e1, w1);
+    v[2] = cadd(e2, w2);
+    v[6] = csub(e2, w2);
+    v[3] = cadd(e3, w3);
+    v[7] = csub(e3, w3);
+  }
+};
+
+// Odd radix: X_k = x0 + sum_m [(v_m + v_{R-m}) cos(2 pi mk/R) - i (v_m - v_{R-m}) sin(2 pi mk/R)].
+template <int R>
+struct DFT {
+  __device__ __forceinline__ static void run(double2 (&v)[R]) {
+    constexpr int H = (R - 1) / 2;
+    double2 s[H], d[H];
+    const double2 x0 = v[0];
+    double2 sum = x0;
+#pragma unroll
+    for (int m = 1; m <= H; ++m) {
+      s[m - 1] = cadd(v[m], v[R - m]);
+      d[m - 1] = csub(v[m], v[R - m]);
+      sum = cadd(sum, s[m - 1]);
+    }
+    v[0] = sum;
+#pragma unroll
+    for (int k = 1; k <= H; ++k) {
+      double2 A = x0;
+      double2 B = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int m = 1; m <= H; ++m) {
+        const int idx = (m * k) % R;
+        const double c = c_rcos[R * (kMaxOddRadix + 1) + idx];
+        const double sn = c_rsin[R * (kMaxOddRadix + 1) + idx];
+        A.x = fma(c, s[m - 1].x, A.x);
+        A.y = fma(c, s[m - 1].y, A.y);
+        B.x = fma(sn, d[m - 1].x, B.x);
+        B.y = fma(sn, d[m - 1].y, B.y);
+      }
+      v[k] = make_double2(A.x + B.y, A.y - B.x);
+      v[R - k] = make_double2(A.x - B.y, A.y + B.x);
+    }
+  }
+};
+
+// One Stockham radix-R stage over npair transforms of length M held back
+// to back in shared memory.
+template <int R>
+__device__ __forceinline__ void stage(const double2* __restrict__ in, double2* __restrict__ out, int M, int Ns,
+                                      const double2* __restrict__ tw, int npair) {
+  const int nbf = M / R;
+  const int tws = M / (Ns * R);
+  for (int t = threadIdx.x; t < npair * nbf; t += blockDim.x) {
+    const int pr = t / nbf;
+    const int j = t - pr * nbf;
+    const double2* src = in + pr * M;
+    double2* dst = out + pr * M;
+    double2 v[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) v[m] = src[j + m * nbf];
+    const int k = j % Ns;
+    if (Ns > 1) {
+#pragma unroll
+      for (int m = 1; m < R; ++m) v[m] = cmul(v[m], __ldg(&tw[k * m * tws]));
+    }
+    DFT<R>::run(v);
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int m = 0; m < R; ++m) dst[base + m * Ns] = v[m];
+  }
+}
+
+// Runs all stages; returns the buffer holding the result.
+__device__ double2* fft_all(double2* A, double2* B, const FFTDev& p, int npair) {
+  int Ns = 1;
+  for (int s = 0; s < p.nst; ++s) {
+    const int r = p.radix[s];
+    switch (r) {
+      case 2: stage<2>(A, B, p.M, Ns, p.tw, npair); break;
+      case 3: stage<3>(A, B, p.M, Ns, p.tw, npair); break;
+      case 4: stage<4>(A, B, p.M, Ns, p.tw, npair); break;
+      case 5: stage<5>(A, B, p.M, Ns, p.tw, npair); break;
+      case 7: stage<7>(A, B, p.M, Ns, p.tw, npair); break;
+      case 8: stage<8>(A, B, p.M, Ns, p.tw, npair); break;
+      case 11: stage<11>(A, B, p.M, Ns, p.tw, npair); break;
+      case 13: stage<13>(A, B, p.M, Ns, p.tw, npair); break;
+      case 17: stage<17>(A, B, p.M, Ns, p.tw, npair); break;
+      case 19: stage<19>(A, B, p.M, Ns, p.tw, npair); break;
+      case 23: stage<23>(A, B, p.M, Ns, p.tw, npair); break;
+      case 29: stage<29>(A, B, p.M, Ns, p.tw, npair); break;
+      case 31: stage<31>(A, B, p.M, Ns, p.tw, npair); break;
+      default: break;
+    }
+    __syncthreads();
+    Ns *= r;
+    double2* t = A;
+    A = B;
+    B = t;
+  }
+  return A;
+}
+
+// Odd extension of the loaded real pairs: z[0] = z[N] = 0, z[M-j] = -z[j].
+__device__ __forceinline__ void odd_extend(double2* z, const FFTDev& p, int npair) {
+  for (int t = threadIdx.x; t < npair * p.N; t += blockDim.x) {
+    const int pr = t / p.N, j = t - pr * p.N;
+    double2* zz = z + pr * p.M;
+    if (j == 0) {
+      zz[0] = make_double2(0.0, 0.0);
+      zz[p.N] = make_double2(0.0, 0.0);
+    } else {
+      const double2 v = zz[j];
+      zz[p.M - j] = make_double2(-v.x, -v.y);
+    }
+  }
+}
+
+// ------------------------------------------------------------ passes ----
+struct Box {
+  int dims[3];  // node array dims
+  int o[3];     // node offset of interior (a,b,c) = (0,0,0)
+  int m[3];     // interior counts
+};
+
+// x pass, forward: rhs (+ folded boundary values) -> work, scaled.
+__global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict__ rhs, const double* __restrict__ sol,
+                                                        int zero_bc, double* __restrict__ work, Box b, FFTDev p,
+                                                        double ihx2, double ihy2, double ihz2, double scale) {
+  extern __shared__ double2 smem[];
+  double2* A = smem;
+  double2* B = smem + kPairs * p.M;
+  const int nlines = b.m[1] * b.m[2];
+  const int l0 = blockIdx.x * (2 * kPairs);
+  const int n = p.n;
+  const size_t sy = b.dims[0], sz = (size_t)b.dims[0] * b.dims[1];
+  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
+    const int li = t / n, a = t - li * n;
+    const int l = l0 + li;
+    double v = 0.0;
+    if (l < nlines) {
+      const int q = l % b.m[1], c = l / b.m[1];
+      const size_t node = (size_t)(b.o[0] + a) + sy * (b.o[1] + q) + sz * (b.o[2] + c);
+      v = rhs[node];
+      if (!zero_bc) {
+        if (a == 0) v -= sol[node - 1] * ihx2;
+        if (a == b.m[0] - 1) v -= sol[node + 1] * ihx2;
+        if (q == 0) v -= sol[node - sy] * ihy2;
+        if (q == b.m[1] - 1) v -= sol[node + sy] * ihy2;
+        if (c == 0) v -= sol[node - sz] * ihz2;
+        if (c == b.m[2] - 1) v -= sol[node + sz] * ihz2;
+      }
+      v *= scale;
+    }
+    double* zp = reinterpret_cast<double*>(A + (li >> 1) * p.M + (a + 1));
+    zp[li & 1] = v;
+  }
+  __syncthreads();
+  odd_extend(A, p, kPairs);
+  __syncthreads();
+  double2* R = fft_all(A, B, p, kPairs);
+  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
+    const int li = t / n, k = t - li * n;
+    const int l = l0 + li;
+    if (l >= nlines) continue;
+    const double2 W = R[(li >> 1) * p.M + (k + 1)];
+    work[(size_t)l * n + k] = (li & 1) ? 0.5 * W.x : -0.5 * W.y;
+  }
+}
+
+// y pass (forward or inverse): in place on work (m0 x m1 x m2, x fastest).
+__global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, int m0, int m1, int m2, FFTDev p) {
+  extern __shared__ double2 smem[];
+  double2* A = smem;
+  double2* B = smem + kPairs * p.M;
+  const int nlines = m0 * m2;
+  const int l0 = blockIdx.x * (2 * kPairs);
+  const int n = p.n;  // == m1
+  const size_t plane = (size_t)m0 * m1;
+  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
+    const int li = t % (2 * kPairs), e = t / (2 * kPairs);
+    const int l = l0 + li;
+    double v = 0.0;
+    if (l < nlines) {
+      const int a = l % m0, c = l / m0;
+      v = work[(size_t)a + (size_t)m0 * e + plane * c];
+    }
+    double* zp = reinterpret_cast<double*>(A + (li >> 1) * p.M + (e + 1));
+    zp[li & 1] = v;
+  }
+  __syncthreads();
+  odd_extend(A, p, kPairs);
+  __syncthreads();
+  double2* R = fft_all(A, B, p, kPairs);
+  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
+    const int li = t % (2 * kPairs), k = t / (2 * kPairs);
+    const int l = l0 + li;
+    if (l >= nlines) continue;
+    const int a = l % m0, c = l / m0;
+    const double2 W = R[(li >> 1) * p.M + (k + 1)];
+    work[(size_t)a + (size_t)m0 * k + plane * c] = (li & 1) ? 0.5 * W.x : -0.5 * W.y;
+  }
+}
+
+// x pass, inverse: work -> interior of sol.
+__global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict__ work, double* __restrict__ sol, Box b,
+                                                        FFTDev p) {
+  extern __shared__ double2 smem[];
+  double2* A = smem;
+  double2* B = smem + kPairs * p.M;
+  const int nlines = b.m[1] * b.m[2];
+  const int l0 = blockIdx.x * (2 * kPairs);
+  const int n = p.n;
+  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
+    const int li = t / n, a = t - li * n;
+    const int l = l0 + li;
+    const double v = (l < nlines) ? work[(size_t)l * n + a] : 0.0;
+    double* zp = reinterpret_cast<double*>(A + (li >> 1) * p.M + (a + 1));
+    zp[li & 1] = v;
+  }
+  __syncthreads();
+  odd_extend(A, p, kPairs);
+  __syncthreads();
+  double2* R = fft_all(A, B, p, kPairs);
+  const size_t sy = b.dims[0], sz = (size_t)b.dims[0] * b.dims[1];
+  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
+    const int li = t / n, k = t - li * n;
+    const int l = l0 + li;
+    if (l >= nlines) continue;
+    const int q = l % b.m[1], c = l / b.m[1];
+    const double2 W = R[(li >> 1) * p.M + (k + 1)];
+    sol[(size_t)(b.o[0] + k) + sy * (b.o[1] + q) + sz * (b.o[2] + c)] = (li & 1) ? 0.5 * W.x : -0.5 * W.y;
+  }
+}
+
+// z pass: Thomas sweep per (p,q) with the reciprocal pivot table.
+__global__ void k_thomas(double* __restrict__ g, const double* __restrict__ rinv, int m0, int m1, int m2) {
+  const int pq = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pq >= m0 * m1) return;
+  const size_t plane = (size_t)m0 * m1;
+  double y = g[pq];
+  double ri = rinv[pq];
+  for (int c = 1; c < m2; ++c) {
+    const size_t id = pq + plane * c;
+    y = fma(y, ri, g[id]);
+    g[id] = y;
+    ri = rinv[id];
+  }
+  double u = y * ri;
+  g[pq + plane * (m2 - 1)] = u;
+  for (int c = m2 - 2; c >= 0; --c) {
+    const size_t id = pq + plane * c;
+    u = (g[id] + u) * rinv[id];
+    g[id] = u;
+  }
+}
+
+__global__ void k_pivots(double* __restrict__ rinv, const double* __restrict__ mux, const double* __restrict__ muy,
+                         int m0, int m1, int m2, double cx, double cy) {
+  const int pq = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pq >= m0 * m1) return;
+  const int p = pq % m0, q = pq / m0;
+  const double d = 2.0 + (mux[p] * cx + muy[q] * cy);
+  const size_t plane = (size_t)m0 * m1;
+  double r = 1.0 / d;
+  rinv[pq] = r;
+  for (int c = 1; c < m2; ++c) {
+    r = 1.0 / (d - r);
+    rinv[pq + plane * c] = r;
+  }
+}
+
+__global__ void k_zero_box_faces(double* __restrict__ sol, Box b) {
+  // faces of the box [o-1, o+m] in each direction
+  const int ex = b.m[0] + 2, ey = b.m[1] + 2, ez = b.m[2] + 2;
+  const long total = 2L * ey * ez + 2L * ex * ez + 2L * ex * ey;
+  const size_t sy = b.dims[0], sz = (size_t)b.dims[0] * b.dims[1];
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    long r = t;
+    if (r < 2L * ey * ez) {
+      const int f = (int)(r / ((long)ey * ez));
+      r -= (long)f * ey * ez;
+      j = (int)(r % ey); k = (int)(r / ey); i = f ? ex - 1 : 0;
+    } else if ((r -= 2L * ey * ez) < 2L * ex * ez) {
+      const int f = (int)(r / ((long)ex * ez));
+      r -= (long)f * ex * ez;
+      i = (int)(r % ex); k = (int)(r / ex); j = f ? ey - 1 : 0;
+    } else {
+      r -= 2L * ex * ez;
+      const int f = (int)(r / ((long)ex * ey));
+      r -= (long)f * ex * ey;
+      i = (int)(r % ex); j = (int)(r / ex); k = f ? ez - 1 : 0;
+    }
+    sol[(size_t)(b.o[0] - 1 + i) + sy * (b.o[1] - 1 + j) + sz * (b.o[2] - 1 + k)] = 0.0;
+  }
+}
+
+FFTDev dev_plan(const FFTPlan& p) {
+  FFTDev d;
+  d.n = p.n; d.N = p.N; d.M = p.M; d.nst = p.nst;
+  for (int i = 0; i < 24; ++i) d.radix[i] = p.radix[i];
+  d.tw = p.tw.p;
+  return d;
+}
+
+void ensure_tables() {
+  if (g_tables_ready) return;
+  static double hc[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)], hs[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
+  for (int R = 1; R <= kMaxOddRadix; ++R)
+    for (int i = 0; i < R; ++i) {
+      hc[R * (kMaxOddRadix + 1) + i] = std::cos(2.0 * kPI * i / R);
+      hs[R * (kMaxOddRadix + 1) + i] = std::sin(2.0 * kPI * i / R);
+    }
+  VPMG_CUDA(cudaMemcpyToSymbol(c_rcos, hc, sizeof(hc)));
+  VPMG_CUDA(cudaMemcpyToSymbol(c_rsin, hs, sizeof(hs)));
+  g_tables_ready = true;
+}
+
+size_t smem_bytes(const FFTPlan& p) { return (size_t)2 * kPairs * p.M * sizeof(double2); }
+
+}  // namespace
+
+void make_fft_plan(FFTPlan& p, int n) {
+  ensure_tables();
+  p.n = n;
+  p.N = n + 1;
+  p.M = 2 * p.N;
+  // factor M: odd primes first (largest first), then 8s, a 4, a 2
+  int m = p.M, twos = 0;
+  std::vector<int> odd;
+  while (m % 2 == 0) { m /= 2; ++twos; }
+  for (int f = 3; m > 1; f += 2)
+    while (m % f == 0) { odd.push_back(f); m /= f; }
+  std::sort(odd.begin(), odd.end(), [](int a, int b) { return a > b; });
+  p.nst = 0;
+  for (int f : odd) {
+    VPMG_CHECK(f <= kMaxOddRadix, VPMG_ERR_UNSUPPORTED, "mesh size has a prime factor > 31 in 2*(cells)");
+    p.radix[p.nst++] = f;
+  }
+  while (twos >= 3) { p.radix[p.nst++] = 8; twos -= 3; }
+  if (twos == 2) p.radix[p.nst++] = 4;
+  if (twos == 1) p.radix[p.nst++] = 2;
+  VPMG_CHECK(p.nst <= 24, VPMG_ERR_UNSUPPORTED, "too many FFT stages");
+  std::vector<double2> h(p.M);
+  for (int t = 0; t < p.M; ++t) {
+    const double a = -2.0 * kPI * (double)t / (double)p.M;
+    h[t] = make_double2(std::cos(a), std::sin(a));
+  }
+  p.tw.ensure(p.M);
+  VPMG_CUDA(cudaMemcpy(p.tw.p, h.data(), sizeof(double2) * p.M, cudaMemcpyHostToDevice));
+}
+
+void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], const double h[3], cudaStream_t s) {
+  bool same = P.ready;
+  for (int d = 0; d < 3; ++d) same = same && P.dims[d] == dims[d] && P.h[d] == h[d];
+  for (int d = 0; d < 6; ++d) same = same && P.box[d] == box[d];
+  if (same) return;
+  for (int d = 0; d < 3; ++d) { P.dims[d] = dims[d]; P.h[d] = h[d]; }
+  for (int d = 0; d < 6; ++d) P.box[d] = box[d];
+  for (int d = 0; d < 3; ++d) {
+    P.m[d] = box[d + 3] - box[d] - 1;
+    VPMG_CHECK(P.m[d] >= 1, VPMG_ERR_ARG, "Dirichlet box without interior");
+  }
+  make_fft_plan(P.fx, P.m[0]);
+  make_fft_plan(P.fy, P.m[1]);
+  const size_t smax = std::max(smem_bytes(P.fx), smem_bytes(P.fy));
+  VPMG_CHECK(smax <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "mesh too large for the shared-memory DST");
+  // The attribute is per kernel (not per plan): only ever raise it.
+  static int s_smem_set = 0;
+  if ((int)smax > s_smem_set) {
+    VPMG_CUDA(cudaFuncSetAttribute(k_dst_x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+    VPMG_CUDA(cudaFuncSetAttribute(k_dst_x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+    VPMG_CUDA(cudaFuncSetAttribute(k_dst_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+    s_smem_set = (int)smax;
+  }
+  // eigenvalues mu_p = 4 sin^2(pi p / 2N), pivots for d = 2 + hz^2 (mu_p/hx^2 + mu_q/hy^2)
+  std::vector<double> mux(P.m[0]), muy(P.m[1]);
+  for (int p = 0; p < P.m[0]; ++p) { const double sn = std::sin(kPI * (p + 1) / (2.0 * (P.m[0] + 1))); mux[p] = 4.0 * sn * sn; }
+  for (int q = 0; q < P.m[1]; ++q) { const double sn = std::sin(kPI * (q + 1) / (2.0 * (P.m[1] + 1))); muy[q] = 4.0 * sn * sn; }
+  DBuf<double> dmx, dmy;
+  dmx.ensure(P.m[0]);
+  dmy.ensure(P.m[1]);
+  VPMG_CUDA(cudaMemcpy(dmx.p, mux.data(), sizeof(double) * P.m[0], cudaMemcpyHostToDevice));
+  VPMG_CUDA(cudaMemcpy(dmy.p, muy.data(), sizeof(double) * P.m[1], cudaMemcpyHostToDevice));
+  P.rinv.ensure((size_t)P.m[0] * P.m[1] * P.m[2]);
+  const double hz2 = h[2] * h[2];
+  const int nl = P.m[0] * P.m[1];
+  k_pivots<<<(nl + 255) / 256, 256, 0, s>>>(P.rinv.p, dmx.p, dmy.p, P.m[0], P.m[1], P.m[2], hz2 / (h[0] * h[0]),
+                                            hz2 / (h[1] * h[1]));
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  P.ready = true;
+}
+
+void dirichlet_solve(DirichletPlan& P, const double* rhs, double* sol, bool zero_bc, double* work, cudaStream_t s) {
+  Box b;
+  for (int d = 0; d < 3; ++d) { b.dims[d] = P.dims[d]; b.o[d] = P.box[d] + 1; b.m[d] = P.m[d]; }
+  const FFTDev px = dev_plan(P.fx), py = dev_plan(P.fy);
+  const double hx2 = P.h[0] * P.h[0], hy2 = P.h[1] * P.h[1], hz2 = P.h[2] * P.h[2];
+  // Thomas RHS r = -hz^2 * ghat, with the inverse DST normalisation 4/(Nx Ny).
+  const double scale = -hz2 * 4.0 / ((double)(P.m[0] + 1) * (double)(P.m[1] + 1));
+  const int lx = P.m[1] * P.m[2], ly = P.m[0] * P.m[2];
+  const int gx = (lx + 2 * kPairs - 1) / (2 * kPairs), gy = (ly + 2 * kPairs - 1) / (2 * kPairs);
+  k_dst_x_fwd<<<gx, kThreads, smem_bytes(P.fx), s>>>(rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2,
+                                                     1.0 / hz2, scale);
+  k_dst_y<<<gy, kThreads, smem_bytes(P.fy), s>>>(work, P.m[0], P.m[1], P.m[2], py);
+  const int nl = P.m[0] * P.m[1];
+  k_thomas<<<(nl + 127) / 128, 128, 0, s>>>(work, P.rinv.p, P.m[0], P.m[1], P.m[2]);
+  k_dst_y<<<gy, kThreads, smem_bytes(P.fy), s>>>(work, P.m[0], P.m[1], P.m[2], py);
+  k_dst_x_inv<<<gx, kThreads, smem_bytes(P.fx), s>>>(work, sol, b, px);
+  count_launch(5);
+  if (zero_bc) {
+    k_zero_box_faces<<<256, 256, 0, s>>>(sol, b);
+    VPMG_LAUNCHED();
+  }
+  VPMG_CUDA(cudaGetLastError());
+}
+
+}  // namespace vpmg

@@ -1,0 +1,141 @@
+// vpmg_internal.h -- shared declarations of the sm_103a particle-mesh library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/vpmg.h"
+
+namespace vpmg {
+
+constexpr double kPI = 3.14159265358979323846264338327950288;
+
+// ------------------------------------------------------------ errors ----
+struct Error {
+  int status;
+  std::string msg;
+};
+#define VPMG_CUDA(x)                                                                      \
+  do {                                                                                    \
+    cudaError_t e_ = (x);                                                                 \
+    if (e_ != cudaSuccess)                                                                \
+      throw ::vpmg::Error{VPMG_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)}; \
+  } while (0)
+#define VPMG_CHECK(cond, code, text)                                  \
+  do {                                                                \
+    if (!(cond)) throw ::vpmg::Error{(code), std::string(text)};      \
+  } while (0)
+
+// Kernel launch counter shared by every launch site (instrumentation).
+extern thread_local long long* g_launch_counter;
+inline void count_launch(int n = 1) {
+  if (g_launch_counter) *g_launch_counter += n;
+}
+#define VPMG_LAUNCHED() ::vpmg::count_launch()
+
+// ---------------------------------------------------- device buffers ----
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void ensure(size_t count) {
+    if (count <= n && p) return;
+    release();
+    if (count == 0) return;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      throw Error{VPMG_ERR_NOMEM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed"};
+    }
+    n = count;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// ------------------------------------------------------------- grids ----
+// A node grid: origin, spacing and node counts (1-based node i sits at
+// xmin + (i-1)*d, as everywhere in the reference).
+struct Grid {
+  double xmin[3], d[3];
+  int n[3];
+  size_t count() const { return (size_t)n[0] * n[1] * n[2]; }
+};
+
+// --------------------------------------------------- Dirichlet solver ----
+// FFT plan for the odd-extended DST-I of n = N-1 points: complex length M = 2N.
+struct FFTPlan {
+  int n = 0, N = 0, M = 0;
+  int nst = 0;
+  int radix[24];
+  DBuf<double2> tw;  // e^{-2 pi i t / M}, t = 0..M-1
+};
+void make_fft_plan(FFTPlan& p, int n);
+
+// A Dirichlet box inside a node array of dims dims[3]: nodes box[0..2] to
+// box[3..5] (0-based, inclusive).  Interior m[d] = box[d+3]-box[d]-1.
+struct DirichletPlan {
+  int dims[3] = {0, 0, 0};
+  int box[6] = {0, 0, 0, 0, 0, 0};
+  int m[3] = {0, 0, 0};
+  double h[3] = {0, 0, 0};
+  FFTPlan fx, fy;
+  DBuf<double> rinv;  // reciprocal Thomas pivots, [k][q][p]
+  bool ready = false;
+};
+void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], const double h[3], cudaStream_t s);
+// Interior of sol <- solution of Lap_h u = rhs with the box faces of sol as
+// boundary values (zero_bc = false) or zero (true; then the box faces of
+// sol are zeroed).  work: >= m0*m1*m2 doubles.
+void dirichlet_solve(DirichletPlan& P, const double* rhs, double* sol, bool zero_bc, double* work, cudaStream_t s);
+
+// ------------------------------------------------- boundary operator ----
+struct TreeGeom;  // host-built quadtree of one grid (tree_host.cpp)
+struct BoundaryOp {
+  // panels (level 0) and aggregated levels, device copies
+  int nbound = 0, levmax = 0, ncell_total = 0, ntarget = 0;
+  std::vector<int> lev_off;    // flat offset of each level's cells
+  std::vector<int> nbound_lev; // cumulative cells per level (all faces)
+  DBuf<double> cx, cy, cz, cds, cthr;   // per flat cell: centre, area, 10*sqrt(ds)
+  DBuf<int> child;                      // per flat cell: 4 flat child ids (-1 unused)
+  DBuf<int> flags;                      // per flat cell: ilev_t(.,.,6)
+  DBuf<int> agg_leaf0;                  // per flat cell: first leaf (flat) or -1 (dummy)
+  DBuf<int> agg_rowlen;                 // per flat cell: fast-axis leaf count of its face
+  DBuf<int> agg_istep;
+  DBuf<double> csrc;                    // 3 * ncell_total aggregated sources
+  // panels: face geometry for the normal derivative
+  DBuf<int> pan_face, pan_i, pan_j, pan_k;  // lower-corner node (0-based) of each panel
+  // targets
+  DBuf<int> tgt_node;                   // linear node index of each boundary node
+  DBuf<double> tx, ty, tz;
+  // precomputed operator (CSR over targets)
+  bool precomputed = false;
+  long long nnz = 0;
+  DBuf<long long> rowptr;
+  DBuf<int> col;
+  DBuf<double> w;
+  long long bytes() const;
+};
+void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s);
+// Per component: normal-derivative panels from the zero-BC solution sol0,
+// aggregate, then add the boundary values into the faces of sol.
+void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp, cudaStream_t s);
+void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStream_t s);
+
+// ---------------------------------------------------- small kernels ----
+void fill_zero(double* p, size_t n, cudaStream_t s);
+void exclusive_scan_int(const int* in, int* out, size_t n, int* block_sums, cudaStream_t s);
+size_t scan_block_sums_needed(size_t n);
+
+}  // namespace vpmg
