@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Particle-steps/s of vpm_free's particle-mesh time step, FP64, on GB300.
+
+Workload: two coaxial leapfrogging vortex rings (R = 1 and 0.7, 0.5 apart,
+sigma = 0.08, circulation 1, seeded jittered lattice) on a 256^3 mesh over
+[-1.5,1.5]^2 x [-1,2.5], M4' projection, infinite-domain quadtree
+boundary values, one YAPS block (ncoarse = 8, 3 tree levels), remesh every
+step, dt = 0.005.  One step = field step (vpm WhatToDo = 2) + forward Euler
++ remesh_particles_3d(1), as source/test.f90:83-150.  Unit of work: a
+particle-step = particles at the start of a step x 1 step.
+
+  value : device-resident steps timed with CUDA events on the library's
+          stream (vpmg_run), inputs resident in HBM.
+  e2e   : the same loop through the reference-facing C-ABI calls with host
+          arrays (vpm(...,2,...), host Euler, vpm(...,0,...),
+          remesh_particles_3d(1)), host<->device copies inside, host clock.
+  --impl reference : the oracle (C++ restatement of the reference's CPU
+          path; the Fortran/MPI/MKL original cannot be built on this
+          hardware) on all host cores.
+
+Multi-GPU: the path runs one YAPS block per GPU; N GPUs run N independent
+replicas (torchrun, one process per GPU); value = total particle-steps /
+max time over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s at 256^3 FP64"
+UNIT = "particle-steps/s"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max/sum reductions across ranks (torch.distributed when N > 1)."""
+
+    def __init__(self, ws, rank, local, backend):
+        self.ws, self.rank = ws, rank
+        self.td = None
+        if ws > 1:
+            import torch
+            import torch.distributed as td
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            td.init_process_group(backend=backend)
+            self.td, self.torch = td, torch
+            self.dev = torch.device("cuda", local) if backend == "nccl" else torch.device("cpu")
+
+    def barrier(self):
+        if self.td:
+            self.td.barrier()
+
+    def reduce(self, v, op):
+        if not self.td:
+            return v
+        t = self.torch.tensor([float(v)], dtype=self.torch.float64, device=self.dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX if op == "max" else self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.td:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.proc:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    mx.append(float(p[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, p[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def _workload():
+    from vpm_free_gb300 import workloads as W
+    xp, qp, w = W.leapfrog256()
+    return xp, qp, w
+
+
+def _measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _traffic_table():
+    """Per-launch DRAM bytes of the profiled kernels (summaries of ncu captures)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def cpu_step_sample(xp, qp, w, steps, threads):
+    """The oracle's step (field step + Euler + remesh) on `steps` steps of the
+    workload; returns (particle-steps/s, seconds, particle-steps)."""
+    from oracle import oracle as O
+    O.build()
+    cfg = O.make_config(dpm=w["dpm"], box=w["box"], ompthreads=threads)
+    s = O.define_sizes(cfg, xp)
+    xr, qr = O.remesh(cfg, s, xp, qp, nthreads=threads)
+    ps = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ps += xr.shape[0]
+        up, gp = O.step_fields(cfg, s, xr, qr, nthreads=threads)
+        O.euler(xr, qr, up, gp, w["dt"])
+        xr, qr = O.remesh(cfg, s, xr, qr, nthreads=threads)
+    t = time.perf_counter() - t0
+    return ps / t, t, ps
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    xp, qp, w = _workload()
+    warm = min(args.warmup, 1)
+    steps = max(1, min(args.steps, 3))
+    if warm:
+        cpu_step_sample(xp, qp, w, warm, threads)
+    v, t, ps = cpu_step_sample(xp, qp, w, steps, threads)
+    sample = (f"{steps} full steps (field step + Euler + remesh) of the 256^3 leapfrog workload after {warm} warm-up "
+              f"step(s); oracle = C++ restatement of the reference's CPU path (Fortran/MPI/MKL original not buildable)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "warmup": warm, "ms_per_step": 1e3 * t / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded leapfrogging rings)",
+        "config": {"workload": "leapfrog256", "mesh": [256, 256, 256], "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, dist):
+    import vpm_free_gb300 as V
+    from vpm_free_gb300 import build as B
+    B.build()
+    ws, rank, local = _dist()
+    xp, qp, w = _workload()
+    cfg = V.VPMConfig.make(dpm=w["dpm"], box=w["box"])
+    h = V.VPM(cfg, device=local)
+    h.define_sizes(xp)
+    xr, qr = h.remesh_particles_3d(1, xp, qp)
+    h.set_particles(xr, qr)
+    dt = w["dt"]
+    # warm-up (untimed)
+    if args.warmup:
+        h.run(args.warmup, dt)
+    dist.barrier()
+    clocks = Clocks(local)
+    if rank == 0:
+        clocks.start()
+    l0 = h.kernel_launches()
+    ms, ps = h.run(args.steps, dt)
+    launches = h.kernel_launches() - l0
+    clk = clocks.stop() if rank == 0 else {}
+    dist.barrier()
+    t_max = dist.reduce(ms, "max")
+    ps_all = dist.reduce(ps, "sum")
+    value = ps_all / (t_max * 1e-3)
+    # ---- per-kernel roofline figures (replays on the resident state) -------
+    fp64 = h.fp64_peak()
+    peaks = _measured_peaks()
+    kernels = []
+    for which, name, per_step in ((0, "k_apply_csr (boundary operator, fine block)", 1),
+                                  (1, "fine-block Dirichlet solve (k_dst_x_fwd, k_dst_y x2, k_thomas, k_dst_x_inv)", 6),
+                                  (2, "k_deposit (M4' gather deposition)", 2)):
+        kms, fl, by = h.bench_kernel(which, reps=3)
+        kernels.append({"kernel": name, "ms_per_launch": kms, "launches_per_step": per_step,
+                        "share_ms_per_step": kms * per_step, "flops": fl, "bytes": by})
+    dom = max(kernels, key=lambda k: k["share_ms_per_step"])
+    traffic = _traffic_table()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    roofs = []
+    for k in kernels:
+        tf = k["flops"] / (k["ms_per_launch"] * 1e-3) / 1e12
+        gbs = k["bytes"] / (k["ms_per_launch"] * 1e-3) / 1e9
+        if k["kernel"].startswith("k_deposit"):
+            r = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm}
+        else:
+            r = {"bound": "fp64", "achieved": tf, "peak": fp64, "unit": "TFLOP/s", "frac": tf / fp64}
+        r["kernel"] = k["kernel"]
+        r["ms_per_launch"] = k["ms_per_launch"]
+        r["traffic"] = traffic.get(k["kernel"].split(" ")[0])
+        roofs.append(r)
+    roof = dict(roofs[kernels.index(dom)])
+    roof["peak_source"] = ("FP64: DFMA-loop TFLOP/s measured in this run (no FP64 entry in MEASURED_PEAKS.json); "
+                           "HBM: MEASURED_PEAKS.json hbm_gbs")
+    # ---- end to end through the reference-facing calls, host arrays -------
+    ke = max(1, min(args.steps, args.e2e_steps))
+    he = V.VPM(cfg, device=local)
+    he.vpm(xp, qp, None, None, xp.shape[0], WhatToDo=0, NTIME=0)
+    XP, QP = he.remesh_particles_3d(1, xp, qp)
+    for _ in range(min(args.warmup, 1)):
+        UP = np.zeros((XP.shape[0], 3)); GP = np.zeros((XP.shape[0], 3))
+        he.vpm(XP, QP, UP, GP, XP.shape[0], WhatToDo=2, NTIME=1)
+    dist.barrier()
+    h2d = d2h = eps = 0
+    t0 = time.perf_counter()
+    for it in range(ke):
+        n = XP.shape[0]
+        eps += n
+        UP = np.zeros((n, 3))
+        GP = np.zeros((n, 3))
+        he.vpm(XP, QP, UP, GP, n, WhatToDo=2, NTIME=it + 1)
+        XP += UP * dt                      # test.f90:104-117, UINF = 0
+        QP[:, :3] -= GP * dt
+        he.vpm(XP, QP, None, None, n, WhatToDo=0, NTIME=it + 1)
+        XP, QP = he.remesh_particles_3d(1, XP, QP)
+        h2d += n * 7 * 8 * 2
+        d2h += n * 6 * 8 + XP.shape[0] * 7 * 8
+    te = time.perf_counter() - t0
+    te_max = dist.reduce(te, "max")
+    e2e = {"value": dist.reduce(eps, "sum") / te_max, "unit": UNIT, "h2d_bytes_per_step": h2d // ke,
+           "d2h_bytes_per_step": d2h // ke, "steps": ke,
+           "timing": "host clock around synchronous vpm()/remesh_particles_3d() C-ABI calls"}
+    # ---- CPU baseline (rank 0, N = 1, bounded sample) -----------------------
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, t, _ = cpu_step_sample(xp, qp, w, 1, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"1 full step (field step + Euler + remesh) of this workload, {t:.1f} s on {threads} threads"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded leapfrogging rings)",
+        "config": {"workload": "leapfrog256 (two coaxial rings, 256^3 mesh, M4', tree levels 3, ncoarse 8, remesh "
+                               "every step, dt 0.005)",
+                   "mesh": [256, 256, 256], "block": list(h.sizes().nnbl),
+                   "particles_start": int(xr.shape[0]), "particles_end": h.num_particles(),
+                   "l2": "inputs larger than L2 (each field component 135 MB, boundary operator 53 GB)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "clocks": clk if rank == 0 else None,
+        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "roofline_kernels": roofs,
+        "tree": h.tree_stats(), "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    h.close()
+    he.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    ws, rank, local = _dist()
+    if args.impl == "reference":
+        # rank 0 alone times the host-CPU path; other ranks exit without work
+        dist = Dist(1, rank, local, "gloo")
+    else:
+        dist = Dist(ws, rank, local, "nccl")
+    try:
+        rc = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+    finally:
+        dist.close()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -149,6 +149,23 @@ int vpmg_phase_times(const vpmg_handle* h, double ms[9]);
 int vpmg_tree_stats(const vpmg_handle* h, long long* interactions, long long* bytes, int* precomputed);
 /* Turns per-phase event timing on/off (default off). */
 int vpmg_set_profiling(vpmg_handle* h, int on);
+/* Runs nsteps device-resident steps (as vpmg_step) between two CUDA events
+ * on the handle's stream; *ms = elapsed device time, *particle_steps = sum
+ * of the particle counts at the start of each step.                      */
+int vpmg_run(vpmg_handle* h, int nsteps, double dt, const double uinf[3], int remesh, double* ms,
+             long long* particle_steps);
+/* Replays one kernel of the last step `reps` times between CUDA events on
+ * the handle's stream (instrumentation for roofline figures).
+ *   which = 0: boundary operator apply on the fine block (k_apply_csr or
+ *              the tree walk), 1: one fine-block Dirichlet solve (5 kernels),
+ *   2: deposition gather (k_deposit).
+ * Outputs: mean device ms per replay, algorithmic FP64 flops and DRAM
+ * bytes per replay (figures of the algorithm, not counters).  The replay
+ * writes only scratch buffers.                                          */
+int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* flops, double* bytes);
+/* FP64 FMA throughput of this GPU (TFLOP/s, FMA = 2 flops) from a
+ * register-resident DFMA loop: the roofline peak of the FP64-bound kernels. */
+int vpmg_fp64_peak(vpmg_handle* h, double* tflops);
 /* Memory limit (bytes) for the precomputed boundary operator; 0 = never
  * precompute (walk the tree every step).  Default: 100 GiB.              */
 int vpmg_set_operator_budget(vpmg_handle* h, long long bytes);

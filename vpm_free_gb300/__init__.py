@@ -35,7 +35,7 @@ EXPORTS = [
     "vpmg_remesh_particles_3d", "vpmg_pmesh", "vpmg_project_particles_3d", "vpmg_define_sizes", "vpmg_get_sizes",
     "vpmg_set_particles", "vpmg_get_particles", "vpmg_get_particle_velocity", "vpmg_step", "vpmg_remesh_device",
     "vpmg_num_particles", "vpmg_get_field", "vpmg_kernel_launches", "vpmg_phase_times", "vpmg_tree_stats",
-    "vpmg_set_profiling", "vpmg_set_operator_budget",
+    "vpmg_set_profiling", "vpmg_set_operator_budget", "vpmg_run", "vpmg_bench_kernel", "vpmg_fp64_peak",
 ]
 
 
@@ -124,6 +124,9 @@ def load_library():
     L.vpmg_tree_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]
     L.vpmg_set_profiling.argtypes = [C.c_void_p, C.c_int]
     L.vpmg_set_operator_budget.argtypes = [C.c_void_p, C.c_longlong]
+    L.vpmg_run.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, C.c_int, _dp, C.POINTER(C.c_longlong)]
+    L.vpmg_bench_kernel.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp]
+    L.vpmg_fp64_peak.argtypes = [C.c_void_p, _dp]
     _LIB = L
     return L
 
@@ -268,6 +271,27 @@ class VPM:
     def step(self, dt, uinf=(0.0, 0.0, 0.0), remesh=True):
         u = np.asarray(uinf, dtype=np.float64)
         self._chk(self._L.vpmg_step(self._h, float(dt), _p(u), 1 if remesh else 0))
+
+    def run(self, nsteps, dt, uinf=(0.0, 0.0, 0.0), remesh=True):
+        """nsteps device-resident steps timed with CUDA events on the handle's
+        stream.  Returns (device ms, sum of particle counts)."""
+        u = np.asarray(uinf, dtype=np.float64)
+        ms = C.c_double(0.0)
+        ps = C.c_longlong(0)
+        self._chk(self._L.vpmg_run(self._h, int(nsteps), float(dt), _p(u), 1 if remesh else 0, C.byref(ms),
+                                   C.byref(ps)))
+        return ms.value, ps.value
+
+    def bench_kernel(self, which, reps=5):
+        """(ms per replay, algorithmic flops, algorithmic bytes) of one kernel."""
+        ms, fl, by = C.c_double(0), C.c_double(0), C.c_double(0)
+        self._chk(self._L.vpmg_bench_kernel(self._h, int(which), int(reps), C.byref(ms), C.byref(fl), C.byref(by)))
+        return ms.value, fl.value, by.value
+
+    def fp64_peak(self):
+        t = C.c_double(0)
+        self._chk(self._L.vpmg_fp64_peak(self._h, C.byref(t)))
+        return t.value
 
     def remesh(self):
         self._chk(self._L.vpmg_remesh_device(self._h))

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <sstream>
 #include <string>
 
@@ -43,6 +44,7 @@ struct vpmg_handle {
   Binning bins;
   int np = 0;
   DBuf<double> stage;  // AoS staging for host copies
+  DBuf<double> bench_scratch;  // replay outputs of vpmg_bench_kernel
   // timing
   bool profile = false;
   cudaEvent_t ev[10] = {};
@@ -552,18 +554,116 @@ int vpmg_num_particles(const vpmg_handle* h, int* nvr) {
   return VPMG_OK;
 }
 
+namespace {
+void one_step(vpmg_handle* h, double dt, const double uinf[3], int do_remesh) {
+  VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
+  const double u0[3] = {uinf ? uinf[0] : 0.0, uinf ? uinf[1] : 0.0, uinf ? uinf[2] : 0.0};
+  ev_mark(h, 0);
+  bin_particles(h->parts, h->np, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
+  field_step(h);
+  m2p_step(h, true, true, dt, u0);
+  if (do_remesh) remesh(h);
+  else ev_mark(h, 9);
+}
+}  // namespace
+
 int vpmg_step(vpmg_handle* h, double dt, const double uinf[3], int do_remesh) {
   return guarded(h, [&] {
-    VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
-    const double u0[3] = {uinf ? uinf[0] : 0.0, uinf ? uinf[1] : 0.0, uinf ? uinf[2] : 0.0};
-    ev_mark(h, 0);
-    bin_particles(h->parts, h->np, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
-    field_step(h);
-    m2p_step(h, true, true, dt, u0);
-    if (do_remesh) remesh(h);
-    else ev_mark(h, 9);
+    one_step(h, dt, uinf, do_remesh);
     VPMG_CUDA(cudaStreamSynchronize(h->stream));
     finish_phase_times(h);
+  });
+}
+
+int vpmg_run(vpmg_handle* h, int nsteps, double dt, const double uinf[3], int do_remesh, double* ms,
+             long long* particle_steps) {
+  return guarded(h, [&] {
+    VPMG_CHECK(nsteps >= 0, VPMG_ERR_ARG, "nsteps < 0");
+    cudaEvent_t a, b;
+    VPMG_CUDA(cudaEventCreate(&a));
+    VPMG_CUDA(cudaEventCreate(&b));
+    const bool prof = h->profile;
+    h->profile = false;
+    long long ps = 0;
+    try {
+      VPMG_CUDA(cudaStreamSynchronize(h->stream));
+      VPMG_CUDA(cudaEventRecord(a, h->stream));
+      for (int k = 0; k < nsteps; ++k) {
+        ps += h->np;
+        one_step(h, dt, uinf, do_remesh);
+      }
+      VPMG_CUDA(cudaEventRecord(b, h->stream));
+      VPMG_CUDA(cudaEventSynchronize(b));
+    } catch (...) {
+      h->profile = prof;
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      throw;
+    }
+    h->profile = prof;
+    float t = 0.f;
+    VPMG_CUDA(cudaEventElapsedTime(&t, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (ms) *ms = t;
+    if (particle_steps) *particle_steps = ps;
+  });
+}
+
+int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* flops, double* bytes) {
+  return guarded(h, [&] {
+    VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
+    VPMG_CHECK(reps >= 1, VPMG_ERR_ARG, "reps < 1");
+    const size_t N = h->gglob.count(), NB = h->gbl.count();
+    cudaStream_t st = h->stream;
+    double fl = 0, by = 0;
+    std::function<void()> f;
+    if (which == 0) {
+      h->bench_scratch.ensure(3 * NB);
+      double* o[3] = {h->bench_scratch.p, h->bench_scratch.p + NB, h->bench_scratch.p + 2 * NB};
+      f = [h, o, st] { boundary_apply(h->bo_bl, h->gbl, o, st); };
+      const double nnz = (double)h->bo_bl.nnz;
+      fl = 2.0 * 3.0 * nnz;  // three FMAs per interaction
+      by = h->bo_bl.precomputed ? nnz * (sizeof(int) + sizeof(double)) : 0.0;
+    } else if (which == 1) {
+      h->bench_scratch.ensure(NB);
+      double* o = h->bench_scratch.p;
+      f = [h, o, st] { dirichlet_solve(h->dp_bl, h->rhs_bl.p, o, true, h->work.p, st); };
+      const DirichletPlan& P = h->dp_bl;
+      const double nint = (double)P.m[0] * P.m[1] * P.m[2];
+      fl = nint * (5.0 * std::log2(2.0 * (P.m[0] + 1)) + 5.0 * std::log2(2.0 * (P.m[1] + 1)) + 9.0);
+      by = 16.0 * (double)NB;
+    } else if (which == 2) {
+      h->bench_scratch.ensure(3 * N);
+      double* o[3] = {h->bench_scratch.p, h->bench_scratch.p + N, h->bench_scratch.p + 2 * N};
+      const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
+      // the last step ended with a remesh, which reuses the binning buffers
+      // for its compaction: bin the current particles on the global mesh again
+      bin_particles(h->parts, h->np, mg, h->bins, st);
+      f = [h, o, mg, st] { deposit(h->parts, mg, h->bins, o, st); };
+      const double P = (double)h->bins.nsorted;
+      const int w = mg.ips + mg.ipf + 1;
+      fl = P * w * w * w * 8.0;
+      by = 56.0 * P + 24.0 * (double)N;
+    } else {
+      throw Error{VPMG_ERR_ARG, "unknown kernel id"};
+    }
+    cudaEvent_t a, b;
+    VPMG_CUDA(cudaEventCreate(&a));
+    VPMG_CUDA(cudaEventCreate(&b));
+    f();  // warm
+    VPMG_CUDA(cudaStreamSynchronize(st));
+    VPMG_CUDA(cudaEventRecord(a, st));
+    for (int r = 0; r < reps; ++r) f();
+    VPMG_CUDA(cudaEventRecord(b, st));
+    VPMG_CUDA(cudaEventSynchronize(b));
+    float t = 0.f;
+    VPMG_CUDA(cudaEventElapsedTime(&t, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (ms) *ms = t / reps;
+    if (flops) *flops = fl;
+    if (bytes) *bytes = by;
   });
 }
 
@@ -719,6 +819,13 @@ int vpmg_set_profiling(vpmg_handle* h, int on) {
   h->profile = on != 0;
   h->keep_intermediates = on >= 2;
   return VPMG_OK;
+}
+
+int vpmg_fp64_peak(vpmg_handle* h, double* tflops) {
+  return guarded(h, [&] {
+    const double t = measure_fp64_peak(h->stream);
+    if (tflops) *tflops = t;
+  });
 }
 
 int vpmg_set_operator_budget(vpmg_handle* h, long long bytes) {

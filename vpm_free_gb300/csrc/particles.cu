@@ -142,6 +142,7 @@ __global__ void k_deposit(const int* __restrict__ starts, const double* __restri
       for (int t = s; t < e; ++t) {
         const double* r = rec + (size_t)t * kRecLen;
         const int ix = i - (int)r[15] + m.ips;
+        if ((unsigned)ix > (unsigned)w) continue;  // only for a binning that does not match rec
         const double f = (r[ix] * r[4 + iy]) * r[8 + iz];
         a0 = fma(f, r[12], a0);
         a1 = fma(f, r[13], a1);
@@ -149,7 +150,6 @@ __global__ void k_deposit(const int* __restrict__ starts, const double* __restri
       }
     }
   }
-  (void)w;
   r0[id] = a0 * inv_dv;
   r1[id] = a1 * inv_dv;
   r2[id] = a2 * inv_dv;

@@ -84,7 +84,42 @@ __global__ void __launch_bounds__(kScanThreads) k_tile_scan(const int* __restric
     run += v[i];
   }
 }
+
+// Dependent-chain DFMA loop: 8 independent chains per thread.
+__global__ void k_dfma_peak(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+         x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
 }  // namespace
+
+double measure_fp64_peak(cudaStream_t s) {
+  int dev = 0, sms = 0;
+  VPMG_CUDA(cudaGetDevice(&dev));
+  VPMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 8, threads = 256, iters = 4000;
+  DBuf<double> o;
+  o.ensure((size_t)blocks * threads);
+  k_dfma_peak<<<blocks, threads, 0, s>>>(o.p, 100, 0.999, 1e-3);
+  VPMG_LAUNCHED();
+  cudaEvent_t a, b;
+  VPMG_CUDA(cudaEventCreate(&a));
+  VPMG_CUDA(cudaEventCreate(&b));
+  VPMG_CUDA(cudaEventRecord(a, s));
+  k_dfma_peak<<<blocks, threads, 0, s>>>(o.p, iters, 0.999, 1e-3);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaEventRecord(b, s));
+  VPMG_CUDA(cudaEventSynchronize(b));
+  float ms = 0.f;
+  VPMG_CUDA(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return (double)blocks * threads * iters * 8 * 2 / (ms * 1e-3) / 1e12;
+}
 
 void fill_zero(double* p, size_t n, cudaStream_t s) {
   if (!n) return;

@@ -137,5 +137,6 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
 void fill_zero(double* p, size_t n, cudaStream_t s);
 void exclusive_scan_int(const int* in, int* out, size_t n, int* block_sums, cudaStream_t s);
 size_t scan_block_sums_needed(size_t n);
+double measure_fp64_peak(cudaStream_t s);  // TFLOP/s of a DFMA loop
 
 }  // namespace vpmg
