@@ -132,10 +132,18 @@ class Clocks:
         return out
 
 
-def _workload():
+WORKLOADS = {"leapfrog256": "leapfrog256", "ring64": "ring64", "ring128": "ring128"}
+
+
+def _workload(name="leapfrog256"):
+    """Headline workload (leapfrog256); ring64 / ring128 are the small cases
+    used for profiler captures."""
     from vpm_free_gb300 import workloads as W
-    xp, qp, w = W.leapfrog256()
-    return xp, qp, w
+    if name == "ring64":
+        return W.ring64()
+    if name == "ring128":
+        return W.scaled_ring(128)
+    return W.leapfrog256()
 
 
 def _measured_peaks():
@@ -203,9 +211,11 @@ def run_ours(args, dist):
     from vpm_free_gb300 import build as B
     B.build()
     ws, rank, local = _dist()
-    xp, qp, w = _workload()
+    xp, qp, w = _workload(args.workload)
     cfg = V.VPMConfig.make(dpm=w["dpm"], box=w["box"])
     h = V.VPM(cfg, device=local)
+    if args.operator_budget >= 0:
+        h.set_operator_budget(args.operator_budget)
     h.define_sizes(xp)
     xr, qr = h.remesh_particles_3d(1, xp, qp)
     h.set_particles(xr, qr)
@@ -256,6 +266,8 @@ def run_ours(args, dist):
     # ---- end to end through the reference-facing calls, host arrays -------
     ke = max(1, min(args.steps, args.e2e_steps))
     he = V.VPM(cfg, device=local)
+    if args.operator_budget >= 0:
+        he.set_operator_budget(args.operator_budget)
     he.vpm(xp, qp, None, None, xp.shape[0], WhatToDo=0, NTIME=0)
     XP, QP = he.remesh_particles_3d(1, xp, qp)
     for _ in range(min(args.warmup, 1)):
@@ -283,7 +295,7 @@ def run_ours(args, dist):
            "timing": "host clock around synchronous vpm()/remesh_particles_3d() C-ABI calls"}
     # ---- CPU baseline (rank 0, N = 1, bounded sample) -----------------------
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
+    if rank == 0 and ws == 1 and not args.no_cpu and args.workload == "leapfrog256":
         threads = os.cpu_count() or 1
         v, t, _ = cpu_step_sample(xp, qp, w, 1, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
@@ -292,9 +304,9 @@ def run_ours(args, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded leapfrogging rings)",
-        "config": {"workload": "leapfrog256 (two coaxial rings, 256^3 mesh, M4', tree levels 3, ncoarse 8, remesh "
-                               "every step, dt 0.005)",
-                   "mesh": [256, 256, 256], "block": list(h.sizes().nnbl),
+        "config": {"workload": ("leapfrog256 (two coaxial rings, 256^3 mesh, M4', tree levels 3, ncoarse 8, remesh "
+                                "every step, dt 0.005)") if args.workload == "leapfrog256" else args.workload,
+                   "mesh": [n - 1 for n in h.sizes().nn], "block": list(h.sizes().nnbl),
                    "particles_start": int(xr.shape[0]), "particles_end": h.num_particles(),
                    "l2": "inputs larger than L2 (each field component 135 MB, boundary operator 53 GB)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
@@ -317,6 +329,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="leapfrog256",
+                    help="leapfrog256 is the benchmark; the rings are small profiling cases")
+    ap.add_argument("--operator-budget", type=int, default=-1,
+                    help="bytes for the precomputed boundary operator (0: walk the tree each step)")
     args = ap.parse_args()
     ws, rank, local = _dist()
     if args.impl == "reference":

@@ -26,3 +26,7 @@ def gpulib():
     from vpm_free_gb300 import build
     build.build()
     return V
+
+TESTS = os.path.dirname(os.path.abspath(__file__))
+if TESTS not in sys.path:
+    sys.path.insert(0, TESTS)

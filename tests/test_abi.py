@@ -1,0 +1,79 @@
+"""C-ABI checks that need no GPU: the library loads, exports every entry
+point declared in include/vpmg.h, parses pm.inp like the reference and
+fails with status codes (never aborts) where a GPU is required."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            text = open(os.path.join(inc, f)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names |= set(re.findall(r"\b(vpmg_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+def test_library_exports_every_declared_symbol(gpulib):
+    path = gpulib.library_path()
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (vpmg_[a-z0-9_]+)", out))
+    declared = _declared()
+    assert len(declared) >= 25
+    assert declared <= exported, declared - exported
+    L = gpulib.load_library()
+    for n in declared:
+        assert hasattr(L, n)
+
+
+def test_read_pm_inp_reference_format(gpulib):
+    cfg = gpulib.read_pm_inp(os.path.join(ROOT, "tests", "golden", "pm.inp"))
+    assert list(cfg.dpm) == [4.0, 4.0, 4.0]
+    assert (cfg.interf_iproj, cfg.ibctyp, cfg.idvpm, cfg.ncoarse) == (4, 2, 1, 8)
+    assert (cfg.nbi, cfg.nbj, cfg.nbk, cfg.nremesh, cfg.ncell_rem) == (6, 1, 1, 1, 1)
+    assert (cfg.iyntree, cfg.ilevmax, cfg.idefine, cfg.iynslice) == (1, 3, 1, 0)
+
+
+def test_read_pm_inp_rejects_bad_input(gpulib, tmp_path):
+    p = tmp_path / "pm.inp"
+    p.write_text("1.0 1.0\n")
+    with pytest.raises(gpulib.VPMError):
+        gpulib.read_pm_inp(str(p))
+    lines = open(os.path.join(ROOT, "tests", "golden", "pm.inp")).read().splitlines()
+    lines[12] = " 11   ! more than 10 write windows stops the reference (vpm.f90:146)"
+    p.write_text("\n".join(lines) + "\n")
+    with pytest.raises(gpulib.VPMError):
+        gpulib.read_pm_inp(str(p))
+
+
+def test_status_strings_and_bad_configs(gpulib):
+    L = gpulib.load_library()
+    for st in range(0, -9, -1):
+        assert L.vpmg_status_string(st)
+    cfg = gpulib.VPMConfig.make(dpm=(0.1, 0.1, 0.1))
+    for field, val, code in (("interf_iproj", 9, -1), ("ibctyp", 3, -6), ("idvpm", 0, -6), ("ncell_rem", 2, -6)):
+        c = gpulib.VPMConfig.make(dpm=(0.1, 0.1, 0.1))
+        setattr(c, field, val)
+        h = C.c_void_p()
+        assert L.vpmg_create(C.byref(c), -1, C.byref(h)) == code
+    assert L.vpmg_destroy(None) == -1
+    assert L.vpmg_step(None, 0.1, None, 1) == -1
+
+
+def test_no_gpu_means_error_not_abort(gpulib):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    with pytest.raises(gpulib.VPMError):
+        gpulib.VPM(gpulib.VPMConfig.make(dpm=(0.1, 0.1, 0.1), box=(0, 0, 0, 0.8, 0.8, 0.8)))
