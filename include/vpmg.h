@@ -109,6 +109,32 @@ int vpmg_pmesh(vpmg_handle* h, double* const sol[3], const double* const rhs[3],
 int vpmg_project_particles_3d(vpmg_handle* h, const double* xp, const double* qp, int nvr,
                               double* const rhs[3]);
 
+/* ---- allocation-free Dirichlet solve ----------------------------------
+ * No counterpart in the reference: an extra entry point of this library.
+ * The Dirichlet 7-point solve of vpmg_pmesh(iynbc = 0), for callers that
+ * cannot let a library allocate device memory -- a host code that hands
+ * the whole GPU to its own pool allocator, or one that runs inside a fixed
+ * memory budget where an extra cudaMalloc would fail.  This call makes no
+ * cudaMalloc, cudaFree or allocating library call: its temporaries live in
+ * one static device array of 33.6 MB that every GPU which loads this
+ * library holds until the process exits.
+ *   rhs, sol  device pointers to dims[0]*dims[1]*dims[2] doubles, x fastest;
+ *             the interior of the 0-based inclusive node box `box` of sol
+ *             receives the solution of Lap_h u = rhs; the box faces of sol
+ *             are the Dirichlet values (zero_bc = 0) or are zeroed (1);
+ *   h         mesh spacings;  stream: a cudaStream_t (NULL = default
+ *             stream); the call is asynchronous on that stream.
+ * Limits: at most 2^21 interior nodes and 900 along x and along y; larger
+ * boxes return VPMG_ERR_ARG before any GPU work.  2*(cells) along x and y
+ * must have no prime factor above 31 (else VPMG_ERR_UNSUPPORTED).
+ * The first call on a device does that device's set-up (looks up the
+ * array's device address, loads constant tables): make it from one thread,
+ * and before any stream capture.  Every call shares the one array, which
+ * keeps the last call's contents; each call rebuilds what it reads, but
+ * calls whose GPU work overlaps (other streams, threads) race on it.     */
+int vpmg_dirichlet_static(const double* rhs, double* sol, const int dims[3], const int box[6], const double h[3],
+                          int zero_bc, void* stream);
+
 /* ---- device-resident loop (test.f90:83-150 without the AVATAR inflow) -- */
 int vpmg_define_sizes(vpmg_handle* h, const double* xp, int nvr, int ntime);
 int vpmg_get_sizes(const vpmg_handle* h, vpmg_sizes* out);

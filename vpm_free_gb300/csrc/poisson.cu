@@ -502,4 +502,155 @@ void dirichlet_solve(DirichletPlan& P, const double* rhs, double* sol, bool zero
   VPMG_CUDA(cudaGetLastError());
 }
 
+// ------------------------------------------ allocation-free variant -----
+// vpmg_dirichlet_static: the same five-kernel solve, with every temporary
+// (DST work array, reciprocal pivot table, twiddles, eigenvalues) carved
+// out of one file-scope device array instead of cudaMalloc'd buffers.
+namespace {
+
+constexpr size_t kStaticMaxInterior = (size_t)1 << 21;  // interior nodes (e.g. 128 x 128 x 128)
+constexpr int kStaticMaxLine = 900;                     // interior nodes along x and along y
+constexpr size_t kStaticTw = 2 * (kStaticMaxLine + 1);  // complex FFT length bound
+// doubles: work | pivots | twiddles x (2 per complex) | twiddles y | mu x | mu y
+constexpr size_t kStaticDoubles = 2 * kStaticMaxInterior + 4 * kStaticTw + 2 * kStaticMaxLine;
+
+// 33.6 MB per GPU that loads the library, held until the process exits.
+__device__ __align__(256) double g_static_scratch[kStaticDoubles];
+
+constexpr int kStaticMaxDevices = 64;
+double* g_static_base[kStaticMaxDevices] = {nullptr};
+bool g_static_consts[kStaticMaxDevices] = {false};
+int g_static_smem[kStaticMaxDevices] = {0};
+
+__global__ void k_static_tables(double2* __restrict__ twx, int mx, double2* __restrict__ twy, int my,
+                                double* __restrict__ mux, int nx, double* __restrict__ muy, int ny) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double sn, cs;
+  if (t < mx) {
+    sincospi(-2.0 * t / mx, &sn, &cs);
+    twx[t] = make_double2(cs, sn);
+  }
+  if (t < my) {
+    sincospi(-2.0 * t / my, &sn, &cs);
+    twy[t] = make_double2(cs, sn);
+  }
+  if (t < nx) {
+    sn = sinpi((t + 1) / (2.0 * (nx + 1)));
+    mux[t] = 4.0 * sn * sn;
+  }
+  if (t < ny) {
+    sn = sinpi((t + 1) / (2.0 * (ny + 1)));
+    muy[t] = 4.0 * sn * sn;
+  }
+}
+
+// Radix list of the odd-extended DST-I of n points (no allocation).
+bool static_plan(int n, const double2* tw, FFTDev& d) {
+  d.n = n;
+  d.N = n + 1;
+  d.M = 2 * (n + 1);
+  d.tw = tw;
+  int m = d.M, twos = 0, odd[24], no = 0;
+  while (m % 2 == 0) { m /= 2; ++twos; }
+  for (int f = 3; m > 1; f += 2)
+    while (m % f == 0) {
+      if (f > kMaxOddRadix || no >= 24) return false;
+      odd[no++] = f;
+      m /= f;
+    }
+  d.nst = 0;
+  for (int i = no - 1; i >= 0; --i) d.radix[d.nst++] = odd[i];  // largest first
+  while (twos >= 3) { if (d.nst >= 24) return false; d.radix[d.nst++] = 8; twos -= 3; }
+  if (twos == 2 && d.nst < 24) d.radix[d.nst++] = 4;
+  if (twos == 1 && d.nst < 24) d.radix[d.nst++] = 2;
+  return d.nst <= 24;
+}
+
+}  // namespace
+
 }  // namespace vpmg
+
+extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int dims[3], const int box[6],
+                                     const double h[3], int zero_bc, void* stream) {
+  using namespace vpmg;
+  if (!rhs || !sol || !dims || !box || !h) return VPMG_ERR_ARG;
+  int m[3];
+  for (int d = 0; d < 3; ++d) {
+    m[d] = box[d + 3] - box[d] - 1;
+    if (box[d] < 0 || box[d + 3] >= dims[d] || m[d] < 1 || !(h[d] > 0.0)) return VPMG_ERR_ARG;
+  }
+  // sizes beyond the static scratch are refused, never truncated
+  if (m[0] > kStaticMaxLine || m[1] > kStaticMaxLine || (size_t)m[0] * m[1] * m[2] > kStaticMaxInterior)
+    return VPMG_ERR_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kStaticMaxDevices) {
+    cudaGetLastError();
+    return VPMG_ERR_CUDA;
+  }
+  // once per device, with that device current: the scratch's device address
+  // and the odd-radix DFT constants
+  if (!g_static_base[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return VPMG_ERR_CUDA;
+    }
+    g_static_base[dev] = static_cast<double*>(p);
+  }
+  if (!g_static_consts[dev]) {
+    static double hc[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)], hs[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
+    for (int R = 1; R <= kMaxOddRadix; ++R)
+      for (int i = 0; i < R; ++i) {
+        hc[R * (kMaxOddRadix + 1) + i] = std::cos(2.0 * kPI * i / R);
+        hs[R * (kMaxOddRadix + 1) + i] = std::sin(2.0 * kPI * i / R);
+      }
+    if (cudaMemcpyToSymbol(c_rcos, hc, sizeof(hc)) != cudaSuccess ||
+        cudaMemcpyToSymbol(c_rsin, hs, sizeof(hs)) != cudaSuccess) {
+      cudaGetLastError();
+      return VPMG_ERR_CUDA;
+    }
+    g_static_consts[dev] = true;
+  }
+  double* base = g_static_base[dev];
+  double* work = base;
+  double* rinv = base + kStaticMaxInterior;
+  double2* twx = reinterpret_cast<double2*>(base + 2 * kStaticMaxInterior);
+  double2* twy = twx + kStaticTw;
+  double* mux = reinterpret_cast<double*>(twy + kStaticTw);
+  double* muy = mux + kStaticMaxLine;
+  FFTDev px, py;
+  if (!static_plan(m[0], twx, px) || !static_plan(m[1], twy, py)) return VPMG_ERR_UNSUPPORTED;
+  const int smax = 2 * kPairs * std::max(px.M, py.M) * (int)sizeof(double2);
+  if (smax > 227 * 1024) return VPMG_ERR_UNSUPPORTED;
+  if (smax > g_static_smem[dev]) {
+    if (cudaFuncSetAttribute(k_dst_x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_dst_x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_dst_y, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess) {
+      cudaGetLastError();
+      return VPMG_ERR_CUDA;
+    }
+    g_static_smem[dev] = smax;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // tables and pivots are rebuilt on every call: the array keeps whatever the
+  // previous call (possibly another grid) left in it
+  const int nt = std::max(std::max(px.M, py.M), std::max(m[0], m[1]));
+  k_static_tables<<<(nt + 255) / 256, 256, 0, s>>>(twx, px.M, twy, py.M, mux, m[0], muy, m[1]);
+  const double hz2 = h[2] * h[2], hx2 = h[0] * h[0], hy2 = h[1] * h[1];
+  const int nl = m[0] * m[1];
+  k_pivots<<<(nl + 255) / 256, 256, 0, s>>>(rinv, mux, muy, m[0], m[1], m[2], hz2 / hx2, hz2 / hy2);
+  Box b;
+  for (int d = 0; d < 3; ++d) { b.dims[d] = dims[d]; b.o[d] = box[d] + 1; b.m[d] = m[d]; }
+  const double scale = -hz2 * 4.0 / ((double)(m[0] + 1) * (double)(m[1] + 1));
+  const int lx = m[1] * m[2], ly = m[0] * m[2];
+  const int gx = (lx + 2 * kPairs - 1) / (2 * kPairs), gy = (ly + 2 * kPairs - 1) / (2 * kPairs);
+  const size_t shx = (size_t)2 * kPairs * px.M * sizeof(double2), shy = (size_t)2 * kPairs * py.M * sizeof(double2);
+  k_dst_x_fwd<<<gx, kThreads, shx, s>>>(rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2, 1.0 / hz2, scale);
+  k_dst_y<<<gy, kThreads, shy, s>>>(work, m[0], m[1], m[2], py);
+  k_thomas<<<(nl + 127) / 128, 128, 0, s>>>(work, rinv, m[0], m[1], m[2]);
+  k_dst_y<<<gy, kThreads, shy, s>>>(work, m[0], m[1], m[2], py);
+  k_dst_x_inv<<<gx, kThreads, shx, s>>>(work, sol, b, px);
+  if (zero_bc) k_zero_box_faces<<<256, 256, 0, s>>>(sol, b);
+  if (cudaGetLastError() != cudaSuccess) return VPMG_ERR_CUDA;
+  return VPMG_OK;
+}
