@@ -182,6 +182,63 @@ def cpu_step_sample(xp, qp, w, steps, threads):
     return ps / t, t, ps
 
 
+def run_batched(args, local):
+    """Batched solves/s: 64 independent ring problems on meshes drawn from
+    {32,48,64,96,128}^3 plus the 128^3 two-level (ncoarse = 2) case,
+    advanced together (one captured step graph per problem, replayed
+    concurrently on per-problem streams), against looping the plain path
+    (one problem after the other, vpmg_step with its host sync per step)."""
+    import vpm_free_gb300 as V
+    from vpm_free_gb300 import workloads as W
+    probs = W.batched_rings(64)
+    xp2, qp2, w2 = W.two_level_128()
+    probs.append((xp2, qp2, w2))
+    hs, init = [], []
+    t0 = time.perf_counter()
+    for xp, qp, w in probs:
+        cfg = V.VPMConfig.make(dpm=w["dpm"], box=w["box"], ncoarse=w.get("ncoarse", 8))
+        h = V.VPM(cfg, device=local)
+        h.set_operator_budget(args.batch_operator_budget)
+        h.define_sizes(xp)
+        xr, qr = h.remesh_particles_3d(1, xp, qp)
+        init.append((xr, qr))
+        hs.append(h)
+    setup_s = time.perf_counter() - t0
+    dt = 0.01
+    k = max(1, args.batch_steps)
+
+    def reset():  # every phase starts from the same remeshed particles
+        for h, (xr, qr) in zip(hs, init):
+            h.set_particles(xr, qr)
+    reset()
+    V.VPM.batch_run(hs, 1, dt)                       # warm-up, captures the graphs
+    reset()
+    ms_b, solves, ps_b = V.VPM.batch_run(hs, k, dt)
+    reset()
+    for h in hs:                                     # plain loop: problem after problem
+        h.step(dt)
+    reset()
+    t1 = time.perf_counter()
+    for h in hs:
+        for _ in range(k):
+            h.step(dt)
+    loop_s = time.perf_counter() - t1
+    reset()
+    t2 = time.perf_counter()
+    for h in hs:                                     # looped graph replays, one problem at a time
+        h.run(k, dt)
+    graph_loop_s = time.perf_counter() - t2
+    precomputed = sum(1 for h in hs if h.tree_stats()["precomputed"])
+    for h in hs:
+        h.close()
+    return {"problems": len(hs), "steps": k, "solves_per_s": solves / (ms_b * 1e-3),
+            "particle_steps_per_s": ps_b / (ms_b * 1e-3), "ms": ms_b,
+            "loop_plain_solves_per_s": len(hs) * k / loop_s, "loop_graph_solves_per_s": len(hs) * k / graph_loop_s,
+            "speedup_vs_plain_loop": (solves / (ms_b * 1e-3)) / (len(hs) * k / loop_s),
+            "setup_s": setup_s, "precomputed_operators": precomputed,
+            "timing": "batched: CUDA events over all streams; loops: host clock (each step synchronous)"}
+
+
 def run_reference(args, dist):
     if dist.rank != 0:
         return 0
@@ -240,7 +297,7 @@ def run_ours(args, dist):
     peaks = _measured_peaks()
     kernels = []
     for which, name, per_step in ((0, "k_apply_csr (boundary operator, fine block)", 1),
-                                  (1, "fine-block Dirichlet solve (k_dst_x_fwd, k_dst_y x2, k_thomas, k_dst_x_inv)", 6),
+                                  (1, "inner-box Dirichlet solve (k_dst_x_fwd, k_dst_y x2, k_thomas, k_dst_x_inv)", 3),
                                   (2, "k_deposit (M4' gather deposition)", 2)):
         kms, fl, by = h.bench_kernel(which, reps=3)
         kernels.append({"kernel": name, "ms_per_launch": kms, "launches_per_step": per_step,
@@ -263,6 +320,10 @@ def run_ours(args, dist):
     roof = dict(roofs[kernels.index(dom)])
     roof["peak_source"] = ("FP64: DFMA-loop TFLOP/s measured in this run (no FP64 entry in MEASURED_PEAKS.json); "
                            "HBM: MEASURED_PEAKS.json hbm_gbs")
+    tree = h.tree_stats()
+    sizes_bl = list(h.sizes().nnbl)
+    sizes_nn = list(h.sizes().nn)
+    np_end = h.num_particles()
     # ---- end to end through the reference-facing calls, host arrays -------
     ke = max(1, min(args.steps, args.e2e_steps))
     he = V.VPM(cfg, device=local)
@@ -300,24 +361,27 @@ def run_ours(args, dist):
         v, t, _ = cpu_step_sample(xp, qp, w, 1, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"1 full step (field step + Euler + remesh) of this workload, {t:.1f} s on {threads} threads"}
+    h.close()
+    he.close()
+    batched = None
+    if not args.no_batched and args.workload == "leapfrog256":
+        batched = run_batched(args, local)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded leapfrogging rings)",
         "config": {"workload": ("leapfrog256 (two coaxial rings, 256^3 mesh, M4', tree levels 3, ncoarse 8, remesh "
                                 "every step, dt 0.005)") if args.workload == "leapfrog256" else args.workload,
-                   "mesh": [n - 1 for n in h.sizes().nn], "block": list(h.sizes().nnbl),
-                   "particles_start": int(xr.shape[0]), "particles_end": h.num_particles(),
+                   "mesh": [n - 1 for n in sizes_nn], "block": sizes_bl,
+                   "particles_start": int(xr.shape[0]), "particles_end": np_end,
                    "l2": "inputs larger than L2 (each field component 135 MB, boundary operator 53 GB)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "clocks": clk if rank == 0 else None,
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "roofline_kernels": roofs,
-        "tree": h.tree_stats(), "cpu_baseline": cpu,
+        "tree": tree, "cpu_baseline": cpu, "batched": batched,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    h.close()
-    he.close()
     return 0
 
 
@@ -331,6 +395,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="leapfrog256",
                     help="leapfrog256 is the benchmark; the rings are small profiling cases")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-problems measurement")
+    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--batch-operator-budget", type=int, default=12 << 30,
+                    help="bytes of recorded boundary operator per batched problem")
     ap.add_argument("--operator-budget", type=int, default=-1,
                     help="bytes for the precomputed boundary operator (0: walk the tree each step)")
     args = ap.parse_args()

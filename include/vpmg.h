@@ -126,7 +126,7 @@ int vpmg_project_particles_3d(vpmg_handle* h, const double* xp, const double* qp
  *             stream); the call is asynchronous on that stream.
  * Limits: at most 2^21 interior nodes and 900 along x and along y; larger
  * boxes return VPMG_ERR_ARG before any GPU work.  2*(cells) along x and y
- * must have no prime factor above 31 (else VPMG_ERR_UNSUPPORTED).
+ * must have no prime factor above 17 (else VPMG_ERR_UNSUPPORTED).
  * The first call on a device does that device's set-up (looks up the
  * array's device address, loads constant tables): make it from one thread,
  * and before any stream capture.  Every call shares the one array, which
@@ -173,13 +173,25 @@ long long vpmg_kernel_launches(const vpmg_handle* h);
 int vpmg_phase_times(const vpmg_handle* h, double ms[9]);
 /* Boundary-operator statistics: interactions per fine solve, bytes held. */
 int vpmg_tree_stats(const vpmg_handle* h, long long* interactions, long long* bytes, int* precomputed);
-/* Turns per-phase event timing on/off (default off). */
+/* Per-phase event timing: 0 off (default), 1 on; 2 also keeps the
+ * intermediate block fields readable by vpmg_get_field and evaluates the
+ * block solves on the whole block (as the reference does) instead of only
+ * where the step reads them; 3 = 2. */
 int vpmg_set_profiling(vpmg_handle* h, int on);
 /* Runs nsteps device-resident steps (as vpmg_step) between two CUDA events
  * on the handle's stream; *ms = elapsed device time, *particle_steps = sum
- * of the particle counts at the start of each step.                      */
+ * of the particle counts at the start of each step.  The step is captured
+ * once as a CUDA graph (counts stay on the device) and replayed.         */
 int vpmg_run(vpmg_handle* h, int nsteps, double dt, const double uinf[3], int remesh, double* ms,
              long long* particle_steps);
+/* Batched problems: n independent handles (each its own mesh, particles,
+ * stream) advance nsteps device-resident steps.  Each handle's step is
+ * captured once as a CUDA graph; the graphs of all problems are replayed
+ * step by step on their own streams so that small problems run
+ * concurrently.  *ms = device time of the whole batch, *solves = n*nsteps,
+ * *particle_steps = sum over problems and steps of the particle count.   */
+int vpmg_batch_run(vpmg_handle* const* hs, int n, int nsteps, double dt, int remesh, double* ms,
+                   long long* solves, long long* particle_steps);
 /* Replays one kernel of the last step `reps` times between CUDA events on
  * the handle's stream (instrumentation for roofline figures).
  *   which = 0: boundary operator apply on the fine block (k_apply_csr or

@@ -94,3 +94,90 @@ def test_deposition_matches_oracle(gpulib, oracle):
         got = h.project_particles_3D(xp, qp)
     for c in range(3):
         assert rel_l2(got[c], ref[c]) <= 1e-13
+
+
+@pytest.mark.parametrize("ncell", [32, 64])
+def test_partial_block_solves_equal_full_solves(gpulib, ncell):
+    """The block solves evaluated only where the step reads them give the
+    same step as solving the whole padded block (the reference's way)."""
+    from vpm_free_gb300 import workloads as W
+    V = gpulib
+    xp, qp, w = W.scaled_ring(ncell)
+    _, gcfg = configs_for(w)
+    out = {}
+    for mode in (0, 3):
+        with V.VPM(gcfg) as h:
+            h.set_profiling(mode)
+            h.define_sizes(xp)
+            up = np.zeros((xp.shape[0], 3))
+            gp = np.zeros((xp.shape[0], 3))
+            h.vpm(xp, qp, up, gp, xp.shape[0], WhatToDo=2)
+            out[mode] = (up, gp, h.field("sol"), h.field("vel"), h.field("coarse_sol"))
+    for a, b in zip(out[0], out[3]):
+        assert rel_l2(a, b) <= 1e-12
+
+
+def _ring_handle(V, ncell, **kw):
+    from vpm_free_gb300 import workloads as W
+    xp, qp, w = W.scaled_ring(ncell)
+    _, gcfg = configs_for(w, **kw)
+    h = V.VPM(gcfg)
+    h.define_sizes(xp)
+    xr, qr = h.remesh_particles_3d(1, xp, qp)
+    h.set_particles(xr, qr)
+    return h, w
+
+
+def test_graph_replay_equals_uncaptured_steps(gpulib):
+    """vpmg_run replays one captured step graph; it must reproduce the
+    uncaptured vpmg_step loop bit for bit (deterministic kernels)."""
+    V = gpulib
+    a, w = _ring_handle(V, 48)
+    b, _ = _ring_handle(V, 48)
+    for _ in range(4):
+        a.step(w["dt"])
+    ms, ps = b.run(4, w["dt"])
+    xa, qa = a.get_particles()
+    xb, qb = b.get_particles()
+    assert np.array_equal(xa, xb) and np.array_equal(qa, qb)
+    assert ms > 0 and ps > 0
+    a.close()
+    b.close()
+
+
+def test_batched_problems_equal_individual_runs(gpulib):
+    V = gpulib
+    sizes = (32, 48, 64)
+    solo = []
+    for n in sizes:
+        h, w = _ring_handle(V, n)
+        h.run(3, w["dt"])
+        solo.append(h.get_particles())
+        h.close()
+    hs = [_ring_handle(V, n)[0] for n in sizes]
+    ms, solves, ps = V.VPM.batch_run(hs, 3, 0.01)
+    assert solves == 3 * len(sizes) and ms > 0 and ps > 0
+    for h, (x0, q0) in zip(hs, solo):
+        x1, q1 = h.get_particles()
+        assert np.array_equal(x0, x1) and np.array_equal(q0, q1)
+        h.close()
+
+
+def test_two_level_ncoarse2_matches_oracle(gpulib, oracle):
+    """YAPS with ncoarse = 2: the padded block (cells = 4 mod 8) has dummy
+    quadtree cells at levels 2 and 3 (build_level_nbound_3d)."""
+    from vpm_free_gb300 import workloads as W
+    V, O = gpulib, oracle
+    xp, qp, w = W.scaled_ring(32)  # padded block of 36 cells: 36 = 4 mod 8
+    ocfg, gcfg = configs_for(w, ncoarse=2)
+    s = O.define_sizes(ocfg, xp)
+    assert (s.nnbl[0] - 1) % 8 != 0
+    up_o, gp_o = O.step_fields(ocfg, s, xp, qp)
+    with V.VPM(gcfg) as h:
+        h.define_sizes(xp)
+        up = np.zeros_like(up_o)
+        gp = np.zeros_like(gp_o)
+        h.vpm(xp, qp, up, gp, xp.shape[0], WhatToDo=2)
+        for name, fid in (("sol", O.F_SOL), ("vel", O.F_VEL)):
+            assert rel_l2(h.field(name).ravel(), O.get_field(fid)) <= FIELD_TOL, name
+    assert rel_l2(up, up_o) <= PART_TOL and rel_l2(gp, gp_o) <= PART_TOL

@@ -35,7 +35,7 @@ EXPORTS = [
     "vpmg_remesh_particles_3d", "vpmg_pmesh", "vpmg_project_particles_3d", "vpmg_define_sizes", "vpmg_get_sizes",
     "vpmg_set_particles", "vpmg_get_particles", "vpmg_get_particle_velocity", "vpmg_step", "vpmg_remesh_device",
     "vpmg_num_particles", "vpmg_get_field", "vpmg_kernel_launches", "vpmg_phase_times", "vpmg_tree_stats",
-    "vpmg_set_profiling", "vpmg_set_operator_budget", "vpmg_run", "vpmg_bench_kernel", "vpmg_fp64_peak",
+    "vpmg_set_profiling", "vpmg_set_operator_budget", "vpmg_run", "vpmg_bench_kernel", "vpmg_fp64_peak", "vpmg_batch_run",
 ]
 
 
@@ -127,6 +127,8 @@ def load_library():
     L.vpmg_run.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, C.c_int, _dp, C.POINTER(C.c_longlong)]
     L.vpmg_bench_kernel.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp]
     L.vpmg_fp64_peak.argtypes = [C.c_void_p, _dp]
+    L.vpmg_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_double, C.c_int, _dp,
+                                 C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     _LIB = L
     return L
 
@@ -281,6 +283,19 @@ class VPM:
         self._chk(self._L.vpmg_run(self._h, int(nsteps), float(dt), _p(u), 1 if remesh else 0, C.byref(ms),
                                    C.byref(ps)))
         return ms.value, ps.value
+
+    @staticmethod
+    def batch_run(handles, nsteps, dt, remesh=True):
+        """Advances independent problems together (one graph per problem,
+        replayed concurrently).  Returns (device ms, solves, particle-steps)."""
+        L = load_library()
+        arr = (C.c_void_p * len(handles))(*[h._h for h in handles])
+        ms, sv, ps = C.c_double(0), C.c_longlong(0), C.c_longlong(0)
+        rc = L.vpmg_batch_run(arr, len(handles), int(nsteps), float(dt), 1 if remesh else 0, C.byref(ms), C.byref(sv),
+                              C.byref(ps))
+        if rc != 0:
+            handles[0]._chk(rc)
+        return ms.value, sv.value, ps.value
 
     def bench_kernel(self, which, reps=5):
         """(ms per replay, algorithmic flops, algorithmic bytes) of one kernel."""

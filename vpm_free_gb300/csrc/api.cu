@@ -13,6 +13,7 @@
 #include <sstream>
 #include <string>
 
+#include "block_solve.h"
 #include "fields.h"
 #include "particles.h"
 #include "vpmg_internal.h"
@@ -36,6 +37,8 @@ struct vpmg_handle {
   DBuf<double> rhs_bl, sol_bl, sol0, work, bl_sol1_copy;
   DBuf<double> samp, crhs, csol, csol0;
   DirichletPlan dp_bl, dp_inner, dp_c;
+  BlockSolve bsolve;      // partially evaluated block solves
+  bool full_block_solves = false;  // evaluate the block solves everywhere (parity / debugging)
   BoundaryOp bo_bl, bo_c;
   YapsDev yaps;
   bool keep_intermediates = false;
@@ -47,7 +50,16 @@ struct vpmg_handle {
   DBuf<double> bench_scratch;  // replay outputs of vpmg_bench_kernel
   // timing
   bool profile = false;
+  bool no_graphs = false;
   cudaEvent_t ev[10] = {};
+  // graph of one device-resident step, and the per-step particle-count log
+  struct {
+    cudaGraphExec_t exec = nullptr;
+    double dt = 0, u[3] = {0, 0, 0};
+    int remesh = -1;
+    long long launches = 0;
+  } graph;
+  DBuf<int> hist, hist_counter;
   double phase_ms[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 };
 
@@ -204,6 +216,7 @@ void prepare(vpmg_handle* h) {
   size_t wmax = 0;
   for (DirichletPlan* p : {&h->dp_bl, &h->dp_inner, &h->dp_c}) wmax = std::max(wmax, (size_t)p->m[0] * p->m[1] * p->m[2]);
   h->work.ensure(wmax);
+  h->bsolve.prepare(h->dp_bl, s.nnbl_bl, h->cfg.ncoarse);
   for (int d = 0; d < 3; ++d) {
     h->inner_lo[d] = s.nnbl_bl[d] - 1;
     h->inner_ext[d] = s.nnbl_bl[d + 3] - s.nnbl_bl[d] + 1;
@@ -267,16 +280,23 @@ void field_step(vpmg_handle* h) {
   for (int c = 0; c < 3; ++c) box_copy(R[c], s.nn, go, comp(h->rhs_bl, NB, c), s.nnbl, h->inner_lo, h->inner_ext, st);
   fill_zero(h->sol_bl.p, 3 * NB, st);
   ev_mark(h, 1);
-  // yaps3d (a): fine infinite-domain solve on the padded block
+  // yaps3d (a): fine infinite-domain solve on the padded block.  By default
+  // both block solves are evaluated only where the step reads them
+  // (block_solve.cu); the full solves remain for parity checks.
+  const bool full = h->full_block_solves || h->keep_intermediates;
   for (int c = 0; c < 3; ++c) {
-    dirichlet_solve(h->dp_bl, comp(h->rhs_bl, NB, c), h->sol0.p, true, h->work.p, st);
+    if (full) dirichlet_solve(h->dp_bl, comp(h->rhs_bl, NB, c), h->sol0.p, true, h->work.p, st);
+    else block_solve_zero_bc(h->bsolve, h->dp_bl, comp(h->rhs_bl, NB, c), c, h->sol0.p, st);
     boundary_panels(h->bo_bl, h->gbl, h->sol0.p, c, st);
   }
   ev_mark(h, 2);
   double* SB[3] = {comp(h->sol_bl, NB, 0), comp(h->sol_bl, NB, 1), comp(h->sol_bl, NB, 2)};
   boundary_apply(h->bo_bl, h->gbl, SB, st);
   ev_mark(h, 3);
-  for (int c = 0; c < 3; ++c) dirichlet_solve(h->dp_bl, comp(h->rhs_bl, NB, c), SB[c], false, h->work.p, st);
+  for (int c = 0; c < 3; ++c) {
+    if (full) dirichlet_solve(h->dp_bl, comp(h->rhs_bl, NB, c), SB[c], false, h->work.p, st);
+    else block_solve_bc(h->bsolve, h->dp_bl, c, SB[c], st);
+  }
   if (h->keep_intermediates) {
     h->bl_sol1_copy.ensure(3 * NB);
     VPMG_CUDA(cudaMemcpyAsync(h->bl_sol1_copy.p, h->sol_bl.p, sizeof(double) * 3 * NB, cudaMemcpyDeviceToDevice, st));
@@ -325,17 +345,24 @@ void remesh(vpmg_handle* h) {
   for (int d = 0; d < 3; ++d) gr.d[d] = (s.xbound[d + 3] - s.xbound[d]) / (double)(s.nn[d] - 1);
   const MeshDev mr = mesh_dev(gr, h->cfg.interf_iproj);
   const size_t N = gr.count();
-  bin_particles(h->parts, h->np, mr, h->bins, st);
+  bin_particles(h->parts, mr, h->bins, st);
   double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
   deposit(h->parts, mr, h->bins, R, st);
   const int hh = h->cfg.interf_iproj / 2;
   const int lo[3] = {s.nn_bl[0] - 1 + hh, s.nn_bl[1] - 1 + hh, s.nn_bl[2] - 1 + hh};
   const int hi[3] = {s.nn_bl[3] - 1 - hh, s.nn_bl[4] - 1 - hh, s.nn_bl[5] - 1 - hh};
   const double thr = (double)1e-09f;  // default-REAL literal of vpm_remesh.f90:184
-  const int n = remesh_emit(h->parts, mr, h->bins, R, lo, hi, thr, h->parts.capacity, st);
-  VPMG_CHECK(n <= h->parts.capacity, VPMG_ERR_CAPACITY, "remesh exceeds the particle capacity");
-  h->np = n;
+  remesh_emit(h->parts, mr, h->bins, R, lo, hi, thr, st);  // count stays on the device
   ev_mark(h, 9);
+}
+
+__global__ void k_set_int(int* __restrict__ d, int v) { *d = v; }
+
+// Host mirror of the device particle count, and the errors flagged since
+// the last sync (stencil outside the mesh, remesh over capacity).
+void sync_np(vpmg_handle* h) {
+  check_particle_errors(h->bins, h->stream);
+  h->np = read_count(h->parts.d_np.p, h->stream);
 }
 
 __global__ void k_aos_to_soa(const double* __restrict__ xa, const double* __restrict__ qa, int n, double* x, double* y,
@@ -368,6 +395,8 @@ void upload_particles(vpmg_handle* h, const double* xp, const double* qp, int n)
     VPMG_LAUNCHED();
     VPMG_CUDA(cudaGetLastError());
   }
+  k_set_int<<<1, 1, 0, h->stream>>>(h->parts.d_np.p, n);
+  VPMG_LAUNCHED();
   h->np = n;
 }
 
@@ -495,6 +524,7 @@ int vpmg_destroy(vpmg_handle* h) {
   if (!h) return VPMG_ERR_ARG;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph.exec) cudaGraphExecDestroy(h->graph.exec);
   for (int i = 0; i < 10; ++i)
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -532,6 +562,7 @@ int vpmg_set_particles(vpmg_handle* h, const double* xp, const double* qp, int n
 int vpmg_get_particles(vpmg_handle* h, double* xp, double* qp, int* nvr, int capacity) {
   return guarded(h, [&] {
     VPMG_CHECK(nvr, VPMG_ERR_ARG, "nvr is null");
+    sync_np(h);
     *nvr = h->np;
     VPMG_CHECK(h->np <= capacity, VPMG_ERR_CAPACITY, "caller arrays too small");
     download_particles(h, xp, qp, h->np);
@@ -555,15 +586,77 @@ int vpmg_num_particles(const vpmg_handle* h, int* nvr) {
 }
 
 namespace {
+// hist[(*counter)++] = particle count at the start of a step (graph node).
+__global__ void k_log_count(int* __restrict__ hist, int* __restrict__ counter, const int* __restrict__ np, int cap) {
+  const int c = *counter;
+  if (c < cap) hist[c] = *np;
+  *counter = c + 1;
+}
+
+constexpr int kHistCap = 1 << 16;
+
 void one_step(vpmg_handle* h, double dt, const double uinf[3], int do_remesh) {
   VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
   const double u0[3] = {uinf ? uinf[0] : 0.0, uinf ? uinf[1] : 0.0, uinf ? uinf[2] : 0.0};
   ev_mark(h, 0);
-  bin_particles(h->parts, h->np, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
+  bin_particles(h->parts, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
   field_step(h);
   m2p_step(h, true, true, dt, u0);
   if (do_remesh) remesh(h);
   else ev_mark(h, 9);
+}
+
+// One step (field step + Euler + remesh, preceded by the count log) as a
+// CUDA graph on the handle's stream.  Re-captured when dt, uinf or the
+// remesh flag change.
+void ensure_graph(vpmg_handle* h, double dt, const double uinf[3], int do_remesh) {
+  VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
+  VPMG_CHECK(!h->keep_intermediates, VPMG_ERR_STATE, "graph capture is off while intermediates are kept");
+  const double u0[3] = {uinf ? uinf[0] : 0.0, uinf ? uinf[1] : 0.0, uinf ? uinf[2] : 0.0};
+  auto& G = h->graph;
+  if (G.exec && G.dt == dt && G.u[0] == u0[0] && G.u[1] == u0[1] && G.u[2] == u0[2] && G.remesh == do_remesh) return;
+  if (G.exec) {
+    cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
+  }
+  h->hist.ensure(kHistCap);
+  h->hist_counter.ensure(1);
+  const bool prof = h->profile;
+  h->profile = false;
+  const long long l0 = h->launches;
+  cudaGraph_t g = nullptr;
+  VPMG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    k_log_count<<<1, 1, 0, h->stream>>>(h->hist.p, h->hist_counter.p, h->parts.d_np.p, kHistCap);
+    VPMG_LAUNCHED();
+    one_step(h, dt, u0, do_remesh);
+  } catch (...) {
+    cudaStreamEndCapture(h->stream, &g);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    h->profile = prof;
+    h->launches = l0;
+    throw;
+  }
+  h->profile = prof;
+  VPMG_CUDA(cudaStreamEndCapture(h->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&G.exec, g, 0);
+  cudaGraphDestroy(g);
+  VPMG_CUDA(e);
+  G.launches = h->launches - l0;  // counted per replay from now on
+  h->launches = l0;
+  G.dt = dt;
+  for (int d = 0; d < 3; ++d) G.u[d] = u0[d];
+  G.remesh = do_remesh;
+}
+
+long long read_hist(vpmg_handle* h, int n) {
+  std::vector<int> v(std::max(n, 1));
+  if (n > 0) VPMG_CUDA(cudaMemcpyAsync(v.data(), h->hist.p, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+  VPMG_CUDA(cudaStreamSynchronize(h->stream));
+  long long s = 0;
+  for (int i = 0; i < n; ++i) s += v[i];
+  return s;
 }
 }  // namespace
 
@@ -571,6 +664,7 @@ int vpmg_step(vpmg_handle* h, double dt, const double uinf[3], int do_remesh) {
   return guarded(h, [&] {
     one_step(h, dt, uinf, do_remesh);
     VPMG_CUDA(cudaStreamSynchronize(h->stream));
+    sync_np(h);
     finish_phase_times(h);
   });
 }
@@ -579,21 +673,44 @@ int vpmg_run(vpmg_handle* h, int nsteps, double dt, const double uinf[3], int do
              long long* particle_steps) {
   return guarded(h, [&] {
     VPMG_CHECK(nsteps >= 0, VPMG_ERR_ARG, "nsteps < 0");
+    const bool use_graph = !h->keep_intermediates && !h->no_graphs;
+    if (use_graph) ensure_graph(h, dt, uinf, do_remesh);
     cudaEvent_t a, b;
     VPMG_CUDA(cudaEventCreate(&a));
     VPMG_CUDA(cudaEventCreate(&b));
     const bool prof = h->profile;
     h->profile = false;
     long long ps = 0;
+    float t = 0.f;
     try {
-      VPMG_CUDA(cudaStreamSynchronize(h->stream));
-      VPMG_CUDA(cudaEventRecord(a, h->stream));
-      for (int k = 0; k < nsteps; ++k) {
-        ps += h->np;
-        one_step(h, dt, uinf, do_remesh);
+      for (int done = 0; done < nsteps || (nsteps == 0 && done == 0);) {
+        const int chunk = std::min(nsteps - done, kHistCap);
+        VPMG_CUDA(cudaStreamSynchronize(h->stream));
+        if (use_graph) VPMG_CUDA(cudaMemsetAsync(h->hist_counter.p, 0, sizeof(int), h->stream));
+        VPMG_CUDA(cudaEventRecord(a, h->stream));
+        for (int k = 0; k < chunk; ++k) {
+          if (use_graph) {
+            VPMG_CUDA(cudaGraphLaunch(h->graph.exec, h->stream));
+          } else {
+            ps += h->np;
+            one_step(h, dt, uinf, do_remesh);
+            VPMG_CUDA(cudaStreamSynchronize(h->stream));
+            sync_np(h);
+          }
+        }
+        VPMG_CUDA(cudaEventRecord(b, h->stream));
+        VPMG_CUDA(cudaEventSynchronize(b));
+        float tc = 0.f;
+        VPMG_CUDA(cudaEventElapsedTime(&tc, a, b));
+        t += tc;
+        if (use_graph) {
+          ps += read_hist(h, chunk);
+          h->launches += (long long)chunk * h->graph.launches;
+        }
+        done += chunk;
+        if (nsteps == 0) break;
       }
-      VPMG_CUDA(cudaEventRecord(b, h->stream));
-      VPMG_CUDA(cudaEventSynchronize(b));
+      sync_np(h);
     } catch (...) {
       h->profile = prof;
       cudaEventDestroy(a);
@@ -601,11 +718,60 @@ int vpmg_run(vpmg_handle* h, int nsteps, double dt, const double uinf[3], int do
       throw;
     }
     h->profile = prof;
-    float t = 0.f;
-    VPMG_CUDA(cudaEventElapsedTime(&t, a, b));
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (ms) *ms = t;
+    if (particle_steps) *particle_steps = ps;
+  });
+}
+
+int vpmg_batch_run(vpmg_handle* const* hs, int n, int nsteps, double dt, int do_remesh, double* ms,
+                   long long* solves, long long* particle_steps) {
+  if (!hs || n <= 0 || nsteps < 0) return VPMG_ERR_ARG;
+  for (int i = 0; i < n; ++i)
+    if (!hs[i]) return VPMG_ERR_ARG;
+  // each problem: its own handle, stream and step graph; the graphs of all
+  // problems are replayed step by step, interleaved, on their own streams
+  for (int i = 0; i < n; ++i) {
+    const int rc = guarded(hs[i], [&] {
+      ensure_graph(hs[i], dt, nullptr, do_remesh);
+      VPMG_CUDA(cudaMemsetAsync(hs[i]->hist_counter.p, 0, sizeof(int), hs[i]->stream));
+      VPMG_CUDA(cudaStreamSynchronize(hs[i]->stream));
+    });
+    if (rc != VPMG_OK) return rc;
+  }
+  vpmg_handle* h0 = hs[0];
+  return guarded(h0, [&] {
+    VPMG_CHECK(nsteps <= kHistCap, VPMG_ERR_ARG, "too many steps for one batched run");
+    cudaEvent_t start, stop;
+    std::vector<cudaEvent_t> done(n);
+    VPMG_CUDA(cudaEventCreateWithFlags(&start, cudaEventDefault));
+    VPMG_CUDA(cudaEventCreateWithFlags(&stop, cudaEventDefault));
+    for (int i = 0; i < n; ++i) VPMG_CUDA(cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming));
+    VPMG_CUDA(cudaEventRecord(start, h0->stream));
+    for (int i = 1; i < n; ++i) VPMG_CUDA(cudaStreamWaitEvent(hs[i]->stream, start, 0));
+    for (int k = 0; k < nsteps; ++k)
+      for (int i = 0; i < n; ++i) VPMG_CUDA(cudaGraphLaunch(hs[i]->graph.exec, hs[i]->stream));
+    for (int i = 1; i < n; ++i) {
+      VPMG_CUDA(cudaEventRecord(done[i], hs[i]->stream));
+      VPMG_CUDA(cudaStreamWaitEvent(h0->stream, done[i], 0));
+    }
+    VPMG_CUDA(cudaEventRecord(stop, h0->stream));
+    VPMG_CUDA(cudaEventSynchronize(stop));
+    float t = 0.f;
+    VPMG_CUDA(cudaEventElapsedTime(&t, start, stop));
+    cudaEventDestroy(start);
+    cudaEventDestroy(stop);
+    for (int i = 0; i < n; ++i) cudaEventDestroy(done[i]);
+    long long ps = 0;
+    for (int i = 0; i < n; ++i) {
+      ps += read_hist(hs[i], nsteps);
+      hs[i]->launches += (long long)nsteps * hs[i]->graph.launches;
+      LaunchScope ls(hs[i]);
+      sync_np(hs[i]);
+    }
+    if (ms) *ms = t;
+    if (solves) *solves = (long long)n * nsteps;
     if (particle_steps) *particle_steps = ps;
   });
 }
@@ -628,8 +794,8 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
     } else if (which == 1) {
       h->bench_scratch.ensure(NB);
       double* o = h->bench_scratch.p;
-      f = [h, o, st] { dirichlet_solve(h->dp_bl, h->rhs_bl.p, o, true, h->work.p, st); };
-      const DirichletPlan& P = h->dp_bl;
+      f = [h, o, st] { dirichlet_solve(h->dp_inner, h->rhs_bl.p, o, true, h->work.p, st); };
+      const DirichletPlan& P = h->dp_inner;
       const double nint = (double)P.m[0] * P.m[1] * P.m[2];
       fl = nint * (5.0 * std::log2(2.0 * (P.m[0] + 1)) + 5.0 * std::log2(2.0 * (P.m[1] + 1)) + 9.0);
       by = 16.0 * (double)NB;
@@ -639,9 +805,9 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
       const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
       // the last step ended with a remesh, which reuses the binning buffers
       // for its compaction: bin the current particles on the global mesh again
-      bin_particles(h->parts, h->np, mg, h->bins, st);
+      bin_particles(h->parts, mg, h->bins, st);
       f = [h, o, mg, st] { deposit(h->parts, mg, h->bins, o, st); };
-      const double P = (double)h->bins.nsorted;
+      const double P = (double)read_count(h->bins.nsorted_dev, st);
       const int w = mg.ips + mg.ipf + 1;
       fl = P * w * w * w * 8.0;
       by = 56.0 * P + 24.0 * (double)N;
@@ -672,6 +838,7 @@ int vpmg_remesh_device(vpmg_handle* h) {
     VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
     remesh(h);
     VPMG_CUDA(cudaStreamSynchronize(h->stream));
+    sync_np(h);
   });
 }
 
@@ -696,12 +863,13 @@ int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int
     if (*nvr == 0) return;  // vpm.f90:171
     upload_particles(h, xp, qp, *nvr);
     const double u0[3] = {0, 0, 0};
-    bin_particles(h->parts, h->np, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
+    bin_particles(h->parts, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
     field_step(h);
     m2p_step(h, true, false, 0.0, u0);
     VPMG_CUDA(cudaMemcpyAsync(up, h->parts.up.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost, h->stream));
     VPMG_CUDA(cudaMemcpyAsync(gp, h->parts.gp.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost, h->stream));
     VPMG_CUDA(cudaStreamSynchronize(h->stream));
+    check_particle_errors(h->bins, h->stream);
   });
 }
 
@@ -711,6 +879,7 @@ int vpmg_remesh_particles_3d(vpmg_handle* h, int iflag, double* xp, double* qp, 
     VPMG_CHECK(nvr, VPMG_ERR_ARG, "NVR is null");
     upload_particles(h, xp, qp, *nvr);
     remesh(h);
+    sync_np(h);
     *nvr = h->np;
     VPMG_CHECK(h->np <= capacity, VPMG_ERR_CAPACITY, "remesh produced more particles than the caller's capacity");
     download_particles(h, xp, qp, h->np);
@@ -719,6 +888,7 @@ int vpmg_remesh_particles_3d(vpmg_handle* h, int iflag, double* xp, double* qp, 
 
 int vpmg_pmesh(vpmg_handle* h, double* const sol[3], const double* const rhs[3], const double xbound[6],
                const double dpm[3], const int nn[3], const int nn_bl[6], int iynbc, int itree, int levmax) {
+
   return guarded(h, [&] {
     VPMG_CHECK(sol && rhs && xbound && dpm && nn && nn_bl, VPMG_ERR_ARG, "null argument");
     const Grid g = make_grid(xbound, dpm, nn);
@@ -761,7 +931,7 @@ int vpmg_project_particles_3d(vpmg_handle* h, const double* xp, const double* qp
   return guarded(h, [&] {
     upload_particles(h, xp, qp, nvr);
     const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
-    bin_particles(h->parts, h->np, mg, h->bins, h->stream);
+    bin_particles(h->parts, mg, h->bins, h->stream);
     const size_t N = h->gglob.count();
     double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
     deposit(h->parts, mg, h->bins, R, h->stream);
@@ -818,6 +988,7 @@ int vpmg_set_profiling(vpmg_handle* h, int on) {
   if (!h) return VPMG_ERR_ARG;
   h->profile = on != 0;
   h->keep_intermediates = on >= 2;
+  h->full_block_solves = on >= 3;
   return VPMG_OK;
 }
 

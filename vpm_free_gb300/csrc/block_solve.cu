@@ -1,0 +1,380 @@
+// block_solve.cu -- the padded YAPS block's infinite-domain solve, evaluated
+// only where the reference's step reads it.
+//
+// yaps3d (source/yaps3d.f90:52-53 -> pmlib.f90:115-154) solves the padded
+// block twice per component with the same right-hand side:
+//   1. zero boundary values (solve_eq_0_3d, pmsolve.f90:367-432), of which
+//      calc_normalderiv_3d (pinfdomain.f90:294-547) reads only the 4
+//      interior layers next to each face;
+//   2. the quadtree boundary values (solve_eq_3d, pmsolve.f90:284-365), of
+//      which the step reads only the every-nc-th samples
+//      (yaps3d.f90:104-138) and the six faces of the inner block box
+//      (interp_stencil targets, yaps3d.f90:340-395; final-solve boundary).
+// Both share the forward transform ghat = DST_y DST_x RHS: the boundary
+// values of solve 2 enter in transform space as rank-structured face terms
+// added inside the Thomas sweep.  The inverse transforms are evaluated only
+// on the needed layers: dot products with the selected sine rows along one
+// axis, then a full inverse DST along the other.  The values produced are
+// those of the full discrete solves (same linear algebra, different
+// rounding).
+#include <cmath>
+
+#include "block_solve.h"
+
+namespace vpmg {
+
+namespace {
+
+constexpr int kLines = 16;  // lines per CTA of the x dot-product kernel
+
+// out[i + nsel*(q + m1*kk)] = sum_p S[i][p] * W[p + m0*(q + m1*k)],  k = klist ? klist[kk] : kk
+__global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W, int m0, int m1, int nk,
+                                                   const int* __restrict__ klist, const double* __restrict__ S,
+                                                   int nsel, double* __restrict__ out) {
+  extern __shared__ double sm[];
+  double* tile = sm;                    // kLines x m0
+  double* Ss = sm + (size_t)kLines * m0;  // nsel x m0
+  const int nlines = m1 * nk;
+  const int l0 = blockIdx.x * kLines;
+  for (int t = threadIdx.x; t < nsel * m0; t += blockDim.x) Ss[t] = S[t];
+  for (int t = threadIdx.x; t < kLines * m0; t += blockDim.x) {
+    const int li = t / m0, p = t - li * m0;
+    const int l = l0 + li;
+    double v = 0.0;
+    if (l < nlines) {
+      const int q = l % m1, kk = l / m1;
+      const int k = klist ? klist[kk] : kk;
+      v = W[(size_t)p + (size_t)m0 * (q + (size_t)m1 * k)];
+    }
+    tile[t] = v;
+  }
+  __syncthreads();
+  for (int o = threadIdx.x; o < kLines * nsel; o += blockDim.x) {
+    const int li = o % kLines, i = o / kLines;
+    const int l = l0 + li;
+    if (l >= nlines) continue;
+    const double* a = tile + (size_t)li * m0;
+    const double* b = Ss + (size_t)i * m0;
+    double acc = 0.0;
+    for (int p = 0; p < m0; ++p) acc = fma(a[p], b[p], acc);
+    const int q = l % m1, kk = l / m1;
+    out[i + (size_t)nsel * (q + (size_t)m1 * kk)] = acc;
+  }
+}
+
+// out[p + m0*(j + nsel*kk)] = sum_q S[j][q] * W[p + m0*(q + m1*k)]
+__global__ void k_partial_y(const double* __restrict__ W, int m0, int m1, int nk, const int* __restrict__ klist,
+                            const double* __restrict__ S, int nsel, double* __restrict__ out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int kk = blockIdx.y;
+  if (p >= m0 || kk >= nk) return;
+  const int k = klist ? klist[kk] : kk;
+  const double* col = W + (size_t)p + (size_t)m0 * m1 * k;
+  for (int j0 = 0; j0 < nsel; j0 += 8) {
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int nj = min(8, nsel - j0);
+    for (int q = 0; q < m1; ++q) {
+      const double w = col[(size_t)m0 * q];
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj)
+        if (jj < nj) acc[jj] = fma(__ldg(&S[(size_t)(j0 + jj) * m1 + q]), w, acc[jj]);
+    }
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj)
+      if (jj < nj) out[(size_t)p + (size_t)m0 * ((j0 + jj) + (size_t)nsel * kk)] = acc[jj];
+  }
+}
+
+// dst node (ia[a], ib[b], ic[c]) <- src[a + na*(b + nb*c)]; a null list means identity + off.
+__global__ void k_scatter3(const double* __restrict__ src, int na, int nb, int nc, const int* __restrict__ ia,
+                           const int* __restrict__ ib, const int* __restrict__ ic, int off, double* __restrict__ dst,
+                           int dx, int dy) {
+  const size_t n = (size_t)na * nb * nc;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int a = (int)(t % na), b = (int)((t / na) % nb), c = (int)(t / ((size_t)na * nb));
+    const int i = ia ? ia[a] : a + off, j = ib ? ib[b] : b + off, k = ic ? ic[c] : c + off;
+    dst[(size_t)i + (size_t)dx * (j + (size_t)dy * k)] = src[t];
+  }
+}
+
+// Interior values of the six faces of the block: fx* [k][j], fy* [k][i], fz* [j][i].
+__global__ void k_extract_faces(const double* __restrict__ s, int NX, int NY, int NZ, double* __restrict__ fx0,
+                                double* __restrict__ fxN, double* __restrict__ fy0, double* __restrict__ fyN,
+                                double* __restrict__ fz0, double* __restrict__ fzN) {
+  const int m0 = NX - 2, m1 = NY - 2, m2 = NZ - 2;
+  const size_t sy = NX, sz = (size_t)NX * NY;
+  const long nx = (long)m1 * m2, ny = (long)m0 * m2, nz = (long)m0 * m1;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nx + ny + nz; t += (long)gridDim.x * blockDim.x) {
+    if (t < nx) {
+      const int j = (int)(t % m1) + 1, k = (int)(t / m1) + 1;
+      fx0[t] = s[sy * j + sz * k];
+      fxN[t] = s[(NX - 1) + sy * j + sz * k];
+    } else if (t < nx + ny) {
+      const long u = t - nx;
+      const int i = (int)(u % m0) + 1, k = (int)(u / m0) + 1;
+      fy0[u] = s[i + sz * k];
+      fyN[u] = s[i + sy * (NY - 1) + sz * k];
+    } else {
+      const long u = t - nx - ny;
+      const int i = (int)(u % m0) + 1, j = (int)(u / m0) + 1;
+      fz0[u] = s[i + sy * j];
+      fzN[u] = s[i + sy * j + sz * (NZ - 1)];
+    }
+  }
+}
+
+struct FaceTerms {
+  const double *fx0, *fxN, *fy0, *fyN, *fz0, *fzN;  // transforms: [k][q], [k][p], [q][p]
+  const double *ex1, *exN, *ey1, *eyN;              // sin(pi (p+1)/N), sin(pi m (p+1)/N)
+  double cx, cy, cz;                                // -scale / h^2
+};
+
+// Thomas sweep of -u[k-1] + d u[k] - u[k+1] = r[k] with the reciprocal pivot
+// table; r = ghat (+ the transformed Dirichlet face terms when bc).
+__global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict__ out, const double* __restrict__ rinv,
+                               int m0, int m1, int m2, int bc, FaceTerms F) {
+  const int pq = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pq >= m0 * m1) return;
+  const int p = pq % m0, q = pq / m0;
+  const size_t plane = (size_t)m0 * m1;
+  double ax = 0.0, bx = 0.0, ay = 0.0, by = 0.0;
+  if (bc) {
+    ax = F.cx * F.ex1[p];
+    bx = F.cx * F.exN[p];
+    ay = F.cy * F.ey1[q];
+    by = F.cy * F.eyN[q];
+  }
+  auto rhs = [&](int k) -> double {
+    double r = g[pq + plane * k];
+    if (bc) {
+      r += ax * F.fx0[(size_t)k * m1 + q] + bx * F.fxN[(size_t)k * m1 + q];
+      r += ay * F.fy0[(size_t)k * m0 + p] + by * F.fyN[(size_t)k * m0 + p];
+      if (k == 0) r += F.cz * F.fz0[pq];
+      if (k == m2 - 1) r += F.cz * F.fzN[pq];
+    }
+    return r;
+  };
+  double y = rhs(0);
+  out[pq] = y;
+  double ri = rinv[pq];
+  for (int k = 1; k < m2; ++k) {
+    const size_t id = pq + plane * k;
+    y = fma(y, ri, rhs(k));
+    out[id] = y;
+    ri = rinv[id];
+  }
+  double u = y * ri;
+  out[pq + plane * (m2 - 1)] = u;
+  for (int k = m2 - 2; k >= 0; --k) {
+    const size_t id = pq + plane * k;
+    u = (out[id] + u) * rinv[id];
+    out[id] = u;
+  }
+}
+
+std::vector<double> sine_rows(const std::vector<int>& sel, int m) {
+  std::vector<double> S(sel.size() * (size_t)m);
+  const double N = m + 1;
+  for (size_t i = 0; i < sel.size(); ++i)
+    for (int p = 0; p < m; ++p) S[i * m + p] = std::sin(kPI * (double)(sel[i] + 1) * (double)(p + 1) / N);
+  return S;
+}
+
+template <class T>
+void up(DBuf<T>& b, const std::vector<T>& h) {
+  b.ensure(std::max<size_t>(h.size(), 1));
+  if (!h.empty()) VPMG_CUDA(cudaMemcpy(b.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+}
+
+std::vector<int> plus1(const std::vector<int>& v) {
+  std::vector<int> r(v);
+  for (int& x : r) x += 1;
+  return r;
+}
+
+size_t g_partial_smem = 0;  // dynamic shared memory granted to k_partial_x so far
+
+// Raises k_partial_x's shared-memory limit (called at set-up, outside any
+// stream capture).
+void partial_x_reserve(int m0, int nsel) {
+  const size_t sm = sizeof(double) * ((size_t)kLines * m0 + (size_t)nsel * m0);
+  VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
+  if (sm > g_partial_smem) {
+    VPMG_CUDA(cudaFuncSetAttribute(k_partial_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    g_partial_smem = sm;
+  }
+}
+
+void partial_x(const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel, double* out,
+               cudaStream_t s) {
+  const int nlines = m1 * nk;
+  const size_t sm = sizeof(double) * ((size_t)kLines * m0 + (size_t)nsel * m0);
+  VPMG_CHECK(sm <= g_partial_smem, VPMG_ERR_STATE, "k_partial_x shared memory not reserved");
+  k_partial_x<<<(nlines + kLines - 1) / kLines, 128, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out);
+  VPMG_LAUNCHED();
+}
+
+void partial_y(const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel, double* out,
+               cudaStream_t s) {
+  dim3 g((m0 + 127) / 128, nk);
+  k_partial_y<<<g, 128, 0, s>>>(W, m0, m1, nk, klist, S, nsel, out);
+  VPMG_LAUNCHED();
+}
+
+void scatter3(const double* src, int na, int nb, int nc, const int* ia, const int* ib, const int* ic, int off,
+              double* dst, const int dims[3], cudaStream_t s) {
+  const size_t n = (size_t)na * nb * nc;
+  k_scatter3<<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(src, na, nb, nc, ia, ib, ic, off,
+                                                                                   dst, dims[0], dims[1]);
+  VPMG_LAUNCHED();
+}
+
+}  // namespace
+
+void BlockSolve::prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoarse) {
+  for (int d = 0; d < 3; ++d) { dims[d] = P.dims[d]; m[d] = P.m[d]; }
+  VPMG_CHECK(m[0] >= 8 && m[1] >= 8 && m[2] >= 8, VPMG_ERR_UNSUPPORTED, "block too small for the partial solve");
+  const size_t nint = (size_t)m[0] * m[1] * m[2];
+  ghat.ensure(3 * nint);
+  W.ensure(nint);
+  // normal-derivative layers: interior indices 0..3 and m-4..m-1
+  std::vector<int> fx = {0, 1, 2, 3, m[0] - 4, m[0] - 3, m[0] - 2, m[0] - 1};
+  std::vector<int> fylo = {0, 1, 2, 3}, fyhi = {m[1] - 4, m[1] - 3, m[1] - 2, m[1] - 1};
+  up(S_fx, sine_rows(fx, m[0]));
+  up(S_fy_lo, sine_rows(fylo, m[1]));
+  up(S_fy_hi, sine_rows(fyhi, m[1]));
+  up(l_fx, plus1(fx));
+  // inner-box faces: 1-based node nnbl_bl -> interior index nnbl_bl - 2
+  for (int d = 0; d < 3; ++d) {
+    inner_lo[d] = nnbl_bl[d] - 2;
+    inner_hi[d] = nnbl_bl[d + 3] - 2;
+    VPMG_CHECK(inner_lo[d] >= 0 && inner_hi[d] < m[d] && inner_lo[d] < inner_hi[d], VPMG_ERR_ARG,
+               "inner block box outside the padded block");
+  }
+  std::vector<int> ix = {inner_lo[0], inner_hi[0]};
+  up(S_ix, sine_rows(ix, m[0]));
+  up(S_iy_lo, sine_rows({inner_lo[1]}, m[1]));
+  up(S_iy_hi, sine_rows({inner_hi[1]}, m[1]));
+  up(l_ix, plus1(ix));
+  // samples: 0-based nodes nc*t inside the block interior -> interior index nc*t - 1
+  auto samples = [&](int d) {
+    std::vector<int> v;
+    for (int t = 1; ncoarse * t <= dims[d] - 2; ++t) v.push_back(ncoarse * t - 1);
+    return v;
+  };
+  std::vector<int> sx = samples(0), sy = samples(1), sz = samples(2);
+  nsx = (int)sx.size(); nsy = (int)sy.size(); nsz = (int)sz.size();
+  up(S_sx, sine_rows(sx, m[0]));
+  up(S_sy, sine_rows(sy, m[1]));
+  up(l_sx, plus1(sx));
+  up(l_sy, plus1(sy));
+  up(l_sz, sz);  // plane list (interior index) for the y dots
+  std::vector<int> idz(sz);
+  up(l_idz, plus1(idz));  // node list for the scatter
+  // first/last layer sines for the face terms
+  auto edge = [&](int mm, bool last) {
+    std::vector<double> e(mm);
+    const double N = mm + 1;
+    for (int p = 0; p < mm; ++p) e[p] = std::sin(kPI * (double)(last ? mm : 1) * (double)(p + 1) / N);
+    return e;
+  };
+  up(e_x1, edge(m[0], false)); up(e_xN, edge(m[0], true));
+  up(e_y1, edge(m[1], false)); up(e_yN, edge(m[1], true));
+  partial_x_reserve(m[0], std::max(8, nsx));
+  X8.ensure((size_t)8 * m[1] * m[2]);
+  Y4.ensure((size_t)m[0] * 4 * m[2]);
+  X2.ensure((size_t)2 * m[1] * m[2]);
+  Y1.ensure((size_t)m[0] * m[2]);
+  Ys.ensure((size_t)m[0] * nsy * nsz);
+  XS.ensure((size_t)nsx * nsy * nsz);
+  fx0.ensure((size_t)m[1] * m[2]); fxN.ensure((size_t)m[1] * m[2]);
+  fy0.ensure((size_t)m[0] * m[2]); fyN.ensure((size_t)m[0] * m[2]);
+  fz0.ensure((size_t)m[0] * m[1]); fzN.ensure((size_t)m[0] * m[1]);
+  ready = true;
+}
+
+void block_solve_zero_bc(BlockSolve& B, DirichletPlan& P, const double* rhs_c, int c, double* sol0, cudaStream_t s) {
+  const int m0 = B.m[0], m1 = B.m[1], m2 = B.m[2];
+  const size_t nint = (size_t)m0 * m1 * m2, plane = (size_t)m0 * m1;
+  double* g = B.ghat.p + (size_t)c * nint;
+  dst_forward_xy(P, rhs_c, nullptr, true, g, s);
+  FaceTerms F{};
+  k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(g, B.W.p, P.rinv.p, m0, m1, m2, 0, F);
+  VPMG_LAUNCHED();
+  // x faces: 8 layers by dot products along x, then inverse y
+  partial_x(B.W.p, m0, m1, m2, nullptr, B.S_fx.p, 8, B.X8.p, s);
+  dst_lines_y(P.fy, B.X8.p, 8, m1, m2, s);
+  scatter3(B.X8.p, 8, m1, m2, B.l_fx.p, nullptr, nullptr, 1, sol0, B.dims, s);
+  // y faces: 4 + 4 rows by dot products along y, then inverse x
+  const int my[3] = {m0, 4, m2};
+  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_fy_lo.p, 4, B.Y4.p, s);
+  const int olo[3] = {1, 1, 1};
+  dst_x_inv_to_box(P.fx, B.Y4.p, sol0, B.dims, olo, my, s);
+  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_fy_hi.p, 4, B.Y4.p, s);
+  const int ohi[3] = {1, 1 + m1 - 4, 1};
+  dst_x_inv_to_box(P.fx, B.Y4.p, sol0, B.dims, ohi, my, s);
+  // z faces: the first and last 4 planes, full inverse (in place on W, after the dots)
+  const int mz[3] = {m0, m1, 4};
+  dst_lines_y(P.fy, B.W.p, m0, m1, 4, s);
+  dst_x_inv_to_box(P.fx, B.W.p, sol0, B.dims, olo, mz, s);
+  double* top = B.W.p + plane * (m2 - 4);
+  dst_lines_y(P.fy, top, m0, m1, 4, s);
+  const int oz[3] = {1, 1, 1 + m2 - 4};
+  dst_x_inv_to_box(P.fx, top, sol0, B.dims, oz, mz, s);
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void block_solve_bc(BlockSolve& B, DirichletPlan& P, int c, double* sol_c, cudaStream_t s) {
+  const int m0 = B.m[0], m1 = B.m[1], m2 = B.m[2];
+  const size_t nint = (size_t)m0 * m1 * m2, plane = (size_t)m0 * m1;
+  // boundary values of the faces, transformed along the face's axes
+  k_extract_faces<<<256, 256, 0, s>>>(sol_c, B.dims[0], B.dims[1], B.dims[2], B.fx0.p, B.fxN.p, B.fy0.p, B.fyN.p,
+                                      B.fz0.p, B.fzN.p);
+  VPMG_LAUNCHED();
+  dst_lines_y(P.fy, B.fx0.p, 1, m1, m2, s);   // rows over j -> q
+  dst_lines_y(P.fy, B.fxN.p, 1, m1, m2, s);
+  dst_lines_y(P.fx, B.fy0.p, 1, m0, m2, s);   // rows over i -> p
+  dst_lines_y(P.fx, B.fyN.p, 1, m0, m2, s);
+  dst_lines_y(P.fx, B.fz0.p, 1, m0, m1, s);   // rows over i, then columns over j
+  dst_lines_y(P.fy, B.fz0.p, m0, m1, 1, s);
+  dst_lines_y(P.fx, B.fzN.p, 1, m0, m1, s);
+  dst_lines_y(P.fy, B.fzN.p, m0, m1, 1, s);
+  const double scale = dirichlet_scale(P);
+  FaceTerms F;
+  F.fx0 = B.fx0.p; F.fxN = B.fxN.p; F.fy0 = B.fy0.p; F.fyN = B.fyN.p; F.fz0 = B.fz0.p; F.fzN = B.fzN.p;
+  F.ex1 = B.e_x1.p; F.exN = B.e_xN.p; F.ey1 = B.e_y1.p; F.eyN = B.e_yN.p;
+  F.cx = -scale / (P.h[0] * P.h[0]);
+  F.cy = -scale / (P.h[1] * P.h[1]);
+  F.cz = -scale / (P.h[2] * P.h[2]);
+  const double* g = B.ghat.p + (size_t)c * nint;
+  k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(g, B.W.p, P.rinv.p, m0, m1, m2, 1, F);
+  VPMG_LAUNCHED();
+  // inner-box x faces
+  partial_x(B.W.p, m0, m1, m2, nullptr, B.S_ix.p, 2, B.X2.p, s);
+  dst_lines_y(P.fy, B.X2.p, 2, m1, m2, s);
+  scatter3(B.X2.p, 2, m1, m2, B.l_ix.p, nullptr, nullptr, 1, sol_c, B.dims, s);
+  // inner-box y faces
+  const int m1r[3] = {m0, 1, m2};
+  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_iy_lo.p, 1, B.Y1.p, s);
+  const int oylo[3] = {1, B.inner_lo[1] + 1, 1};
+  dst_x_inv_to_box(P.fx, B.Y1.p, sol_c, B.dims, oylo, m1r, s);
+  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_iy_hi.p, 1, B.Y1.p, s);
+  const int oyhi[3] = {1, B.inner_hi[1] + 1, 1};
+  dst_x_inv_to_box(P.fx, B.Y1.p, sol_c, B.dims, oyhi, m1r, s);
+  // interior samples: dots along y on the sampled planes, then along x
+  partial_y(B.W.p, m0, m1, B.nsz, B.l_sz.p, B.S_sy.p, B.nsy, B.Ys.p, s);
+  partial_x(B.Ys.p, m0, B.nsy, B.nsz, nullptr, B.S_sx.p, B.nsx, B.XS.p, s);
+  scatter3(B.XS.p, B.nsx, B.nsy, B.nsz, B.l_sx.p, B.l_sy.p, B.l_idz.p, 0, sol_c, B.dims, s);
+  // inner-box z faces: full inverse of the two planes (in place, after the dots)
+  const int mz1[3] = {m0, m1, 1};
+  const int kz[2] = {B.inner_lo[2], B.inner_hi[2]};
+  for (int t = 0; t < 2; ++t) {
+    double* pl = B.W.p + plane * kz[t];
+    dst_lines_y(P.fy, pl, m0, m1, 1, s);
+    const int oz[3] = {1, 1, kz[t] + 1};
+    dst_x_inv_to_box(P.fx, pl, sol_c, B.dims, oz, mz1, s);
+  }
+  VPMG_CUDA(cudaGetLastError());
+}
+
+}  // namespace vpmg

@@ -45,10 +45,11 @@ __device__ __forceinline__ double proj_fun(int itype, double x) {
 // Cell index exactly as int((x - XMIN)/DX) (IEEE division, truncation).
 __device__ __forceinline__ int cell_of(double x, double xmin, double d) { return (int)__ddiv_rn(__dsub_rn(x, xmin), d); }
 
-__global__ void k_keys(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z, int np,
-                       MeshDev m, int* __restrict__ key, int* __restrict__ counts, int* __restrict__ err) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np) return;
+__global__ void k_keys(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
+                       const int* __restrict__ np_dev, MeshDev m, int* __restrict__ key, int* __restrict__ counts,
+                       int* __restrict__ err) {
+  const int np = *np_dev;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
   const int i0 = cell_of(x[p], m.xmin[0], m.d[0]);
   const int j0 = cell_of(y[p], m.xmin[1], m.d[1]);
   const int k0 = cell_of(z[p], m.xmin[2], m.d[2]);
@@ -59,21 +60,23 @@ __global__ void k_keys(const double* __restrict__ x, const double* __restrict__ 
   if (!ok) {
     key[p] = -1;
     atomicExch(err, 1);
-    return;
+    continue;
   }
   const int kk = i0 + m.n[0] * (j0 + m.n[1] * k0);
   key[p] = kk;
   atomicAdd(&counts[kk], 1);
+  }
 }
 
-__global__ void k_scatter(const int* __restrict__ key, int np, const int* __restrict__ starts, int* __restrict__ cursor,
-                          int* __restrict__ perm) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np) return;
-  const int kk = key[p];
-  if (kk < 0) return;
-  const int slot = starts[kk] + atomicAdd(&cursor[kk], 1);
-  perm[slot] = p;
+__global__ void k_scatter(const int* __restrict__ key, const int* __restrict__ np_dev, const int* __restrict__ starts,
+                          int* __restrict__ cursor, int* __restrict__ perm) {
+  const int np = *np_dev;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    const int kk = key[p];
+    if (kk < 0) continue;
+    const int slot = starts[kk] + atomicAdd(&cursor[kk], 1);
+    perm[slot] = p;
+  }
 }
 
 // Restores particle-index order inside each cell (determinism).
@@ -96,9 +99,10 @@ __global__ void k_cell_order(const int* __restrict__ starts, int ncell, int* __r
 // Sorted records: per slot 4+4+4 stencil weights, 3 strengths, base cell x.
 __global__ void k_records(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
                           const double* __restrict__ q0, const double* __restrict__ q1, const double* __restrict__ q2,
-                          const int* __restrict__ perm, int nsorted, MeshDev m, double* __restrict__ rec) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsorted) return;
+                          const int* __restrict__ perm, const int* __restrict__ nsorted_dev, MeshDev m,
+                          double* __restrict__ rec) {
+  const int nsorted = *nsorted_dev;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
   const int p = perm[s];
   const double pos[3] = {x[p], y[p], z[p]};
   double* r = rec + (size_t)s * kRecLen;
@@ -117,6 +121,7 @@ __global__ void k_records(const double* __restrict__ x, const double* __restrict
   r[12] = q0[p];
   r[13] = q1[p];
   r[14] = q2[p];
+  }
 }
 
 // One thread per node: gathers the particles of the (ips+ipf+1)^3 cells
@@ -157,14 +162,15 @@ __global__ void k_deposit(const int* __restrict__ starts, const double* __restri
 
 // M2P over sorted slots: UP = sum W vel, GP = (sum W def) * vol; optionally
 // the forward Euler push.
-__global__ void k_m2p(const int* __restrict__ perm, int nsorted, const double* __restrict__ rec, MeshDev m,
+__global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsorted_dev, const double* __restrict__ rec,
+                      MeshDev m,
                       const double* __restrict__ v0, const double* __restrict__ v1, const double* __restrict__ v2,
                       const double* __restrict__ g0, const double* __restrict__ g1, const double* __restrict__ g2,
                       double* __restrict__ up, double* __restrict__ gp, double* __restrict__ x, double* __restrict__ y,
                       double* __restrict__ z, double* __restrict__ q0, double* __restrict__ q1, double* __restrict__ q2,
                       const double* __restrict__ vol, int do_euler, double dt, double ux, double uy, double uz) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsorted) return;
+  const int nsorted = *nsorted_dev;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
   const int p = perm[s];
   const double* r = rec + (size_t)s * kRecLen;
   double w[12];
@@ -211,6 +217,7 @@ __global__ void k_m2p(const int* __restrict__ perm, int nsorted, const double* _
     q1[p] = q1[p] - gg1 * dt;
     q2[p] = q2[p] - gg2 * dt;
   }
+  }
 }
 
 // Remesh: flag nodes inside [lo, hi] (0-based, per axis) with |w| >= thr.
@@ -256,6 +263,21 @@ __global__ void k_remesh_emit(const double* __restrict__ r0, const double* __res
 
 __global__ void k_set_total(int* __restrict__ dst, const int* __restrict__ src) { *dst = *src; }
 
+// New particle count of a remesh, clamped to the capacity (overflow -> error 2).
+__global__ void k_set_count(int* __restrict__ np, const int* __restrict__ total, int capacity, int* __restrict__ err) {
+  const int t = *total;
+  if (t > capacity) {
+    *np = capacity;
+    atomicExch(err, 2);
+  } else {
+    *np = t;
+  }
+}
+
+unsigned stride_grid(int capacity, int threads) {
+  return (unsigned)std::max(1, std::min((capacity + threads - 1) / threads, 152 * 32));
+}
+
 }  // namespace
 
 void Particles::ensure(int cap) {
@@ -265,6 +287,7 @@ void Particles::ensure(int cap) {
   up.ensure(3 * (size_t)cap); gp.ensure(3 * (size_t)cap);
   key.ensure(cap); perm.ensure(cap);
   rec.ensure((size_t)kRecLen * cap);
+  d_np.ensure(1);
   capacity = cap;
 }
 
@@ -274,43 +297,52 @@ void Binning::ensure(size_t ncell) {
   cursor.ensure(ncell);
   sums.ensure(scan_block_sums_needed(ncell) + 1);
   err.ensure(1);
+  VPMG_CUDA(cudaMemset(err.p, 0, sizeof(int)));
   ncells = ncell;
 }
 
-// Sort + records.  Returns the number of sorted (in-mesh) particles.
-void bin_particles(Particles& P, int np, const MeshDev& m, Binning& B, cudaStream_t s) {
+// Sort by cell + records, all on the stream (no host round trip): the
+// particle count is read from P.d_np, the sorted count lands in starts[N].
+// Errors (stencil outside the mesh = 1, remesh overflow = 2) accumulate in
+// B.err and are reported by check_particle_errors at the next host sync.
+void bin_particles(Particles& P, const MeshDev& m, Binning& B, cudaStream_t s) {
   const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
   B.ensure(N);
   VPMG_CUDA(cudaMemsetAsync(B.cursor.p, 0, sizeof(int) * N, s));
-  VPMG_CUDA(cudaMemsetAsync(B.err.p, 0, sizeof(int), s));
-  if (np > 0) {
-    k_keys<<<(np + 255) / 256, 256, 0, s>>>(P.x.p, P.y.p, P.z.p, np, m, P.key.p, B.cursor.p, B.err.p);
-    VPMG_LAUNCHED();
-  }
+  k_keys<<<stride_grid(P.capacity, 256), 256, 0, s>>>(P.x.p, P.y.p, P.z.p, P.d_np.p, m, P.key.p, B.cursor.p, B.err.p);
+  VPMG_LAUNCHED();
   VPMG_CUDA(cudaMemsetAsync(B.sums.p, 0, sizeof(int) * B.sums.n, s));
   exclusive_scan_int(B.cursor.p, B.starts.p, N, B.sums.p, s);
   const int nt = (int)scan_block_sums_needed(N) - 1;
   k_set_total<<<1, 1, 0, s>>>(B.starts.p + N, B.sums.p + nt);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaMemsetAsync(B.cursor.p, 0, sizeof(int) * N, s));
-  if (np > 0) {
-    k_scatter<<<(np + 255) / 256, 256, 0, s>>>(P.key.p, np, B.starts.p, B.cursor.p, P.perm.p);
-    VPMG_LAUNCHED();
-  }
+  k_scatter<<<stride_grid(P.capacity, 256), 256, 0, s>>>(P.key.p, P.d_np.p, B.starts.p, B.cursor.p, P.perm.p);
+  VPMG_LAUNCHED();
   k_cell_order<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(B.starts.p, (int)N, P.perm.p);
   VPMG_LAUNCHED();
-  int h[2] = {0, 0};
-  VPMG_CUDA(cudaMemcpyAsync(&h[0], B.starts.p + N, sizeof(int), cudaMemcpyDeviceToHost, s));
-  VPMG_CUDA(cudaMemcpyAsync(&h[1], B.err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  VPMG_CUDA(cudaStreamSynchronize(s));
-  B.nsorted = h[0];
-  VPMG_CHECK(h[1] == 0, VPMG_ERR_OUTSIDE, "a particle's projection stencil leaves the mesh");
-  if (B.nsorted > 0) {
-    k_records<<<(B.nsorted + 255) / 256, 256, 0, s>>>(P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.perm.p, B.nsorted,
-                                                     m, P.rec.p);
-    VPMG_LAUNCHED();
-  }
+  B.nsorted_dev = B.starts.p + N;
+  k_records<<<stride_grid(P.capacity, 256), 256, 0, s>>>(P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.perm.p,
+                                                         B.nsorted_dev, m, P.rec.p);
+  VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
+}
+
+void check_particle_errors(Binning& B, cudaStream_t s) {
+  if (!B.err.p) return;
+  int e = 0;
+  VPMG_CUDA(cudaMemcpyAsync(&e, B.err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  if (e) VPMG_CUDA(cudaMemsetAsync(B.err.p, 0, sizeof(int), s));
+  VPMG_CHECK(e != 1, VPMG_ERR_OUTSIDE, "a particle's projection stencil leaves the mesh");
+  VPMG_CHECK(e != 2, VPMG_ERR_CAPACITY, "remesh produced more particles than the capacity");
+}
+
+int read_count(const int* d, cudaStream_t s) {
+  int v = 0;
+  VPMG_CUDA(cudaMemcpyAsync(&v, d, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  return v;
 }
 
 void deposit(const Particles& P, const MeshDev& m, const Binning& B, double* const rhs[3], cudaStream_t s) {
@@ -323,16 +355,18 @@ void deposit(const Particles& P, const MeshDev& m, const Binning& B, double* con
 
 void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const vel[3], const double* const def[3],
          bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s) {
-  if (B.nsorted <= 0) return;
-  k_m2p<<<(B.nsorted + 127) / 128, 128, 0, s>>>(P.perm.p, B.nsorted, P.rec.p, m, vel[0], vel[1], vel[2], def[0], def[1],
-                                               def[2], write_up ? P.up.p : nullptr, P.gp.p, P.x.p, P.y.p, P.z.p, P.q0.p,
-                                               P.q1.p, P.q2.p, P.vol.p, euler ? 1 : 0, dt, uinf[0], uinf[1], uinf[2]);
+  k_m2p<<<stride_grid(P.capacity, 128), 128, 0, s>>>(P.perm.p, B.nsorted_dev, P.rec.p, m, vel[0], vel[1], vel[2],
+                                                      def[0], def[1], def[2], write_up ? P.up.p : nullptr, P.gp.p,
+                                                      P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.vol.p,
+                                                      euler ? 1 : 0, dt, uinf[0], uinf[1], uinf[2]);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
 
-int remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3], const int hi[3],
-                double thr, int capacity, cudaStream_t s) {
+// Ordered compaction of the flagged nodes; the new count goes to P.d_np
+// (clamped to the capacity, overflow flagged in B.err), on the stream.
+void remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3],
+                 const int hi[3], double thr, cudaStream_t s) {
   const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
   B.ensure(N);
   const double dv = m.d[0] * m.d[1] * m.d[2];
@@ -342,15 +376,13 @@ int remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const 
   VPMG_CUDA(cudaMemsetAsync(B.sums.p, 0, sizeof(int) * B.sums.n, s));
   exclusive_scan_int(B.cursor.p, B.starts.p, N, B.sums.p, s);
   const int nt = (int)scan_block_sums_needed(N) - 1;
-  int total = 0;
-  VPMG_CUDA(cudaMemcpyAsync(&total, B.sums.p + nt, sizeof(int), cudaMemcpyDeviceToHost, s));
   k_remesh_emit<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], B.cursor.p, B.starts.p, m, dv,
-                                                             capacity, P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p,
+                                                             P.capacity, P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p,
                                                              P.vol.p);
   VPMG_LAUNCHED();
-  VPMG_CUDA(cudaStreamSynchronize(s));
+  k_set_count<<<1, 1, 0, s>>>(P.d_np.p, B.sums.p + nt, P.capacity, B.err.p);
+  VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
-  return total;
 }
 
 }  // namespace vpmg

@@ -1,5 +1,7 @@
 // particles.h -- device particle storage and the particle/mesh kernels.
 #pragma once
+#include <algorithm>
+
 #include "vpmg_internal.h"
 
 namespace vpmg {
@@ -19,21 +21,26 @@ struct Particles {
   DBuf<double> up, gp;                    // (3, cap) AoS like UP/GP
   DBuf<int> key, perm;
   DBuf<double> rec;                       // kRecLen per sorted slot
+  DBuf<int> d_np;                         // particle count, on the device
   void ensure(int cap);
 };
 
 struct Binning {
   size_t ncells = 0;
   DBuf<int> starts, cursor, sums, err;
-  int nsorted = 0;
+  const int* nsorted_dev = nullptr;       // starts[N] after bin_particles
   void ensure(size_t ncell);
 };
 
-void bin_particles(Particles& P, int np, const MeshDev& m, Binning& B, cudaStream_t s);
+// All of these only enqueue work on the stream (no host round trip).
+void bin_particles(Particles& P, const MeshDev& m, Binning& B, cudaStream_t s);
 void deposit(const Particles& P, const MeshDev& m, const Binning& B, double* const rhs[3], cudaStream_t s);
 void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const vel[3], const double* const def[3],
          bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s);
-int remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3], const int hi[3],
-                double thr, int capacity, cudaStream_t s);
+void remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3],
+                 const int hi[3], double thr, cudaStream_t s);
+// Host sync points.
+void check_particle_errors(Binning& B, cudaStream_t s);
+int read_count(const int* d, cudaStream_t s);
 
 }  // namespace vpmg

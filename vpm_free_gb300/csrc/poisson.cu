@@ -15,7 +15,8 @@
 //      divisions per step);
 //   4. inverse y and x passes (DST-I is its own inverse up to 2/N).
 // FFTs run in shared memory as mixed-radix Stockham stages (radix 2,4,8
-// and odd primes up to 31 through the symmetric direct DFT).
+// and odd primes up to 17 through the symmetric direct DFT), instantiated
+// twice: power-of-two radices only, and with the odd radices.
 #include <algorithm>
 #include <cmath>
 
@@ -27,7 +28,7 @@ namespace {
 
 constexpr int kPairs = 4;         // line pairs (8 real lines) per CTA
 constexpr int kThreads = 128;
-constexpr int kMaxOddRadix = 31;
+constexpr int kMaxOddRadix = 17;  // largest odd prime radix (2*(cells) must factor into 2..17)
 
 __constant__ double c_rcos[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
 __constant__ double c_rsin[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
@@ -35,6 +36,7 @@ bool g_tables_ready = false;
 
 struct FFTDev {
   int n, N, M, nst;
+  int odd;  // 1 if a stage has an odd radix
   int radix[24];
   const double2* tw;
 };
@@ -155,26 +157,32 @@ __device__ __forceinline__ void stage(const double2* __restrict__ in, double2* _
   }
 }
 
-// Runs all stages; returns the buffer holding the result.
+// Runs all stages; returns the buffer holding the result.  ODD = false
+// instantiates only the power-of-two radices, which keeps the register
+// count (and so the occupancy) of those kernels independent of the large
+// odd-radix butterflies.
+template <bool ODD>
 __device__ double2* fft_all(double2* A, double2* B, const FFTDev& p, int npair) {
   int Ns = 1;
   for (int s = 0; s < p.nst; ++s) {
     const int r = p.radix[s];
     switch (r) {
       case 2: stage<2>(A, B, p.M, Ns, p.tw, npair); break;
-      case 3: stage<3>(A, B, p.M, Ns, p.tw, npair); break;
       case 4: stage<4>(A, B, p.M, Ns, p.tw, npair); break;
-      case 5: stage<5>(A, B, p.M, Ns, p.tw, npair); break;
-      case 7: stage<7>(A, B, p.M, Ns, p.tw, npair); break;
       case 8: stage<8>(A, B, p.M, Ns, p.tw, npair); break;
-      case 11: stage<11>(A, B, p.M, Ns, p.tw, npair); break;
-      case 13: stage<13>(A, B, p.M, Ns, p.tw, npair); break;
-      case 17: stage<17>(A, B, p.M, Ns, p.tw, npair); break;
-      case 19: stage<19>(A, B, p.M, Ns, p.tw, npair); break;
-      case 23: stage<23>(A, B, p.M, Ns, p.tw, npair); break;
-      case 29: stage<29>(A, B, p.M, Ns, p.tw, npair); break;
-      case 31: stage<31>(A, B, p.M, Ns, p.tw, npair); break;
-      default: break;
+      default:
+        if constexpr (ODD) {
+          switch (r) {
+            case 3: stage<3>(A, B, p.M, Ns, p.tw, npair); break;
+            case 5: stage<5>(A, B, p.M, Ns, p.tw, npair); break;
+            case 7: stage<7>(A, B, p.M, Ns, p.tw, npair); break;
+            case 11: stage<11>(A, B, p.M, Ns, p.tw, npair); break;
+            case 13: stage<13>(A, B, p.M, Ns, p.tw, npair); break;
+            case 17: stage<17>(A, B, p.M, Ns, p.tw, npair); break;
+            default: break;
+          }
+        }
+        break;
     }
     __syncthreads();
     Ns *= r;
@@ -208,6 +216,7 @@ struct Box {
 };
 
 // x pass, forward: rhs (+ folded boundary values) -> work, scaled.
+template <bool ODD>
 __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict__ rhs, const double* __restrict__ sol,
                                                         int zero_bc, double* __restrict__ work, Box b, FFTDev p,
                                                         double ihx2, double ihy2, double ihz2, double scale) {
@@ -242,7 +251,7 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict
   __syncthreads();
   odd_extend(A, p, kPairs);
   __syncthreads();
-  double2* R = fft_all(A, B, p, kPairs);
+  double2* R = fft_all<ODD>(A, B, p, kPairs);
   for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
     const int l = l0 + li;
@@ -253,6 +262,7 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict
 }
 
 // y pass (forward or inverse): in place on work (m0 x m1 x m2, x fastest).
+template <bool ODD>
 __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, int m0, int m1, int m2, FFTDev p) {
   extern __shared__ double2 smem[];
   double2* A = smem;
@@ -275,7 +285,7 @@ __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, i
   __syncthreads();
   odd_extend(A, p, kPairs);
   __syncthreads();
-  double2* R = fft_all(A, B, p, kPairs);
+  double2* R = fft_all<ODD>(A, B, p, kPairs);
   for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
     const int li = t % (2 * kPairs), k = t / (2 * kPairs);
     const int l = l0 + li;
@@ -287,6 +297,7 @@ __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, i
 }
 
 // x pass, inverse: work -> interior of sol.
+template <bool ODD>
 __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict__ work, double* __restrict__ sol, Box b,
                                                         FFTDev p) {
   extern __shared__ double2 smem[];
@@ -305,7 +316,7 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict
   __syncthreads();
   odd_extend(A, p, kPairs);
   __syncthreads();
-  double2* R = fft_all(A, B, p, kPairs);
+  double2* R = fft_all<ODD>(A, B, p, kPairs);
   const size_t sy = b.dims[0], sz = (size_t)b.dims[0] * b.dims[1];
   for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
@@ -380,10 +391,40 @@ __global__ void k_zero_box_faces(double* __restrict__ sol, Box b) {
   }
 }
 
+// Launches picking the instantiation that the plan's radices need.
+void launch_x_fwd(dim3 g, int t, size_t sm, cudaStream_t s, const double* rhs, const double* sol, int zbc,
+                  double* work, Box b, FFTDev p, double ihx2, double ihy2, double ihz2, double scale) {
+  if (p.odd) k_dst_x_fwd<true><<<g, t, sm, s>>>(rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+  else k_dst_x_fwd<false><<<g, t, sm, s>>>(rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+}
+void launch_y(dim3 g, int t, size_t sm, cudaStream_t s, double* work, int m0, int m1, int m2, FFTDev p) {
+  if (p.odd) k_dst_y<true><<<g, t, sm, s>>>(work, m0, m1, m2, p);
+  else k_dst_y<false><<<g, t, sm, s>>>(work, m0, m1, m2, p);
+}
+void launch_x_inv(dim3 g, int t, size_t sm, cudaStream_t s, const double* work, double* sol, Box b, FFTDev p) {
+  if (p.odd) k_dst_x_inv<true><<<g, t, sm, s>>>(work, sol, b, p);
+  else k_dst_x_inv<false><<<g, t, sm, s>>>(work, sol, b, p);
+}
+cudaError_t set_dst_smem(int smax) {
+  cudaError_t e = cudaSuccess;
+  const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_fwd<true>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_fwd<false>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y<true>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y<false>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<true>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<false>, a, smax);
+  return e;
+}
+
 FFTDev dev_plan(const FFTPlan& p) {
   FFTDev d;
   d.n = p.n; d.N = p.N; d.M = p.M; d.nst = p.nst;
-  for (int i = 0; i < 24; ++i) d.radix[i] = p.radix[i];
+  d.odd = 0;
+  for (int i = 0; i < 24; ++i) {
+    d.radix[i] = p.radix[i];
+    if (i < p.nst && (p.radix[i] & 1)) d.odd = 1;
+  }
   d.tw = p.tw.p;
   return d;
 }
@@ -419,7 +460,7 @@ void make_fft_plan(FFTPlan& p, int n) {
   std::sort(odd.begin(), odd.end(), [](int a, int b) { return a > b; });
   p.nst = 0;
   for (int f : odd) {
-    VPMG_CHECK(f <= kMaxOddRadix, VPMG_ERR_UNSUPPORTED, "mesh size has a prime factor > 31 in 2*(cells)");
+    VPMG_CHECK(f <= kMaxOddRadix, VPMG_ERR_UNSUPPORTED, "mesh size has a prime factor > 17 in 2*(cells)");
     p.radix[p.nst++] = f;
   }
   while (twos >= 3) { p.radix[p.nst++] = 8; twos -= 3; }
@@ -453,9 +494,7 @@ void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], co
   // The attribute is per kernel (not per plan): only ever raise it.
   static int s_smem_set = 0;
   if ((int)smax > s_smem_set) {
-    VPMG_CUDA(cudaFuncSetAttribute(k_dst_x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
-    VPMG_CUDA(cudaFuncSetAttribute(k_dst_x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
-    VPMG_CUDA(cudaFuncSetAttribute(k_dst_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+    VPMG_CUDA(set_dst_smem((int)smax));
     s_smem_set = (int)smax;
   }
   // eigenvalues mu_p = 4 sin^2(pi p / 2N), pivots for d = 2 + hz^2 (mu_p/hx^2 + mu_q/hy^2)
@@ -487,18 +526,67 @@ void dirichlet_solve(DirichletPlan& P, const double* rhs, double* sol, bool zero
   const double scale = -hz2 * 4.0 / ((double)(P.m[0] + 1) * (double)(P.m[1] + 1));
   const int lx = P.m[1] * P.m[2], ly = P.m[0] * P.m[2];
   const int gx = (lx + 2 * kPairs - 1) / (2 * kPairs), gy = (ly + 2 * kPairs - 1) / (2 * kPairs);
-  k_dst_x_fwd<<<gx, kThreads, smem_bytes(P.fx), s>>>(rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2,
+  launch_x_fwd(gx, kThreads, smem_bytes(P.fx), s, rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2,
                                                      1.0 / hz2, scale);
-  k_dst_y<<<gy, kThreads, smem_bytes(P.fy), s>>>(work, P.m[0], P.m[1], P.m[2], py);
+  launch_y(gy, kThreads, smem_bytes(P.fy), s, work, P.m[0], P.m[1], P.m[2], py);
   const int nl = P.m[0] * P.m[1];
   k_thomas<<<(nl + 127) / 128, 128, 0, s>>>(work, P.rinv.p, P.m[0], P.m[1], P.m[2]);
-  k_dst_y<<<gy, kThreads, smem_bytes(P.fy), s>>>(work, P.m[0], P.m[1], P.m[2], py);
-  k_dst_x_inv<<<gx, kThreads, smem_bytes(P.fx), s>>>(work, sol, b, px);
+  launch_y(gy, kThreads, smem_bytes(P.fy), s, work, P.m[0], P.m[1], P.m[2], py);
+  launch_x_inv(gx, kThreads, smem_bytes(P.fx), s, work, sol, b, px);
   count_launch(5);
   if (zero_bc) {
     k_zero_box_faces<<<256, 256, 0, s>>>(sol, b);
     VPMG_LAUNCHED();
   }
+  VPMG_CUDA(cudaGetLastError());
+}
+
+// ----------------------------- pieces of a partially evaluated solve ----
+// Forward x and y passes only: ghat = scale * DST_y DST_x (rhs - folded
+// boundary values), the input of the Thomas sweep.
+void dst_forward_xy(DirichletPlan& P, const double* rhs, const double* sol, bool zero_bc, double* ghat,
+                    cudaStream_t s) {
+  Box b;
+  for (int d = 0; d < 3; ++d) { b.dims[d] = P.dims[d]; b.o[d] = P.box[d] + 1; b.m[d] = P.m[d]; }
+  const FFTDev px = dev_plan(P.fx), py = dev_plan(P.fy);
+  const double hx2 = P.h[0] * P.h[0], hy2 = P.h[1] * P.h[1], hz2 = P.h[2] * P.h[2];
+  const double scale = dirichlet_scale(P);
+  const int lx = P.m[1] * P.m[2], ly = P.m[0] * P.m[2];
+  const int gx = (lx + 2 * kPairs - 1) / (2 * kPairs), gy = (ly + 2 * kPairs - 1) / (2 * kPairs);
+  launch_x_fwd(gx, kThreads, smem_bytes(P.fx), s, rhs, sol, zero_bc ? 1 : 0, ghat, b, px, 1.0 / hx2, 1.0 / hy2,
+                                                     1.0 / hz2, scale);
+  launch_y(gy, kThreads, smem_bytes(P.fy), s, ghat, P.m[0], P.m[1], P.m[2], py);
+  count_launch(2);
+  VPMG_CUDA(cudaGetLastError());
+}
+
+double dirichlet_scale(const DirichletPlan& P) {
+  const double hz2 = P.h[2] * P.h[2];
+  return -hz2 * 4.0 / ((double)(P.m[0] + 1) * (double)(P.m[1] + 1));
+}
+
+// In-place DST-I along the middle axis of an m0 x m1 x m2 array (m1 = p.n).
+// With m0 = 1 it transforms contiguous rows.
+void dst_lines_y(const FFTPlan& p, double* data, int m0, int m1, int m2, cudaStream_t s) {
+  if (m0 <= 0 || m2 <= 0) return;
+  VPMG_CHECK(m1 == p.n, VPMG_ERR_ARG, "dst_lines_y: line length differs from the plan");
+  const int ly = m0 * m2;
+  launch_y((ly + 2 * kPairs - 1) / (2 * kPairs), kThreads, smem_bytes(p), s, data, m0, m1, m2, dev_plan(p));
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+// Inverse DST-I along x of the m[0] x m[1] x m[2] array `data`; line (q, c)
+// lands on nodes (o0 + k, o1 + q, o2 + c) of the node array sol (dims).
+void dst_x_inv_to_box(const FFTPlan& p, const double* data, double* sol, const int dims[3], const int o[3],
+                      const int m[3], cudaStream_t s) {
+  if (m[1] <= 0 || m[2] <= 0) return;
+  VPMG_CHECK(m[0] == p.n, VPMG_ERR_ARG, "dst_x_inv_to_box: line length differs from the plan");
+  Box b;
+  for (int d = 0; d < 3; ++d) { b.dims[d] = dims[d]; b.o[d] = o[d]; b.m[d] = m[d]; }
+  const int lx = m[1] * m[2];
+  launch_x_inv((lx + 2 * kPairs - 1) / (2 * kPairs), kThreads, smem_bytes(p), s, data, sol, b, dev_plan(p));
+  VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
 
@@ -559,6 +647,7 @@ bool static_plan(int n, const double2* tw, FFTDev& d) {
       m /= f;
     }
   d.nst = 0;
+  d.odd = no > 0 ? 1 : 0;
   for (int i = no - 1; i >= 0; --i) d.radix[d.nst++] = odd[i];  // largest first
   while (twos >= 3) { if (d.nst >= 24) return false; d.radix[d.nst++] = 8; twos -= 3; }
   if (twos == 2 && d.nst < 24) d.radix[d.nst++] = 4;
@@ -623,9 +712,7 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
   const int smax = 2 * kPairs * std::max(px.M, py.M) * (int)sizeof(double2);
   if (smax > 227 * 1024) return VPMG_ERR_UNSUPPORTED;
   if (smax > g_static_smem[dev]) {
-    if (cudaFuncSetAttribute(k_dst_x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess ||
-        cudaFuncSetAttribute(k_dst_x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess ||
-        cudaFuncSetAttribute(k_dst_y, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess) {
+    if (set_dst_smem(smax) != cudaSuccess) {
       cudaGetLastError();
       return VPMG_ERR_CUDA;
     }
@@ -645,11 +732,11 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
   const int lx = m[1] * m[2], ly = m[0] * m[2];
   const int gx = (lx + 2 * kPairs - 1) / (2 * kPairs), gy = (ly + 2 * kPairs - 1) / (2 * kPairs);
   const size_t shx = (size_t)2 * kPairs * px.M * sizeof(double2), shy = (size_t)2 * kPairs * py.M * sizeof(double2);
-  k_dst_x_fwd<<<gx, kThreads, shx, s>>>(rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2, 1.0 / hz2, scale);
-  k_dst_y<<<gy, kThreads, shy, s>>>(work, m[0], m[1], m[2], py);
+  launch_x_fwd(gx, kThreads, shx, s, rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2, 1.0 / hz2, scale);
+  launch_y(gy, kThreads, shy, s, work, m[0], m[1], m[2], py);
   k_thomas<<<(nl + 127) / 128, 128, 0, s>>>(work, rinv, m[0], m[1], m[2]);
-  k_dst_y<<<gy, kThreads, shy, s>>>(work, m[0], m[1], m[2], py);
-  k_dst_x_inv<<<gx, kThreads, shx, s>>>(work, sol, b, px);
+  launch_y(gy, kThreads, shy, s, work, m[0], m[1], m[2], py);
+  launch_x_inv(gx, kThreads, shx, s, work, sol, b, px);
   if (zero_bc) k_zero_box_faces<<<256, 256, 0, s>>>(sol, b);
   if (cudaGetLastError() != cudaSuccess) return VPMG_ERR_CUDA;
   return VPMG_OK;

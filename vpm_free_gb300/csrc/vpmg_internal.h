@@ -99,6 +99,13 @@ void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], co
 // boundary values (zero_bc = false) or zero (true; then the box faces of
 // sol are zeroed).  work: >= m0*m1*m2 doubles.
 void dirichlet_solve(DirichletPlan& P, const double* rhs, double* sol, bool zero_bc, double* work, cudaStream_t s);
+// Pieces of a partially evaluated solve (block_solve.cu).
+double dirichlet_scale(const DirichletPlan& P);  // factor applied in the forward x pass
+void dst_forward_xy(DirichletPlan& P, const double* rhs, const double* sol, bool zero_bc, double* ghat,
+                    cudaStream_t s);
+void dst_lines_y(const FFTPlan& p, double* data, int m0, int m1, int m2, cudaStream_t s);
+void dst_x_inv_to_box(const FFTPlan& p, const double* data, double* sol, const int dims[3], const int o[3],
+                      const int m[3], cudaStream_t s);
 
 // ------------------------------------------------- boundary operator ----
 struct TreeGeom;  // host-built quadtree of one grid (tree_host.cpp)

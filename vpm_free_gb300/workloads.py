@@ -92,3 +92,35 @@ def scaled_ring(n_cells, seed=7):
     h = 2 * L / n_cells
     xp, qp = _ring_particles(1.0, 0.15, 1.0, (0.0, 0.0, 0.0), (0, 0, 1), (h,) * 3, 0.45)
     return xp, qp, dict(name=f"ring{n_cells}", box=(-L, -L, -L, L, L, L), dpm=(h, h, h), steps=2, dt=0.01)
+
+
+BATCH_MESHES = (32, 48, 64, 96, 128)
+
+
+def batched_rings(n=64, seed=2025):
+    """Independent problems: one ring each, radius U(0.5,1.5), random unit
+    axis, sigma = 0.1 R, circulation U(0.5,2), mesh edge drawn from
+    {32,48,64,96,128} cells on a cube of half-width 2.5 R around the ring
+    (room for about 20 steps of self-advection at the largest Gamma / R).
+    Returns a list of (xp, qp, workload dict)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        R = rng.uniform(0.5, 1.5)
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        gamma = rng.uniform(0.5, 2.0)
+        cells = int(rng.choice(BATCH_MESHES))
+        L = 2.5 * R
+        h = 2 * L / cells
+        xp, qp = _ring_particles(R, 0.1 * R, gamma, (0.0, 0.0, 0.0), axis, (h, h, h), 0.35 * R)
+        out.append((xp, qp, dict(name=f"ring{cells}", box=(-L, -L, -L, L, L, L), dpm=(h, h, h), steps=20, dt=0.01)))
+    return out
+
+
+def two_level_128():
+    """128^3 ring problem solved with ncoarse = 2: the fine block and a
+    2x-coarser grid of the two-level YAPS coupling."""
+    xp, qp, w = scaled_ring(128)
+    w = dict(w, name="ring128_nc2", ncoarse=2)
+    return xp, qp, w
