@@ -239,6 +239,43 @@ def run_batched(args, local):
             "timing": "batched: CUDA events over all streams; loops: host clock (each step synchronous)"}
 
 
+def run_adjoint(args, local, reps=3):
+    """Adjoint:forward time ratio on the 64^3 ring: 10 steps (dt 0.01) and a
+    loss on 1024 probes in the shell 1.2 <= r <= 1.4 plus 0.1 x the mesh
+    kinetic energy; gradient with respect to every particle position and
+    strength (checkpointed forward, recomputed step by step backward)."""
+    import vpm_free_gb300 as V
+    from vpm_free_gb300 import workloads as W
+    xp, qp, w = W.ring64()
+    cfg = V.VPMConfig.make(dpm=w["dpm"], box=w["box"])
+    rng = np.random.default_rng(11)
+    v = rng.normal(size=(1024, 3))
+    probes = v / np.linalg.norm(v, axis=1)[:, None] * rng.uniform(1.2, 1.4, size=1024)[:, None]
+    with V.VPM(cfg, device=local) as h:
+        h.define_sizes(xp)
+        xr, qr = h.remesh_particles_3d(1, xp, qp)
+        h.set_particles(xr, qr)
+        h.adjoint_run(w["steps"], w["dt"], probes, 0.1)       # warm-up (allocations, graph capture)
+        fw, bw = [], []
+        for _ in range(reps):
+            loss, xbar, qbar, f, b = h.adjoint_run(w["steps"], w["dt"], probes, 0.1)
+            fw.append(f)
+            bw.append(b)
+        h.run(1, w["dt"])                                      # plain forward of the same steps
+        h.set_particles(xr, qr)
+        plain = []
+        for _ in range(reps):
+            ms, _ = h.run(w["steps"], w["dt"])
+            plain.append(ms)
+            h.set_particles(xr, qr)
+    f, b, p = float(np.median(fw)), float(np.median(bw)), float(np.median(plain))
+    return {"workload": "ring64 (64^3, 10 steps, dt 0.01, 1024 probes, ke 0.1)", "particles": int(xr.shape[0]),
+            "ms_forward": f, "ms_backward": b, "ratio": b / f, "ms_plain_forward": p, "ratio_vs_plain": b / p,
+            "loss": loss, "timing": "CUDA events on the library stream, median of %d" % reps,
+            "forward": "checkpointed steps (step graph) + final field + loss",
+            "backward": "per step: recompute + remesh/Euler/M2P/stretching/curl/Poisson/deposition transposes"}
+
+
 def run_reference(args, dist):
     if dist.rank != 0:
         return 0
@@ -366,6 +403,9 @@ def run_ours(args, dist):
     batched = None
     if not args.no_batched and args.workload == "leapfrog256":
         batched = run_batched(args, local)
+    adjoint = None
+    if not args.no_adjoint and args.workload == "leapfrog256":
+        adjoint = run_adjoint(args, local)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -378,7 +418,7 @@ def run_ours(args, dist):
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "clocks": clk if rank == 0 else None,
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "roofline_kernels": roofs,
-        "tree": tree, "cpu_baseline": cpu, "batched": batched,
+        "tree": tree, "cpu_baseline": cpu, "batched": batched, "adjoint": adjoint,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -396,6 +436,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="leapfrog256",
                     help="leapfrog256 is the benchmark; the rings are small profiling cases")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-problems measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint:forward measurement")
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--batch-operator-budget", type=int, default=12 << 30,
                     help="bytes of recorded boundary operator per batched problem")

@@ -208,6 +208,45 @@ int vpmg_fp64_peak(vpmg_handle* h, double* tflops);
  * precompute (walk the tree every step).  Default: 100 GiB.              */
 int vpmg_set_operator_budget(vpmg_handle* h, long long bytes);
 
+/* ---- reverse mode (no counterpart in the reference) -------------------- */
+/* The vector-potential solve alone (rhsscat_3d, yaps3d, solget_3d of
+ * source/vpm.f90:171-314) on host arrays: psi = L r, both 3 x NN
+ * components back to back, node (i,j,k) at i + NN1 (j + NN2 k).         */
+int vpmg_apply_poisson(vpmg_handle* h, const double* r, double* psi);
+/* Its exact transpose: rbar = L^T psibar (same layout).                  */
+int vpmg_adjoint_poisson(vpmg_handle* h, const double* psibar, double* rbar);
+/* Vector-Jacobian product of the field step vpm(..., WhatToDo = 2, ...):
+ * with (UP, GP) = F(XP, QP), returns xbar (3, nvr) and qbar (3, nvr; for
+ * QP(1:3)) = (dF / d(XP, QP(1:3)))^T (upbar, gpbar).  The handle's
+ * particles become XP/QP, as vpm(...) leaves them.  M4' projection only.  */
+int vpmg_vjp_fields(vpmg_handle* h, const double* xp, const double* qp, int nvr, const double* upbar,
+                    const double* gpbar, double* xbar, double* qbar);
+/* Vector-Jacobian product of remesh_particles_3d(1) (source/vpm_remesh.f90:
+ * 5-225) with respect to the input XP and QP(1:3): qbar_new (3, nnew) is
+ * the adjoint of the emitted strengths, nnew the count the remesh emits
+ * (VPMG_ERR_ARG otherwise); the |w| cut is a fixed mask.                  */
+int vpmg_vjp_remesh(vpmg_handle* h, const double* xp, const double* qp, int nvr, const double* qbar_new, int nnew,
+                    double* xbar, double* qbar);
+/* Loss of nsteps steps (field step, Euler push with uinf = 0, remesh)
+ * from the handle's particles, evaluated on the velocity field of the
+ * final particles:
+ *   loss = sum_p |u(probe_p)|^2 + ke_weight * 0.5 * DV * sum_nodes |u|^2
+ * with u(probe) the M4' interpolation.  probes: (3, nprobe) like XP.
+ * mask_mode 0: the reference's remesh |w| cut; 1: the cut, recording each
+ * step's node mask; 2: the masks recorded by the last vpmg_adjoint_run (or
+ * mode-1 call): the fixed-mask map that the gradient differentiates.
+ * The handle's particles are left as they were.  M4' projection only.   */
+int vpmg_adjoint_loss(vpmg_handle* h, int nsteps, double dt, const double* probes, int nprobe, double ke_weight,
+                      int mask_mode, double* loss);
+/* The same loss and its gradient with respect to the initial particle
+ * positions xbar (3, NVR) and strengths qbar (3, NVR; QP(1:3)), by the
+ * exact transpose of every step, with the particle states checkpointed on
+ * the forward pass (7 doubles per mesh node and step of device memory)
+ * and each step's remesh mask recorded (the |w| cut is held fixed).
+ * ms_forward / ms_backward: device milliseconds of the two passes.       */
+int vpmg_adjoint_run(vpmg_handle* h, int nsteps, double dt, const double* probes, int nprobe, double ke_weight,
+                     double* loss, double* xbar, double* qbar, double* ms_forward, double* ms_backward);
+
 #ifdef __cplusplus
 }
 #endif

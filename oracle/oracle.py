@@ -71,6 +71,9 @@ def lib():
         L.vpmo_euler.argtypes = [_dp, _dp, _dp, _dp, C.c_int, C.c_double, _dp]
         L.vpmo_remesh.argtypes = [C.POINTER(Config), C.POINTER(Sizes), _dp, _dp, C.c_int, _dp, _dp, C.c_long, C.c_int]
         L.vpmo_remesh.restype = C.c_long
+        L.vpmo_remesh_masked.argtypes = [C.POINTER(Config), C.POINTER(Sizes), _dp, _dp, C.c_int, _dp, _dp, C.c_long,
+                                         C.c_int, C.POINTER(C.c_int), C.c_int]
+        L.vpmo_remesh_masked.restype = C.c_long
         L.vpmo_boundary_values.argtypes = [_PP, _PP, _dp, _dp, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int]
         L.vpmo_boundary_values.restype = C.c_long
         _LIB = L
@@ -184,4 +187,20 @@ def remesh(cfg, sizes, xp, qp, nthreads=0):
     n = lib().vpmo_remesh(C.byref(cfg), C.byref(sizes), xp, qp, xp.shape[0], xo, qo, cap, nthreads)
     if n < 0:
         raise RuntimeError(f"vpmo_remesh failed: {n}")
+    return xo[:n].copy(), qo[:n].copy()
+
+
+def remesh_masked(cfg, sizes, xp, qp, mask, mode, nthreads=0):
+    """remesh with the |w| cut recorded into (mode 1) or replaced by (mode 2)
+    the int32 node mask `mask` of NN1*NN2*NN3 entries."""
+    xp = np.ascontiguousarray(xp, dtype=np.float64)
+    qp = np.ascontiguousarray(qp, dtype=np.float64)
+    cap = int(np.prod(list(sizes.nn)))
+    assert mask.dtype == np.int32 and mask.size == cap and mask.flags.c_contiguous
+    xo = np.empty((cap, 3))
+    qo = np.empty((cap, 4))
+    n = lib().vpmo_remesh_masked(C.byref(cfg), C.byref(sizes), xp, qp, xp.shape[0], xo, qo, cap, nthreads,
+                                 mask.ctypes.data_as(C.POINTER(C.c_int)), int(mode))
+    if n < 0:
+        raise RuntimeError(f"vpmo_remesh_masked failed: {n}")
     return xo[:n].copy(), qo[:n].copy()

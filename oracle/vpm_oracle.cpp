@@ -923,6 +923,11 @@ void vpmo_euler(double* xp, double* qp, const double* up, const double* gp, int 
 
 long vpmo_remesh(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, int nvr,
                  double* xp_out, double* qp_out, long capacity, int nthreads) {
+  return vpmo_remesh_masked(cfg, s, xp, qp, nvr, xp_out, qp_out, capacity, nthreads, nullptr, 0);
+}
+
+long vpmo_remesh_masked(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, int nvr,
+                        double* xp_out, double* qp_out, long capacity, int nthreads, int* mask, int mode) {
   // remesh_particles_3d(1), ncell_rem = 1, mrem = 1 (vpm_remesh.f90:5-225)
   vpmo_sizes r = *s;
   const int NX = s->nn[0], NY = s->nn[1], NZ = s->nn[2];
@@ -937,12 +942,15 @@ long vpmo_remesh(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, 
   const int* nb = s->nn_bl;
   const double thr = (double)1e-09f;  // default-REAL literal of vpm_remesh.f90:184
   long npar = 0;
+  if (mask && mode == 1) std::fill(mask, mask + N, 0);
   for (int k = nb[2] + h; k <= nb[5] - h; ++k)
     for (int j = nb[1] + h; j <= nb[4] - h; ++j)
       for (int i = nb[0] + h; i <= nb[3] - h; ++i) {
         const size_t id = lin(NX, NY, i, j, k);
         const double wmag = std::sqrt(R0[id] * R0[id] + R1[id] * R1[id] + R2[id] * R2[id]);
-        if (wmag < thr) continue;
+        const bool emit = (mask && mode == 2) ? mask[id] != 0 : !(wmag < thr);
+        if (mask && mode == 1) mask[id] = emit ? 1 : 0;
+        if (!emit) continue;
         if (npar < capacity) {
           xp_out[3 * npar + 0] = s->xbound[0] + r.dpm[0] * (double)(i - 1);
           xp_out[3 * npar + 1] = s->xbound[1] + r.dpm[1] * (double)(j - 1);

@@ -119,6 +119,11 @@ void vpmo_euler(double* xp, double* qp, const double* up, const double* gp, int 
  * is written). */
 long vpmo_remesh(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp,
                  int nvr, double* xp_out, double* qp_out, long capacity, int nthreads);
+/* The same with the |w| cut replaced by a node mask (N = NN1*NN2*NN3
+ * ints): mode 1 records the cut's mask, mode 2 emits exactly the masked
+ * nodes (the fixed-mask map whose derivative the reverse mode computes). */
+long vpmo_remesh_masked(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, int nvr,
+                        double* xp_out, double* qp_out, long capacity, int nthreads, int* mask, int mode);
 
 /* Tree-accelerated boundary values alone (source/pinfdomain.f90:86-158
  * minus the final solve): given a zero-BC solution sol0 on an nn grid,

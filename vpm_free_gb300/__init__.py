@@ -36,6 +36,8 @@ EXPORTS = [
     "vpmg_set_particles", "vpmg_get_particles", "vpmg_get_particle_velocity", "vpmg_step", "vpmg_remesh_device",
     "vpmg_num_particles", "vpmg_get_field", "vpmg_kernel_launches", "vpmg_phase_times", "vpmg_tree_stats",
     "vpmg_set_profiling", "vpmg_set_operator_budget", "vpmg_run", "vpmg_bench_kernel", "vpmg_fp64_peak", "vpmg_batch_run",
+    "vpmg_apply_poisson", "vpmg_adjoint_poisson", "vpmg_vjp_fields", "vpmg_vjp_remesh", "vpmg_adjoint_loss",
+    "vpmg_adjoint_run",
 ]
 
 
@@ -129,6 +131,12 @@ def load_library():
     L.vpmg_fp64_peak.argtypes = [C.c_void_p, _dp]
     L.vpmg_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_double, C.c_int, _dp,
                                  C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.vpmg_apply_poisson.argtypes = [C.c_void_p, _dp, _dp]
+    L.vpmg_adjoint_poisson.argtypes = [C.c_void_p, _dp, _dp]
+    L.vpmg_vjp_fields.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp]
+    L.vpmg_vjp_remesh.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, C.c_int, _dp, _dp]
+    L.vpmg_adjoint_loss.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, C.c_int, C.c_double, C.c_int, _dp]
+    L.vpmg_adjoint_run.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp]
     _LIB = L
     return L
 
@@ -346,3 +354,70 @@ class VPM:
 
     def set_operator_budget(self, nbytes):
         self._chk(self._L.vpmg_set_operator_budget(self._h, int(nbytes)))
+
+    # ---- reverse mode -------------------------------------------------------
+    def _mesh_shape(self):
+        s = self.sizes()
+        return (3, s.nn[2], s.nn[1], s.nn[0])
+
+    def apply_poisson(self, r):
+        """psi = L r: the vector-potential solve of one step on a (3, NZ, NY, NX) RHS."""
+        r = _f64(r, self._mesh_shape())
+        psi = np.empty_like(r)
+        self._chk(self._L.vpmg_apply_poisson(self._h, _p(r), _p(psi)))
+        return psi
+
+    def adjoint_poisson(self, psibar):
+        """rbar = L^T psibar (exact transpose of apply_poisson)."""
+        psibar = _f64(psibar, self._mesh_shape())
+        rbar = np.empty_like(psibar)
+        self._chk(self._L.vpmg_adjoint_poisson(self._h, _p(psibar), _p(rbar)))
+        return rbar
+
+    def vjp_fields(self, XP, QP, UPbar, GPbar):
+        """(xbar, qbar) = (d(UP, GP) / d(XP, QP[:, :3]))^T (UPbar, GPbar) of vpm(WhatToDo = 2)."""
+        n = XP.shape[0]
+        XP, QP = _f64(XP, (n, 3)), _f64(QP, (n, 4))
+        UPbar, GPbar = _f64(UPbar, (n, 3)), _f64(GPbar, (n, 3))
+        xb, qb = np.zeros((max(n, 1), 3)), np.zeros((max(n, 1), 3))
+        self._chk(self._L.vpmg_vjp_fields(self._h, _p(XP), _p(QP), n, _p(UPbar), _p(GPbar), _p(xb), _p(qb)))
+        return xb[:n], qb[:n]
+
+    def vjp_remesh(self, XP, QP, Qbar_new):
+        """(xbar, qbar) of remesh_particles_3d(1) for the adjoint Qbar_new (nnew, 3) of the emitted strengths."""
+        n = XP.shape[0]
+        XP, QP = _f64(XP, (n, 3)), _f64(QP, (n, 4))
+        qn = _f64(Qbar_new)
+        xb, qb = np.zeros((max(n, 1), 3)), np.zeros((max(n, 1), 3))
+        self._chk(self._L.vpmg_vjp_remesh(self._h, _p(XP), _p(QP), n, _p(qn), qn.shape[0], _p(xb), _p(qb)))
+        return xb[:n], qb[:n]
+
+    @staticmethod
+    def _probes(probes):
+        if probes is None or len(probes) == 0:
+            return np.zeros((1, 3)), 0
+        pr = _f64(probes)
+        if pr.ndim != 2 or pr.shape[1] != 3:
+            raise ValueError("probes must be (nprobe, 3)")
+        return pr, pr.shape[0]
+
+    def adjoint_loss(self, nsteps, dt, probes=None, ke_weight=0.0, mask_mode=0):
+        """Loss of nsteps steps from the current particles (which are kept):
+        sum |u(probe)|^2 + ke_weight * 0.5 * DV * sum |u|^2 on the final field.
+        mask_mode 0: the reference's remesh cut; 1: record its masks; 2: the
+        masks of the last adjoint_run (the map its gradient differentiates)."""
+        pr, n = self._probes(probes)
+        loss = C.c_double(0.0)
+        self._chk(self._L.vpmg_adjoint_loss(self._h, int(nsteps), float(dt), _p(pr), n, float(ke_weight),
+                                            int(mask_mode), C.byref(loss)))
+        return loss.value
+
+    def adjoint_run(self, nsteps, dt, probes=None, ke_weight=0.0):
+        """(loss, dloss/dXP (NVR, 3), dloss/dQP[:, :3] (NVR, 3), forward ms, backward ms)."""
+        pr, n = self._probes(probes)
+        nvr = self.num_particles()
+        xbar, qbar = np.zeros((max(nvr, 1), 3)), np.zeros((max(nvr, 1), 3))
+        loss, tf, tb = C.c_double(0.0), C.c_double(0.0), C.c_double(0.0)
+        self._chk(self._L.vpmg_adjoint_run(self._h, int(nsteps), float(dt), _p(pr), n, float(ke_weight),
+                                           C.byref(loss), _p(xbar), _p(qbar), C.byref(tf), C.byref(tb)))
+        return loss.value, xbar[:nvr], qbar[:nvr], tf.value, tb.value

@@ -13,80 +13,15 @@
 #include <sstream>
 #include <string>
 
-#include "block_solve.h"
-#include "fields.h"
-#include "particles.h"
-#include "vpmg_internal.h"
+#include "handle.h"
 
 using namespace vpmg;
 
-struct vpmg_handle {
-  vpmg_config cfg{};
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  long long launches = 0;
-  vpmg_sizes sz{};
-  bool sized = false, prepared = false;
-  long long op_budget = 100LL << 30;
-  // grids
-  Grid gglob{}, gbl{}, gco{};
-  int inner_lo[3] = {0, 0, 0}, inner_ext[3] = {0, 0, 0};  // block inner box (0-based) and extent
-  // fields (3 components back to back)
-  DBuf<double> rhs, sol, vel, def;
-  DBuf<double> rhs_bl, sol_bl, sol0, work, bl_sol1_copy;
-  DBuf<double> samp, crhs, csol, csol0;
-  DirichletPlan dp_bl, dp_inner, dp_c;
-  BlockSolve bsolve;      // partially evaluated block solves
-  bool full_block_solves = false;  // evaluate the block solves everywhere (parity / debugging)
-  BoundaryOp bo_bl, bo_c;
-  YapsDev yaps;
-  bool keep_intermediates = false;
-  // particles
-  Particles parts;
-  Binning bins;
-  int np = 0;
-  DBuf<double> stage;  // AoS staging for host copies
-  DBuf<double> bench_scratch;  // replay outputs of vpmg_bench_kernel
-  // timing
-  bool profile = false;
-  bool no_graphs = false;
-  cudaEvent_t ev[10] = {};
-  // graph of one device-resident step, and the per-step particle-count log
-  struct {
-    cudaGraphExec_t exec = nullptr;
-    double dt = 0, u[3] = {0, 0, 0};
-    int remesh = -1;
-    long long launches = 0;
-  } graph;
-  DBuf<int> hist, hist_counter;
-  double phase_ms[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-};
+using vpmg::hx::guarded;
+using vpmg::hx::LaunchScope;
+using vpmg::hx::comp;
 
 namespace {
-
-struct LaunchScope {  // routes VPMG_LAUNCHED() to the handle's counter
-  long long* prev;
-  explicit LaunchScope(vpmg_handle* h) : prev(g_launch_counter) { g_launch_counter = &h->launches; }
-  ~LaunchScope() { g_launch_counter = prev; }
-};
-
-template <class F>
-int guarded(vpmg_handle* h, F&& f) {
-  if (!h) return VPMG_ERR_ARG;
-  try {
-    LaunchScope ls(h);
-    VPMG_CUDA(cudaSetDevice(h->device));
-    f();
-    return VPMG_OK;
-  } catch (const Error& e) {
-    h->err = e.msg;
-    return e.status;
-  } catch (const std::exception& e) {
-    h->err = e.what();
-    return VPMG_ERR_ARG;
-  }
-}
 
 inline int fnint(double x) { return (int)std::lround(x); }
 
@@ -190,7 +125,6 @@ Grid make_grid(const double xb[6], const double d[3], const int n[3]) {
   return g;
 }
 
-double* comp(DBuf<double>& b, size_t n, int c) { return b.p + (size_t)c * n; }
 
 void prepare(vpmg_handle* h) {
   const vpmg_sizes& s = h->sz;
@@ -267,14 +201,13 @@ void infinite_domain(vpmg_handle* h, DirichletPlan& dp, BoundaryOp& bo, const Gr
   for (int c = 0; c < 3; ++c) dirichlet_solve(dp, rhs3 + c * n, sol3 + c * n, false, h->work.p, st);
 }
 
-// Field part of vpm(WhatToDo = 2) on binned particles (vpm.f90:171-314 + yaps3d).
-void field_step(vpmg_handle* h) {
+// The vector-potential solve: global RHS (h->rhs) -> global SOL (h->sol),
+// i.e. rhsscat_3d, yaps3d (one block) and solget_3d.
+void poisson_part(vpmg_handle* h) {
   cudaStream_t st = h->stream;
   const vpmg_sizes& s = h->sz;
   const size_t N = h->gglob.count(), NB = h->gbl.count(), NC = h->gco.count();
-  const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
   double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
-  deposit(h->parts, mg, h->bins, R, st);
   // rhsscat_3d: global interior -> block inner box; the block padding stays zero
   const int go[3] = {s.nn_bl[0] - 1, s.nn_bl[1] - 1, s.nn_bl[2] - 1};
   for (int c = 0; c < 3; ++c) box_copy(R[c], s.nn, go, comp(h->rhs_bl, NB, c), s.nnbl, h->inner_lo, h->inner_ext, st);
@@ -320,6 +253,18 @@ void field_step(vpmg_handle* h) {
   double* S[3] = {comp(h->sol, N, 0), comp(h->sol, N, 1), comp(h->sol, N, 2)};
   for (int c = 0; c < 3; ++c) box_copy(SB[c], s.nnbl, h->inner_lo, S[c], s.nn, go, h->inner_ext, st);
   ev_mark(h, 6);
+}
+
+// Field part of vpm(WhatToDo = 2) on binned particles (vpm.f90:171-314 + yaps3d).
+void field_step(vpmg_handle* h) {
+  cudaStream_t st = h->stream;
+  const vpmg_sizes& s = h->sz;
+  const size_t N = h->gglob.count();
+  const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
+  double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
+  deposit(h->parts, mg, h->bins, R, st);
+  poisson_part(h);
+  double* S[3] = {comp(h->sol, N, 0), comp(h->sol, N, 1), comp(h->sol, N, 2)};
   // calc_velocity_serial_3d(1)
   double* V[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
   double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
@@ -525,6 +470,7 @@ int vpmg_destroy(vpmg_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->graph.exec) cudaGraphExecDestroy(h->graph.exec);
+  vpmg::hx::destroy_adjoint(h);
   for (int i = 0; i < 10; ++i)
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1006,3 +952,32 @@ int vpmg_set_operator_budget(vpmg_handle* h, long long bytes) {
 }
 
 }  // extern "C"
+
+// ---- step helpers shared with adjoint.cu -------------------------------
+namespace vpmg {
+namespace hx {
+MeshDev mesh_dev(const Grid& g, int itype) { return ::mesh_dev(g, itype); }
+Grid remesh_grid(const vpmg_handle* h) {
+  Grid gr = h->gglob;
+  for (int d = 0; d < 3; ++d) gr.d[d] = (h->sz.xbound[d + 3] - h->sz.xbound[d]) / (double)(h->sz.nn[d] - 1);
+  return gr;
+}
+void field_step(vpmg_handle* h) { ::field_step(h); }
+void remesh(vpmg_handle* h) { ::remesh(h); }
+void sync_np(vpmg_handle* h) { ::sync_np(h); }
+void upload_particles(vpmg_handle* h, const double* xp, const double* qp, int n) { ::upload_particles(h, xp, qp, n); }
+void download_particles(vpmg_handle* h, double* xp, double* qp, int n) { ::download_particles(h, xp, qp, n); }
+void poisson_part(vpmg_handle* h) { ::poisson_part(h); }
+void step_on_stream(vpmg_handle* h, double dt) {
+  const double u0[3] = {0.0, 0.0, 0.0};
+  if (h->keep_intermediates || h->no_graphs) {
+    ::one_step(h, dt, u0, 1);
+    return;
+  }
+  ensure_graph(h, dt, u0, 1);
+  VPMG_CUDA(cudaMemsetAsync(h->hist_counter.p, 0, sizeof(int), h->stream));
+  VPMG_CUDA(cudaGraphLaunch(h->graph.exec, h->stream));
+  h->launches += h->graph.launches;
+}
+}  // namespace hx
+}  // namespace vpmg

@@ -41,7 +41,7 @@ struct WalkDev {
   double inv_pi4;
 };
 
-enum { kAccum = 0, kCount = 1, kFill = 2 };
+enum { kAccum = 0, kCount = 1, kFill = 2, kTranspose = 3 };
 
 template <int MODE>
 __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ o1, double* __restrict__ o2,
@@ -57,6 +57,8 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
   int ni = 0;
   long long out = 0;
   if (MODE == kFill) out = rowptr[t];
+  double bcv = 0.0;  // transpose: o1 is the adjoint of the boundary values, o0 the cell adjoints
+  if (MODE == kTranspose) bcv = -W.inv_pi4 * o1[W.tgt_node[t]];
   while (true) {
     int c;
     if (L == W.levmax) {
@@ -89,6 +91,8 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
       col[out] = c;
       wgt[out] = w;
       ++out;
+    } else if (MODE == kTranspose) {
+      if (bcv != 0.0) atomicAdd(&o0[c], w * bcv);
     } else {
       a0 = fma(-W.s0[c], w, a0);
       a1 = fma(-W.s1[c], w, a1);
@@ -255,6 +259,17 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
         }
       }
     }
+  // ancestor of every leaf at each level >= 1 (for the aggregation transpose)
+  std::vector<int> anc((size_t)std::max(levmax, 1) * B.nbound, -1);
+  for (int l = 1; l <= levmax; ++l)
+    for (int ic = 0; ic < T.nbound_lev[l]; ++ic) {
+      const Cell& c = T.cells[(size_t)l * T.nbound + ic];
+      if (c.leaf0 < 0) continue;
+      for (int mm = 0; mm < c.istep; ++mm)
+        for (int nn = 0; nn < c.istep; ++nn)
+          anc[(size_t)(l - 1) * B.nbound + c.leaf0 + mm * c.rowlen + nn] = B.lev_off[l] + ic;
+    }
+  upload(B.anc, anc);
   upload(B.cx, cx); upload(B.cy, cy); upload(B.cz, cz); upload(B.cds, cds); upload(B.cthr, thr);
   upload(B.child, child); upload(B.flags, flags); upload(B.agg_leaf0, leaf0); upload(B.agg_rowlen, rowlen);
   upload(B.agg_istep, istep);
@@ -339,6 +354,94 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
     const WalkDev W = walk_dev(B);
     k_walk<kAccum><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, sol[0], sol[1], sol[2], nullptr, nullptr, nullptr, nullptr);
   }
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+}  // namespace vpmg
+
+// ---------------------------------------------------------- transposes ----
+// Adjoints of the boundary-value chain for the whole-step gradient: with
+// BC = -(1/4pi) T agg N (sol0), these apply N^T agg^T T^T (-1/4pi) to the
+// adjoint of the boundary values of one component.
+namespace vpmg {
+namespace {
+
+__global__ void __launch_bounds__(256) k_csr_T(const long long* __restrict__ rowptr, const int* __restrict__ col,
+                                               const double* __restrict__ wgt, const int* __restrict__ tgt_node,
+                                               int ntarget, double scale, const double* __restrict__ bcbar,
+                                               double* __restrict__ cellbar) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ntarget) return;
+  const double v = scale * bcbar[tgt_node[warp]];
+  if (v == 0.0) return;
+  for (long long k = rowptr[warp] + lane; k < rowptr[warp + 1]; k += 32) atomicAdd(&cellbar[col[k]], wgt[k] * v);
+}
+
+// leaf adjoint = its own level-0 adjoint + sum over ancestors of ds_leaf / ds_cell * cell adjoint
+__global__ void k_agg_T(const int* __restrict__ anc, const double* __restrict__ cds, int nbound, int levmax,
+                        const double* __restrict__ cellbar, double* __restrict__ panelbar) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nbound) return;
+  double v = cellbar[p];
+  const double ds = cds[p];
+  for (int l = 1; l <= levmax; ++l) {
+    const int a = anc[(size_t)(l - 1) * nbound + p];
+    if (a >= 0) v += ds / cds[a] * cellbar[a];
+  }
+  panelbar[p] = v;
+}
+
+__global__ void k_normal_deriv_T(const double* __restrict__ panelbar, int NX, int NY, const int* __restrict__ face,
+                                 const int* __restrict__ pi, const int* __restrict__ pj, const int* __restrict__ pk,
+                                 int nbound, double invx, double invy, double invz, double* __restrict__ sol0bar) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nbound) return;
+  const double g = 0.25 * panelbar[p];
+  if (g == 0.0) return;
+  const double a[5] = {25.0 / 12.0, -4.0, 3.0, -4.0 / 3.0, 0.25};
+  const int f = face[p];
+  const long long sx = 1, sy = NX, sz = (long long)NX * NY;
+  long long step, e1, e2;
+  double inv;
+  if (f < 2) { step = (f == 0) ? sx : -sx; e1 = sy; e2 = sz; inv = invx; }
+  else if (f < 4) { step = (f == 2) ? sy : -sy; e1 = sx; e2 = sz; inv = invy; }
+  else { step = (f == 4) ? sz : -sz; e1 = sx; e2 = sy; inv = invz; }
+  const long long base = (long long)(pi[p] - 1) * sx + (long long)(pj[p] - 1) * sy + (long long)(pk[p] - 1) * sz;
+  const long long corner[4] = {base, base + e1, base + e1 + e2, base + e2};
+  for (int m = 0; m < 4; ++m)
+    for (int k = 0; k < 5; ++k) atomicAdd(&sol0bar[corner[m] + k * step], g * inv * a[k]);
+}
+
+}  // namespace
+
+void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s) {
+  VPMG_CUDA(cudaMemsetAsync(cellbar, 0, sizeof(double) * B.ncell_total, s));
+  const double scale = -1.0 / (4.0 * kPI);
+  if (B.precomputed) {
+    const long long threads = (long long)B.ntarget * 32;
+    k_csr_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, B.tgt_node.p, B.ntarget,
+                                                              scale, bcbar, cellbar);
+  } else {
+    const WalkDev W = walk_dev(B);
+    k_walk<kTranspose><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, cellbar, const_cast<double*>(bcbar), nullptr,
+                                                               nullptr, nullptr, nullptr, nullptr);
+  }
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void boundary_agg_T(BoundaryOp& B, const double* cellbar, double* panelbar, cudaStream_t s) {
+  k_agg_T<<<(B.nbound + 255) / 256, 256, 0, s>>>(B.anc.p, B.cds.p, B.nbound, B.levmax, cellbar, panelbar);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void boundary_panels_T(BoundaryOp& B, const Grid& g, const double* panelbar, double* sol0bar, cudaStream_t s) {
+  k_normal_deriv_T<<<(B.nbound + 255) / 256, 256, 0, s>>>(panelbar, g.n[0], g.n[1], B.pan_face.p, B.pan_i.p, B.pan_j.p,
+                                                          B.pan_k.p, B.nbound, 1.0 / g.d[0], 1.0 / g.d[1],
+                                                          1.0 / g.d[2], sol0bar);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }

@@ -365,16 +365,22 @@ void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const v
 
 // Ordered compaction of the flagged nodes; the new count goes to P.d_np
 // (clamped to the capacity, overflow flagged in B.err), on the stream.
-void remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3],
-                 const int hi[3], double thr, cudaStream_t s) {
+void remesh_mask(const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3], const int hi[3],
+                 double thr, cudaStream_t s) {
   const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
   B.ensure(N);
-  const double dv = m.d[0] * m.d[1] * m.d[2];
   k_remesh_flags<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], m, lo[0], lo[1], lo[2], hi[0], hi[1],
                                                               hi[2], thr, B.cursor.p);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaMemsetAsync(B.sums.p, 0, sizeof(int) * B.sums.n, s));
   exclusive_scan_int(B.cursor.p, B.starts.p, N, B.sums.p, s);
+}
+
+namespace {
+// Emission of the nodes flagged in B.cursor (slots in B.starts) and the new count.
+void emit_flagged(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], cudaStream_t s) {
+  const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
+  const double dv = m.d[0] * m.d[1] * m.d[2];
   const int nt = (int)scan_block_sums_needed(N) - 1;
   k_remesh_emit<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], B.cursor.p, B.starts.p, m, dv,
                                                              P.capacity, P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p,
@@ -383,6 +389,23 @@ void remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const
   k_set_count<<<1, 1, 0, s>>>(P.d_np.p, B.sums.p + nt, P.capacity, B.err.p);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
+}
+}  // namespace
+
+void remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3],
+                 const int hi[3], double thr, cudaStream_t s) {
+  remesh_mask(m, B, rhs, lo, hi, thr, s);
+  emit_flagged(P, m, B, rhs, s);
+}
+
+void remesh_emit_masked(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int* mask,
+                        cudaStream_t s) {
+  const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
+  B.ensure(N);
+  VPMG_CUDA(cudaMemcpyAsync(B.cursor.p, mask, sizeof(int) * N, cudaMemcpyDeviceToDevice, s));
+  VPMG_CUDA(cudaMemsetAsync(B.sums.p, 0, sizeof(int) * B.sums.n, s));
+  exclusive_scan_int(B.cursor.p, B.starts.p, N, B.sums.p, s);
+  emit_flagged(P, m, B, rhs, s);
 }
 
 }  // namespace vpmg

@@ -39,6 +39,13 @@ void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const v
          bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s);
 void remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3],
                  const int hi[3], double thr, cudaStream_t s);
+// The emission mask alone: B.cursor = node flag, B.starts = emit slot (exclusive scan).
+void remesh_mask(const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3], const int hi[3],
+                 double thr, cudaStream_t s);
+// Emission of exactly the nodes flagged in mask (N ints, 0/1): the remesh
+// with a frozen |w| cut.
+void remesh_emit_masked(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int* mask,
+                        cudaStream_t s);
 // Host sync points.
 void check_particle_errors(Binning& B, cudaStream_t s);
 int read_count(const int* d, cudaStream_t s);

@@ -120,6 +120,7 @@ struct BoundaryOp {
   DBuf<int> agg_leaf0;                  // per flat cell: first leaf (flat) or -1 (dummy)
   DBuf<int> agg_rowlen;                 // per flat cell: fast-axis leaf count of its face
   DBuf<int> agg_istep;
+  DBuf<int> anc;                        // [(lev-1)*nbound + leaf]: flat ancestor cell or -1
   DBuf<double> csrc;                    // 3 * ncell_total aggregated sources
   // panels: face geometry for the normal derivative
   DBuf<int> pan_face, pan_i, pan_j, pan_k;  // lower-corner node (0-based) of each panel
@@ -139,6 +140,11 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
 // aggregate, then add the boundary values into the faces of sol.
 void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp, cudaStream_t s);
 void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStream_t s);
+// Transposes (one component): boundary-value adjoint (grid node array) ->
+// cell adjoints -> panel adjoints -> accumulated into the sol0 adjoint.
+void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s);
+void boundary_agg_T(BoundaryOp& B, const double* cellbar, double* panelbar, cudaStream_t s);
+void boundary_panels_T(BoundaryOp& B, const Grid& g, const double* panelbar, double* sol0bar, cudaStream_t s);
 
 // ---------------------------------------------------- small kernels ----
 void fill_zero(double* p, size_t n, cudaStream_t s);
