@@ -6,8 +6,13 @@
 //
 // Method (GB300-first: FP64 is the scarce resource, ~1.2 TFLOP/s):
 //   1. x pass: fold the boundary values into the RHS of the first/last
-//      interior layers, DST-I along x (two real lines packed in one complex
-//      FFT of the odd extension, length 2N), scaled for the later inverse;
+//      interior layers, DST-I along x, scaled for the later inverse.  For
+//      even N = n+1 the DST-I is computed in its real-symmetric form: the
+//      line is pre-twiddled, y_j = sin(pi j/N)(x_j + x_{N-j}) + (x_j - x_{N-j})/2,
+//      two lines share one complex FFT of length N, and the outputs come
+//      from the split spectrum, X_{2m} = -Im F_m and X_{2m+1} = X_{2m-1} + Re F_m
+//      (a prefix sum, X_1 = Re F_0 / 2).  Odd N falls back to the odd
+//      extension (two lines in one complex FFT of length 2N);
 //   2. y pass: the same DST-I along y, in place;
 //   3. z pass: per (p,q) mode the constant-coefficient tridiagonal system
 //      -u[k-1] + d_pq u[k] - u[k+1] = r[k] by a Thomas sweep whose
@@ -28,6 +33,9 @@ namespace {
 
 constexpr int kPairs = 4;         // line pairs (8 real lines) per CTA
 constexpr int kThreads = 128;
+constexpr int kScanLanes = kThreads / (2 * kPairs);  // threads per line in the real-symmetric prefix sum
+static_assert(kThreads % (2 * kPairs) == 0 && kScanLanes <= 32 && (kScanLanes & (kScanLanes - 1)) == 0,
+              "the prefix sum splits a warp into whole power-of-two lane groups, one per line");
 constexpr int kMaxOddRadix = 17;  // largest odd prime radix (2*(cells) must factor into 2..17)
 
 __constant__ double c_rcos[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
@@ -37,8 +45,10 @@ bool g_tables_ready = false;
 struct FFTDev {
   int n, N, M, nst;
   int odd;  // 1 if a stage has an odd radix
+  int rs;   // 1: real-symmetric DST-I (M = N), 0: odd extension (M = 2N)
   int radix[24];
   const double2* tw;
+  const double* sn;  // sin(pi j / N) (rs only)
 };
 
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
@@ -208,6 +218,87 @@ __device__ __forceinline__ void odd_extend(double2* z, const FFTDev& p, int npai
   }
 }
 
+// Real-symmetric DST-I, input side: the pair's lines sit in L at 1..n;
+// Z_0 = 0, Z_j = s_j (L_j + L_{N-j}) + (L_j - L_{N-j}) / 2, s_j = sin(pi j / N).
+__device__ __forceinline__ void rs_pre(const double2* __restrict__ L, double2* __restrict__ Z, const FFTDev& p,
+                                       int npair) {
+  for (int t = threadIdx.x; t < npair * p.N; t += blockDim.x) {
+    const int pr = t / p.N, j = t - pr * p.N;
+    double2 z = make_double2(0.0, 0.0);
+    if (j > 0) {
+      const double2 a = L[pr * p.M + j], b = L[pr * p.M + p.N - j];
+      const double s = __ldg(&p.sn[j]);
+      z.x = fma(s, a.x + b.x, 0.5 * (a.x - b.x));
+      z.y = fma(s, a.y + b.y, 0.5 * (a.y - b.y));
+    }
+    Z[pr * p.M + j] = z;
+  }
+}
+
+// Output side: Z is the length-N FFT of a packed pair.  With Z_m = a + ib,
+// Z_{N-m} = c + id the two lines' spectra are F = ((a+c) + i(b-d))/2 and
+// G = ((b+d) - i(a-c))/2, so X_{2m} = (d-b)/2 and (a-c)/2, and the odd
+// outputs are the prefix sums of r_0 = Z_0 / 2, r_m = ((a+c)/2, (b+d)/2).
+// O[pair * M + k] receives X_k of both lines, k = 1..n.
+__device__ __forceinline__ void rs_post(const double2* __restrict__ Z, double2* __restrict__ O, const FFTDev& p,
+                                        int npair) {
+  const int H = p.N >> 1;
+  for (int t = threadIdx.x; t < npair * H; t += blockDim.x) {
+    const int pr = t / H, m = t - pr * H;
+    const double2 u = Z[pr * p.M + m];
+    if (m == 0) {
+      O[pr * p.M + 1] = make_double2(0.5 * u.x, 0.5 * u.y);
+    } else {
+      const double2 v = Z[pr * p.M + p.N - m];
+      O[pr * p.M + 2 * m] = make_double2(0.5 * (v.y - u.y), 0.5 * (u.x - v.x));
+      O[pr * p.M + 2 * m + 1] = make_double2(0.5 * (u.x + v.x), 0.5 * (u.y + v.y));
+    }
+  }
+  __syncthreads();
+  // inclusive prefix sum over the odd outputs, kScanLanes threads per line:
+  // each sums a contiguous chunk, the lane group scans the chunk sums
+  const int line = threadIdx.x / kScanLanes, lane = threadIdx.x - line * kScanLanes;
+  double* o = reinterpret_cast<double*>(O + (line >> 1) * p.M) + (line & 1);  // X_k at o[2k]
+  const int C = (H + kScanLanes - 1) / kScanLanes;
+  const int m0 = min(H, lane * C), m1 = min(H, m0 + C);
+  double s = 0.0;
+  for (int m = m0; m < m1; ++m) s += o[2 * (2 * m + 1)];
+  double inc = s;
+#pragma unroll
+  for (int off = 1; off < kScanLanes; off <<= 1) {
+    const double y = __shfl_up_sync(0xffffffffu, inc, off, kScanLanes);
+    if (lane >= off) inc += y;
+  }
+  double run = inc - s;
+  for (int m = m0; m < m1; ++m) {
+    run += o[2 * (2 * m + 1)];
+    o[2 * (2 * m + 1)] = run;
+  }
+}
+
+// The transform of the 2*npair lines loaded into `L` (the staging buffer
+// of the plan's mode, see staging()): returns the buffer holding X_k of
+// line (pair, c) at index pair * M + k (k = 1..n) as component c (rs), or
+// the raw odd-extension spectrum (X_k = -W.y / 2 and W.x / 2).
+template <bool ODD>
+__device__ __forceinline__ double2* dst_pairs(double2* A, double2* B, const FFTDev& p, int npair) {
+  if (p.rs) rs_pre(B, A, p, npair);
+  else odd_extend(A, p, npair);
+  __syncthreads();
+  double2* R = fft_all<ODD>(A, B, p, npair);
+  if (!p.rs) return R;
+  double2* O = (R == A) ? B : A;
+  rs_post(R, O, p, npair);
+  __syncthreads();
+  return O;
+}
+__device__ __forceinline__ double2* staging(double2* A, double2* B, const FFTDev& p) { return p.rs ? B : A; }
+__device__ __forceinline__ double dst_out(const double2* O, const FFTDev& p, int li, int k) {
+  const double2 W = O[(li >> 1) * p.M + (k + 1)];
+  if (p.rs) return (li & 1) ? W.y : W.x;
+  return (li & 1) ? 0.5 * W.x : -0.5 * W.y;
+}
+
 // ------------------------------------------------------------ passes ----
 struct Box {
   int dims[3];  // node array dims
@@ -245,19 +336,16 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict
       }
       v *= scale;
     }
-    double* zp = reinterpret_cast<double*>(A + (li >> 1) * p.M + (a + 1));
+    double* zp = reinterpret_cast<double*>(staging(A, B, p) + (li >> 1) * p.M + (a + 1));
     zp[li & 1] = v;
   }
   __syncthreads();
-  odd_extend(A, p, kPairs);
-  __syncthreads();
-  double2* R = fft_all<ODD>(A, B, p, kPairs);
+  const double2* R = dst_pairs<ODD>(A, B, p, kPairs);
   for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
     const int l = l0 + li;
     if (l >= nlines) continue;
-    const double2 W = R[(li >> 1) * p.M + (k + 1)];
-    work[(size_t)l * n + k] = (li & 1) ? 0.5 * W.x : -0.5 * W.y;
+    work[(size_t)l * n + k] = dst_out(R, p, li, k);
   }
 }
 
@@ -279,20 +367,17 @@ __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, i
       const int a = l % m0, c = l / m0;
       v = work[(size_t)a + (size_t)m0 * e + plane * c];
     }
-    double* zp = reinterpret_cast<double*>(A + (li >> 1) * p.M + (e + 1));
+    double* zp = reinterpret_cast<double*>(staging(A, B, p) + (li >> 1) * p.M + (e + 1));
     zp[li & 1] = v;
   }
   __syncthreads();
-  odd_extend(A, p, kPairs);
-  __syncthreads();
-  double2* R = fft_all<ODD>(A, B, p, kPairs);
+  const double2* R = dst_pairs<ODD>(A, B, p, kPairs);
   for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
     const int li = t % (2 * kPairs), k = t / (2 * kPairs);
     const int l = l0 + li;
     if (l >= nlines) continue;
     const int a = l % m0, c = l / m0;
-    const double2 W = R[(li >> 1) * p.M + (k + 1)];
-    work[(size_t)a + (size_t)m0 * k + plane * c] = (li & 1) ? 0.5 * W.x : -0.5 * W.y;
+    work[(size_t)a + (size_t)m0 * k + plane * c] = dst_out(R, p, li, k);
   }
 }
 
@@ -310,21 +395,18 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict
     const int li = t / n, a = t - li * n;
     const int l = l0 + li;
     const double v = (l < nlines) ? work[(size_t)l * n + a] : 0.0;
-    double* zp = reinterpret_cast<double*>(A + (li >> 1) * p.M + (a + 1));
+    double* zp = reinterpret_cast<double*>(staging(A, B, p) + (li >> 1) * p.M + (a + 1));
     zp[li & 1] = v;
   }
   __syncthreads();
-  odd_extend(A, p, kPairs);
-  __syncthreads();
-  double2* R = fft_all<ODD>(A, B, p, kPairs);
+  const double2* R = dst_pairs<ODD>(A, B, p, kPairs);
   const size_t sy = b.dims[0], sz = (size_t)b.dims[0] * b.dims[1];
   for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
     const int l = l0 + li;
     if (l >= nlines) continue;
     const int q = l % b.m[1], c = l / b.m[1];
-    const double2 W = R[(li >> 1) * p.M + (k + 1)];
-    sol[(size_t)(b.o[0] + k) + sy * (b.o[1] + q) + sz * (b.o[2] + c)] = (li & 1) ? 0.5 * W.x : -0.5 * W.y;
+    sol[(size_t)(b.o[0] + k) + sy * (b.o[1] + q) + sz * (b.o[2] + c)] = dst_out(R, p, li, k);
   }
 }
 
@@ -420,6 +502,8 @@ cudaError_t set_dst_smem(int smax) {
 FFTDev dev_plan(const FFTPlan& p) {
   FFTDev d;
   d.n = p.n; d.N = p.N; d.M = p.M; d.nst = p.nst;
+  d.rs = p.rs;
+  d.sn = p.sn.p;
   d.odd = 0;
   for (int i = 0; i < 24; ++i) {
     d.radix[i] = p.radix[i];
@@ -450,7 +534,8 @@ void make_fft_plan(FFTPlan& p, int n) {
   ensure_tables();
   p.n = n;
   p.N = n + 1;
-  p.M = 2 * p.N;
+  p.rs = (p.N % 2 == 0) ? 1 : 0;
+  p.M = p.rs ? p.N : 2 * p.N;
   // factor M: odd primes first (largest first), then 8s, a 4, a 2
   int m = p.M, twos = 0;
   std::vector<int> odd;
@@ -474,6 +559,12 @@ void make_fft_plan(FFTPlan& p, int n) {
   }
   p.tw.ensure(p.M);
   VPMG_CUDA(cudaMemcpy(p.tw.p, h.data(), sizeof(double2) * p.M, cudaMemcpyHostToDevice));
+  if (p.rs) {
+    std::vector<double> sn(p.N);
+    for (int j = 0; j < p.N; ++j) sn[j] = std::sin(kPI * (double)j / (double)p.N);
+    p.sn.ensure(p.N);
+    VPMG_CUDA(cudaMemcpy(p.sn.p, sn.data(), sizeof(double) * p.N, cudaMemcpyHostToDevice));
+  }
 }
 
 void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], const double h[3], cudaStream_t s) {
@@ -599,8 +690,9 @@ namespace {
 constexpr size_t kStaticMaxInterior = (size_t)1 << 21;  // interior nodes (e.g. 128 x 128 x 128)
 constexpr int kStaticMaxLine = 900;                     // interior nodes along x and along y
 constexpr size_t kStaticTw = 2 * (kStaticMaxLine + 1);  // complex FFT length bound
-// doubles: work | pivots | twiddles x (2 per complex) | twiddles y | mu x | mu y
-constexpr size_t kStaticDoubles = 2 * kStaticMaxInterior + 4 * kStaticTw + 2 * kStaticMaxLine;
+constexpr size_t kStaticSn = kStaticMaxLine + 1;         // sin(pi j / N) table bound
+// doubles: work | pivots | twiddles x (2 per complex) | twiddles y | mu x | mu y | sin x | sin y
+constexpr size_t kStaticDoubles = 2 * kStaticMaxInterior + 4 * kStaticTw + 2 * kStaticMaxLine + 2 * kStaticSn;
 
 // 33.6 MB per GPU that loads the library, held until the process exits.
 __device__ __align__(256) double g_static_scratch[kStaticDoubles];
@@ -611,9 +703,12 @@ bool g_static_consts[kStaticMaxDevices] = {false};
 int g_static_smem[kStaticMaxDevices] = {0};
 
 __global__ void k_static_tables(double2* __restrict__ twx, int mx, double2* __restrict__ twy, int my,
-                                double* __restrict__ mux, int nx, double* __restrict__ muy, int ny) {
+                                double* __restrict__ mux, int nx, double* __restrict__ muy, int ny,
+                                double* __restrict__ snx, int sx, double* __restrict__ sny, int sy) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   double sn, cs;
+  if (t < sx) snx[t] = sinpi((double)t / sx);
+  if (t < sy) sny[t] = sinpi((double)t / sy);
   if (t < mx) {
     sincospi(-2.0 * t / mx, &sn, &cs);
     twx[t] = make_double2(cs, sn);
@@ -632,12 +727,15 @@ __global__ void k_static_tables(double2* __restrict__ twx, int mx, double2* __re
   }
 }
 
-// Radix list of the odd-extended DST-I of n points (no allocation).
-bool static_plan(int n, const double2* tw, FFTDev& d) {
+// Radix list of the DST-I of n points (no allocation), in the same form
+// as make_fft_plan (real-symmetric for even N).
+bool static_plan(int n, const double2* tw, const double* sn, FFTDev& d) {
   d.n = n;
   d.N = n + 1;
-  d.M = 2 * (n + 1);
+  d.rs = (d.N % 2 == 0) ? 1 : 0;
+  d.M = d.rs ? d.N : 2 * d.N;
   d.tw = tw;
+  d.sn = sn;
   int m = d.M, twos = 0, odd[24], no = 0;
   while (m % 2 == 0) { m /= 2; ++twos; }
   for (int f = 3; m > 1; f += 2)
@@ -707,8 +805,10 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
   double2* twy = twx + kStaticTw;
   double* mux = reinterpret_cast<double*>(twy + kStaticTw);
   double* muy = mux + kStaticMaxLine;
+  double* snx = muy + kStaticMaxLine;
+  double* sny = snx + kStaticSn;
   FFTDev px, py;
-  if (!static_plan(m[0], twx, px) || !static_plan(m[1], twy, py)) return VPMG_ERR_UNSUPPORTED;
+  if (!static_plan(m[0], twx, snx, px) || !static_plan(m[1], twy, sny, py)) return VPMG_ERR_UNSUPPORTED;
   const int smax = 2 * kPairs * std::max(px.M, py.M) * (int)sizeof(double2);
   if (smax > 227 * 1024) return VPMG_ERR_UNSUPPORTED;
   if (smax > g_static_smem[dev]) {
@@ -721,8 +821,9 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // tables and pivots are rebuilt on every call: the array keeps whatever the
   // previous call (possibly another grid) left in it
-  const int nt = std::max(std::max(px.M, py.M), std::max(m[0], m[1]));
-  k_static_tables<<<(nt + 255) / 256, 256, 0, s>>>(twx, px.M, twy, py.M, mux, m[0], muy, m[1]);
+  const int nt = std::max(std::max(px.M, py.M), std::max(px.N, py.N));
+  k_static_tables<<<(nt + 255) / 256, 256, 0, s>>>(twx, px.M, twy, py.M, mux, m[0], muy, m[1], snx,
+                                                   px.rs ? px.N : 0, sny, py.rs ? py.N : 0);
   const double hz2 = h[2] * h[2], hx2 = h[0] * h[0], hy2 = h[1] * h[1];
   const int nl = m[0] * m[1];
   k_pivots<<<(nl + 255) / 256, 256, 0, s>>>(rinv, mux, muy, m[0], m[1], m[2], hz2 / hx2, hz2 / hy2);

@@ -74,12 +74,16 @@ struct Grid {
 };
 
 // --------------------------------------------------- Dirichlet solver ----
-// FFT plan for the odd-extended DST-I of n = N-1 points: complex length M = 2N.
+// FFT plan for a DST-I of n = N-1 points.  N even: real-symmetric form,
+// two real lines packed in one complex FFT of length M = N (rs = 1);
+// N odd: the odd extension, complex length M = 2N (rs = 0).
 struct FFTPlan {
   int n = 0, N = 0, M = 0;
+  int rs = 0;
   int nst = 0;
   int radix[24];
   DBuf<double2> tw;  // e^{-2 pi i t / M}, t = 0..M-1
+  DBuf<double> sn;   // sin(pi j / N), j = 0..N-1 (rs only)
 };
 void make_fft_plan(FFTPlan& p, int n);
 
