@@ -132,7 +132,7 @@ class Clocks:
         return out
 
 
-WORKLOADS = {"leapfrog256": "leapfrog256", "ring64": "ring64", "ring128": "ring128"}
+WORKLOADS = {"leapfrog256": "leapfrog256", "ring64": "ring64", "ring128": "ring128", "dirichlet273": "dirichlet273"}
 
 
 def _workload(name="leapfrog256"):
@@ -300,11 +300,34 @@ def run_reference(args, dist):
     return 0
 
 
+def run_dirichlet(args, local):
+    """Profiling case for the DST solver alone: pmesh(iynbc = 0), three
+    component Dirichlet solves on a 273^3 box (the padded block of the
+    headline mesh; interior 271^3, so each line is a 272-point DST-I),
+    about 1.3 GB on the device.  Prints ms per 3-component solve."""
+    import vpm_free_gb300 as V
+    n = 273
+    rng = np.random.default_rng(0)
+    R = [rng.normal(size=(n, n, n)) for _ in range(3)]
+    S = [np.zeros((n, n, n)) for _ in range(3)]
+    with V.VPM(V.VPMConfig.make(), device=local) as h:
+        t = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            h.pmesh(S, R, [0.0, 0.0, 0.0, 1.0, 1.0, 1.0], [1.0 / (n - 1)] * 3, 0)
+            t.append(time.perf_counter() - t0)
+    print(json.dumps({"workload": "dirichlet273", "unit": "s per pmesh(iynbc=0) call, host clock incl. copies",
+                      "s": t}))
+    return 0
+
+
 def run_ours(args, dist):
     import vpm_free_gb300 as V
     from vpm_free_gb300 import build as B
     B.build()
     ws, rank, local = _dist()
+    if args.workload == "dirichlet273":
+        return run_dirichlet(args, local)
     xp, qp, w = _workload(args.workload)
     cfg = V.VPMConfig.make(dpm=w["dpm"], box=w["box"])
     h = V.VPM(cfg, device=local)

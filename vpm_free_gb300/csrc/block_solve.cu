@@ -63,25 +63,35 @@ __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W,
 }
 
 // out[p + m0*(j + nsel*kk)] = sum_q S[j][q] * W[p + m0*(q + m1*k)]
-__global__ void k_partial_y(const double* __restrict__ W, int m0, int m1, int nk, const int* __restrict__ klist,
-                            const double* __restrict__ S, int nsel, double* __restrict__ out) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+// A CTA stages the m1 x 32 column tile (p0..p0+31, all q) of plane k in
+// shared memory with coalesced row loads -- W is read from HBM once -- and
+// its threads then form the nsel x 32 dot products from the tile.
+constexpr int kColTile = 32;
+__global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W, int m0, int m1, int nk,
+                                                   const int* __restrict__ klist, const double* __restrict__ S,
+                                                   int nsel, double* __restrict__ out) {
+  extern __shared__ double tile[];  // [q][lane], m1 x kColTile
+  const int p0 = blockIdx.x * kColTile;
   const int kk = blockIdx.y;
-  if (p >= m0 || kk >= nk) return;
   const int k = klist ? klist[kk] : kk;
-  const double* col = W + (size_t)p + (size_t)m0 * m1 * k;
-  for (int j0 = 0; j0 < nsel; j0 += 8) {
-    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const int nj = min(8, nsel - j0);
-    for (int q = 0; q < m1; ++q) {
-      const double w = col[(size_t)m0 * q];
-#pragma unroll
-      for (int jj = 0; jj < 8; ++jj)
-        if (jj < nj) acc[jj] = fma(__ldg(&S[(size_t)(j0 + jj) * m1 + q]), w, acc[jj]);
+  const double* plane = W + (size_t)m0 * m1 * k;
+  const int lane = threadIdx.x % kColTile, row = threadIdx.x / kColTile, rows = blockDim.x / kColTile;
+  const int p = p0 + lane;
+  for (int q = row; q < m1; q += rows) tile[q * kColTile + lane] = (p < m0) ? plane[(size_t)m0 * q + p] : 0.0;
+  __syncthreads();
+  if (p >= m0) return;
+  for (int j = row; j < nsel; j += rows) {
+    const double* Sj = S + (size_t)j * m1;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int q = 0;
+    for (; q + 3 < m1; q += 4) {
+      a0 = fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
+      a1 = fma(__ldg(&Sj[q + 1]), tile[(q + 1) * kColTile + lane], a1);
+      a2 = fma(__ldg(&Sj[q + 2]), tile[(q + 2) * kColTile + lane], a2);
+      a3 = fma(__ldg(&Sj[q + 3]), tile[(q + 3) * kColTile + lane], a3);
     }
-#pragma unroll
-    for (int jj = 0; jj < 8; ++jj)
-      if (jj < nj) out[(size_t)p + (size_t)m0 * ((j0 + jj) + (size_t)nsel * kk)] = acc[jj];
+    for (; q < m1; ++q) a0 = fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
+    out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = (a0 + a1) + (a2 + a3);
   }
 }
 
@@ -214,10 +224,23 @@ void partial_x(const double* W, int m0, int m1, int nk, const int* klist, const 
   VPMG_LAUNCHED();
 }
 
+size_t g_partial_y_smem = 0;  // dynamic shared memory granted to k_partial_y so far
+
+void partial_y_reserve(int m1) {
+  const size_t sm = sizeof(double) * (size_t)m1 * kColTile;
+  VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
+  if (sm > g_partial_y_smem) {
+    VPMG_CUDA(cudaFuncSetAttribute(k_partial_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    g_partial_y_smem = sm;
+  }
+}
+
 void partial_y(const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel, double* out,
                cudaStream_t s) {
-  dim3 g((m0 + 127) / 128, nk);
-  k_partial_y<<<g, 128, 0, s>>>(W, m0, m1, nk, klist, S, nsel, out);
+  const size_t sm = sizeof(double) * (size_t)m1 * kColTile;
+  VPMG_CHECK(sm <= g_partial_y_smem, VPMG_ERR_STATE, "k_partial_y shared memory not reserved");
+  dim3 g((m0 + kColTile - 1) / kColTile, nk);
+  k_partial_y<<<g, 256, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out);
   VPMG_LAUNCHED();
 }
 
@@ -281,6 +304,7 @@ void BlockSolve::prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoar
   up(e_x1, edge(m[0], false)); up(e_xN, edge(m[0], true));
   up(e_y1, edge(m[1], false)); up(e_yN, edge(m[1], true));
   partial_x_reserve(m[0], std::max(8, nsx));
+  partial_y_reserve(m[1]);
   X8.ensure((size_t)8 * m[1] * m[2]);
   Y4.ensure((size_t)m[0] * 4 * m[2]);
   X2.ensure((size_t)2 * m[1] * m[2]);
