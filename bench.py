@@ -381,6 +381,7 @@ def run_ours(args, dist):
     roof["peak_source"] = ("FP64: DFMA-loop TFLOP/s measured in this run (no FP64 entry in MEASURED_PEAKS.json); "
                            "HBM: MEASURED_PEAKS.json hbm_gbs")
     tree = h.tree_stats()
+    tiles = h.dst_tiles()
     sizes_bl = list(h.sizes().nnbl)
     sizes_nn = list(h.sizes().nn)
     np_end = h.num_particles()
@@ -441,7 +442,7 @@ def run_ours(args, dist):
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "clocks": clk if rank == 0 else None,
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "roofline_kernels": roofs,
-        "tree": tree, "cpu_baseline": cpu, "batched": batched, "adjoint": adjoint,
+        "tree": tree, "dst_tiles_autotuned": tiles, "cpu_baseline": cpu, "batched": batched, "adjoint": adjoint,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -204,6 +204,10 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
 /* FP64 FMA throughput of this GPU (TFLOP/s, FMA = 2 flops) from a
  * register-resident DFMA loop: the roofline peak of the FP64-bound kernels. */
 int vpmg_fp64_peak(vpmg_handle* h, double* tflops);
+/* DST tile shapes chosen by the set-up autotuner (line pairs per CTA, 2, 4
+ * or 8) of the padded block's x and y transforms, the inner box's and the
+ * coarse grid's, in that order.                                         */
+int vpmg_dst_tiles(const vpmg_handle* h, int pairs[6]);
 /* Memory limit (bytes) for the precomputed boundary operator; 0 = never
  * precompute (walk the tree every step).  Default: 100 GiB.              */
 int vpmg_set_operator_budget(vpmg_handle* h, long long bytes);

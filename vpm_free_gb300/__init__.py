@@ -36,7 +36,7 @@ EXPORTS = [
     "vpmg_set_particles", "vpmg_get_particles", "vpmg_get_particle_velocity", "vpmg_step", "vpmg_remesh_device",
     "vpmg_num_particles", "vpmg_get_field", "vpmg_kernel_launches", "vpmg_phase_times", "vpmg_tree_stats",
     "vpmg_set_profiling", "vpmg_set_operator_budget", "vpmg_run", "vpmg_bench_kernel", "vpmg_fp64_peak", "vpmg_batch_run",
-    "vpmg_apply_poisson", "vpmg_adjoint_poisson", "vpmg_vjp_fields", "vpmg_vjp_remesh", "vpmg_adjoint_loss",
+    "vpmg_dst_tiles", "vpmg_apply_poisson", "vpmg_adjoint_poisson", "vpmg_vjp_fields", "vpmg_vjp_remesh", "vpmg_adjoint_loss",
     "vpmg_adjoint_run",
 ]
 
@@ -131,6 +131,7 @@ def load_library():
     L.vpmg_fp64_peak.argtypes = [C.c_void_p, _dp]
     L.vpmg_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_double, C.c_int, _dp,
                                  C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.vpmg_dst_tiles.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     L.vpmg_apply_poisson.argtypes = [C.c_void_p, _dp, _dp]
     L.vpmg_adjoint_poisson.argtypes = [C.c_void_p, _dp, _dp]
     L.vpmg_vjp_fields.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp]
@@ -348,6 +349,13 @@ class VPM:
         a, b, c = C.c_longlong(0), C.c_longlong(0), C.c_int(0)
         self._chk(self._L.vpmg_tree_stats(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return {"interactions": a.value, "bytes": b.value, "precomputed": bool(c.value)}
+
+    def dst_tiles(self):
+        """Autotuned DST tile shapes (line pairs per CTA) of the block x/y, inner-box x/y and coarse x/y plans."""
+        t = (C.c_int * 6)()
+        self._chk(self._L.vpmg_dst_tiles(self._h, t))
+        keys = ["block_x", "block_y", "inner_x", "inner_y", "coarse_x", "coarse_y"]
+        return dict(zip(keys, list(t)))
 
     def set_profiling(self, level):
         self._chk(self._L.vpmg_set_profiling(self._h, int(level)))

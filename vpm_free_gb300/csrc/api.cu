@@ -945,6 +945,14 @@ int vpmg_fp64_peak(vpmg_handle* h, double* tflops) {
   });
 }
 
+int vpmg_dst_tiles(const vpmg_handle* h, int pairs[6]) {
+  if (!h || !pairs) return VPMG_ERR_ARG;
+  if (!h->prepared) return VPMG_ERR_STATE;
+  const vpmg::FFTPlan* p[6] = {&h->dp_bl.fx, &h->dp_bl.fy, &h->dp_inner.fx, &h->dp_inner.fy, &h->dp_c.fx, &h->dp_c.fy};
+  for (int i = 0; i < 6; ++i) pairs[i] = p[i]->pairs;
+  return VPMG_OK;
+}
+
 int vpmg_set_operator_budget(vpmg_handle* h, long long bytes) {
   if (!h) return VPMG_ERR_ARG;
   h->op_budget = bytes;

@@ -24,6 +24,7 @@
 // twice: power-of-two radices only, and with the odd radices.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "vpmg_internal.h"
 
@@ -31,11 +32,16 @@ namespace vpmg {
 
 namespace {
 
-constexpr int kPairs = 4;         // line pairs (8 real lines) per CTA
+// Tile shape: a CTA of kThreads transforms PAIRS line pairs (2 * PAIRS real
+// lines).  PAIRS is 2, 4 or 8, chosen per plan by timing (tune_pairs).
 constexpr int kThreads = 128;
-constexpr int kScanLanes = kThreads / (2 * kPairs);  // threads per line in the real-symmetric prefix sum
-static_assert(kThreads % (2 * kPairs) == 0 && kScanLanes <= 32 && (kScanLanes & (kScanLanes - 1)) == 0,
-              "the prefix sum splits a warp into whole power-of-two lane groups, one per line");
+constexpr int kDefaultPairs = 4;
+template <int PAIRS>
+struct Tile {
+  static constexpr int lanes = kThreads / (2 * PAIRS);  // threads per line in the real-symmetric prefix sum
+  static_assert(kThreads % (2 * PAIRS) == 0 && lanes <= 32 && (lanes & (lanes - 1)) == 0,
+                "the prefix sum splits a warp into whole power-of-two lane groups, one per line");
+};
 constexpr int kMaxOddRadix = 17;  // largest odd prime radix (2*(cells) must factor into 2..17)
 
 __constant__ double c_rcos[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
@@ -44,8 +50,9 @@ bool g_tables_ready = false;
 
 struct FFTDev {
   int n, N, M, nst;
-  int odd;  // 1 if a stage has an odd radix
-  int rs;   // 1: real-symmetric DST-I (M = N), 0: odd extension (M = 2N)
+  int odd;    // 1 if a stage has an odd radix
+  int rs;     // 1: real-symmetric DST-I (M = N), 0: odd extension (M = 2N)
+  int pairs;  // line pairs per CTA
   int radix[24];
   const double2* tw;
   const double* sn;  // sin(pi j / N) (rs only)
@@ -240,6 +247,7 @@ __device__ __forceinline__ void rs_pre(const double2* __restrict__ L, double2* _
 // G = ((b+d) - i(a-c))/2, so X_{2m} = (d-b)/2 and (a-c)/2, and the odd
 // outputs are the prefix sums of r_0 = Z_0 / 2, r_m = ((a+c)/2, (b+d)/2).
 // O[pair * M + k] receives X_k of both lines, k = 1..n.
+template <int LANES>
 __device__ __forceinline__ void rs_post(const double2* __restrict__ Z, double2* __restrict__ O, const FFTDev& p,
                                         int npair) {
   const int H = p.N >> 1;
@@ -255,18 +263,18 @@ __device__ __forceinline__ void rs_post(const double2* __restrict__ Z, double2* 
     }
   }
   __syncthreads();
-  // inclusive prefix sum over the odd outputs, kScanLanes threads per line:
+  // inclusive prefix sum over the odd outputs, LANES threads per line:
   // each sums a contiguous chunk, the lane group scans the chunk sums
-  const int line = threadIdx.x / kScanLanes, lane = threadIdx.x - line * kScanLanes;
+  const int line = threadIdx.x / LANES, lane = threadIdx.x - line * LANES;
   double* o = reinterpret_cast<double*>(O + (line >> 1) * p.M) + (line & 1);  // X_k at o[2k]
-  const int C = (H + kScanLanes - 1) / kScanLanes;
+  const int C = (H + LANES - 1) / LANES;
   const int m0 = min(H, lane * C), m1 = min(H, m0 + C);
   double s = 0.0;
   for (int m = m0; m < m1; ++m) s += o[2 * (2 * m + 1)];
   double inc = s;
 #pragma unroll
-  for (int off = 1; off < kScanLanes; off <<= 1) {
-    const double y = __shfl_up_sync(0xffffffffu, inc, off, kScanLanes);
+  for (int off = 1; off < LANES; off <<= 1) {
+    const double y = __shfl_up_sync(0xffffffffu, inc, off, LANES);
     if (lane >= off) inc += y;
   }
   double run = inc - s;
@@ -280,15 +288,16 @@ __device__ __forceinline__ void rs_post(const double2* __restrict__ Z, double2* 
 // of the plan's mode, see staging()): returns the buffer holding X_k of
 // line (pair, c) at index pair * M + k (k = 1..n) as component c (rs), or
 // the raw odd-extension spectrum (X_k = -W.y / 2 and W.x / 2).
-template <bool ODD>
-__device__ __forceinline__ double2* dst_pairs(double2* A, double2* B, const FFTDev& p, int npair) {
+template <bool ODD, int PAIRS>
+__device__ __forceinline__ double2* dst_pairs(double2* A, double2* B, const FFTDev& p) {
+  constexpr int npair = PAIRS;
   if (p.rs) rs_pre(B, A, p, npair);
   else odd_extend(A, p, npair);
   __syncthreads();
   double2* R = fft_all<ODD>(A, B, p, npair);
   if (!p.rs) return R;
   double2* O = (R == A) ? B : A;
-  rs_post(R, O, p, npair);
+  rs_post<Tile<PAIRS>::lanes>(R, O, p, npair);
   __syncthreads();
   return O;
 }
@@ -307,18 +316,18 @@ struct Box {
 };
 
 // x pass, forward: rhs (+ folded boundary values) -> work, scaled.
-template <bool ODD>
+template <bool ODD, int PAIRS>
 __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict__ rhs, const double* __restrict__ sol,
                                                         int zero_bc, double* __restrict__ work, Box b, FFTDev p,
                                                         double ihx2, double ihy2, double ihz2, double scale) {
   extern __shared__ double2 smem[];
   double2* A = smem;
-  double2* B = smem + kPairs * p.M;
+  double2* B = smem + PAIRS * p.M;
   const int nlines = b.m[1] * b.m[2];
-  const int l0 = blockIdx.x * (2 * kPairs);
+  const int l0 = blockIdx.x * (2 * PAIRS);
   const int n = p.n;
   const size_t sy = b.dims[0], sz = (size_t)b.dims[0] * b.dims[1];
-  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
+  for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, a = t - li * n;
     const int l = l0 + li;
     double v = 0.0;
@@ -340,8 +349,8 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict
     zp[li & 1] = v;
   }
   __syncthreads();
-  const double2* R = dst_pairs<ODD>(A, B, p, kPairs);
-  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
+  const double2* R = dst_pairs<ODD, PAIRS>(A, B, p);
+  for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
     const int l = l0 + li;
     if (l >= nlines) continue;
@@ -350,17 +359,17 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict
 }
 
 // y pass (forward or inverse): in place on work (m0 x m1 x m2, x fastest).
-template <bool ODD>
+template <bool ODD, int PAIRS>
 __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, int m0, int m1, int m2, FFTDev p) {
   extern __shared__ double2 smem[];
   double2* A = smem;
-  double2* B = smem + kPairs * p.M;
+  double2* B = smem + PAIRS * p.M;
   const int nlines = m0 * m2;
-  const int l0 = blockIdx.x * (2 * kPairs);
+  const int l0 = blockIdx.x * (2 * PAIRS);
   const int n = p.n;  // == m1
   const size_t plane = (size_t)m0 * m1;
-  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
-    const int li = t % (2 * kPairs), e = t / (2 * kPairs);
+  for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
+    const int li = t % (2 * PAIRS), e = t / (2 * PAIRS);
     const int l = l0 + li;
     double v = 0.0;
     if (l < nlines) {
@@ -371,9 +380,9 @@ __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, i
     zp[li & 1] = v;
   }
   __syncthreads();
-  const double2* R = dst_pairs<ODD>(A, B, p, kPairs);
-  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
-    const int li = t % (2 * kPairs), k = t / (2 * kPairs);
+  const double2* R = dst_pairs<ODD, PAIRS>(A, B, p);
+  for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
+    const int li = t % (2 * PAIRS), k = t / (2 * PAIRS);
     const int l = l0 + li;
     if (l >= nlines) continue;
     const int a = l % m0, c = l / m0;
@@ -382,16 +391,16 @@ __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, i
 }
 
 // x pass, inverse: work -> interior of sol.
-template <bool ODD>
+template <bool ODD, int PAIRS>
 __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict__ work, double* __restrict__ sol, Box b,
                                                         FFTDev p) {
   extern __shared__ double2 smem[];
   double2* A = smem;
-  double2* B = smem + kPairs * p.M;
+  double2* B = smem + PAIRS * p.M;
   const int nlines = b.m[1] * b.m[2];
-  const int l0 = blockIdx.x * (2 * kPairs);
+  const int l0 = blockIdx.x * (2 * PAIRS);
   const int n = p.n;
-  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
+  for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, a = t - li * n;
     const int l = l0 + li;
     const double v = (l < nlines) ? work[(size_t)l * n + a] : 0.0;
@@ -399,9 +408,9 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict
     zp[li & 1] = v;
   }
   __syncthreads();
-  const double2* R = dst_pairs<ODD>(A, B, p, kPairs);
+  const double2* R = dst_pairs<ODD, PAIRS>(A, B, p);
   const size_t sy = b.dims[0], sz = (size_t)b.dims[0] * b.dims[1];
-  for (int t = threadIdx.x; t < 2 * kPairs * n; t += blockDim.x) {
+  for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
     const int l = l0 + li;
     if (l >= nlines) continue;
@@ -473,29 +482,62 @@ __global__ void k_zero_box_faces(double* __restrict__ sol, Box b) {
   }
 }
 
-// Launches picking the instantiation that the plan's radices need.
-void launch_x_fwd(dim3 g, int t, size_t sm, cudaStream_t s, const double* rhs, const double* sol, int zbc,
-                  double* work, Box b, FFTDev p, double ihx2, double ihy2, double ihz2, double scale) {
-  if (p.odd) k_dst_x_fwd<true><<<g, t, sm, s>>>(rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
-  else k_dst_x_fwd<false><<<g, t, sm, s>>>(rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+// Launches picking the instantiation of the plan's radices and tile shape;
+// grid and shared memory follow from the plan.
+size_t tile_smem(const FFTDev& p) { return (size_t)2 * p.pairs * p.M * sizeof(double2); }
+unsigned tile_grid(int lines, const FFTDev& p) { return (unsigned)((lines + 2 * p.pairs - 1) / (2 * p.pairs)); }
+
+template <int PAIRS>
+void x_fwd_t(cudaStream_t s, const double* rhs, const double* sol, int zbc, double* work, Box b, FFTDev p,
+             double ihx2, double ihy2, double ihz2, double scale) {
+  const unsigned g = tile_grid(b.m[1] * b.m[2], p);
+  if (p.odd) k_dst_x_fwd<true, PAIRS><<<g, kThreads, tile_smem(p), s>>>(rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+  else k_dst_x_fwd<false, PAIRS><<<g, kThreads, tile_smem(p), s>>>(rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
 }
-void launch_y(dim3 g, int t, size_t sm, cudaStream_t s, double* work, int m0, int m1, int m2, FFTDev p) {
-  if (p.odd) k_dst_y<true><<<g, t, sm, s>>>(work, m0, m1, m2, p);
-  else k_dst_y<false><<<g, t, sm, s>>>(work, m0, m1, m2, p);
+template <int PAIRS>
+void y_t(cudaStream_t s, double* work, int m0, int m1, int m2, FFTDev p) {
+  const unsigned g = tile_grid(m0 * m2, p);
+  if (p.odd) k_dst_y<true, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, m0, m1, m2, p);
+  else k_dst_y<false, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, m0, m1, m2, p);
 }
-void launch_x_inv(dim3 g, int t, size_t sm, cudaStream_t s, const double* work, double* sol, Box b, FFTDev p) {
-  if (p.odd) k_dst_x_inv<true><<<g, t, sm, s>>>(work, sol, b, p);
-  else k_dst_x_inv<false><<<g, t, sm, s>>>(work, sol, b, p);
+template <int PAIRS>
+void x_inv_t(cudaStream_t s, const double* work, double* sol, Box b, FFTDev p) {
+  const unsigned g = tile_grid(b.m[1] * b.m[2], p);
+  if (p.odd) k_dst_x_inv<true, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, sol, b, p);
+  else k_dst_x_inv<false, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, sol, b, p);
 }
-cudaError_t set_dst_smem(int smax) {
+void launch_x_fwd(cudaStream_t s, const double* rhs, const double* sol, int zbc, double* work, Box b, FFTDev p,
+                  double ihx2, double ihy2, double ihz2, double scale) {
+  if (p.pairs == 2) x_fwd_t<2>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+  else if (p.pairs == 8) x_fwd_t<8>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+  else x_fwd_t<4>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+}
+void launch_y(cudaStream_t s, double* work, int m0, int m1, int m2, FFTDev p) {
+  if (p.pairs == 2) y_t<2>(s, work, m0, m1, m2, p);
+  else if (p.pairs == 8) y_t<8>(s, work, m0, m1, m2, p);
+  else y_t<4>(s, work, m0, m1, m2, p);
+}
+void launch_x_inv(cudaStream_t s, const double* work, double* sol, Box b, FFTDev p) {
+  if (p.pairs == 2) x_inv_t<2>(s, work, sol, b, p);
+  else if (p.pairs == 8) x_inv_t<8>(s, work, sol, b, p);
+  else x_inv_t<4>(s, work, sol, b, p);
+}
+template <int PAIRS>
+cudaError_t set_smem_t(int smax) {
   cudaError_t e = cudaSuccess;
   const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_fwd<true>, a, smax);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_fwd<false>, a, smax);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y<true>, a, smax);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y<false>, a, smax);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<true>, a, smax);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<false>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_fwd<true, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_fwd<false, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y<true, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y<false, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<true, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<false, PAIRS>, a, smax);
+  return e;
+}
+cudaError_t set_dst_smem(int smax) {
+  cudaError_t e = set_smem_t<2>(smax);
+  if (e == cudaSuccess) e = set_smem_t<4>(smax);
+  if (e == cudaSuccess) e = set_smem_t<8>(smax);
   return e;
 }
 
@@ -503,6 +545,7 @@ FFTDev dev_plan(const FFTPlan& p) {
   FFTDev d;
   d.n = p.n; d.N = p.N; d.M = p.M; d.nst = p.nst;
   d.rs = p.rs;
+  d.pairs = p.pairs;
   d.sn = p.sn.p;
   d.odd = 0;
   for (int i = 0; i < 24; ++i) {
@@ -526,7 +569,73 @@ void ensure_tables() {
   g_tables_ready = true;
 }
 
-size_t smem_bytes(const FFTPlan& p) { return (size_t)2 * kPairs * p.M * sizeof(double2); }
+size_t smem_bytes(const FFTPlan& p, int pairs) { return (size_t)2 * pairs * p.M * sizeof(double2); }
+constexpr size_t kMaxDstSmem = 227 * 1024;
+
+// The DST kernels' shared-memory limit is an attribute of each kernel on
+// each device, shared by every plan and by the allocation-free entry
+// point: it is only ever raised (set-up time, outside any stream capture).
+constexpr int kMaxDevices = 64;
+size_t g_dst_smem[kMaxDevices] = {0};
+cudaError_t raise_dst_smem_status(size_t need) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  if (need <= g_dst_smem[dev]) return cudaSuccess;
+  e = set_dst_smem((int)need);
+  if (e == cudaSuccess) g_dst_smem[dev] = need;
+  return e;
+}
+void raise_dst_smem(size_t need) { VPMG_CUDA(raise_dst_smem_status(need)); }
+
+// Tile-shape autotuner: times the DST pass of this plan with 2, 4 and 8
+// line pairs per CTA on a scratch array shaped like the solve's lines
+// (m0 x n x m2, lines along the middle axis; m0 = 1 gives contiguous rows as
+// in the x passes) and keeps the fastest.  The transform of a line does not
+// depend on the tile, so neither do the results.  Set VPMG_DST_PAIRS=2|4|8
+// to fix the choice.
+void tune_pairs(FFTPlan& p, int lines, int m0, int n, int m2, cudaStream_t s) {
+  static const char* fixed = std::getenv("VPMG_DST_PAIRS");
+  int cand[3] = {2, 4, 8}, ncand = 0, ok[3];
+  for (int c : cand)
+    if (smem_bytes(p, c) <= kMaxDstSmem) ok[ncand++] = c;
+  raise_dst_smem(smem_bytes(p, ok[ncand - 1]));
+  if (fixed) {
+    const int f = std::atoi(fixed);
+    for (int i = 0; i < ncand; ++i)
+      if (ok[i] == f) { p.pairs = f; return; }
+  }
+  if (lines < 64 || ncand == 1) {  // too few lines to time; keep the smallest tile that fits
+    p.pairs = std::min(kDefaultPairs, ok[ncand - 1]);
+    return;
+  }
+  DBuf<double> scratch;
+  scratch.ensure((size_t)m0 * n * m2);
+  fill_zero(scratch.p, scratch.n, s);
+  cudaEvent_t e0, e1;
+  VPMG_CUDA(cudaEventCreate(&e0));
+  VPMG_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int pick = ok[0];
+  for (int i = 0; i < ncand; ++i) {
+    p.pairs = ok[i];
+    const FFTDev d = dev_plan(p);
+    launch_y(s, scratch.p, m0, n, m2, d);  // warm-up
+    VPMG_CUDA(cudaEventRecord(e0, s));
+    for (int r = 0; r < 3; ++r) launch_y(s, scratch.p, m0, n, m2, d);
+    VPMG_CUDA(cudaEventRecord(e1, s));
+    VPMG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    VPMG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    count_launch(4);
+    if (ms < best) { best = ms; pick = ok[i]; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  VPMG_CUDA(cudaGetLastError());
+  p.pairs = pick;
+}
 
 }  // namespace
 
@@ -534,6 +643,7 @@ void make_fft_plan(FFTPlan& p, int n) {
   ensure_tables();
   p.n = n;
   p.N = n + 1;
+  p.pairs = kDefaultPairs;
   p.rs = (p.N % 2 == 0) ? 1 : 0;
   p.M = p.rs ? p.N : 2 * p.N;
   // factor M: odd primes first (largest first), then 8s, a 4, a 2
@@ -580,14 +690,10 @@ void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], co
   }
   make_fft_plan(P.fx, P.m[0]);
   make_fft_plan(P.fy, P.m[1]);
-  const size_t smax = std::max(smem_bytes(P.fx), smem_bytes(P.fy));
-  VPMG_CHECK(smax <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "mesh too large for the shared-memory DST");
-  // The attribute is per kernel (not per plan): only ever raise it.
-  static int s_smem_set = 0;
-  if ((int)smax > s_smem_set) {
-    VPMG_CUDA(set_dst_smem((int)smax));
-    s_smem_set = (int)smax;
-  }
+  VPMG_CHECK(std::max(smem_bytes(P.fx, 2), smem_bytes(P.fy, 2)) <= kMaxDstSmem, VPMG_ERR_UNSUPPORTED,
+             "mesh too large for the shared-memory DST");
+  tune_pairs(P.fx, P.m[1] * P.m[2], 1, P.m[0], P.m[1] * P.m[2], s);  // rows along x
+  tune_pairs(P.fy, P.m[0] * P.m[2], P.m[0], P.m[1], P.m[2], s);      // columns along y
   // eigenvalues mu_p = 4 sin^2(pi p / 2N), pivots for d = 2 + hz^2 (mu_p/hx^2 + mu_q/hy^2)
   std::vector<double> mux(P.m[0]), muy(P.m[1]);
   for (int p = 0; p < P.m[0]; ++p) { const double sn = std::sin(kPI * (p + 1) / (2.0 * (P.m[0] + 1))); mux[p] = 4.0 * sn * sn; }
@@ -615,15 +721,12 @@ void dirichlet_solve(DirichletPlan& P, const double* rhs, double* sol, bool zero
   const double hx2 = P.h[0] * P.h[0], hy2 = P.h[1] * P.h[1], hz2 = P.h[2] * P.h[2];
   // Thomas RHS r = -hz^2 * ghat, with the inverse DST normalisation 4/(Nx Ny).
   const double scale = -hz2 * 4.0 / ((double)(P.m[0] + 1) * (double)(P.m[1] + 1));
-  const int lx = P.m[1] * P.m[2], ly = P.m[0] * P.m[2];
-  const int gx = (lx + 2 * kPairs - 1) / (2 * kPairs), gy = (ly + 2 * kPairs - 1) / (2 * kPairs);
-  launch_x_fwd(gx, kThreads, smem_bytes(P.fx), s, rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2,
-                                                     1.0 / hz2, scale);
-  launch_y(gy, kThreads, smem_bytes(P.fy), s, work, P.m[0], P.m[1], P.m[2], py);
+  launch_x_fwd(s, rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2, 1.0 / hz2, scale);
+  launch_y(s, work, P.m[0], P.m[1], P.m[2], py);
   const int nl = P.m[0] * P.m[1];
   k_thomas<<<(nl + 127) / 128, 128, 0, s>>>(work, P.rinv.p, P.m[0], P.m[1], P.m[2]);
-  launch_y(gy, kThreads, smem_bytes(P.fy), s, work, P.m[0], P.m[1], P.m[2], py);
-  launch_x_inv(gx, kThreads, smem_bytes(P.fx), s, work, sol, b, px);
+  launch_y(s, work, P.m[0], P.m[1], P.m[2], py);
+  launch_x_inv(s, work, sol, b, px);
   count_launch(5);
   if (zero_bc) {
     k_zero_box_faces<<<256, 256, 0, s>>>(sol, b);
@@ -642,11 +745,8 @@ void dst_forward_xy(DirichletPlan& P, const double* rhs, const double* sol, bool
   const FFTDev px = dev_plan(P.fx), py = dev_plan(P.fy);
   const double hx2 = P.h[0] * P.h[0], hy2 = P.h[1] * P.h[1], hz2 = P.h[2] * P.h[2];
   const double scale = dirichlet_scale(P);
-  const int lx = P.m[1] * P.m[2], ly = P.m[0] * P.m[2];
-  const int gx = (lx + 2 * kPairs - 1) / (2 * kPairs), gy = (ly + 2 * kPairs - 1) / (2 * kPairs);
-  launch_x_fwd(gx, kThreads, smem_bytes(P.fx), s, rhs, sol, zero_bc ? 1 : 0, ghat, b, px, 1.0 / hx2, 1.0 / hy2,
-                                                     1.0 / hz2, scale);
-  launch_y(gy, kThreads, smem_bytes(P.fy), s, ghat, P.m[0], P.m[1], P.m[2], py);
+  launch_x_fwd(s, rhs, sol, zero_bc ? 1 : 0, ghat, b, px, 1.0 / hx2, 1.0 / hy2, 1.0 / hz2, scale);
+  launch_y(s, ghat, P.m[0], P.m[1], P.m[2], py);
   count_launch(2);
   VPMG_CUDA(cudaGetLastError());
 }
@@ -661,8 +761,7 @@ double dirichlet_scale(const DirichletPlan& P) {
 void dst_lines_y(const FFTPlan& p, double* data, int m0, int m1, int m2, cudaStream_t s) {
   if (m0 <= 0 || m2 <= 0) return;
   VPMG_CHECK(m1 == p.n, VPMG_ERR_ARG, "dst_lines_y: line length differs from the plan");
-  const int ly = m0 * m2;
-  launch_y((ly + 2 * kPairs - 1) / (2 * kPairs), kThreads, smem_bytes(p), s, data, m0, m1, m2, dev_plan(p));
+  launch_y(s, data, m0, m1, m2, dev_plan(p));
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
@@ -675,8 +774,7 @@ void dst_x_inv_to_box(const FFTPlan& p, const double* data, double* sol, const i
   VPMG_CHECK(m[0] == p.n, VPMG_ERR_ARG, "dst_x_inv_to_box: line length differs from the plan");
   Box b;
   for (int d = 0; d < 3; ++d) { b.dims[d] = dims[d]; b.o[d] = o[d]; b.m[d] = m[d]; }
-  const int lx = m[1] * m[2];
-  launch_x_inv((lx + 2 * kPairs - 1) / (2 * kPairs), kThreads, smem_bytes(p), s, data, sol, b, dev_plan(p));
+  launch_x_inv(s, data, sol, b, dev_plan(p));
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
@@ -700,7 +798,6 @@ __device__ __align__(256) double g_static_scratch[kStaticDoubles];
 constexpr int kStaticMaxDevices = 64;
 double* g_static_base[kStaticMaxDevices] = {nullptr};
 bool g_static_consts[kStaticMaxDevices] = {false};
-int g_static_smem[kStaticMaxDevices] = {0};
 
 __global__ void k_static_tables(double2* __restrict__ twx, int mx, double2* __restrict__ twy, int my,
                                 double* __restrict__ mux, int nx, double* __restrict__ muy, int ny,
@@ -809,14 +906,12 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
   double* sny = snx + kStaticSn;
   FFTDev px, py;
   if (!static_plan(m[0], twx, snx, px) || !static_plan(m[1], twy, sny, py)) return VPMG_ERR_UNSUPPORTED;
-  const int smax = 2 * kPairs * std::max(px.M, py.M) * (int)sizeof(double2);
+  px.pairs = py.pairs = kDefaultPairs;
+  const int smax = 2 * kDefaultPairs * std::max(px.M, py.M) * (int)sizeof(double2);
   if (smax > 227 * 1024) return VPMG_ERR_UNSUPPORTED;
-  if (smax > g_static_smem[dev]) {
-    if (set_dst_smem(smax) != cudaSuccess) {
-      cudaGetLastError();
-      return VPMG_ERR_CUDA;
-    }
-    g_static_smem[dev] = smax;
+  if (raise_dst_smem_status((size_t)smax) != cudaSuccess) {
+    cudaGetLastError();
+    return VPMG_ERR_CUDA;
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // tables and pivots are rebuilt on every call: the array keeps whatever the
@@ -830,14 +925,11 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
   Box b;
   for (int d = 0; d < 3; ++d) { b.dims[d] = dims[d]; b.o[d] = box[d] + 1; b.m[d] = m[d]; }
   const double scale = -hz2 * 4.0 / ((double)(m[0] + 1) * (double)(m[1] + 1));
-  const int lx = m[1] * m[2], ly = m[0] * m[2];
-  const int gx = (lx + 2 * kPairs - 1) / (2 * kPairs), gy = (ly + 2 * kPairs - 1) / (2 * kPairs);
-  const size_t shx = (size_t)2 * kPairs * px.M * sizeof(double2), shy = (size_t)2 * kPairs * py.M * sizeof(double2);
-  launch_x_fwd(gx, kThreads, shx, s, rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2, 1.0 / hz2, scale);
-  launch_y(gy, kThreads, shy, s, work, m[0], m[1], m[2], py);
+  launch_x_fwd(s, rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2, 1.0 / hz2, scale);
+  launch_y(s, work, m[0], m[1], m[2], py);
   k_thomas<<<(nl + 127) / 128, 128, 0, s>>>(work, rinv, m[0], m[1], m[2]);
-  launch_y(gy, kThreads, shy, s, work, m[0], m[1], m[2], py);
-  launch_x_inv(gx, kThreads, shx, s, work, sol, b, px);
+  launch_y(s, work, m[0], m[1], m[2], py);
+  launch_x_inv(s, work, sol, b, px);
   if (zero_bc) k_zero_box_faces<<<256, 256, 0, s>>>(sol, b);
   if (cudaGetLastError() != cudaSuccess) return VPMG_ERR_CUDA;
   return VPMG_OK;

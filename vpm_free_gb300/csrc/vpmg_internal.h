@@ -80,6 +80,7 @@ struct Grid {
 struct FFTPlan {
   int n = 0, N = 0, M = 0;
   int rs = 0;
+  int pairs = 4;     // line pairs per CTA of the DST kernels (tuned per plan)
   int nst = 0;
   int radix[24];
   DBuf<double2> tw;  // e^{-2 pi i t / M}, t = 0..M-1
