@@ -228,13 +228,33 @@ def run_batched(args, local):
     for h in hs:                                     # looped graph replays, one problem at a time
         h.run(k, dt)
     graph_loop_s = time.perf_counter() - t2
+    # the loop of a drop-in host (source/test.f90:83-150) over the problems:
+    # per problem and step vpm(WhatToDo = 2) with host arrays, host Euler,
+    # remesh_particles_3d(1) -- copies in and out inside the calls
+    t3 = time.perf_counter()
+    for h, (xr, qr) in zip(hs, init):
+        XP, QP = xr.copy(), qr.copy()
+        for it in range(k):
+            n = XP.shape[0]
+            UP, GP = np.zeros((n, 3)), np.zeros((n, 3))
+            h.vpm(XP, QP, UP, GP, n, WhatToDo=2, NTIME=it + 1)
+            XP += UP * dt
+            QP[:, :3] -= GP * dt
+            XP, QP = h.remesh_particles_3d(1, XP, QP)
+    ref_loop_s = time.perf_counter() - t3
     precomputed = sum(1 for h in hs if h.tree_stats()["precomputed"])
     for h in hs:
         h.close()
     return {"problems": len(hs), "steps": k, "solves_per_s": solves / (ms_b * 1e-3),
             "particle_steps_per_s": ps_b / (ms_b * 1e-3), "ms": ms_b,
             "loop_plain_solves_per_s": len(hs) * k / loop_s, "loop_graph_solves_per_s": len(hs) * k / graph_loop_s,
+            "loop_reference_calls_solves_per_s": len(hs) * k / ref_loop_s,
             "speedup_vs_plain_loop": (solves / (ms_b * 1e-3)) / (len(hs) * k / loop_s),
+            "speedup_vs_reference_call_loop": (solves / (ms_b * 1e-3)) / (len(hs) * k / ref_loop_s),
+            "loops": {"plain": "vpmg_step per problem and step (device-resident particles, host sync per step)",
+                      "graph": "vpmg_run per problem (one captured step graph, problems one after another)",
+                      "reference_calls": "vpm(WhatToDo=2) + host Euler + remesh_particles_3d per problem and step, "
+                                         "host arrays (what a drop-in Fortran host runs)"},
             "setup_s": setup_s, "precomputed_operators": precomputed,
             "timing": "batched: CUDA events over all streams; loops: host clock (each step synchronous)"}
 

@@ -51,6 +51,9 @@ typedef struct vpmg_config {
   int iynslice;         /* writer option (ignored)                pm.inp:12 */
   int use_box;          /* 1: box[] is the global mesh (no shrink-wrap)     */
   double box[6];        /* XMIN YMIN ZMIN XMAX YMAX ZMAX                    */
+  int ipmwrite;         /* solution-file windows (<= 10)          pm.inp:13 */
+  int ipmwstart[10];    /* window i: NTIME in [start, start + steps]        */
+  int ipmwsteps[10];    /*                                        pm.inp:14+ */
 } vpmg_config;
 
 /* Mesh descriptors of define_sizes (source/vpm.f90:477-660), one block. */
@@ -85,7 +88,9 @@ const char* vpmg_status_string(int status);
  * (source/vpm.f90:54-475).  WhatToDo 0 = read sizes (define_sizes, with
  * the pm.inp already given to vpmg_create), 2 = field step: UP is
  * overwritten with the interpolated velocity and GP with the stretching
- * term times the particle volume (vpm_time.f90:62-107).  neqpm must be 3.
+ * term times the particle volume (vpm_time.f90:62-107); 5 = viscous
+ * diffusion (vpm.f90:345-372): GP = volume x interpolated -NI Lap_h RHS
+ * (diffuse_vort_3d, vpm_gcalc.f90:138-210), UP untouched.  neqpm must be 3.
  * Host pointers; the copies to and from the device happen inside.          */
 int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int* nvr, int neqpm,
              int whattodo, int ntime, double ni, int nvrm);
@@ -211,6 +216,26 @@ int vpmg_dst_tiles(const vpmg_handle* h, int pairs[6]);
 /* Memory limit (bytes) for the precomputed boundary operator; 0 = never
  * precompute (walk the tree every step).  Default: 100 GiB.              */
 int vpmg_set_operator_budget(vpmg_handle* h, long long bytes);
+
+/* ---- the reference's files ------------------------------------------- */
+/* particles.bin of source/test.f90:24-37 (Fortran sequential unformatted:
+ * NVR, Vref, then NVR records X Y Z w1 w2 w3).  Returns XP(3,NVR) and
+ * QP(4,NVR) with QP(1:3) = -w*Vref and QP(4) = Vref.  With xp = qp = NULL
+ * only *nvr and *vref are read (size query).  No GPU needed.              */
+int vpmg_read_particles_bin(const char* path, int* nvr, double* vref, double* xp, double* qp, int capacity);
+/* The inverse: writes XP/QP so that vpmg_read_particles_bin returns them.  */
+int vpmg_write_particles_bin(const char* path, int nvr, double vref, const double* xp, const double* qp);
+/* writesol (source/vpm.f90:662-709): <dir>/NNNNNsolution.bin of the block
+ * range with X Y Z U V W and the vorticity -RHS of the last field step.   */
+int vpmg_write_solution(vpmg_handle* h, const char* dir, int ntime);
+/* writeline (source/vpm.f90:789-833): appends the nine velocity lines to
+ * <dir>/01hist.bin .. 09hist.bin (NTIME = 1 restarts them with a header). */
+int vpmg_write_hist(vpmg_handle* h, const char* dir, int ntime);
+/* The writers vpm(..., WhatToDo = 2, ...) calls, as the reference does
+ * after the velocity (vpm.f90:276-284): flags bit 0 = solution files in
+ * the pm.inp windows (NTIME in [IPMWSTART, IPMWSTART + IPMWSTEPS]), bit 1 =
+ * the hist lines every field step.  Default: off.  dir NULL = cwd.        */
+int vpmg_set_output(vpmg_handle* h, const char* dir, int flags);
 
 /* ---- reverse mode (no counterpart in the reference) -------------------- */
 /* The vector-potential solve alone (rhsscat_3d, yaps3d, solget_3d of

@@ -71,6 +71,7 @@ def lib():
         L.vpmo_euler.argtypes = [_dp, _dp, _dp, _dp, C.c_int, C.c_double, _dp]
         L.vpmo_remesh.argtypes = [C.POINTER(Config), C.POINTER(Sizes), _dp, _dp, C.c_int, _dp, _dp, C.c_long, C.c_int]
         L.vpmo_remesh.restype = C.c_long
+        L.vpmo_diffuse.argtypes = [C.POINTER(Config), C.POINTER(Sizes), _dp, _dp, C.c_double, _dp, C.c_int, C.c_int]
         L.vpmo_remesh_masked.argtypes = [C.POINTER(Config), C.POINTER(Sizes), _dp, _dp, C.c_int, _dp, _dp, C.c_long,
                                          C.c_int, C.POINTER(C.c_int), C.c_int]
         L.vpmo_remesh_masked.restype = C.c_long
@@ -163,6 +164,17 @@ def step_fields(cfg, sizes, xp, qp, nthreads=0):
     if rc != 0:
         raise RuntimeError(f"vpmo_step_fields failed: {rc}")
     return up, gp
+
+
+def diffuse(cfg, sizes, xp, qp, ni, nthreads=0):
+    """vpm(WhatToDo = 5) on one block: returns GP (nvr, 3) = vol * sum W (-NI Lap_h RHS)."""
+    xp = np.ascontiguousarray(xp, dtype=np.float64)
+    qp = np.ascontiguousarray(qp, dtype=np.float64)
+    gp = np.zeros((xp.shape[0], 3))
+    rc = lib().vpmo_diffuse(C.byref(cfg), C.byref(sizes), xp, qp, float(ni), gp, xp.shape[0], nthreads)
+    if rc != 0:
+        raise RuntimeError(f"vpmo_diffuse failed: {rc}")
+    return gp
 
 
 def get_field(which):

@@ -890,6 +890,55 @@ int vpmo_step_fields(const vpmo_config* cfg, const vpmo_sizes* s, const double* 
   return 0;
 }
 
+int vpmo_diffuse(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, double ni, double* gp,
+                 int nvr, int nthreads) {
+  // vpm(WhatToDo = 5) (vpm.f90:345-372): deposition, diffuse_vort_3d
+  // (vpm_gcalc.f90:138-210, neqpm = 3: VIS = NI), back_to_particles_3D(itype = 2)
+  // (vpm_time.f90:109-151).
+  Scratch& W = g_scr;
+  const int NX = s->nn[0], NY = s->nn[1], NZ = s->nn[2];
+  const size_t N = (size_t)NX * NY * NZ;
+  for (int d = 0; d < 3; ++d) { W.nn[d] = s->nn[d]; W.nnbl[d] = s->nnbl[d]; W.nnc[d] = s->nn_coarse[d]; }
+  for (int c = 0; c < 3; ++c) { W.rhs[c].assign(N, 0.0); W.sol[c].assign(N, 0.0); W.vel[c].assign(N, 0.0); W.def[c].assign(N, 0.0); }
+  int e = vpmo_project_particles(s, cfg->interf_iproj, xp, qp, nvr, W.rhs[0].data(), W.rhs[1].data(), W.rhs[2].data(), nthreads);
+  if (e) return e;
+  const double DXpm2 = s->dpm[0] * s->dpm[0], DYpm2 = s->dpm[1] * s->dpm[1], DZpm2 = s->dpm[2] * s->dpm[2];
+  const int* nb = s->nn_bl;
+  const double VIS = ni;
+  for (int k = nb[2] + 1; k <= nb[5] - 1; ++k)
+    for (int j = nb[1] + 1; j <= nb[4] - 1; ++j)
+      for (int i = nb[0] + 1; i <= nb[3] - 1; ++i)
+        for (int c = 0; c < 3; ++c) {
+          const std::vector<double>& R = W.rhs[c];
+          const double dwxdx = (R[lin(NX, NY, i + 1, j, k)] - 2 * R[lin(NX, NY, i, j, k)] + R[lin(NX, NY, i - 1, j, k)]) / DXpm2;
+          const double dwydy = (R[lin(NX, NY, i, j + 1, k)] - 2 * R[lin(NX, NY, i, j, k)] + R[lin(NX, NY, i, j - 1, k)]) / DYpm2;
+          const double dwzdz = (R[lin(NX, NY, i, j, k + 1)] - 2 * R[lin(NX, NY, i, j, k)] + R[lin(NX, NY, i, j, k - 1)]) / DZpm2;
+          W.sol[c][lin(NX, NY, i, j, k)] = -VIS * (dwxdx + dwydy + dwzdz);  // because RHS = -w
+        }
+  const int itype = cfg->interf_iproj;
+  const int ips = (itype == 2) ? 0 : 1, ipf = (itype == 2) ? 1 : 2;
+  const double XMIN = s->xbound[0], YMIN = s->xbound[1], ZMIN = s->xbound[2];
+  const double DX = s->dpm[0], DY = s->dpm[1], DZ = s->dpm[2];
+  for (int nv = 0; nv < nvr; ++nv) {
+    const double px = xp[3 * (size_t)nv], py = xp[3 * (size_t)nv + 1], pz = xp[3 * (size_t)nv + 2];
+    const int inode = (int)((px - XMIN) / DX) + 1, jnode = (int)((py - YMIN) / DY) + 1, knode = (int)((pz - ZMIN) / DZ) + 1;
+    double g[3] = {0, 0, 0};
+    for (int k = knode - ips; k <= knode + ipf; ++k)
+      for (int j = jnode - ips; j <= jnode + ipf; ++j)
+        for (int i = inode - ips; i <= inode + ipf; ++i) {
+          const double fx = projection_fun(itype, (px - XMIN - (double)(i - 1) * DX) / DX);
+          const double fy = projection_fun(itype, (py - YMIN - (double)(j - 1) * DY) / DY);
+          const double fz = projection_fun(itype, (pz - ZMIN - (double)(k - 1) * DZ) / DZ);
+          const double f = fx * fy * fz;
+          if (i < 1 || i > NX || j < 1 || j > NY || k < 1 || k > NZ) return -1;
+          const size_t id = lin(NX, NY, i, j, k);
+          for (int c = 0; c < 3; ++c) g[c] = g[c] + f * W.sol[c][id];
+        }
+    for (int c = 0; c < 3; ++c) gp[3 * (size_t)nv + c] = g[c] * qp[4 * (size_t)nv + 3];
+  }
+  return 0;
+}
+
 long vpmo_get_field(int which, double* out, long capacity) {
   Scratch& W = g_scr;
   std::vector<double>* f = nullptr;

@@ -109,6 +109,12 @@ enum {
  * element count per component, or -1. */
 long vpmo_get_field(int which, double* out, long capacity);
 
+/* vpm(WhatToDo = 5): deposition, diffuse_vort_3d (SOL = -NI Lap_h RHS on the
+ * block interior) and back_to_particles_3D(itype = 2): GP = vol sum W SOL.
+ * The fields are kept for vpmo_get_field (RHS, SOL). */
+int vpmo_diffuse(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, double ni, double* gp,
+                 int nvr, int nthreads);
+
 /* Forward Euler of source/test.f90:104-117. */
 void vpmo_euler(double* xp, double* qp, const double* up, const double* gp, int nvr, double dt,
                 const double uinf[3]);

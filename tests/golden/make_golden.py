@@ -7,8 +7,17 @@ that the reference implements in source/test_applic.f90:2-77
 
 ring16_oracle.npz: one oracle field step on a 16^3 ring case (regression
 snapshot of the checker itself: particle velocities, stretching and field
-norms).  Regenerate with ``python tests/golden/make_golden.py``.
+norms).
+
+particles_ring16.bin: the 16^3 ring particles in the particles.bin format
+that source/test.f90:24-33 reads (Fortran sequential unformatted: NVR as a
+4-byte integer, Vref, then one record X Y Z w1 w2 w3 per particle), written
+here with ``struct`` -- independently of the library -- with Vref = the
+particle volume and w = -QP(1:3) / Vref.
+
+Regenerate with ``python tests/golden/make_golden.py``.
 """
+import struct
 import os
 import sys
 
@@ -38,6 +47,19 @@ def hill(X, Y, Z, a=1.0, us=-1.0):
     return np.stack([ur * erx, ur * ery, uz]), np.stack([om * ephx, om * ephy, 0 * om])
 
 
+def fortran_records(path, records):
+    """Sequential unformatted records, each framed by its 4-byte length."""
+    with open(path, "wb") as f:
+        for r in records:
+            f.write(struct.pack("<i", len(r)) + r + struct.pack("<i", len(r)))
+
+
+def particles_bin(path, xp, w, vref):
+    recs = [struct.pack("<i", xp.shape[0]), struct.pack("<d", vref)]
+    recs += [struct.pack("<6d", *xp[i], *w[i]) for i in range(xp.shape[0])]
+    fortran_records(path, recs)
+
+
 def main():
     rng = np.random.default_rng(31)
     pts = rng.uniform(-1.6, 1.6, (256, 3))
@@ -46,6 +68,8 @@ def main():
     from oracle import oracle as O
     from vpm_free_gb300 import workloads as W
     xp, qp, wk = W.scaled_ring(16)
+    vref = float(qp[0, 3])
+    particles_bin(os.path.join(HERE, "particles_ring16.bin"), xp, -qp[:, :3] / vref, vref)
     cfg = O.make_config(dpm=wk["dpm"], box=wk["box"])
     s = O.define_sizes(cfg, xp)
     up, gp = O.step_fields(cfg, s, xp, qp, nthreads=1)

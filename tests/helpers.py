@@ -16,3 +16,20 @@ def configs_for(w, **kw):
     args = dict(dpm=w["dpm"], box=w["box"])
     args.update(kw)
     return O.make_config(**args), VPMConfig.make(**args)
+
+
+def fortran_records(path):
+    """Payloads of a Fortran sequential unformatted file (4-byte length markers)."""
+    import struct
+    out = []
+    with open(path, "rb") as f:
+        data = f.read()
+    pos = 0
+    while pos < len(data):
+        (n,) = struct.unpack_from("<i", data, pos)
+        rec = data[pos + 4:pos + 4 + n]
+        (m,) = struct.unpack_from("<i", data, pos + 4 + n)
+        assert m == n, "broken record marker"
+        out.append(rec)
+        pos += 8 + n
+    return out

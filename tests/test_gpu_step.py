@@ -181,3 +181,25 @@ def test_two_level_ncoarse2_matches_oracle(gpulib, oracle):
         for name, fid in (("sol", O.F_SOL), ("vel", O.F_VEL)):
             assert rel_l2(h.field(name).ravel(), O.get_field(fid)) <= FIELD_TOL, name
     assert rel_l2(up, up_o) <= PART_TOL and rel_l2(gp, gp_o) <= PART_TOL
+
+
+def test_viscous_diffusion_matches_oracle(gpulib, oracle):
+    """vpm(WhatToDo = 5): deposition, diffuse_vort_3d and the GP gather of
+    back_to_particles_3D(itype = 2) (source/vpm.f90:345-372)."""
+    from vpm_free_gb300 import workloads as W
+    V, O = gpulib, oracle
+    xp, qp, w = W.scaled_ring(32)
+    ocfg, gcfg = configs_for(w)
+    s = O.define_sizes(ocfg, xp)
+    ni = -0.1  # NI_in of source/test.f90:17
+    gp_o = O.diffuse(ocfg, s, xp, qp, ni)
+    with V.VPM(gcfg) as h:
+        h.vpm(xp, qp, None, None, xp.shape[0], WhatToDo=0)
+        up = np.full((xp.shape[0], 3), 7.0)
+        gp = np.zeros((xp.shape[0], 3))
+        h.vpm(np.ascontiguousarray(xp), np.ascontiguousarray(qp), up, gp, xp.shape[0], WhatToDo=5, NI=ni)
+        assert np.all(up == 7.0)  # itype 2 leaves UP alone
+        assert rel_l2(h.field("rhs").ravel(), O.get_field(O.F_RHS)) <= FIELD_TOL
+        assert rel_l2(h.field("sol").ravel(), O.get_field(O.F_SOL)) <= FIELD_TOL
+    assert rel_l2(gp, gp_o) <= PART_TOL
+    assert np.abs(gp).max() > 0

@@ -23,7 +23,8 @@ import os
 
 import numpy as np
 
-__all__ = ["VPMConfig", "VPM", "VPMError", "read_pm_inp", "load_library", "library_path", "FIELDS"]
+__all__ = ["VPMConfig", "VPM", "VPMError", "read_pm_inp", "read_particles_bin", "write_particles_bin", "load_library",
+           "library_path", "FIELDS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
@@ -36,6 +37,7 @@ EXPORTS = [
     "vpmg_set_particles", "vpmg_get_particles", "vpmg_get_particle_velocity", "vpmg_step", "vpmg_remesh_device",
     "vpmg_num_particles", "vpmg_get_field", "vpmg_kernel_launches", "vpmg_phase_times", "vpmg_tree_stats",
     "vpmg_set_profiling", "vpmg_set_operator_budget", "vpmg_run", "vpmg_bench_kernel", "vpmg_fp64_peak", "vpmg_batch_run",
+    "vpmg_read_particles_bin", "vpmg_write_particles_bin", "vpmg_write_solution", "vpmg_write_hist", "vpmg_set_output",
     "vpmg_dst_tiles", "vpmg_apply_poisson", "vpmg_adjoint_poisson", "vpmg_vjp_fields", "vpmg_vjp_remesh", "vpmg_adjoint_loss",
     "vpmg_adjoint_run",
 ]
@@ -54,7 +56,7 @@ class VPMConfig(C.Structure):
         ("epsvol", C.c_double), ("ncoarse", C.c_int), ("nbi", C.c_int), ("nbj", C.c_int), ("nbk", C.c_int),
         ("nremesh", C.c_int), ("ncell_rem", C.c_int), ("iyntree", C.c_int), ("ilevmax", C.c_int),
         ("ompthreads", C.c_int), ("idefine", C.c_int), ("iynslice", C.c_int), ("use_box", C.c_int),
-        ("box", C.c_double * 6),
+        ("box", C.c_double * 6), ("ipmwrite", C.c_int), ("ipmwstart", C.c_int * 10), ("ipmwsteps", C.c_int * 10),
     ]
 
     @classmethod
@@ -131,6 +133,11 @@ def load_library():
     L.vpmg_fp64_peak.argtypes = [C.c_void_p, _dp]
     L.vpmg_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_double, C.c_int, _dp,
                                  C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.vpmg_read_particles_bin.argtypes = [C.c_char_p, C.POINTER(C.c_int), _dp, _dp, _dp, C.c_int]
+    L.vpmg_write_particles_bin.argtypes = [C.c_char_p, C.c_int, C.c_double, _dp, _dp]
+    L.vpmg_write_solution.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+    L.vpmg_write_hist.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+    L.vpmg_set_output.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
     L.vpmg_dst_tiles.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     L.vpmg_apply_poisson.argtypes = [C.c_void_p, _dp, _dp]
     L.vpmg_adjoint_poisson.argtypes = [C.c_void_p, _dp, _dp]
@@ -161,6 +168,30 @@ def read_pm_inp(path):
     if rc != 0:
         raise VPMError(rc, f"cannot parse {path}")
     return cfg
+
+
+def read_particles_bin(path):
+    """particles.bin (source/test.f90:24-37) -> (XP (NVR,3), QP (NVR,4), Vref),
+    QP[:, :3] = -w * Vref and QP[:, 3] = Vref.  Needs no GPU."""
+    L = load_library()
+    n, vref = C.c_int(0), C.c_double(0.0)
+    rc = L.vpmg_read_particles_bin(os.fsencode(path), C.byref(n), C.byref(vref), None, None, 0)
+    if rc != 0:
+        raise VPMError(rc, f"cannot read {path}")
+    xp, qp = np.zeros((max(n.value, 1), 3)), np.zeros((max(n.value, 1), 4))
+    rc = L.vpmg_read_particles_bin(os.fsencode(path), C.byref(n), C.byref(vref), _p(xp), _p(qp), xp.shape[0])
+    if rc != 0:
+        raise VPMError(rc, f"cannot read {path}")
+    return xp[:n.value], qp[:n.value], vref.value
+
+
+def write_particles_bin(path, XP, QP, vref):
+    """Writes particles.bin so that read_particles_bin returns XP, QP[:, :3] (QP[:, 3] = vref)."""
+    L = load_library()
+    n = XP.shape[0]
+    rc = L.vpmg_write_particles_bin(os.fsencode(path), n, float(vref), _p(_f64(XP, (n, 3))), _p(_f64(QP, (n, 4))))
+    if rc != 0:
+        raise VPMError(rc, f"cannot write {path}")
 
 
 class VPM:
@@ -349,6 +380,21 @@ class VPM:
         a, b, c = C.c_longlong(0), C.c_longlong(0), C.c_int(0)
         self._chk(self._L.vpmg_tree_stats(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return {"interactions": a.value, "bytes": b.value, "precomputed": bool(c.value)}
+
+    def write_solution(self, ntime, directory=None):
+        """NNNNNsolution.bin of the last field step (writesol, source/vpm.f90:662-709)."""
+        d = os.fsencode(directory) if directory else None
+        self._chk(self._L.vpmg_write_solution(self._h, d, int(ntime)))
+
+    def write_hist(self, ntime, directory=None):
+        """Appends the nine velocity lines to NNhist.bin (writeline, source/vpm.f90:789-833)."""
+        d = os.fsencode(directory) if directory else None
+        self._chk(self._L.vpmg_write_hist(self._h, d, int(ntime)))
+
+    def set_output(self, directory=None, solution=True, hist=True):
+        """The writers vpm(WhatToDo = 2) calls after the velocity, as the reference does."""
+        d = os.fsencode(directory) if directory else None
+        self._chk(self._L.vpmg_set_output(self._h, d, (1 if solution else 0) | (2 if hist else 0)))
 
     def dst_tiles(self):
         """Autotuned DST tile shapes (line pairs per CTA) of the block x/y, inner-box x/y and coarse x/y plans."""

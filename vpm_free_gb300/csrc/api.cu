@@ -14,6 +14,7 @@
 #include <string>
 
 #include "handle.h"
+#include "io_files.h"
 
 using namespace vpmg;
 
@@ -431,7 +432,13 @@ int vpmg_read_pm_inp(const char* path, vpmg_config* c) {
     if (!rec(1, v)) return VPMG_ERR_ARG; c->idefine = std::stoi(v[0]);
     if (!rec(1, v)) return VPMG_ERR_ARG; c->iynslice = std::stoi(v[0]);
     if (!rec(1, v)) return VPMG_ERR_ARG;
-    if (std::stoi(v[0]) > 10) return VPMG_ERR_ARG;  // IPMWRITE > 10 stops the reference (vpm.f90:146)
+    c->ipmwrite = std::stoi(v[0]);
+    if (c->ipmwrite > 10) return VPMG_ERR_ARG;  // IPMWRITE > 10 stops the reference (vpm.f90:146)
+    for (int i = 0; i < c->ipmwrite; ++i) {
+      if (!rec(2, v)) return VPMG_ERR_ARG;
+      c->ipmwstart[i] = std::stoi(v[0]);
+      c->ipmwsteps[i] = std::stoi(v[1]);
+    }
   } catch (...) {
     return VPMG_ERR_ARG;
   }
@@ -788,9 +795,85 @@ int vpmg_remesh_device(vpmg_handle* h) {
   });
 }
 
+}  // extern "C"
+
+namespace {
+// writesol: the resident velocity and RHS (last field step) on the host.
+void solution_file(vpmg_handle* h, const char* dir, int ntime) {
+  VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
+  const size_t N = h->gglob.count();
+  std::vector<double> vel(3 * N), rhs(3 * N);
+  VPMG_CUDA(cudaMemcpyAsync(vel.data(), h->vel.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->stream));
+  VPMG_CUDA(cudaMemcpyAsync(rhs.data(), h->rhs.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->stream));
+  VPMG_CUDA(cudaStreamSynchronize(h->stream));
+  io::SolutionView v{};
+  v.vel = vel.data();
+  v.rhs = rhs.data();
+  for (int d = 0; d < 3; ++d) { v.nn[d] = h->sz.nn[d]; v.xmin[d] = h->sz.xbound[d]; v.d[d] = h->sz.dpm[d]; }
+  for (int d = 0; d < 6; ++d) v.nn_bl[d] = h->sz.nn_bl[d];
+  const int st = io::write_solution(dir, ntime, v);
+  VPMG_CHECK(st == VPMG_OK, st, "cannot write the solution file");
+}
+
+// writeline: the nine velocity lines along x of the block range.
+void hist_file(vpmg_handle* h, const char* dir, int ntime) {
+  VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
+  const vpmg_sizes& s = h->sz;
+  int jk[9][2];
+  io::hist_lines(s.nn_bl, jk);
+  const int nl = s.nn_bl[3] - s.nn_bl[0] + 1;
+  const size_t N = h->gglob.count();
+  std::vector<double> lines((size_t)27 * nl);
+  for (int l = 0; l < 9; ++l) {
+    const int j = jk[l][0], k = jk[l][1];
+    VPMG_CHECK(j >= 1 && j <= s.nn[1] && k >= 1 && k <= s.nn[2], VPMG_ERR_UNSUPPORTED,
+               "mesh too small for the reference's hist lines");
+    const size_t base = (size_t)(s.nn_bl[0] - 1) + (size_t)s.nn[0] * ((size_t)(j - 1) + (size_t)s.nn[1] * (k - 1));
+    for (int c = 0; c < 3; ++c)
+      VPMG_CUDA(cudaMemcpyAsync(lines.data() + ((size_t)l * 3 + c) * nl, h->vel.p + (size_t)c * N + base,
+                                sizeof(double) * nl, cudaMemcpyDeviceToHost, h->stream));
+  }
+  VPMG_CUDA(cudaStreamSynchronize(h->stream));
+  io::HistView v{};
+  v.lines = lines.data();
+  for (int d = 0; d < 3; ++d) { v.xmin[d] = s.xbound[d]; v.d[d] = s.dpm[d]; }
+  for (int d = 0; d < 6; ++d) v.nn_bl[d] = s.nn_bl[d];
+  const int st = io::write_hist(dir, ntime, v);
+  VPMG_CHECK(st == VPMG_OK, st, "cannot write the hist files");
+}
+
+// The writers of vpm(WhatToDo = 2) after the velocity (vpm.f90:276-284).
+void step_writers(vpmg_handle* h, int ntime) {
+  const char* dir = h->out_dir.empty() ? nullptr : h->out_dir.c_str();
+  if (h->out_flags & 1) {
+    bool hit = false;
+    for (int i = 0; i < h->cfg.ipmwrite && i < 10; ++i)
+      hit = hit || (ntime >= h->cfg.ipmwstart[i] && ntime <= h->cfg.ipmwstart[i] + h->cfg.ipmwsteps[i]);
+    if (hit) solution_file(h, dir, ntime);
+  }
+  if (h->out_flags & 2) hist_file(h, dir, ntime);
+}
+}  // namespace
+
+extern "C" {
+
+int vpmg_write_solution(vpmg_handle* h, const char* dir, int ntime) {
+  return guarded(h, [&] { solution_file(h, dir, ntime); });
+}
+
+int vpmg_write_hist(vpmg_handle* h, const char* dir, int ntime) {
+  return guarded(h, [&] { hist_file(h, dir, ntime); });
+}
+
+int vpmg_set_output(vpmg_handle* h, const char* dir, int flags) {
+  if (!h || flags < 0 || flags > 3) return VPMG_ERR_ARG;
+  h->out_dir = dir ? dir : "";
+  h->out_flags = flags;
+  return VPMG_OK;
+}
+
 int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int* nvr, int neqpm, int whattodo,
              int ntime, double ni, int nvrm) {
-  (void)ni;
   return guarded(h, [&] {
     VPMG_CHECK(nvr, VPMG_ERR_ARG, "NVR is null");
     VPMG_CHECK(neqpm == 3, VPMG_ERR_UNSUPPORTED, "neqpm must be 3");
@@ -805,12 +888,35 @@ int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int
       }
       return;
     }
-    VPMG_CHECK(whattodo == 2, VPMG_ERR_UNSUPPORTED, "WhatToDo 1, 4, 5 are outside the single-block step");
+    VPMG_CHECK(whattodo == 2 || whattodo == 5, VPMG_ERR_UNSUPPORTED, "WhatToDo 1 and 4 are not built");
     if (*nvr == 0) return;  // vpm.f90:171
+    if (whattodo == 5) {
+      // vpm.f90:345-372: deposition, diffuse_vort_3d, back_to_particles_3D(itype = 2)
+      VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes (WhatToDo = 0) must come first");
+      VPMG_CHECK(gp, VPMG_ERR_ARG, "GP is null");
+      upload_particles(h, xp, qp, *nvr);
+      const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
+      bin_particles(h->parts, mg, h->bins, h->stream);
+      const size_t N = h->gglob.count();
+      double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
+      double* S[3] = {comp(h->sol, N, 0), comp(h->sol, N, 1), comp(h->sol, N, 2)};
+      deposit(h->parts, mg, h->bins, R, h->stream);
+      viscous_diffusion(h->sz.nn, h->sz.nn_bl, h->sz.dpm, ni, R, S, h->stream);
+      const double* Vp[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
+      const double* Sp[3] = {S[0], S[1], S[2]};
+      const double u0[3] = {0, 0, 0};
+      m2p(h->parts, mg, h->bins, Vp, Sp, true, false, 0.0, u0, h->stream);  // GP = vol I(X) SOL; UP untouched
+      VPMG_CUDA(cudaMemcpyAsync(gp, h->parts.gp.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost,
+                                h->stream));
+      VPMG_CUDA(cudaStreamSynchronize(h->stream));
+      check_particle_errors(h->bins, h->stream);
+      return;
+    }
     upload_particles(h, xp, qp, *nvr);
     const double u0[3] = {0, 0, 0};
     bin_particles(h->parts, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
     field_step(h);
+    if (h->out_flags) step_writers(h, ntime);
     m2p_step(h, true, false, 0.0, u0);
     VPMG_CUDA(cudaMemcpyAsync(up, h->parts.up.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost, h->stream));
     VPMG_CUDA(cudaMemcpyAsync(gp, h->parts.gp.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost, h->stream));

@@ -117,6 +117,32 @@ __global__ void k_deformation(const double* __restrict__ r0, const double* __res
   }
 }
 
+// diffuse_vort_3d (source/vpm_gcalc.f90:138-210), neqpm = 3 (VIS = NI):
+// SOL(m) = -NI Lap_h RHS(m) on the nodes strictly inside [lo, hi] (0-based);
+// SOL is zero elsewhere (cleared by the caller).
+__global__ void k_diffuse(const double* __restrict__ r0, const double* __restrict__ r1, const double* __restrict__ r2,
+                          int NX, int NY, int lo0, int lo1, int lo2, int e0, int e1, int e2, double idx2, double idy2,
+                          double idz2, double ni, double* __restrict__ s0, double* __restrict__ s1,
+                          double* __restrict__ s2) {
+  const size_t n = (size_t)e0 * e1 * e2;
+  const size_t sy = NX, sz = (size_t)NX * NY;
+  const double* R[3] = {r0, r1, r2};
+  double* S[3] = {s0, s1, s2};
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int i = lo0 + (int)(t % e0), j = lo1 + (int)((t / e0) % e1), k = lo2 + (int)(t / ((size_t)e0 * e1));
+    const size_t id = (size_t)i + sy * j + sz * k;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const double* r = R[m];
+      const double c = r[id];
+      const double dxx = ((r[id + 1] - 2.0 * c) + r[id - 1]) * idx2;
+      const double dyy = ((r[id + sy] - 2.0 * c) + r[id - sy]) * idy2;
+      const double dzz = ((r[id + sz] - 2.0 * c) + r[id - sz]) * idz2;
+      S[m][id] = -ni * ((dxx + dyy) + dzz);
+    }
+  }
+}
+
 template <class T>
 void upload(DBuf<T>& b, const std::vector<T>& h) {
   b.ensure(h.size());
@@ -187,6 +213,21 @@ void yaps_face_interp(const YapsDev& Y, const int cdims[3], const double* const 
                                                          Y.nface, csol[c], samp[c], cdims[0], cdims[1], sbl[c]);
     VPMG_LAUNCHED();
   }
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void viscous_diffusion(const int dims[3], const int nn_bl[6], const double h[3], double ni, const double* const rhs[3],
+                       double* const sol[3], cudaStream_t s) {
+  // interior of the block range: 1-based NXs_bl+1 .. NXf_bl-1 -> 0-based nn_bl[d] .. nn_bl[d+3]-2
+  const int lo[3] = {nn_bl[0], nn_bl[1], nn_bl[2]};
+  const int e[3] = {nn_bl[3] - nn_bl[0] - 1, nn_bl[4] - nn_bl[1] - 1, nn_bl[5] - nn_bl[2] - 1};
+  for (int c = 0; c < 3; ++c) fill_zero(sol[c], (size_t)dims[0] * dims[1] * dims[2], s);
+  if (e[0] <= 0 || e[1] <= 0 || e[2] <= 0) return;
+  const size_t n = (size_t)e[0] * e[1] * e[2];
+  k_diffuse<<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 32), 256, 0, s>>>(
+      rhs[0], rhs[1], rhs[2], dims[0], dims[1], lo[0], lo[1], lo[2], e[0], e[1], e[2], 1.0 / (h[0] * h[0]),
+      1.0 / (h[1] * h[1]), 1.0 / (h[2] * h[2]), ni, sol[0], sol[1], sol[2]);
+  VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
 

@@ -21,6 +21,9 @@ void yaps_coarse_rhs(const YapsDev& Y, const int cdims[3], const double dc[3], c
                      double* const crhs[3], cudaStream_t s);
 void yaps_face_interp(const YapsDev& Y, const int cdims[3], const double* const csol[3], const double* const samp[3],
                       double* const sbl[3], cudaStream_t s);
+// diffuse_vort_3d: sol = -ni Lap_h rhs inside the block range nn_bl (1-based), zero elsewhere.
+void viscous_diffusion(const int dims[3], const int nn_bl[6], const double h[3], double ni, const double* const rhs[3],
+                       double* const sol[3], cudaStream_t s);
 void velocity_and_stretching(const int dims[3], const double h[3], const double* const psi[3], const double* const rhs[3],
                              double* const vel[3], double* const def[3], cudaStream_t s);
 

@@ -52,6 +52,9 @@ struct vpmg_handle {
   vpmg::DBuf<int> hist, hist_counter;
   double phase_ms[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   AdjointState* adj = nullptr;
+  // writers called by vpm(WhatToDo = 2): bit 0 solution windows, bit 1 hist lines
+  std::string out_dir;
+  int out_flags = 0;
 };
 
 namespace vpmg {

@@ -26,6 +26,7 @@ module vpmg_c
      integer(c_int)  :: ncoarse, nbi, nbj, nbk, nremesh, ncell_rem, iyntree, ilevmax
      integer(c_int)  :: ompthreads, idefine, iynslice, use_box
      real(c_double)  :: box(6)
+     integer(c_int)  :: ipmwrite, ipmwstart(10), ipmwsteps(10)
   end type vpmg_config
 
   type, bind(C) :: vpmg_sizes
@@ -83,6 +84,13 @@ module vpmg_c
        import :: c_ptr
        type(c_ptr), value :: h
      end function vpmg_last_error
+
+     integer(c_int) function vpmg_set_output(h, dir, flags) bind(C, name="vpmg_set_output")
+       import :: c_int, c_ptr, c_char
+       type(c_ptr), value :: h
+       character(kind=c_char), dimension(*) :: dir
+       integer(c_int), value :: flags
+     end function vpmg_set_output
   end interface
 end module vpmg_c
 
@@ -152,6 +160,8 @@ contains
     if (.not. c_associated(vpmg_h)) then
        call check(vpmg_read_pm_inp('pm.inp'//c_null_char, cfg), 'pm.inp')
        call check(vpmg_create(cfg, -1_c_int, vpmg_h), 'vpmg_create')
+       ! the reference's writers after the velocity: solution windows and hist lines
+       call check(vpmg_set_output(vpmg_h, '.'//c_null_char, 3_c_int), 'vpmg_set_output')
     end if
     nvr = NVR_in
     if (WhatToDo == 0) then
