@@ -86,7 +86,10 @@ const char* vpmg_status_string(int status);
 /* ---- the reference's driver call --------------------------------------- */
 /* vpm(XP,QP,UP,GP,NVR,neqpm,WhatToDo,RHS_pm,velx,vely,velz,NTIME,NI,NVRM)
  * (source/vpm.f90:54-475).  WhatToDo 0 = read sizes (define_sizes, with
- * the pm.inp already given to vpmg_create), 2 = field step: UP is
+ * the pm.inp already given to vpmg_create), 1 = Poisson solve and velocity
+ * field only (read it with vpmg_get_field; UP/GP untouched), 4 = stretching
+ * from a new deposition and the resident velocity, then UP/GP (no solve),
+ * 2 = field step: UP is
  * overwritten with the interpolated velocity and GP with the stretching
  * term times the particle volume (vpm_time.f90:62-107); 5 = viscous
  * diffusion (vpm.f90:345-372): GP = volume x interpolated -NI Lap_h RHS

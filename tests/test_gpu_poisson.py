@@ -5,6 +5,8 @@ right-hand sides; the oracle restates MKL's 7-point Dirichlet semantics
 (source/pmsolve.f90:284-432) and the tree boundary values.
 Tolerance: relative L2 <= 1e-10 (fields), as the spec parity bar.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -53,3 +55,32 @@ def test_infinite_domain_matches_oracle(gpulib, oracle, n, levmax):
         hd.pmesh(out, rhs, xb, (h, h, h), iynbc=1, itree=1, levmax=levmax)
     for c in range(3):
         assert rel_l2(out[c], ref[c]) <= 1e-10, c
+
+
+def test_dst_tile_shape_does_not_change_results(gpulib):
+    """The autotuned tile (line pairs per CTA) must not change a single bit:
+    the same Dirichlet solve with each tile forced through VPMG_DST_PAIRS,
+    in separate processes (the choice is read once per process).  Lines of
+    18, 20, 34 and 40 points take the real-symmetric form (34 = 2 x 17),
+    81 and 85 the odd extension."""
+    import hashlib
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = (
+        "import hashlib, numpy as np, vpm_free_gb300 as V\n"
+        "rng = np.random.default_rng(5)\n"
+        "for nz, ny, nx in ((23, 21, 19), (30, 41, 35), (20, 86, 82)):\n"
+        "    R = [rng.normal(size=(nz, ny, nx)) for _ in range(3)]\n"
+        "    S = [np.zeros_like(R[0]) for _ in range(3)]\n"
+        "    S[0][0] = 1.0\n"
+        "    with V.VPM(V.VPMConfig.make()) as h:\n"
+        "        h.pmesh(S, R, [0, 0, 0, 1, 1, 1], [0.1, 0.11, 0.09], 0)\n"
+        "    print(hashlib.sha256(b''.join(s.tobytes() for s in S)).hexdigest())\n")
+    outs = []
+    for pairs in ("2", "4", "8"):
+        env = dict(os.environ, VPMG_DST_PAIRS=pairs)
+        r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        outs.append(r.stdout.split())
+    assert outs[0] == outs[1] == outs[2] and len(outs[0]) == 3

@@ -203,3 +203,31 @@ def test_viscous_diffusion_matches_oracle(gpulib, oracle):
         assert rel_l2(h.field("sol").ravel(), O.get_field(O.F_SOL)) <= FIELD_TOL
     assert rel_l2(gp, gp_o) <= PART_TOL
     assert np.abs(gp).max() > 0
+
+
+def test_whattodo_1_and_4(gpulib):
+    """WhatToDo 1 (solve + velocity field only) and 4 (stretching from the
+    resident velocity, then UP/GP) reproduce the pieces of WhatToDo 2."""
+    from vpm_free_gb300 import workloads as W
+    V = gpulib
+    xp, qp, w = W.scaled_ring(32)
+    _, gcfg = configs_for(w)
+    n = xp.shape[0]
+    x, q = np.ascontiguousarray(xp), np.ascontiguousarray(qp)
+    with V.VPM(gcfg) as h:
+        h.vpm(xp, qp, None, None, n, WhatToDo=0)
+        up2, gp2 = np.zeros((n, 3)), np.zeros((n, 3))
+        h.vpm(x, q, up2, gp2, n, WhatToDo=2)
+        vel2 = h.field("vel")
+        up1, gp1 = np.full((n, 3), 3.0), np.full((n, 3), 3.0)
+        h.vpm(x, q, up1, gp1, n, WhatToDo=1)
+        assert np.array_equal(h.field("vel"), vel2)
+        assert np.all(up1 == 3.0) and np.all(gp1 == 3.0)
+        up4, gp4 = np.zeros((n, 3)), np.zeros((n, 3))
+        h.vpm(x, q, up4, gp4, n, WhatToDo=4)
+        assert np.array_equal(up4, up2) and np.array_equal(gp4, gp2)
+        # new particles: GP from their own deposition and the kept velocity
+        x2 = x + 0.3 * np.asarray(w["dpm"])
+        h.vpm(np.ascontiguousarray(x2), q, up4, gp4, n, WhatToDo=4)
+        assert np.array_equal(h.field("vel"), vel2)
+        assert not np.array_equal(gp4, gp2)

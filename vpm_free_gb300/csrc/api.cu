@@ -888,8 +888,43 @@ int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int
       }
       return;
     }
-    VPMG_CHECK(whattodo == 2 || whattodo == 5, VPMG_ERR_UNSUPPORTED, "WhatToDo 1 and 4 are not built");
+    VPMG_CHECK(whattodo == 1 || whattodo == 2 || whattodo == 4 || whattodo == 5, VPMG_ERR_UNSUPPORTED,
+               "WhatToDo must be 0, 1, 2, 4 or 5");
     if (*nvr == 0) return;  // vpm.f90:171
+    if (whattodo == 1 || whattodo == 4) {
+      // 1 (vpm.f90:221-262): Poisson solve and the velocity field only
+      //   (calc_velocity_serial_3d(0)); no particle output -- the field is
+      //   read with vpmg_get_field.
+      // 4 (vpm.f90:316-343): no solve; stretching from the new deposition
+      //   and the resident velocity (calc_velocity_serial_3d(-1)), then UP
+      //   and GP (back_to_particles_3D(itype = 1)).
+      VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes (WhatToDo = 0) must come first");
+      upload_particles(h, xp, qp, *nvr);
+      const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
+      bin_particles(h->parts, mg, h->bins, h->stream);
+      const size_t N = h->gglob.count();
+      double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
+      double* S[3] = {comp(h->sol, N, 0), comp(h->sol, N, 1), comp(h->sol, N, 2)};
+      double* Vv[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
+      double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
+      deposit(h->parts, mg, h->bins, R, h->stream);
+      if (whattodo == 1) {
+        poisson_part(h);
+        velocity_and_stretching(h->sz.nn, h->sz.dpm, S, R, Vv, G, h->stream, 1);
+      } else {
+        VPMG_CHECK(up && gp, VPMG_ERR_ARG, "UP or GP is null");
+        velocity_and_stretching(h->sz.nn, h->sz.dpm, S, R, Vv, G, h->stream, 2);
+        const double u0[3] = {0.0, 0.0, 0.0};
+        m2p_step(h, true, false, 0.0, u0);
+        VPMG_CUDA(cudaMemcpyAsync(up, h->parts.up.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost,
+                                  h->stream));
+        VPMG_CUDA(cudaMemcpyAsync(gp, h->parts.gp.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost,
+                                  h->stream));
+      }
+      VPMG_CUDA(cudaStreamSynchronize(h->stream));
+      check_particle_errors(h->bins, h->stream);
+      return;
+    }
     if (whattodo == 5) {
       // vpm.f90:345-372: deposition, diffuse_vort_3d, back_to_particles_3D(itype = 2)
       VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes (WhatToDo = 0) must come first");

@@ -232,15 +232,15 @@ void viscous_diffusion(const int dims[3], const int nn_bl[6], const double h[3],
 }
 
 void velocity_and_stretching(const int dims[3], const double h[3], const double* const psi[3], const double* const rhs[3],
-                             double* const vel[3], double* const def[3], cudaStream_t s) {
+                             double* const vel[3], double* const def[3], cudaStream_t s, int parts) {
   const int NX = dims[0], NY = dims[1], NZ = dims[2];
   const double i2x = 1.0 / (2 * h[0]), i2y = 1.0 / (2 * h[1]), i2z = 1.0 / (2 * h[2]);
-  if (NX > 2 && NY > 2 && NZ > 2) {
+  if ((parts & 1) && NX > 2 && NY > 2 && NZ > 2) {
     const size_t n = (size_t)(NX - 2) * (NY - 2) * (NZ - 2);
     k_velocity<<<grid_for(n, 256), 256, 0, s>>>(psi[0], psi[1], psi[2], NX, NY, NZ, i2x, i2y, i2z, vel[0], vel[1], vel[2]);
     VPMG_LAUNCHED();
   }
-  if (NX > 4 && NY > 4 && NZ > 4) {
+  if ((parts & 2) && NX > 4 && NY > 4 && NZ > 4) {
     const size_t n = (size_t)(NX - 4) * (NY - 4) * (NZ - 4);
     k_deformation<<<grid_for(n, 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], vel[0], vel[1], vel[2], NX, NY, NZ, i2x, i2y,
                                                    i2z, def[0], def[1], def[2]);

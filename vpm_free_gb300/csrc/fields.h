@@ -24,7 +24,9 @@ void yaps_face_interp(const YapsDev& Y, const int cdims[3], const double* const 
 // diffuse_vort_3d: sol = -ni Lap_h rhs inside the block range nn_bl (1-based), zero elsewhere.
 void viscous_diffusion(const int dims[3], const int nn_bl[6], const double h[3], double ni, const double* const rhs[3],
                        double* const sol[3], cudaStream_t s);
+// calc_velocity_serial_3d: parts bit 0 = velocity (curl psi), bit 1 = stretching
+// (from rhs and the velocity in vel); idcalc 1 = both, 0 = velocity, -1 = stretching.
 void velocity_and_stretching(const int dims[3], const double h[3], const double* const psi[3], const double* const rhs[3],
-                             double* const vel[3], double* const def[3], cudaStream_t s);
+                             double* const vel[3], double* const def[3], cudaStream_t s, int parts = 3);
 
 }  // namespace vpmg

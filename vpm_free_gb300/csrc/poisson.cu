@@ -33,15 +33,10 @@ namespace vpmg {
 namespace {
 
 // Tile shape: a CTA of kThreads transforms PAIRS line pairs (2 * PAIRS real
-// lines).  PAIRS is 2, 4 or 8, chosen per plan by timing (tune_pairs).
+// lines).  PAIRS is 2, 4 or 8, chosen per plan by timing (tune_pairs); the
+// values computed do not depend on it.
 constexpr int kThreads = 128;
 constexpr int kDefaultPairs = 4;
-template <int PAIRS>
-struct Tile {
-  static constexpr int lanes = kThreads / (2 * PAIRS);  // threads per line in the real-symmetric prefix sum
-  static_assert(kThreads % (2 * PAIRS) == 0 && lanes <= 32 && (lanes & (lanes - 1)) == 0,
-                "the prefix sum splits a warp into whole power-of-two lane groups, one per line");
-};
 constexpr int kMaxOddRadix = 17;  // largest odd prime radix (2*(cells) must factor into 2..17)
 
 __constant__ double c_rcos[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
@@ -246,9 +241,11 @@ __device__ __forceinline__ void rs_pre(const double2* __restrict__ L, double2* _
 // Z_{N-m} = c + id the two lines' spectra are F = ((a+c) + i(b-d))/2 and
 // G = ((b+d) - i(a-c))/2, so X_{2m} = (d-b)/2 and (a-c)/2, and the odd
 // outputs are the prefix sums of r_0 = Z_0 / 2, r_m = ((a+c)/2, (b+d)/2).
-// O[pair * M + k] receives X_k of both lines, k = 1..n.
-template <int LANES>
-__device__ __forceinline__ void rs_post(const double2* __restrict__ Z, double2* __restrict__ O, const FFTDev& p,
+// O[pair * M + k] receives X_k of both lines, k = 1..n.  The prefix sum
+// runs over kScanSegs fixed segments of each line in a fixed order, so the
+// result does not depend on the tile shape; Z is its scratch afterwards.
+constexpr int kScanSegs = 32;
+__device__ __forceinline__ void rs_post(double2* __restrict__ Z, double2* __restrict__ O, const FFTDev& p,
                                         int npair) {
   const int H = p.N >> 1;
   for (int t = threadIdx.x; t < npair * H; t += blockDim.x) {
@@ -263,24 +260,39 @@ __device__ __forceinline__ void rs_post(const double2* __restrict__ Z, double2* 
     }
   }
   __syncthreads();
-  // inclusive prefix sum over the odd outputs, LANES threads per line:
-  // each sums a contiguous chunk, the lane group scans the chunk sums
-  const int line = threadIdx.x / LANES, lane = threadIdx.x - line * LANES;
-  double* o = reinterpret_cast<double*>(O + (line >> 1) * p.M) + (line & 1);  // X_k at o[2k]
-  const int C = (H + LANES - 1) / LANES;
-  const int m0 = min(H, lane * C), m1 = min(H, m0 + C);
-  double s = 0.0;
-  for (int m = m0; m < m1; ++m) s += o[2 * (2 * m + 1)];
-  double inc = s;
-#pragma unroll
-  for (int off = 1; off < LANES; off <<= 1) {
-    const double y = __shfl_up_sync(0xffffffffu, inc, off, LANES);
-    if (lane >= off) inc += y;
+  // segments per line: min(kScanSegs, H) -- a function of N only; the
+  // scratch (2 npair S doubles) fits in Z (2 npair M doubles, M >= 2H >= 2S)
+  const int S = min(kScanSegs, H);
+  double* seg = reinterpret_cast<double*>(Z);  // [line][S]
+  const int C = (H + S - 1) / S;
+  const int nls = 2 * npair * S;
+  for (int t = threadIdx.x; t < nls; t += blockDim.x) {  // segment sums
+    const int line = t / S, g = t - line * S;
+    const double* o = reinterpret_cast<const double*>(O + (line >> 1) * p.M) + (line & 1);  // X_k at o[2k]
+    const int m0 = min(H, g * C), m1 = min(H, m0 + C);
+    double s = 0.0;
+    for (int m = m0; m < m1; ++m) s += o[2 * (2 * m + 1)];
+    seg[t] = s;
   }
-  double run = inc - s;
-  for (int m = m0; m < m1; ++m) {
-    run += o[2 * (2 * m + 1)];
-    o[2 * (2 * m + 1)] = run;
+  __syncthreads();
+  for (int line = threadIdx.x; line < 2 * npair; line += blockDim.x) {  // exclusive scan of the segment sums
+    double run = 0.0;
+    for (int g = 0; g < S; ++g) {
+      const double v = seg[line * S + g];
+      seg[line * S + g] = run;
+      run += v;
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nls; t += blockDim.x) {  // inclusive values inside each segment
+    const int line = t / S, g = t - line * S;
+    double* o = reinterpret_cast<double*>(O + (line >> 1) * p.M) + (line & 1);
+    const int m0 = min(H, g * C), m1 = min(H, m0 + C);
+    double run = seg[t];
+    for (int m = m0; m < m1; ++m) {
+      run += o[2 * (2 * m + 1)];
+      o[2 * (2 * m + 1)] = run;
+    }
   }
 }
 
@@ -297,7 +309,7 @@ __device__ __forceinline__ double2* dst_pairs(double2* A, double2* B, const FFTD
   double2* R = fft_all<ODD>(A, B, p, npair);
   if (!p.rs) return R;
   double2* O = (R == A) ? B : A;
-  rs_post<Tile<PAIRS>::lanes>(R, O, p, npair);
+  rs_post(R, O, p, npair);
   __syncthreads();
   return O;
 }
