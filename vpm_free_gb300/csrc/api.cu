@@ -178,7 +178,7 @@ void prepare(vpmg_handle* h) {
 
 MeshDev mesh_dev(const Grid& g, int itype) {
   MeshDev m;
-  for (int k = 0; k < 3; ++k) { m.xmin[k] = g.xmin[k]; m.d[k] = g.d[k]; m.n[k] = g.n[k]; }
+  for (int k = 0; k < 3; ++k) { m.xmin[k] = g.xmin[k]; m.d[k] = g.d[k]; m.inv[k] = 1.0 / g.d[k]; m.n[k] = g.n[k]; }
   m.itype = itype;
   m.ips = (itype == 2) ? 0 : 1;
   m.ipf = (itype == 2) ? 1 : 2;

@@ -164,10 +164,26 @@ __global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict_
     }
     return r;
   };
+  // loads four planes ahead of the dependent chain; same arithmetic order
   double y = rhs(0);
   out[pq] = y;
   double ri = rinv[pq];
-  for (int k = 1; k < m2; ++k) {
+  int k = 1;
+  for (; k + 3 < m2; k += 4) {
+    const size_t id = pq + plane * k;
+    const double q0 = rhs(k), q1 = rhs(k + 1), q2 = rhs(k + 2), q3 = rhs(k + 3);
+    const double r0 = rinv[id], r1 = rinv[id + plane], r2 = rinv[id + 2 * plane], r3 = rinv[id + 3 * plane];
+    y = fma(y, ri, q0);
+    out[id] = y;
+    y = fma(y, r0, q1);
+    out[id + plane] = y;
+    y = fma(y, r1, q2);
+    out[id + 2 * plane] = y;
+    y = fma(y, r2, q3);
+    out[id + 3 * plane] = y;
+    ri = r3;
+  }
+  for (; k < m2; ++k) {
     const size_t id = pq + plane * k;
     y = fma(y, ri, rhs(k));
     out[id] = y;
@@ -175,7 +191,21 @@ __global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict_
   }
   double u = y * ri;
   out[pq + plane * (m2 - 1)] = u;
-  for (int k = m2 - 2; k >= 0; --k) {
+  k = m2 - 2;
+  for (; k - 3 >= 0; k -= 4) {
+    const size_t id = pq + plane * k;
+    const double o0 = out[id], o1 = out[id - plane], o2 = out[id - 2 * plane], o3 = out[id - 3 * plane];
+    const double r0 = rinv[id], r1 = rinv[id - plane], r2 = rinv[id - 2 * plane], r3 = rinv[id - 3 * plane];
+    u = (o0 + u) * r0;
+    out[id] = u;
+    u = (o1 + u) * r1;
+    out[id - plane] = u;
+    u = (o2 + u) * r2;
+    out[id - 2 * plane] = u;
+    u = (o3 + u) * r3;
+    out[id - 3 * plane] = u;
+  }
+  for (; k >= 0; --k) {
     const size_t id = pq + plane * k;
     u = (out[id] + u) * rinv[id];
     out[id] = u;

@@ -109,14 +109,14 @@ __global__ void k_records(const double* __restrict__ x, const double* __restrict
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int c0 = cell_of(pos[d], m.xmin[d], m.d[d]);
-    const double inv = 1.0 / m.d[d];
+    const double inv = m.inv[d];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       const int node = c0 - m.ips + a;  // 0-based node = (i-1) of the reference
       const double t = (pos[d] - m.xmin[d] - (double)node * m.d[d]) * inv;
       r[4 * d + a] = (a <= m.ips + m.ipf) ? proj_fun(m.itype, t) : 0.0;
     }
-    if (d == 0) r[15] = (double)c0;
+    if (d == 0) r[15] = cell_bits(c0);
   }
   r[12] = q0[p];
   r[13] = q1[p];
@@ -146,7 +146,7 @@ __global__ void k_deposit(const int* __restrict__ starts, const double* __restri
       const int s = starts[row + xlo], e = starts[row + xhi + 1];
       for (int t = s; t < e; ++t) {
         const double* r = rec + (size_t)t * kRecLen;
-        const int ix = i - (int)r[15] + m.ips;
+        const int ix = i - record_cell(r) + m.ips;
         if ((unsigned)ix > (unsigned)w) continue;  // only for a binning that does not match rec
         const double f = (r[ix] * r[4 + iy]) * r[8 + iz];
         a0 = fma(f, r[12], a0);
@@ -176,7 +176,7 @@ __global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsor
   double w[12];
 #pragma unroll
   for (int a = 0; a < 12; ++a) w[a] = r[a];
-  const int c0 = (int)r[15];
+  const int c0 = record_cell(r);
   const int cj = cell_of(y[p], m.xmin[1], m.d[1]), ck = cell_of(z[p], m.xmin[2], m.d[2]);
   const int nw = m.ips + m.ipf + 1;
   double u[3] = {0, 0, 0}, gl[3] = {0, 0, 0};

@@ -11,9 +11,22 @@ constexpr int kRecLen = 16;  // doubles per sorted particle record
 // Mesh parameters as the kernels see them (0-based nodes).
 struct MeshDev {
   double xmin[3], d[3];
+  double inv[3];        // 1 / d, computed once on the host (same IEEE quotient)
   int n[3];
   int itype, ips, ipf;  // projection function and stencil extents
 };
+// Cell index of a sorted record (slot 15), stored as the integer's bits.
+__host__ __device__ inline double cell_bits(int c) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)c);
+#else
+  long long v = c;
+  double d;
+  __builtin_memcpy(&d, &v, sizeof(d));
+  return d;
+#endif
+}
+__device__ __forceinline__ int record_cell(const double* r) { return (int)__double_as_longlong(r[15]); }
 
 struct Particles {
   int capacity = 0;

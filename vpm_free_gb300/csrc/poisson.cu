@@ -432,13 +432,31 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict
 }
 
 // z pass: Thomas sweep per (p,q) with the reciprocal pivot table.
+// The column's loads are issued four planes ahead of the dependent FMA
+// chain (the sweep is latency-bound otherwise); the arithmetic and its
+// order are those of the plain recurrence.
 __global__ void k_thomas(double* __restrict__ g, const double* __restrict__ rinv, int m0, int m1, int m2) {
   const int pq = blockIdx.x * blockDim.x + threadIdx.x;
   if (pq >= m0 * m1) return;
   const size_t plane = (size_t)m0 * m1;
   double y = g[pq];
   double ri = rinv[pq];
-  for (int c = 1; c < m2; ++c) {
+  int c = 1;
+  for (; c + 3 < m2; c += 4) {
+    const size_t id = pq + plane * c;
+    const double g0 = g[id], g1 = g[id + plane], g2 = g[id + 2 * plane], g3 = g[id + 3 * plane];
+    const double r0 = rinv[id], r1 = rinv[id + plane], r2 = rinv[id + 2 * plane], r3 = rinv[id + 3 * plane];
+    y = fma(y, ri, g0);
+    g[id] = y;
+    y = fma(y, r0, g1);
+    g[id + plane] = y;
+    y = fma(y, r1, g2);
+    g[id + 2 * plane] = y;
+    y = fma(y, r2, g3);
+    g[id + 3 * plane] = y;
+    ri = r3;
+  }
+  for (; c < m2; ++c) {
     const size_t id = pq + plane * c;
     y = fma(y, ri, g[id]);
     g[id] = y;
@@ -446,7 +464,21 @@ __global__ void k_thomas(double* __restrict__ g, const double* __restrict__ rinv
   }
   double u = y * ri;
   g[pq + plane * (m2 - 1)] = u;
-  for (int c = m2 - 2; c >= 0; --c) {
+  c = m2 - 2;
+  for (; c - 3 >= 0; c -= 4) {
+    const size_t id = pq + plane * c;
+    const double g0 = g[id], g1 = g[id - plane], g2 = g[id - 2 * plane], g3 = g[id - 3 * plane];
+    const double r0 = rinv[id], r1 = rinv[id - plane], r2 = rinv[id - 2 * plane], r3 = rinv[id - 3 * plane];
+    u = (g0 + u) * r0;
+    g[id] = u;
+    u = (g1 + u) * r1;
+    g[id - plane] = u;
+    u = (g2 + u) * r2;
+    g[id - 2 * plane] = u;
+    u = (g3 + u) * r3;
+    g[id - 3 * plane] = u;
+  }
+  for (; c >= 0; --c) {
     const size_t id = pq + plane * c;
     u = (g[id] + u) * rinv[id];
     g[id] = u;
