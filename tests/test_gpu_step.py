@@ -231,3 +231,35 @@ def test_whattodo_1_and_4(gpulib):
         h.vpm(np.ascontiguousarray(x2), q, up4, gp4, n, WhatToDo=4)
         assert np.array_equal(h.field("vel"), vel2)
         assert not np.array_equal(gp4, gp2)
+
+
+def test_leapfrog256_step_matches_oracle(gpulib, oracle):
+    """The headline configuration itself (two rings on the 256^3 mesh,
+    ~2e6 particles): initial remesh, one field step on identical particles
+    (every mesh field and UP/GP), then one full step (field step, Euler,
+    remesh) against the oracle."""
+    from vpm_free_gb300 import workloads as W
+    V, O = gpulib, oracle
+    xp, qp, w = W.leapfrog256()
+    ocfg, gcfg = configs_for(w)
+    s = O.define_sizes(ocfg, xp)
+    xo, qo = O.remesh(ocfg, s, xp, qp)
+    with V.VPM(gcfg) as h:
+        h.define_sizes(xp)
+        xg, qg = h.remesh_particles_3d(1, xp, qp)
+        assert xg.shape == xo.shape
+        assert rel_l2(xg, xo) <= PART_TOL and rel_l2(qg, qo) <= PART_TOL
+        n = xo.shape[0]
+        up_o, gp_o = O.step_fields(ocfg, s, xo, qo)
+        up, gp = np.zeros((n, 3)), np.zeros((n, 3))
+        h.vpm(np.ascontiguousarray(xo), np.ascontiguousarray(qo), up, gp, n, WhatToDo=2)
+        for name, fid in _pairs(V, O):
+            assert rel_l2(h.field(name).ravel(), O.get_field(fid)) <= FIELD_TOL, name
+        assert rel_l2(up, up_o) <= PART_TOL and rel_l2(gp, gp_o) <= PART_TOL
+        O.euler(xo, qo, up_o, gp_o, w["dt"])
+        xo2, qo2 = O.remesh(ocfg, s, xo, qo)
+        h.set_particles(xg, qg)
+        h.step(w["dt"])
+        xg2, qg2 = h.get_particles()
+        assert xg2.shape[0] == xo2.shape[0]
+        assert rel_l2(xg2, xo2) <= PART_TOL and rel_l2(qg2, qo2) <= PART_TOL
