@@ -40,8 +40,17 @@ struct AdjointState {
   vpmg::DBuf<double> lossv;                      // block partial sums
   vpmg::DBuf<double> out;                        // AoS gradients for the host copy
   vpmg::DBuf<int> masks;                         // remesh node masks of the last recorded run: K x N
+  vpmg::DBuf<int> kidx;                          // checkpoint index read by the copies (device side)
   int nprobe = 0;
   int masks_steps = -1;                          // steps recorded in masks (-1: none)
+  // one backward step captured as a CUDA graph, replayed once per step
+  cudaGraphExec_t bwd = nullptr;
+  double bwd_dt = 0.0;
+  const void* bwd_key[3] = {nullptr, nullptr, nullptr};
+  long long bwd_launches = 0;
+  ~AdjointState() {
+    if (bwd) cudaGraphExecDestroy(bwd);
+  }
 };
 
 namespace vpmg {
@@ -421,10 +430,15 @@ __global__ void k_sumsq(const double* __restrict__ v, size_t n, double* __restri
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
-// Checkpoint copies of the particle arrays (dir 0: particles -> ck, 1: back).
-__global__ void k_copy_particles(int dir, const int* __restrict__ np_src, int cap, double* x, double* y, double* z,
-                                 double* q0, double* q1, double* q2, double* vol, double* __restrict__ ck) {
-  const int n = *np_src;
+// Checkpoint copies of the particle arrays (dir 0: particles -> checkpoint
+// *kidx, 1: back); the index is read on the device so that one captured
+// backward step serves every step.
+__global__ void k_copy_particles(int dir, const int* __restrict__ kidx, const int* __restrict__ np_live,
+                                 const int* __restrict__ ckpt_np, int cap, double* x, double* y, double* z, double* q0,
+                                 double* q1, double* q2, double* vol, double* __restrict__ ckpt) {
+  const int k = *kidx;
+  const int n = dir == 0 ? *np_live : ckpt_np[k];
+  double* ck = ckpt + (size_t)k * 7 * cap;
   double* arr[7] = {x, y, z, q0, q1, q2, vol};
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
     for (int a = 0; a < 7; ++a) {
@@ -432,7 +446,14 @@ __global__ void k_copy_particles(int dir, const int* __restrict__ np_src, int ca
       else arr[a][p] = ck[(size_t)a * cap + p];
     }
 }
-__global__ void k_copy_count(const int* __restrict__ src, int* __restrict__ dst) { *dst = *src; }
+// The count moves after the copy, whose blocks all read it.
+__global__ void k_copy_count(int dir, const int* __restrict__ kidx, int* __restrict__ np_live, int* __restrict__ ckpt_np) {
+  const int k = *kidx;
+  if (dir == 0) ckpt_np[k] = *np_live;
+  else *np_live = ckpt_np[k];
+}
+__global__ void k_set_index(int* __restrict__ kidx, int v) { *kidx = v; }
+__global__ void k_step_back(int* __restrict__ kidx) { *kidx -= 1; }
 
 // Three component arrays (cap apart) -> AoS (3, n).
 __global__ void k_to_aos(const int* __restrict__ np_dev, const double* __restrict__ v, int cap, double* __restrict__ o) {
@@ -541,15 +562,17 @@ void poisson_T(vpmg_handle* h, const double* psibar, double* rbar) {
 }
 
 // ------------------------------------------------------------ steps ------
-void copy_ckpt(vpmg_handle* h, int k, int dir) {
+void set_index(vpmg_handle* h, int k) {
+  k_set_index<<<1, 1, 0, h->stream>>>(h->adj->kidx.p, k);
+  VPMG_LAUNCHED();
+}
+// Copy between the particles and checkpoint *kidx (set_index).
+void copy_ckpt(vpmg_handle* h, int dir) {
   AdjointState& S = *h->adj;
   Particles& P = h->parts;
-  int* cnt = S.ckpt_np.p + k;
-  const int* src = dir == 0 ? P.d_np.p : cnt;
-  int* dst = dir == 0 ? cnt : P.d_np.p;
-  k_copy_particles<<<grid(S.cap), 256, 0, h->stream>>>(dir, src, S.cap, P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p,
-                                                      P.vol.p, S.ckpt.p + (size_t)k * 7 * S.cap);
-  k_copy_count<<<1, 1, 0, h->stream>>>(src, dst);  // after the copy, whose blocks all read the count
+  k_copy_particles<<<grid(S.cap), 256, 0, h->stream>>>(dir, S.kidx.p, P.d_np.p, S.ckpt_np.p, S.cap, P.x.p, P.y.p, P.z.p,
+                                                      P.q0.p, P.q1.p, P.q2.p, P.vol.p, S.ckpt.p);
+  k_copy_count<<<1, 1, 0, h->stream>>>(dir, S.kidx.p, P.d_np.p, S.ckpt_np.p);
   count_launch(2);
 }
 
@@ -571,7 +594,10 @@ void ensure_state(vpmg_handle* h, int K, int nprobe) {
   S.uprobe.ensure(3 * (size_t)std::max(nprobe, 1));
   S.lossv.ensure(2 * kSumBlocks);
   S.out.ensure(3 * (size_t)S.cap);
+  S.kidx.ensure(1);
   S.nprobe = nprobe;
+  boundary_transpose_prepare(h->bo_bl, h->stream);
+  boundary_transpose_prepare(h->bo_c, h->stream);
 }
 
 // Probe stencils must stay on the mesh (checked on the host, as the kernels do).
@@ -727,9 +753,10 @@ void remesh_vjp(vpmg_handle* h, const double* qnew, double* xb, double* qb) {
   VPMG_LAUNCHED();
 }
 
-// Adjoint of step k (particles X_k, Q_k from checkpoint k): on entry
-// qnew = d loss / d Q_{k+1}; on exit qnew = d loss / d Q_k, xb = d loss / d X_k.
-void backward_step(vpmg_handle* h, int k, double dt) {
+// Adjoint of step k = *kidx (particles X_k, Q_k from checkpoint k): on
+// entry qnew = d loss / d Q_{k+1}; on exit qnew = d loss / d Q_k,
+// xb = d loss / d X_k, and *kidx = k - 1.  Stream work only (capturable).
+void backward_step(vpmg_handle* h, double dt) {
   AdjointState& S = *h->adj;
   cudaStream_t st = h->stream;
   const int cap = S.cap;
@@ -744,7 +771,7 @@ void backward_step(vpmg_handle* h, int k, double dt) {
   double* qb1 = S.pbar.p + 18 * (size_t)cap;
   const MeshDev mg = hx::mesh_dev(h->gglob, 4);
   // 1. recompute: fields at X_k, UP and GP, the pushed state X', Q'
-  copy_ckpt(h, k, 1);
+  copy_ckpt(h, 1);
   forward_fields(h);
   {
     const double* V[3] = {h->vel.p, h->vel.p + N, h->vel.p + 2 * N};
@@ -762,10 +789,43 @@ void backward_step(vpmg_handle* h, int k, double dt) {
   k_euler_T<<<grid(cap), 256, 0, st>>>(P.d_np.p, cap, dt, xb1, qb1, xb, qb, upb, gpb);
   VPMG_LAUNCHED();
   // 4. back at X_k (the fields are still those of X_k): the field step's VJP
-  copy_ckpt(h, k, 1);
+  copy_ckpt(h, 1);
   bin_particles(P, mg, h->bins, st);
   VPMG_CUDA(cudaMemcpyAsync(qnew, qb, sizeof(double) * 3 * cap, cudaMemcpyDeviceToDevice, st));
   fields_vjp(h, upb, gpb, xb, qnew);
+  k_step_back<<<1, 1, 0, st>>>(S.kidx.p);
+  VPMG_LAUNCHED();
+}
+
+// The backward step as a CUDA graph (re-captured when dt or a buffer moves).
+void ensure_backward_graph(vpmg_handle* h, double dt) {
+  AdjointState& S = *h->adj;
+  const void* key[3] = {S.ckpt.p, S.pbar.p, h->parts.x.p};
+  if (S.bwd && S.bwd_dt == dt && key[0] == S.bwd_key[0] && key[1] == S.bwd_key[1] && key[2] == S.bwd_key[2]) return;
+  if (S.bwd) {
+    cudaGraphExecDestroy(S.bwd);
+    S.bwd = nullptr;
+  }
+  const long long l0 = h->launches;
+  cudaGraph_t g = nullptr;
+  VPMG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    backward_step(h, dt);
+  } catch (...) {
+    cudaStreamEndCapture(h->stream, &g);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    h->launches = l0;
+    throw;
+  }
+  VPMG_CUDA(cudaStreamEndCapture(h->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&S.bwd, g, 0);
+  cudaGraphDestroy(g);
+  VPMG_CUDA(e);
+  S.bwd_launches = h->launches - l0;
+  h->launches = l0;
+  S.bwd_dt = dt;
+  for (int i = 0; i < 3; ++i) S.bwd_key[i] = key[i];
 }
 
 // One step with the remesh's |w| cut replaced by a recorded node mask.
@@ -792,7 +852,8 @@ void forward_pass(vpmg_handle* h, int nsteps, double dt, int mask_mode) {
   AdjointState& S = *h->adj;
   const size_t N = h->gglob.count();
   for (int k = 0; k < nsteps; ++k) {
-    copy_ckpt(h, k, 0);
+    set_index(h, k);
+    copy_ckpt(h, 0);
     if (mask_mode == 2) {
       step_masked(h, dt, S.masks.p + (size_t)k * N);
     } else {
@@ -802,7 +863,8 @@ void forward_pass(vpmg_handle* h, int nsteps, double dt, int mask_mode) {
                                   cudaMemcpyDeviceToDevice, h->stream));
     }
   }
-  copy_ckpt(h, nsteps, 0);
+  set_index(h, nsteps);
+  copy_ckpt(h, 0);
   forward_fields(h);
 }
 
@@ -860,12 +922,25 @@ double adjoint_common(vpmg_handle* h, int nsteps, double dt, const double* probe
       fill_zero(S.pbar.p, 3 * (size_t)cap, st);                 // xbar
       fill_zero(S.pbar.p + 12 * (size_t)cap, 3 * (size_t)cap, st);  // qnew
       fields_T(h, false, S.pbar.p, S.pbar.p + 12 * (size_t)cap);
-      for (int k = nsteps - 1; k >= 0; --k) backward_step(h, k, dt);
+      if (nsteps > 0) {
+        const bool graphs = !h->no_graphs;
+        if (graphs) ensure_backward_graph(h, dt);
+        set_index(h, nsteps - 1);
+        for (int k = nsteps - 1; k >= 0; --k) {
+          if (graphs) {
+            VPMG_CUDA(cudaGraphLaunch(S.bwd, st));
+            h->launches += S.bwd_launches;
+          } else {
+            backward_step(h, dt);
+          }
+        }
+      }
     }
     VPMG_CUDA(cudaEventRecord(T.e[2], st));
     VPMG_CUDA(cudaEventSynchronize(T.e[2]));
     // leave the handle holding the initial particles
-    copy_ckpt(h, 0, 1);
+    set_index(h, 0);
+    copy_ckpt(h, 1);
     hx::sync_np(h);
   } catch (...) {
     h->profile = prof;

@@ -220,7 +220,8 @@ WalkDev walk_dev(const BoundaryOp& B) {
 }  // namespace
 
 long long BoundaryOp::bytes() const {
-  return (long long)(rowptr.bytes() + col.bytes() + w.bytes() + cx.bytes() * 5 + child.bytes() + csrc.bytes());
+  return (long long)(rowptr.bytes() + col.bytes() + w.bytes() + colptr.bytes() + trow.bytes() + tw.bytes() +
+                     cx.bytes() * 5 + child.bytes() + csrc.bytes());
 }
 
 void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s) {
@@ -379,6 +380,44 @@ __global__ void __launch_bounds__(256) k_csr_T(const long long* __restrict__ row
   for (long long k = rowptr[warp] + lane; k < rowptr[warp + 1]; k += 32) atomicAdd(&cellbar[col[k]], wgt[k] * v);
 }
 
+// Transposed interaction list: per-cell counts, then a fill through per-cell
+// cursors (the order inside a cell's list follows the atomics, fixed once built).
+__global__ void k_col_count(const long long* __restrict__ rowptr, const int* __restrict__ col, int ntarget,
+                            int* __restrict__ cnt) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ntarget) return;
+  for (long long k = rowptr[warp] + lane; k < rowptr[warp + 1]; k += 32) atomicAdd(&cnt[col[k]], 1);
+}
+__global__ void k_col_fill(const long long* __restrict__ rowptr, const int* __restrict__ col,
+                           const double* __restrict__ wgt, int ntarget, const long long* __restrict__ colptr,
+                           int* __restrict__ cursor, int* __restrict__ trow, double* __restrict__ tw) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ntarget) return;
+  for (long long k = rowptr[warp] + lane; k < rowptr[warp + 1]; k += 32) {
+    const int c = col[k];
+    const long long slot = colptr[c] + atomicAdd(&cursor[c], 1);
+    trow[slot] = warp;
+    tw[slot] = wgt[k];
+  }
+}
+// cellbar[c] = scale * sum over the cell's targets of w * bcbar(target node); warp per cell.
+__global__ void __launch_bounds__(256) k_csc_T(const long long* __restrict__ colptr, const int* __restrict__ trow,
+                                               const double* __restrict__ tw, const int* __restrict__ tgt_node,
+                                               int ncell, double scale, const double* __restrict__ bcbar,
+                                               double* __restrict__ cellbar) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ncell) return;
+  double a = 0.0;
+  for (long long k = colptr[warp] + lane; k < colptr[warp + 1]; k += 32)
+    a = fma(__ldg(&tw[k]), __ldg(&bcbar[__ldg(&tgt_node[__ldg(&trow[k])])]), a);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if (lane == 0) cellbar[warp] = scale * a;
+}
+
 // leaf adjoint = its own level-0 adjoint + sum over ancestors of ds_leaf / ds_cell * cell adjoint
 __global__ void k_agg_T(const int* __restrict__ anc, const double* __restrict__ cds, int nbound, int levmax,
                         const double* __restrict__ cellbar, double* __restrict__ panelbar) {
@@ -416,9 +455,53 @@ __global__ void k_normal_deriv_T(const double* __restrict__ panelbar, int NX, in
 
 }  // namespace
 
+void boundary_transpose_prepare(BoundaryOp& B, cudaStream_t s) {
+  if (!B.precomputed || B.transposed || B.nnz == 0) return;
+  const long long need = B.nnz * (long long)(sizeof(int) + sizeof(double)) + 8LL * (B.ncell_total + 1);
+  size_t free_b = 0, total_b = 0;
+  VPMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  if (need > (long long)(0.5 * (double)free_b)) return;  // keep the atomic scatter
+  DBuf<int> cnt;
+  cnt.ensure(B.ncell_total);
+  VPMG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int) * B.ncell_total, s));
+  const long long threads = (long long)B.ntarget * 32;
+  const unsigned blocks = (unsigned)((threads + 255) / 256);
+  k_col_count<<<blocks, 256, 0, s>>>(B.rowptr.p, B.col.p, B.ntarget, cnt.p);
+  VPMG_LAUNCHED();
+  std::vector<int> hc(B.ncell_total);
+  VPMG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, sizeof(int) * B.ncell_total, cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  std::vector<long long> cp(B.ncell_total + 1, 0);
+  for (int c = 0; c < B.ncell_total; ++c) cp[c + 1] = cp[c] + hc[c];
+  VPMG_CHECK(cp[B.ncell_total] == B.nnz, VPMG_ERR_TREE, "transposed interaction list lost entries");
+  try {
+    upload(B.colptr, cp);
+    B.trow.ensure((size_t)B.nnz);
+    B.tw.ensure((size_t)B.nnz);
+  } catch (const Error& e) {
+    if (e.status != VPMG_ERR_NOMEM) throw;
+    B.colptr.release(); B.trow.release(); B.tw.release();
+    return;
+  }
+  VPMG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int) * B.ncell_total, s));
+  k_col_fill<<<blocks, 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, B.ntarget, B.colptr.p, cnt.p, B.trow.p, B.tw.p);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  B.transposed = true;
+}
+
 void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s) {
-  VPMG_CUDA(cudaMemsetAsync(cellbar, 0, sizeof(double) * B.ncell_total, s));
   const double scale = -1.0 / (4.0 * kPI);
+  if (B.transposed) {
+    const long long threads = (long long)B.ncell_total * 32;
+    k_csc_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.colptr.p, B.trow.p, B.tw.p, B.tgt_node.p,
+                                                              B.ncell_total, scale, bcbar, cellbar);
+    VPMG_LAUNCHED();
+    VPMG_CUDA(cudaGetLastError());
+    return;
+  }
+  VPMG_CUDA(cudaMemsetAsync(cellbar, 0, sizeof(double) * B.ncell_total, s));
   if (B.precomputed) {
     const long long threads = (long long)B.ntarget * 32;
     k_csr_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, B.tgt_node.p, B.ntarget,

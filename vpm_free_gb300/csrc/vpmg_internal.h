@@ -138,6 +138,11 @@ struct BoundaryOp {
   DBuf<long long> rowptr;
   DBuf<int> col;
   DBuf<double> w;
+  // its transpose (CSR over cells, for the reverse mode), built on first use
+  bool transposed = false;
+  DBuf<long long> colptr;
+  DBuf<int> trow;
+  DBuf<double> tw;
   long long bytes() const;
 };
 void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s);
@@ -148,6 +153,11 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
 // Transposes (one component): boundary-value adjoint (grid node array) ->
 // cell adjoints -> panel adjoints -> accumulated into the sol0 adjoint.
 void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s);
+// Builds the transposed interaction list when the operator is recorded and
+// the copy fits in half of the free device memory (set-up time, outside
+// stream capture); boundary_apply_T then gathers per cell instead of
+// scattering with atomics.
+void boundary_transpose_prepare(BoundaryOp& B, cudaStream_t s);
 void boundary_agg_T(BoundaryOp& B, const double* cellbar, double* panelbar, cudaStream_t s);
 void boundary_panels_T(BoundaryOp& B, const Grid& g, const double* panelbar, double* sol0bar, cudaStream_t s);
 
