@@ -86,6 +86,21 @@ def scatter384(n=8_000_000, seed=42):
     return xp, qp, SCATTER384
 
 
+def scatter_scaled(cells=96, seed=42):
+    """The scatter stress case at a smaller mesh with the same particle
+    density (8e6 particles on 384^3): uniform in [-1,1]^3, strengths
+    N(0, 1e-3), volume h^3, cells^3 mesh plus the 8-cell pad, dt 0.002."""
+    rng = np.random.default_rng(seed)
+    h = 2.0 / cells
+    n = int(round(8_000_000 * (cells / 384.0) ** 3))
+    xp = rng.uniform(-1.0, 1.0, (n, 3))
+    qp = np.empty((n, 4))
+    qp[:, :3] = rng.normal(0.0, 1e-3, (n, 3))
+    qp[:, 3] = h ** 3
+    L = 1.0 + 8 * h
+    return xp, qp, dict(name=f"scatter{cells}", box=(-L, -L, -L, L, L, L), dpm=(h, h, h), steps=5, dt=0.002)
+
+
 def scaled_ring(n_cells, seed=7):
     """Small ring case on an n_cells^3 mesh (parity tests at oracle-friendly sizes)."""
     L = 1.6
