@@ -238,8 +238,10 @@ def run_batched(args, local):
             n = XP.shape[0]
             UP, GP = np.zeros((n, 3)), np.zeros((n, 3))
             h.vpm(XP, QP, UP, GP, n, WhatToDo=2, NTIME=it + 1)
-            XP += UP * dt
-            QP[:, :3] -= GP * dt
+            np.multiply(UP, dt, out=UP)
+            XP += UP
+            np.multiply(GP, dt, out=GP)
+            QP[:, :3] -= GP
             XP, QP = h.remesh_particles_3d(1, XP, QP)
     ref_loop_s = time.perf_counter() - t3
     precomputed = sum(1 for h in hs if h.tree_stats()["precomputed"])
@@ -415,30 +417,47 @@ def run_ours(args, dist):
     if args.operator_budget >= 0:
         he.set_operator_budget(args.operator_budget)
     he.vpm(xp, qp, None, None, xp.shape[0], WhatToDo=0, NTIME=0)
-    XP, QP = he.remesh_particles_3d(1, xp, qp)
+    # the host's particle arrays hold NVRM = mesh nodes rows, the most a
+    # remesh can emit; UP / GP likewise (test.f90 keeps XPR/QPR/UPR/GPR)
+    nvrm = int(np.prod(sizes_nn))
+
+    def host_array(rows, cols):  # pinned host memory (page-locked), numpy view
+        try:
+            import torch
+            return torch.empty((rows, cols), dtype=torch.float64).pin_memory().numpy()
+        except Exception:
+            return np.empty((rows, cols))
+    XP, QP = host_array(nvrm, 3), host_array(nvrm, 4)
+    UP, GP = host_array(nvrm, 3), host_array(nvrm, 3)
+    XP[:xp.shape[0]], QP[:qp.shape[0]] = xp, qp
+    n = he.remesh_in_place(XP, QP, xp.shape[0])
     for _ in range(min(args.warmup, 1)):
-        UP = np.zeros((XP.shape[0], 3)); GP = np.zeros((XP.shape[0], 3))
-        he.vpm(XP, QP, UP, GP, XP.shape[0], WhatToDo=2, NTIME=1)
+        UP[:n] = 0.0; GP[:n] = 0.0
+        he.vpm(XP[:n], QP[:n], UP[:n], GP[:n], n, WhatToDo=2, NTIME=1)
     dist.barrier()
     h2d = d2h = eps = 0
     t0 = time.perf_counter()
     for it in range(ke):
-        n = XP.shape[0]
         eps += n
-        UP = np.zeros((n, 3))
-        GP = np.zeros((n, 3))
-        he.vpm(XP, QP, UP, GP, n, WhatToDo=2, NTIME=it + 1)
-        XP += UP * dt                      # test.f90:104-117, UINF = 0
-        QP[:, :3] -= GP * dt
-        he.vpm(XP, QP, None, None, n, WhatToDo=0, NTIME=it + 1)
-        XP, QP = he.remesh_particles_3d(1, XP, QP)
-        h2d += n * 7 * 8 * 2
-        d2h += n * 6 * 8 + XP.shape[0] * 7 * 8
+        up, gp = UP[:n], GP[:n]
+        up[...] = 0.0                      # the caller zeroes UP/GP (test.f90:90-91)
+        gp[...] = 0.0
+        he.vpm(XP[:n], QP[:n], up, gp, n, WhatToDo=2, NTIME=it + 1)
+        np.multiply(up, dt, out=up)        # test.f90:104-117, UINF = 0 (in place, as a compiled host loop)
+        XP[:n] += up
+        np.multiply(gp, dt, out=gp)
+        QP[:n, :3] -= gp
+        he.vpm(XP[:n], QP[:n], None, None, n, WhatToDo=0, NTIME=it + 1)
+        n_old = n
+        n = he.remesh_in_place(XP, QP, n)
+        h2d += n_old * 7 * 8 * 2
+        d2h += n_old * 6 * 8 + n * 7 * 8
     te = time.perf_counter() - t0
     te_max = dist.reduce(te, "max")
     e2e = {"value": dist.reduce(eps, "sum") / te_max, "unit": UNIT, "h2d_bytes_per_step": h2d // ke,
            "d2h_bytes_per_step": d2h // ke, "steps": ke,
-           "timing": "host clock around synchronous vpm()/remesh_particles_3d() C-ABI calls"}
+           "timing": "host clock around synchronous vpm()/remesh_particles_3d() C-ABI calls on pinned host arrays "
+                     "of NVRM rows (host Euler in place between them)"}
     # ---- CPU baseline (rank 0, N = 1, bounded sample) -----------------------
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu and args.workload == "leapfrog256":

@@ -252,16 +252,29 @@ class VPM:
         return s
 
     def remesh_particles_3d(self, iflag, XP, QP, capacity=None):
-        """remesh_particles_3d(iflag) on (XP, QP); returns new (XP, QP) arrays."""
+        """remesh_particles_3d(iflag) on (XP, QP); returns new (XP, QP) arrays.
+        The in/out arrays of the C call (capacity = mesh nodes, the most a
+        remesh can emit) are kept by the handle and reused."""
         nn = list(self.sizes().nn)
         cap = int(capacity or max(int(np.prod(nn)), XP.shape[0]))
-        xb = np.zeros((cap, 3))
-        qb = np.zeros((cap, 4))
+        if getattr(self, "_rbuf", None) is None or self._rbuf[0].shape[0] < cap:
+            self._rbuf = (np.empty((cap, 3)), np.empty((cap, 4)))
+        xb, qb = self._rbuf
         xb[:XP.shape[0]] = XP
         qb[:QP.shape[0]] = QP
         n = C.c_int(XP.shape[0])
         self._chk(self._L.vpmg_remesh_particles_3d(self._h, iflag, _p(xb), _p(qb), C.byref(n), cap))
         return xb[:n.value].copy(), qb[:n.value].copy()
+
+    def remesh_in_place(self, XP, QP, n, iflag=1):
+        """remesh_particles_3d(iflag) on caller-owned arrays of NVRM rows, as a
+        Fortran host passes XPR/QPR: reads n particles, writes the new set in
+        place and returns its count (VPMGError if it exceeds NVRM)."""
+        if XP.dtype != np.float64 or QP.dtype != np.float64 or not (XP.flags.c_contiguous and QP.flags.c_contiguous):
+            raise ValueError("XP, QP must be C-contiguous float64 (NVRM, 3) / (NVRM, 4)")
+        m = C.c_int(int(n))
+        self._chk(self._L.vpmg_remesh_particles_3d(self._h, iflag, _p(XP), _p(QP), C.byref(m), XP.shape[0]))
+        return m.value
 
     def pmesh(self, SOL, RHS, Xbound, Dpm, iynbc, itree=1, levmax=3, NN_bl=None):
         """pmesh (source/pmlib.f90:69-192), 3 components, ibctyp = 2.
