@@ -39,7 +39,7 @@ typedef enum vpmg_status {
 typedef struct vpmg_config {
   double dpm[3];        /* DXpm DYpm DZpm                         pm.inp:1  */
   int interf_iproj;     /* projection function (2,3,4,5,6; 4=M4') pm.inp:2  */
-  int ibctyp;           /* 2: infinite-domain sources             pm.inp:3  */
+  int ibctyp;           /* 2 point sources, 3 constant panels     pm.inp:3  */
   int idvpm;            /* 1: constant volume                     pm.inp:4  */
   double epsvol;        /*                                        pm.inp:5  */
   int ncoarse;          /* coarse/fine ratio of YAPS              pm.inp:6  */
@@ -107,7 +107,8 @@ int vpmg_remesh_particles_3d(vpmg_handle* h, int iflag, double* xp, double* qp, 
 
 /* ---- the reference's single-block library calls ------------------------ */
 /* pmesh(SOL,RHS,...,Xbound,Dpm,NN,NN_bl,...,ibctyp,neqs,neqf,iynbc,NVR,itree,levmax)
- * (source/pmlib.f90:69-192), 3-D, ibctyp = 2, neqs = 1, neqf = 3.
+ * (source/pmlib.f90:69-192), 3-D, neqs = 1, neqf = 3; ibctyp is the
+ * handle's (pm.inp): 2 point-source or 3 constant-source panel boundary.
  * sol/rhs: 3 host arrays of NN[0]*NN[1]*NN[2] doubles each.              */
 int vpmg_pmesh(vpmg_handle* h, double* const sol[3], const double* const rhs[3], const double xbound[6],
                const double dpm[3], const int nn[3], const int nn_bl[6], int iynbc, int itree, int levmax);

@@ -77,6 +77,13 @@ def lib():
         L.vpmo_remesh_masked.restype = C.c_long
         L.vpmo_boundary_values.argtypes = [_PP, _PP, _dp, _dp, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int]
         L.vpmo_boundary_values.restype = C.c_long
+        L.vpmo_boundary_values_bc.argtypes = [_PP, _PP, _dp, _dp, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int,
+                                              C.c_int]
+        L.vpmo_boundary_values_bc.restype = C.c_long
+        L.vpmo_pmesh_bc.argtypes = [_PP, _PP, _dp, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
+                                    C.c_int, C.c_int, C.c_int]
+        L.vpmo_fsour_a4.argtypes = [_dp, _dp, C.c_int, _dp, C.c_double]
+        L.vpmo_fsour_a4.restype = C.c_double
         _LIB = L
     return _LIB
 
@@ -132,25 +139,33 @@ def dirichlet(rhs, sol, d, box=None, zero_bc=False, nthreads=0):
     return sol
 
 
-def pmesh(sol, rhs, xbound, dpm, iynbc, itree, levmax, nn_bl=None, nthreads=0):
+def pmesh(sol, rhs, xbound, dpm, iynbc, itree, levmax, nn_bl=None, nthreads=0, ibctyp=2):
     """sol, rhs: lists of 3 arrays (nz, ny, nx); sol modified in place."""
     nz, ny, nx = rhs[0].shape
     nn_bl = nn_bl if nn_bl is not None else (1, 1, 1, nx, ny, nz)
-    rc = lib().vpmo_pmesh(_pp(sol), _pp(rhs), np.asarray(xbound, dtype=np.float64), np.asarray(dpm, dtype=np.float64),
-                          _ivec((nx, ny, nz)), _ivec(nn_bl), iynbc, itree, levmax, nthreads)
+    rc = lib().vpmo_pmesh_bc(_pp(sol), _pp(rhs), np.asarray(xbound, dtype=np.float64),
+                             np.asarray(dpm, dtype=np.float64), _ivec((nx, ny, nz)), _ivec(nn_bl), iynbc, itree,
+                             levmax, nthreads, ibctyp)
     if rc != 0:
         raise RuntimeError(f"vpmo_pmesh failed: {rc}")
     return sol
 
 
-def boundary_values(sol0, xbound, dpm, levmax, direct=False, nthreads=0):
+def boundary_values(sol0, xbound, dpm, levmax, direct=False, nthreads=0, ibctyp=2):
     nz, ny, nx = sol0[0].shape
     bnd = [np.zeros_like(sol0[0]) for _ in range(3)]
-    n = lib().vpmo_boundary_values(_pp(sol0), _pp(bnd), np.asarray(xbound, dtype=np.float64),
-                                   np.asarray(dpm, dtype=np.float64), _ivec((nx, ny, nz)), levmax, 1 if direct else 0, nthreads)
+    n = lib().vpmo_boundary_values_bc(_pp(sol0), _pp(bnd), np.asarray(xbound, dtype=np.float64),
+                                      np.asarray(dpm, dtype=np.float64), _ivec((nx, ny, nz)), levmax,
+                                      1 if direct else 0, nthreads, ibctyp)
     if n < 0:
         raise RuntimeError(f"vpmo_boundary_values failed: {n}")
     return bnd, n
+
+
+def fsour_a4(xo, rg, iplane, dpm, area):
+    """FSOUR_A4 (source/pmbound.f90:1540-1620) in the frame of target plane iplane."""
+    return lib().vpmo_fsour_a4(np.asarray(xo, dtype=np.float64), np.asarray(rg, dtype=np.float64), int(iplane),
+                               np.asarray(dpm, dtype=np.float64), float(area))
 
 
 def step_fields(cfg, sizes, xp, qp, nthreads=0):

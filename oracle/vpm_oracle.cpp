@@ -453,19 +453,145 @@ void tree_calc(const Tree& T, int nv, int nlev, double X, double Y, double Z, do
   }
 }
 
+// ---- ibctyp = 3: constant-source panels ---------------------------------
+// Target-plane constants of calc_boundinf_3d_s / calc_boundinf_3d_lev_s
+// (source/pmbound.f90:536-606, 1270-1340).  iplane: +-1 Y plane, +-2 X plane,
+// +-3 Z plane; the sign is negative on the max faces (Bounds3d_lev,
+// pmbound.f90:1004-1054).
+struct Frame {
+  double E1[3], E2[3], E3[3], S[4], T[4], D[4], diag, area;
+};
+
+Frame make_frame(int iplane, const double Dpm[3]) {
+  Frame F;
+  const double DX = Dpm[0], DY = Dpm[1], DZ = Dpm[2];
+  const double si = iplane > 0 ? 1.0 : -1.0;
+  for (int m = 0; m < 3; ++m) F.E1[m] = F.E2[m] = F.E3[m] = 0.0;
+  double a = 0, b = 0;  // in-plane spacings along E1 and E2
+  switch (iplane > 0 ? iplane : -iplane) {
+    case 1:  // Y = const
+      F.E1[0] = 1.0 * si; F.E2[2] = 1.0; F.E3[1] = -1.0 * si;
+      F.diag = std::sqrt(DX * DX + DZ * DZ); F.area = DX * DZ; a = DX; b = DZ;
+      break;
+    case 2:  // X = const
+      F.E1[2] = 1.0; F.E2[1] = -1.0 * si; F.E3[0] = -1.0 * si;
+      F.diag = std::sqrt(DY * DY + DZ * DZ); F.area = DY * DZ; a = DY; b = DZ;
+      break;
+    default:  // Z = const
+      F.E1[0] = 1.0; F.E2[1] = -1.0 * si; F.E3[2] = -1.0 * si;
+      F.diag = std::sqrt(DX * DX + DY * DY); F.area = DX * DY; a = DX; b = DY;
+      break;
+  }
+  F.S[0] = -0.5 * a; F.S[1] = -0.5 * a; F.S[2] = 0.5 * a; F.S[3] = 0.5 * a;
+  F.T[0] = -0.5 * b; F.T[1] = 0.5 * b; F.T[2] = 0.5 * b; F.T[3] = -0.5 * b;
+  F.D[0] = b; F.D[1] = a; F.D[2] = b; F.D[3] = a;
+  return F;
+}
+
+// FSOUR_A4 (source/pmbound.f90:1540-1620) with NSIDE = 0, ISING = 0,
+// EPSS = 1e-14: potential at XO of a flat quadrilateral of unit constant
+// source centred at RG, corners (S, T) in the frame (E1, E2, E3).
+double fsour_a4(const double XO[3], const double RG[3], const Frame& F, double AREA) {
+  const double COSB[4] = {0.0, 1.0, 0.0, -1.0}, SINB[4] = {1.0, 0.0, -1.0, 0.0};
+  const double TINY = 1e-10, EPSS = 1e-14;
+  const double d0 = XO[0] - RG[0], d1 = XO[1] - RG[1], d2 = XO[2] - RG[2];
+  const double X = (d0 * F.E1[0] + d1 * F.E1[1]) + d2 * F.E1[2];
+  const double Y = (d0 * F.E2[0] + d1 * F.E2[1]) + d2 * F.E2[2];
+  double Z = (d0 * F.E3[0] + d1 * F.E3[1]) + d2 * F.E3[2];
+  const double RO = std::sqrt((X * X + Y * Y) + Z * Z);
+  const double RATIO = RO / F.diag;
+  if (RATIO > 10) {
+    const double AREA1 = AREA / PI4;
+    return -AREA1 / RO;
+  }
+  double FIL = 0.0;
+  const double ZP = (Z < 0.0) ? -1.0 : 1.0;
+  double AZ = std::max(EPSS, std::fabs(Z));
+  Z = AZ * ZP;
+  const double ZK = Z * Z;
+  double R[4], E[4], H[4];
+  for (int k = 0; k < 4; ++k) {
+    const double XK = (X - F.S[k]) * (X - F.S[k]);
+    const double YK = (Y - F.T[k]) * (Y - F.T[k]);
+    H[k] = (X - F.S[k]) * (Y - F.T[k]);
+    R[k] = std::sqrt((XK + YK) + ZK);
+    E[k] = ZK + XK;
+  }
+  for (int k = 0; k < 4; ++k) {
+    const int k1 = k, k2 = (k == 3) ? 0 : k + 1;
+    const double A2 = (R[k1] + R[k2]) + F.D[k];
+    const double A1 = (R[k1] + R[k2]) - F.D[k];
+    if (std::fabs(A1 * A2) < TINY) continue;
+    const double AK = std::log(A1 / A2);
+    const double TOO = -(X - F.S[k1]) * SINB[k] + (Y - F.T[k1]) * COSB[k];
+    FIL = FIL - TOO * AK;
+  }
+  AZ = std::max(TINY, AZ);
+  Z = AZ * ZP;
+  double UL3 = 0.0;
+  for (int k = 0; k < 4; ++k) {
+    if (std::fabs(COSB[k]) < TINY) continue;
+    const int k1 = k, k2 = (k == 3) ? 0 : k + 1;
+    UL3 = UL3 + std::atan((SINB[k] * E[k1] - COSB[k] * H[k1]) / ((Z * COSB[k]) * R[k1])) -
+          std::atan((SINB[k] * E[k2] - COSB[k] * H[k2]) / ((Z * COSB[k]) * R[k2]));
+  }
+  return (FIL + Z * UL3) / PI4;
+}
+
+// Recursive walk, literal restatement of tree_calc_3d_s (source/pmbound.f90:1379-1501).
+// Kept as written: the opening test divides (r / sqrt(dS) < 10); only
+// ilev_t(.,.,6) == -1 dummies are always opened (a -2 dummy has dS = 0, so
+// it is never opened and its children are not visited); at the coarsest
+// level an unopened cell contributes FSOUR_A4(cell) times the source of
+// the cell the walk started from (nv = 1), not of the visited cell.
+void tree_calc_s(const Tree& T, int nv, int nlev, const double XO[3], const Frame& F, double src[3], long& nint) {
+  int list[4] = {0, 0, 0, 0};
+  int lfin;
+  bool all = false;
+  if (nlev == T.levmax) { all = true; lfin = T.nbound_lev[nlev]; }
+  else if (T.IL(nv, nlev + 1, 6) < 0) { list[0] = T.IL(nv, nlev + 1, 1); list[1] = T.IL(nv, nlev + 1, 2); lfin = 2; }
+  else { for (int m = 0; m < 4; ++m) list[m] = T.IL(nv, nlev + 1, m + 1); lfin = 4; }
+  for (int nlf = 1; nlf <= lfin; ++nlf) {
+    const int nleaf = all ? nlf : list[nlf - 1];
+    const size_t a = T.at(nleaf, nlev);
+    const double RG[3] = {T.xs[a], T.ys[a], T.zs[a]};
+    const double r = std::sqrt(((XO[0] - RG[0]) * (XO[0] - RG[0]) + (XO[1] - RG[1]) * (XO[1] - RG[1])) +
+                               (XO[2] - RG[2]) * (XO[2] - RG[2]));
+    const double DS = T.dsl[a];
+    const double RATIO = r / std::sqrt(DS);
+    if ((RATIO < 10 && nlev > 0) || T.IL(nleaf, nlev, 6) == -1) {
+      tree_calc_s(T, nleaf, nlev - 1, XO, F, src, nint);
+    } else {
+      ++nint;
+      if (nlev != T.levmax) {
+        for (int c = 0; c < 3; ++c) src[c] = src[c] - T.s[c][a] * DS / (PI4 * r);
+      } else {
+        const double FIS = fsour_a4(XO, RG, F, DS);
+        const size_t av = T.at(nv, nlev);
+        for (int c = 0; c < 3; ++c) src[c] = src[c] + T.s[c][av] * FIS;
+      }
+    }
+  }
+}
+
 // Bounds3d_lev (source/pmbound.f90:980-1133) on the whole grid 1..N; and
-// the untreed calc_boundinf_3d (source/pmbound.f90:415-515) when direct.
+// the untreed Bounds3d (source/pmbound.f90:80-157) when direct.  ibctyp 2:
+// calc_boundinf_3d_lev / calc_boundinf_3d; ibctyp 3: calc_boundinf_3d_lev_s
+// / calc_boundinf_3d_s (source/pmbound.f90:1255-1353, 520-648).
 long bounds(int NX, int NY, int NZ, const double xb[6], const double D[3], const Tree* T, const Panels* P,
-            double* const sol[3], int nthreads) {
+            double* const sol[3], int nthreads, int ibctyp) {
   const double XMIN = xb[0], YMIN = xb[1], ZMIN = xb[2], DX = D[0], DY = D[1], DZ = D[2];
-  struct Tg { int i, j, k; };
+  struct Tg { int i, j, k, iplane; };
   std::vector<Tg> tg;
-  for (int k = 1; k <= NZ; ++k) for (int j = 1; j <= NY; ++j) tg.push_back({1, j, k});
-  for (int k = 1; k <= NZ; ++k) for (int j = 1; j <= NY; ++j) tg.push_back({NX, j, k});
-  for (int k = 1; k <= NZ; ++k) for (int i = 2; i <= NX - 1; ++i) tg.push_back({i, 1, k});
-  for (int k = 1; k <= NZ; ++k) for (int i = 2; i <= NX - 1; ++i) tg.push_back({i, NY, k});
-  for (int j = 2; j <= NY - 1; ++j) for (int i = 2; i <= NX - 1; ++i) tg.push_back({i, j, 1});
-  for (int j = 2; j <= NY - 1; ++j) for (int i = 2; i <= NX - 1; ++i) tg.push_back({i, j, NZ});
+  for (int k = 1; k <= NZ; ++k) for (int j = 1; j <= NY; ++j) tg.push_back({1, j, k, 2});
+  for (int k = 1; k <= NZ; ++k) for (int j = 1; j <= NY; ++j) tg.push_back({NX, j, k, -2});
+  for (int k = 1; k <= NZ; ++k) for (int i = 2; i <= NX - 1; ++i) tg.push_back({i, 1, k, 1});
+  for (int k = 1; k <= NZ; ++k) for (int i = 2; i <= NX - 1; ++i) tg.push_back({i, NY, k, -1});
+  for (int j = 2; j <= NY - 1; ++j) for (int i = 2; i <= NX - 1; ++i) tg.push_back({i, j, 1, 3});
+  for (int j = 2; j <= NY - 1; ++j) for (int i = 2; i <= NX - 1; ++i) tg.push_back({i, j, NZ, -3});
+  Frame frames[7];
+  for (int p = -3; p <= 3; ++p)
+    if (p != 0) frames[p + 3] = make_frame(p, D);
   long total = 0;
   const int Tn = nthr(nthreads);
   const double lg = std::log((std::sqrt(2.0) - 1) / (std::sqrt(2.0) + 1));
@@ -473,16 +599,31 @@ long bounds(int NX, int NY, int NZ, const double xb[6], const double D[3], const
   for (long t = 0; t < (long)tg.size(); ++t) {
     const int i = tg[t].i, j = tg[t].j, k = tg[t].k;
     const double X = coord(XMIN, i, DX), Y = coord(YMIN, j, DY), Z = coord(ZMIN, k, DZ);
+    const size_t node = lin(NX, NY, i, j, k);
+    const Frame& F = frames[tg[t].iplane + 3];
+    const double XO[3] = {X, Y, Z};
     double src[3] = {0, 0, 0};
     long ni = 0;
-    if (T) {
+    if (ibctyp == 3 && T) {
+      tree_calc_s(*T, 1, T->levmax, XO, F, src, ni);
+      for (int c = 0; c < 3; ++c) sol[c][node] += src[c];
+    } else if (ibctyp == 3) {
+      double acc[3] = {sol[0][node], sol[1][node], sol[2][node]};
+      for (int nv = 0; nv < P->nbound; ++nv) {
+        const double RG[3] = {P->xc[nv], P->yc[nv], P->zc[nv]};
+        const double FIS = fsour_a4(XO, RG, F, F.area);  // AREA of the target plane, as written
+        ++ni;
+        for (int c = 0; c < 3; ++c) acc[c] = acc[c] + FIS * P->src[c][nv];
+      }
+      for (int c = 0; c < 3; ++c) sol[c][node] = acc[c];
+    } else if (T) {
       tree_calc(*T, 1, T->levmax, X, Y, Z, src, ni);
-      for (int c = 0; c < 3; ++c) sol[c][lin(NX, NY, i, j, k)] += src[c] / PI4;
+      for (int c = 0; c < 3; ++c) sol[c][node] += src[c] / PI4;
     } else {
       // direct sum; target-plane-dependent self term (h1 + h2) as in the reference
       const int plane = (i == 1 || i == NX) ? 2 : ((j == 1 || j == NY) ? 1 : 3);
       const double hsum = plane == 2 ? (DY + DZ) : (plane == 1 ? (DX + DZ) : (DX + DY));
-      double acc[3] = {sol[0][lin(NX, NY, i, j, k)], sol[1][lin(NX, NY, i, j, k)], sol[2][lin(NX, NY, i, j, k)]};
+      double acc[3] = {sol[0][node], sol[1][node], sol[2][node]};
       for (int nv = 0; nv < P->nbound; ++nv) {
         const double XR = P->xc[nv] - X, YR = P->yc[nv] - Y, ZR = P->zc[nv] - Z;
         const double r = std::sqrt(XR * XR + YR * YR + ZR * ZR);
@@ -493,17 +634,17 @@ long bounds(int NX, int NY, int NZ, const double xb[6], const double D[3], const
           else acc[c] = acc[c] + P->src[c][nv] * hsum * lg / PI4;
         }
       }
-      for (int c = 0; c < 3; ++c) sol[c][lin(NX, NY, i, j, k)] = acc[c];
+      for (int c = 0; c < 3; ++c) sol[c][node] = acc[c];
     }
     total += ni;
   }
   return total;
 }
 
-// pmesh (source/pmlib.f90:69-192), 3-D, ibctyp = 2.
+// pmesh (source/pmlib.f90:69-192), 3-D, ibctyp 2 or 3.
 long g_last_interactions = 0;
 int pmesh(double* const sol[3], double* const rhs[3], const double xb[6], const double D[3], const int NN[3],
-          const int NN_bl[6], int iynbc, int itree, int levmax, int nthreads) {
+          const int NN_bl[6], int iynbc, int itree, int levmax, int nthreads, int ibctyp = 2) {
   const int NX = NN[0], NY = NN[1], NZ = NN[2];
   if (iynbc == 1) {
     // infdomain_3d (source/pinfdomain.f90:86-158)
@@ -517,9 +658,9 @@ int pmesh(double* const sol[3], double* const rhs[3], const double xb[6], const 
     if (itree == 1) {
       Tree T;
       if (!build_tree(P, levmax, T)) return -3;
-      g_last_interactions = bounds(NX, NY, NZ, xb, D, &T, nullptr, sol, nthreads);
+      g_last_interactions = bounds(NX, NY, NZ, xb, D, &T, nullptr, sol, nthreads, ibctyp);
     } else {
-      g_last_interactions = bounds(NX, NY, NZ, xb, D, nullptr, &P, sol, nthreads);
+      g_last_interactions = bounds(NX, NY, NZ, xb, D, nullptr, &P, sol, nthreads, ibctyp);
     }
     for (int c = 0; c < 3; ++c) dirichlet(NX, NY, NZ, full, D, rhs[c], sol[c], false, nthreads);
   } else {
@@ -691,14 +832,30 @@ int vpmo_pmesh(double* const sol[3], double* const rhs[3], const double xbound[6
   return pmesh(sol, rhs, xbound, dpm, nn, nn_bl, iynbc, itree, levmax, nthreads);
 }
 
-long vpmo_boundary_values(double* const sol0[3], double* const bnd[3], const double xb[6], const double D[3],
-                          const int nn[3], int levmax, int direct, int nthreads) {
+int vpmo_pmesh_bc(double* const sol[3], double* const rhs[3], const double xbound[6], const double dpm[3],
+                  const int nn[3], const int nn_bl[6], int iynbc, int itree, int levmax, int nthreads, int ibctyp) {
+  if (ibctyp != 2 && ibctyp != 3) return -6;
+  return pmesh(sol, rhs, xbound, dpm, nn, nn_bl, iynbc, itree, levmax, nthreads, ibctyp);
+}
+
+long vpmo_boundary_values_bc(double* const sol0[3], double* const bnd[3], const double xb[6], const double D[3],
+                             const int nn[3], int levmax, int direct, int nthreads, int ibctyp) {
+  if (ibctyp != 2 && ibctyp != 3) return -6;
   Panels P;
   normal_deriv(nn[0], nn[1], nn[2], xb, D, sol0, P);
-  if (direct) return bounds(nn[0], nn[1], nn[2], xb, D, nullptr, &P, bnd, nthreads);
+  if (direct) return bounds(nn[0], nn[1], nn[2], xb, D, nullptr, &P, bnd, nthreads, ibctyp);
   Tree T;
   if (!build_tree(P, levmax, T)) return -3;
-  return bounds(nn[0], nn[1], nn[2], xb, D, &T, nullptr, bnd, nthreads);
+  return bounds(nn[0], nn[1], nn[2], xb, D, &T, nullptr, bnd, nthreads, ibctyp);
+}
+
+long vpmo_boundary_values(double* const sol0[3], double* const bnd[3], const double xb[6], const double D[3],
+                          const int nn[3], int levmax, int direct, int nthreads) {
+  return vpmo_boundary_values_bc(sol0, bnd, xb, D, nn, levmax, direct, nthreads, 2);
+}
+
+double vpmo_fsour_a4(const double xo[3], const double rg[3], int iplane, const double dpm[3], double area) {
+  return fsour_a4(xo, rg, make_frame(iplane, dpm), area);
 }
 
 int vpmo_step_fields(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, double* up,
@@ -730,7 +887,7 @@ int vpmo_step_fields(const vpmo_config* cfg, const vpmo_sizes* s, const double* 
   // 3. yaps3d (yaps3d.f90:1-453), one block
   double* sp[3] = {sbl[0].data(), sbl[1].data(), sbl[2].data()};
   double* rp[3] = {rbl[0].data(), rbl[1].data(), rbl[2].data()};
-  e = pmesh(sp, rp, s->xbound_bl, s->dpm, s->nnbl, s->nnbl_bl, 1, cfg->iyntree, s->ilevmax, nthreads);
+  e = pmesh(sp, rp, s->xbound_bl, s->dpm, s->nnbl, s->nnbl_bl, 1, cfg->iyntree, s->ilevmax, nthreads, cfg->ibctyp);
   if (e) return e;
   for (int c = 0; c < 3; ++c) W.bl_sol1[c] = sbl[c];
   // 3b. sampling every nc-th node (yaps3d.f90:104-138)
@@ -776,7 +933,7 @@ int vpmo_step_fields(const vpmo_config* cfg, const vpmo_sizes* s, const double* 
     double* cr[3] = {W.c_rhs[0].data(), W.c_rhs[1].data(), W.c_rhs[2].data()};
     const int itree = cfg->iyntree == 1 ? 1 : 0;
     const int lmax = itree ? s->ilevmax - 1 : 1;
-    e = pmesh(cs, cr, s->xbound_coarse, s->dpm_coarse, s->nn_coarse, s->nn_bl_coarse, 1, itree, lmax, nthreads);
+    e = pmesh(cs, cr, s->xbound_coarse, s->dpm_coarse, s->nn_coarse, s->nn_bl_coarse, 1, itree, lmax, nthreads, cfg->ibctyp);
     if (e) return e;
   }
   // 3e. interp_stencil on the inner-box faces (yaps3d.f90:340-395, 1914-1983), one block:

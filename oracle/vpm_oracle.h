@@ -86,6 +86,21 @@ void vpmo_dirichlet(int nx, int ny, int nz, const int box[6], const double d[3],
 int vpmo_pmesh(double* const sol[3], double* const rhs[3], const double xbound[6],
                const double dpm[3], const int nn[3], const int nn_bl[6], int iynbc, int itree,
                int levmax, int nthreads);
+/* The same with the boundary type of pm.inp: ibctyp 2 (point sources,
+ * calc_boundinf_3d[_lev]) or 3 (constant-source panels, FSOUR_A4,
+ * calc_boundinf_3d[_lev]_s, source/pmbound.f90:520-648, 1255-1620). */
+int vpmo_pmesh_bc(double* const sol[3], double* const rhs[3], const double xbound[6],
+                  const double dpm[3], const int nn[3], const int nn_bl[6], int iynbc, int itree,
+                  int levmax, int nthreads, int ibctyp);
+
+/* vpmo_boundary_values (below) with the boundary type: 2 or 3. */
+long vpmo_boundary_values_bc(double* const sol0[3], double* const bnd[3], const double xb[6],
+                             const double D[3], const int nn[3], int levmax, int direct, int nthreads,
+                             int ibctyp);
+
+/* FSOUR_A4 (source/pmbound.f90:1540-1620) in the frame of target plane
+ * iplane (+-1 Y, +-2 X, +-3 Z; negative on max faces). */
+double vpmo_fsour_a4(const double xo[3], const double rg[3], int iplane, const double dpm[3], double area);
 
 /* Full field step, WhatToDo = 2 (source/vpm.f90:171-314 with yaps3d) for
  * one block.  xp(3,nvr), qp(4,nvr) column-major; up/gp(3,nvr) outputs.

@@ -59,7 +59,7 @@ def test_status_strings_and_bad_configs(gpulib):
     for st in range(0, -9, -1):
         assert L.vpmg_status_string(st)
     cfg = gpulib.VPMConfig.make(dpm=(0.1, 0.1, 0.1))
-    for field, val, code in (("interf_iproj", 9, -1), ("ibctyp", 3, -6), ("idvpm", 0, -6), ("ncell_rem", 2, -6)):
+    for field, val, code in (("interf_iproj", 9, -1), ("ibctyp", 1, -6), ("ibctyp", 4, -6), ("idvpm", 0, -6), ("ncell_rem", 2, -6)):
         c = gpulib.VPMConfig.make(dpm=(0.1, 0.1, 0.1))
         setattr(c, field, val)
         h = C.c_void_p()

@@ -82,7 +82,7 @@ def _directions(x0, q0, n, seed=5):
     return out
 
 
-@pytest.mark.parametrize("case", ["ring32", "ring64", "ring32_nc2"])
+@pytest.mark.parametrize("case", ["ring32", "ring64", "ring32_nc2", "ring32_panels"])
 def test_poisson_transpose_identity(gpulib, case):
     from vpm_free_gb300 import workloads as W
     V = gpulib
@@ -92,6 +92,9 @@ def test_poisson_transpose_identity(gpulib, case):
     elif case == "ring64":
         xp, qp, w = W.ring64()
         _, gcfg = configs_for(w)
+    elif case == "ring32_panels":  # ibctyp = 3: constant-source panel boundary
+        xp, qp, w = W.scaled_ring(32)
+        _, gcfg = configs_for(w, ibctyp=3)
     else:  # ncoarse = 2: dummy quadtree cells on the padded block
         xp, qp, w = W.scaled_ring(32)
         _, gcfg = configs_for(w, ncoarse=2)

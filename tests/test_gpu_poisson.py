@@ -57,6 +57,30 @@ def test_infinite_domain_matches_oracle(gpulib, oracle, n, levmax):
         assert rel_l2(out[c], ref[c]) <= 1e-10, c
 
 
+@pytest.mark.parametrize("n,levmax,itree,d", [(33, 2, 1, (0.1, 0.1, 0.1)), (37, 3, 1, (0.1, 0.08, 0.12)),
+                                               (29, 0, 1, (0.1, 0.1, 0.1)), (21, 0, 0, (0.1, 0.09, 0.11))])
+def test_constant_panel_boundary_matches_oracle(gpulib, oracle, n, levmax, itree, d):
+    """ibctyp = 3 (constant-source panels, FSOUR_A4): the tree walk
+    tree_calc_3d_s (37: dummy cells at level 3, anisotropic spacing;
+    levmax 0: every cell at the coarsest level) and the untreed
+    calc_boundinf_3d_s, through pmesh(iynbc = 1)."""
+    V = gpulib
+    rng = np.random.default_rng(9)
+    xb = tuple(-(n - 1) * d[k] / 2 for k in range(3)) + tuple((n - 1) * d[k] / 2 for k in range(3))
+    ax = [xb[k] + d[k] * np.arange(n) for k in range(3)]
+    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    blob = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (0.25 * xb[3] ** 2))
+    rhs = [blob * rng.uniform(0.5, 1.5) + 0.01 * rng.standard_normal(blob.shape) * blob for _ in range(3)]
+    ref = [np.zeros_like(blob) for _ in range(3)]
+    oracle.pmesh(ref, rhs, xb, d, iynbc=1, itree=itree, levmax=levmax, ibctyp=3)
+    cfg = V.VPMConfig.make(dpm=d, box=(0, 0, 0, 0.8, 0.8, 0.8), ibctyp=3)
+    with V.VPM(cfg) as hd:
+        out = [np.zeros_like(blob) for _ in range(3)]
+        hd.pmesh(out, rhs, xb, d, iynbc=1, itree=itree, levmax=levmax)
+    for c in range(3):
+        assert rel_l2(out[c], ref[c]) <= 1e-10, c
+
+
 def test_dst_tile_shape_does_not_change_results(gpulib):
     """The autotuned tile (line pairs per CTA) must not change a single bit:
     the same Dirichlet solve with each tile forced through VPMG_DST_PAIRS,

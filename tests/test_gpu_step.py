@@ -183,6 +183,26 @@ def test_two_level_ncoarse2_matches_oracle(gpulib, oracle):
     assert rel_l2(up, up_o) <= PART_TOL and rel_l2(gp, gp_o) <= PART_TOL
 
 
+@pytest.mark.parametrize("iyntree", [1, 0])
+def test_constant_panel_step_matches_oracle(gpulib, oracle, iyntree):
+    """A whole WhatToDo = 2 step with ibctyp = 3 on the fine block and the
+    coarse YAPS grid, treed and untreed."""
+    from vpm_free_gb300 import workloads as W
+    V, O = gpulib, oracle
+    xp, qp, w = W.scaled_ring(32)
+    ocfg, gcfg = configs_for(w, ibctyp=3, iyntree=iyntree)
+    s = O.define_sizes(ocfg, xp)
+    up_o, gp_o = O.step_fields(ocfg, s, xp, qp)
+    with V.VPM(gcfg) as h:
+        h.define_sizes(xp)
+        up = np.zeros_like(up_o)
+        gp = np.zeros_like(gp_o)
+        h.vpm(xp, qp, up, gp, xp.shape[0], WhatToDo=2)
+        for name, fid in _pairs(V, O):
+            assert rel_l2(h.field(name).ravel(), O.get_field(fid)) <= FIELD_TOL, name
+    assert rel_l2(up, up_o) <= PART_TOL and rel_l2(gp, gp_o) <= PART_TOL
+
+
 def test_viscous_diffusion_matches_oracle(gpulib, oracle):
     """vpm(WhatToDo = 5): deposition, diffuse_vort_3d and the GP gather of
     back_to_particles_3D(itype = 2) (source/vpm.f90:345-372)."""

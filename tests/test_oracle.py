@@ -116,6 +116,62 @@ def test_tree_close_to_direct_sum_and_levmax0_equals_direct(oracle):
     assert nt < nd and nf == nd
 
 
+def test_fsour_a4_is_the_constant_source_panel_potential(oracle):
+    """FSOUR_A4 (source/pmbound.f90:1540-1620) against the integral
+    -1/(4 pi) ∫∫ dS / |x - y| over the panel, by adaptive quadrature, for
+    points above, beside (in the panel's plane) and below the panel, in
+    the frame of every target plane; far points take the monopole branch."""
+    from scipy import integrate
+    d = (0.1, 0.07, 0.05)
+    frames = {1: ((1, 0, 0), (0, 0, 1), (0, -1, 0), 0.1, 0.05), 2: ((0, 0, 1), (0, -1, 0), (-1, 0, 0), 0.07, 0.05),
+              3: ((1, 0, 0), (0, -1, 0), (0, 0, -1), 0.1, 0.07)}
+    rg = np.array([0.3, -0.2, 0.1])
+    for iplane in (1, -1, 2, -2, 3, -3):
+        e1, e2, e3, a, b = frames[abs(iplane)]
+        si = 1 if iplane > 0 else -1
+        E1, E2, E3 = np.array(e1, float), np.array(e2, float), np.array(e3, float)
+        if abs(iplane) == 1:
+            E1, E3 = E1 * si, E3 * si
+        else:
+            E2, E3 = E2 * si, E3 * si
+        for off in ((0.03, 0.02, 0.04), (0.0, 0.0, 0.01), (0.2, -0.1, 0.03), (0.05, 0.035, 1e-4),
+                    (0.01, 0.01, -0.02), (0.09, 0.0, 0.0), (0.0, -0.06, 0.0)):
+            xo = rg + off[0] * E1 + off[1] * E2 + off[2] * E3
+            got = oracle.fsour_a4(xo, rg, iplane, d, a * b)
+            val, _ = integrate.dblquad(lambda t, s: 1.0 / np.linalg.norm(xo - (rg + s * E1 + t * E2)),
+                                       -a / 2, a / 2, -b / 2, b / 2, epsabs=1e-14, epsrel=1e-12)
+            assert abs(got + val / (4 * np.pi)) <= 1e-12 * abs(val), (iplane, off)
+        far = rg + 3.0 * E3
+        assert oracle.fsour_a4(far, rg, iplane, d, a * b) == -(a * b / (4 * np.pi)) / 3.0
+
+
+def test_constant_panel_boundary_values(oracle):
+    """ibctyp = 3: the untreed panel sum (calc_boundinf_3d_s) is close to
+    the point-source sum of ibctyp = 2 (the two differ only in the near
+    field of each node); the tree walk of ibctyp = 3 (tree_calc_3d_s) runs
+    with its start-cell source at the coarsest level, as written."""
+    n, h = 25, 0.1
+    L = (n - 1) * h / 2
+    x = -L + h * np.arange(n)
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    blob = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (0.2 * L * L))
+    sol0 = [np.zeros_like(blob) for _ in range(3)]
+    for c in range(3):
+        oracle.dirichlet(-blob * (c + 1), sol0[c], (h, h, h), zero_bc=True)
+    xb = (-L, -L, -L, L, L, L)
+    face = np.zeros(blob.shape, bool)
+    face[0] = face[-1] = True
+    face[:, 0] = face[:, -1] = True
+    face[:, :, 0] = face[:, :, -1] = True
+    p2, n2 = oracle.boundary_values(sol0, xb, (h, h, h), 0, direct=True, ibctyp=2)
+    p3, n3 = oracle.boundary_values(sol0, xb, (h, h, h), 0, direct=True, ibctyp=3)
+    t3, nt = oracle.boundary_values(sol0, xb, (h, h, h), 3, ibctyp=3)
+    assert n2 == n3 and nt < n3
+    for c in range(3):
+        assert 0 < rel_l2(p3[c][face], p2[c][face]) <= 3e-2
+        assert np.all(np.isfinite(t3[c][face])) and np.all(t3[c][~face] == 0)
+
+
 def test_sizes_known_answers(oracle):
     from vpm_free_gb300 import workloads as W
     for gen, nn, nnbl, nnc in ((W.ring64, 65, 81, 17), (W.leapfrog256, 257, 273, 41)):

@@ -277,7 +277,7 @@ class VPM:
         return m.value
 
     def pmesh(self, SOL, RHS, Xbound, Dpm, iynbc, itree=1, levmax=3, NN_bl=None):
-        """pmesh (source/pmlib.f90:69-192), 3 components, ibctyp = 2.
+        """pmesh (source/pmlib.f90:69-192), 3 components, the handle's ibctyp.
         SOL, RHS: lists of 3 arrays shaped (NZ, NY, NX); SOL updated in place."""
         nz, ny, nx = RHS[0].shape
         sol = [_f64(s) for s in SOL]

@@ -158,8 +158,8 @@ void prepare(vpmg_handle* h) {
   }
   // boundary operators: fine block (levels ilevmax), coarse (ilevmax-1); iyntree = 0 -> untreed sum
   const bool tree = h->cfg.iyntree == 1;
-  boundary_prepare(h->bo_bl, h->gbl, tree ? std::max(s.ilevmax, 0) : 0, h->op_budget, st);
-  boundary_prepare(h->bo_c, h->gco, tree ? std::max(s.ilevmax - 1, 0) : 0, h->op_budget, st);
+  boundary_prepare(h->bo_bl, h->gbl, tree ? std::max(s.ilevmax, 0) : 0, h->op_budget, st, h->cfg.ibctyp, tree);
+  boundary_prepare(h->bo_c, h->gco, tree ? std::max(s.ilevmax - 1, 0) : 0, h->op_budget, st, h->cfg.ibctyp, tree);
   // YAPS maps
   YapsGeom Y;
   try {
@@ -449,7 +449,7 @@ int vpmg_create(const vpmg_config* cfg, int device, vpmg_handle** out) {
   if (!cfg || !out) return VPMG_ERR_ARG;
   *out = nullptr;
   if (cfg->interf_iproj < 2 || cfg->interf_iproj > 6) return VPMG_ERR_ARG;
-  if (cfg->ibctyp != 2) return VPMG_ERR_UNSUPPORTED;
+  if (cfg->ibctyp != 2 && cfg->ibctyp != 3) return VPMG_ERR_UNSUPPORTED;
   if (cfg->idvpm != 1) return VPMG_ERR_UNSUPPORTED;
   if (cfg->ncell_rem != 1) return VPMG_ERR_UNSUPPORTED;
   if (cfg->ncoarse < 1 || cfg->dpm[0] <= 0 || cfg->dpm[1] <= 0 || cfg->dpm[2] <= 0) return VPMG_ERR_ARG;
@@ -993,7 +993,7 @@ int vpmg_pmesh(vpmg_handle* h, double* const sol[3], const double* const rhs[3],
       w.ensure((size_t)dp.m[0] * dp.m[1] * dp.m[2]);
       fill_zero(s0.p, n, h->stream);
       BoundaryOp bo;
-      boundary_prepare(bo, g, itree == 1 ? levmax : 0, h->op_budget, h->stream);
+      boundary_prepare(bo, g, itree == 1 ? levmax : 0, h->op_budget, h->stream, h->cfg.ibctyp, itree == 1);
       for (int c = 0; c < 3; ++c) {
         dirichlet_solve(dp, r.p + c * n, s0.p, true, w.p, h->stream);
         boundary_panels(bo, g, s0.p, c, h->stream);

@@ -8,7 +8,11 @@
 //     of every quadtree cell (topology and geometry come from the host);
 //   * Bounds3d_lev / tree_calc_3d (pmbound.f90:980-1249): for every
 //     boundary node, sum of -s dS / r over the tree with the opening test
-//     r < 10 sqrt(dS), then SOL += sum / (4 pi).
+//     r < 10 sqrt(dS), then SOL += sum / (4 pi)  (ibctyp = 2);
+//   * ibctyp = 3, constant-source panels: tree_calc_3d_s
+//     (pmbound.f90:1379-1501) and the untreed calc_boundinf_3d_s
+//     (pmbound.f90:520-648), whose unopened cells contribute the panel
+//     potential FSOUR_A4 (pmbound.f90:1540-1620) where the reference calls it.
 // The walk is evaluated with explicitly rounded operations so its opening
 // decisions are those of the reference's expressions.  Because the mesh is
 // frozen after the first step, the walk's interaction list (cell, dS/r) is
@@ -38,8 +42,66 @@ struct WalkDev {
   const double *tx, *ty, *tz;
   int top0, ntop, levmax, ntarget;
   double lg;      // log((sqrt2-1)/(sqrt2+1))
-  double inv_pi4;
+  double inv_pi4, pi4;
+  int bctype;     // 2 or 3
+  int tree;       // 1: Bounds3d_lev walk; 0: untreed sum (levmax = 0)
+  const int* tgt_frame;
+  PanelFrame frame[6];
 };
+
+// FSOUR_A4 (source/pmbound.f90:1540-1620) with NSIDE = 0, ISING = 0,
+// EPSS = 1e-14: potential at XO of a flat quadrilateral of unit constant
+// source centred at RG, corners (S, T) in the frame (E1, E2, E3) of the
+// target's plane.  Sums and products are explicitly rounded in the
+// reference's order so the RATIO > 10 branch and the near-edge
+// |A1*A2| < TINY cut decide as its expressions do.
+__device__ double fsour_a4(const double XO[3], const double RG[3], const PanelFrame& F, double AREA, double PI4) {
+  const double COSB[4] = {0.0, 1.0, 0.0, -1.0}, SINB[4] = {1.0, 0.0, -1.0, 0.0};
+  const double TINY = 1e-10, EPSS = 1e-14;
+  const double d0 = __dsub_rn(XO[0], RG[0]), d1 = __dsub_rn(XO[1], RG[1]), d2 = __dsub_rn(XO[2], RG[2]);
+  const double X = __dadd_rn(__dadd_rn(__dmul_rn(d0, F.E1[0]), __dmul_rn(d1, F.E1[1])), __dmul_rn(d2, F.E1[2]));
+  const double Y = __dadd_rn(__dadd_rn(__dmul_rn(d0, F.E2[0]), __dmul_rn(d1, F.E2[1])), __dmul_rn(d2, F.E2[2]));
+  double Z = __dadd_rn(__dadd_rn(__dmul_rn(d0, F.E3[0]), __dmul_rn(d1, F.E3[1])), __dmul_rn(d2, F.E3[2]));
+  const double RO = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(X, X), __dmul_rn(Y, Y)), __dmul_rn(Z, Z)));
+  if (__ddiv_rn(RO, F.diag) > 10.0) return -__ddiv_rn(__ddiv_rn(AREA, PI4), RO);
+  const double ZP = (Z < 0.0) ? -1.0 : 1.0;
+  double AZ = fmax(EPSS, fabs(Z));
+  Z = __dmul_rn(AZ, ZP);
+  const double ZK = __dmul_rn(Z, Z);
+  double R[4], E[4], H[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double xs = __dsub_rn(X, F.S[k]), yt = __dsub_rn(Y, F.T[k]);
+    const double XK = __dmul_rn(xs, xs), YK = __dmul_rn(yt, yt);
+    H[k] = __dmul_rn(xs, yt);
+    R[k] = __dsqrt_rn(__dadd_rn(__dadd_rn(XK, YK), ZK));
+    E[k] = __dadd_rn(ZK, XK);
+  }
+  double FIL = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int k2 = (k == 3) ? 0 : k + 1;
+    const double rr = __dadd_rn(R[k], R[k2]);
+    const double A2 = __dadd_rn(rr, F.D[k]), A1 = __dsub_rn(rr, F.D[k]);
+    if (fabs(__dmul_rn(A1, A2)) < TINY) continue;
+    const double AK = log(__ddiv_rn(A1, A2));
+    const double TOO = __dadd_rn(__dmul_rn(-__dsub_rn(X, F.S[k]), SINB[k]), __dmul_rn(__dsub_rn(Y, F.T[k]), COSB[k]));
+    FIL = __dsub_rn(FIL, __dmul_rn(TOO, AK));
+  }
+  AZ = fmax(TINY, AZ);
+  Z = __dmul_rn(AZ, ZP);
+  double UL3 = 0.0;
+#pragma unroll
+  for (int k = 1; k < 4; k += 2) {  // COSB != 0 on sides 2 and 4 only
+    const int k2 = (k == 3) ? 0 : k + 1;
+    const double zc = __dmul_rn(Z, COSB[k]);
+    const double t1 = atan(__ddiv_rn(__dsub_rn(__dmul_rn(SINB[k], E[k]), __dmul_rn(COSB[k], H[k])), __dmul_rn(zc, R[k])));
+    const double t2 =
+        atan(__ddiv_rn(__dsub_rn(__dmul_rn(SINB[k], E[k2]), __dmul_rn(COSB[k], H[k2])), __dmul_rn(zc, R[k2])));
+    UL3 = __dsub_rn(__dadd_rn(UL3, t1), t2);
+  }
+  return __ddiv_rn(__dadd_rn(FIL, __dmul_rn(Z, UL3)), PI4);
+}
 
 enum { kAccum = 0, kCount = 1, kFill = 2, kTranspose = 3 };
 
@@ -74,7 +136,11 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
     const double XR = __dsub_rn(W.cx[c], X), YR = __dsub_rn(W.cy[c], Y), ZR = __dsub_rn(W.cz[c], Z);
     const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(XR, XR), __dmul_rn(YR, YR)), __dmul_rn(ZR, ZR)));
     const int fl = W.flags[c];
-    if ((r < W.cthr[c] && L > 0) || fl < 0) {
+    // ibctyp 3 (tree_calc_3d_s) tests r / sqrt(dS) < 10 and always opens
+    // only the -1 dummies; a -2 dummy has dS = 0 and is never opened.
+    const bool open = (W.bctype == 3) ? ((__ddiv_rn(r, __dsqrt_rn(W.cds[c])) < 10.0 && L > 0) || fl == -1)
+                                      : ((r < W.cthr[c] && L > 0) || fl < 0);
+    if (open) {
       parent[L - 1] = c;
       cnt[L - 1] = (fl < 0) ? 2 : 4;
       pos[L - 1] = 0;
@@ -86,17 +152,35 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
       continue;
     }
     const double DS = W.cds[c];
-    const double w = (r > 1e-05) ? __ddiv_rn(DS, r) : -2.0 * __dsqrt_rn(DS) * W.lg;
+    double w;
+    int cc = c;
+    if (W.bctype == 3) {
+      if (L == W.levmax) {
+        // coarsest level: FSOUR_A4 of the cell (area dS in the tree, the
+        // target plane's cell area in the untreed sum), weighting the
+        // source of the walk's start cell nv = 1 in the tree
+        // (pmbound.f90:1492-1496) and the cell's own in the untreed sum
+        const PanelFrame& F = W.frame[W.tgt_frame[t]];
+        const double XO[3] = {X, Y, Z}, RG[3] = {W.cx[c], W.cy[c], W.cz[c]};
+        const double fis = fsour_a4(XO, RG, F, W.tree ? DS : F.area, W.pi4);
+        w = -fis * W.pi4;
+        if (W.tree) cc = W.top0;
+      } else {
+        w = __ddiv_rn(DS, r);
+      }
+    } else {
+      w = (r > 1e-05) ? __ddiv_rn(DS, r) : -2.0 * __dsqrt_rn(DS) * W.lg;
+    }
     if (MODE == kFill) {
-      col[out] = c;
+      col[out] = cc;
       wgt[out] = w;
       ++out;
     } else if (MODE == kTranspose) {
-      if (bcv != 0.0) atomicAdd(&o0[c], w * bcv);
+      if (bcv != 0.0) atomicAdd(&o0[cc], w * bcv);
     } else {
-      a0 = fma(-W.s0[c], w, a0);
-      a1 = fma(-W.s1[c], w, a1);
-      a2 = fma(-W.s2[c], w, a2);
+      a0 = fma(-W.s0[cc], w, a0);
+      a1 = fma(-W.s1[cc], w, a1);
+      a2 = fma(-W.s2[cc], w, a2);
     }
   }
   if (MODE == kCount) {
@@ -214,7 +298,43 @@ WalkDev walk_dev(const BoundaryOp& B) {
   W.ntarget = B.ntarget;
   W.lg = std::log((std::sqrt(2.0) - 1.0) / (std::sqrt(2.0) + 1.0));
   W.inv_pi4 = 1.0 / (4.0 * kPI);
+  W.pi4 = 4.0 * kPI;
+  W.bctype = B.ibctyp;
+  W.tree = B.tree ? 1 : 0;
+  W.tgt_frame = B.tgt_frame.p;
+  for (int f = 0; f < 6; ++f) W.frame[f] = B.frame[f];
   return W;
+}
+
+// Slot of Bounds3d_lev's plane argument: 2/-2 X min/max, 1/-1 Y, 3/-3 Z.
+int frame_slot(int iplane) { return 2 * ((iplane > 0 ? iplane : -iplane) - 1) + (iplane < 0 ? 1 : 0); }
+
+// Constants of calc_boundinf_3d_s / calc_boundinf_3d_lev_s for one plane
+// (source/pmbound.f90:536-606, 1270-1340).
+PanelFrame make_frame(int iplane, const double d[3]) {
+  PanelFrame F;
+  const double DX = d[0], DY = d[1], DZ = d[2];
+  const double si = iplane > 0 ? 1.0 : -1.0;
+  for (int m = 0; m < 3; ++m) F.E1[m] = F.E2[m] = F.E3[m] = 0.0;
+  double a, b;  // cell sides along E1 and E2
+  switch (iplane > 0 ? iplane : -iplane) {
+    case 1:
+      F.E1[0] = si; F.E2[2] = 1.0; F.E3[1] = -si;
+      F.diag = std::sqrt(DX * DX + DZ * DZ); F.area = DX * DZ; a = DX; b = DZ;
+      break;
+    case 2:
+      F.E1[2] = 1.0; F.E2[1] = -si; F.E3[0] = -si;
+      F.diag = std::sqrt(DY * DY + DZ * DZ); F.area = DY * DZ; a = DY; b = DZ;
+      break;
+    default:
+      F.E1[0] = 1.0; F.E2[1] = -si; F.E3[2] = -si;
+      F.diag = std::sqrt(DX * DX + DY * DY); F.area = DX * DY; a = DX; b = DY;
+      break;
+  }
+  F.S[0] = -0.5 * a; F.S[1] = -0.5 * a; F.S[2] = 0.5 * a; F.S[3] = 0.5 * a;
+  F.T[0] = -0.5 * b; F.T[1] = 0.5 * b; F.T[2] = 0.5 * b; F.T[3] = -0.5 * b;
+  F.D[0] = b; F.D[1] = a; F.D[2] = b; F.D[3] = a;
+  return F;
 }
 
 }  // namespace
@@ -224,8 +344,17 @@ long long BoundaryOp::bytes() const {
                      cx.bytes() * 5 + child.bytes() + csrc.bytes());
 }
 
-void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s) {
+void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s, int ibctyp,
+                      bool tree) {
   VPMG_CHECK(levmax >= 0 && levmax < kMaxLev - 1, VPMG_ERR_ARG, "levmax out of range");
+  VPMG_CHECK(ibctyp == 2 || ibctyp == 3, VPMG_ERR_UNSUPPORTED, "ibctyp must be 2 or 3");
+  VPMG_CHECK(tree || levmax == 0, VPMG_ERR_ARG, "the untreed sum has one level");
+  B.ibctyp = ibctyp;
+  B.tree = tree;
+  for (int p = 1; p <= 3; ++p) {
+    B.frame[frame_slot(p)] = make_frame(p, g.d);
+    B.frame[frame_slot(-p)] = make_frame(-p, g.d);
+  }
   TreeGeom T;
   try {
     build_tree_geometry(g.xmin, g.d, g.n, levmax, T);
@@ -281,12 +410,13 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
   }
   upload(B.pan_face, pf); upload(B.pan_i, pi); upload(B.pan_j, pj); upload(B.pan_k, pk);
   B.ntarget = (int)T.targets.size();
-  std::vector<int> tn(B.ntarget);
+  std::vector<int> tn(B.ntarget), tf(B.ntarget);
   std::vector<double> tx(B.ntarget), ty(B.ntarget), tz(B.ntarget);
   for (int t = 0; t < B.ntarget; ++t) {
     tn[t] = (int)T.targets[t].node; tx[t] = T.targets[t].x; ty[t] = T.targets[t].y; tz[t] = T.targets[t].z;
+    tf[t] = frame_slot(T.targets[t].iplane);
   }
-  upload(B.tgt_node, tn); upload(B.tx, tx); upload(B.ty, ty); upload(B.tz, tz);
+  upload(B.tgt_node, tn); upload(B.tx, tx); upload(B.ty, ty); upload(B.tz, tz); upload(B.tgt_frame, tf);
   // ---- record the interaction lists if they fit --------------------------
   B.precomputed = false;
   B.nnz = 0;

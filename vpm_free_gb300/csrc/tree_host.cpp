@@ -152,18 +152,19 @@ void build_tree_geometry(const double xmin[3], const double d[3], const int n[3]
     }
   // ---- targets, Bounds3d_lev order ---------------------------------------
   T.targets.clear();
-  auto tgt = [&](int i, int j, int k) {
+  auto tgt = [&](int i, int j, int k, int iplane) {
     Target t;
     t.node = (long long)(i - 1) + (long long)NX * ((j - 1) + (long long)NY * (k - 1));
     t.x = node_coord(XMIN, i, DX); t.y = node_coord(YMIN, j, DY); t.z = node_coord(ZMIN, k, DZ);
+    t.iplane = iplane;
     T.targets.push_back(t);
   };
-  for (int k = 1; k <= NZ; ++k) for (int j = 1; j <= NY; ++j) tgt(1, j, k);
-  for (int k = 1; k <= NZ; ++k) for (int j = 1; j <= NY; ++j) tgt(NX, j, k);
-  for (int k = 1; k <= NZ; ++k) for (int i = 2; i <= NX - 1; ++i) tgt(i, 1, k);
-  for (int k = 1; k <= NZ; ++k) for (int i = 2; i <= NX - 1; ++i) tgt(i, NY, k);
-  for (int j = 2; j <= NY - 1; ++j) for (int i = 2; i <= NX - 1; ++i) tgt(i, j, 1);
-  for (int j = 2; j <= NY - 1; ++j) for (int i = 2; i <= NX - 1; ++i) tgt(i, j, NZ);
+  for (int k = 1; k <= NZ; ++k) for (int j = 1; j <= NY; ++j) tgt(1, j, k, 2);
+  for (int k = 1; k <= NZ; ++k) for (int j = 1; j <= NY; ++j) tgt(NX, j, k, -2);
+  for (int k = 1; k <= NZ; ++k) for (int i = 2; i <= NX - 1; ++i) tgt(i, 1, k, 1);
+  for (int k = 1; k <= NZ; ++k) for (int i = 2; i <= NX - 1; ++i) tgt(i, NY, k, -1);
+  for (int j = 2; j <= NY - 1; ++j) for (int i = 2; i <= NX - 1; ++i) tgt(i, j, 1, 3);
+  for (int j = 2; j <= NY - 1; ++j) for (int i = 2; i <= NX - 1; ++i) tgt(i, j, NZ, -3);
 }
 
 }  // namespace vpmg

@@ -19,6 +19,7 @@ struct Cell {       // one entry of the level arrays xs_lev.. / ilev_t
 struct Target {
   long long node;   // linear 0-based node index in the grid array
   double x, y, z;
+  int iplane;       // plane argument of Bounds3d_lev: 2/-2 X min/max, 1/-1 Y, 3/-3 Z
 };
 
 struct TreeGeom {

@@ -114,9 +114,19 @@ void dst_x_inv_to_box(const FFTPlan& p, const double* data, double* sol, const i
 
 // ------------------------------------------------- boundary operator ----
 struct TreeGeom;  // host-built quadtree of one grid (tree_host.cpp)
+// Frame of one boundary plane for the constant-source panel potential
+// (FSOUR_A4): unit vectors E1..E3, corner offsets S/T, side lengths D,
+// diagonal and area of one cell of that plane.
+struct PanelFrame {
+  double E1[3], E2[3], E3[3], S[4], T[4], D[4], diag, area;
+};
+
 struct BoundaryOp {
   // panels (level 0) and aggregated levels, device copies
   int nbound = 0, levmax = 0, ncell_total = 0, ntarget = 0;
+  int ibctyp = 2;     // 2: point sources -dS/(4 pi r); 3: constant-source panels
+  bool tree = true;   // Bounds3d_lev (tree) or the untreed Bounds3d
+  PanelFrame frame[6];                  // ibctyp 3: one per target plane
   std::vector<int> lev_off;    // flat offset of each level's cells
   std::vector<int> nbound_lev; // cumulative cells per level (all faces)
   DBuf<double> cx, cy, cz, cds, cthr;   // per flat cell: centre, area, 10*sqrt(ds)
@@ -132,6 +142,7 @@ struct BoundaryOp {
   // targets
   DBuf<int> tgt_node;                   // linear node index of each boundary node
   DBuf<double> tx, ty, tz;
+  DBuf<int> tgt_frame;                  // ibctyp 3: frame slot of each target's plane
   // precomputed operator (CSR over targets)
   bool precomputed = false;
   long long nnz = 0;
@@ -145,7 +156,8 @@ struct BoundaryOp {
   DBuf<double> tw;
   long long bytes() const;
 };
-void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s);
+void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s,
+                      int ibctyp = 2, bool tree = true);
 // Per component: normal-derivative panels from the zero-BC solution sol0,
 // aggregate, then add the boundary values into the faces of sol.
 void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp, cudaStream_t s);
