@@ -84,6 +84,7 @@ def lib():
                                     C.c_int, C.c_int, C.c_int]
         L.vpmo_fsour_a4.argtypes = [_dp, _dp, C.c_int, _dp, C.c_double]
         L.vpmo_fsour_a4.restype = C.c_double
+        L.vpmo_yaps_seam.restype = C.c_double
         _LIB = L
     return _LIB
 

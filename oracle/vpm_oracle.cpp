@@ -724,8 +724,8 @@ void vpmo_definepm(int itype, double Xbound[6], double Dpm[3], int ndum, const i
 }
 
 int vpmo_define_sizes(const vpmo_config* cfg, const double* xp, int nvr, int ntime, vpmo_sizes* s) {
-  // source/vpm.f90:477-660, one block (BLOCKS = np = 1)
-  if (cfg->nbi != 1 || cfg->nbj != 1 || cfg->nbk != 1) return -2;
+  // source/vpm.f90:477-660; the sizes are block 1's, which all blocks share
+  if (cfg->nbi < 1 || cfg->nbj < 1 || cfg->nbk < 1) return -2;
   const bool recompute = (ntime == 0 && cfg->idefine == 1) || cfg->idefine == 0 || !s->defined;
   if (recompute) {
     double Xb[6], Dpm[3] = {cfg->dpm[0], cfg->dpm[1], cfg->dpm[2]};
@@ -858,6 +858,305 @@ double vpmo_fsour_a4(const double xo[3], const double rg[3], int iplane, const d
   return fsour_a4(xo, rg, make_frame(iplane, dpm), area);
 }
 
+// yaps3d (source/yaps3d.f90:1-453) for NBI x NBJ x NBK blocks, the blocks
+// run one after the other as the ranks would; with rhsscat_3d and
+// solget_3d (source/vpm_mpi.f90:199-328).  Writes the global SOL into W.sol.
+static double g_yaps_seam = 0.0;
+static int yaps_multi(const vpmo_config* cfg, const vpmo_sizes* s, Scratch& W, int nthreads) {
+  const int NBI = cfg->nbi, NBJ = cfg->nbj, NBK = cfg->nbk, B = NBI * NBJ * NBK;
+  const int NX = s->nn[0], NY = s->nn[1];
+  const int BX = s->nnbl[0], BY = s->nnbl[1], BZ = s->nnbl[2];
+  const size_t NB = (size_t)BX * BY * BZ;
+  const int CX = s->nn_coarse[0], CY = s->nn_coarse[1], CZ = s->nn_coarse[2];
+  const size_t NC = (size_t)CX * CY * CZ;
+  const int* nbb = s->nnbl_bl;
+  const int NXs = nbb[0], NYs = nbb[1], NZs = nbb[2], NXf = nbb[3], NYf = nbb[4], NZf = nbb[5];
+  const int nc = cfg->ncoarse;
+  const double* Xb = s->xbound;
+  const double* D = s->dpm;
+  // block boxes (vpm.f90:561-596): all blocks have the sizes of block 1
+  const int NXbl = fnint((Xb[3] - Xb[0]) / D[0]) / NBI, NYbl = fnint((Xb[4] - Xb[1]) / D[1]) / NBJ,
+            NZbl = fnint((Xb[5] - Xb[2]) / D[2]) / NBK;
+  std::vector<double> xbl(6 * (size_t)B);
+  for (int k = 1; k <= NBK; ++k)
+    for (int j = 1; j <= NBJ; ++j)
+      for (int i = 1; i <= NBI; ++i) {
+        const int nb = (k - 1) * NBJ * NBI + (j - 1) * NBI + i;
+        double Xt[6] = {Xb[0] + (double)((i - 1) * NXbl) * D[0], Xb[1] + (double)((j - 1) * NYbl) * D[1],
+                        Xb[2] + (double)((k - 1) * NZbl) * D[2], Xb[0] + (double)(i * NXbl) * D[0],
+                        Xb[1] + (double)(j * NYbl) * D[1], Xb[2] + (double)(k * NZbl) * D[2]};
+        double Dt[3] = {D[0], D[1], D[2]};
+        const int nsb[3] = {nc, nc, nc};
+        int nnt[3], nnbt[6];
+        vpmo_definepm(1, Xt, Dt, nc, nsb, nnt, nnbt);
+        for (int d = 0; d < 3; ++d)
+          if (nnt[d] != s->nnbl[d]) return -7;
+        for (int d = 0; d < 6; ++d) xbl[6 * (size_t)(nb - 1) + d] = Xt[d];
+      }
+  auto coords = [&](int nb, int& bi, int& bj, int& bk) {  // 1-based block position of block nb (1-based)
+    bi = (nb - 1) % NBI + 1; bj = ((nb - 1) / NBI) % NBJ + 1; bk = (nb - 1) / (NBI * NBJ) + 1;
+  };
+  std::vector<std::vector<double>> rbl((size_t)B * 3), sbl((size_t)B * 3);
+  for (int b = 0; b < B; ++b) {
+    int bi, bj, bk;
+    coords(b + 1, bi, bj, bk);
+    // rhsscat_3d
+    const int ixs = (bi - 1) * (NXf - NXs) + s->nn_bl[0], jxs = (bj - 1) * (NYf - NYs) + s->nn_bl[1],
+              kxs = (bk - 1) * (NZf - NZs) + s->nn_bl[2];
+    for (int c = 0; c < 3; ++c) {
+      std::vector<double>& R = rbl[3 * b + c];
+      R.assign(NB, 0.0);
+      sbl[3 * b + c].assign(NB, 0.0);
+      for (int k = NZs; k <= NZf; ++k)
+        for (int j = NYs; j <= NYf; ++j)
+          for (int i = NXs; i <= NXf; ++i)
+            R[lin(BX, BY, i, j, k)] = W.rhs[c][lin(NX, NY, ixs + i - NXs, jxs + j - NYs, kxs + k - NZs)];
+      for (int k = 1; k <= BZ; ++k)
+        for (int j = 1; j <= BY; ++j)
+          for (int i = 1; i <= BX; ++i)
+            if ((bi > 1 && i == NXs) || (bj > 1 && j == NYs) || (bk > 1 && k == NZs)) R[lin(BX, BY, i, j, k)] = 0.0;
+    }
+    // pmesh(iynbc = 1) on the padded block
+    double* sp[3] = {sbl[3 * b].data(), sbl[3 * b + 1].data(), sbl[3 * b + 2].data()};
+    double* rp[3] = {rbl[3 * b].data(), rbl[3 * b + 1].data(), rbl[3 * b + 2].data()};
+    const int e = pmesh(sp, rp, &xbl[6 * (size_t)b], s->dpm, s->nnbl, s->nnbl_bl, 1, cfg->iyntree, s->ilevmax,
+                        nthreads, cfg->ibctyp);
+    if (e) return e;
+  }
+  // sampling and map_nodes of every block (yaps3d.f90:104-138)
+  std::vector<std::vector<double>> samp((size_t)B * 3);
+  std::vector<std::vector<char>> mapn(B);
+  std::vector<int> cmap(6 * (size_t)B, -1);
+  for (int b = 0; b < B; ++b) {
+    for (int c = 0; c < 3; ++c) samp[3 * b + c].assign(NC, 0.0);
+    mapn[b].assign(NC, 0);
+    const double* xb = &xbl[6 * (size_t)b];
+    int* mp = &cmap[6 * (size_t)b];
+    for (int k = 1; k <= BZ; k += nc)
+      for (int j = 1; j <= BY; j += nc)
+        for (int i = 1; i <= BX; i += nc) {
+          const double X0 = xb[0] + (double)(i - 1) * s->dpm[0];
+          const double X1 = xb[1] + (double)(j - 1) * s->dpm[1];
+          const double X2 = xb[2] + (double)(k - 1) * s->dpm[2];
+          const int in = fnint((X0 - s->xbound_coarse[0]) / s->dpm_coarse[0]) + 1;
+          const int jn = fnint((X1 - s->xbound_coarse[1]) / s->dpm_coarse[1]) + 1;
+          const int kn = fnint((X2 - s->xbound_coarse[2]) / s->dpm_coarse[2]) + 1;
+          if (i == 1) mp[0] = in;
+          if (i == BX) mp[3] = in;
+          if (j == 1) mp[1] = jn;
+          if (j == BY) mp[4] = jn;
+          if (k == 1) mp[2] = kn;
+          if (k == BZ) mp[5] = kn;
+          if (in < 1 || in > CX || jn < 1 || jn > CY || kn < 1 || kn > CZ) return -5;
+          for (int c = 0; c < 3; ++c) samp[3 * b + c][lin(CX, CY, in, jn, kn)] = sbl[3 * b + c][lin(BX, BY, i, j, k)];
+          mapn[b][lin(CX, CY, in, jn, kn)] = 1;
+        }
+  }
+  // coarse RHS: sum over blocks of calc_laplacian_coarse_3d inside each map (yaps3d.f90:254-261, 1990-2016)
+  const double dc2[3] = {s->dpm_coarse[0] * s->dpm_coarse[0], s->dpm_coarse[1] * s->dpm_coarse[1],
+                         s->dpm_coarse[2] * s->dpm_coarse[2]};
+  for (int c = 0; c < 3; ++c) W.c_rhs[c].assign(NC, 0.0);
+  for (int b = 0; b < B; ++b) {
+    const int* mp = &cmap[6 * (size_t)b];
+    for (int c = 0; c < 3; ++c) {
+      const std::vector<double>& S = samp[3 * b + c];
+      auto Sm = [&](int i, int j, int k) { return S[lin(CX, CY, i, j, k)]; };
+      std::vector<double> tmp(NC, 0.0);
+      for (int k = mp[2] + 1; k <= mp[5] - 1; ++k)
+        for (int j = mp[1] + 1; j <= mp[4] - 1; ++j)
+          for (int i = mp[0] + 1; i <= mp[3] - 1; ++i)
+            tmp[lin(CX, CY, i, j, k)] = ((Sm(i + 1, j, k) - 2.0 * Sm(i, j, k)) + Sm(i - 1, j, k)) / dc2[0] +
+                                        ((Sm(i, j + 1, k) - 2.0 * Sm(i, j, k)) + Sm(i, j - 1, k)) / dc2[1] +
+                                        ((Sm(i, j, k + 1) - 2.0 * Sm(i, j, k)) + Sm(i, j, k - 1)) / dc2[2];
+      for (size_t n = 0; n < NC; ++n) W.c_rhs[c][n] = W.c_rhs[c][n] + tmp[n];
+    }
+  }
+  // coarse infinite-domain solve (yaps3d.f90:286-299)
+  {
+    for (int c = 0; c < 3; ++c) W.c_sol[c].assign(NC, 0.0);
+    double* cs[3] = {W.c_sol[0].data(), W.c_sol[1].data(), W.c_sol[2].data()};
+    double* cr[3] = {W.c_rhs[0].data(), W.c_rhs[1].data(), W.c_rhs[2].data()};
+    const int itree = cfg->iyntree == 1 ? 1 : 0;
+    const int lmax = itree ? s->ilevmax - 1 : 1;
+    const int e = pmesh(cs, cr, s->xbound_coarse, s->dpm_coarse, s->nn_coarse, s->nn_bl_coarse, 1, itree, lmax,
+                        nthreads, cfg->ibctyp);
+    if (e) return e;
+  }
+  // mapnodes_bl (yaps3d.f90:457-1912): every block sends each of its 26
+  // neighbours the values of its first solution at the neighbour's inner-face
+  // nodes that lie in its padded block, faces facing it only.  Restated from
+  // the 26 transfers as one rule: along an axis with offset o = +1 (receiver
+  // above the sender) the receiver range is [s, s+nc], o = -1 gives [f-nc, f],
+  // o = 0 the inner range [s, f]; the sender index is the receiver's plus
+  // o * (f - s); a face is sent when the offset along its normal is 0 or
+  // points from the sender to it.  BBound(node, 1:3, sender) per receiver.
+  const int isx = BX, isy = BY, isz = BZ;
+  const int iface12 = isy * isz, iface34 = isx * isz, iface56 = isx * isy;
+  const int ibound = 2 * (iface12 + iface34 + iface56);
+  std::vector<double> bbound((size_t)B * B * ibound * 3, 0.0);  // [recv][sender][node][c]
+  auto BBv = [&](int r, int snd, int node, int c) -> double& {
+    return bbound[(((size_t)r * B + snd) * ibound + (node - 1)) * 3 + c];
+  };
+  const int lo[3] = {NXs, NYs, NZs}, hi[3] = {NXf, NYf, NZf};
+  for (int sb = 1; sb <= B; ++sb) {
+    int si, sj, sk;
+    coords(sb, si, sj, sk);
+    for (int oz = -1; oz <= 1; ++oz)
+      for (int oy = -1; oy <= 1; ++oy)
+        for (int ox = -1; ox <= 1; ++ox) {
+          if (!ox && !oy && !oz) continue;
+          const int ri = si + ox, rj = sj + oy, rk = sk + oz;
+          if (ri < 1 || ri > NBI || rj < 1 || rj > NBJ || rk < 1 || rk > NBK) continue;
+          const int rb = (rk - 1) * NBJ * NBI + (rj - 1) * NBI + ri;
+          const int o[3] = {ox, oy, oz};
+          auto range = [&](int d, int& a, int& z) {
+            if (o[d] > 0) { a = lo[d]; z = lo[d] + nc; }
+            else if (o[d] < 0) { a = hi[d] - nc; z = hi[d]; }
+            else { a = lo[d]; z = hi[d]; }
+          };
+          for (int face = 0; face < 6; ++face) {
+            const int ax = face / 2, side = face % 2;  // side 0: min face, 1: max face
+            if (side == 0 && o[ax] < 0) continue;
+            if (side == 1 && o[ax] > 0) continue;
+            const int plane = side == 0 ? lo[ax] : hi[ax];
+            const int u = ax == 0 ? 1 : 0, v = ax == 2 ? 1 : 2;  // in-plane axes, u fastest
+            int ua, uz, va, vz;
+            range(u, ua, uz);
+            range(v, va, vz);
+            const int nodstart = ax == 0 ? side * iface12 : (ax == 1 ? 2 * iface12 + side * iface34
+                                                                     : 2 * iface12 + 2 * iface34 + side * iface56);
+            const int ustride = ax == 0 ? isy : isx;
+            for (int vv = va; vv <= vz; ++vv)
+              for (int uu = ua; uu <= uz; ++uu) {
+                int rcv[3];
+                rcv[ax] = plane; rcv[u] = uu; rcv[v] = vv;
+                int snd[3];
+                for (int d = 0; d < 3; ++d) snd[d] = rcv[d] + o[d] * (hi[d] - lo[d]);
+                const int node = nodstart + (vv - 1) * ustride + uu;
+                for (int c = 0; c < 3; ++c)
+                  BBv(rb - 1, sb - 1, node, c) = BBv(rb - 1, sb - 1, node, c) +
+                                                 sbl[3 * (sb - 1) + c][lin(BX, BY, snd[0], snd[1], snd[2])];
+              }
+          }
+        }
+  }
+  // interp_stencil on every block's inner faces (yaps3d.f90:340-395, 1914-1983)
+  for (int nb = 1; nb <= B; ++nb) {
+    int bi, bj, bk;
+    coords(nb, bi, bj, bk);
+    const double* xb = &xbl[6 * (size_t)(nb - 1)];
+    std::vector<double>* S = &sbl[3 * (size_t)(nb - 1)];
+    std::vector<int> nnb(B);
+    auto interp = [&](int i, int j, int k, int node) {
+      const double X0 = xb[0] + (double)(i - 1) * s->dpm[0];
+      const double X1 = xb[1] + (double)(j - 1) * s->dpm[1];
+      const double X2 = xb[2] + (double)(k - 1) * s->dpm[2];
+      const int in = fnint((X0 - s->xbound_coarse[0]) / s->dpm_coarse[0]) + 1;
+      const int jn = fnint((X1 - s->xbound_coarse[1]) / s->dpm_coarse[1]) + 1;
+      const int kn = fnint((X2 - s->xbound_coarse[2]) / s->dpm_coarse[2]) + 1;
+      for (int b = 0; b < B; ++b)
+        nnb[b] = !(mapn[b][lin(CX, CY, in - 1, jn - 1, kn - 1)] == 1 && mapn[b][lin(CX, CY, in + 1, jn + 1, kn + 1)] == 1);
+      for (int kc = kn - 1; kc <= kn + 1; ++kc)
+        for (int jc = jn - 1; jc <= jn + 1; ++jc)
+          for (int ic = in - 1; ic <= in + 1; ++ic) {
+            const size_t cid = lin(CX, CY, ic, jc, kc);
+            double add[3] = {0, 0, 0}, add_sample[3] = {0, 0, 0};
+            for (int b = 0; b < B; ++b)
+              for (int c = 0; c < 3; ++c) {
+                add_sample[c] = samp[3 * b + c][cid] + add_sample[c];
+                if (nnb[b] == 1) add[c] = samp[3 * b + c][cid] + add[c];
+              }
+            const double xc = (X0 - s->xbound_coarse[0] - (double)(ic - 1) * s->dpm_coarse[0]) / s->dpm_coarse[0];
+            const double fx = projection_fun(3, xc);
+            const double yc = (X1 - s->xbound_coarse[1] - (double)(jc - 1) * s->dpm_coarse[1]) / s->dpm_coarse[1];
+            const double fy = projection_fun(3, yc);
+            const double zc = (X2 - s->xbound_coarse[2] - (double)(kc - 1) * s->dpm_coarse[2]) / s->dpm_coarse[2];
+            const double fz = projection_fun(3, zc);
+            const double f = fx * fy * fz;
+            for (int c = 0; c < 3; ++c) {
+              double& v = S[c][lin(BX, BY, i, j, k)];
+              v = v + f * ((W.c_sol[c][cid] - add_sample[c]) + add[c]);
+            }
+          }
+      for (int kb = bk - 1; kb <= bk + 1; ++kb)
+        for (int jb = bj - 1; jb <= bj + 1; ++jb)
+          for (int ib = bi - 1; ib <= bi + 1; ++ib) {
+            if (ib < 1 || ib > NBI || jb < 1 || jb > NBJ || kb < 1 || kb > NBK) continue;
+            const int nbc = (kb - 1) * NBI * NBJ + (jb - 1) * NBI + ib;
+            if (nnb[nbc - 1] == 1 || nbc == nb) continue;
+            for (int c = 0; c < 3; ++c) {
+              double& v = S[c][lin(BX, BY, i, j, k)];
+              v = v + BBv(nb - 1, nbc - 1, node, c);
+            }
+          }
+    };
+    // BBound is read from the first solutions: interp_stencil of every block
+    // runs after mapnodes_bl has copied them, so updating S here is safe.
+    for (int k = NZs; k <= NZf; ++k) for (int j = NYs; j <= NYf; ++j) interp(NXs, j, k, (k - 1) * isy + j);
+    for (int k = NZs; k <= NZf; ++k) for (int j = NYs; j <= NYf; ++j) interp(NXf, j, k, iface12 + (k - 1) * isy + j);
+    for (int k = NZs; k <= NZf; ++k)
+      for (int i = NXs + 1; i <= NXf - 1; ++i) interp(i, NYs, k, 2 * iface12 + (k - 1) * isx + i);
+    for (int k = NZs; k <= NZf; ++k)
+      for (int i = NXs + 1; i <= NXf - 1; ++i) interp(i, NYf, k, 2 * iface12 + iface34 + (k - 1) * isx + i);
+    for (int j = NYs + 1; j <= NYf - 1; ++j)
+      for (int i = NXs + 1; i <= NXf - 1; ++i) interp(i, j, NZs, 2 * iface12 + 2 * iface34 + (j - 1) * isx + i);
+    for (int j = NYs + 1; j <= NYf - 1; ++j)
+      for (int i = NXs + 1; i <= NXf - 1; ++i)
+        interp(i, j, NZf, 2 * iface12 + 2 * iface34 + iface56 + (j - 1) * isx + i);
+  }
+  // seam check: nodes shared by the inner faces of several blocks must get
+  // the same boundary value from every block (same terms, other order)
+  {
+    std::vector<double> first(3 * (size_t)W.rhs[0].size(), 0.0);
+    std::vector<char> seen(W.rhs[0].size(), 0);
+    double worst = 0.0, scale = 0.0;
+    for (int b = 0; b < B; ++b) {
+      int bi, bj, bk;
+      coords(b + 1, bi, bj, bk);
+      const int ixs = (bi - 1) * (NXf - NXs) + s->nn_bl[0], jxs = (bj - 1) * (NYf - NYs) + s->nn_bl[1],
+                kxs = (bk - 1) * (NZf - NZs) + s->nn_bl[2];
+      for (int k = NZs; k <= NZf; ++k)
+        for (int j = NYs; j <= NYf; ++j)
+          for (int i = NXs; i <= NXf; ++i) {
+            if (i != NXs && i != NXf && j != NYs && j != NYf && k != NZs && k != NZf) continue;
+            const size_t g = lin(NX, NY, ixs + i - NXs, jxs + j - NYs, kxs + k - NZs);
+            for (int c = 0; c < 3; ++c) {
+              const double v = sbl[3 * b + c][lin(BX, BY, i, j, k)];
+              scale = std::max(scale, std::fabs(v));
+              if (seen[g]) worst = std::max(worst, std::fabs(v - first[3 * g + c]));
+              else first[3 * g + c] = v;
+            }
+            seen[g] = 1;
+          }
+    }
+    g_yaps_seam = scale > 0 ? worst / scale : 0.0;
+  }
+  // final Dirichlet solve on each inner box (yaps3d.f90:415-421), then solget_3d in block order
+  for (int b = 0; b < B; ++b) {
+    double* sp[3] = {sbl[3 * b].data(), sbl[3 * b + 1].data(), sbl[3 * b + 2].data()};
+    double* rp[3] = {rbl[3 * b].data(), rbl[3 * b + 1].data(), rbl[3 * b + 2].data()};
+    const int e = pmesh(sp, rp, &xbl[6 * (size_t)b], s->dpm, s->nnbl, s->nnbl_bl, 0, 0, 0, nthreads);
+    if (e) return e;
+  }
+  for (int b = 0; b < B; ++b) {
+    int bi, bj, bk;
+    coords(b + 1, bi, bj, bk);
+    const int ixs = (bi - 1) * (NXf - NXs) + s->nn_bl[0], jxs = (bj - 1) * (NYf - NYs) + s->nn_bl[1],
+              kxs = (bk - 1) * (NZf - NZs) + s->nn_bl[2];
+    for (int c = 0; c < 3; ++c)
+      for (int k = NZs; k <= NZf; ++k)
+        for (int j = NYs; j <= NYf; ++j)
+          for (int i = NXs; i <= NXf; ++i)
+            W.sol[c][lin(NX, NY, ixs + i - NXs, jxs + j - NYs, kxs + k - NZs)] = sbl[3 * b + c][lin(BX, BY, i, j, k)];
+  }
+  if (B >= 1) {  // block 1's fields for vpmo_get_field
+    for (int c = 0; c < 3; ++c) W.bl_final[c] = sbl[c];
+  }
+  return 0;
+}
+
+double vpmo_yaps_seam(void) { return g_yaps_seam; }
+
 int vpmo_step_fields(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, double* up,
                      double* gp, int nvr, int nthreads) {
   Scratch& W = g_scr;
@@ -875,6 +1174,10 @@ int vpmo_step_fields(const vpmo_config* cfg, const vpmo_sizes* s, const double* 
   // 1. deposition + volume division (vpm.f90:408-444)
   int e = vpmo_project_particles(s, cfg->interf_iproj, xp, qp, nvr, W.rhs[0].data(), W.rhs[1].data(), W.rhs[2].data(), nthreads);
   if (e) return e;
+  if (cfg->nbi * cfg->nbj * cfg->nbk > 1) {
+    e = yaps_multi(cfg, s, W, nthreads);
+    if (e) return e;
+  } else {
   // 2. rhsscat_3d (vpm_mpi.f90:199-238), one block
   std::vector<double> rbl[3], sbl[3];
   for (int c = 0; c < 3; ++c) { rbl[c].assign(NB, 0.0); sbl[c].assign(NB, 0.0); }
@@ -984,6 +1287,7 @@ int vpmo_step_fields(const vpmo_config* cfg, const vpmo_sizes* s, const double* 
       for (int j = nbb[1]; j <= nbb[4]; ++j)
         for (int i = nbb[0]; i <= nbb[3]; ++i)
           W.sol[c][lin(NX, NY, i - nbb[0] + s->nn_bl[0], j - nbb[1] + s->nn_bl[1], k - nbb[2] + s->nn_bl[2])] = sbl[c][lin(BX, BY, i, j, k)];
+  }
   // 5. calc_velocity_serial_3d(1) (vpm_gcalc.f90:1-136)
   {
     const double DX2 = 2 * s->dpm[0], DY2 = 2 * s->dpm[1], DZ2 = 2 * s->dpm[2];

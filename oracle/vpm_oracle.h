@@ -109,6 +109,12 @@ double vpmo_fsour_a4(const double xo[3], const double rg[3], int iplane, const d
 int vpmo_step_fields(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp,
                      const double* qp, double* up, double* gp, int nvr, int nthreads);
 
+/* With NBI x NBJ x NBK > 1 blocks: the largest difference, relative to the
+ * largest face value, between the boundary values that blocks sharing an
+ * inner-face node assign to it in the last vpmo_step_fields (a check of
+ * the neighbour transfers; 0 with one block). */
+double vpmo_yaps_seam(void);
+
 /* Field ids for vpmo_get_field / the CUDA library's vpmg_get_field. */
 enum {
   VPMO_F_RHS = 0,      /* global RHS_pm(1:3) after project_vol3d      [3 x N]   */

@@ -203,6 +203,53 @@ def test_constant_panel_step_matches_oracle(gpulib, oracle, iyntree):
     assert rel_l2(up, up_o) <= PART_TOL and rel_l2(gp, gp_o) <= PART_TOL
 
 
+@pytest.mark.parametrize("nb,nc,ncell,extra", [((2, 1, 1), 8, 32, {}), ((2, 2, 2), 4, 32, {}),
+                                               ((3, 2, 1), 4, 48, {}), ((2, 2, 1), 4, 32, {"ibctyp": 3}),
+                                               ((1, 2, 2), 4, 32, {"iyntree": 0})])
+def test_multiblock_step_matches_oracle(gpulib, oracle, nb, nc, ncell, extra):
+    """YAPS on NBI x NBJ x NBK blocks of one GPU (rhsscat, per-block
+    infinite-domain solves, neighbour transfers as gathers, solget) against
+    the oracle's block-by-block restatement: every mesh field and the
+    particle velocities and stretching of one WhatToDo = 2 step."""
+    from vpm_free_gb300 import workloads as W
+    V, O = gpulib, oracle
+    xp, qp, w = W.scaled_ring(ncell)
+    ocfg, gcfg = configs_for(w, nb=nb, ncoarse=nc, **extra)
+    s = O.define_sizes(ocfg, xp)
+    up_o, gp_o = O.step_fields(ocfg, s, xp, qp)
+    with V.VPM(gcfg) as h:
+        h.define_sizes(xp)
+        up = np.zeros_like(up_o)
+        gp = np.zeros_like(gp_o)
+        h.vpm(xp, qp, up, gp, xp.shape[0], WhatToDo=2)
+        for name, fid in _pairs(V, O):
+            assert rel_l2(h.field(name).ravel(), O.get_field(fid)) <= FIELD_TOL, name
+    assert rel_l2(up, up_o) <= PART_TOL and rel_l2(gp, gp_o) <= PART_TOL
+
+
+def test_multiblock_steps_on_device_match_oracle(gpulib, oracle):
+    """2 x 2 x 2 blocks through the device-resident loop (graph replay,
+    Euler, remesh) for three steps against the oracle's steps."""
+    from vpm_free_gb300 import workloads as W
+    V, O = gpulib, oracle
+    xp, qp, w = W.scaled_ring(32)
+    ocfg, gcfg = configs_for(w, nb=(2, 2, 2), ncoarse=4)
+    s = O.define_sizes(ocfg, xp)
+    xo, qo = O.remesh(ocfg, s, xp, qp)
+    with V.VPM(gcfg) as h:
+        h.define_sizes(xp)
+        xg, qg = h.remesh_particles_3d(1, xp, qp)
+        h.set_particles(xg, qg)
+        for step in range(3):
+            up, gp = O.step_fields(ocfg, s, xo, qo)
+            O.euler(xo, qo, up, gp, w["dt"])
+            xo, qo = O.remesh(ocfg, s, xo, qo)
+            h.step(w["dt"])
+            xg, qg = h.get_particles()
+            assert xg.shape[0] == xo.shape[0], step
+            assert rel_l2(xg, xo) <= PART_TOL and rel_l2(qg, qo) <= PART_TOL, step
+
+
 def test_viscous_diffusion_matches_oracle(gpulib, oracle):
     """vpm(WhatToDo = 5): deposition, diffuse_vort_3d and the GP gather of
     back_to_particles_3D(itype = 2) (source/vpm.f90:345-372)."""

@@ -172,6 +172,38 @@ def test_constant_panel_boundary_values(oracle):
         assert np.all(np.isfinite(t3[c][face])) and np.all(t3[c][~face] == 0)
 
 
+@pytest.mark.parametrize("nb,nc,ncell", [((2, 1, 1), 4, 32), ((1, 1, 2), 4, 32), ((2, 2, 2), 4, 32),
+                                         ((3, 2, 1), 4, 48), ((3, 3, 3), 8, 48)])
+def test_multiblock_seams_agree(oracle, nb, nc, ncell):
+    """NBI x NBJ x NBK YAPS blocks (yaps3d.f90 with mapnodes_bl's neighbour
+    transfers): every node that lies on the inner faces of several blocks
+    (shared planes, edges, corners) gets the same boundary value from each
+    of them, because the same terms reach it through the neighbours'
+    transfers.  A wrong transfer shows as a seam of the size of the field."""
+    from vpm_free_gb300 import workloads as W
+    xp, qp, w = W.scaled_ring(ncell)
+    cfg = oracle.make_config(dpm=w["dpm"], box=w["box"], nb=nb, ncoarse=nc)
+    s = oracle.define_sizes(cfg, xp)
+    oracle.step_fields(cfg, s, xp, qp, nthreads=4)
+    assert oracle.lib().vpmo_yaps_seam() <= 1e-14
+
+
+def test_multiblock_close_to_one_block(oracle):
+    """The block decomposition changes the YAPS approximation, not the
+    problem: psi of 2 x 2 x 2 blocks stays within the coarse-correction
+    error (a few 1e-2 with ncoarse = 4 on 32^3) of the one-block psi."""
+    from vpm_free_gb300 import workloads as W
+    xp, qp, w = W.scaled_ring(32)
+    out = []
+    for nb in ((1, 1, 1), (2, 2, 2)):
+        cfg = oracle.make_config(dpm=w["dpm"], box=w["box"], nb=nb, ncoarse=4)
+        s = oracle.define_sizes(cfg, xp)
+        up, _ = oracle.step_fields(cfg, s, xp, qp, nthreads=4)
+        out.append((oracle.get_field(oracle.F_SOL).copy(), up))
+    assert 1e-4 < rel_l2(out[1][0], out[0][0]) < 3e-2
+    assert rel_l2(out[1][1], out[0][1]) < 3e-2
+
+
 def test_sizes_known_answers(oracle):
     from vpm_free_gb300 import workloads as W
     for gen, nn, nnbl, nnc in ((W.ring64, 65, 81, 17), (W.leapfrog256, 257, 273, 41)):

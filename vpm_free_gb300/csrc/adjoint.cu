@@ -577,6 +577,7 @@ void copy_ckpt(vpmg_handle* h, int dir) {
 }
 
 void ensure_state(vpmg_handle* h, int K, int nprobe) {
+  VPMG_CHECK(h->nblk == 1, VPMG_ERR_UNSUPPORTED, "the reverse mode runs one YAPS block (NBI = NBJ = NBK = 1)");
   if (!h->adj) h->adj = new AdjointState();
   AdjointState& S = *h->adj;
   const size_t N = h->gglob.count(), NB = h->gbl.count(), NC = h->gco.count();

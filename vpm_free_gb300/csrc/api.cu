@@ -56,8 +56,8 @@ void definepm(int itype, double Xb[6], const double D[3], int ndum, const int ns
 // define_sizes (source/vpm.f90:477-660), one block.  xp: XP(3,nvr).
 void define_sizes(vpmg_handle* h, const double* xp, int nvr, int ntime, vpmg_sizes& s) {
   const vpmg_config& cfg = h->cfg;
-  VPMG_CHECK(cfg.nbi == 1 && cfg.nbj == 1 && cfg.nbk == 1, VPMG_ERR_UNSUPPORTED,
-             "one GPU runs one YAPS block: NBI = NBJ = NBK = 1");
+  VPMG_CHECK(cfg.nbi >= 1 && cfg.nbj >= 1 && cfg.nbk >= 1, VPMG_ERR_ARG, "NBI, NBJ, NBK must be >= 1");
+  const int nbd[3] = {cfg.nbi, cfg.nbj, cfg.nbk};
   const bool recompute = (ntime == 0 && cfg.idefine == 1) || cfg.idefine == 0 || !h->sized;
   if (recompute) {
     double Xb[6], Dpm[3] = {cfg.dpm[0], cfg.dpm[1], cfg.dpm[2]};
@@ -68,7 +68,8 @@ void define_sizes(vpmg_handle* h, const double* xp, int nvr, int ntime, vpmg_siz
         NN[d] = fnint(std::fabs(Xb[d + 3] - Xb[d]) / Dpm[d]) + 1;
         NN_bl[d] = 1;
         NN_bl[d + 3] = NN[d];
-        VPMG_CHECK((NN[d] - 1) % cfg.ncoarse == 0, VPMG_ERR_ARG, "explicit box: cells must divide by ncoarse");
+        VPMG_CHECK((NN[d] - 1) % (nbd[d] * cfg.ncoarse) == 0, VPMG_ERR_ARG,
+                   "explicit box: cells must divide by the block count times ncoarse");
       }
     } else {
       VPMG_CHECK(nvr > 0 && xp, VPMG_ERR_ARG, "define_sizes needs particles to size the box");
@@ -134,11 +135,15 @@ void prepare(vpmg_handle* h) {
   h->gbl = make_grid(s.xbound_bl, s.dpm, s.nnbl);
   h->gco = make_grid(s.xbound_coarse, s.dpm_coarse, s.nn_coarse);
   const size_t N = h->gglob.count(), NB = h->gbl.count(), NC = h->gco.count();
+  h->nb3[0] = h->cfg.nbi; h->nb3[1] = h->cfg.nbj; h->nb3[2] = h->cfg.nbk;
+  h->nblk = h->nb3[0] * h->nb3[1] * h->nb3[2];
+  const size_t B = (size_t)h->nblk;
   h->rhs.ensure(3 * N); h->sol.ensure(3 * N); h->vel.ensure(3 * N); h->def.ensure(3 * N);
-  h->rhs_bl.ensure(3 * NB); h->sol_bl.ensure(3 * NB); h->sol0.ensure(NB);
-  h->samp.ensure(3 * NC); h->crhs.ensure(3 * NC); h->csol.ensure(3 * NC); h->csol0.ensure(NC);
+  h->rhs_bl.ensure(B * 3 * NB); h->sol_bl.ensure(B * 3 * NB); h->sol0.ensure(NB);
+  h->samp.ensure(B * 3 * NC); h->crhs.ensure(3 * NC); h->csol.ensure(3 * NC); h->csol0.ensure(NC);
+  h->sampsum.ensure(3 * NC);
   for (DBuf<double>* b : {&h->rhs, &h->sol, &h->vel, &h->def, &h->rhs_bl, &h->sol_bl, &h->sol0, &h->samp, &h->crhs,
-                          &h->csol, &h->csol0})
+                          &h->csol, &h->csol0, &h->sampsum})
     fill_zero(b->p, b->n, st);
   // Dirichlet plans: whole block, inner block box, whole coarse grid
   const int bl_full[6] = {0, 0, 0, s.nnbl[0] - 1, s.nnbl[1] - 1, s.nnbl[2] - 1};
@@ -151,24 +156,45 @@ void prepare(vpmg_handle* h) {
   size_t wmax = 0;
   for (DirichletPlan* p : {&h->dp_bl, &h->dp_inner, &h->dp_c}) wmax = std::max(wmax, (size_t)p->m[0] * p->m[1] * p->m[2]);
   h->work.ensure(wmax);
-  h->bsolve.prepare(h->dp_bl, s.nnbl_bl, h->cfg.ncoarse);
+  if (h->nblk == 1) h->bsolve.prepare(h->dp_bl, s.nnbl_bl, h->cfg.ncoarse);
   for (int d = 0; d < 3; ++d) {
     h->inner_lo[d] = s.nnbl_bl[d] - 1;
     h->inner_ext[d] = s.nnbl_bl[d + 3] - s.nnbl_bl[d] + 1;
   }
   // boundary operators: fine block (levels ilevmax), coarse (ilevmax-1); iyntree = 0 -> untreed sum
   const bool tree = h->cfg.iyntree == 1;
-  boundary_prepare(h->bo_bl, h->gbl, tree ? std::max(s.ilevmax, 0) : 0, h->op_budget, st, h->cfg.ibctyp, tree);
   boundary_prepare(h->bo_c, h->gco, tree ? std::max(s.ilevmax - 1, 0) : 0, h->op_budget, st, h->cfg.ibctyp, tree);
-  // YAPS maps
-  YapsGeom Y;
-  try {
-    build_yaps_geometry(s.xbound_bl, s.dpm, s.nnbl, s.nnbl_bl, s.xbound_coarse, s.dpm_coarse, s.nn_coarse,
-                        h->cfg.ncoarse, Y);
-  } catch (const std::exception& e) {
-    throw Error{VPMG_ERR_UNSUPPORTED, e.what()};
+  if (h->nblk == 1) {
+    boundary_prepare(h->bo_bl, h->gbl, tree ? std::max(s.ilevmax, 0) : 0, h->op_budget, st, h->cfg.ibctyp, tree);
+    // YAPS maps
+    YapsGeom Y;
+    try {
+      build_yaps_geometry(s.xbound_bl, s.dpm, s.nnbl, s.nnbl_bl, s.xbound_coarse, s.dpm_coarse, s.nn_coarse,
+                          h->cfg.ncoarse, Y);
+    } catch (const std::exception& e) {
+      throw Error{VPMG_ERR_UNSUPPORTED, e.what()};
+    }
+    h->yaps.prepare(Y);
+  } else {
+    // several blocks: block boxes, one boundary operator each (the tree
+    // geometry is built from each block's own coordinates), gather maps
+    YapsMultiGeom Y;
+    try {
+      build_yaps_multi(h->nb3, s.xbound, s.dpm, h->cfg.ncoarse, s.nnbl, s.nnbl_bl, s.xbound_coarse, s.dpm_coarse,
+                       s.nn_coarse, Y);
+    } catch (const std::exception& e) {
+      throw Error{VPMG_ERR_UNSUPPORTED, e.what()};
+    }
+    h->g_blk.assign(h->nblk, Grid{});
+    h->bo_blk.clear();
+    for (int b = 0; b < h->nblk; ++b) {
+      h->g_blk[b] = make_grid(&Y.xbl[6 * (size_t)b], s.dpm, s.nnbl);
+      h->bo_blk.push_back(std::make_unique<BoundaryOp>());
+      boundary_prepare(*h->bo_blk[b], h->g_blk[b], tree ? std::max(s.ilevmax, 0) : 0, h->op_budget / h->nblk, st,
+                       h->cfg.ibctyp, tree);
+    }
+    h->ym.prepare(Y);
   }
-  h->yaps.prepare(Y);
   // particles: capacity for a full remesh of the global mesh
   h->parts.ensure((int)std::min<size_t>(N, (size_t)INT32_MAX / 16));
   h->bins.ensure(N);
@@ -204,7 +230,52 @@ void infinite_domain(vpmg_handle* h, DirichletPlan& dp, BoundaryOp& bo, const Gr
 
 // The vector-potential solve: global RHS (h->rhs) -> global SOL (h->sol),
 // i.e. rhsscat_3d, yaps3d (one block) and solget_3d.
+// yaps3d with NBI x NBJ x NBK blocks (yaps_multi.cu): the blocks' solves run
+// one after the other on the stream, every block solve in full.
+void poisson_part_multi(vpmg_handle* h) {
+  cudaStream_t st = h->stream;
+  const vpmg_sizes& s = h->sz;
+  const size_t N = h->gglob.count(), NB = h->gbl.count(), NC = h->gco.count();
+  yaps_multi_rhsscat(h->ym, h->rhs.p, s.nn, s.nn_bl, s.nnbl, s.nnbl_bl, h->nb3, h->rhs_bl.p, st);
+  fill_zero(h->sol_bl.p, (size_t)h->nblk * 3 * NB, st);
+  ev_mark(h, 1);
+  for (int b = 0; b < h->nblk; ++b) {
+    double* RB = h->rhs_bl.p + (size_t)b * 3 * NB;
+    double* SB[3] = {h->sol_bl.p + (size_t)b * 3 * NB, h->sol_bl.p + ((size_t)b * 3 + 1) * NB,
+                     h->sol_bl.p + ((size_t)b * 3 + 2) * NB};
+    BoundaryOp& bo = *h->bo_blk[b];
+    for (int c = 0; c < 3; ++c) {
+      dirichlet_solve(h->dp_bl, RB + c * NB, h->sol0.p, true, h->work.p, st);
+      boundary_panels(bo, h->g_blk[b], h->sol0.p, c, st);
+    }
+    boundary_apply(bo, h->g_blk[b], SB, st);
+    for (int c = 0; c < 3; ++c) dirichlet_solve(h->dp_bl, RB + c * NB, SB[c], false, h->work.p, st);
+  }
+  if (h->keep_intermediates) {
+    h->bl_sol1_copy.ensure(3 * NB);
+    VPMG_CUDA(cudaMemcpyAsync(h->bl_sol1_copy.p, h->sol_bl.p, sizeof(double) * 3 * NB, cudaMemcpyDeviceToDevice, st));
+  }
+  ev_mark(h, 4);
+  fill_zero(h->csol.p, 3 * NC, st);
+  yaps_multi_coarse(h->ym, h->sol_bl.p, NB, s.nn_coarse, s.dpm_coarse, h->samp.p, h->sampsum.p, h->crhs.p, st);
+  infinite_domain(h, h->dp_c, h->bo_c, h->gco, h->crhs.p, h->csol.p, h->csol0.p, NC);
+  yaps_multi_faces(h->ym, s.nn_coarse, h->csol.p, h->sampsum.p, h->samp.p, h->sol_bl.p, NB, st);
+  ev_mark(h, 5);
+  for (int b = 0; b < h->nblk; ++b)
+    for (int c = 0; c < 3; ++c) {
+      const size_t off = ((size_t)b * 3 + c) * NB;
+      dirichlet_solve(h->dp_inner, h->rhs_bl.p + off, h->sol_bl.p + off, false, h->work.p, st);
+    }
+  yaps_multi_solget(h->sol_bl.p, s.nnbl, s.nnbl_bl, h->nb3, s.nn, s.nn_bl, h->sol.p, st);
+  (void)N;
+  ev_mark(h, 6);
+}
+
 void poisson_part(vpmg_handle* h) {
+  if (h->nblk > 1) {
+    poisson_part_multi(h);
+    return;
+  }
   cudaStream_t st = h->stream;
   const vpmg_sizes& s = h->sz;
   const size_t N = h->gglob.count(), NB = h->gbl.count(), NC = h->gco.count();
@@ -740,10 +811,12 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
     if (which == 0) {
       h->bench_scratch.ensure(3 * NB);
       double* o[3] = {h->bench_scratch.p, h->bench_scratch.p + NB, h->bench_scratch.p + 2 * NB};
-      f = [h, o, st] { boundary_apply(h->bo_bl, h->gbl, o, st); };
-      const double nnz = (double)h->bo_bl.nnz;
+      BoundaryOp* bo = h->nblk > 1 ? h->bo_blk[0].get() : &h->bo_bl;
+      const Grid* g = h->nblk > 1 ? &h->g_blk[0] : &h->gbl;
+      f = [bo, g, o, st] { boundary_apply(*bo, *g, o, st); };
+      const double nnz = (double)bo->nnz;
       fl = 2.0 * 3.0 * nnz;  // three FMAs per interaction
-      by = h->bo_bl.precomputed ? nnz * (sizeof(int) + sizeof(double)) : 0.0;
+      by = bo->precomputed ? nnz * (sizeof(int) + sizeof(double)) : 0.0;
     } else if (which == 1) {
       h->bench_scratch.ensure(NB);
       double* o = h->bench_scratch.p;
@@ -1065,9 +1138,10 @@ int vpmg_phase_times(const vpmg_handle* h, double ms[9]) {
 
 int vpmg_tree_stats(const vpmg_handle* h, long long* interactions, long long* bytes, int* precomputed) {
   if (!h) return VPMG_ERR_ARG;
-  if (interactions) *interactions = h->bo_bl.nnz;
-  if (bytes) *bytes = h->bo_bl.bytes();
-  if (precomputed) *precomputed = h->bo_bl.precomputed ? 1 : 0;
+  const BoundaryOp& bo = h->nblk > 1 && !h->bo_blk.empty() ? *h->bo_blk[0] : h->bo_bl;
+  if (interactions) *interactions = bo.nnz;
+  if (bytes) *bytes = bo.bytes();
+  if (precomputed) *precomputed = bo.precomputed ? 1 : 0;
   return VPMG_OK;
 }
 

@@ -7,6 +7,10 @@
 #include "fields.h"
 #include "particles.h"
 #include "vpmg_internal.h"
+#include "yaps_multi.h"
+
+#include <memory>
+#include <vector>
 
 struct AdjointState;  // adjoint.cu
 
@@ -31,6 +35,13 @@ struct vpmg_handle {
   bool full_block_solves = false;  // evaluate the block solves everywhere (parity / debugging)
   vpmg::BoundaryOp bo_bl, bo_c;
   vpmg::YapsDev yaps;
+  // NBI x NBJ x NBK blocks (nblk > 1): rhs_bl / sol_bl hold [block][3][NB],
+  // samp [block][3][NC]; one boundary operator per block
+  int nblk = 1, nb3[3] = {1, 1, 1};
+  std::vector<std::unique_ptr<vpmg::BoundaryOp>> bo_blk;
+  std::vector<vpmg::Grid> g_blk;
+  vpmg::YapsMultiDev ym;
+  vpmg::DBuf<double> sampsum;
   bool keep_intermediates = false;
   // particles
   vpmg::Particles parts;
