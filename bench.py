@@ -351,7 +351,8 @@ def run_ours(args, dist):
     if args.workload == "dirichlet273":
         return run_dirichlet(args, local)
     xp, qp, w = _workload(args.workload)
-    cfg = V.VPMConfig.make(dpm=w["dpm"], box=w["box"])
+    blocks = tuple(int(v) for v in args.blocks.split(","))
+    cfg = V.VPMConfig.make(dpm=w["dpm"], box=w["box"], nb=blocks)
     h = V.VPM(cfg, device=local)
     if args.operator_budget >= 0:
         h.set_operator_budget(args.operator_budget)
@@ -460,7 +461,7 @@ def run_ours(args, dist):
                      "of NVRM rows (host Euler in place between them)"}
     # ---- CPU baseline (rank 0, N = 1, bounded sample) -----------------------
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu and args.workload == "leapfrog256":
+    if rank == 0 and ws == 1 and not args.no_cpu and args.workload == "leapfrog256" and blocks == (1, 1, 1):
         threads = os.cpu_count() or 1
         v, t, _ = cpu_step_sample(xp, qp, w, 1, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
@@ -479,7 +480,7 @@ def run_ours(args, dist):
         "dtype": "f64", "data": "synthetic (seeded leapfrogging rings)",
         "config": {"workload": ("leapfrog256 (two coaxial rings, 256^3 mesh, M4', tree levels 3, ncoarse 8, remesh "
                                 "every step, dt 0.005)") if args.workload == "leapfrog256" else args.workload,
-                   "mesh": [n - 1 for n in sizes_nn], "block": sizes_bl,
+                   "mesh": [n - 1 for n in sizes_nn], "block": sizes_bl, "yaps_blocks": list(blocks),
                    "particles_start": int(xr.shape[0]), "particles_end": np_end,
                    "l2": "inputs larger than L2 (each field component 135 MB, boundary operator 53 GB)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
@@ -507,6 +508,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--batch-operator-budget", type=int, default=12 << 30,
                     help="bytes of recorded boundary operator per batched problem")
+    ap.add_argument("--blocks", default="1,1,1",
+                    help="YAPS blocks NBI,NBJ,NBK on the one GPU (pm.inp line 7); the headline is 1,1,1")
     ap.add_argument("--operator-budget", type=int, default=-1,
                     help="bytes for the precomputed boundary operator (0: walk the tree each step)")
     args = ap.parse_args()
