@@ -18,8 +18,14 @@
 // frozen after the first step, the walk's interaction list (cell, dS/r) is
 // the same every step: when it fits the memory budget it is recorded once
 // (count + fill passes) and each step is a CSR product with the three
-// source components (3 FP64 FMAs per interaction instead of ~30 FP64
-// operations for sqrt + division + geometry).
+// source components.  The product runs in float-float arithmetic: weights
+// and sources are stored as pairs of floats (hi + lo, a 48-bit mantissa),
+// products are split exactly with an FMA and sums are error-free
+// (two-sum), so the FP32 pipes, about thirty times GB300's FP64 rate, do
+// the work; each lane's partial sum is converted to FP64 before the warp
+// reduction.  The relative error stays near 1e-14, and the product is
+// bound by the 12 bytes per interaction it streams from HBM.
+#include <algorithm>
 #include <cmath>
 
 #include "tree_host.h"
@@ -108,7 +114,7 @@ enum { kAccum = 0, kCount = 1, kFill = 2, kTranspose = 3 };
 template <int MODE>
 __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ o1, double* __restrict__ o2,
                        int* __restrict__ counts, const long long* __restrict__ rowptr, int* __restrict__ col,
-                       double* __restrict__ wgt) {
+                       float2* __restrict__ wgt) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= W.ntarget) return;
   const double X = W.tx[t], Y = W.ty[t], Z = W.tz[t];
@@ -173,7 +179,8 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
     }
     if (MODE == kFill) {
       col[out] = cc;
-      wgt[out] = w;
+      const float hi = __double2float_rn(w);
+      wgt[out] = make_float2(hi, __double2float_rn(w - (double)hi));
       ++out;
     } else if (MODE == kTranspose) {
       if (bcv != 0.0) atomicAdd(&o0[cc], w * bcv);
@@ -193,11 +200,39 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
   }
 }
 
+// Float-float accumulate acc += w * s: the hi product and its exact error
+// (FMA), the cross terms, an error-free two-sum into acc.hi and the errors
+// into acc.lo.  Explicitly rounded intrinsics keep the compiler from
+// fusing the two-sum's operations.
+struct FF {
+  float hi = 0.0f, lo = 0.0f;
+};
+__device__ __forceinline__ void ff_mac(FF& a, float2 w, float2 s) {
+  const float ph = __fmul_rn(w.x, s.x);
+  float pe = __fmaf_rn(w.x, s.x, -ph);
+  pe = __fmaf_rn(w.x, s.y, pe);
+  pe = __fmaf_rn(w.y, s.x, pe);
+  const float t = __fadd_rn(a.hi, ph);
+  const float bp = __fsub_rn(t, a.hi);
+  const float er = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
+  a.lo = __fadd_rn(a.lo, __fadd_rn(er, pe));
+  a.hi = t;
+}
+
+// Sources to float-float pairs, once per apply.
+__global__ void k_split(const double* __restrict__ x, size_t n, float2* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float hi = __double2float_rn(v);
+    out[i] = make_float2(hi, __double2float_rn(v - (double)hi));
+  }
+}
+
 // One warp per boundary node: lanes stride over the node's interaction
 // list (coalesced), fixed-shape shuffle reduction (deterministic).
 __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__ rowptr, const int* __restrict__ col,
-                                                   const double* __restrict__ wgt, const double* __restrict__ s0,
-                                                   const double* __restrict__ s1, const double* __restrict__ s2,
+                                                   const float2* __restrict__ wgt, const float2* __restrict__ s0,
+                                                   const float2* __restrict__ s1, const float2* __restrict__ s2,
                                                    const int* __restrict__ tgt_node, int ntarget, double inv_pi4,
                                                    double* __restrict__ o0, double* __restrict__ o1,
                                                    double* __restrict__ o2) {
@@ -205,14 +240,15 @@ __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
   const long long b = rowptr[warp], e = rowptr[warp + 1];
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  FF f0, f1, f2;
   for (long long k = b + lane; k < e; k += 32) {
     const int c = __ldg(&col[k]);
-    const double w = __ldg(&wgt[k]);
-    a0 = fma(__ldg(&s0[c]), w, a0);
-    a1 = fma(__ldg(&s1[c]), w, a1);
-    a2 = fma(__ldg(&s2[c]), w, a2);
+    const float2 w = __ldg(&wgt[k]);
+    ff_mac(f0, w, __ldg(&s0[c]));
+    ff_mac(f1, w, __ldg(&s1[c]));
+    ff_mac(f2, w, __ldg(&s2[c]));
   }
+  double a0 = (double)f0.hi + (double)f0.lo, a1 = (double)f1.hi + (double)f1.lo, a2 = (double)f2.hi + (double)f2.lo;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     a0 += __shfl_xor_sync(0xffffffffu, a0, o);
@@ -478,8 +514,15 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
     VPMG_LAUNCHED();
   }
   if (B.precomputed) {
+    const size_t nc3 = 3 * (size_t)B.ncell_total;
+    B.csrc_ff.ensure(nc3);
+    k_split<<<(unsigned)std::min<size_t>((nc3 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, nc3, B.csrc_ff.p);
+    VPMG_LAUNCHED();
+    const float2* f0 = B.csrc_ff.p;
+    const float2* f1 = B.csrc_ff.p + B.ncell_total;
+    const float2* f2 = B.csrc_ff.p + 2 * (size_t)B.ncell_total;
     const long long threads = (long long)B.ntarget * 32;
-    k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, s0, s1, s2, B.tgt_node.p,
+    k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, f0, f1, f2, B.tgt_node.p,
                                                                   B.ntarget, 1.0 / (4.0 * kPI), sol[0], sol[1], sol[2]);
   } else {
     const WalkDev W = walk_dev(B);
@@ -499,7 +542,7 @@ namespace vpmg {
 namespace {
 
 __global__ void __launch_bounds__(256) k_csr_T(const long long* __restrict__ rowptr, const int* __restrict__ col,
-                                               const double* __restrict__ wgt, const int* __restrict__ tgt_node,
+                                               const float2* __restrict__ wgt, const int* __restrict__ tgt_node,
                                                int ntarget, double scale, const double* __restrict__ bcbar,
                                                double* __restrict__ cellbar) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -507,7 +550,8 @@ __global__ void __launch_bounds__(256) k_csr_T(const long long* __restrict__ row
   if (warp >= ntarget) return;
   const double v = scale * bcbar[tgt_node[warp]];
   if (v == 0.0) return;
-  for (long long k = rowptr[warp] + lane; k < rowptr[warp + 1]; k += 32) atomicAdd(&cellbar[col[k]], wgt[k] * v);
+  for (long long k = rowptr[warp] + lane; k < rowptr[warp + 1]; k += 32)
+    atomicAdd(&cellbar[col[k]], ((double)wgt[k].x + (double)wgt[k].y) * v);
 }
 
 // Transposed interaction list: per-cell counts, then a fill through per-cell
@@ -520,7 +564,7 @@ __global__ void k_col_count(const long long* __restrict__ rowptr, const int* __r
   for (long long k = rowptr[warp] + lane; k < rowptr[warp + 1]; k += 32) atomicAdd(&cnt[col[k]], 1);
 }
 __global__ void k_col_fill(const long long* __restrict__ rowptr, const int* __restrict__ col,
-                           const double* __restrict__ wgt, int ntarget, const long long* __restrict__ colptr,
+                           const float2* __restrict__ wgt, int ntarget, const long long* __restrict__ colptr,
                            int* __restrict__ cursor, int* __restrict__ trow, double* __restrict__ tw) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -529,7 +573,7 @@ __global__ void k_col_fill(const long long* __restrict__ rowptr, const int* __re
     const int c = col[k];
     const long long slot = colptr[c] + atomicAdd(&cursor[c], 1);
     trow[slot] = warp;
-    tw[slot] = wgt[k];
+    tw[slot] = (double)wgt[k].x + (double)wgt[k].y;
   }
 }
 // cellbar[c] = scale * sum over the cell's targets of w * bcbar(target node); warp per cell.

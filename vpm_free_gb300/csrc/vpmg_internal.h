@@ -137,6 +137,7 @@ struct BoundaryOp {
   DBuf<int> agg_istep;
   DBuf<int> anc;                        // [(lev-1)*nbound + leaf]: flat ancestor cell or -1
   DBuf<double> csrc;                    // 3 * ncell_total aggregated sources
+  DBuf<float2> csrc_ff;                 // the same as float-float pairs (recorded operator)
   // panels: face geometry for the normal derivative
   DBuf<int> pan_face, pan_i, pan_j, pan_k;  // lower-corner node (0-based) of each panel
   // targets
@@ -148,7 +149,7 @@ struct BoundaryOp {
   long long nnz = 0;
   DBuf<long long> rowptr;
   DBuf<int> col;
-  DBuf<double> w;
+  DBuf<float2> w;                       // weights dS/r as float-float pairs (hi, lo), hi + lo = dS/r to 2^-48
   // its transpose (CSR over cells, for the reverse mode), built on first use
   bool transposed = false;
   DBuf<long long> colptr;
