@@ -482,6 +482,7 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
       VPMG_LAUNCHED();
       VPMG_CUDA(cudaGetLastError());
       VPMG_CUDA(cudaStreamSynchronize(s));
+      B.csrc_ff.ensure(3 * (size_t)B.ncell_total);  // here, not in the apply: steps may be captured in graphs
       B.precomputed = true;
     } catch (const Error& e) {
       if (e.status != VPMG_ERR_NOMEM) throw;
@@ -515,7 +516,7 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
   }
   if (B.precomputed) {
     const size_t nc3 = 3 * (size_t)B.ncell_total;
-    B.csrc_ff.ensure(nc3);
+    VPMG_CHECK(B.csrc_ff.n >= nc3, VPMG_ERR_STATE, "boundary operator recorded without its source buffer");
     k_split<<<(unsigned)std::min<size_t>((nc3 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, nc3, B.csrc_ff.p);
     VPMG_LAUNCHED();
     const float2* f0 = B.csrc_ff.p;
