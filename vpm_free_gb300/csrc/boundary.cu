@@ -219,20 +219,26 @@ __device__ __forceinline__ void ff_mac(FF& a, float2 w, float2 s) {
   a.hi = t;
 }
 
-// Sources to float-float pairs, once per apply.
-__global__ void k_split(const double* __restrict__ x, size_t n, float2* __restrict__ out) {
+// Sources to float-float pairs, once per apply, packed per cell as
+// (s0, s1, s2, 0): one 32-byte sector serves a gather of all components.
+__global__ void k_split(const double* __restrict__ x, int ncell, float2* __restrict__ out) {
+  const size_t n = 4 * (size_t)ncell;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double v = x[i];
-    const float hi = __double2float_rn(v);
-    out[i] = make_float2(hi, __double2float_rn(v - (double)hi));
+    const int cell = (int)(i >> 2), comp = (int)(i & 3);
+    float2 v = make_float2(0.0f, 0.0f);
+    if (comp < 3) {
+      const double d = x[(size_t)comp * ncell + cell];
+      const float hi = __double2float_rn(d);
+      v = make_float2(hi, __double2float_rn(d - (double)hi));
+    }
+    out[i] = v;
   }
 }
 
 // One warp per boundary node: lanes stride over the node's interaction
 // list (coalesced), fixed-shape shuffle reduction (deterministic).
 __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__ rowptr, const int* __restrict__ col,
-                                                   const float2* __restrict__ wgt, const float2* __restrict__ s0,
-                                                   const float2* __restrict__ s1, const float2* __restrict__ s2,
+                                                   const float2* __restrict__ wgt, const float4* __restrict__ src,
                                                    const int* __restrict__ tgt_node, int ntarget, double inv_pi4,
                                                    double* __restrict__ o0, double* __restrict__ o1,
                                                    double* __restrict__ o2) {
@@ -240,15 +246,47 @@ __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
   const long long b = rowptr[warp], e = rowptr[warp + 1];
-  FF f0, f1, f2;
-  for (long long k = b + lane; k < e; k += 32) {
+  // Four interactions per lane per trip: their ids and weights are loaded
+  // before any gather so the loads overlap; two accumulator sets break the
+  // two-sum dependency chain.
+  FF f0, f1, f2, g0, g1, g2;
+  long long k = b + lane;
+  for (; k + 96 < e; k += 128) {
+    int c[4];
+    float2 w[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) c[u] = __ldg(&col[k + 32 * u]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) w[u] = __ldg(&wgt[k + 32 * u]);
+    float2 x0[4], x1[4], x2[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float4 a = __ldg(&src[2 * (size_t)c[u]]), z = __ldg(&src[2 * (size_t)c[u] + 1]);
+      x0[u] = make_float2(a.x, a.y);
+      x1[u] = make_float2(a.z, a.w);
+      x2[u] = make_float2(z.x, z.y);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u += 2) {
+      ff_mac(f0, w[u], x0[u]);
+      ff_mac(f1, w[u], x1[u]);
+      ff_mac(f2, w[u], x2[u]);
+      ff_mac(g0, w[u + 1], x0[u + 1]);
+      ff_mac(g1, w[u + 1], x1[u + 1]);
+      ff_mac(g2, w[u + 1], x2[u + 1]);
+    }
+  }
+  for (; k < e; k += 32) {
     const int c = __ldg(&col[k]);
     const float2 w = __ldg(&wgt[k]);
-    ff_mac(f0, w, __ldg(&s0[c]));
-    ff_mac(f1, w, __ldg(&s1[c]));
-    ff_mac(f2, w, __ldg(&s2[c]));
+    const float4 a = __ldg(&src[2 * (size_t)c]), z = __ldg(&src[2 * (size_t)c + 1]);
+    ff_mac(f0, w, make_float2(a.x, a.y));
+    ff_mac(f1, w, make_float2(a.z, a.w));
+    ff_mac(f2, w, make_float2(z.x, z.y));
   }
-  double a0 = (double)f0.hi + (double)f0.lo, a1 = (double)f1.hi + (double)f1.lo, a2 = (double)f2.hi + (double)f2.lo;
+  double a0 = ((double)f0.hi + (double)f0.lo) + ((double)g0.hi + (double)g0.lo);
+  double a1 = ((double)f1.hi + (double)f1.lo) + ((double)g1.hi + (double)g1.lo);
+  double a2 = ((double)f2.hi + (double)f2.lo) + ((double)g2.hi + (double)g2.lo);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     a0 += __shfl_xor_sync(0xffffffffu, a0, o);
@@ -482,7 +520,7 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
       VPMG_LAUNCHED();
       VPMG_CUDA(cudaGetLastError());
       VPMG_CUDA(cudaStreamSynchronize(s));
-      B.csrc_ff.ensure(3 * (size_t)B.ncell_total);  // here, not in the apply: steps may be captured in graphs
+      B.csrc_ff.ensure(4 * (size_t)B.ncell_total);  // here, not in the apply: steps may be captured in graphs
       B.precomputed = true;
     } catch (const Error& e) {
       if (e.status != VPMG_ERR_NOMEM) throw;
@@ -515,16 +553,16 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
     VPMG_LAUNCHED();
   }
   if (B.precomputed) {
-    const size_t nc3 = 3 * (size_t)B.ncell_total;
-    VPMG_CHECK(B.csrc_ff.n >= nc3, VPMG_ERR_STATE, "boundary operator recorded without its source buffer");
-    k_split<<<(unsigned)std::min<size_t>((nc3 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, nc3, B.csrc_ff.p);
+    const size_t nc4 = 4 * (size_t)B.ncell_total;
+    VPMG_CHECK(B.csrc_ff.n >= nc4, VPMG_ERR_STATE, "boundary operator recorded without its source buffer");
+    k_split<<<(unsigned)std::min<size_t>((nc4 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, B.ncell_total,
+                                                                                    B.csrc_ff.p);
     VPMG_LAUNCHED();
-    const float2* f0 = B.csrc_ff.p;
-    const float2* f1 = B.csrc_ff.p + B.ncell_total;
-    const float2* f2 = B.csrc_ff.p + 2 * (size_t)B.ncell_total;
     const long long threads = (long long)B.ntarget * 32;
-    k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, f0, f1, f2, B.tgt_node.p,
-                                                                  B.ntarget, 1.0 / (4.0 * kPI), sol[0], sol[1], sol[2]);
+    k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p,
+                                                                  reinterpret_cast<const float4*>(B.csrc_ff.p),
+                                                                  B.tgt_node.p, B.ntarget, 1.0 / (4.0 * kPI), sol[0],
+                                                                  sol[1], sol[2]);
   } else {
     const WalkDev W = walk_dev(B);
     k_walk<kAccum><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, sol[0], sol[1], sol[2], nullptr, nullptr, nullptr, nullptr);

@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cstdlib>
 
+#include "ff.cuh"
 #include "vpmg_internal.h"
 
 namespace vpmg {
@@ -39,8 +40,8 @@ constexpr int kThreads = 128;
 constexpr int kDefaultPairs = 4;
 constexpr int kMaxOddRadix = 17;  // largest odd prime radix (2*(cells) must factor into 2..17)
 
-__constant__ double c_rcos[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
-__constant__ double c_rsin[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
+__constant__ float2 c_rcos_f[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];  // cos(2 pi i/R), float-float
+__constant__ float2 c_rsin_f[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
 bool g_tables_ready = false;
 
 struct FFTDev {
@@ -49,53 +50,60 @@ struct FFTDev {
   int rs;     // 1: real-symmetric DST-I (M = N), 0: odd extension (M = 2N)
   int pairs;  // line pairs per CTA
   int radix[24];
-  const double2* tw;
+  const float4* tw;  // e^{-2 pi i t / M} as float-float (re.hi, re.lo, im.hi, im.lo)
   const double* sn;  // sin(pi j / N) (rs only)
 };
 
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
-}
+// ---- FFT stages in float-float arithmetic (ff.cuh) ----------------------
+// The stages are the FP64-heaviest part of the solve; on GB300 they run
+// about as fast again in float-float on the FP32 pipes (48-bit significand,
+// error-free sums and products), entered and left by bit operations.
+using ff::cadd;
+using ff::csub;
+using ff::cmul;
 
 template <int R>
 struct DFT;
 
 template <>
 struct DFT<2> {
-  __device__ __forceinline__ static void run(double2 (&v)[2]) {
-    const double2 a = v[0], b = v[1];
+  __device__ __forceinline__ static void run(float4 (&v)[2]) {
+    const float4 a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
   }
 };
 
-__device__ __forceinline__ void dft4(double2& v0, double2& v1, double2& v2, double2& v3) {
-  const double2 t0 = cadd(v0, v2), t1 = csub(v0, v2), t2 = cadd(v1, v3), t3 = csub(v1, v3);
+__device__ __forceinline__ float4 mul_mi(float4 t) { return make_float4(t.z, t.w, -t.x, -t.y); }  // -i t
+__device__ __forceinline__ float4 mul_pi(float4 t) { return make_float4(-t.z, -t.w, t.x, t.y); }  // +i t
+
+__device__ __forceinline__ void dft4(float4& v0, float4& v1, float4& v2, float4& v3) {
+  const float4 t0 = cadd(v0, v2), t1 = csub(v0, v2), t2 = cadd(v1, v3), t3 = csub(v1, v3);
   v0 = cadd(t0, t2);
   v2 = csub(t0, t2);
-  v1 = make_double2(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
-  v3 = make_double2(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
+  v1 = cadd(t1, mul_mi(t3));  // t1 - i t3
+  v3 = cadd(t1, mul_pi(t3));  // t1 + i t3
 }
 
 template <>
 struct DFT<4> {
-  __device__ __forceinline__ static void run(double2 (&v)[4]) { dft4(v[0], v[1], v[2], v[3]); }
+  __device__ __forceinline__ static void run(float4 (&v)[4]) { dft4(v[0], v[1], v[2], v[3]); }
 };
 
 template <>
 struct DFT<8> {
-  __device__ __forceinline__ static void run(double2 (&v)[8]) {
-    double2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
-    double2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  __device__ __forceinline__ static void run(float4 (&v)[8]) {
+    float4 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    float4 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
     dft4(e0, e1, e2, e3);
     dft4(o0, o1, o2, o3);
-    const double r = 0.70710678118654752440084436210484904;
+    const float2 r = make_float2(0.7071067690849304f, 1.2101617485882343e-08f);  // 1/sqrt(2) as hi + lo
     // W8^1 o1 = ((x+y) + i(y-x))/sqrt2 ; W8^2 o2 = -i o2 ; W8^3 o3 = ((y-x) - i(x+y))/sqrt2
-    const double2 w1 = make_double2((o1.x + o1.y) * r, (o1.y - o1.x) * r);
-    const double2 w2 = make_double2(o2.y, -o2.x);
-    const double2 w3 = make_double2((o3.y - o3.x) * r, -(o3.x + o3.y) * r);
+    const float2 s1 = ff::add(ff::re(o1), ff::im(o1)), d1 = ff::sub(ff::im(o1), ff::re(o1));
+    const float2 s3 = ff::add(ff::re(o3), ff::im(o3)), d3 = ff::sub(ff::im(o3), ff::re(o3));
+    const float4 w1 = ff::cplx(ff::mul(s1, r), ff::mul(d1, r));
+    const float4 w2 = mul_mi(o2);
+    const float4 w3 = ff::cplx(ff::mul(d3, r), ff::neg(ff::mul(s3, r)));
     v[0] = cadd(e0, o0);
     v[4] = csub(e0, o0);
     v[1] = cadd(e1, w1);
@@ -110,11 +118,11 @@ struct DFT<8> {
 // Odd radix: X_k = x0 + sum_m [(v_m + v_{R-m}) cos(2 pi mk/R) - i (v_m - v_{R-m}) sin(2 pi mk/R)].
 template <int R>
 struct DFT {
-  __device__ __forceinline__ static void run(double2 (&v)[R]) {
+  __device__ __forceinline__ static void run(float4 (&v)[R]) {
     constexpr int H = (R - 1) / 2;
-    double2 s[H], d[H];
-    const double2 x0 = v[0];
-    double2 sum = x0;
+    float4 s[H], d[H];
+    const float4 x0 = v[0];
+    float4 sum = x0;
 #pragma unroll
     for (int m = 1; m <= H; ++m) {
       s[m - 1] = cadd(v[m], v[R - m]);
@@ -124,20 +132,19 @@ struct DFT {
     v[0] = sum;
 #pragma unroll
     for (int k = 1; k <= H; ++k) {
-      double2 A = x0;
-      double2 B = make_double2(0.0, 0.0);
+      float2 ar = ff::re(x0), ai = ff::im(x0), br = make_float2(0.0f, 0.0f), bi = make_float2(0.0f, 0.0f);
 #pragma unroll
       for (int m = 1; m <= H; ++m) {
         const int idx = (m * k) % R;
-        const double c = c_rcos[R * (kMaxOddRadix + 1) + idx];
-        const double sn = c_rsin[R * (kMaxOddRadix + 1) + idx];
-        A.x = fma(c, s[m - 1].x, A.x);
-        A.y = fma(c, s[m - 1].y, A.y);
-        B.x = fma(sn, d[m - 1].x, B.x);
-        B.y = fma(sn, d[m - 1].y, B.y);
+        const float2 c = c_rcos_f[R * (kMaxOddRadix + 1) + idx];
+        const float2 sn = c_rsin_f[R * (kMaxOddRadix + 1) + idx];
+        ar = ff::fma(c, ff::re(s[m - 1]), ar);
+        ai = ff::fma(c, ff::im(s[m - 1]), ai);
+        br = ff::fma(sn, ff::re(d[m - 1]), br);
+        bi = ff::fma(sn, ff::im(d[m - 1]), bi);
       }
-      v[k] = make_double2(A.x + B.y, A.y - B.x);
-      v[R - k] = make_double2(A.x - B.y, A.y + B.x);
+      v[k] = ff::cplx(ff::add(ar, bi), ff::sub(ai, br));
+      v[R - k] = ff::cplx(ff::sub(ar, bi), ff::add(ai, br));
     }
   }
 };
@@ -145,16 +152,16 @@ struct DFT {
 // One Stockham radix-R stage over npair transforms of length M held back
 // to back in shared memory.
 template <int R>
-__device__ __forceinline__ void stage(const double2* __restrict__ in, double2* __restrict__ out, int M, int Ns,
-                                      const double2* __restrict__ tw, int npair) {
+__device__ __forceinline__ void stage(const float4* __restrict__ in, float4* __restrict__ out, int M, int Ns,
+                                      const float4* __restrict__ tw, int npair) {
   const int nbf = M / R;
   const int tws = M / (Ns * R);
   for (int t = threadIdx.x; t < npair * nbf; t += blockDim.x) {
     const int pr = t / nbf;
     const int j = t - pr * nbf;
-    const double2* src = in + pr * M;
-    double2* dst = out + pr * M;
-    double2 v[R];
+    const float4* src = in + pr * M;
+    float4* dst = out + pr * M;
+    float4 v[R];
 #pragma unroll
     for (int m = 0; m < R; ++m) v[m] = src[j + m * nbf];
     const int k = j % Ns;
@@ -174,7 +181,7 @@ __device__ __forceinline__ void stage(const double2* __restrict__ in, double2* _
 // count (and so the occupancy) of those kernels independent of the large
 // odd-radix butterflies.
 template <bool ODD>
-__device__ double2* fft_all(double2* A, double2* B, const FFTDev& p, int npair) {
+__device__ float4* fft_all(float4* A, float4* B, const FFTDev& p, int npair) {
   int Ns = 1;
   for (int s = 0; s < p.nst; ++s) {
     const int r = p.radix[s];
@@ -198,11 +205,26 @@ __device__ double2* fft_all(double2* A, double2* B, const FFTDev& p, int npair) 
     }
     __syncthreads();
     Ns *= r;
-    double2* t = A;
+    float4* t = A;
     A = B;
     B = t;
   }
   return A;
+}
+
+// In place, the npair * M complex values of a buffer: FP64 <-> float-float
+// (same 16 bytes per value).
+__device__ __forceinline__ void to_ff(double2* z, int n) {
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const double2 v = z[t];
+    reinterpret_cast<float4*>(z)[t] = ff::from_double2(v);
+  }
+}
+__device__ __forceinline__ void from_ff(float4* z, int n) {
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    const float4 v = z[t];
+    reinterpret_cast<double2*>(z)[t] = ff::to_double2(v);
+  }
 }
 
 // Odd extension of the loaded real pairs: z[0] = z[N] = 0, z[M-j] = -z[j].
@@ -306,7 +328,12 @@ __device__ __forceinline__ double2* dst_pairs(double2* A, double2* B, const FFTD
   if (p.rs) rs_pre(B, A, p, npair);
   else odd_extend(A, p, npair);
   __syncthreads();
-  double2* R = fft_all<ODD>(A, B, p, npair);
+  to_ff(A, npair * p.M);
+  __syncthreads();
+  float4* Rf = fft_all<ODD>(reinterpret_cast<float4*>(A), reinterpret_cast<float4*>(B), p, npair);
+  from_ff(Rf, npair * p.M);
+  __syncthreads();
+  double2* R = reinterpret_cast<double2*>(Rf);
   if (!p.rs) return R;
   double2* O = (R == A) ? B : A;
   rs_post(R, O, p, npair);
@@ -600,16 +627,27 @@ FFTDev dev_plan(const FFTPlan& p) {
   return d;
 }
 
-void ensure_tables() {
-  if (g_tables_ready) return;
-  static double hc[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)], hs[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
+// A double as a float-float pair (hi = v rounded to float, lo = the rest).
+float2 host_split(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+
+// cos / sin (2 pi i / R) of the odd radices, float-float.
+void odd_radix_tables(float2* hc, float2* hs) {
   for (int R = 1; R <= kMaxOddRadix; ++R)
     for (int i = 0; i < R; ++i) {
-      hc[R * (kMaxOddRadix + 1) + i] = std::cos(2.0 * kPI * i / R);
-      hs[R * (kMaxOddRadix + 1) + i] = std::sin(2.0 * kPI * i / R);
+      hc[R * (kMaxOddRadix + 1) + i] = host_split(std::cos(2.0 * kPI * i / R));
+      hs[R * (kMaxOddRadix + 1) + i] = host_split(std::sin(2.0 * kPI * i / R));
     }
-  VPMG_CUDA(cudaMemcpyToSymbol(c_rcos, hc, sizeof(hc)));
-  VPMG_CUDA(cudaMemcpyToSymbol(c_rsin, hs, sizeof(hs)));
+}
+
+void ensure_tables() {
+  if (g_tables_ready) return;
+  static float2 hc[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)], hs[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
+  odd_radix_tables(hc, hs);
+  VPMG_CUDA(cudaMemcpyToSymbol(c_rcos_f, hc, sizeof(hc)));
+  VPMG_CUDA(cudaMemcpyToSymbol(c_rsin_f, hs, sizeof(hs)));
   g_tables_ready = true;
 }
 
@@ -711,8 +749,13 @@ void make_fft_plan(FFTPlan& p, int n) {
     const double a = -2.0 * kPI * (double)t / (double)p.M;
     h[t] = make_double2(std::cos(a), std::sin(a));
   }
+  std::vector<float4> hf(p.M);
+  for (int t = 0; t < p.M; ++t) {
+    const float2 r = host_split(h[t].x), i = host_split(h[t].y);
+    hf[t] = make_float4(r.x, r.y, i.x, i.y);
+  }
   p.tw.ensure(p.M);
-  VPMG_CUDA(cudaMemcpy(p.tw.p, h.data(), sizeof(double2) * p.M, cudaMemcpyHostToDevice));
+  VPMG_CUDA(cudaMemcpy(p.tw.p, hf.data(), sizeof(float4) * p.M, cudaMemcpyHostToDevice));
   if (p.rs) {
     std::vector<double> sn(p.N);
     for (int j = 0; j < p.N; ++j) sn[j] = std::sin(kPI * (double)j / (double)p.N);
@@ -843,7 +886,7 @@ constexpr int kStaticMaxDevices = 64;
 double* g_static_base[kStaticMaxDevices] = {nullptr};
 bool g_static_consts[kStaticMaxDevices] = {false};
 
-__global__ void k_static_tables(double2* __restrict__ twx, int mx, double2* __restrict__ twy, int my,
+__global__ void k_static_tables(float4* __restrict__ twx, int mx, float4* __restrict__ twy, int my,
                                 double* __restrict__ mux, int nx, double* __restrict__ muy, int ny,
                                 double* __restrict__ snx, int sx, double* __restrict__ sny, int sy) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -852,11 +895,11 @@ __global__ void k_static_tables(double2* __restrict__ twx, int mx, double2* __re
   if (t < sy) sny[t] = sinpi((double)t / sy);
   if (t < mx) {
     sincospi(-2.0 * t / mx, &sn, &cs);
-    twx[t] = make_double2(cs, sn);
+    twx[t] = ff::from_double2(make_double2(cs, sn));
   }
   if (t < my) {
     sincospi(-2.0 * t / my, &sn, &cs);
-    twy[t] = make_double2(cs, sn);
+    twy[t] = ff::from_double2(make_double2(cs, sn));
   }
   if (t < nx) {
     sn = sinpi((t + 1) / (2.0 * (nx + 1)));
@@ -870,7 +913,7 @@ __global__ void k_static_tables(double2* __restrict__ twx, int mx, double2* __re
 
 // Radix list of the DST-I of n points (no allocation), in the same form
 // as make_fft_plan (real-symmetric for even N).
-bool static_plan(int n, const double2* tw, const double* sn, FFTDev& d) {
+bool static_plan(int n, const float4* tw, const double* sn, FFTDev& d) {
   d.n = n;
   d.N = n + 1;
   d.rs = (d.N % 2 == 0) ? 1 : 0;
@@ -926,14 +969,10 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
     g_static_base[dev] = static_cast<double*>(p);
   }
   if (!g_static_consts[dev]) {
-    static double hc[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)], hs[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
-    for (int R = 1; R <= kMaxOddRadix; ++R)
-      for (int i = 0; i < R; ++i) {
-        hc[R * (kMaxOddRadix + 1) + i] = std::cos(2.0 * kPI * i / R);
-        hs[R * (kMaxOddRadix + 1) + i] = std::sin(2.0 * kPI * i / R);
-      }
-    if (cudaMemcpyToSymbol(c_rcos, hc, sizeof(hc)) != cudaSuccess ||
-        cudaMemcpyToSymbol(c_rsin, hs, sizeof(hs)) != cudaSuccess) {
+    static float2 hc[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)], hs[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
+    odd_radix_tables(hc, hs);
+    if (cudaMemcpyToSymbol(c_rcos_f, hc, sizeof(hc)) != cudaSuccess ||
+        cudaMemcpyToSymbol(c_rsin_f, hs, sizeof(hs)) != cudaSuccess) {
       cudaGetLastError();
       return VPMG_ERR_CUDA;
     }
@@ -942,8 +981,8 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
   double* base = g_static_base[dev];
   double* work = base;
   double* rinv = base + kStaticMaxInterior;
-  double2* twx = reinterpret_cast<double2*>(base + 2 * kStaticMaxInterior);
-  double2* twy = twx + kStaticTw;
+  float4* twx = reinterpret_cast<float4*>(base + 2 * kStaticMaxInterior);  // float-float twiddles, 16 B each
+  float4* twy = twx + kStaticTw;
   double* mux = reinterpret_cast<double*>(twy + kStaticTw);
   double* muy = mux + kStaticMaxLine;
   double* snx = muy + kStaticMaxLine;

@@ -83,7 +83,7 @@ struct FFTPlan {
   int pairs = 4;     // line pairs per CTA of the DST kernels (tuned per plan)
   int nst = 0;
   int radix[24];
-  DBuf<double2> tw;  // e^{-2 pi i t / M}, t = 0..M-1
+  DBuf<float4> tw;   // e^{-2 pi i t / M}, t = 0..M-1, float-float (re.hi, re.lo, im.hi, im.lo)
   DBuf<double> sn;   // sin(pi j / N), j = 0..N-1 (rs only)
 };
 void make_fft_plan(FFTPlan& p, int n);
@@ -137,7 +137,7 @@ struct BoundaryOp {
   DBuf<int> agg_istep;
   DBuf<int> anc;                        // [(lev-1)*nbound + leaf]: flat ancestor cell or -1
   DBuf<double> csrc;                    // 3 * ncell_total aggregated sources
-  DBuf<float2> csrc_ff;                 // the same as float-float pairs (recorded operator)
+  DBuf<float2> csrc_ff;                 // the same as float-float pairs, [cell][s0 s1 s2 0] (recorded operator)
   // panels: face geometry for the normal derivative
   DBuf<int> pan_face, pan_i, pan_j, pan_k;  // lower-corner node (0-based) of each panel
   // targets
