@@ -212,18 +212,12 @@ __device__ float4* fft_all(float4* A, float4* B, const FFTDev& p, int npair) {
   return A;
 }
 
-// In place, the npair * M complex values of a buffer: FP64 <-> float-float
+// In place, the npair * M complex values of a buffer: FP64 -> float-float
 // (same 16 bytes per value).
 __device__ __forceinline__ void to_ff(double2* z, int n) {
   for (int t = threadIdx.x; t < n; t += blockDim.x) {
     const double2 v = z[t];
     reinterpret_cast<float4*>(z)[t] = ff::from_double2(v);
-  }
-}
-__device__ __forceinline__ void from_ff(float4* z, int n) {
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    const float4 v = z[t];
-    reinterpret_cast<double2*>(z)[t] = ff::to_double2(v);
   }
 }
 
@@ -244,16 +238,17 @@ __device__ __forceinline__ void odd_extend(double2* z, const FFTDev& p, int npai
 
 // Real-symmetric DST-I, input side: the pair's lines sit in L at 1..n;
 // Z_0 = 0, Z_j = s_j (L_j + L_{N-j}) + (L_j - L_{N-j}) / 2, s_j = sin(pi j / N).
-__device__ __forceinline__ void rs_pre(const double2* __restrict__ L, double2* __restrict__ Z, const FFTDev& p,
+// The doubles are split into float-float here and Z is float-float.
+__device__ __forceinline__ void rs_pre(const double2* __restrict__ L, float4* __restrict__ Z, const FFTDev& p,
                                        int npair) {
   for (int t = threadIdx.x; t < npair * p.N; t += blockDim.x) {
     const int pr = t / p.N, j = t - pr * p.N;
-    double2 z = make_double2(0.0, 0.0);
+    float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (j > 0) {
-      const double2 a = L[pr * p.M + j], b = L[pr * p.M + p.N - j];
-      const double s = __ldg(&p.sn[j]);
-      z.x = fma(s, a.x + b.x, 0.5 * (a.x - b.x));
-      z.y = fma(s, a.y + b.y, 0.5 * (a.y - b.y));
+      const float4 a = ff::from_double2(L[pr * p.M + j]), b = ff::from_double2(L[pr * p.M + p.N - j]);
+      const float2 sj = ff::split(__ldg(&p.sn[j]));
+      z = ff::cplx(ff::fma(sj, ff::add(ff::re(a), ff::re(b)), ff::scale(ff::sub(ff::re(a), ff::re(b)), 0.5f)),
+                   ff::fma(sj, ff::add(ff::im(a), ff::im(b)), ff::scale(ff::sub(ff::im(a), ff::im(b)), 0.5f)));
     }
     Z[pr * p.M + j] = z;
   }
@@ -263,56 +258,59 @@ __device__ __forceinline__ void rs_pre(const double2* __restrict__ L, double2* _
 // Z_{N-m} = c + id the two lines' spectra are F = ((a+c) + i(b-d))/2 and
 // G = ((b+d) - i(a-c))/2, so X_{2m} = (d-b)/2 and (a-c)/2, and the odd
 // outputs are the prefix sums of r_0 = Z_0 / 2, r_m = ((a+c)/2, (b+d)/2).
-// O[pair * M + k] receives X_k of both lines, k = 1..n.  The prefix sum
-// runs over kScanSegs fixed segments of each line in a fixed order, so the
-// result does not depend on the tile shape; Z is its scratch afterwards.
+// O[pair * M + k] receives X_k of both lines, k = 1..n, in float-float.
+// The prefix sum runs over kScanSegs fixed segments of each line in a
+// fixed order, so the result does not depend on the tile shape; Z is its
+// scratch afterwards.
 constexpr int kScanSegs = 32;
-__device__ __forceinline__ void rs_post(double2* __restrict__ Z, double2* __restrict__ O, const FFTDev& p,
+__device__ __forceinline__ void rs_post(float4* __restrict__ Z, float4* __restrict__ O, const FFTDev& p,
                                         int npair) {
   const int H = p.N >> 1;
   for (int t = threadIdx.x; t < npair * H; t += blockDim.x) {
     const int pr = t / H, m = t - pr * H;
-    const double2 u = Z[pr * p.M + m];
+    const float4 u = Z[pr * p.M + m];
     if (m == 0) {
-      O[pr * p.M + 1] = make_double2(0.5 * u.x, 0.5 * u.y);
+      O[pr * p.M + 1] = ff::cplx(ff::scale(ff::re(u), 0.5f), ff::scale(ff::im(u), 0.5f));
     } else {
-      const double2 v = Z[pr * p.M + p.N - m];
-      O[pr * p.M + 2 * m] = make_double2(0.5 * (v.y - u.y), 0.5 * (u.x - v.x));
-      O[pr * p.M + 2 * m + 1] = make_double2(0.5 * (u.x + v.x), 0.5 * (u.y + v.y));
+      const float4 v = Z[pr * p.M + p.N - m];
+      O[pr * p.M + 2 * m] = ff::cplx(ff::scale(ff::sub(ff::im(v), ff::im(u)), 0.5f),
+                                     ff::scale(ff::sub(ff::re(u), ff::re(v)), 0.5f));
+      O[pr * p.M + 2 * m + 1] = ff::cplx(ff::scale(ff::add(ff::re(u), ff::re(v)), 0.5f),
+                                         ff::scale(ff::add(ff::im(u), ff::im(v)), 0.5f));
     }
   }
   __syncthreads();
   // segments per line: min(kScanSegs, H) -- a function of N only; the
-  // scratch (2 npair S doubles) fits in Z (2 npair M doubles, M >= 2H >= 2S)
+  // scratch (2 npair S float-float values) fits in Z (npair M complex, M >= 2H >= 2S)
   const int S = min(kScanSegs, H);
-  double* seg = reinterpret_cast<double*>(Z);  // [line][S]
+  float2* seg = reinterpret_cast<float2*>(Z);  // [line][S]
   const int C = (H + S - 1) / S;
   const int nls = 2 * npair * S;
   for (int t = threadIdx.x; t < nls; t += blockDim.x) {  // segment sums
     const int line = t / S, g = t - line * S;
-    const double* o = reinterpret_cast<const double*>(O + (line >> 1) * p.M) + (line & 1);  // X_k at o[2k]
+    const float2* o = reinterpret_cast<const float2*>(O + (line >> 1) * p.M) + (line & 1);  // X_k at o[2k]
     const int m0 = min(H, g * C), m1 = min(H, m0 + C);
-    double s = 0.0;
-    for (int m = m0; m < m1; ++m) s += o[2 * (2 * m + 1)];
-    seg[t] = s;
+    float2 sum = make_float2(0.0f, 0.0f);
+    for (int m = m0; m < m1; ++m) sum = ff::add(sum, o[2 * (2 * m + 1)]);
+    seg[t] = sum;
   }
   __syncthreads();
   for (int line = threadIdx.x; line < 2 * npair; line += blockDim.x) {  // exclusive scan of the segment sums
-    double run = 0.0;
+    float2 run = make_float2(0.0f, 0.0f);
     for (int g = 0; g < S; ++g) {
-      const double v = seg[line * S + g];
+      const float2 v = seg[line * S + g];
       seg[line * S + g] = run;
-      run += v;
+      run = ff::add(run, v);
     }
   }
   __syncthreads();
   for (int t = threadIdx.x; t < nls; t += blockDim.x) {  // inclusive values inside each segment
     const int line = t / S, g = t - line * S;
-    double* o = reinterpret_cast<double*>(O + (line >> 1) * p.M) + (line & 1);
+    float2* o = reinterpret_cast<float2*>(O + (line >> 1) * p.M) + (line & 1);
     const int m0 = min(H, g * C), m1 = min(H, m0 + C);
-    double run = seg[t];
+    float2 run = seg[t];
     for (int m = m0; m < m1; ++m) {
-      run += o[2 * (2 * m + 1)];
+      run = ff::add(run, o[2 * (2 * m + 1)]);
       o[2 * (2 * m + 1)] = run;
     }
   }
@@ -322,29 +320,33 @@ __device__ __forceinline__ void rs_post(double2* __restrict__ Z, double2* __rest
 // of the plan's mode, see staging()): returns the buffer holding X_k of
 // line (pair, c) at index pair * M + k (k = 1..n) as component c (rs), or
 // the raw odd-extension spectrum (X_k = -W.y / 2 and W.x / 2).
+// The values in shared memory are float-float from the pre-twiddle (or the
+// odd extension) to the output; dst_out joins them back into doubles.
 template <bool ODD, int PAIRS>
-__device__ __forceinline__ double2* dst_pairs(double2* A, double2* B, const FFTDev& p) {
+__device__ __forceinline__ float4* dst_pairs(double2* A, double2* B, const FFTDev& p) {
   constexpr int npair = PAIRS;
-  if (p.rs) rs_pre(B, A, p, npair);
-  else odd_extend(A, p, npair);
+  float4* Af = reinterpret_cast<float4*>(A);
+  float4* Bf = reinterpret_cast<float4*>(B);
+  if (p.rs) {
+    rs_pre(B, Af, p, npair);
+  } else {
+    odd_extend(A, p, npair);
+    __syncthreads();
+    to_ff(A, npair * p.M);
+  }
   __syncthreads();
-  to_ff(A, npair * p.M);
-  __syncthreads();
-  float4* Rf = fft_all<ODD>(reinterpret_cast<float4*>(A), reinterpret_cast<float4*>(B), p, npair);
-  from_ff(Rf, npair * p.M);
-  __syncthreads();
-  double2* R = reinterpret_cast<double2*>(Rf);
+  float4* R = fft_all<ODD>(Af, Bf, p, npair);
   if (!p.rs) return R;
-  double2* O = (R == A) ? B : A;
+  float4* O = (R == Af) ? Bf : Af;
   rs_post(R, O, p, npair);
   __syncthreads();
   return O;
 }
 __device__ __forceinline__ double2* staging(double2* A, double2* B, const FFTDev& p) { return p.rs ? B : A; }
-__device__ __forceinline__ double dst_out(const double2* O, const FFTDev& p, int li, int k) {
-  const double2 W = O[(li >> 1) * p.M + (k + 1)];
-  if (p.rs) return (li & 1) ? W.y : W.x;
-  return (li & 1) ? 0.5 * W.x : -0.5 * W.y;
+__device__ __forceinline__ double dst_out(const float4* O, const FFTDev& p, int li, int k) {
+  const float4 W = O[(li >> 1) * p.M + (k + 1)];
+  if (p.rs) return ff::to_double((li & 1) ? ff::im(W) : ff::re(W));
+  return ff::to_double((li & 1) ? ff::scale(ff::re(W), 0.5f) : ff::scale(ff::im(W), -0.5f));
 }
 
 // ------------------------------------------------------------ passes ----
@@ -388,7 +390,7 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict
     zp[li & 1] = v;
   }
   __syncthreads();
-  const double2* R = dst_pairs<ODD, PAIRS>(A, B, p);
+  const float4* R = dst_pairs<ODD, PAIRS>(A, B, p);
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
     const int l = l0 + li;
@@ -419,7 +421,7 @@ __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, i
     zp[li & 1] = v;
   }
   __syncthreads();
-  const double2* R = dst_pairs<ODD, PAIRS>(A, B, p);
+  const float4* R = dst_pairs<ODD, PAIRS>(A, B, p);
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t % (2 * PAIRS), k = t / (2 * PAIRS);
     const int l = l0 + li;
@@ -447,7 +449,7 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict
     zp[li & 1] = v;
   }
   __syncthreads();
-  const double2* R = dst_pairs<ODD, PAIRS>(A, B, p);
+  const float4* R = dst_pairs<ODD, PAIRS>(A, B, p);
   const size_t sy = b.dims[0], sz = (size_t)b.dims[0] * b.dims[1];
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
