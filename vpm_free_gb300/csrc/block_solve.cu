@@ -20,6 +20,7 @@
 #include <cmath>
 
 #include "block_solve.h"
+#include "ff.cuh"
 
 namespace vpmg {
 
@@ -27,24 +28,28 @@ namespace {
 
 constexpr int kLines = 16;  // lines per CTA of the x dot-product kernel
 
+// The dot products below run in float-float arithmetic (ff.cuh): the
+// sine rows are stored as float-float pairs, W is split by bit operations
+// as it is staged, and each result is joined back into a double.
+
 // out[i + nsel*(q + m1*kk)] = sum_p S[i][p] * W[p + m0*(q + m1*k)],  k = klist ? klist[kk] : kk
 __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W, int m0, int m1, int nk,
-                                                   const int* __restrict__ klist, const double* __restrict__ S,
+                                                   const int* __restrict__ klist, const float2* __restrict__ S,
                                                    int nsel, double* __restrict__ out) {
-  extern __shared__ double sm[];
-  double* tile = sm;                    // kLines x m0
-  double* Ss = sm + (size_t)kLines * m0;  // nsel x m0
+  extern __shared__ float2 smf[];
+  float2* tile = smf;                     // kLines x m0
+  float2* Ss = smf + (size_t)kLines * m0;  // nsel x m0
   const int nlines = m1 * nk;
   const int l0 = blockIdx.x * kLines;
   for (int t = threadIdx.x; t < nsel * m0; t += blockDim.x) Ss[t] = S[t];
   for (int t = threadIdx.x; t < kLines * m0; t += blockDim.x) {
     const int li = t / m0, p = t - li * m0;
     const int l = l0 + li;
-    double v = 0.0;
+    float2 v = make_float2(0.0f, 0.0f);
     if (l < nlines) {
       const int q = l % m1, kk = l / m1;
       const int k = klist ? klist[kk] : kk;
-      v = W[(size_t)p + (size_t)m0 * (q + (size_t)m1 * k)];
+      v = ff::split(W[(size_t)p + (size_t)m0 * (q + (size_t)m1 * k)]);
     }
     tile[t] = v;
   }
@@ -53,12 +58,17 @@ __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W,
     const int li = o % kLines, i = o / kLines;
     const int l = l0 + li;
     if (l >= nlines) continue;
-    const double* a = tile + (size_t)li * m0;
-    const double* b = Ss + (size_t)i * m0;
-    double acc = 0.0;
-    for (int p = 0; p < m0; ++p) acc = fma(a[p], b[p], acc);
+    const float2* a = tile + (size_t)li * m0;
+    const float2* b = Ss + (size_t)i * m0;
+    float2 a0 = make_float2(0.0f, 0.0f), a1 = a0;
+    int p = 0;
+    for (; p + 1 < m0; p += 2) {
+      a0 = ff::fma(a[p], b[p], a0);
+      a1 = ff::fma(a[p + 1], b[p + 1], a1);
+    }
+    if (p < m0) a0 = ff::fma(a[p], b[p], a0);
     const int q = l % m1, kk = l / m1;
-    out[i + (size_t)nsel * (q + (size_t)m1 * kk)] = acc;
+    out[i + (size_t)nsel * (q + (size_t)m1 * kk)] = ff::to_double(ff::add(a0, a1));
   }
 }
 
@@ -68,30 +78,31 @@ __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W,
 // its threads then form the nsel x 32 dot products from the tile.
 constexpr int kColTile = 32;
 __global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W, int m0, int m1, int nk,
-                                                   const int* __restrict__ klist, const double* __restrict__ S,
+                                                   const int* __restrict__ klist, const float2* __restrict__ S,
                                                    int nsel, double* __restrict__ out) {
-  extern __shared__ double tile[];  // [q][lane], m1 x kColTile
+  extern __shared__ float2 tile[];  // [q][lane], m1 x kColTile
   const int p0 = blockIdx.x * kColTile;
   const int kk = blockIdx.y;
   const int k = klist ? klist[kk] : kk;
   const double* plane = W + (size_t)m0 * m1 * k;
   const int lane = threadIdx.x % kColTile, row = threadIdx.x / kColTile, rows = blockDim.x / kColTile;
   const int p = p0 + lane;
-  for (int q = row; q < m1; q += rows) tile[q * kColTile + lane] = (p < m0) ? plane[(size_t)m0 * q + p] : 0.0;
+  for (int q = row; q < m1; q += rows)
+    tile[q * kColTile + lane] = (p < m0) ? ff::split(plane[(size_t)m0 * q + p]) : make_float2(0.0f, 0.0f);
   __syncthreads();
   if (p >= m0) return;
   for (int j = row; j < nsel; j += rows) {
-    const double* Sj = S + (size_t)j * m1;
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    const float2* Sj = S + (size_t)j * m1;
+    float2 a0 = make_float2(0.0f, 0.0f), a1 = a0, a2 = a0, a3 = a0;
     int q = 0;
     for (; q + 3 < m1; q += 4) {
-      a0 = fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
-      a1 = fma(__ldg(&Sj[q + 1]), tile[(q + 1) * kColTile + lane], a1);
-      a2 = fma(__ldg(&Sj[q + 2]), tile[(q + 2) * kColTile + lane], a2);
-      a3 = fma(__ldg(&Sj[q + 3]), tile[(q + 3) * kColTile + lane], a3);
+      a0 = ff::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
+      a1 = ff::fma(__ldg(&Sj[q + 1]), tile[(q + 1) * kColTile + lane], a1);
+      a2 = ff::fma(__ldg(&Sj[q + 2]), tile[(q + 2) * kColTile + lane], a2);
+      a3 = ff::fma(__ldg(&Sj[q + 3]), tile[(q + 3) * kColTile + lane], a3);
     }
-    for (; q < m1; ++q) a0 = fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
-    out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = (a0 + a1) + (a2 + a3);
+    for (; q < m1; ++q) a0 = ff::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
+    out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = ff::to_double(ff::add(ff::add(a0, a1), ff::add(a2, a3)));
   }
 }
 
@@ -140,83 +151,94 @@ struct FaceTerms {
 };
 
 // Thomas sweep of -u[k-1] + d u[k] - u[k+1] = r[k] with the reciprocal pivot
-// table; r = ghat (+ the transformed Dirichlet face terms when bc).
-__global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict__ out, const double* __restrict__ rinv,
+// table; r = ghat (+ the transformed Dirichlet face terms when bc).  In
+// float-float arithmetic (ff.cuh): the forward values go to `out` as
+// float-float pairs, the backward sweep overwrites them with doubles.
+__global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict__ out, const float2* __restrict__ rinv,
                                int m0, int m1, int m2, int bc, FaceTerms F) {
   const int pq = blockIdx.x * blockDim.x + threadIdx.x;
   if (pq >= m0 * m1) return;
   const int p = pq % m0, q = pq / m0;
   const size_t plane = (size_t)m0 * m1;
-  double ax = 0.0, bx = 0.0, ay = 0.0, by = 0.0;
+  float2* of = reinterpret_cast<float2*>(out);
+  float2 ax = make_float2(0.0f, 0.0f), bx = ax, ay = ax, by = ax, cz = ax;
   if (bc) {
-    ax = F.cx * F.ex1[p];
-    bx = F.cx * F.exN[p];
-    ay = F.cy * F.ey1[q];
-    by = F.cy * F.eyN[q];
+    ax = ff::split(F.cx * F.ex1[p]);
+    bx = ff::split(F.cx * F.exN[p]);
+    ay = ff::split(F.cy * F.ey1[q]);
+    by = ff::split(F.cy * F.eyN[q]);
+    cz = ff::split(F.cz);
   }
-  auto rhs = [&](int k) -> double {
-    double r = g[pq + plane * k];
+  auto rhs = [&](int k) -> float2 {
+    float2 r = ff::split(g[pq + plane * k]);
     if (bc) {
-      r += ax * F.fx0[(size_t)k * m1 + q] + bx * F.fxN[(size_t)k * m1 + q];
-      r += ay * F.fy0[(size_t)k * m0 + p] + by * F.fyN[(size_t)k * m0 + p];
-      if (k == 0) r += F.cz * F.fz0[pq];
-      if (k == m2 - 1) r += F.cz * F.fzN[pq];
+      r = ff::fma(ax, ff::split(F.fx0[(size_t)k * m1 + q]), r);
+      r = ff::fma(bx, ff::split(F.fxN[(size_t)k * m1 + q]), r);
+      r = ff::fma(ay, ff::split(F.fy0[(size_t)k * m0 + p]), r);
+      r = ff::fma(by, ff::split(F.fyN[(size_t)k * m0 + p]), r);
+      if (k == 0) r = ff::fma(cz, ff::split(F.fz0[pq]), r);
+      if (k == m2 - 1) r = ff::fma(cz, ff::split(F.fzN[pq]), r);
     }
     return r;
   };
-  // loads four planes ahead of the dependent chain; same arithmetic order
-  double y = rhs(0);
-  out[pq] = y;
-  double ri = rinv[pq];
+  // loads four planes ahead of the dependent chain
+  float2 y = rhs(0);
+  of[pq] = y;
+  float2 ri = rinv[pq];
   int k = 1;
   for (; k + 3 < m2; k += 4) {
     const size_t id = pq + plane * k;
-    const double q0 = rhs(k), q1 = rhs(k + 1), q2 = rhs(k + 2), q3 = rhs(k + 3);
-    const double r0 = rinv[id], r1 = rinv[id + plane], r2 = rinv[id + 2 * plane], r3 = rinv[id + 3 * plane];
-    y = fma(y, ri, q0);
-    out[id] = y;
-    y = fma(y, r0, q1);
-    out[id + plane] = y;
-    y = fma(y, r1, q2);
-    out[id + 2 * plane] = y;
-    y = fma(y, r2, q3);
-    out[id + 3 * plane] = y;
+    const float2 q0 = rhs(k), q1 = rhs(k + 1), q2 = rhs(k + 2), q3 = rhs(k + 3);
+    const float2 r0 = rinv[id], r1 = rinv[id + plane], r2 = rinv[id + 2 * plane], r3 = rinv[id + 3 * plane];
+    y = ff::fma(y, ri, q0);
+    of[id] = y;
+    y = ff::fma(y, r0, q1);
+    of[id + plane] = y;
+    y = ff::fma(y, r1, q2);
+    of[id + 2 * plane] = y;
+    y = ff::fma(y, r2, q3);
+    of[id + 3 * plane] = y;
     ri = r3;
   }
   for (; k < m2; ++k) {
     const size_t id = pq + plane * k;
-    y = fma(y, ri, rhs(k));
-    out[id] = y;
+    y = ff::fma(y, ri, rhs(k));
+    of[id] = y;
     ri = rinv[id];
   }
-  double u = y * ri;
-  out[pq + plane * (m2 - 1)] = u;
+  float2 u = ff::mul(y, ri);
+  out[pq + plane * (m2 - 1)] = ff::to_double(u);
   k = m2 - 2;
   for (; k - 3 >= 0; k -= 4) {
     const size_t id = pq + plane * k;
-    const double o0 = out[id], o1 = out[id - plane], o2 = out[id - 2 * plane], o3 = out[id - 3 * plane];
-    const double r0 = rinv[id], r1 = rinv[id - plane], r2 = rinv[id - 2 * plane], r3 = rinv[id - 3 * plane];
-    u = (o0 + u) * r0;
-    out[id] = u;
-    u = (o1 + u) * r1;
-    out[id - plane] = u;
-    u = (o2 + u) * r2;
-    out[id - 2 * plane] = u;
-    u = (o3 + u) * r3;
-    out[id - 3 * plane] = u;
+    const float2 o0 = of[id], o1 = of[id - plane], o2 = of[id - 2 * plane], o3 = of[id - 3 * plane];
+    const float2 r0 = rinv[id], r1 = rinv[id - plane], r2 = rinv[id - 2 * plane], r3 = rinv[id - 3 * plane];
+    u = ff::mul(ff::add(o0, u), r0);
+    out[id] = ff::to_double(u);
+    u = ff::mul(ff::add(o1, u), r1);
+    out[id - plane] = ff::to_double(u);
+    u = ff::mul(ff::add(o2, u), r2);
+    out[id - 2 * plane] = ff::to_double(u);
+    u = ff::mul(ff::add(o3, u), r3);
+    out[id - 3 * plane] = ff::to_double(u);
   }
   for (; k >= 0; --k) {
     const size_t id = pq + plane * k;
-    u = (out[id] + u) * rinv[id];
-    out[id] = u;
+    u = ff::mul(ff::add(of[id], u), rinv[id]);
+    out[id] = ff::to_double(u);
   }
 }
 
-std::vector<double> sine_rows(const std::vector<int>& sel, int m) {
-  std::vector<double> S(sel.size() * (size_t)m);
+// sin(pi (i+1)(p+1)/N) of the selected rows, as float-float pairs
+std::vector<float2> sine_rows(const std::vector<int>& sel, int m) {
+  std::vector<float2> S(sel.size() * (size_t)m);
   const double N = m + 1;
   for (size_t i = 0; i < sel.size(); ++i)
-    for (int p = 0; p < m; ++p) S[i * m + p] = std::sin(kPI * (double)(sel[i] + 1) * (double)(p + 1) / N);
+    for (int p = 0; p < m; ++p) {
+      const double v = std::sin(kPI * (double)(sel[i] + 1) * (double)(p + 1) / N);
+      const float hi = (float)v;
+      S[i * m + p] = make_float2(hi, (float)(v - (double)hi));
+    }
   return S;
 }
 
@@ -237,7 +259,7 @@ size_t g_partial_smem = 0;  // dynamic shared memory granted to k_partial_x so f
 // Raises k_partial_x's shared-memory limit (called at set-up, outside any
 // stream capture).
 void partial_x_reserve(int m0, int nsel) {
-  const size_t sm = sizeof(double) * ((size_t)kLines * m0 + (size_t)nsel * m0);
+  const size_t sm = sizeof(float2) * ((size_t)kLines * m0 + (size_t)nsel * m0);
   VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
   if (sm > g_partial_smem) {
     VPMG_CUDA(cudaFuncSetAttribute(k_partial_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -245,10 +267,10 @@ void partial_x_reserve(int m0, int nsel) {
   }
 }
 
-void partial_x(const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel, double* out,
+void partial_x(const double* W, int m0, int m1, int nk, const int* klist, const float2* S, int nsel, double* out,
                cudaStream_t s) {
   const int nlines = m1 * nk;
-  const size_t sm = sizeof(double) * ((size_t)kLines * m0 + (size_t)nsel * m0);
+  const size_t sm = sizeof(float2) * ((size_t)kLines * m0 + (size_t)nsel * m0);
   VPMG_CHECK(sm <= g_partial_smem, VPMG_ERR_STATE, "k_partial_x shared memory not reserved");
   k_partial_x<<<(nlines + kLines - 1) / kLines, 128, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out);
   VPMG_LAUNCHED();
@@ -257,7 +279,7 @@ void partial_x(const double* W, int m0, int m1, int nk, const int* klist, const 
 size_t g_partial_y_smem = 0;  // dynamic shared memory granted to k_partial_y so far
 
 void partial_y_reserve(int m1) {
-  const size_t sm = sizeof(double) * (size_t)m1 * kColTile;
+  const size_t sm = sizeof(float2) * (size_t)m1 * kColTile;
   VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
   if (sm > g_partial_y_smem) {
     VPMG_CUDA(cudaFuncSetAttribute(k_partial_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -265,9 +287,9 @@ void partial_y_reserve(int m1) {
   }
 }
 
-void partial_y(const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel, double* out,
+void partial_y(const double* W, int m0, int m1, int nk, const int* klist, const float2* S, int nsel, double* out,
                cudaStream_t s) {
-  const size_t sm = sizeof(double) * (size_t)m1 * kColTile;
+  const size_t sm = sizeof(float2) * (size_t)m1 * kColTile;
   VPMG_CHECK(sm <= g_partial_y_smem, VPMG_ERR_STATE, "k_partial_y shared memory not reserved");
   dim3 g((m0 + kColTile - 1) / kColTile, nk);
   k_partial_y<<<g, 256, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out);

@@ -460,61 +460,65 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict
   }
 }
 
-// z pass: Thomas sweep per (p,q) with the reciprocal pivot table.
-// The column's loads are issued four planes ahead of the dependent FMA
-// chain (the sweep is latency-bound otherwise); the arithmetic and its
-// order are those of the plain recurrence.
-__global__ void k_thomas(double* __restrict__ g, const double* __restrict__ rinv, int m0, int m1, int m2) {
+// z pass: Thomas sweep per (p,q) with the reciprocal pivot table, in
+// float-float arithmetic (ff.cuh): the forward sweep leaves its values in
+// place as float-float pairs, the backward sweep writes the doubles.  The
+// column's loads are issued four planes ahead of the dependent chain (the
+// sweep is latency-bound otherwise).
+__global__ void k_thomas(double* __restrict__ g, const float2* __restrict__ rinv, int m0, int m1, int m2) {
   const int pq = blockIdx.x * blockDim.x + threadIdx.x;
   if (pq >= m0 * m1) return;
   const size_t plane = (size_t)m0 * m1;
-  double y = g[pq];
-  double ri = rinv[pq];
+  float2* gf = reinterpret_cast<float2*>(g);
+  float2 y = ff::split(g[pq]);
+  gf[pq] = y;
+  float2 ri = rinv[pq];
   int c = 1;
   for (; c + 3 < m2; c += 4) {
     const size_t id = pq + plane * c;
     const double g0 = g[id], g1 = g[id + plane], g2 = g[id + 2 * plane], g3 = g[id + 3 * plane];
-    const double r0 = rinv[id], r1 = rinv[id + plane], r2 = rinv[id + 2 * plane], r3 = rinv[id + 3 * plane];
-    y = fma(y, ri, g0);
-    g[id] = y;
-    y = fma(y, r0, g1);
-    g[id + plane] = y;
-    y = fma(y, r1, g2);
-    g[id + 2 * plane] = y;
-    y = fma(y, r2, g3);
-    g[id + 3 * plane] = y;
+    const float2 r0 = rinv[id], r1 = rinv[id + plane], r2 = rinv[id + 2 * plane], r3 = rinv[id + 3 * plane];
+    y = ff::fma(y, ri, ff::split(g0));
+    gf[id] = y;
+    y = ff::fma(y, r0, ff::split(g1));
+    gf[id + plane] = y;
+    y = ff::fma(y, r1, ff::split(g2));
+    gf[id + 2 * plane] = y;
+    y = ff::fma(y, r2, ff::split(g3));
+    gf[id + 3 * plane] = y;
     ri = r3;
   }
   for (; c < m2; ++c) {
     const size_t id = pq + plane * c;
-    y = fma(y, ri, g[id]);
-    g[id] = y;
+    y = ff::fma(y, ri, ff::split(g[id]));
+    gf[id] = y;
     ri = rinv[id];
   }
-  double u = y * ri;
-  g[pq + plane * (m2 - 1)] = u;
+  float2 u = ff::mul(y, ri);
+  g[pq + plane * (m2 - 1)] = ff::to_double(u);
   c = m2 - 2;
   for (; c - 3 >= 0; c -= 4) {
     const size_t id = pq + plane * c;
-    const double g0 = g[id], g1 = g[id - plane], g2 = g[id - 2 * plane], g3 = g[id - 3 * plane];
-    const double r0 = rinv[id], r1 = rinv[id - plane], r2 = rinv[id - 2 * plane], r3 = rinv[id - 3 * plane];
-    u = (g0 + u) * r0;
-    g[id] = u;
-    u = (g1 + u) * r1;
-    g[id - plane] = u;
-    u = (g2 + u) * r2;
-    g[id - 2 * plane] = u;
-    u = (g3 + u) * r3;
-    g[id - 3 * plane] = u;
+    const float2 g0 = gf[id], g1 = gf[id - plane], g2 = gf[id - 2 * plane], g3 = gf[id - 3 * plane];
+    const float2 r0 = rinv[id], r1 = rinv[id - plane], r2 = rinv[id - 2 * plane], r3 = rinv[id - 3 * plane];
+    u = ff::mul(ff::add(g0, u), r0);
+    g[id] = ff::to_double(u);
+    u = ff::mul(ff::add(g1, u), r1);
+    g[id - plane] = ff::to_double(u);
+    u = ff::mul(ff::add(g2, u), r2);
+    g[id - 2 * plane] = ff::to_double(u);
+    u = ff::mul(ff::add(g3, u), r3);
+    g[id - 3 * plane] = ff::to_double(u);
   }
   for (; c >= 0; --c) {
     const size_t id = pq + plane * c;
-    u = (g[id] + u) * rinv[id];
-    g[id] = u;
+    u = ff::mul(ff::add(gf[id], u), rinv[id]);
+    g[id] = ff::to_double(u);
   }
 }
 
-__global__ void k_pivots(double* __restrict__ rinv, const double* __restrict__ mux, const double* __restrict__ muy,
+// Reciprocal pivots 1/d, 1/(d - r), ... in FP64, stored as float-float pairs.
+__global__ void k_pivots(float2* __restrict__ rinv, const double* __restrict__ mux, const double* __restrict__ muy,
                          int m0, int m1, int m2, double cx, double cy) {
   const int pq = blockIdx.x * blockDim.x + threadIdx.x;
   if (pq >= m0 * m1) return;
@@ -522,10 +526,10 @@ __global__ void k_pivots(double* __restrict__ rinv, const double* __restrict__ m
   const double d = 2.0 + (mux[p] * cx + muy[q] * cy);
   const size_t plane = (size_t)m0 * m1;
   double r = 1.0 / d;
-  rinv[pq] = r;
+  rinv[pq] = ff::split(r);
   for (int c = 1; c < m2; ++c) {
     r = 1.0 / (d - r);
-    rinv[pq + plane * c] = r;
+    rinv[pq + plane * c] = ff::split(r);
   }
 }
 
@@ -982,7 +986,7 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
   }
   double* base = g_static_base[dev];
   double* work = base;
-  double* rinv = base + kStaticMaxInterior;
+  float2* rinv = reinterpret_cast<float2*>(base + kStaticMaxInterior);  // 8 bytes per pivot
   float4* twx = reinterpret_cast<float4*>(base + 2 * kStaticMaxInterior);  // float-float twiddles, 16 B each
   float4* twy = twx + kStaticTw;
   double* mux = reinterpret_cast<double*>(twy + kStaticTw);

@@ -96,7 +96,7 @@ struct DirichletPlan {
   int m[3] = {0, 0, 0};
   double h[3] = {0, 0, 0};
   FFTPlan fx, fy;
-  DBuf<double> rinv;  // reciprocal Thomas pivots, [k][q][p]
+  DBuf<float2> rinv;  // reciprocal Thomas pivots, [k][q][p], float-float pairs
   bool ready = false;
 };
 void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], const double h[3], cudaStream_t s);
