@@ -151,81 +151,79 @@ struct FaceTerms {
 };
 
 // Thomas sweep of -u[k-1] + d u[k] - u[k+1] = r[k] with the reciprocal pivot
-// table; r = ghat (+ the transformed Dirichlet face terms when bc).  In
-// float-float arithmetic (ff.cuh): the forward values go to `out` as
-// float-float pairs, the backward sweep overwrites them with doubles.
-__global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict__ out, const float2* __restrict__ rinv,
+// table; r = ghat (+ the transformed Dirichlet face terms when bc).  The
+// recurrence stays in FP64: each line is a dependent chain and the lines
+// are too few to hide the longer chain of float-float operations.  The
+// pivots come from the float-float table, joined to doubles as they load.
+__global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict__ out, const float2* __restrict__ rinvf,
                                int m0, int m1, int m2, int bc, FaceTerms F) {
   const int pq = blockIdx.x * blockDim.x + threadIdx.x;
   if (pq >= m0 * m1) return;
   const int p = pq % m0, q = pq / m0;
   const size_t plane = (size_t)m0 * m1;
-  float2* of = reinterpret_cast<float2*>(out);
-  float2 ax = make_float2(0.0f, 0.0f), bx = ax, ay = ax, by = ax, cz = ax;
+  auto rinv = [&](size_t id) { return ff::to_double(rinvf[id]); };
+  double ax = 0.0, bx = 0.0, ay = 0.0, by = 0.0;
   if (bc) {
-    ax = ff::split(F.cx * F.ex1[p]);
-    bx = ff::split(F.cx * F.exN[p]);
-    ay = ff::split(F.cy * F.ey1[q]);
-    by = ff::split(F.cy * F.eyN[q]);
-    cz = ff::split(F.cz);
+    ax = F.cx * F.ex1[p];
+    bx = F.cx * F.exN[p];
+    ay = F.cy * F.ey1[q];
+    by = F.cy * F.eyN[q];
   }
-  auto rhs = [&](int k) -> float2 {
-    float2 r = ff::split(g[pq + plane * k]);
+  auto rhs = [&](int k) -> double {
+    double r = g[pq + plane * k];
     if (bc) {
-      r = ff::fma(ax, ff::split(F.fx0[(size_t)k * m1 + q]), r);
-      r = ff::fma(bx, ff::split(F.fxN[(size_t)k * m1 + q]), r);
-      r = ff::fma(ay, ff::split(F.fy0[(size_t)k * m0 + p]), r);
-      r = ff::fma(by, ff::split(F.fyN[(size_t)k * m0 + p]), r);
-      if (k == 0) r = ff::fma(cz, ff::split(F.fz0[pq]), r);
-      if (k == m2 - 1) r = ff::fma(cz, ff::split(F.fzN[pq]), r);
+      r += ax * F.fx0[(size_t)k * m1 + q] + bx * F.fxN[(size_t)k * m1 + q];
+      r += ay * F.fy0[(size_t)k * m0 + p] + by * F.fyN[(size_t)k * m0 + p];
+      if (k == 0) r += F.cz * F.fz0[pq];
+      if (k == m2 - 1) r += F.cz * F.fzN[pq];
     }
     return r;
   };
-  // loads four planes ahead of the dependent chain
-  float2 y = rhs(0);
-  of[pq] = y;
-  float2 ri = rinv[pq];
+  // loads four planes ahead of the dependent chain; same arithmetic order
+  double y = rhs(0);
+  out[pq] = y;
+  double ri = rinv(pq);
   int k = 1;
   for (; k + 3 < m2; k += 4) {
     const size_t id = pq + plane * k;
-    const float2 q0 = rhs(k), q1 = rhs(k + 1), q2 = rhs(k + 2), q3 = rhs(k + 3);
-    const float2 r0 = rinv[id], r1 = rinv[id + plane], r2 = rinv[id + 2 * plane], r3 = rinv[id + 3 * plane];
-    y = ff::fma(y, ri, q0);
-    of[id] = y;
-    y = ff::fma(y, r0, q1);
-    of[id + plane] = y;
-    y = ff::fma(y, r1, q2);
-    of[id + 2 * plane] = y;
-    y = ff::fma(y, r2, q3);
-    of[id + 3 * plane] = y;
+    const double q0 = rhs(k), q1 = rhs(k + 1), q2 = rhs(k + 2), q3 = rhs(k + 3);
+    const double r0 = rinv(id), r1 = rinv(id + plane), r2 = rinv(id + 2 * plane), r3 = rinv(id + 3 * plane);
+    y = fma(y, ri, q0);
+    out[id] = y;
+    y = fma(y, r0, q1);
+    out[id + plane] = y;
+    y = fma(y, r1, q2);
+    out[id + 2 * plane] = y;
+    y = fma(y, r2, q3);
+    out[id + 3 * plane] = y;
     ri = r3;
   }
   for (; k < m2; ++k) {
     const size_t id = pq + plane * k;
-    y = ff::fma(y, ri, rhs(k));
-    of[id] = y;
-    ri = rinv[id];
+    y = fma(y, ri, rhs(k));
+    out[id] = y;
+    ri = rinv(id);
   }
-  float2 u = ff::mul(y, ri);
-  out[pq + plane * (m2 - 1)] = ff::to_double(u);
+  double u = y * ri;
+  out[pq + plane * (m2 - 1)] = u;
   k = m2 - 2;
   for (; k - 3 >= 0; k -= 4) {
     const size_t id = pq + plane * k;
-    const float2 o0 = of[id], o1 = of[id - plane], o2 = of[id - 2 * plane], o3 = of[id - 3 * plane];
-    const float2 r0 = rinv[id], r1 = rinv[id - plane], r2 = rinv[id - 2 * plane], r3 = rinv[id - 3 * plane];
-    u = ff::mul(ff::add(o0, u), r0);
-    out[id] = ff::to_double(u);
-    u = ff::mul(ff::add(o1, u), r1);
-    out[id - plane] = ff::to_double(u);
-    u = ff::mul(ff::add(o2, u), r2);
-    out[id - 2 * plane] = ff::to_double(u);
-    u = ff::mul(ff::add(o3, u), r3);
-    out[id - 3 * plane] = ff::to_double(u);
+    const double o0 = out[id], o1 = out[id - plane], o2 = out[id - 2 * plane], o3 = out[id - 3 * plane];
+    const double r0 = rinv(id), r1 = rinv(id - plane), r2 = rinv(id - 2 * plane), r3 = rinv(id - 3 * plane);
+    u = (o0 + u) * r0;
+    out[id] = u;
+    u = (o1 + u) * r1;
+    out[id - plane] = u;
+    u = (o2 + u) * r2;
+    out[id - 2 * plane] = u;
+    u = (o3 + u) * r3;
+    out[id - 3 * plane] = u;
   }
   for (; k >= 0; --k) {
     const size_t id = pq + plane * k;
-    u = ff::mul(ff::add(of[id], u), rinv[id]);
-    out[id] = ff::to_double(u);
+    u = (out[id] + u) * rinv(id);
+    out[id] = u;
   }
 }
 
