@@ -176,6 +176,57 @@ __device__ __forceinline__ void stage(const float4* __restrict__ in, float4* __r
   }
 }
 
+// Odd-radix stage, streamed: the inputs are folded into v_m + v_{R-m} and
+// v_m - v_{R-m} as they load and every output pair goes straight to shared
+// memory, so only the 2H folded values stay live (the arithmetic is
+// DFT<R>'s, in the same order).
+template <int R>
+__device__ __forceinline__ void stage_odd(const float4* __restrict__ in, float4* __restrict__ out, int M, int Ns,
+                                          const float4* __restrict__ tw, int npair) {
+  constexpr int H = (R - 1) / 2;
+  const int nbf = M / R;
+  const int tws = M / (Ns * R);
+  for (int t = threadIdx.x; t < npair * nbf; t += blockDim.x) {
+    const int pr = t / nbf;
+    const int j = t - pr * nbf;
+    const float4* src = in + pr * M;
+    float4* dst = out + pr * M;
+    const int k = j % Ns;
+    const int base = (j - k) * R + k;
+    const float4 x0 = src[j];
+    float4 s[H], d[H];
+    float4 sum = x0;
+#pragma unroll
+    for (int m = 1; m <= H; ++m) {
+      float4 a = src[j + m * nbf], b = src[j + (R - m) * nbf];
+      if (Ns > 1) {
+        a = cmul(a, __ldg(&tw[k * m * tws]));
+        b = cmul(b, __ldg(&tw[k * (R - m) * tws]));
+      }
+      s[m - 1] = cadd(a, b);
+      d[m - 1] = csub(a, b);
+      sum = cadd(sum, s[m - 1]);
+    }
+    dst[base] = sum;
+#pragma unroll
+    for (int q = 1; q <= H; ++q) {
+      float2 ar = ff::re(x0), ai = ff::im(x0), br = make_float2(0.0f, 0.0f), bi = make_float2(0.0f, 0.0f);
+#pragma unroll
+      for (int m = 1; m <= H; ++m) {
+        const int idx = (m * q) % R;
+        const float2 c = c_rcos_f[R * (kMaxOddRadix + 1) + idx];
+        const float2 sn = c_rsin_f[R * (kMaxOddRadix + 1) + idx];
+        ar = ff::fma(c, ff::re(s[m - 1]), ar);
+        ai = ff::fma(c, ff::im(s[m - 1]), ai);
+        br = ff::fma(sn, ff::re(d[m - 1]), br);
+        bi = ff::fma(sn, ff::im(d[m - 1]), bi);
+      }
+      dst[base + q * Ns] = ff::cplx(ff::add(ar, bi), ff::sub(ai, br));
+      dst[base + (R - q) * Ns] = ff::cplx(ff::sub(ar, bi), ff::add(ai, br));
+    }
+  }
+}
+
 // Runs all stages; returns the buffer holding the result.  ODD = false
 // instantiates only the power-of-two radices, which keeps the register
 // count (and so the occupancy) of those kernels independent of the large
@@ -192,12 +243,12 @@ __device__ float4* fft_all(float4* A, float4* B, const FFTDev& p, int npair) {
       default:
         if constexpr (ODD) {
           switch (r) {
-            case 3: stage<3>(A, B, p.M, Ns, p.tw, npair); break;
-            case 5: stage<5>(A, B, p.M, Ns, p.tw, npair); break;
-            case 7: stage<7>(A, B, p.M, Ns, p.tw, npair); break;
-            case 11: stage<11>(A, B, p.M, Ns, p.tw, npair); break;
-            case 13: stage<13>(A, B, p.M, Ns, p.tw, npair); break;
-            case 17: stage<17>(A, B, p.M, Ns, p.tw, npair); break;
+            case 3: stage_odd<3>(A, B, p.M, Ns, p.tw, npair); break;
+            case 5: stage_odd<5>(A, B, p.M, Ns, p.tw, npair); break;
+            case 7: stage_odd<7>(A, B, p.M, Ns, p.tw, npair); break;
+            case 11: stage_odd<11>(A, B, p.M, Ns, p.tw, npair); break;
+            case 13: stage_odd<13>(A, B, p.M, Ns, p.tw, npair); break;
+            case 17: stage_odd<17>(A, B, p.M, Ns, p.tw, npair); break;
             default: break;
           }
         }
