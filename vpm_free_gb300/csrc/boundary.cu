@@ -28,7 +28,6 @@
 #include <algorithm>
 #include <cmath>
 
-#include "ff.cuh"
 #include "tree_host.h"
 #include "vpmg_internal.h"
 
@@ -112,14 +111,10 @@ __device__ double fsour_a4(const double XO[3], const double RG[3], const PanelFr
 
 enum { kAccum = 0, kCount = 1, kFill = 2, kTranspose = 3 };
 
-// kCount: counts[t] = interactions of target t, ntops[t] = those at the
-// coarsest level.  kFill: a row holds its coarsest-level interactions first
-// (in cell order), then the finer levels' (in walk order), so the product
-// gathers the first part coalesced.
 template <int MODE>
 __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ o1, double* __restrict__ o2,
                        int* __restrict__ counts, const long long* __restrict__ rowptr, int* __restrict__ col,
-                       float2* __restrict__ wgt, int* __restrict__ ntops) {
+                       float2* __restrict__ wgt) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= W.ntarget) return;
   const double X = W.tx[t], Y = W.ty[t], Z = W.tz[t];
@@ -127,12 +122,9 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
   int L = W.levmax;
   pos[L] = 0;
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-  int ni = 0, nt = 0;
-  long long out = 0, out_fine = 0;
-  if (MODE == kFill) {
-    out = rowptr[t];
-    out_fine = out + ntops[t];
-  }
+  int ni = 0;
+  long long out = 0;
+  if (MODE == kFill) out = rowptr[t];
   double bcv = 0.0;  // transpose: o1 is the adjoint of the boundary values, o0 the cell adjoints
   if (MODE == kTranspose) bcv = -W.inv_pi4 * o1[W.tgt_node[t]];
   while (true) {
@@ -163,7 +155,6 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
     }
     if (MODE == kCount) {
       ++ni;
-      if (L == W.levmax) ++nt;
       continue;
     }
     const double DS = W.cds[c];
@@ -187,10 +178,10 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
       w = (r > 1e-05) ? __ddiv_rn(DS, r) : -2.0 * __dsqrt_rn(DS) * W.lg;
     }
     if (MODE == kFill) {
-      const long long slot = (L == W.levmax) ? out++ : out_fine++;
-      col[slot] = cc;
+      col[out] = cc;
       const float hi = __double2float_rn(w);
-      wgt[slot] = make_float2(hi, __double2float_rn(w - (double)hi));
+      wgt[out] = make_float2(hi, __double2float_rn(w - (double)hi));
+      ++out;
     } else if (MODE == kTranspose) {
       if (bcv != 0.0) atomicAdd(&o0[cc], w * bcv);
     } else {
@@ -201,7 +192,6 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
   }
   if (MODE == kCount) {
     counts[t] = ni;
-    ntops[t] = nt;
   } else if (MODE == kAccum) {
     const int node = W.tgt_node[t];
     o0[node] += a0 * W.inv_pi4;
@@ -229,69 +219,38 @@ __device__ __forceinline__ void ff_mac(FF& a, float2 w, float2 s) {
   a.hi = t;
 }
 
-// Sources to float-float pairs, once per apply: packed per cell as
-// (s0, s1, s2, 0), one 32-byte sector per gather of all components (the
-// finer levels' scattered gathers), and per component for the coarsest
-// level's cells (ntop from top0), gathered in cell order.
-__global__ void k_split(const double* __restrict__ x, int ncell, int top0, int ntop, float2* __restrict__ out,
-                        float2* __restrict__ top) {
-  const size_t n = 4 * (size_t)ncell, nt = 3 * (size_t)ntop;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n + nt; i += (size_t)gridDim.x * blockDim.x) {
-    if (i < n) {
-      const int cell = (int)(i >> 2), comp = (int)(i & 3);
-      out[i] = (comp < 3) ? ff::split(x[(size_t)comp * ncell + cell]) : make_float2(0.0f, 0.0f);
-    } else {
-      const size_t u = i - n;
-      const int comp = (int)(u / ntop), c = (int)(u % ntop);
-      top[u] = ff::split(x[(size_t)comp * ncell + top0 + c]);
+// Sources to float-float pairs, once per apply, packed per cell as
+// (s0, s1, s2, 0): one 32-byte sector serves a gather of all components.
+__global__ void k_split(const double* __restrict__ x, int ncell, float2* __restrict__ out) {
+  const size_t n = 4 * (size_t)ncell;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cell = (int)(i >> 2), comp = (int)(i & 3);
+    float2 v = make_float2(0.0f, 0.0f);
+    if (comp < 3) {
+      const double d = x[(size_t)comp * ncell + cell];
+      const float hi = __double2float_rn(d);
+      v = make_float2(hi, __double2float_rn(d - (double)hi));
     }
+    out[i] = v;
   }
 }
 
 // One warp per boundary node: lanes stride over the node's interaction
 // list (coalesced), fixed-shape shuffle reduction (deterministic).
 __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__ rowptr, const int* __restrict__ col,
-                                                   const float2* __restrict__ wgt, const int* __restrict__ ntops,
-                                                   const float4* __restrict__ src, const float2* __restrict__ top,
-                                                   int top0, int ntop, const int* __restrict__ tgt_node, int ntarget,
-                                                   double inv_pi4,
+                                                   const float2* __restrict__ wgt, const float4* __restrict__ src,
+                                                   const int* __restrict__ tgt_node, int ntarget, double inv_pi4,
                                                    double* __restrict__ o0, double* __restrict__ o1,
                                                    double* __restrict__ o2) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
-  const long long b = rowptr[warp], mid = b + ntops[warp], e = rowptr[warp + 1];
+  const long long b = rowptr[warp], e = rowptr[warp + 1];
+  // Four interactions per lane per trip: their ids and weights are loaded
+  // before any gather so the loads overlap; two accumulator sets break the
+  // two-sum dependency chain.
   FF f0, f1, f2, g0, g1, g2;
-  // coarsest level: cells in increasing order, per-component gathers
-  {
-    const float2* t0 = top - top0;
-    const float2* t1 = top + ntop - top0;
-    const float2* t2 = top + 2 * (size_t)ntop - top0;
-    long long k = b + lane;
-    for (; k + 32 < mid; k += 64) {
-      const int ca = __ldg(&col[k]), cb = __ldg(&col[k + 32]);
-      const float2 wa = __ldg(&wgt[k]), wb = __ldg(&wgt[k + 32]);
-      const float2 xa0 = __ldg(&t0[ca]), xa1 = __ldg(&t1[ca]), xa2 = __ldg(&t2[ca]);
-      const float2 xb0 = __ldg(&t0[cb]), xb1 = __ldg(&t1[cb]), xb2 = __ldg(&t2[cb]);
-      ff_mac(f0, wa, xa0);
-      ff_mac(f1, wa, xa1);
-      ff_mac(f2, wa, xa2);
-      ff_mac(g0, wb, xb0);
-      ff_mac(g1, wb, xb1);
-      ff_mac(g2, wb, xb2);
-    }
-    for (; k < mid; k += 32) {
-      const int c = __ldg(&col[k]);
-      const float2 w = __ldg(&wgt[k]);
-      ff_mac(f0, w, __ldg(&t0[c]));
-      ff_mac(f1, w, __ldg(&t1[c]));
-      ff_mac(f2, w, __ldg(&t2[c]));
-    }
-  }
-  // finer levels: four interactions per lane per trip, ids and weights
-  // loaded before any gather so the loads overlap; two accumulator sets
-  // break the two-sum dependency chain
-  long long k = mid + lane;
+  long long k = b + lane;
   for (; k + 96 < e; k += 128) {
     int c[4];
     float2 w[4];
@@ -540,8 +499,7 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
   const int blocks = (B.ntarget + 127) / 128;
   DBuf<int> counts;
   counts.ensure(B.ntarget);
-  B.rowtop.ensure(B.ntarget);
-  k_walk<kCount><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, counts.p, nullptr, nullptr, nullptr, B.rowtop.p);
+  k_walk<kCount><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, counts.p, nullptr, nullptr, nullptr);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
   std::vector<int> hc(B.ntarget);
@@ -558,13 +516,11 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
       upload(B.rowptr, rp);
       B.col.ensure((size_t)B.nnz);
       B.w.ensure((size_t)B.nnz);
-      k_walk<kFill><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, nullptr, B.rowptr.p, B.col.p, B.w.p,
-                                           B.rowtop.p);
+      k_walk<kFill><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, nullptr, B.rowptr.p, B.col.p, B.w.p);
       VPMG_LAUNCHED();
       VPMG_CUDA(cudaGetLastError());
       VPMG_CUDA(cudaStreamSynchronize(s));
-      // here, not in the apply: steps may be captured in graphs
-      B.csrc_ff.ensure(4 * (size_t)B.ncell_total + 3 * (size_t)B.nbound_lev[B.levmax]);
+      B.csrc_ff.ensure(4 * (size_t)B.ncell_total);  // here, not in the apply: steps may be captured in graphs
       B.precomputed = true;
     } catch (const Error& e) {
       if (e.status != VPMG_ERR_NOMEM) throw;
@@ -598,22 +554,18 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
   }
   if (B.precomputed) {
     const size_t nc4 = 4 * (size_t)B.ncell_total;
-    const int top0 = B.lev_off[B.levmax], ntop = B.nbound_lev[B.levmax];
-    VPMG_CHECK(B.csrc_ff.n >= nc4 + 3 * (size_t)ntop, VPMG_ERR_STATE,
-               "boundary operator recorded without its source buffer");
-    float2* top = B.csrc_ff.p + nc4;
-    const size_t nsplit = nc4 + 3 * (size_t)ntop;
-    k_split<<<(unsigned)std::min<size_t>((nsplit + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, B.ncell_total, top0,
-                                                                                       ntop, B.csrc_ff.p, top);
+    VPMG_CHECK(B.csrc_ff.n >= nc4, VPMG_ERR_STATE, "boundary operator recorded without its source buffer");
+    k_split<<<(unsigned)std::min<size_t>((nc4 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, B.ncell_total,
+                                                                                    B.csrc_ff.p);
     VPMG_LAUNCHED();
     const long long threads = (long long)B.ntarget * 32;
-    k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
-        B.rowptr.p, B.col.p, B.w.p, B.rowtop.p, reinterpret_cast<const float4*>(B.csrc_ff.p), top, top0, ntop,
-        B.tgt_node.p, B.ntarget, 1.0 / (4.0 * kPI), sol[0], sol[1], sol[2]);
+    k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p,
+                                                                  reinterpret_cast<const float4*>(B.csrc_ff.p),
+                                                                  B.tgt_node.p, B.ntarget, 1.0 / (4.0 * kPI), sol[0],
+                                                                  sol[1], sol[2]);
   } else {
     const WalkDev W = walk_dev(B);
-    k_walk<kAccum><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, sol[0], sol[1], sol[2], nullptr, nullptr, nullptr, nullptr,
-                                                           nullptr);
+    k_walk<kAccum><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, sol[0], sol[1], sol[2], nullptr, nullptr, nullptr, nullptr);
   }
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
@@ -770,7 +722,7 @@ void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaS
   } else {
     const WalkDev W = walk_dev(B);
     k_walk<kTranspose><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, cellbar, const_cast<double*>(bcbar), nullptr,
-                                                               nullptr, nullptr, nullptr, nullptr, nullptr);
+                                                               nullptr, nullptr, nullptr, nullptr);
   }
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());

@@ -137,8 +137,7 @@ struct BoundaryOp {
   DBuf<int> agg_istep;
   DBuf<int> anc;                        // [(lev-1)*nbound + leaf]: flat ancestor cell or -1
   DBuf<double> csrc;                    // 3 * ncell_total aggregated sources
-  DBuf<float2> csrc_ff;                 // the same as float-float pairs: [cell][s0 s1 s2 0], then the
-                                        // coarsest level per component (recorded operator)
+  DBuf<float2> csrc_ff;                 // the same as float-float pairs, [cell][s0 s1 s2 0] (recorded operator)
   // panels: face geometry for the normal derivative
   DBuf<int> pan_face, pan_i, pan_j, pan_k;  // lower-corner node (0-based) of each panel
   // targets
@@ -151,7 +150,6 @@ struct BoundaryOp {
   DBuf<long long> rowptr;
   DBuf<int> col;
   DBuf<float2> w;                       // weights dS/r as float-float pairs (hi, lo), hi + lo = dS/r to 2^-48
-  DBuf<int> rowtop;                     // per target: interactions at the coarsest level (stored first)
   // its transpose (CSR over cells, for the reverse mode), built on first use
   bool transposed = false;
   DBuf<long long> colptr;
