@@ -328,7 +328,7 @@ def run_dirichlet(args, local):
     headline mesh; interior 271^3, so each line is a 272-point DST-I),
     about 1.3 GB on the device.  Prints ms per 3-component solve."""
     import vpm_free_gb300 as V
-    n = 273
+    n = args.dirichlet_nodes
     rng = np.random.default_rng(0)
     R = [rng.normal(size=(n, n, n)) for _ in range(3)]
     S = [np.zeros((n, n, n)) for _ in range(3)]
@@ -338,7 +338,7 @@ def run_dirichlet(args, local):
             t0 = time.perf_counter()
             h.pmesh(S, R, [0.0, 0.0, 0.0, 1.0, 1.0, 1.0], [1.0 / (n - 1)] * 3, 0)
             t.append(time.perf_counter() - t0)
-    print(json.dumps({"workload": "dirichlet273", "unit": "s per pmesh(iynbc=0) call, host clock incl. copies",
+    print(json.dumps({"workload": f"dirichlet{n}", "unit": "s per pmesh(iynbc=0) call, host clock incl. copies",
                       "s": t}))
     return 0
 
@@ -516,6 +516,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--batch-operator-budget", type=int, default=12 << 30,
                     help="bytes of recorded boundary operator per batched problem")
+    ap.add_argument("--dirichlet-nodes", type=int, default=273,
+                    help="nodes per axis of the dirichlet273 profiling workload (257: the inner box)")
     ap.add_argument("--blocks", default="1,1,1",
                     help="YAPS blocks NBI,NBJ,NBK on the one GPU (pm.inp line 7); the headline is 1,1,1")
     ap.add_argument("--operator-budget", type=int, default=-1,

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <vector>
 
+#include "ff.cuh"
 #include "handle.h"
 
 struct AdjointState {
@@ -155,15 +156,15 @@ __global__ void k_particle_adj(MeshDev m, const int* __restrict__ np_dev, const 
 }
 
 // Strength slots of the sorted records <- scale * w_p * v_p (w = QP(4) or 1).
-__global__ void k_records_set_q(double* __restrict__ rec, const int* __restrict__ perm, const int* __restrict__ nsorted,
+__global__ void k_records_set_q(float2* __restrict__ rec, const int* __restrict__ perm, const int* __restrict__ nsorted,
                                 const double* __restrict__ v, int cap, double scale, const double* __restrict__ w) {
   const int n = *nsorted;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     const int p = perm[s];
     const double f = scale * (w ? w[p] : 1.0);
-    rec[(size_t)s * kRecLen + 12] = f * v[p];
-    rec[(size_t)s * kRecLen + 13] = f * v[cap + p];
-    rec[(size_t)s * kRecLen + 14] = f * v[2 * (size_t)cap + p];
+    rec[(size_t)s * kRecLen + 12] = ff::split(f * v[p]);
+    rec[(size_t)s * kRecLen + 13] = ff::split(f * v[cap + p]);
+    rec[(size_t)s * kRecLen + 14] = ff::split(f * v[2 * (size_t)cap + p]);
   }
 }
 

@@ -9,6 +9,7 @@
 //    ordered stream compaction in (k,j,i) node order.
 #include <cmath>
 
+#include "ff.cuh"
 #include "particles.h"
 
 namespace vpmg {
@@ -100,12 +101,12 @@ __global__ void k_cell_order(const int* __restrict__ starts, int ncell, int* __r
 __global__ void k_records(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
                           const double* __restrict__ q0, const double* __restrict__ q1, const double* __restrict__ q2,
                           const int* __restrict__ perm, const int* __restrict__ nsorted_dev, MeshDev m,
-                          double* __restrict__ rec) {
+                          float2* __restrict__ rec) {
   const int nsorted = *nsorted_dev;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
   const int p = perm[s];
   const double pos[3] = {x[p], y[p], z[p]};
-  double* r = rec + (size_t)s * kRecLen;
+  float2* r = rec + (size_t)s * kRecLen;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int c0 = cell_of(pos[d], m.xmin[d], m.d[d]);
@@ -114,19 +115,20 @@ __global__ void k_records(const double* __restrict__ x, const double* __restrict
     for (int a = 0; a < 4; ++a) {
       const int node = c0 - m.ips + a;  // 0-based node = (i-1) of the reference
       const double t = (pos[d] - m.xmin[d] - (double)node * m.d[d]) * inv;
-      r[4 * d + a] = (a <= m.ips + m.ipf) ? proj_fun(m.itype, t) : 0.0;
+      r[4 * d + a] = ff::split((a <= m.ips + m.ipf) ? proj_fun(m.itype, t) : 0.0);
     }
     if (d == 0) r[15] = cell_bits(c0);
   }
-  r[12] = q0[p];
-  r[13] = q1[p];
-  r[14] = q2[p];
+  r[12] = ff::split(q0[p]);
+  r[13] = ff::split(q1[p]);
+  r[14] = ff::split(q2[p]);
   }
 }
 
 // One thread per node: gathers the particles of the (ips+ipf+1)^3 cells
-// whose stencil covers the node, in fixed cell and slot order.
-__global__ void k_deposit(const int* __restrict__ starts, const double* __restrict__ rec, MeshDev m, double inv_dv,
+// whose stencil covers the node, in fixed cell and slot order.  The weight
+// products and sums run in float-float on the FP32 pipes (ff.cuh).
+__global__ void k_deposit(const int* __restrict__ starts, const float2* __restrict__ rec, MeshDev m, double inv_dv,
                           double* __restrict__ r0, double* __restrict__ r1, double* __restrict__ r2) {
   const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
   const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -137,7 +139,7 @@ __global__ void k_deposit(const int* __restrict__ starts, const double* __restri
   const int w = m.ips + m.ipf;  // stencil width - 1
   // particle base cell c covers nodes c-ips .. c+ipf  =>  c in [node-ipf, node+ips]
   const int xlo = max(i - m.ipf, 0), xhi = min(i + m.ips, m.n[0] - 1);
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  float2 a0 = make_float2(0.0f, 0.0f), a1 = a0, a2 = a0;
   for (int ck = max(k - m.ipf, 0); ck <= min(k + m.ips, m.n[2] - 1); ++ck) {
     const int iz = k - ck + m.ips;
     for (int cj = max(j - m.ipf, 0); cj <= min(j + m.ips, m.n[1] - 1); ++cj) {
@@ -145,24 +147,24 @@ __global__ void k_deposit(const int* __restrict__ starts, const double* __restri
       const size_t row = (size_t)m.n[0] * (cj + (size_t)m.n[1] * ck);
       const int s = starts[row + xlo], e = starts[row + xhi + 1];
       for (int t = s; t < e; ++t) {
-        const double* r = rec + (size_t)t * kRecLen;
+        const float2* r = rec + (size_t)t * kRecLen;
         const int ix = i - record_cell(r) + m.ips;
         if ((unsigned)ix > (unsigned)w) continue;  // only for a binning that does not match rec
-        const double f = (r[ix] * r[4 + iy]) * r[8 + iz];
-        a0 = fma(f, r[12], a0);
-        a1 = fma(f, r[13], a1);
-        a2 = fma(f, r[14], a2);
+        const float2 f = ff::mul(ff::mul(r[ix], r[4 + iy]), r[8 + iz]);
+        a0 = ff::fma(f, r[12], a0);
+        a1 = ff::fma(f, r[13], a1);
+        a2 = ff::fma(f, r[14], a2);
       }
     }
   }
-  r0[id] = a0 * inv_dv;
-  r1[id] = a1 * inv_dv;
-  r2[id] = a2 * inv_dv;
+  r0[id] = ff::to_double(a0) * inv_dv;
+  r1[id] = ff::to_double(a1) * inv_dv;
+  r2[id] = ff::to_double(a2) * inv_dv;
 }
 
 // M2P over sorted slots: UP = sum W vel, GP = (sum W def) * vol; optionally
-// the forward Euler push.
-__global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsorted_dev, const double* __restrict__ rec,
+// the forward Euler push.  Weight products and sums in float-float.
+__global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsorted_dev, const float2* __restrict__ rec,
                       MeshDev m,
                       const double* __restrict__ v0, const double* __restrict__ v1, const double* __restrict__ v2,
                       const double* __restrict__ g0, const double* __restrict__ g1, const double* __restrict__ g2,
@@ -172,47 +174,49 @@ __global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsor
   const int nsorted = *nsorted_dev;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
   const int p = perm[s];
-  const double* r = rec + (size_t)s * kRecLen;
-  double w[12];
+  const float2* r = rec + (size_t)s * kRecLen;
+  float2 w[12];
 #pragma unroll
   for (int a = 0; a < 12; ++a) w[a] = r[a];
   const int c0 = record_cell(r);
   const int cj = cell_of(y[p], m.xmin[1], m.d[1]), ck = cell_of(z[p], m.xmin[2], m.d[2]);
   const int nw = m.ips + m.ipf + 1;
-  double u[3] = {0, 0, 0}, gl[3] = {0, 0, 0};
+  const float2 zero = make_float2(0.0f, 0.0f);
+  float2 u[3] = {zero, zero, zero}, gl[3] = {zero, zero, zero};
   for (int c = 0; c < nw; ++c) {
     const int kk = ck - m.ips + c;
     for (int b = 0; b < nw; ++b) {
       const int jj = cj - m.ips + b;
-      const double wyz = w[4 + b] * w[8 + c];
+      const float2 wyz = ff::mul(w[4 + b], w[8 + c]);
       const size_t row = (size_t)m.n[0] * (jj + (size_t)m.n[1] * kk) + (c0 - m.ips);
 #pragma unroll 4
       for (int a = 0; a < nw; ++a) {
-        const double f = w[a] * wyz;
+        const float2 f = ff::mul(w[a], wyz);
         const size_t id = row + a;
-        u[0] = fma(f, v0[id], u[0]);
-        u[1] = fma(f, v1[id], u[1]);
-        u[2] = fma(f, v2[id], u[2]);
-        gl[0] = fma(f, g0[id], gl[0]);
-        gl[1] = fma(f, g1[id], gl[1]);
-        gl[2] = fma(f, g2[id], gl[2]);
+        u[0] = ff::fma(f, ff::split(v0[id]), u[0]);
+        u[1] = ff::fma(f, ff::split(v1[id]), u[1]);
+        u[2] = ff::fma(f, ff::split(v2[id]), u[2]);
+        gl[0] = ff::fma(f, ff::split(g0[id]), gl[0]);
+        gl[1] = ff::fma(f, ff::split(g1[id]), gl[1]);
+        gl[2] = ff::fma(f, ff::split(g2[id]), gl[2]);
       }
     }
   }
   const double vp = vol[p];
-  const double gg0 = gl[0] * vp, gg1 = gl[1] * vp, gg2 = gl[2] * vp;
+  const double ud[3] = {ff::to_double(u[0]), ff::to_double(u[1]), ff::to_double(u[2])};
+  const double gg0 = ff::to_double(gl[0]) * vp, gg1 = ff::to_double(gl[1]) * vp, gg2 = ff::to_double(gl[2]) * vp;
   if (up) {
-    up[3 * (size_t)p] = u[0];
-    up[3 * (size_t)p + 1] = u[1];
-    up[3 * (size_t)p + 2] = u[2];
+    up[3 * (size_t)p] = ud[0];
+    up[3 * (size_t)p + 1] = ud[1];
+    up[3 * (size_t)p + 2] = ud[2];
     gp[3 * (size_t)p] = gg0;
     gp[3 * (size_t)p + 1] = gg1;
     gp[3 * (size_t)p + 2] = gg2;
   }
   if (do_euler) {
-    x[p] = x[p] + (u[0] + ux) * dt;
-    y[p] = y[p] + (u[1] + uy) * dt;
-    z[p] = z[p] + (u[2] + uz) * dt;
+    x[p] = x[p] + (ud[0] + ux) * dt;
+    y[p] = y[p] + (ud[1] + uy) * dt;
+    z[p] = z[p] + (ud[2] + uz) * dt;
     q0[p] = q0[p] - gg0 * dt;
     q1[p] = q1[p] - gg1 * dt;
     q2[p] = q2[p] - gg2 * dt;

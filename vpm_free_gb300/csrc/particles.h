@@ -6,7 +6,10 @@
 
 namespace vpmg {
 
-constexpr int kRecLen = 16;  // doubles per sorted particle record
+// A sorted particle record: 16 float-float slots (ff.cuh), 128 bytes --
+// the 4 stencil weights per axis (0..11), the strengths (12..14) and the
+// base cell's x index as the bits of slot 15's high float.
+constexpr int kRecLen = 16;
 
 // Mesh parameters as the kernels see them (0-based nodes).
 struct MeshDev {
@@ -16,24 +19,15 @@ struct MeshDev {
   int itype, ips, ipf;  // projection function and stencil extents
 };
 // Cell index of a sorted record (slot 15), stored as the integer's bits.
-__host__ __device__ inline double cell_bits(int c) {
-#ifdef __CUDA_ARCH__
-  return __longlong_as_double((long long)c);
-#else
-  long long v = c;
-  double d;
-  __builtin_memcpy(&d, &v, sizeof(d));
-  return d;
-#endif
-}
-__device__ __forceinline__ int record_cell(const double* r) { return (int)__double_as_longlong(r[15]); }
+__device__ __forceinline__ float2 cell_bits(int c) { return make_float2(__int_as_float(c), 0.0f); }
+__device__ __forceinline__ int record_cell(const float2* r) { return __float_as_int(r[15].x); }
 
 struct Particles {
   int capacity = 0;
   DBuf<double> x, y, z, q0, q1, q2, vol;  // SoA, QP(1:3) and QP(4)
   DBuf<double> up, gp;                    // (3, cap) AoS like UP/GP
   DBuf<int> key, perm;
-  DBuf<double> rec;                       // kRecLen per sorted slot
+  DBuf<float2> rec;                       // kRecLen float-float slots per sorted particle
   DBuf<int> d_np;                         // particle count, on the device
   void ensure(int cap);
 };
