@@ -153,15 +153,14 @@ struct FaceTerms {
 // Thomas sweep of -u[k-1] + d u[k] - u[k+1] = r[k] with the reciprocal pivot
 // table; r = ghat (+ the transformed Dirichlet face terms when bc).  The
 // recurrence stays in FP64: each line is a dependent chain and the lines
-// are too few to hide the longer chain of float-float operations.  The
-// pivots come from the float-float table, joined to doubles as they load.
-__global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict__ out, const float2* __restrict__ rinvf,
+// are too few to hide the longer chain of float-float operations.
+__global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict__ out, const double* __restrict__ rinvt,
                                int m0, int m1, int m2, int bc, FaceTerms F) {
   const int pq = blockIdx.x * blockDim.x + threadIdx.x;
   if (pq >= m0 * m1) return;
   const int p = pq % m0, q = pq / m0;
   const size_t plane = (size_t)m0 * m1;
-  auto rinv = [&](size_t id) { return ff::to_double(rinvf[id]); };
+  auto rinv = [&](size_t id) { return rinvt[id]; };
   double ax = 0.0, bx = 0.0, ay = 0.0, by = 0.0;
   if (bc) {
     ax = F.cx * F.ex1[p];
@@ -373,7 +372,7 @@ void block_solve_zero_bc(BlockSolve& B, DirichletPlan& P, const double* rhs_c, i
   double* g = B.ghat.p + (size_t)c * nint;
   dst_forward_xy(P, rhs_c, nullptr, true, g, s);
   FaceTerms F{};
-  k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(g, B.W.p, P.rinv.p, m0, m1, m2, 0, F);
+  k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(g, B.W.p, P.rinvd.p, m0, m1, m2, 0, F);
   VPMG_LAUNCHED();
   // x faces: 8 layers by dot products along x, then inverse y
   partial_x(B.W.p, m0, m1, m2, nullptr, B.S_fx.p, 8, B.X8.p, s);
@@ -421,7 +420,7 @@ void block_solve_bc(BlockSolve& B, DirichletPlan& P, int c, double* sol_c, cudaS
   F.cy = -scale / (P.h[1] * P.h[1]);
   F.cz = -scale / (P.h[2] * P.h[2]);
   const double* g = B.ghat.p + (size_t)c * nint;
-  k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(g, B.W.p, P.rinv.p, m0, m1, m2, 1, F);
+  k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(g, B.W.p, P.rinvd.p, m0, m1, m2, 1, F);
   VPMG_LAUNCHED();
   // inner-box x faces
   partial_x(B.W.p, m0, m1, m2, nullptr, B.S_ix.p, 2, B.X2.p, s);

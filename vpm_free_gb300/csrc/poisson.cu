@@ -568,9 +568,10 @@ __global__ void k_thomas(double* __restrict__ g, const float2* __restrict__ rinv
   }
 }
 
-// Reciprocal pivots 1/d, 1/(d - r), ... in FP64, stored as float-float pairs.
-__global__ void k_pivots(float2* __restrict__ rinv, const double* __restrict__ mux, const double* __restrict__ muy,
-                         int m0, int m1, int m2, double cx, double cy) {
+// Reciprocal pivots 1/d, 1/(d - r), ... in FP64, stored as float-float
+// pairs (and as doubles when rinvd is given).
+__global__ void k_pivots(float2* __restrict__ rinv, double* __restrict__ rinvd, const double* __restrict__ mux,
+                         const double* __restrict__ muy, int m0, int m1, int m2, double cx, double cy) {
   const int pq = blockIdx.x * blockDim.x + threadIdx.x;
   if (pq >= m0 * m1) return;
   const int p = pq % m0, q = pq / m0;
@@ -578,9 +579,11 @@ __global__ void k_pivots(float2* __restrict__ rinv, const double* __restrict__ m
   const size_t plane = (size_t)m0 * m1;
   double r = 1.0 / d;
   rinv[pq] = ff::split(r);
+  if (rinvd) rinvd[pq] = r;
   for (int c = 1; c < m2; ++c) {
     r = 1.0 / (d - r);
     rinv[pq + plane * c] = ff::split(r);
+    if (rinvd) rinvd[pq + plane * c] = r;
   }
 }
 
@@ -848,9 +851,10 @@ void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], co
   VPMG_CUDA(cudaMemcpy(dmx.p, mux.data(), sizeof(double) * P.m[0], cudaMemcpyHostToDevice));
   VPMG_CUDA(cudaMemcpy(dmy.p, muy.data(), sizeof(double) * P.m[1], cudaMemcpyHostToDevice));
   P.rinv.ensure((size_t)P.m[0] * P.m[1] * P.m[2]);
+  P.rinvd.ensure((size_t)P.m[0] * P.m[1] * P.m[2]);
   const double hz2 = h[2] * h[2];
   const int nl = P.m[0] * P.m[1];
-  k_pivots<<<(nl + 255) / 256, 256, 0, s>>>(P.rinv.p, dmx.p, dmy.p, P.m[0], P.m[1], P.m[2], hz2 / (h[0] * h[0]),
+  k_pivots<<<(nl + 255) / 256, 256, 0, s>>>(P.rinv.p, P.rinvd.p, dmx.p, dmy.p, P.m[0], P.m[1], P.m[2], hz2 / (h[0] * h[0]),
                                             hz2 / (h[1] * h[1]));
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
@@ -1061,7 +1065,7 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
                                                    px.rs ? px.N : 0, sny, py.rs ? py.N : 0);
   const double hz2 = h[2] * h[2], hx2 = h[0] * h[0], hy2 = h[1] * h[1];
   const int nl = m[0] * m[1];
-  k_pivots<<<(nl + 255) / 256, 256, 0, s>>>(rinv, mux, muy, m[0], m[1], m[2], hz2 / hx2, hz2 / hy2);
+  k_pivots<<<(nl + 255) / 256, 256, 0, s>>>(rinv, nullptr, mux, muy, m[0], m[1], m[2], hz2 / hx2, hz2 / hy2);
   Box b;
   for (int d = 0; d < 3; ++d) { b.dims[d] = dims[d]; b.o[d] = box[d] + 1; b.m[d] = m[d]; }
   const double scale = -hz2 * 4.0 / ((double)(m[0] + 1) * (double)(m[1] + 1));

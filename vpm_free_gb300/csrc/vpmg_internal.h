@@ -97,6 +97,7 @@ struct DirichletPlan {
   double h[3] = {0, 0, 0};
   FFTPlan fx, fy;
   DBuf<float2> rinv;  // reciprocal Thomas pivots, [k][q][p], float-float pairs
+  DBuf<double> rinvd; // the same in FP64, for the FP64 recurrence of the block solves
   bool ready = false;
 };
 void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], const double h[3], cudaStream_t s);
