@@ -176,12 +176,16 @@ __device__ __forceinline__ void stage(const float4* __restrict__ in, float4* __r
   }
 }
 
-// Odd-radix stage, streamed: the inputs are folded into v_m + v_{R-m} and
-// v_m - v_{R-m} as they load and every output pair goes straight to shared
-// memory, so only the 2H folded values stay live (the arithmetic is
-// DFT<R>'s, in the same order).
+// Odd-radix stage in two phases, so that a transform's few butterflies
+// (16 per radix-17 stage of a 272-point line) do not leave most threads
+// idle: (A) one thread per butterfly folds its twiddled inputs into
+// s_m = v_m + v_{R-m} and d_m = v_m - v_{R-m}, in place in the stage's input
+// buffer (free after the stage), and writes X_0 = v_0 + sum s_m; (B) one
+// thread per output pair q = 1..H reads x0, s_m, d_m back from shared
+// memory and writes X_q and X_{R-q}.  The arithmetic and its order per
+// output are DFT<R>'s.
 template <int R>
-__device__ __forceinline__ void stage_odd(const float4* __restrict__ in, float4* __restrict__ out, int M, int Ns,
+__device__ __forceinline__ void stage_odd(float4* __restrict__ in, float4* __restrict__ out, int M, int Ns,
                                           const float4* __restrict__ tw, int npair) {
   constexpr int H = (R - 1) / 2;
   const int nbf = M / R;
@@ -189,13 +193,10 @@ __device__ __forceinline__ void stage_odd(const float4* __restrict__ in, float4*
   for (int t = threadIdx.x; t < npair * nbf; t += blockDim.x) {
     const int pr = t / nbf;
     const int j = t - pr * nbf;
-    const float4* src = in + pr * M;
-    float4* dst = out + pr * M;
+    float4* src = in + pr * M;
     const int k = j % Ns;
     const int base = (j - k) * R + k;
-    const float4 x0 = src[j];
-    float4 s[H], d[H];
-    float4 sum = x0;
+    float4 sum = src[j];
 #pragma unroll
     for (int m = 1; m <= H; ++m) {
       float4 a = src[j + m * nbf], b = src[j + (R - m) * nbf];
@@ -203,27 +204,38 @@ __device__ __forceinline__ void stage_odd(const float4* __restrict__ in, float4*
         a = cmul(a, __ldg(&tw[k * m * tws]));
         b = cmul(b, __ldg(&tw[k * (R - m) * tws]));
       }
-      s[m - 1] = cadd(a, b);
-      d[m - 1] = csub(a, b);
-      sum = cadd(sum, s[m - 1]);
+      const float4 sm = cadd(a, b);
+      src[j + m * nbf] = sm;
+      src[j + (R - m) * nbf] = csub(a, b);
+      sum = cadd(sum, sm);
     }
-    dst[base] = sum;
+    out[pr * M + base] = sum;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < npair * nbf * H; t += blockDim.x) {
+    const int q = t % H + 1;
+    const int bf = t / H;
+    const int pr = bf / nbf;
+    const int j = bf - pr * nbf;
+    const float4* src = in + pr * M;
+    const int k = j % Ns;
+    const int base = (j - k) * R + k;
+    const float4 x0 = src[j];
+    float2 ar = ff::re(x0), ai = ff::im(x0), br = make_float2(0.0f, 0.0f), bi = make_float2(0.0f, 0.0f);
 #pragma unroll
-    for (int q = 1; q <= H; ++q) {
-      float2 ar = ff::re(x0), ai = ff::im(x0), br = make_float2(0.0f, 0.0f), bi = make_float2(0.0f, 0.0f);
-#pragma unroll
-      for (int m = 1; m <= H; ++m) {
-        const int idx = (m * q) % R;
-        const float2 c = c_rcos_f[R * (kMaxOddRadix + 1) + idx];
-        const float2 sn = c_rsin_f[R * (kMaxOddRadix + 1) + idx];
-        ar = ff::fma(c, ff::re(s[m - 1]), ar);
-        ai = ff::fma(c, ff::im(s[m - 1]), ai);
-        br = ff::fma(sn, ff::re(d[m - 1]), br);
-        bi = ff::fma(sn, ff::im(d[m - 1]), bi);
-      }
-      dst[base + q * Ns] = ff::cplx(ff::add(ar, bi), ff::sub(ai, br));
-      dst[base + (R - q) * Ns] = ff::cplx(ff::sub(ar, bi), ff::add(ai, br));
+    for (int m = 1; m <= H; ++m) {
+      const float4 sm = src[j + m * nbf], dm = src[j + (R - m) * nbf];
+      const int idx = (m * q) % R;
+      const float2 c = c_rcos_f[R * (kMaxOddRadix + 1) + idx];
+      const float2 sn = c_rsin_f[R * (kMaxOddRadix + 1) + idx];
+      ar = ff::fma(c, ff::re(sm), ar);
+      ai = ff::fma(c, ff::im(sm), ai);
+      br = ff::fma(sn, ff::re(dm), br);
+      bi = ff::fma(sn, ff::im(dm), bi);
     }
+    float4* dst = out + pr * M;
+    dst[base + q * Ns] = ff::cplx(ff::add(ar, bi), ff::sub(ai, br));
+    dst[base + (R - q) * Ns] = ff::cplx(ff::sub(ar, bi), ff::add(ai, br));
   }
 }
 
