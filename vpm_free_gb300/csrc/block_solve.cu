@@ -77,9 +77,12 @@ __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W,
 // shared memory with coalesced row loads -- W is read from HBM once -- and
 // its threads then form the nsel x 32 dot products from the tile.
 constexpr int kColTile = 32;
+// A second row set (S2, nsel2 -> out2, same layout) is served from the
+// same staged tile when given, so two face sets cost one pass over W.
 __global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W, int m0, int m1, int nk,
                                                    const int* __restrict__ klist, const float2* __restrict__ S,
-                                                   int nsel, double* __restrict__ out) {
+                                                   int nsel, double* __restrict__ out, const float2* __restrict__ S2,
+                                                   int nsel2, double* __restrict__ out2) {
   extern __shared__ float2 tile[];  // [q][lane], m1 x kColTile
   const int p0 = blockIdx.x * kColTile;
   const int kk = blockIdx.y;
@@ -91,8 +94,10 @@ __global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W,
     tile[q * kColTile + lane] = (p < m0) ? ff::split(plane[(size_t)m0 * q + p]) : make_float2(0.0f, 0.0f);
   __syncthreads();
   if (p >= m0) return;
-  for (int j = row; j < nsel; j += rows) {
-    const float2* Sj = S + (size_t)j * m1;
+  for (int jj = row; jj < nsel + nsel2; jj += rows) {
+    const bool second = jj >= nsel;
+    const int j = second ? jj - nsel : jj;
+    const float2* Sj = (second ? S2 : S) + (size_t)j * m1;
     float2 a0 = make_float2(0.0f, 0.0f), a1 = a0, a2 = a0, a3 = a0;
     int q = 0;
     for (; q + 3 < m1; q += 4) {
@@ -102,7 +107,9 @@ __global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W,
       a3 = ff::fma(__ldg(&Sj[q + 3]), tile[(q + 3) * kColTile + lane], a3);
     }
     for (; q < m1; ++q) a0 = ff::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
-    out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = ff::to_double(ff::add(ff::add(a0, a1), ff::add(a2, a3)));
+    const double v = ff::to_double(ff::add(ff::add(a0, a1), ff::add(a2, a3)));
+    if (second) out2[(size_t)p + (size_t)m0 * (j + (size_t)nsel2 * kk)] = v;
+    else out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = v;
   }
 }
 
@@ -285,11 +292,11 @@ void partial_y_reserve(int m1) {
 }
 
 void partial_y(const double* W, int m0, int m1, int nk, const int* klist, const float2* S, int nsel, double* out,
-               cudaStream_t s) {
+               cudaStream_t s, const float2* S2 = nullptr, int nsel2 = 0, double* out2 = nullptr) {
   const size_t sm = sizeof(float2) * (size_t)m1 * kColTile;
   VPMG_CHECK(sm <= g_partial_y_smem, VPMG_ERR_STATE, "k_partial_y shared memory not reserved");
   dim3 g((m0 + kColTile - 1) / kColTile, nk);
-  k_partial_y<<<g, 256, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out);
+  k_partial_y<<<g, 256, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out, S2, nsel2, out2);
   VPMG_LAUNCHED();
 }
 
@@ -355,9 +362,9 @@ void BlockSolve::prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoar
   partial_x_reserve(m[0], std::max(8, nsx));
   partial_y_reserve(m[1]);
   X8.ensure((size_t)8 * m[1] * m[2]);
-  Y4.ensure((size_t)m[0] * 4 * m[2]);
+  Y4.ensure((size_t)m[0] * 8 * m[2]);  // low and high face rows
   X2.ensure((size_t)2 * m[1] * m[2]);
-  Y1.ensure((size_t)m[0] * m[2]);
+  Y1.ensure((size_t)m[0] * 2 * m[2]);
   Ys.ensure((size_t)m[0] * nsy * nsz);
   XS.ensure((size_t)nsx * nsy * nsz);
   fx0.ensure((size_t)m[1] * m[2]); fxN.ensure((size_t)m[1] * m[2]);
@@ -380,12 +387,12 @@ void block_solve_zero_bc(BlockSolve& B, DirichletPlan& P, const double* rhs_c, i
   scatter3(B.X8.p, 8, m1, m2, B.l_fx.p, nullptr, nullptr, 1, sol0, B.dims, s);
   // y faces: 4 + 4 rows by dot products along y, then inverse x
   const int my[3] = {m0, 4, m2};
-  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_fy_lo.p, 4, B.Y4.p, s);
+  double* Y4b = B.Y4.p + (size_t)m0 * 4 * m2;
+  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_fy_lo.p, 4, B.Y4.p, s, B.S_fy_hi.p, 4, Y4b);
   const int olo[3] = {1, 1, 1};
   dst_x_inv_to_box(P.fx, B.Y4.p, sol0, B.dims, olo, my, s);
-  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_fy_hi.p, 4, B.Y4.p, s);
   const int ohi[3] = {1, 1 + m1 - 4, 1};
-  dst_x_inv_to_box(P.fx, B.Y4.p, sol0, B.dims, ohi, my, s);
+  dst_x_inv_to_box(P.fx, Y4b, sol0, B.dims, ohi, my, s);
   // z faces: the first and last 4 planes, full inverse (in place on W, after the dots)
   const int mz[3] = {m0, m1, 4};
   dst_lines_y(P.fy, B.W.p, m0, m1, 4, s);
@@ -428,12 +435,12 @@ void block_solve_bc(BlockSolve& B, DirichletPlan& P, int c, double* sol_c, cudaS
   scatter3(B.X2.p, 2, m1, m2, B.l_ix.p, nullptr, nullptr, 1, sol_c, B.dims, s);
   // inner-box y faces
   const int m1r[3] = {m0, 1, m2};
-  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_iy_lo.p, 1, B.Y1.p, s);
+  double* Y1b = B.Y1.p + (size_t)m0 * m2;
+  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_iy_lo.p, 1, B.Y1.p, s, B.S_iy_hi.p, 1, Y1b);
   const int oylo[3] = {1, B.inner_lo[1] + 1, 1};
   dst_x_inv_to_box(P.fx, B.Y1.p, sol_c, B.dims, oylo, m1r, s);
-  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_iy_hi.p, 1, B.Y1.p, s);
   const int oyhi[3] = {1, B.inner_hi[1] + 1, 1};
-  dst_x_inv_to_box(P.fx, B.Y1.p, sol_c, B.dims, oyhi, m1r, s);
+  dst_x_inv_to_box(P.fx, Y1b, sol_c, B.dims, oyhi, m1r, s);
   // interior samples: dots along y on the sampled planes, then along x
   partial_y(B.W.p, m0, m1, B.nsz, B.l_sz.p, B.S_sy.p, B.nsy, B.Ys.p, s);
   partial_x(B.Ys.p, m0, B.nsy, B.nsz, nullptr, B.S_sx.p, B.nsx, B.XS.p, s);
