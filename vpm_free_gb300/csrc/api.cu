@@ -814,9 +814,10 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
       BoundaryOp* bo = h->nblk > 1 ? h->bo_blk[0].get() : &h->bo_bl;
       const Grid* g = h->nblk > 1 ? &h->g_blk[0] : &h->gbl;
       f = [bo, g, o, st] { boundary_apply(*bo, *g, o, st); };
-      const double nnz = (double)bo->nnz;
+      const double nnz = (double)(bo->nnz + bo->ndense_acc);  // accepted interactions
       fl = 2.0 * 3.0 * nnz;  // three FMAs per interaction
-      by = bo->precomputed ? nnz * (sizeof(int) + sizeof(double)) : 0.0;
+      // streamed bytes: 12 per row entry (cell id + weight pair), 8 per slot of the dense block
+      by = bo->precomputed ? (double)bo->nnz * (sizeof(int) + sizeof(float2)) + (double)bo->wtop.bytes() : 0.0;
     } else if (which == 1) {
       h->bench_scratch.ensure(NB);
       double* o = h->bench_scratch.p;
@@ -1139,7 +1140,7 @@ int vpmg_phase_times(const vpmg_handle* h, double ms[9]) {
 int vpmg_tree_stats(const vpmg_handle* h, long long* interactions, long long* bytes, int* precomputed) {
   if (!h) return VPMG_ERR_ARG;
   const BoundaryOp& bo = h->nblk > 1 && !h->bo_blk.empty() ? *h->bo_blk[0] : h->bo_bl;
-  if (interactions) *interactions = bo.nnz;
+  if (interactions) *interactions = bo.nnz + bo.ndense_acc;
   if (bytes) *bytes = bo.bytes();
   if (precomputed) *precomputed = bo.precomputed ? 1 : 0;
   return VPMG_OK;

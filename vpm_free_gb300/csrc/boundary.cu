@@ -51,6 +51,7 @@ struct WalkDev {
   double inv_pi4, pi4;
   int bctype;     // 2 or 3
   int tree;       // 1: Bounds3d_lev walk; 0: untreed sum (levmax = 0)
+  int dense;      // 1: the coarsest level goes to the dense block (count / fill)
   const int* tgt_frame;
   PanelFrame frame[6];
 };
@@ -111,10 +112,14 @@ __device__ double fsour_a4(const double XO[3], const double RG[3], const PanelFr
 
 enum { kAccum = 0, kCount = 1, kFill = 2, kTranspose = 3 };
 
+// With W.dense, kCount counts only the finer levels (and adds the coarsest
+// level's accepted cells to *dcount) and kFill writes the coarsest level
+// into the dense block wtop.
 template <int MODE>
 __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ o1, double* __restrict__ o2,
                        int* __restrict__ counts, const long long* __restrict__ rowptr, int* __restrict__ col,
-                       float2* __restrict__ wgt) {
+                       float2* __restrict__ wgt, float2* __restrict__ wtop = nullptr,
+                       unsigned long long* __restrict__ dcount = nullptr) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= W.ntarget) return;
   const double X = W.tx[t], Y = W.ty[t], Z = W.tz[t];
@@ -122,7 +127,7 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
   int L = W.levmax;
   pos[L] = 0;
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-  int ni = 0;
+  int ni = 0, nd = 0;
   long long out = 0;
   if (MODE == kFill) out = rowptr[t];
   double bcv = 0.0;  // transpose: o1 is the adjoint of the boundary values, o0 the cell adjoints
@@ -154,7 +159,8 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
       continue;
     }
     if (MODE == kCount) {
-      ++ni;
+      if (W.dense && L == W.levmax) ++nd;
+      else ++ni;
       continue;
     }
     const double DS = W.cds[c];
@@ -178,10 +184,15 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
       w = (r > 1e-05) ? __ddiv_rn(DS, r) : -2.0 * __dsqrt_rn(DS) * W.lg;
     }
     if (MODE == kFill) {
-      col[out] = cc;
       const float hi = __double2float_rn(w);
-      wgt[out] = make_float2(hi, __double2float_rn(w - (double)hi));
-      ++out;
+      const float2 wf = make_float2(hi, __double2float_rn(w - (double)hi));
+      if (W.dense && L == W.levmax) {
+        wtop[((size_t)(t >> 5) * W.ntop + (c - W.top0)) * 32 + (t & 31)] = wf;
+      } else {
+        col[out] = cc;
+        wgt[out] = wf;
+        ++out;
+      }
     } else if (MODE == kTranspose) {
       if (bcv != 0.0) atomicAdd(&o0[cc], w * bcv);
     } else {
@@ -192,6 +203,7 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
   }
   if (MODE == kCount) {
     counts[t] = ni;
+    if (nd) atomicAdd(dcount, (unsigned long long)nd);
   } else if (MODE == kAccum) {
     const int node = W.tgt_node[t];
     o0[node] += a0 * W.inv_pi4;
@@ -235,13 +247,61 @@ __global__ void k_split(const double* __restrict__ x, int ncell, float2* __restr
   }
 }
 
+// The coarsest level's dense block: a warp per 32 targets walks the level's
+// cells in order, each lane streaming its target's weights (coalesced
+// across the warp) against the cell's sources (one broadcast record).
+__global__ void __launch_bounds__(256) k_apply_dense(const float2* __restrict__ wtop, const float4* __restrict__ src,
+                                                     int top0, int ntop, int ntarget, double* __restrict__ dsum) {
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (g >= (ntarget + 31) / 32) return;
+  const float2* wp = wtop + (size_t)g * ntop * 32 + lane;
+  const float4* sp = src + 2 * (size_t)top0;
+  FF f0, f1, f2, g0, g1, g2;
+  int c = 0;
+  for (; c + 3 < ntop; c += 4) {
+    float2 w[4];
+    float4 a[4], z[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) w[u] = __ldg(&wp[(size_t)(c + u) * 32]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a[u] = __ldg(&sp[2 * (size_t)(c + u)]);
+      z[u] = __ldg(&sp[2 * (size_t)(c + u) + 1]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u += 2) {
+      ff_mac(f0, w[u], make_float2(a[u].x, a[u].y));
+      ff_mac(f1, w[u], make_float2(a[u].z, a[u].w));
+      ff_mac(f2, w[u], make_float2(z[u].x, z[u].y));
+      ff_mac(g0, w[u + 1], make_float2(a[u + 1].x, a[u + 1].y));
+      ff_mac(g1, w[u + 1], make_float2(a[u + 1].z, a[u + 1].w));
+      ff_mac(g2, w[u + 1], make_float2(z[u + 1].x, z[u + 1].y));
+    }
+  }
+  for (; c < ntop; ++c) {
+    const float2 w = __ldg(&wp[(size_t)c * 32]);
+    const float4 a = __ldg(&sp[2 * (size_t)c]), z = __ldg(&sp[2 * (size_t)c + 1]);
+    ff_mac(f0, w, make_float2(a.x, a.y));
+    ff_mac(f1, w, make_float2(a.z, a.w));
+    ff_mac(f2, w, make_float2(z.x, z.y));
+  }
+  const int t = g * 32 + lane;
+  if (t < ntarget) {
+    dsum[t] = ((double)f0.hi + (double)f0.lo) + ((double)g0.hi + (double)g0.lo);
+    dsum[ntarget + t] = ((double)f1.hi + (double)f1.lo) + ((double)g1.hi + (double)g1.lo);
+    dsum[2 * (size_t)ntarget + t] = ((double)f2.hi + (double)f2.lo) + ((double)g2.hi + (double)g2.lo);
+  }
+}
+
 // One warp per boundary node: lanes stride over the node's interaction
-// list (coalesced), fixed-shape shuffle reduction (deterministic).
+// list (coalesced), fixed-shape shuffle reduction (deterministic); with
+// dsum, the dense block's partial sums join the warp's before the store.
 __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__ rowptr, const int* __restrict__ col,
                                                    const float2* __restrict__ wgt, const float4* __restrict__ src,
                                                    const int* __restrict__ tgt_node, int ntarget, double inv_pi4,
                                                    double* __restrict__ o0, double* __restrict__ o1,
-                                                   double* __restrict__ o2) {
+                                                   double* __restrict__ o2, const double* __restrict__ dsum) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
@@ -294,6 +354,11 @@ __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__
     a2 += __shfl_xor_sync(0xffffffffu, a2, o);
   }
   if (lane == 0) {
+    if (dsum) {
+      a0 += dsum[warp];
+      a1 += dsum[ntarget + warp];
+      a2 += dsum[2 * (size_t)ntarget + warp];
+    }
     const int node = tgt_node[warp];
     o0[node] += -a0 * inv_pi4;
     o1[node] += -a1 * inv_pi4;
@@ -376,6 +441,7 @@ WalkDev walk_dev(const BoundaryOp& B) {
   W.bctype = B.ibctyp;
   W.tree = B.tree ? 1 : 0;
   W.tgt_frame = B.tgt_frame.p;
+  W.dense = B.dense ? 1 : 0;
   for (int f = 0; f < 6; ++f) W.frame[f] = B.frame[f];
   return W;
 }
@@ -415,7 +481,7 @@ PanelFrame make_frame(int iplane, const double d[3]) {
 
 long long BoundaryOp::bytes() const {
   return (long long)(rowptr.bytes() + col.bytes() + w.bytes() + colptr.bytes() + trow.bytes() + tw.bytes() +
-                     cx.bytes() * 5 + child.bytes() + csrc.bytes());
+                     cx.bytes() * 5 + child.bytes() + csrc.bytes() + wtop.bytes() + dsum.bytes());
 }
 
 void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s, int ibctyp,
@@ -494,29 +560,51 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
   // ---- record the interaction lists if they fit --------------------------
   B.precomputed = false;
   B.nnz = 0;
-  B.rowptr.release(); B.col.release(); B.w.release();
+  B.rowptr.release(); B.col.release(); B.w.release(); B.wtop.release(); B.dsum.release();
+  B.ndense_acc = 0;
+  B.ntopd = B.nbound_lev[B.levmax];
+  const int nchunk = (B.ntarget + 31) / 32;
+  const long long dense_bytes =
+      (long long)nchunk * B.ntopd * 32 * (long long)sizeof(float2) + 3LL * B.ntarget * (long long)sizeof(double);
+  // the dense block needs a tree (levmax >= 1), the cells' own columns (not
+  // ibctyp 3's start-cell column) and at most half of the budget
+  B.dense = B.levmax >= 1 && !(B.ibctyp == 3 && B.tree) && budget_bytes > 0 && dense_bytes <= budget_bytes / 2;
   const WalkDev W = walk_dev(B);
   const int blocks = (B.ntarget + 127) / 128;
   DBuf<int> counts;
   counts.ensure(B.ntarget);
-  k_walk<kCount><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, counts.p, nullptr, nullptr, nullptr);
+  B.dcount.ensure(1);
+  VPMG_CUDA(cudaMemsetAsync(B.dcount.p, 0, sizeof(unsigned long long), s));
+  k_walk<kCount><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, counts.p, nullptr, nullptr, nullptr, nullptr,
+                                        B.dcount.p);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
   std::vector<int> hc(B.ntarget);
+  unsigned long long nd = 0;
   VPMG_CUDA(cudaMemcpyAsync(hc.data(), counts.p, sizeof(int) * B.ntarget, cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaMemcpyAsync(&nd, B.dcount.p, sizeof(nd), cudaMemcpyDeviceToHost, s));
   VPMG_CUDA(cudaStreamSynchronize(s));
+  B.ndense_acc = (long long)nd;
   std::vector<long long> rp(B.ntarget + 1, 0);
   for (int t = 0; t < B.ntarget; ++t) rp[t + 1] = rp[t] + hc[t];
   B.nnz = rp[B.ntarget];
-  const long long need = B.nnz * (long long)(sizeof(int) + sizeof(double)) + (long long)sizeof(long long) * (B.ntarget + 1);
+  const long long need = B.nnz * (long long)(sizeof(int) + sizeof(double)) +
+                         (long long)sizeof(long long) * (B.ntarget + 1) + (B.dense ? dense_bytes : 0);
   size_t free_b = 0, total_b = 0;
   VPMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
   if (budget_bytes > 0 && need <= budget_bytes && need < (long long)(0.8 * (double)free_b)) {
     try {
       upload(B.rowptr, rp);
-      B.col.ensure((size_t)B.nnz);
-      B.w.ensure((size_t)B.nnz);
-      k_walk<kFill><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, nullptr, B.rowptr.p, B.col.p, B.w.p);
+      B.col.ensure((size_t)std::max<long long>(B.nnz, 1));
+      B.w.ensure((size_t)std::max<long long>(B.nnz, 1));
+      if (B.dense) {
+        const size_t nw = (size_t)nchunk * B.ntopd * 32;
+        B.wtop.ensure(nw);
+        VPMG_CUDA(cudaMemsetAsync(B.wtop.p, 0, sizeof(float2) * nw, s));  // opened cells weigh 0
+        B.dsum.ensure(3 * (size_t)B.ntarget);
+      }
+      k_walk<kFill><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, nullptr, B.rowptr.p, B.col.p, B.w.p,
+                                           B.dense ? B.wtop.p : nullptr, nullptr);
       VPMG_LAUNCHED();
       VPMG_CUDA(cudaGetLastError());
       VPMG_CUDA(cudaStreamSynchronize(s));
@@ -524,10 +612,11 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
       B.precomputed = true;
     } catch (const Error& e) {
       if (e.status != VPMG_ERR_NOMEM) throw;
-      B.rowptr.release(); B.col.release(); B.w.release();
+      B.rowptr.release(); B.col.release(); B.w.release(); B.wtop.release(); B.dsum.release();
       B.precomputed = false;
     }
   }
+  if (!B.precomputed) B.dense = false;  // the walk covers every level
 }
 
 void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp, cudaStream_t s) {
@@ -558,11 +647,17 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
     k_split<<<(unsigned)std::min<size_t>((nc4 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, B.ncell_total,
                                                                                     B.csrc_ff.p);
     VPMG_LAUNCHED();
+    const float4* src4 = reinterpret_cast<const float4*>(B.csrc_ff.p);
+    if (B.dense) {
+      const long long dthreads = (long long)((B.ntarget + 31) / 32) * 32;
+      k_apply_dense<<<(unsigned)((dthreads + 255) / 256), 256, 0, s>>>(B.wtop.p, src4, B.lev_off[B.levmax], B.ntopd,
+                                                                      B.ntarget, B.dsum.p);
+      VPMG_LAUNCHED();
+    }
     const long long threads = (long long)B.ntarget * 32;
-    k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p,
-                                                                  reinterpret_cast<const float4*>(B.csrc_ff.p),
-                                                                  B.tgt_node.p, B.ntarget, 1.0 / (4.0 * kPI), sol[0],
-                                                                  sol[1], sol[2]);
+    k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, src4, B.tgt_node.p,
+                                                                  B.ntarget, 1.0 / (4.0 * kPI), sol[0], sol[1],
+                                                                  sol[2], B.dense ? B.dsum.p : nullptr);
   } else {
     const WalkDev W = walk_dev(B);
     k_walk<kAccum><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, sol[0], sol[1], sol[2], nullptr, nullptr, nullptr, nullptr);
@@ -629,6 +724,27 @@ __global__ void __launch_bounds__(256) k_csc_T(const long long* __restrict__ col
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
   if (lane == 0) cellbar[warp] = scale * a;
+}
+
+// Transpose of the dense block: cellbar[top0 + c] += scale * sum_t w(t, c) bcbar(node t),
+// a warp per cell reading the 32-target rows of each chunk (coalesced).
+__global__ void __launch_bounds__(256) k_dense_T(const float2* __restrict__ wtop, const int* __restrict__ tgt_node,
+                                                 int top0, int ntop, int ntarget, double scale,
+                                                 const double* __restrict__ bcbar, double* __restrict__ cellbar) {
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= ntop) return;
+  const int nchunk = (ntarget + 31) / 32;
+  double a = 0.0;
+  for (int g = 0; g < nchunk; ++g) {
+    const int t = g * 32 + lane;
+    if (t >= ntarget) continue;
+    const float2 w = __ldg(&wtop[((size_t)g * ntop + c) * 32 + lane]);
+    a = fma((double)w.x + (double)w.y, __ldg(&bcbar[__ldg(&tgt_node[t])]), a);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if (lane == 0) cellbar[top0 + c] += scale * a;
 }
 
 // leaf adjoint = its own level-0 adjoint + sum over ancestors of ds_leaf / ds_cell * cell adjoint
@@ -706,11 +822,19 @@ void boundary_transpose_prepare(BoundaryOp& B, cudaStream_t s) {
 
 void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s) {
   const double scale = -1.0 / (4.0 * kPI);
+  auto dense_T = [&] {
+    if (!B.dense) return;
+    const long long threads = (long long)B.ntopd * 32;
+    k_dense_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.wtop.p, B.tgt_node.p, B.lev_off[B.levmax], B.ntopd,
+                                                                B.ntarget, scale, bcbar, cellbar);
+    VPMG_LAUNCHED();
+  };
   if (B.transposed) {
     const long long threads = (long long)B.ncell_total * 32;
     k_csc_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.colptr.p, B.trow.p, B.tw.p, B.tgt_node.p,
                                                               B.ncell_total, scale, bcbar, cellbar);
     VPMG_LAUNCHED();
+    dense_T();
     VPMG_CUDA(cudaGetLastError());
     return;
   }
@@ -719,12 +843,14 @@ void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaS
     const long long threads = (long long)B.ntarget * 32;
     k_csr_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, B.tgt_node.p, B.ntarget,
                                                               scale, bcbar, cellbar);
+    VPMG_LAUNCHED();
+    dense_T();
   } else {
     const WalkDev W = walk_dev(B);
     k_walk<kTranspose><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, cellbar, const_cast<double*>(bcbar), nullptr,
                                                                nullptr, nullptr, nullptr, nullptr);
+    VPMG_LAUNCHED();
   }
-  VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
 

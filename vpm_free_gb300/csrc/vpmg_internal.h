@@ -151,6 +151,15 @@ struct BoundaryOp {
   DBuf<long long> rowptr;
   DBuf<int> col;
   DBuf<float2> w;                       // weights dS/r as float-float pairs (hi, lo), hi + lo = dS/r to 2^-48
+  // the coarsest level, which every target walks in full, as a dense block:
+  // [target / 32][cell][target % 32] float-float weights, zero where the
+  // cell was opened; the rows above then hold only the finer levels
+  bool dense = false;
+  int ntopd = 0;                        // cells of the coarsest level
+  long long ndense_acc = 0;             // accepted interactions in the block
+  DBuf<float2> wtop;
+  DBuf<double> dsum;                    // 3 x ntarget partial sums of the block
+  DBuf<unsigned long long> dcount;
   // its transpose (CSR over cells, for the reverse mode), built on first use
   bool transposed = false;
   DBuf<long long> colptr;
