@@ -187,7 +187,8 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
       const float hi = __double2float_rn(w);
       const float2 wf = make_float2(hi, __double2float_rn(w - (double)hi));
       if (W.dense && L == W.levmax) {
-        wtop[((size_t)(t >> 5) * W.ntop + (c - W.top0)) * 32 + (t & 31)] = wf;
+        const int cc2 = c - W.top0;  // [chunk][cell pair][lane][2]
+        wtop[(((size_t)(t >> 5) * ((W.ntop + 1) >> 1) + (cc2 >> 1)) * 32 + (t & 31)) * 2 + (cc2 & 1)] = wf;
       } else {
         col[out] = cc;
         wgt[out] = wf;
@@ -248,46 +249,62 @@ __global__ void k_split(const double* __restrict__ x, int ncell, float2* __restr
 }
 
 // The coarsest level's dense block: a warp per 32 targets walks the level's
-// cells in order, each lane streaming its target's weights (coalesced
-// across the warp) against the cell's sources (one broadcast record).
-__global__ void __launch_bounds__(256) k_apply_dense(const float2* __restrict__ wtop, const float4* __restrict__ src,
-                                                     int top0, int ntop, int ntarget, double* __restrict__ dsum) {
-  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// cells in order.  Each lane's weights for cells (2i, 2i+1) sit together
+// (one 16-byte load per lane, 512 coalesced bytes per warp load), and the
+// block stages the cells' packed sources in shared memory a tile at a
+// time, so the warps read them as broadcasts.
+constexpr int kDenseTile = 512;  // cells per staged tile (16 KB of sources)
+__global__ void __launch_bounds__(256) k_apply_dense(const float4* __restrict__ wtop, const float4* __restrict__ src,
+                                                     int top0, int ntop, int ntop2, int ntarget,
+                                                     double* __restrict__ dsum) {
+  __shared__ float4 ss[2 * kDenseTile];
   const int lane = threadIdx.x & 31;
-  if (g >= (ntarget + 31) / 32) return;
-  const float2* wp = wtop + (size_t)g * ntop * 32 + lane;
-  const float4* sp = src + 2 * (size_t)top0;
+  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const bool active = g < (ntarget + 31) / 32;
   FF f0, f1, f2, g0, g1, g2;
-  int c = 0;
-  for (; c + 3 < ntop; c += 4) {
-    float2 w[4];
-    float4 a[4], z[4];
+  for (int c0 = 0; c0 < ntop; c0 += kDenseTile) {
+    const int nc = min(kDenseTile, ntop - c0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < 2 * nc; i += blockDim.x) ss[i] = __ldg(&src[2 * (size_t)(top0 + c0) + i]);
+    __syncthreads();
+    if (!active) continue;
+    const float4* wp = wtop + ((size_t)g * ntop2 + (c0 >> 1)) * 32 + lane;
+    int c = 0;
+    for (; c + 7 < nc; c += 8) {
+      float4 w[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) w[u] = __ldg(&wp[(size_t)(c + u) * 32]);
+      for (int u = 0; u < 4; ++u) w[u] = __ldg(&wp[(size_t)((c >> 1) + u) * 32]);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      a[u] = __ldg(&sp[2 * (size_t)(c + u)]);
-      z[u] = __ldg(&sp[2 * (size_t)(c + u) + 1]);
+      for (int u = 0; u < 4; ++u) {
+        const float4 a = ss[2 * (c + 2 * u)], z = ss[2 * (c + 2 * u) + 1];
+        const float4 a2 = ss[2 * (c + 2 * u + 1)], z2 = ss[2 * (c + 2 * u + 1) + 1];
+        const float2 wa = make_float2(w[u].x, w[u].y), wb = make_float2(w[u].z, w[u].w);
+        ff_mac(f0, wa, make_float2(a.x, a.y));
+        ff_mac(f1, wa, make_float2(a.z, a.w));
+        ff_mac(f2, wa, make_float2(z.x, z.y));
+        ff_mac(g0, wb, make_float2(a2.x, a2.y));
+        ff_mac(g1, wb, make_float2(a2.z, a2.w));
+        ff_mac(g2, wb, make_float2(z2.x, z2.y));
+      }
     }
-#pragma unroll
-    for (int u = 0; u < 4; u += 2) {
-      ff_mac(f0, w[u], make_float2(a[u].x, a[u].y));
-      ff_mac(f1, w[u], make_float2(a[u].z, a[u].w));
-      ff_mac(f2, w[u], make_float2(z[u].x, z[u].y));
-      ff_mac(g0, w[u + 1], make_float2(a[u + 1].x, a[u + 1].y));
-      ff_mac(g1, w[u + 1], make_float2(a[u + 1].z, a[u + 1].w));
-      ff_mac(g2, w[u + 1], make_float2(z[u + 1].x, z[u + 1].y));
+    for (; c < nc; c += 2) {
+      const float4 w = __ldg(&wp[(size_t)(c >> 1) * 32]);
+      const float4 a = ss[2 * c], z = ss[2 * c + 1];
+      const float2 wa = make_float2(w.x, w.y);
+      ff_mac(f0, wa, make_float2(a.x, a.y));
+      ff_mac(f1, wa, make_float2(a.z, a.w));
+      ff_mac(f2, wa, make_float2(z.x, z.y));
+      if (c + 1 < nc) {
+        const float4 a2 = ss[2 * (c + 1)], z2 = ss[2 * (c + 1) + 1];
+        const float2 wb = make_float2(w.z, w.w);
+        ff_mac(g0, wb, make_float2(a2.x, a2.y));
+        ff_mac(g1, wb, make_float2(a2.z, a2.w));
+        ff_mac(g2, wb, make_float2(z2.x, z2.y));
+      }
     }
-  }
-  for (; c < ntop; ++c) {
-    const float2 w = __ldg(&wp[(size_t)c * 32]);
-    const float4 a = __ldg(&sp[2 * (size_t)c]), z = __ldg(&sp[2 * (size_t)c + 1]);
-    ff_mac(f0, w, make_float2(a.x, a.y));
-    ff_mac(f1, w, make_float2(a.z, a.w));
-    ff_mac(f2, w, make_float2(z.x, z.y));
   }
   const int t = g * 32 + lane;
-  if (t < ntarget) {
+  if (active && t < ntarget) {
     dsum[t] = ((double)f0.hi + (double)f0.lo) + ((double)g0.hi + (double)g0.lo);
     dsum[ntarget + t] = ((double)f1.hi + (double)f1.lo) + ((double)g1.hi + (double)g1.lo);
     dsum[2 * (size_t)ntarget + t] = ((double)f2.hi + (double)f2.lo) + ((double)g2.hi + (double)g2.lo);
@@ -564,8 +581,9 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
   B.ndense_acc = 0;
   B.ntopd = B.nbound_lev[B.levmax];
   const int nchunk = (B.ntarget + 31) / 32;
+  const long long ntop2 = (B.ntopd + 1) / 2;
   const long long dense_bytes =
-      (long long)nchunk * B.ntopd * 32 * (long long)sizeof(float2) + 3LL * B.ntarget * (long long)sizeof(double);
+      (long long)nchunk * ntop2 * 64 * (long long)sizeof(float2) + 3LL * B.ntarget * (long long)sizeof(double);
   // the dense block needs a tree (levmax >= 1), the cells' own columns (not
   // ibctyp 3's start-cell column) and at most half of the budget
   B.dense = B.levmax >= 1 && !(B.ibctyp == 3 && B.tree) && budget_bytes > 0 && dense_bytes <= budget_bytes / 2;
@@ -598,7 +616,7 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
       B.col.ensure((size_t)std::max<long long>(B.nnz, 1));
       B.w.ensure((size_t)std::max<long long>(B.nnz, 1));
       if (B.dense) {
-        const size_t nw = (size_t)nchunk * B.ntopd * 32;
+        const size_t nw = (size_t)nchunk * ntop2 * 64;
         B.wtop.ensure(nw);
         VPMG_CUDA(cudaMemsetAsync(B.wtop.p, 0, sizeof(float2) * nw, s));  // opened cells weigh 0
         B.dsum.ensure(3 * (size_t)B.ntarget);
@@ -650,8 +668,9 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
     const float4* src4 = reinterpret_cast<const float4*>(B.csrc_ff.p);
     if (B.dense) {
       const long long dthreads = (long long)((B.ntarget + 31) / 32) * 32;
-      k_apply_dense<<<(unsigned)((dthreads + 255) / 256), 256, 0, s>>>(B.wtop.p, src4, B.lev_off[B.levmax], B.ntopd,
-                                                                      B.ntarget, B.dsum.p);
+      k_apply_dense<<<(unsigned)((dthreads + 255) / 256), 256, 0, s>>>(
+          reinterpret_cast<const float4*>(B.wtop.p), src4, B.lev_off[B.levmax], B.ntopd, (B.ntopd + 1) / 2, B.ntarget,
+          B.dsum.p);
       VPMG_LAUNCHED();
     }
     const long long threads = (long long)B.ntarget * 32;
@@ -739,7 +758,7 @@ __global__ void __launch_bounds__(256) k_dense_T(const float2* __restrict__ wtop
   for (int g = 0; g < nchunk; ++g) {
     const int t = g * 32 + lane;
     if (t >= ntarget) continue;
-    const float2 w = __ldg(&wtop[((size_t)g * ntop + c) * 32 + lane]);
+    const float2 w = __ldg(&wtop[(((size_t)g * ((ntop + 1) >> 1) + (c >> 1)) * 32 + lane) * 2 + (c & 1)]);
     a = fma((double)w.x + (double)w.y, __ldg(&bcbar[__ldg(&tgt_node[t])]), a);
   }
 #pragma unroll
