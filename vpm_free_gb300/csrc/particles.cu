@@ -148,12 +148,15 @@ __global__ void k_deposit(const int* __restrict__ starts, const float2* __restri
       const int s = starts[row + xlo], e = starts[row + xhi + 1];
       for (int t = s; t < e; ++t) {
         const float2* r = rec + (size_t)t * kRecLen;
-        const int ix = i - record_cell(r) + m.ips;
+        // strengths and cell index as two 16-byte loads (slots 12-13, 14-15)
+        const float4 q2c = __ldg(reinterpret_cast<const float4*>(r) + 7);
+        const int ix = i - __float_as_int(q2c.z) + m.ips;
         if ((unsigned)ix > (unsigned)w) continue;  // only for a binning that does not match rec
-        const float2 f = ff::mul(ff::mul(r[ix], r[4 + iy]), r[8 + iz]);
-        a0 = ff::fma(f, r[12], a0);
-        a1 = ff::fma(f, r[13], a1);
-        a2 = ff::fma(f, r[14], a2);
+        const float4 q01 = __ldg(reinterpret_cast<const float4*>(r) + 6);
+        const float2 f = ff::mul(ff::mul(__ldg(&r[ix]), __ldg(&r[4 + iy])), __ldg(&r[8 + iz]));
+        a0 = ff::fma(f, make_float2(q01.x, q01.y), a0);
+        a1 = ff::fma(f, make_float2(q01.z, q01.w), a1);
+        a2 = ff::fma(f, make_float2(q2c.x, q2c.y), a2);
       }
     }
   }
