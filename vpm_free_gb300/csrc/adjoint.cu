@@ -162,9 +162,9 @@ __global__ void k_records_set_q(float2* __restrict__ rec, const int* __restrict_
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     const int p = perm[s];
     const double f = scale * (w ? w[p] : 1.0);
-    rec[(size_t)s * kRecLen + 12] = ff::split(f * v[p]);
-    rec[(size_t)s * kRecLen + 13] = ff::split(f * v[cap + p]);
-    rec[(size_t)s * kRecLen + 14] = ff::split(f * v[2 * (size_t)cap + p]);
+    rec[(size_t)s * kRecLen + kRecQ] = ff::split(f * v[p]);
+    rec[(size_t)s * kRecLen + kRecQ + 1] = ff::split(f * v[cap + p]);
+    rec[(size_t)s * kRecLen + kRecQ + 2] = ff::split(f * v[2 * (size_t)cap + p]);
   }
 }
 

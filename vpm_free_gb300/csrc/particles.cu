@@ -107,6 +107,7 @@ __global__ void k_records(const double* __restrict__ x, const double* __restrict
   const int p = perm[s];
   const double pos[3] = {x[p], y[p], z[p]};
   float2* r = rec + (size_t)s * kRecLen;
+  float2 wgt[3][4];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int c0 = cell_of(pos[d], m.xmin[d], m.d[d]);
@@ -115,13 +116,19 @@ __global__ void k_records(const double* __restrict__ x, const double* __restrict
     for (int a = 0; a < 4; ++a) {
       const int node = c0 - m.ips + a;  // 0-based node = (i-1) of the reference
       const double t = (pos[d] - m.xmin[d] - (double)node * m.d[d]) * inv;
-      r[4 * d + a] = ff::split((a <= m.ips + m.ipf) ? proj_fun(m.itype, t) : 0.0);
+      wgt[d][a] = ff::split((a <= m.ips + m.ipf) ? proj_fun(m.itype, t) : 0.0);
     }
-    if (d == 0) r[15] = cell_bits(c0);
+    if (d == 0) r[23] = cell_bits(c0);
   }
-  r[12] = ff::split(q0[p]);
-  r[13] = ff::split(q1[p]);
-  r[14] = ff::split(q2[p]);
+#pragma unroll
+  for (int a = 0; a < 4; ++a) r[a] = wgt[0][a];
+#pragma unroll
+  for (int b = 0; b < 4; ++b)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) r[4 + 4 * b + c] = ff::mul(wgt[1][b], wgt[2][c]);
+  r[kRecQ] = ff::split(q0[p]);
+  r[kRecQ + 1] = ff::split(q1[p]);
+  r[kRecQ + 2] = ff::split(q2[p]);
   }
 }
 
@@ -148,12 +155,12 @@ __global__ void k_deposit(const int* __restrict__ starts, const float2* __restri
       const int s = starts[row + xlo], e = starts[row + xhi + 1];
       for (int t = s; t < e; ++t) {
         const float2* r = rec + (size_t)t * kRecLen;
-        // strengths and cell index as two 16-byte loads (slots 12-13, 14-15)
-        const float4 q2c = __ldg(reinterpret_cast<const float4*>(r) + 7);
+        // strengths and cell index as two 16-byte loads (slots 20-21, 22-23)
+        const float4 q2c = __ldg(reinterpret_cast<const float4*>(r) + 11);
         const int ix = i - __float_as_int(q2c.z) + m.ips;
         if ((unsigned)ix > (unsigned)w) continue;  // only for a binning that does not match rec
-        const float4 q01 = __ldg(reinterpret_cast<const float4*>(r) + 6);
-        const float2 f = ff::mul(ff::mul(__ldg(&r[ix]), __ldg(&r[4 + iy])), __ldg(&r[8 + iz]));
+        const float4 q01 = __ldg(reinterpret_cast<const float4*>(r) + 10);
+        const float2 f = ff::mul(__ldg(&r[ix]), __ldg(&r[4 + 4 * iy + iz]));
         a0 = ff::fma(f, make_float2(q01.x, q01.y), a0);
         a1 = ff::fma(f, make_float2(q01.z, q01.w), a1);
         a2 = ff::fma(f, make_float2(q2c.x, q2c.y), a2);
@@ -178,9 +185,9 @@ __global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsor
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
   const int p = perm[s];
   const float2* r = rec + (size_t)s * kRecLen;
-  float2 w[12];
+  float2 w[4];
 #pragma unroll
-  for (int a = 0; a < 12; ++a) w[a] = r[a];
+  for (int a = 0; a < 4; ++a) w[a] = r[a];
   const int c0 = record_cell(r);
   const int cj = cell_of(y[p], m.xmin[1], m.d[1]), ck = cell_of(z[p], m.xmin[2], m.d[2]);
   const int nw = m.ips + m.ipf + 1;
@@ -190,7 +197,7 @@ __global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsor
     const int kk = ck - m.ips + c;
     for (int b = 0; b < nw; ++b) {
       const int jj = cj - m.ips + b;
-      const float2 wyz = ff::mul(w[4 + b], w[8 + c]);
+      const float2 wyz = r[4 + 4 * b + c];
       const size_t row = (size_t)m.n[0] * (jj + (size_t)m.n[1] * kk) + (c0 - m.ips);
 #pragma unroll 4
       for (int a = 0; a < nw; ++a) {

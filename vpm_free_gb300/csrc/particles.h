@@ -6,10 +6,13 @@
 
 namespace vpmg {
 
-// A sorted particle record: 16 float-float slots (ff.cuh), 128 bytes --
-// the 4 stencil weights per axis (0..11), the strengths (12..14) and the
-// base cell's x index as the bits of slot 15's high float.
-constexpr int kRecLen = 16;
+// A sorted particle record: 24 float-float slots (ff.cuh), 192 bytes --
+// the 4 x stencil weights (0..3), the 16 products of the y and z weights
+// wy[b] wz[c] at 4 + 4b + c, the strengths (20..22) and the base cell's x
+// index as the bits of slot 23's high float.  A particle-node visit of the
+// deposition reads one x weight, one y-z product and two 16-byte loads.
+constexpr int kRecLen = 24;
+constexpr int kRecQ = 20;  // first strength slot
 
 // Mesh parameters as the kernels see them (0-based nodes).
 struct MeshDev {
@@ -20,7 +23,7 @@ struct MeshDev {
 };
 // Cell index of a sorted record (slot 15), stored as the integer's bits.
 __device__ __forceinline__ float2 cell_bits(int c) { return make_float2(__int_as_float(c), 0.0f); }
-__device__ __forceinline__ int record_cell(const float2* r) { return __float_as_int(r[15].x); }
+__device__ __forceinline__ int record_cell(const float2* r) { return __float_as_int(r[23].x); }
 
 struct Particles {
   int capacity = 0;
