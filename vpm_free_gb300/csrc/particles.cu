@@ -16,31 +16,40 @@ namespace vpmg {
 
 namespace {
 
-// M4' and the other projection kernels of source/pmproject.f90:391-431.
-__device__ __forceinline__ double proj_fun(int itype, double x) {
-  const double xa = fabs(x);
+// M4' and the other projection kernels of source/pmproject.f90:391-431, in
+// float-float (ff.cuh), |x| given as a float-float value; the branch tests
+// compare the whole value (hi, then lo).
+__device__ __forceinline__ bool ff_gt(float2 a, float c) { return a.x > c || (a.x == c && a.y > 0.0f); }
+__device__ __forceinline__ bool ff_ge(float2 a, float c) { return a.x > c || (a.x == c && a.y >= 0.0f); }
+__device__ __forceinline__ float2 ffc(float c) { return make_float2(c, 0.0f); }
+__device__ __forceinline__ float2 proj_fun_ff(int itype, float2 xa) {
+  const float2 zero = ffc(0.0f), one = ffc(1.0f);
   if (itype == 4) {
-    if (xa > 2.0) return 0.0;
-    if (xa >= 1.0) return 0.5 * ((2.0 - xa) * (2.0 - xa)) * (1.0 - xa);
-    return 1.0 - 2.5 * (xa * xa) + 1.5 * (xa * xa * xa);
+    if (ff_gt(xa, 2.0f)) return zero;
+    if (ff_ge(xa, 1.0f)) {
+      const float2 a = ff::sub(ffc(2.0f), xa);
+      return ff::scale(ff::mul(ff::mul(a, a), ff::sub(one, xa)), 0.5f);
+    }
+    const float2 x2 = ff::mul(xa, xa);
+    return ff::fma(ffc(1.5f), ff::mul(x2, xa), ff::fma(ffc(-2.5f), x2, one));
   }
   if (itype == 3) {
-    if (xa > 1.5) return 0.0;
-    if (xa >= 0.5) return 0.5 * (-xa + 1.5) * (-xa + 1.5);
-    return 0.5 * (xa + 1.5) * (xa + 1.5) - 1.5 * (xa + 0.5) * (xa + 0.5);
+    if (ff_gt(xa, 1.5f)) return zero;
+    if (ff_ge(xa, 0.5f)) {
+      const float2 a = ff::sub(ffc(1.5f), xa);
+      return ff::scale(ff::mul(a, a), 0.5f);
+    }
+    const float2 a = ff::add(xa, ffc(1.5f)), b = ff::add(xa, ffc(0.5f));
+    return ff::sub(ff::scale(ff::mul(a, a), 0.5f), ff::mul(ffc(1.5f), ff::mul(b, b)));
   }
-  if (itype == 2) return xa > 1.0 ? 0.0 : 1.0 - xa;
-  if (itype == 5) {
-    if (xa <= 0.5) return 1.0 - xa * xa;
-    if (xa <= 1.5) return 0.5 * (1.0 - xa) * (2.0 - xa);
-    return 0.0;
+  if (itype == 2) return ff_gt(xa, 1.0f) ? zero : ff::sub(one, xa);
+  if (itype == 5 || itype == 6) {
+    const float lim = (itype == 5) ? 0.5f : 1.0f;
+    if (!ff_gt(xa, lim)) return ff::sub(one, ff::mul(xa, xa));
+    if (!ff_gt(xa, lim + 1.0f)) return ff::scale(ff::mul(ff::sub(one, xa), ff::sub(ffc(2.0f), xa)), 0.5f);
+    return zero;
   }
-  if (itype == 6) {
-    if (xa <= 1.0) return 1.0 - xa * xa;
-    if (xa <= 2.0) return 0.5 * (1.0 - xa) * (2.0 - xa);
-    return 0.0;
-  }
-  return 0.0;
+  return zero;
 }
 
 // Cell index exactly as int((x - XMIN)/DX) (IEEE division, truncation).
@@ -111,12 +120,15 @@ __global__ void k_records(const double* __restrict__ x, const double* __restrict
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int c0 = cell_of(pos[d], m.xmin[d], m.d[d]);
-    const double inv = m.inv[d];
+    // t of the first stencil node in FP64, the next ones t - a in float-float,
+    // the kernel in float-float (ff.cuh)
+    const int node0 = c0 - m.ips;  // 0-based node = (i-1) of the reference
+    const float2 t0 = ff::split((pos[d] - m.xmin[d] - (double)node0 * m.d[d]) * m.inv[d]);
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-      const int node = c0 - m.ips + a;  // 0-based node = (i-1) of the reference
-      const double t = (pos[d] - m.xmin[d] - (double)node * m.d[d]) * inv;
-      wgt[d][a] = ff::split((a <= m.ips + m.ipf) ? proj_fun(m.itype, t) : 0.0);
+      float2 t = ff::add(t0, make_float2(-(float)a, 0.0f));
+      if (t.x < 0.0f) t = ff::neg(t);
+      wgt[d][a] = (a <= m.ips + m.ipf) ? proj_fun_ff(m.itype, t) : make_float2(0.0f, 0.0f);
     }
     if (d == 0) r[23] = cell_bits(c0);
   }
