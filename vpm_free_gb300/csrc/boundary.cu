@@ -718,7 +718,7 @@ __global__ void k_col_count(const long long* __restrict__ rowptr, const int* __r
 }
 __global__ void k_col_fill(const long long* __restrict__ rowptr, const int* __restrict__ col,
                            const float2* __restrict__ wgt, int ntarget, const long long* __restrict__ colptr,
-                           int* __restrict__ cursor, int* __restrict__ trow, double* __restrict__ tw) {
+                           int* __restrict__ cursor, int* __restrict__ trow, float2* __restrict__ tw) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
@@ -726,20 +726,27 @@ __global__ void k_col_fill(const long long* __restrict__ rowptr, const int* __re
     const int c = col[k];
     const long long slot = colptr[c] + atomicAdd(&cursor[c], 1);
     trow[slot] = warp;
-    tw[slot] = (double)wgt[k].x + (double)wgt[k].y;
+    tw[slot] = wgt[k];
   }
 }
-// cellbar[c] = scale * sum over the cell's targets of w * bcbar(target node); warp per cell.
+// The boundary-value adjoint of each target, split once per call.
+__global__ void k_split_bc(const double* __restrict__ bcbar, const int* __restrict__ tgt_node, int ntarget,
+                           float2* __restrict__ v) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < ntarget) v[t] = ff::split(bcbar[tgt_node[t]]);
+}
+
+// cellbar[c] = scale * sum over the cell's targets of w * bcbar(target node);
+// warp per cell, products and sums in float-float.
 __global__ void __launch_bounds__(256) k_csc_T(const long long* __restrict__ colptr, const int* __restrict__ trow,
-                                               const double* __restrict__ tw, const int* __restrict__ tgt_node,
-                                               int ncell, double scale, const double* __restrict__ bcbar,
-                                               double* __restrict__ cellbar) {
+                                               const float2* __restrict__ tw, const float2* __restrict__ v,
+                                               int ncell, double scale, double* __restrict__ cellbar) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ncell) return;
-  double a = 0.0;
-  for (long long k = colptr[warp] + lane; k < colptr[warp + 1]; k += 32)
-    a = fma(__ldg(&tw[k]), __ldg(&bcbar[__ldg(&tgt_node[__ldg(&trow[k])])]), a);
+  FF f;
+  for (long long k = colptr[warp] + lane; k < colptr[warp + 1]; k += 32) ff_mac(f, __ldg(&tw[k]), __ldg(&v[__ldg(&trow[k])]));
+  double a = (double)f.hi + (double)f.lo;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
   if (lane == 0) cellbar[warp] = scale * a;
@@ -747,20 +754,21 @@ __global__ void __launch_bounds__(256) k_csc_T(const long long* __restrict__ col
 
 // Transpose of the dense block: cellbar[top0 + c] += scale * sum_t w(t, c) bcbar(node t),
 // a warp per cell reading the 32-target rows of each chunk (coalesced).
-__global__ void __launch_bounds__(256) k_dense_T(const float2* __restrict__ wtop, const int* __restrict__ tgt_node,
+__global__ void __launch_bounds__(256) k_dense_T(const float2* __restrict__ wtop, const float2* __restrict__ v,
                                                  int top0, int ntop, int ntarget, double scale,
-                                                 const double* __restrict__ bcbar, double* __restrict__ cellbar) {
+                                                 double* __restrict__ cellbar) {
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= ntop) return;
   const int nchunk = (ntarget + 31) / 32;
-  double a = 0.0;
+  FF f;
   for (int g = 0; g < nchunk; ++g) {
     const int t = g * 32 + lane;
     if (t >= ntarget) continue;
     const float2 w = __ldg(&wtop[(((size_t)g * ((ntop + 1) >> 1) + (c >> 1)) * 32 + lane) * 2 + (c & 1)]);
-    a = fma((double)w.x + (double)w.y, __ldg(&bcbar[__ldg(&tgt_node[t])]), a);
+    ff_mac(f, w, __ldg(&v[t]));
   }
+  double a = (double)f.hi + (double)f.lo;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
   if (lane == 0) cellbar[top0 + c] += scale * a;
@@ -804,8 +812,9 @@ __global__ void k_normal_deriv_T(const double* __restrict__ panelbar, int NX, in
 }  // namespace
 
 void boundary_transpose_prepare(BoundaryOp& B, cudaStream_t s) {
+  if (B.precomputed) B.vff.ensure((size_t)B.ntarget);  // at set-up: the transposes may be captured in graphs
   if (!B.precomputed || B.transposed || B.nnz == 0) return;
-  const long long need = B.nnz * (long long)(sizeof(int) + sizeof(double)) + 8LL * (B.ncell_total + 1);
+  const long long need = B.nnz * (long long)(sizeof(int) + sizeof(float2)) + 8LL * (B.ncell_total + 1);
   size_t free_b = 0, total_b = 0;
   VPMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
   if (need > (long long)(0.5 * (double)free_b)) return;  // keep the atomic scatter
@@ -841,17 +850,22 @@ void boundary_transpose_prepare(BoundaryOp& B, cudaStream_t s) {
 
 void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s) {
   const double scale = -1.0 / (4.0 * kPI);
+  if (B.transposed || B.dense) {
+    VPMG_CHECK(B.vff.n >= (size_t)B.ntarget, VPMG_ERR_STATE, "boundary transpose not prepared");
+    k_split_bc<<<(B.ntarget + 255) / 256, 256, 0, s>>>(bcbar, B.tgt_node.p, B.ntarget, B.vff.p);
+    VPMG_LAUNCHED();
+  }
   auto dense_T = [&] {
     if (!B.dense) return;
     const long long threads = (long long)B.ntopd * 32;
-    k_dense_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.wtop.p, B.tgt_node.p, B.lev_off[B.levmax], B.ntopd,
-                                                                B.ntarget, scale, bcbar, cellbar);
+    k_dense_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.wtop.p, B.vff.p, B.lev_off[B.levmax], B.ntopd,
+                                                                B.ntarget, scale, cellbar);
     VPMG_LAUNCHED();
   };
   if (B.transposed) {
     const long long threads = (long long)B.ncell_total * 32;
-    k_csc_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.colptr.p, B.trow.p, B.tw.p, B.tgt_node.p,
-                                                              B.ncell_total, scale, bcbar, cellbar);
+    k_csc_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.colptr.p, B.trow.p, B.tw.p, B.vff.p, B.ncell_total,
+                                                              scale, cellbar);
     VPMG_LAUNCHED();
     dense_T();
     VPMG_CUDA(cudaGetLastError());

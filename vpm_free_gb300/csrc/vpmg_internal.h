@@ -164,7 +164,8 @@ struct BoundaryOp {
   bool transposed = false;
   DBuf<long long> colptr;
   DBuf<int> trow;
-  DBuf<double> tw;
+  DBuf<float2> tw;                      // float-float weights of the transposed list
+  DBuf<float2> vff;                     // per target: the boundary-value adjoint, float-float
   long long bytes() const;
 };
 void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s,
