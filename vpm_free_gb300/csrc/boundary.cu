@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "ff.cuh"
 #include "tree_host.h"
 #include "vpmg_internal.h"
 
