@@ -753,17 +753,22 @@ __global__ void __launch_bounds__(256) k_csc_T(const long long* __restrict__ col
   if (lane == 0) cellbar[warp] = scale * a;
 }
 
-// Transpose of the dense block: cellbar[top0 + c] += scale * sum_t w(t, c) bcbar(node t),
-// a warp per cell reading the 32-target rows of each chunk (coalesced).
-__global__ void __launch_bounds__(256) k_dense_T(const float2* __restrict__ wtop, const float2* __restrict__ v,
-                                                 int top0, int ntop, int ntarget, double scale,
-                                                 double* __restrict__ cellbar) {
-  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Transpose of the dense block: cellbar[top0 + c] += scale * sum_t w(t, c) bcbar(node t).
+// A warp per (cell, group of kDenseTGroup target chunks) forms a partial sum
+// (float-float; each chunk's 32 weights are one coalesced row), then
+// k_dense_T_sum adds a cell's groups in order (deterministic).
+constexpr int kDenseTGroup = 64;
+__global__ void __launch_bounds__(256) k_dense_T(const float2* __restrict__ wtop, const float2* __restrict__ v, int ntop,
+                                                 int ntarget, double* __restrict__ part) {
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (c >= ntop) return;
   const int nchunk = (ntarget + 31) / 32;
+  const int ngroup = (nchunk + kDenseTGroup - 1) / kDenseTGroup;
+  if (wid >= (long long)ntop * ngroup) return;
+  const int c = (int)(wid % ntop), grp = (int)(wid / ntop);
+  const int g1 = min(nchunk, (grp + 1) * kDenseTGroup);
   FF f;
-  for (int g = 0; g < nchunk; ++g) {
+  for (int g = grp * kDenseTGroup; g < g1; ++g) {
     const int t = g * 32 + lane;
     if (t >= ntarget) continue;
     const float2 w = __ldg(&wtop[(((size_t)g * ((ntop + 1) >> 1) + (c >> 1)) * 32 + lane) * 2 + (c & 1)]);
@@ -772,7 +777,16 @@ __global__ void __launch_bounds__(256) k_dense_T(const float2* __restrict__ wtop
   double a = (double)f.hi + (double)f.lo;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-  if (lane == 0) cellbar[top0 + c] += scale * a;
+  if (lane == 0) part[(size_t)grp * ntop + c] = a;
+}
+
+__global__ void k_dense_T_sum(const double* __restrict__ part, int ntop, int ngroup, int top0, double scale,
+                              double* __restrict__ cellbar) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ntop) return;
+  double a = 0.0;
+  for (int grp = 0; grp < ngroup; ++grp) a += part[(size_t)grp * ntop + c];
+  cellbar[top0 + c] += scale * a;
 }
 
 // leaf adjoint = its own level-0 adjoint + sum over ancestors of ds_leaf / ds_cell * cell adjoint
@@ -813,7 +827,10 @@ __global__ void k_normal_deriv_T(const double* __restrict__ panelbar, int NX, in
 }  // namespace
 
 void boundary_transpose_prepare(BoundaryOp& B, cudaStream_t s) {
-  if (B.precomputed) B.vff.ensure((size_t)B.ntarget);  // at set-up: the transposes may be captured in graphs
+  if (B.precomputed) {  // at set-up: the transposes may be captured in graphs
+    B.vff.ensure((size_t)B.ntarget);
+    if (B.dense) B.dpart.ensure((size_t)B.ntopd * (((B.ntarget + 31) / 32 + kDenseTGroup - 1) / kDenseTGroup));
+  }
   if (!B.precomputed || B.transposed || B.nnz == 0) return;
   const long long need = B.nnz * (long long)(sizeof(int) + sizeof(float2)) + 8LL * (B.ncell_total + 1);
   size_t free_b = 0, total_b = 0;
@@ -858,9 +875,13 @@ void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaS
   }
   auto dense_T = [&] {
     if (!B.dense) return;
-    const long long threads = (long long)B.ntopd * 32;
-    k_dense_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.wtop.p, B.vff.p, B.lev_off[B.levmax], B.ntopd,
-                                                                B.ntarget, scale, cellbar);
+    const int ngroup = ((B.ntarget + 31) / 32 + kDenseTGroup - 1) / kDenseTGroup;
+    VPMG_CHECK(B.dpart.n >= (size_t)ngroup * B.ntopd, VPMG_ERR_STATE, "boundary transpose not prepared");
+    const long long threads = (long long)B.ntopd * ngroup * 32;
+    k_dense_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.wtop.p, B.vff.p, B.ntopd, B.ntarget, B.dpart.p);
+    VPMG_LAUNCHED();
+    k_dense_T_sum<<<(B.ntopd + 255) / 256, 256, 0, s>>>(B.dpart.p, B.ntopd, ngroup, B.lev_off[B.levmax], scale,
+                                                         cellbar);
     VPMG_LAUNCHED();
   };
   if (B.transposed) {

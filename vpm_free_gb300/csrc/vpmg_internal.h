@@ -166,6 +166,7 @@ struct BoundaryOp {
   DBuf<int> trow;
   DBuf<float2> tw;                      // float-float weights of the transposed list
   DBuf<float2> vff;                     // per target: the boundary-value adjoint, float-float
+  DBuf<double> dpart;                   // dense transpose: partial sums [chunk group][cell]
   long long bytes() const;
 };
 void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s,
