@@ -185,9 +185,11 @@ def cpu_step_sample(xp, qp, w, steps, threads):
 def run_batched(args, local):
     """Batched solves/s: 64 independent ring problems on meshes drawn from
     {32,48,64,96,128}^3 plus the 128^3 two-level (ncoarse = 2) case,
-    advanced together (one captured step graph per problem, replayed
-    concurrently on per-problem streams), against looping the plain path
-    (one problem after the other, vpmg_step with its host sync per step)."""
+    advanced together (problems of one mesh edge share one recorded
+    boundary operator and one apply per step; each group and each other
+    problem is one captured graph, replayed concurrently), against looping
+    the plain path (one problem after the other, vpmg_step with its host
+    sync per step)."""
     import vpm_free_gb300 as V
     from vpm_free_gb300 import workloads as W
     probs = W.batched_rings(64)
@@ -213,7 +215,16 @@ def run_batched(args, local):
     reset()
     V.VPM.batch_run(hs, 1, dt)                       # warm-up, captures the graphs
     reset()
-    ms_b, solves, ps_b = V.VPM.batch_run(hs, k, dt)
+    ms_c, solves_c, _ = V.VPM.batch_run(hs, k, dt)   # one graph per problem, concurrent
+    t0 = time.perf_counter()
+    batch = V.Batch(hs)                              # groups problems that share an operator
+    group_s = time.perf_counter() - t0
+    units, shared, corr_rows = batch.details()
+    reset()
+    batch.run(1, dt)                                 # warm-up, captures the group graphs
+    reset()
+    ms_b, solves, ps_b = batch.run(k, dt)
+    batch.close()
     reset()
     for h in hs:                                     # plain loop: problem after problem
         h.step(dt)
@@ -253,6 +264,13 @@ def run_batched(args, local):
             "loop_reference_calls_solves_per_s": len(hs) * k / ref_loop_s,
             "speedup_vs_plain_loop": (solves / (ms_b * 1e-3)) / (len(hs) * k / loop_s),
             "speedup_vs_reference_call_loop": (solves / (ms_b * 1e-3)) / (len(hs) * k / ref_loop_s),
+            "graphs_per_step": units, "problems_sharing_an_operator": shared, "grouping_s": group_s,
+            "corrected_rows": corr_rows,
+            "concurrent_graphs_solves_per_s": solves_c / (ms_c * 1e-3),
+            "batched": "vpmg_batch_step: problems with the same index geometry share one recorded boundary "
+                       "operator (one apply per group and step); each group and each other problem is one graph, "
+                       "replayed concurrently",
+            "concurrent_graphs": "vpmg_batch_run: one graph per problem, replayed concurrently",
             "loops": {"plain": "vpmg_step per problem and step (device-resident particles, host sync per step)",
                       "graph": "vpmg_run per problem (one captured step graph, problems one after another)",
                       "reference_calls": "vpm(WhatToDo=2) + host Euler + remesh_particles_3d per problem and step, "

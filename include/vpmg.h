@@ -201,6 +201,32 @@ int vpmg_run(vpmg_handle* h, int nsteps, double dt, const double uinf[3], int re
  * *particle_steps = sum over problems and steps of the particle count.   */
 int vpmg_batch_run(vpmg_handle* const* hs, int n, int nsteps, double dt, int remesh, double* ms,
                    long long* solves, long long* particle_steps);
+/* Batch object: the same n problems, grouped at creation by shared
+ * boundary operator.  Single-block problems (ibctyp 2) whose fine-block
+ * operators agree up to the mesh-spacing factor (same index geometry and
+ * tree; weights within 1e-12 of the leader's scaled ones; the cells that
+ * the two tree walks decided differently, at most 2 % of the
+ * interactions, kept as per-problem correction rows) form groups of up to
+ * 16; a group's step is one
+ * CUDA graph that applies the leader's recorded operator to all members'
+ * sources in one launch, so the operator streams from HBM once per group
+ * and step.  Other problems keep their own step graphs.  The handles must
+ * outlive the batch and take no other calls while it runs.
+ * Replaces: the loop over independent problems a host runs around vpm()
+ * (source/test.f90:83-150), one problem after another.                  */
+typedef struct vpmg_batch vpmg_batch;
+int vpmg_batch_create(vpmg_handle* const* hs, int n, vpmg_batch** out);
+/* *units = graphs replayed per step; *shared = problems in groups of >= 2;
+ * *correction_rows = boundary nodes whose recorded row differs from the
+ * group leader's scaled row (a cell exactly on the tree's opening radius in
+ * index units, decided by each problem's own rounding): their differences
+ * are added per problem after the group's apply.                          */
+int vpmg_batch_info(const vpmg_batch* b, int* units, int* shared, long long* correction_rows);
+/* nsteps device-resident steps of every problem (as vpmg_batch_run);
+ * errors are reported through the first handle (vpmg_last_error).       */
+int vpmg_batch_step(vpmg_batch* b, int nsteps, double dt, int remesh, double* ms, long long* solves,
+                    long long* particle_steps);
+int vpmg_batch_destroy(vpmg_batch* b);
 /* Replays one kernel of the last step `reps` times between CUDA events on
  * the handle's stream (instrumentation for roofline figures).
  *   which = 0: boundary operator apply on the fine block (k_apply_csr or

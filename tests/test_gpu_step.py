@@ -163,6 +163,72 @@ def test_batched_problems_equal_individual_runs(gpulib):
         h.close()
 
 
+def _batch_problems(V, names):
+    """Ring problems of the uneven batch (mesh edge 32..128 cells, the box
+    scaled with the ring radius), remeshed and resident."""
+    from vpm_free_gb300 import workloads as W
+    probs = W.batched_rings(64)
+    used = []
+    for n in names:
+        used.append([i for i, p in enumerate(probs) if p[2]["name"] == n and i not in used][0])
+    out = []
+    for xp, qp, w in (probs[i] for i in used):
+        h = V.VPM(V.VPMConfig.make(dpm=w["dpm"], box=w["box"]))
+        h.define_sizes(xp)
+        xr, qr = h.remesh_particles_3d(1, xp, qp)
+        h.set_particles(xr, qr)
+        out.append((h, xr, qr, w))
+    return out
+
+
+def test_shared_operator_batch_equals_individual_runs(gpulib):
+    """Three 32^3 problems with different spacings share one recorded
+    boundary operator (weights scaled by the spacing ratio, one apply for
+    the group); a 48^3 problem runs its own graph.  Each must reproduce its
+    individual run: the grouped ones to rounding (another summation order,
+    scaled weights), the single one bit for bit."""
+    V = gpulib
+    names = ["ring32", "ring32", "ring32", "ring48"]
+    solo = []
+    for h, _, _, w in _batch_problems(V, names):
+        h.run(3, 0.01)
+        solo.append(h.get_particles())
+        h.close()
+    hp = _batch_problems(V, names)
+    hs = [t[0] for t in hp]
+    assert len({t[3]["dpm"][0] for t in hp[:3]}) == 3  # three spacings
+    with V.Batch(hs) as b:
+        assert b.info() == (2, 3)
+        ms, solves, ps = b.run(3, 0.01)
+    assert solves == 12 and ms > 0 and ps > 0
+    for i, (h, (x0, q0)) in enumerate(zip(hs, solo)):
+        x1, q1 = h.get_particles()
+        assert x1.shape == x0.shape
+        if i == 3:
+            assert np.array_equal(x0, x1) and np.array_equal(q0, q1)
+        else:
+            assert rel_l2(x1, x0) <= 1e-12 and rel_l2(q1, q0) <= 1e-11
+        h.close()
+
+
+def test_shared_operator_batch_fields_match_oracle(gpulib, oracle):
+    """One batched step of a two-problem group: the resident vector
+    potential and velocity of each member against the oracle's step on the
+    same particles."""
+    V, O = gpulib, oracle
+    hp = _batch_problems(V, ["ring32", "ring32"])
+    with V.Batch([t[0] for t in hp]) as b:
+        assert b.info() == (1, 2)
+        b.run(1, 0.01)
+    for h, xr, qr, w in hp:
+        ocfg, _ = configs_for(w)
+        s = O.define_sizes(ocfg, xr)
+        O.step_fields(ocfg, s, xr, qr)
+        assert rel_l2(h.field("sol").ravel(), O.get_field(O.F_SOL)) <= FIELD_TOL
+        assert rel_l2(h.field("vel").ravel(), O.get_field(O.F_VEL)) <= FIELD_TOL
+        h.close()
+
+
 def test_two_level_ncoarse2_matches_oracle(gpulib, oracle):
     """YAPS with ncoarse = 2: the padded block (cells = 4 mod 8) has dummy
     quadtree cells at levels 2 and 3 (build_level_nbound_3d)."""

@@ -39,7 +39,7 @@ EXPORTS = [
     "vpmg_set_profiling", "vpmg_set_operator_budget", "vpmg_run", "vpmg_bench_kernel", "vpmg_fp64_peak", "vpmg_batch_run",
     "vpmg_read_particles_bin", "vpmg_write_particles_bin", "vpmg_write_solution", "vpmg_write_hist", "vpmg_set_output",
     "vpmg_dst_tiles", "vpmg_apply_poisson", "vpmg_adjoint_poisson", "vpmg_vjp_fields", "vpmg_vjp_remesh", "vpmg_adjoint_loss",
-    "vpmg_adjoint_run",
+    "vpmg_adjoint_run", "vpmg_batch_create", "vpmg_batch_info", "vpmg_batch_step", "vpmg_batch_destroy",
 ]
 
 
@@ -133,6 +133,11 @@ def load_library():
     L.vpmg_fp64_peak.argtypes = [C.c_void_p, _dp]
     L.vpmg_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_double, C.c_int, _dp,
                                  C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.vpmg_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]
+    L.vpmg_batch_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
+    L.vpmg_batch_step.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, _dp, C.POINTER(C.c_longlong),
+                                  C.POINTER(C.c_longlong)]
+    L.vpmg_batch_destroy.argtypes = [C.c_void_p]
     L.vpmg_read_particles_bin.argtypes = [C.c_char_p, C.POINTER(C.c_int), _dp, _dp, _dp, C.c_int]
     L.vpmg_write_particles_bin.argtypes = [C.c_char_p, C.c_int, C.c_double, _dp, _dp]
     L.vpmg_write_solution.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
@@ -350,6 +355,12 @@ class VPM:
             handles[0]._chk(rc)
         return ms.value, sv.value, ps.value
 
+    @staticmethod
+    def batch(handles):
+        """Batch object over `handles` (problems sharing a boundary operator
+        are grouped); see Batch."""
+        return Batch(handles)
+
     def bench_kernel(self, which, reps=5):
         """(ms per replay, algorithmic flops, algorithmic bytes) of one kernel."""
         ms, fl, by = C.c_double(0), C.c_double(0), C.c_double(0)
@@ -488,3 +499,55 @@ class VPM:
         self._chk(self._L.vpmg_adjoint_run(self._h, int(nsteps), float(dt), _p(pr), n, float(ke_weight),
                                            C.byref(loss), _p(xbar), _p(qbar), C.byref(tf), C.byref(tb)))
         return loss.value, xbar[:nvr], qbar[:nvr], tf.value, tb.value
+
+
+class Batch:
+    """Independent problems advanced together (vpmg_batch_create): problems
+    whose fine-block boundary operators agree up to the mesh spacing share
+    one operator apply per step; every group and every other problem is one
+    captured graph, replayed concurrently.  The handles must stay open."""
+
+    def __init__(self, handles):
+        self._L = load_library()
+        self._hs = list(handles)
+        arr = (C.c_void_p * len(self._hs))(*[h._h for h in self._hs])
+        self._b = C.c_void_p()
+        rc = self._L.vpmg_batch_create(arr, len(self._hs), C.byref(self._b))
+        if rc != 0:
+            self._hs[0]._chk(rc)
+
+    def info(self):
+        """(graphs replayed per step, problems in shared-operator groups)"""
+        return self.details()[:2]
+
+    def details(self):
+        """(graphs per step, problems sharing an operator, corrected rows)"""
+        u, s, r = C.c_int(0), C.c_int(0), C.c_longlong(0)
+        self._L.vpmg_batch_info(self._b, C.byref(u), C.byref(s), C.byref(r))
+        return u.value, s.value, r.value
+
+    def run(self, nsteps, dt, remesh=True):
+        """Returns (device ms, solves, particle-steps)."""
+        ms, sv, ps = C.c_double(0), C.c_longlong(0), C.c_longlong(0)
+        rc = self._L.vpmg_batch_step(self._b, int(nsteps), float(dt), 1 if remesh else 0, C.byref(ms), C.byref(sv),
+                                     C.byref(ps))
+        if rc != 0:
+            self._hs[0]._chk(rc)
+        return ms.value, sv.value, ps.value
+
+    def close(self):
+        if self._b:
+            self._L.vpmg_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -271,14 +271,12 @@ void poisson_part_multi(vpmg_handle* h) {
   ev_mark(h, 6);
 }
 
-void poisson_part(vpmg_handle* h) {
-  if (h->nblk > 1) {
-    poisson_part_multi(h);
-    return;
-  }
+// Single block, up to the fine block's boundary sources: rhsscat_3d and the
+// zero-BC block solves with their normal-derivative panels.
+void poisson_head(vpmg_handle* h) {
   cudaStream_t st = h->stream;
   const vpmg_sizes& s = h->sz;
-  const size_t N = h->gglob.count(), NB = h->gbl.count(), NC = h->gco.count();
+  const size_t N = h->gglob.count(), NB = h->gbl.count();
   double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
   // rhsscat_3d: global interior -> block inner box; the block padding stays zero
   const int go[3] = {s.nn_bl[0] - 1, s.nn_bl[1] - 1, s.nn_bl[2] - 1};
@@ -295,8 +293,17 @@ void poisson_part(vpmg_handle* h) {
     boundary_panels(h->bo_bl, h->gbl, h->sol0.p, c, st);
   }
   ev_mark(h, 2);
+}
+
+// Single block, from the fine block's boundary values on: BC solves,
+// coarse grid, final inner-box solve and solget_3d.
+void poisson_tail(vpmg_handle* h) {
+  cudaStream_t st = h->stream;
+  const vpmg_sizes& s = h->sz;
+  const size_t N = h->gglob.count(), NB = h->gbl.count(), NC = h->gco.count();
+  const int go[3] = {s.nn_bl[0] - 1, s.nn_bl[1] - 1, s.nn_bl[2] - 1};
+  const bool full = h->full_block_solves || h->keep_intermediates;
   double* SB[3] = {comp(h->sol_bl, NB, 0), comp(h->sol_bl, NB, 1), comp(h->sol_bl, NB, 2)};
-  boundary_apply(h->bo_bl, h->gbl, SB, st);
   ev_mark(h, 3);
   for (int c = 0; c < 3; ++c) {
     if (full) dirichlet_solve(h->dp_bl, comp(h->rhs_bl, NB, c), SB[c], false, h->work.p, st);
@@ -327,21 +334,44 @@ void poisson_part(vpmg_handle* h) {
   ev_mark(h, 6);
 }
 
+void poisson_part(vpmg_handle* h) {
+  if (h->nblk > 1) {
+    poisson_part_multi(h);
+    return;
+  }
+  poisson_head(h);
+  const size_t NB = h->gbl.count();
+  double* SB[3] = {comp(h->sol_bl, NB, 0), comp(h->sol_bl, NB, 1), comp(h->sol_bl, NB, 2)};
+  boundary_apply(h->bo_bl, h->gbl, SB, h->stream);
+  poisson_tail(h);
+}
+
 // Field part of vpm(WhatToDo = 2) on binned particles (vpm.f90:171-314 + yaps3d).
-void field_step(vpmg_handle* h) {
-  cudaStream_t st = h->stream;
-  const vpmg_sizes& s = h->sz;
+void deposit_rhs(vpmg_handle* h) {
   const size_t N = h->gglob.count();
   const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
   double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
-  deposit(h->parts, mg, h->bins, R, st);
-  poisson_part(h);
+  deposit(h->parts, mg, h->bins, R, h->stream);
+}
+
+// calc_velocity_serial_3d(1) on h->sol and h->rhs
+void field_velocity(vpmg_handle* h) {
+  cudaStream_t st = h->stream;
+  const vpmg_sizes& s = h->sz;
+  const size_t N = h->gglob.count();
+  double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
   double* S[3] = {comp(h->sol, N, 0), comp(h->sol, N, 1), comp(h->sol, N, 2)};
   // calc_velocity_serial_3d(1)
   double* V[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
   double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
   velocity_and_stretching(s.nn, s.dpm, S, R, V, G, st);
   ev_mark(h, 7);
+}
+
+void field_step(vpmg_handle* h) {
+  deposit_rhs(h);
+  poisson_part(h);
+  field_velocity(h);
 }
 
 void m2p_step(vpmg_handle* h, bool write_up, bool euler, double dt, const double uinf[3]) {
@@ -619,6 +649,23 @@ __global__ void k_log_count(int* __restrict__ hist, int* __restrict__ counter, c
 
 constexpr int kHistCap = 1 << 16;
 
+// A single-block step in two parts around the fine block's boundary
+// operator (one_step = step_head, boundary_apply, step_tail), so that
+// problems sharing an operator can meet at one apply.
+void step_head(vpmg_handle* h) {
+  ev_mark(h, 0);
+  bin_particles(h->parts, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
+  deposit_rhs(h);
+  poisson_head(h);
+}
+void step_tail(vpmg_handle* h, double dt, const double u0[3], int do_remesh) {
+  poisson_tail(h);
+  field_velocity(h);
+  m2p_step(h, true, true, dt, u0);
+  if (do_remesh) remesh(h);
+  else ev_mark(h, 9);
+}
+
 void one_step(vpmg_handle* h, double dt, const double uinf[3], int do_remesh) {
   VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
   const double u0[3] = {uinf ? uinf[0] : 0.0, uinf ? uinf[1] : 0.0, uinf ? uinf[2] : 0.0};
@@ -798,6 +845,271 @@ int vpmg_batch_run(vpmg_handle* const* hs, int n, int nsteps, double dt, int do_
     if (solves) *solves = (long long)n * nsteps;
     if (particle_steps) *particle_steps = ps;
   });
+}
+
+// ---------------------------------------------------------------- batch ----
+// Problems grouped by shared boundary operator.  A unit is one problem (its
+// own step graph) or a group of up to kGroupMax problems whose fine-block
+// operators are one recorded operator up to the mesh-spacing factor: the
+// group's step is one graph in which every member runs its step head on its
+// own stream, one launch applies the leader's operator to all members'
+// sources (the weights stream from HBM once for the group), and the members
+// run their step tails.  Units replay step by step on their leaders' streams.
+struct vpmg_batch {
+  struct Unit {
+    std::vector<int> m;  // indices into hs; m[0] leads
+    std::vector<double> ratio;
+    std::vector<std::unique_ptr<GroupCorrection>> corr;  // per member (the leader's is empty)
+    int lanes_log2 = 0;
+    vpmg::DBuf<float2> gsrc;
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;
+    double dt = 0.0;
+    int remesh = -1;
+  };
+  std::vector<vpmg_handle*> hs;
+  std::vector<std::unique_ptr<Unit>> units;
+  ~vpmg_batch() {
+    for (auto& u : units)
+      if (u->exec) cudaGraphExecDestroy(u->exec);
+  }
+};
+
+namespace {
+// a follower whose recorded operator differs from the leader's in more than
+// this fraction of the interactions keeps its own graph
+constexpr double kGroupMaxCorrected = 0.02;
+
+bool group_eligible(const vpmg_handle* h) {
+  return h->prepared && h->nblk == 1 && h->bo_bl.precomputed && h->bo_bl.ibctyp == 2 && !h->keep_intermediates &&
+         !h->no_graphs && !h->full_block_solves;
+}
+
+void capture_group(vpmg_batch* b, vpmg_batch::Unit& u, double dt, int do_remesh) {
+  const double u0[3] = {0.0, 0.0, 0.0};
+  const int n = (int)u.m.size();
+  std::vector<vpmg_handle*> H(n);
+  for (int k = 0; k < n; ++k) H[k] = b->hs[u.m[k]];
+  vpmg_handle* L = H[0];
+  cudaStream_t ls = L->stream;
+  if (u.exec) {
+    cudaGraphExecDestroy(u.exec);
+    u.exec = nullptr;
+  }
+  GroupOut G{};
+  for (int k = 0; k < n; ++k) {
+    const size_t NB = H[k]->gbl.count();
+    for (int c = 0; c < 3; ++c) G.o[k][c] = H[k]->sol_bl.p + c * NB;
+    G.scale[k] = -u.ratio[k] / (4.0 * kPI);
+    H[k]->hist.ensure(kHistCap);
+    H[k]->hist_counter.ensure(1);
+  }
+  std::vector<cudaEvent_t> ev(2 * n + 1, nullptr);
+  for (auto& e : ev) VPMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  std::vector<char> prof(n);
+  std::vector<long long> l0(n);
+  for (int k = 0; k < n; ++k) {
+    prof[k] = H[k]->profile;
+    H[k]->profile = false;
+    l0[k] = H[k]->launches;
+  }
+  auto restore = [&] {
+    for (int k = 0; k < n; ++k) H[k]->profile = prof[k];
+    for (auto e : ev) cudaEventDestroy(e);
+  };
+  const int lanes = 1 << u.lanes_log2;
+  cudaGraph_t g = nullptr;
+  try {
+    VPMG_CUDA(cudaStreamBeginCapture(ls, cudaStreamCaptureModeThreadLocal));
+    try {
+      VPMG_CUDA(cudaEventRecord(ev[0], ls));
+      for (int k = 1; k < n; ++k) VPMG_CUDA(cudaStreamWaitEvent(H[k]->stream, ev[0], 0));
+      for (int k = 0; k < n; ++k) {
+        LaunchScope sc(H[k]);
+        k_log_count<<<1, 1, 0, H[k]->stream>>>(H[k]->hist.p, H[k]->hist_counter.p, H[k]->parts.d_np.p, kHistCap);
+        VPMG_LAUNCHED();
+        step_head(H[k]);
+        boundary_group_sources(H[k]->bo_bl, u.gsrc.p, k, lanes, H[k]->stream);
+      }
+      for (int k = 1; k < n; ++k) {
+        VPMG_CUDA(cudaEventRecord(ev[k], H[k]->stream));
+        VPMG_CUDA(cudaStreamWaitEvent(ls, ev[k], 0));
+      }
+      {
+        LaunchScope sc(L);
+        boundary_group_apply(L->bo_bl, u.gsrc.p, n, u.lanes_log2, G, ls);
+      }
+      VPMG_CUDA(cudaEventRecord(ev[n], ls));
+      for (int k = 1; k < n; ++k) VPMG_CUDA(cudaStreamWaitEvent(H[k]->stream, ev[n], 0));
+      for (int k = 0; k < n; ++k) {
+        LaunchScope sc(H[k]);
+        const size_t NB = H[k]->gbl.count();
+        double* SB[3] = {H[k]->sol_bl.p, H[k]->sol_bl.p + NB, H[k]->sol_bl.p + 2 * NB};
+        boundary_group_correct(H[k]->bo_bl, *u.corr[k], SB, H[k]->stream);
+        step_tail(H[k], dt, u0, do_remesh);
+      }
+      for (int k = 1; k < n; ++k) {
+        VPMG_CUDA(cudaEventRecord(ev[n + k], H[k]->stream));
+        VPMG_CUDA(cudaStreamWaitEvent(ls, ev[n + k], 0));
+      }
+    } catch (...) {
+      cudaStreamEndCapture(ls, &g);
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      throw;
+    }
+    VPMG_CUDA(cudaStreamEndCapture(ls, &g));
+    cudaError_t e = cudaGraphInstantiate(&u.exec, g, 0);
+    cudaGraphDestroy(g);
+    VPMG_CUDA(e);
+  } catch (...) {
+    for (int k = 0; k < n; ++k) H[k]->launches = l0[k];
+    restore();
+    throw;
+  }
+  u.launches = 0;
+  for (int k = 0; k < n; ++k) {
+    u.launches += H[k]->launches - l0[k];
+    H[k]->launches = l0[k];
+  }
+  restore();
+  u.dt = dt;
+  u.remesh = do_remesh;
+}
+}  // namespace
+
+int vpmg_batch_create(vpmg_handle* const* hs, int n, vpmg_batch** out) {
+  if (!hs || n <= 0 || !out) return VPMG_ERR_ARG;
+  *out = nullptr;
+  for (int i = 0; i < n; ++i)
+    if (!hs[i]) return VPMG_ERR_ARG;
+  std::unique_ptr<vpmg_batch> b(new vpmg_batch);
+  b->hs.assign(hs, hs + n);
+  const int rc = guarded(hs[0], [&] {
+    for (int i = 0; i < n; ++i) {
+      vpmg_handle* h = hs[i];
+      VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first (every problem of a batch)");
+      VPMG_CHECK(h->device == hs[0]->device, VPMG_ERR_ARG, "a batch runs on one device");
+      for (int j = 0; j < i; ++j) VPMG_CHECK(hs[j] != h, VPMG_ERR_ARG, "a problem appears twice in the batch");
+      bool placed = false;
+      if (group_eligible(h)) {
+        for (auto& u : b->units) {
+          vpmg_handle* L = hs[u->m[0]];
+          double r = 1.0;
+          if ((int)u->m.size() >= kGroupMax || !group_eligible(L)) continue;
+          std::unique_ptr<GroupCorrection> c(new GroupCorrection);
+          if (boundary_group_match(L->bo_bl, L->gbl, h->bo_bl, h->gbl, kGroupMaxCorrected, &r, *c, h->stream)) {
+            u->m.push_back(i);
+            u->ratio.push_back(r);
+            u->corr.push_back(std::move(c));
+            placed = true;
+            break;
+          }
+        }
+      }
+      if (!placed) {
+        b->units.emplace_back(new vpmg_batch::Unit);
+        b->units.back()->m.push_back(i);
+        b->units.back()->ratio.push_back(1.0);
+        b->units.back()->corr.emplace_back(new GroupCorrection);
+      }
+    }
+    for (auto& u : b->units) {
+      if (u->m.size() < 2) continue;
+      while ((1 << u->lanes_log2) < (int)u->m.size()) ++u->lanes_log2;
+      const BoundaryOp& L = hs[u->m[0]]->bo_bl;
+      u->gsrc.ensure(4 * (size_t)L.ncell_total << u->lanes_log2);
+      VPMG_CUDA(cudaMemsetAsync(u->gsrc.p, 0, u->gsrc.bytes(), hs[u->m[0]]->stream));
+      VPMG_CUDA(cudaStreamSynchronize(hs[u->m[0]]->stream));
+    }
+  });
+  if (rc != VPMG_OK) return rc;
+  *out = b.release();
+  return VPMG_OK;
+}
+
+int vpmg_batch_info(const vpmg_batch* b, int* units, int* shared, long long* correction_rows) {
+  if (!b) return VPMG_ERR_ARG;
+  int s = 0;
+  long long cr = 0;
+  for (auto& u : b->units) {
+    if (u->m.size() > 1) s += (int)u->m.size();
+    for (auto& c : u->corr) cr += c->nrows;
+  }
+  if (units) *units = (int)b->units.size();
+  if (shared) *shared = s;
+  if (correction_rows) *correction_rows = cr;
+  return VPMG_OK;
+}
+
+int vpmg_batch_step(vpmg_batch* b, int nsteps, double dt, int do_remesh, double* ms, long long* solves,
+                    long long* particle_steps) {
+  if (!b || nsteps < 0) return VPMG_ERR_ARG;
+  vpmg_handle* h0 = b->hs[0];
+  return guarded(h0, [&] {
+    VPMG_CHECK(nsteps <= kHistCap, VPMG_ERR_ARG, "too many steps for one batched run");
+    for (auto& u : b->units) {
+      if (u->m.size() == 1) {
+        vpmg_handle* h = b->hs[u->m[0]];
+        LaunchScope sc(h);
+        ensure_graph(h, dt, nullptr, do_remesh);
+      } else if (!u->exec || u->dt != dt || u->remesh != do_remesh) {
+        capture_group(b, *u, dt, do_remesh);
+      }
+    }
+    for (vpmg_handle* h : b->hs) {
+      VPMG_CUDA(cudaMemsetAsync(h->hist_counter.p, 0, sizeof(int), h->stream));
+      VPMG_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    cudaEvent_t start, stop;
+    VPMG_CUDA(cudaEventCreate(&start));
+    VPMG_CUDA(cudaEventCreate(&stop));
+    const size_t nu = b->units.size();
+    std::vector<cudaEvent_t> done(nu, nullptr);
+    for (auto& e : done) VPMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    auto lead = [&](size_t i) { return b->hs[b->units[i]->m[0]]; };
+    VPMG_CUDA(cudaEventRecord(start, h0->stream));
+    for (size_t i = 0; i < nu; ++i)
+      if (lead(i)->stream != h0->stream) VPMG_CUDA(cudaStreamWaitEvent(lead(i)->stream, start, 0));
+    for (int k = 0; k < nsteps; ++k)
+      for (size_t i = 0; i < nu; ++i) {
+        const auto& u = *b->units[i];
+        cudaGraphExec_t ex = (u.m.size() == 1) ? lead(i)->graph.exec : u.exec;
+        VPMG_CUDA(cudaGraphLaunch(ex, lead(i)->stream));
+      }
+    for (size_t i = 0; i < nu; ++i) {
+      if (lead(i)->stream == h0->stream) continue;
+      VPMG_CUDA(cudaEventRecord(done[i], lead(i)->stream));
+      VPMG_CUDA(cudaStreamWaitEvent(h0->stream, done[i], 0));
+    }
+    VPMG_CUDA(cudaEventRecord(stop, h0->stream));
+    VPMG_CUDA(cudaEventSynchronize(stop));
+    float t = 0.f;
+    VPMG_CUDA(cudaEventElapsedTime(&t, start, stop));
+    cudaEventDestroy(start);
+    cudaEventDestroy(stop);
+    for (auto e : done) cudaEventDestroy(e);
+    long long ps = 0;
+    for (size_t i = 0; i < nu; ++i) {
+      const auto& u = *b->units[i];
+      const long long per = (u.m.size() == 1) ? lead(i)->graph.launches : u.launches;
+      lead(i)->launches += (long long)nsteps * per;
+    }
+    for (vpmg_handle* h : b->hs) {
+      ps += read_hist(h, nsteps);
+      LaunchScope ls(h);
+      sync_np(h);
+    }
+    if (ms) *ms = t;
+    if (solves) *solves = (long long)b->hs.size() * nsteps;
+    if (particle_steps) *particle_steps = ps;
+  });
+}
+
+int vpmg_batch_destroy(vpmg_batch* b) {
+  if (!b) return VPMG_ERR_ARG;
+  delete b;
+  return VPMG_OK;
 }
 
 int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* flops, double* bytes) {

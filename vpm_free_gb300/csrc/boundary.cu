@@ -384,6 +384,212 @@ __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__
   }
 }
 
+// Group sources: problem `slot` of a group writes its float-float records
+// into slot `slot` of [cell][slot][s0 s1 s2 0], so that the problems'
+// records of one cell are adjacent (one coalesced load per warp).
+__global__ void k_split_slot(const double* __restrict__ x, int ncell, int slot, int lanes, float2* __restrict__ out) {
+  const size_t n = 4 * (size_t)ncell;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cell = (int)(i >> 2), comp = (int)(i & 3);
+    float2 v = make_float2(0.0f, 0.0f);
+    if (comp < 3) {
+      const double d = x[(size_t)comp * ncell + cell];
+      const float hi = __double2float_rn(d);
+      v = make_float2(hi, __double2float_rn(d - (double)hi));
+    }
+    out[((size_t)cell * lanes + slot) * 4 + comp] = v;
+  }
+}
+
+__device__ __forceinline__ void ff_mac3(FF& a0, FF& a1, FF& a2, float2 w, const float4* __restrict__ rec) {
+  const float4 a = __ldg(rec), z = __ldg(rec + 1);
+  ff_mac(a0, w, make_float2(a.x, a.y));
+  ff_mac(a1, w, make_float2(a.z, a.w));
+  ff_mac(a2, w, make_float2(z.x, z.y));
+}
+
+// One recorded operator applied to the sources of up to kGroupMax problems
+// with the same index geometry (their weights differ by the factor of the
+// mesh spacing, folded into G.scale).  A warp per boundary node; lane
+// p + LG * grp serves problem p (LG = 2^lanes_log2 lanes per problem set)
+// and every NG-th interaction from grp, so the weight and cell id are read
+// once for all problems and the problems' source records of a cell are one
+// contiguous load.  The dense block (coarsest level) comes first, then the
+// row of the finer levels; the NG partial sums meet in a fixed shuffle tree.
+__global__ void __launch_bounds__(256) k_apply_group(const long long* __restrict__ rowptr, const int* __restrict__ col,
+                                                     const float2* __restrict__ wgt, const float2* __restrict__ wtop,
+                                                     int top0, int ntop, int ntop2, const float4* __restrict__ gsrc,
+                                                     const int* __restrict__ tgt_node, int ntarget, int nprob,
+                                                     int lanes_log2, GroupOut G) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ntarget) return;
+  const int LG = 1 << lanes_log2, NG = 32 >> lanes_log2;
+  const int p = lane & (LG - 1), grp = lane >> lanes_log2;
+  const bool act = p < nprob;
+  const float4* sp = gsrc + 2 * (size_t)p;
+  const size_t cstride = 2 * (size_t)LG;  // float4s per cell
+  FF f0, f1, f2, g0, g1, g2;
+  if (wtop && act) {
+    const float2* wrow = wtop + (size_t)(warp >> 5) * ntop2 * 64 + (warp & 31) * 2;
+    int c = grp;
+    for (; c + NG < ntop; c += 2 * NG) {
+      const int c2 = c + NG;
+      const float2 wa = __ldg(&wrow[(size_t)(c >> 1) * 64 + (c & 1)]);
+      const float2 wb = __ldg(&wrow[(size_t)(c2 >> 1) * 64 + (c2 & 1)]);
+      ff_mac3(f0, f1, f2, wa, sp + (size_t)(top0 + c) * cstride);
+      ff_mac3(g0, g1, g2, wb, sp + (size_t)(top0 + c2) * cstride);
+    }
+    if (c < ntop) ff_mac3(f0, f1, f2, __ldg(&wrow[(size_t)(c >> 1) * 64 + (c & 1)]), sp + (size_t)(top0 + c) * cstride);
+  }
+  const long long b = rowptr[warp], e = rowptr[warp + 1];
+  if (act) {
+    long long k = b + grp;
+    for (; k + 3 * NG < e; k += 4 * NG) {
+      int c[4];
+      float2 w[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) c[u] = __ldg(&col[k + u * NG]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) w[u] = __ldg(&wgt[k + u * NG]);
+#pragma unroll
+      for (int u = 0; u < 4; u += 2) {
+        ff_mac3(f0, f1, f2, w[u], sp + (size_t)c[u] * cstride);
+        ff_mac3(g0, g1, g2, w[u + 1], sp + (size_t)c[u + 1] * cstride);
+      }
+    }
+    for (; k < e; k += NG) ff_mac3(f0, f1, f2, __ldg(&wgt[k]), sp + (size_t)__ldg(&col[k]) * cstride);
+  }
+  double a0 = ((double)f0.hi + (double)f0.lo) + ((double)g0.hi + (double)g0.lo);
+  double a1 = ((double)f1.hi + (double)f1.lo) + ((double)g1.hi + (double)g1.lo);
+  double a2 = ((double)f2.hi + (double)f2.lo) + ((double)g2.hi + (double)g2.lo);
+  for (int o = LG; o < 32; o <<= 1) {
+    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+  }
+  if (grp == 0 && act) {
+    const int node = tgt_node[warp];
+    const double sc = G.scale[p];
+    G.o[p][0][node] += a0 * sc;
+    G.o[p][1][node] += a1 * sc;
+    G.o[p][2][node] += a2 * sc;
+  }
+}
+
+// Set-up comparison of a follower's recorded operator F with the leader's
+// L scaled by `ratio`.  Their rows differ where a cell lies exactly on the
+// opening radius of the tree walk in index units (each problem's rounding
+// decides the tie): one accepted the cell, the other its children.  A walk
+// visits cells in the tree's preorder, so both rows are sorted by pre[cell]
+// and a merge gives their difference: F's cells missing from L (weight
+// +wF) and L's missing from F (weight -ratio wL); for the dense block, the
+// coarsest cells accepted by one of them.  Shared cells must agree within
+// `tol` (relative), else *bad is set.
+__device__ __forceinline__ bool ff_close(float2 a, float2 b, double ratio, double tol) {
+  const double va = (double)a.x + (double)a.y, vb = (double)b.x + (double)b.y;
+  if (va == 0.0 || vb == 0.0) return va == 0.0 && vb == 0.0;
+  return fabs(vb - ratio * va) <= tol * fabs(vb);
+}
+__device__ __forceinline__ size_t dense_at(int t, int c, int ntop2) {
+  return (((size_t)(t >> 5) * ntop2 + (c >> 1)) * 32 + (t & 31)) * 2 + (c & 1);
+}
+__device__ __forceinline__ double ffd(float2 v) { return (double)v.x + (double)v.y; }
+
+struct CorrArgs {
+  const long long *Lr, *Fr;
+  const int *Lc, *Fc;
+  const float2 *Lw, *Fw, *Ld, *Fd;
+  const int* pre;
+  int ntop, top0;
+  double ratio, tol;
+};
+
+template <bool FILL>
+__device__ int corr_row(const CorrArgs& A, int t, int* __restrict__ ocol, double* __restrict__ ow, bool& ok) {
+  long long i = A.Lr[t], j = A.Fr[t];
+  const long long ie = A.Lr[t + 1], je = A.Fr[t + 1];
+  int n = 0;
+  while (i < ie || j < je) {
+    const int ca = (i < ie) ? A.Lc[i] : -1, cb = (j < je) ? A.Fc[j] : -1;
+    const int pa = (ca >= 0) ? A.pre[ca] : 0x7fffffff, pb = (cb >= 0) ? A.pre[cb] : 0x7fffffff;
+    if (pa == pb) {
+      ok &= ff_close(A.Lw[i], A.Fw[j], A.ratio, A.tol);
+      ++i;
+      ++j;
+    } else if (pa < pb) {
+      if (FILL) { ocol[n] = ca; ow[n] = -A.ratio * ffd(A.Lw[i]); }
+      ++n;
+      ++i;
+    } else {
+      if (FILL) { ocol[n] = cb; ow[n] = ffd(A.Fw[j]); }
+      ++n;
+      ++j;
+    }
+  }
+  if (A.Ld) {
+    const int ntop2 = (A.ntop + 1) >> 1;
+    for (int c = 0; c < A.ntop; ++c) {
+      const float2 a = A.Ld[dense_at(t, c, ntop2)], b = A.Fd[dense_at(t, c, ntop2)];
+      const bool za = ffd(a) == 0.0, zb = ffd(b) == 0.0;
+      if (za != zb) {
+        if (FILL) { ocol[n] = A.top0 + c; ow[n] = ffd(b) - A.ratio * ffd(a); }
+        ++n;
+      } else if (!za) {
+        ok &= ff_close(a, b, A.ratio, A.tol);
+      }
+    }
+  }
+  return n;
+}
+
+__global__ void k_corr_count(CorrArgs A, const int* __restrict__ Lt, const int* __restrict__ Ft, int ntarget,
+                             int* __restrict__ cnt, int* __restrict__ bad) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntarget) return;
+  bool ok = Lt[t] == Ft[t];
+  cnt[t] = corr_row<false>(A, t, nullptr, nullptr, ok);
+  if (!ok) atomicOr(bad, 1);
+}
+
+__global__ void k_corr_fill(CorrArgs A, const int* __restrict__ rows, const long long* __restrict__ crp, int nrows,
+                            int* __restrict__ col, double* __restrict__ w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrows) return;
+  bool ok = true;
+  corr_row<true>(A, rows[i], col + crp[i], w + crp[i], ok);
+}
+
+// sol(node of row) += -1/(4 pi) * sum of the correction row (FP64; warp per row).
+__global__ void k_apply_corr(const int* __restrict__ rows, const long long* __restrict__ crp, int nrows,
+                             const int* __restrict__ col, const double* __restrict__ w, const double* __restrict__ src,
+                             int ncell, const int* __restrict__ tgt_node, double scale, double* __restrict__ o0,
+                             double* __restrict__ o1, double* __restrict__ o2) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= nrows) return;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (long long k = crp[i] + lane; k < crp[i + 1]; k += 32) {
+    const int c = col[k];
+    const double wk = w[k];
+    a0 = fma(wk, src[c], a0);
+    a1 = fma(wk, src[(size_t)ncell + c], a1);
+    a2 = fma(wk, src[2 * (size_t)ncell + c], a2);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+  }
+  if (lane == 0) {
+    const int node = tgt_node[rows[i]];
+    o0[node] += a0 * scale;
+    o1[node] += a1 * scale;
+    o2[node] += a2 * scale;
+  }
+}
+
 // calc_normalderiv_3d: one thread per panel.
 __global__ void k_normal_deriv(const double* __restrict__ sol0, int NX, int NY, int NZ, const int* __restrict__ face,
                                const int* __restrict__ pi, const int* __restrict__ pj, const int* __restrict__ pk,
@@ -647,12 +853,11 @@ void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp,
   VPMG_CUDA(cudaGetLastError());
 }
 
-void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStream_t s) {
-  (void)g;
+// Levels 1..levmax aggregate the level-0 panels (source_bound_lev).
+static void aggregate_levels(BoundaryOp& B, cudaStream_t s) {
   double* s0 = B.csrc.p;
   double* s1 = B.csrc.p + B.ncell_total;
   double* s2 = B.csrc.p + 2 * (size_t)B.ncell_total;
-  // levels 1..levmax aggregate level-0 panels (source_bound_lev)
   for (int l = 1; l <= B.levmax; ++l) {
     const int n = B.nbound_lev[l];
     if (n <= 0) continue;
@@ -660,6 +865,11 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
                                                 s0, s1, s2);
     VPMG_LAUNCHED();
   }
+}
+
+void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStream_t s) {
+  (void)g;
+  aggregate_levels(B, s);
   if (B.precomputed) {
     const size_t nc4 = 4 * (size_t)B.ncell_total;
     VPMG_CHECK(B.csrc_ff.n >= nc4, VPMG_ERR_STATE, "boundary operator recorded without its source buffer");
@@ -682,6 +892,115 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
     const WalkDev W = walk_dev(B);
     k_walk<kAccum><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, sol[0], sol[1], sol[2], nullptr, nullptr, nullptr, nullptr);
   }
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+
+bool boundary_group_match(const BoundaryOp& L, const Grid& gl, const BoundaryOp& F, const Grid& gf,
+                          double max_frac, double* ratio, GroupCorrection& C, cudaStream_t s) {
+  if (!L.precomputed || !F.precomputed || L.ibctyp != 2 || F.ibctyp != 2 || L.tree != F.tree) return false;
+  if (L.ntarget != F.ntarget || L.ncell_total != F.ncell_total || L.levmax != F.levmax || L.dense != F.dense ||
+      L.ntopd != F.ntopd || L.lev_off != F.lev_off || L.wtop.n != F.wtop.n)
+    return false;
+  for (int d = 0; d < 3; ++d)
+    if (gl.n[d] != gf.n[d]) return false;
+  // weights dS / r scale with the spacing when the cells are similar
+  const double r = gf.d[0] / gl.d[0];
+  for (int d = 1; d < 3; ++d)
+    if (std::fabs(gf.d[d] / gl.d[d] - r) > 1e-14 * r) return false;
+  // the tree (children, dummy flags) must be the same; preorder of its cells
+  const int nc = L.ncell_total, nt = L.ntarget;
+  std::vector<int> lch(4 * (size_t)nc), fch(4 * (size_t)nc), lfl((size_t)nc), ffl((size_t)nc);
+  VPMG_CUDA(cudaMemcpyAsync(lch.data(), L.child.p, sizeof(int) * lch.size(), cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaMemcpyAsync(fch.data(), F.child.p, sizeof(int) * fch.size(), cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaMemcpyAsync(lfl.data(), L.flags.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaMemcpyAsync(ffl.data(), F.flags.p, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  if (lch != fch || lfl != ffl) return false;
+  std::vector<int> pre((size_t)nc, -1);
+  {
+    int next = 0;
+    std::vector<std::pair<int, int>> st;  // (cell, level)
+    const int top0 = L.lev_off[L.levmax];
+    for (int c = L.ntopd - 1; c >= 0; --c) st.push_back({top0 + c, L.levmax});
+    while (!st.empty()) {
+      const auto [c, lev] = st.back();
+      st.pop_back();
+      if (c < 0 || c >= nc || pre[c] >= 0) continue;
+      pre[c] = next++;
+      if (lev == 0) continue;
+      const int k = (lfl[c] < 0) ? 2 : 4;
+      for (int q = k - 1; q >= 0; --q) st.push_back({lch[4 * (size_t)c + q], lev - 1});
+    }
+    for (int c = 0; c < nc; ++c)
+      if (pre[c] < 0) pre[c] = next++;  // not reachable from the top: never in a row
+  }
+  DBuf<int> dpre, cnt, bad;
+  upload(dpre, pre);
+  cnt.ensure((size_t)nt);
+  bad.ensure(1);
+  VPMG_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+  CorrArgs A{L.rowptr.p, F.rowptr.p, L.col.p, F.col.p, L.w.p, F.w.p, L.dense ? L.wtop.p : nullptr,
+             F.dense ? F.wtop.p : nullptr, dpre.p, L.ntopd, L.lev_off[L.levmax], r, 1e-12};
+  k_corr_count<<<(nt + 127) / 128, 128, 0, s>>>(A, L.tgt_node.p, F.tgt_node.p, nt, cnt.p, bad.p);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+  std::vector<int> hc((size_t)nt);
+  int hb = 1;
+  VPMG_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, sizeof(int) * nt, cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  if (hb) return false;
+  std::vector<int> rows;
+  std::vector<long long> crp(1, 0);
+  for (int t = 0; t < nt; ++t)
+    if (hc[t]) {
+      rows.push_back(t);
+      crp.push_back(crp.back() + hc[t]);
+    }
+  const double all = (double)(L.nnz + L.ndense_acc);
+  if ((double)crp.back() > max_frac * all) return false;
+  C.nrows = (int)rows.size();
+  C.nnz = crp.back();
+  if (C.nrows) {
+    upload(C.rows, rows);
+    upload(C.rowptr, crp);
+    C.col.ensure((size_t)C.nnz);
+    C.w.ensure((size_t)C.nnz);
+    k_corr_fill<<<(C.nrows + 127) / 128, 128, 0, s>>>(A, C.rows.p, C.rowptr.p, C.nrows, C.col.p, C.w.p);
+    VPMG_LAUNCHED();
+    VPMG_CUDA(cudaGetLastError());
+    VPMG_CUDA(cudaStreamSynchronize(s));
+  }
+  *ratio = r;
+  return true;
+}
+
+void boundary_group_correct(const BoundaryOp& F, const GroupCorrection& C, double* const sol[3], cudaStream_t s) {
+  if (!C.nrows) return;
+  k_apply_corr<<<(unsigned)(((long long)C.nrows * 32 + 255) / 256), 256, 0, s>>>(
+      C.rows.p, C.rowptr.p, C.nrows, C.col.p, C.w.p, F.csrc.p, F.ncell_total, F.tgt_node.p, -1.0 / (4.0 * kPI), sol[0],
+      sol[1], sol[2]);
+  VPMG_LAUNCHED();
+}
+
+void boundary_group_sources(BoundaryOp& B, float2* gsrc, int slot, int lanes, cudaStream_t s) {
+  aggregate_levels(B, s);
+  const size_t nc4 = 4 * (size_t)B.ncell_total;
+  k_split_slot<<<(unsigned)std::min<size_t>((nc4 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, B.ncell_total, slot,
+                                                                                        lanes, gsrc);
+  VPMG_LAUNCHED();
+}
+
+void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, int lanes_log2, const GroupOut& G,
+                          cudaStream_t s) {
+  VPMG_CHECK(L.precomputed && nprob >= 1 && nprob <= kGroupMax && (1 << lanes_log2) >= nprob && lanes_log2 <= 5,
+             VPMG_ERR_STATE, "group apply: operator not recorded or group too large");
+  const long long threads = (long long)L.ntarget * 32;
+  k_apply_group<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+      L.rowptr.p, L.col.p, L.w.p, L.dense ? L.wtop.p : nullptr, L.lev_off[L.levmax], L.ntopd, (L.ntopd + 1) / 2,
+      reinterpret_cast<const float4*>(gsrc), L.tgt_node.p, L.ntarget, nprob, lanes_log2, G);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }

@@ -175,6 +175,35 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
 // aggregate, then add the boundary values into the faces of sol.
 void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp, cudaStream_t s);
 void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStream_t s);
+// Problems that share one recorded operator (same index geometry, weights
+// in proportion to the mesh spacing): each problem's sources go to its slot
+// of an interleaved buffer [cell][slot][4] (float2), then one launch adds
+// every problem's boundary values (o[p][c] at the target nodes, times scale[p]).
+constexpr int kGroupMax = 16;
+struct GroupOut {
+  double* o[kGroupMax][3];
+  double scale[kGroupMax];
+};
+// Rows of a follower's operator that are not the leader's times the ratio
+// (ties of the opening test broken by each problem's rounding): the
+// follower's row minus the scaled leader's row, applied after the group.
+struct GroupCorrection {
+  int nrows = 0;
+  long long nnz = 0;
+  DBuf<int> rows;
+  DBuf<long long> rowptr;
+  DBuf<int> col;
+  DBuf<double> w;
+};
+// true when F can share L's recorded operator: same index geometry and
+// tree, weights L's times *ratio except for the cells where the two walks
+// decided differently, which C holds (at most max_frac of the interactions)
+bool boundary_group_match(const BoundaryOp& L, const Grid& gl, const BoundaryOp& F, const Grid& gf, double max_frac,
+                          double* ratio, GroupCorrection& C, cudaStream_t s);
+void boundary_group_correct(const BoundaryOp& F, const GroupCorrection& C, double* const sol[3], cudaStream_t s);
+void boundary_group_sources(BoundaryOp& B, float2* gsrc, int slot, int lanes, cudaStream_t s);
+void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, int lanes_log2, const GroupOut& G,
+                          cudaStream_t s);
 // Transposes (one component): boundary-value adjoint (grid node array) ->
 // cell adjoints -> panel adjoints -> accumulated into the sol0 adjoint.
 void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s);
