@@ -221,7 +221,8 @@ def run_batched(args, local):
     group_s = time.perf_counter() - t0
     units, shared, corr_rows = batch.details()
     reset()
-    batch.run(1, dt)                                 # warm-up, captures the group graphs
+    batch.run(2, dt)                                 # warm-up: captures the group graphs, tunes the schedule
+    sched, sched_ms = batch.schedule()
     reset()
     ms_b, solves, ps_b = batch.run(k, dt)
     batch.close()
@@ -266,6 +267,7 @@ def run_batched(args, local):
             "speedup_vs_reference_call_loop": (solves / (ms_b * 1e-3)) / (len(hs) * k / ref_loop_s),
             "graphs_per_step": units, "problems_sharing_an_operator": shared, "grouping_s": group_s,
             "corrected_rows": corr_rows,
+            "schedule": {"chosen": ["concurrent", "in sequence"][sched], "tuning_step_ms": sched_ms},
             "concurrent_graphs_solves_per_s": solves_c / (ms_c * 1e-3),
             "batched": "vpmg_batch_step: problems with the same index geometry share one recorded boundary "
                        "operator (one apply per group and step); each group and each other problem is one graph, "

@@ -215,7 +215,11 @@ int vpmg_batch_run(vpmg_handle* const* hs, int n, int nsteps, double dt, int rem
  * Replaces: the loop over independent problems a host runs around vpm()
  * (source/test.f90:83-150), one problem after another.                  */
 typedef struct vpmg_batch vpmg_batch;
-int vpmg_batch_create(vpmg_handle* const* hs, int n, vpmg_batch** out);
+/* flags: VPMG_BATCH_RELEASE_SHARED frees the followers' own recorded
+ * operators (the group reads only the leader's); on their own, those
+ * handles then walk the tree at every apply.                            */
+#define VPMG_BATCH_RELEASE_SHARED 1
+int vpmg_batch_create(vpmg_handle* const* hs, int n, int flags, vpmg_batch** out);
 /* *units = graphs replayed per step; *shared = problems in groups of >= 2;
  * *correction_rows = boundary nodes whose recorded row differs from the
  * group leader's scaled row (a cell exactly on the tree's opening radius in
@@ -226,6 +230,13 @@ int vpmg_batch_info(const vpmg_batch* b, int* units, int* shared, long long* cor
  * errors are reported through the first handle (vpmg_last_error).       */
 int vpmg_batch_step(vpmg_batch* b, int nsteps, double dt, int remesh, double* ms, long long* solves,
                     long long* particle_steps);
+/* Replay order of the batch's graphs within a step: 0 concurrent (each on
+ * its own stream), 1 one after another on one stream, -1 (default) chosen
+ * by timing the first two steps of the next call with nsteps >= 2 (one
+ * step each way; tuned_ms gives the two times).  Results do not depend on
+ * the order.                                                             */
+int vpmg_batch_set_schedule(vpmg_batch* b, int schedule);
+int vpmg_batch_get_schedule(const vpmg_batch* b, int* schedule, float tuned_ms[2]);
 int vpmg_batch_destroy(vpmg_batch* b);
 /* Replays one kernel of the last step `reps` times between CUDA events on
  * the handle's stream (instrumentation for roofline figures).

@@ -214,19 +214,29 @@ def test_shared_operator_batch_equals_individual_runs(gpulib):
 def test_shared_operator_batch_fields_match_oracle(gpulib, oracle):
     """One batched step of a two-problem group: the resident vector
     potential and velocity of each member against the oracle's step on the
-    same particles."""
+    same particles.  The follower's own operator is released; afterwards it
+    steps alone by walking the tree."""
     V, O = gpulib, oracle
     hp = _batch_problems(V, ["ring32", "ring32"])
-    with V.Batch([t[0] for t in hp]) as b:
+    with V.Batch([t[0] for t in hp], release_shared=True) as b:
         assert b.info() == (1, 2)
         b.run(1, 0.01)
+    assert hp[1][0].tree_stats()["precomputed"] is False
     for h, xr, qr, w in hp:
         ocfg, _ = configs_for(w)
         s = O.define_sizes(ocfg, xr)
         O.step_fields(ocfg, s, xr, qr)
         assert rel_l2(h.field("sol").ravel(), O.get_field(O.F_SOL)) <= FIELD_TOL
         assert rel_l2(h.field("vel").ravel(), O.get_field(O.F_VEL)) <= FIELD_TOL
-        h.close()
+    h = hp[1][0]
+    h.set_particles(hp[1][1], hp[1][2])
+    h.step(0.01)
+    ocfg, _ = configs_for(hp[1][3])
+    s = O.define_sizes(ocfg, hp[1][1])
+    O.step_fields(ocfg, s, hp[1][1], hp[1][2])
+    assert rel_l2(h.field("sol").ravel(), O.get_field(O.F_SOL)) <= FIELD_TOL
+    for t in hp:
+        t[0].close()
 
 
 def test_two_level_ncoarse2_matches_oracle(gpulib, oracle):

@@ -40,6 +40,7 @@ EXPORTS = [
     "vpmg_read_particles_bin", "vpmg_write_particles_bin", "vpmg_write_solution", "vpmg_write_hist", "vpmg_set_output",
     "vpmg_dst_tiles", "vpmg_apply_poisson", "vpmg_adjoint_poisson", "vpmg_vjp_fields", "vpmg_vjp_remesh", "vpmg_adjoint_loss",
     "vpmg_adjoint_run", "vpmg_batch_create", "vpmg_batch_info", "vpmg_batch_step", "vpmg_batch_destroy",
+    "vpmg_batch_set_schedule", "vpmg_batch_get_schedule",
 ]
 
 
@@ -133,11 +134,13 @@ def load_library():
     L.vpmg_fp64_peak.argtypes = [C.c_void_p, _dp]
     L.vpmg_batch_run.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_double, C.c_int, _dp,
                                  C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
-    L.vpmg_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]
+    L.vpmg_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_void_p)]
     L.vpmg_batch_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
     L.vpmg_batch_step.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, _dp, C.POINTER(C.c_longlong),
                                   C.POINTER(C.c_longlong)]
     L.vpmg_batch_destroy.argtypes = [C.c_void_p]
+    L.vpmg_batch_set_schedule.argtypes = [C.c_void_p, C.c_int]
+    L.vpmg_batch_get_schedule.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     L.vpmg_read_particles_bin.argtypes = [C.c_char_p, C.POINTER(C.c_int), _dp, _dp, _dp, C.c_int]
     L.vpmg_write_particles_bin.argtypes = [C.c_char_p, C.c_int, C.c_double, _dp, _dp]
     L.vpmg_write_solution.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
@@ -507,12 +510,14 @@ class Batch:
     one operator apply per step; every group and every other problem is one
     captured graph, replayed concurrently.  The handles must stay open."""
 
-    def __init__(self, handles):
+    def __init__(self, handles, release_shared=False):
+        """release_shared: free the followers' own recorded operators (their
+        standalone applies then walk the tree)."""
         self._L = load_library()
         self._hs = list(handles)
         arr = (C.c_void_p * len(self._hs))(*[h._h for h in self._hs])
         self._b = C.c_void_p()
-        rc = self._L.vpmg_batch_create(arr, len(self._hs), C.byref(self._b))
+        rc = self._L.vpmg_batch_create(arr, len(self._hs), 1 if release_shared else 0, C.byref(self._b))
         if rc != 0:
             self._hs[0]._chk(rc)
 
@@ -534,6 +539,18 @@ class Batch:
         if rc != 0:
             self._hs[0]._chk(rc)
         return ms.value, sv.value, ps.value
+
+    def set_schedule(self, mode):
+        """0 concurrent, 1 in sequence, -1 tuned on the next run of >= 2 steps."""
+        rc = self._L.vpmg_batch_set_schedule(self._b, int(mode))
+        if rc != 0:
+            raise ValueError("schedule must be -1, 0 or 1")
+
+    def schedule(self):
+        """(mode, [ms of the tuning step run concurrently, in sequence])"""
+        m, t = C.c_int(0), (C.c_float * 2)()
+        self._L.vpmg_batch_get_schedule(self._b, C.byref(m), t)
+        return m.value, [t[0], t[1]]
 
     def close(self):
         if self._b:

@@ -860,7 +860,6 @@ struct vpmg_batch {
     std::vector<int> m;  // indices into hs; m[0] leads
     std::vector<double> ratio;
     std::vector<std::unique_ptr<GroupCorrection>> corr;  // per member (the leader's is empty)
-    int lanes_log2 = 0;
     vpmg::DBuf<float2> gsrc;
     cudaGraphExec_t exec = nullptr;
     long long launches = 0;
@@ -869,6 +868,11 @@ struct vpmg_batch {
   };
   std::vector<vpmg_handle*> hs;
   std::vector<std::unique_ptr<Unit>> units;
+  // replay order of the units within a step: 0 concurrent (each unit on its
+  // leader's stream), 1 one after another on one stream, -1 chosen by timing
+  // the first two steps of a call (one of each)
+  int schedule = -1;
+  float tuned_ms[2] = {0.f, 0.f};
   ~vpmg_batch() {
     for (auto& u : units)
       if (u->exec) cudaGraphExecDestroy(u->exec);
@@ -917,7 +921,7 @@ void capture_group(vpmg_batch* b, vpmg_batch::Unit& u, double dt, int do_remesh)
     for (int k = 0; k < n; ++k) H[k]->profile = prof[k];
     for (auto e : ev) cudaEventDestroy(e);
   };
-  const int lanes = 1 << u.lanes_log2;
+  const int lanes = n;
   cudaGraph_t g = nullptr;
   try {
     VPMG_CUDA(cudaStreamBeginCapture(ls, cudaStreamCaptureModeThreadLocal));
@@ -937,7 +941,7 @@ void capture_group(vpmg_batch* b, vpmg_batch::Unit& u, double dt, int do_remesh)
       }
       {
         LaunchScope sc(L);
-        boundary_group_apply(L->bo_bl, u.gsrc.p, n, u.lanes_log2, G, ls);
+        boundary_group_apply(L->bo_bl, u.gsrc.p, n, G, ls);
       }
       VPMG_CUDA(cudaEventRecord(ev[n], ls));
       for (int k = 1; k < n; ++k) VPMG_CUDA(cudaStreamWaitEvent(H[k]->stream, ev[n], 0));
@@ -978,7 +982,7 @@ void capture_group(vpmg_batch* b, vpmg_batch::Unit& u, double dt, int do_remesh)
 }
 }  // namespace
 
-int vpmg_batch_create(vpmg_handle* const* hs, int n, vpmg_batch** out) {
+int vpmg_batch_create(vpmg_handle* const* hs, int n, int flags, vpmg_batch** out) {
   if (!hs || n <= 0 || !out) return VPMG_ERR_ARG;
   *out = nullptr;
   for (int i = 0; i < n; ++i)
@@ -1016,9 +1020,19 @@ int vpmg_batch_create(vpmg_handle* const* hs, int n, vpmg_batch** out) {
     }
     for (auto& u : b->units) {
       if (u->m.size() < 2) continue;
-      while ((1 << u->lanes_log2) < (int)u->m.size()) ++u->lanes_log2;
+      if (flags & VPMG_BATCH_RELEASE_SHARED) {
+        for (size_t k = 1; k < u->m.size(); ++k) {
+          vpmg_handle* f = hs[u->m[k]];
+          if (f->graph.exec) {
+            cudaGraphExecDestroy(f->graph.exec);
+            f->graph.exec = nullptr;
+          }
+          vpmg::hx::destroy_adjoint(f);
+          boundary_release_recorded(f->bo_bl);
+        }
+      }
       const BoundaryOp& L = hs[u->m[0]]->bo_bl;
-      u->gsrc.ensure(4 * (size_t)L.ncell_total << u->lanes_log2);
+      u->gsrc.ensure(4 * (size_t)L.ncell_total * u->m.size());
       VPMG_CUDA(cudaMemsetAsync(u->gsrc.p, 0, u->gsrc.bytes(), hs[u->m[0]]->stream));
       VPMG_CUDA(cudaStreamSynchronize(hs[u->m[0]]->stream));
     }
@@ -1061,33 +1075,65 @@ int vpmg_batch_step(vpmg_batch* b, int nsteps, double dt, int do_remesh, double*
       VPMG_CUDA(cudaMemsetAsync(h->hist_counter.p, 0, sizeof(int), h->stream));
       VPMG_CUDA(cudaStreamSynchronize(h->stream));
     }
-    cudaEvent_t start, stop;
-    VPMG_CUDA(cudaEventCreate(&start));
-    VPMG_CUDA(cudaEventCreate(&stop));
     const size_t nu = b->units.size();
-    std::vector<cudaEvent_t> done(nu, nullptr);
+    std::vector<cudaEvent_t> mark((size_t)nsteps + 1, nullptr), done(nu, nullptr);
+    for (auto& e : mark) VPMG_CUDA(cudaEventCreate(&e));
     for (auto& e : done) VPMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     auto lead = [&](size_t i) { return b->hs[b->units[i]->m[0]]; };
-    VPMG_CUDA(cudaEventRecord(start, h0->stream));
-    for (size_t i = 0; i < nu; ++i)
-      if (lead(i)->stream != h0->stream) VPMG_CUDA(cudaStreamWaitEvent(lead(i)->stream, start, 0));
-    for (int k = 0; k < nsteps; ++k)
-      for (size_t i = 0; i < nu; ++i) {
-        const auto& u = *b->units[i];
-        cudaGraphExec_t ex = (u.m.size() == 1) ? lead(i)->graph.exec : u.exec;
-        VPMG_CUDA(cudaGraphLaunch(ex, lead(i)->stream));
+    auto exec_of = [&](size_t i) {
+      const auto& u = *b->units[i];
+      return (u.m.size() == 1) ? lead(i)->graph.exec : u.exec;
+    };
+    // one step of every unit, concurrent or in sequence, between two marks on h0's stream
+    auto step = [&](int k, int mode) {
+      if (mode == 1) {
+        for (size_t i = 0; i < nu; ++i) VPMG_CUDA(cudaGraphLaunch(exec_of(i), h0->stream));
+        VPMG_CUDA(cudaEventRecord(mark[k + 1], h0->stream));
+        return;
       }
-    for (size_t i = 0; i < nu; ++i) {
-      if (lead(i)->stream == h0->stream) continue;
-      VPMG_CUDA(cudaEventRecord(done[i], lead(i)->stream));
-      VPMG_CUDA(cudaStreamWaitEvent(h0->stream, done[i], 0));
+      for (size_t i = 0; i < nu; ++i)
+        if (lead(i)->stream != h0->stream) VPMG_CUDA(cudaStreamWaitEvent(lead(i)->stream, mark[k], 0));
+      for (size_t i = 0; i < nu; ++i) VPMG_CUDA(cudaGraphLaunch(exec_of(i), lead(i)->stream));
+      for (size_t i = 0; i < nu; ++i) {
+        if (lead(i)->stream == h0->stream) continue;
+        VPMG_CUDA(cudaEventRecord(done[i], lead(i)->stream));
+        VPMG_CUDA(cudaStreamWaitEvent(h0->stream, done[i], 0));
+      }
+      VPMG_CUDA(cudaEventRecord(mark[k + 1], h0->stream));
+    };
+    VPMG_CUDA(cudaEventRecord(mark[0], h0->stream));
+    int k0 = 0;
+    if (b->schedule < 0 && nsteps >= 2 && nu > 1) {
+      for (int m = 0; m < 2; ++m) {
+        step(m, m);
+        VPMG_CUDA(cudaEventSynchronize(mark[m + 1]));
+        VPMG_CUDA(cudaEventElapsedTime(&b->tuned_ms[m], mark[m], mark[m + 1]));
+      }
+      b->schedule = (b->tuned_ms[1] < b->tuned_ms[0]) ? 1 : 0;
+      k0 = 2;
     }
-    VPMG_CUDA(cudaEventRecord(stop, h0->stream));
-    VPMG_CUDA(cudaEventSynchronize(stop));
+    // the remaining steps: in sequence on h0's stream, or each unit running
+    // through them on its own stream (joined at the end)
+    if (b->schedule == 1) {
+      for (int k = k0; k < nsteps; ++k)
+        for (size_t i = 0; i < nu; ++i) VPMG_CUDA(cudaGraphLaunch(exec_of(i), h0->stream));
+      VPMG_CUDA(cudaEventRecord(mark[nsteps], h0->stream));
+    } else if (k0 < nsteps) {
+      for (size_t i = 0; i < nu; ++i)
+        if (lead(i)->stream != h0->stream) VPMG_CUDA(cudaStreamWaitEvent(lead(i)->stream, mark[k0], 0));
+      for (int k = k0; k < nsteps; ++k)
+        for (size_t i = 0; i < nu; ++i) VPMG_CUDA(cudaGraphLaunch(exec_of(i), lead(i)->stream));
+      for (size_t i = 0; i < nu; ++i) {
+        if (lead(i)->stream == h0->stream) continue;
+        VPMG_CUDA(cudaEventRecord(done[i], lead(i)->stream));
+        VPMG_CUDA(cudaStreamWaitEvent(h0->stream, done[i], 0));
+      }
+      VPMG_CUDA(cudaEventRecord(mark[nsteps], h0->stream));
+    }
+    VPMG_CUDA(cudaEventSynchronize(mark[nsteps]));
     float t = 0.f;
-    VPMG_CUDA(cudaEventElapsedTime(&t, start, stop));
-    cudaEventDestroy(start);
-    cudaEventDestroy(stop);
+    VPMG_CUDA(cudaEventElapsedTime(&t, mark[0], mark[nsteps]));
+    for (auto e : mark) cudaEventDestroy(e);
     for (auto e : done) cudaEventDestroy(e);
     long long ps = 0;
     for (size_t i = 0; i < nu; ++i) {
@@ -1104,6 +1150,22 @@ int vpmg_batch_step(vpmg_batch* b, int nsteps, double dt, int do_remesh, double*
     if (solves) *solves = (long long)b->hs.size() * nsteps;
     if (particle_steps) *particle_steps = ps;
   });
+}
+
+int vpmg_batch_set_schedule(vpmg_batch* b, int schedule) {
+  if (!b || schedule < -1 || schedule > 1) return VPMG_ERR_ARG;
+  b->schedule = schedule;
+  return VPMG_OK;
+}
+
+int vpmg_batch_get_schedule(const vpmg_batch* b, int* schedule, float tuned_ms[2]) {
+  if (!b) return VPMG_ERR_ARG;
+  if (schedule) *schedule = b->schedule;
+  if (tuned_ms) {
+    tuned_ms[0] = b->tuned_ms[0];
+    tuned_ms[1] = b->tuned_ms[1];
+  }
+  return VPMG_OK;
 }
 
 int vpmg_batch_destroy(vpmg_batch* b) {

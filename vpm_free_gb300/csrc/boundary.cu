@@ -411,22 +411,24 @@ __device__ __forceinline__ void ff_mac3(FF& a0, FF& a1, FF& a2, float2 w, const 
 // One recorded operator applied to the sources of up to kGroupMax problems
 // with the same index geometry (their weights differ by the factor of the
 // mesh spacing, folded into G.scale).  A warp per boundary node; lane
-// p + LG * grp serves problem p (LG = 2^lanes_log2 lanes per problem set)
-// and every NG-th interaction from grp, so the weight and cell id are read
-// once for all problems and the problems' source records of a cell are one
-// contiguous load.  The dense block (coarsest level) comes first, then the
-// row of the finer levels; the NG partial sums meet in a fixed shuffle tree.
-__global__ void __launch_bounds__(256) k_apply_group(const long long* __restrict__ rowptr, const int* __restrict__ col,
-                                                     const float2* __restrict__ wgt, const float2* __restrict__ wtop,
-                                                     int top0, int ntop, int ntop2, const float4* __restrict__ gsrc,
-                                                     const int* __restrict__ tgt_node, int ntarget, int nprob,
-                                                     int lanes_log2, GroupOut G) {
+// p + LG * grp serves problem p (LG = nprob lanes per problem set, NG =
+// 32 / LG sets) and every NG-th interaction from grp, so the weight and
+// cell id are read once for all problems and the problems' source records
+// of a cell are one contiguous load.  The dense block (coarsest level)
+// comes first, then the row of the finer levels; the NG partial sums are
+// added in set order.
+__global__ void __launch_bounds__(256) k_apply_group(const long long* __restrict__ rowptr,
+                                                        const int* __restrict__ col, const float2* __restrict__ wgt,
+                                                        const float2* __restrict__ wtop, int top0, int ntop, int ntop2,
+                                                        const float4* __restrict__ gsrc,
+                                                        const int* __restrict__ tgt_node, int ntarget, int nprob,
+                                                        GroupOut G) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
-  const int LG = 1 << lanes_log2, NG = 32 >> lanes_log2;
-  const int p = lane & (LG - 1), grp = lane >> lanes_log2;
-  const bool act = p < nprob;
+  const int LG = nprob, NG = 32 / nprob;
+  const int p = lane % LG, grp = lane / LG;
+  const bool act = grp < NG;
   const float4* sp = gsrc + 2 * (size_t)p;
   const size_t cstride = 2 * (size_t)LG;  // float4s per cell
   FF f0, f1, f2, g0, g1, g2;
@@ -463,12 +465,14 @@ __global__ void __launch_bounds__(256) k_apply_group(const long long* __restrict
   double a0 = ((double)f0.hi + (double)f0.lo) + ((double)g0.hi + (double)g0.lo);
   double a1 = ((double)f1.hi + (double)f1.lo) + ((double)g1.hi + (double)g1.lo);
   double a2 = ((double)f2.hi + (double)f2.lo) + ((double)g2.hi + (double)g2.lo);
-  for (int o = LG; o < 32; o <<= 1) {
-    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+  const double b0 = a0, b1 = a1, b2 = a2;
+  for (int g = 1; g < NG; ++g) {
+    const int src = min(p + g * LG, 31);
+    a0 += __shfl_sync(0xffffffffu, b0, src);
+    a1 += __shfl_sync(0xffffffffu, b1, src);
+    a2 += __shfl_sync(0xffffffffu, b2, src);
   }
-  if (grp == 0 && act) {
+  if (grp == 0) {
     const int node = tgt_node[warp];
     const double sc = G.scale[p];
     G.o[p][0][node] += a0 * sc;
@@ -977,6 +981,16 @@ bool boundary_group_match(const BoundaryOp& L, const Grid& gl, const BoundaryOp&
   return true;
 }
 
+void boundary_release_recorded(BoundaryOp& B) {
+  B.rowptr.release(); B.col.release(); B.w.release(); B.wtop.release(); B.dsum.release(); B.csrc_ff.release();
+  B.colptr.release(); B.trow.release(); B.tw.release(); B.vff.release(); B.dpart.release();
+  B.precomputed = false;
+  B.dense = false;
+  B.transposed = false;
+  B.nnz = 0;
+  B.ndense_acc = 0;
+}
+
 void boundary_group_correct(const BoundaryOp& F, const GroupCorrection& C, double* const sol[3], cudaStream_t s) {
   if (!C.nrows) return;
   k_apply_corr<<<(unsigned)(((long long)C.nrows * 32 + 255) / 256), 256, 0, s>>>(
@@ -993,14 +1007,13 @@ void boundary_group_sources(BoundaryOp& B, float2* gsrc, int slot, int lanes, cu
   VPMG_LAUNCHED();
 }
 
-void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, int lanes_log2, const GroupOut& G,
-                          cudaStream_t s) {
-  VPMG_CHECK(L.precomputed && nprob >= 1 && nprob <= kGroupMax && (1 << lanes_log2) >= nprob && lanes_log2 <= 5,
-             VPMG_ERR_STATE, "group apply: operator not recorded or group too large");
+void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, const GroupOut& G, cudaStream_t s) {
+  VPMG_CHECK(L.precomputed && nprob >= 1 && nprob <= kGroupMax, VPMG_ERR_STATE,
+             "group apply: operator not recorded or group too large");
   const long long threads = (long long)L.ntarget * 32;
   k_apply_group<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
       L.rowptr.p, L.col.p, L.w.p, L.dense ? L.wtop.p : nullptr, L.lev_off[L.levmax], L.ntopd, (L.ntopd + 1) / 2,
-      reinterpret_cast<const float4*>(gsrc), L.tgt_node.p, L.ntarget, nprob, lanes_log2, G);
+      reinterpret_cast<const float4*>(gsrc), L.tgt_node.p, L.ntarget, nprob, G);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }

@@ -177,7 +177,8 @@ void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp,
 void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStream_t s);
 // Problems that share one recorded operator (same index geometry, weights
 // in proportion to the mesh spacing): each problem's sources go to its slot
-// of an interleaved buffer [cell][slot][4] (float2), then one launch adds
+// of an interleaved buffer [cell][slot][4] (float2, nprob slots per cell),
+// then one launch adds
 // every problem's boundary values (o[p][c] at the target nodes, times scale[p]).
 constexpr int kGroupMax = 16;
 struct GroupOut {
@@ -201,9 +202,10 @@ struct GroupCorrection {
 bool boundary_group_match(const BoundaryOp& L, const Grid& gl, const BoundaryOp& F, const Grid& gf, double max_frac,
                           double* ratio, GroupCorrection& C, cudaStream_t s);
 void boundary_group_correct(const BoundaryOp& F, const GroupCorrection& C, double* const sol[3], cudaStream_t s);
+// Frees the recorded operator (and its transpose): applies walk the tree again.
+void boundary_release_recorded(BoundaryOp& B);
 void boundary_group_sources(BoundaryOp& B, float2* gsrc, int slot, int lanes, cudaStream_t s);
-void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, int lanes_log2, const GroupOut& G,
-                          cudaStream_t s);
+void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, const GroupOut& G, cudaStream_t s);
 // Transposes (one component): boundary-value adjoint (grid node array) ->
 // cell adjoints -> panel adjoints -> accumulated into the sol0 adjoint.
 void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s);
