@@ -255,16 +255,20 @@ __global__ void k_split(const double* __restrict__ x, int ncell, float2* __restr
 // block stages the cells' packed sources in shared memory a tile at a
 // time, so the warps read them as broadcasts.
 constexpr int kDenseTile = 512;  // cells per staged tile (16 KB of sources)
+// blockIdx.y = segment of cseg (even) cells; its partial sums go to
+// dsum[segment][component][node] (more, shorter warps: a fuller last wave).
 __global__ void __launch_bounds__(256) k_apply_dense(const float4* __restrict__ wtop, const float4* __restrict__ src,
-                                                     int top0, int ntop, int ntop2, int ntarget,
+                                                     int top0, int ntop, int ntop2, int ntarget, int cseg,
                                                      double* __restrict__ dsum) {
   __shared__ float4 ss[2 * kDenseTile];
   const int lane = threadIdx.x & 31;
   const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const bool active = g < (ntarget + 31) / 32;
+  const int cb = blockIdx.y * cseg, ce = min(ntop, cb + cseg);
+  dsum += (size_t)blockIdx.y * 3 * ntarget;
   FF f0, f1, f2, g0, g1, g2;
-  for (int c0 = 0; c0 < ntop; c0 += kDenseTile) {
-    const int nc = min(kDenseTile, ntop - c0);
+  for (int c0 = cb; c0 < ce; c0 += kDenseTile) {
+    const int nc = min(kDenseTile, ce - c0);
     __syncthreads();
     for (int i = threadIdx.x; i < 2 * nc; i += blockDim.x) ss[i] = __ldg(&src[2 * (size_t)(top0 + c0) + i]);
     __syncthreads();
@@ -319,7 +323,8 @@ __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__
                                                    const float2* __restrict__ wgt, const float4* __restrict__ src,
                                                    const int* __restrict__ tgt_node, int ntarget, double inv_pi4,
                                                    double* __restrict__ o0, double* __restrict__ o1,
-                                                   double* __restrict__ o2, const double* __restrict__ dsum) {
+                                                   double* __restrict__ o2, const double* __restrict__ dsum,
+                                                   int nseg) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
@@ -372,10 +377,11 @@ __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__
     a2 += __shfl_xor_sync(0xffffffffu, a2, o);
   }
   if (lane == 0) {
-    if (dsum) {
-      a0 += dsum[warp];
-      a1 += dsum[ntarget + warp];
-      a2 += dsum[2 * (size_t)ntarget + warp];
+    for (int q = 0; dsum && q < nseg; ++q) {
+      const double* d = dsum + (size_t)q * 3 * ntarget;
+      a0 += d[warp];
+      a1 += d[ntarget + warp];
+      a2 += d[2 * (size_t)ntarget + warp];
     }
     const int node = tgt_node[warp];
     o0[node] += -a0 * inv_pi4;
@@ -830,7 +836,16 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
         const size_t nw = (size_t)nchunk * ntop2 * 64;
         B.wtop.ensure(nw);
         VPMG_CUDA(cudaMemsetAsync(B.wtop.p, 0, sizeof(float2) * nw, s));  // opened cells weigh 0
-        B.dsum.ensure(3 * (size_t)B.ntarget);
+        // segments of the coarsest cells per 32-node chunk: at least three
+        // waves of warps (5 resident CTAs of 8 warps per SM), 64+ cells each
+        int dev = 0, sms = 0;
+        VPMG_CUDA(cudaGetDevice(&dev));
+        VPMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const long long slots = 40LL * sms;
+        int seg = 1;
+        while (seg < 8 && (long long)nchunk * seg < 3 * slots && B.ntopd / (2 * seg) >= 64) seg *= 2;
+        B.dseg = seg;
+        B.dsum.ensure(3 * (size_t)B.ntarget * seg);
       }
       k_walk<kFill><<<blocks, 128, 0, s>>>(W, nullptr, nullptr, nullptr, nullptr, B.rowptr.p, B.col.p, B.w.p,
                                            B.dense ? B.wtop.p : nullptr, nullptr);
@@ -856,6 +871,11 @@ void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp,
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
+
+// Coarsest cells per dense-block segment (even: cell pairs stay whole) and
+// the number of segments that covers them.
+static int dense_cseg(const BoundaryOp& B) { return (((B.ntopd + B.dseg - 1) / B.dseg) + 1) & ~1; }
+static int dense_nseg(const BoundaryOp& B) { return (B.ntopd + dense_cseg(B) - 1) / dense_cseg(B); }
 
 // Levels 1..levmax aggregate the level-0 panels (source_bound_lev).
 static void aggregate_levels(BoundaryOp& B, cudaStream_t s) {
@@ -883,15 +903,17 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
     const float4* src4 = reinterpret_cast<const float4*>(B.csrc_ff.p);
     if (B.dense) {
       const long long dthreads = (long long)((B.ntarget + 31) / 32) * 32;
-      k_apply_dense<<<(unsigned)((dthreads + 255) / 256), 256, 0, s>>>(
-          reinterpret_cast<const float4*>(B.wtop.p), src4, B.lev_off[B.levmax], B.ntopd, (B.ntopd + 1) / 2, B.ntarget,
-          B.dsum.p);
+      const int cseg = dense_cseg(B);
+      const dim3 grid((unsigned)((dthreads + 255) / 256), (unsigned)dense_nseg(B));
+      k_apply_dense<<<grid, 256, 0, s>>>(reinterpret_cast<const float4*>(B.wtop.p), src4, B.lev_off[B.levmax],
+                                         B.ntopd, (B.ntopd + 1) / 2, B.ntarget, cseg, B.dsum.p);
       VPMG_LAUNCHED();
     }
     const long long threads = (long long)B.ntarget * 32;
     k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, src4, B.tgt_node.p,
                                                                   B.ntarget, 1.0 / (4.0 * kPI), sol[0], sol[1],
-                                                                  sol[2], B.dense ? B.dsum.p : nullptr);
+                                                                  sol[2], B.dense ? B.dsum.p : nullptr,
+                                                                  B.dense ? dense_nseg(B) : 0);
   } else {
     const WalkDev W = walk_dev(B);
     k_walk<kAccum><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, sol[0], sol[1], sol[2], nullptr, nullptr, nullptr, nullptr);

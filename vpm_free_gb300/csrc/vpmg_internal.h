@@ -158,7 +158,8 @@ struct BoundaryOp {
   int ntopd = 0;                        // cells of the coarsest level
   long long ndense_acc = 0;             // accepted interactions in the block
   DBuf<float2> wtop;
-  DBuf<double> dsum;                    // 3 x ntarget partial sums of the block
+  int dseg = 1;                         // segments of the coarsest cells (k_apply_dense grid y)
+  DBuf<double> dsum;                    // [segment][3][ntarget] partial sums of the block
   DBuf<unsigned long long> dcount;
   // its transpose (CSR over cells, for the reverse mode), built on first use
   bool transposed = false;
