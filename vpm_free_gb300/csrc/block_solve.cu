@@ -185,24 +185,27 @@ __global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict_
     }
     return r;
   };
-  // loads four planes ahead of the dependent chain; same arithmetic order
+  // loads eight planes ahead of the dependent chain (one thread per line
+  // leaves few warps per SM: the loads in flight set the speed); same
+  // arithmetic order
+  constexpr int U = 8;
   double y = rhs(0);
   out[pq] = y;
   double ri = rinv(pq);
   int k = 1;
-  for (; k + 3 < m2; k += 4) {
+  for (; k + U - 1 < m2; k += U) {
     const size_t id = pq + plane * k;
-    const double q0 = rhs(k), q1 = rhs(k + 1), q2 = rhs(k + 2), q3 = rhs(k + 3);
-    const double r0 = rinv(id), r1 = rinv(id + plane), r2 = rinv(id + 2 * plane), r3 = rinv(id + 3 * plane);
-    y = fma(y, ri, q0);
-    out[id] = y;
-    y = fma(y, r0, q1);
-    out[id + plane] = y;
-    y = fma(y, r1, q2);
-    out[id + 2 * plane] = y;
-    y = fma(y, r2, q3);
-    out[id + 3 * plane] = y;
-    ri = r3;
+    double qv[U], rv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) qv[u] = rhs(k + u);
+#pragma unroll
+    for (int u = 0; u < U; ++u) rv[u] = rinv(id + plane * u);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      y = fma(y, u ? rv[u - 1] : ri, qv[u]);
+      out[id + plane * u] = y;
+    }
+    ri = rv[U - 1];
   }
   for (; k < m2; ++k) {
     const size_t id = pq + plane * k;
@@ -213,18 +216,18 @@ __global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict_
   double u = y * ri;
   out[pq + plane * (m2 - 1)] = u;
   k = m2 - 2;
-  for (; k - 3 >= 0; k -= 4) {
+  for (; k - (U - 1) >= 0; k -= U) {
     const size_t id = pq + plane * k;
-    const double o0 = out[id], o1 = out[id - plane], o2 = out[id - 2 * plane], o3 = out[id - 3 * plane];
-    const double r0 = rinv(id), r1 = rinv(id - plane), r2 = rinv(id - 2 * plane), r3 = rinv(id - 3 * plane);
-    u = (o0 + u) * r0;
-    out[id] = u;
-    u = (o1 + u) * r1;
-    out[id - plane] = u;
-    u = (o2 + u) * r2;
-    out[id - 2 * plane] = u;
-    u = (o3 + u) * r3;
-    out[id - 3 * plane] = u;
+    double ov[U], rv[U];
+#pragma unroll
+    for (int v = 0; v < U; ++v) ov[v] = out[id - plane * v];
+#pragma unroll
+    for (int v = 0; v < U; ++v) rv[v] = rinv(id - plane * v);
+#pragma unroll
+    for (int v = 0; v < U; ++v) {
+      u = (ov[v] + u) * rv[v];
+      out[id - plane * v] = u;
+    }
   }
   for (; k >= 0; --k) {
     const size_t id = pq + plane * k;
