@@ -201,6 +201,13 @@ int vpmg_run(vpmg_handle* h, int nsteps, double dt, const double uinf[3], int re
  * *particle_steps = sum over problems and steps of the particle count.   */
 int vpmg_batch_run(vpmg_handle* const* hs, int n, int nsteps, double dt, int remesh, double* ms,
                    long long* solves, long long* particle_steps);
+/* Host helper: the forward Euler of the reference's time loop
+ * (source/test.f90:104-117, FACDEF = 1) on host arrays, one pass:
+ *   XP(:,j) = XP(:,j) + (UP(:,j) + UINF) * dt,  QP(1:3,j) = QP(1:3,j) - GP(:,j) * dt
+ * for j < n (uinf may be NULL).  The compiled loop a Fortran host runs,
+ * for C and Python hosts; no GPU work.                                  */
+int vpmg_host_euler(double* xp, double* qp, const double* up, const double* gp, int n, double dt,
+                    const double uinf[3]);
 /* Batch object: the same n problems, grouped at creation by shared
  * boundary operator.  Single-block problems (ibctyp 2) whose fine-block
  * operators agree up to the mesh-spacing factor (same index geometry and

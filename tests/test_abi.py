@@ -77,3 +77,24 @@ def test_no_gpu_means_error_not_abort(gpulib):
         pass
     with pytest.raises(gpulib.VPMError):
         gpulib.VPM(gpulib.VPMConfig.make(dpm=(0.1, 0.1, 0.1), box=(0, 0, 0, 0.8, 0.8, 0.8)))
+
+
+def test_host_euler_is_the_reference_update(gpulib):
+    """vpmg_host_euler (host only) against the test.f90:104-117 update
+    written out in numpy: XP += (UP + UINF) dt, QP[:, :3] -= GP dt, rows
+    past n untouched."""
+    import numpy as np
+    V = gpulib
+    rng = np.random.default_rng(5)
+    n, rows, dt, uinf = 1000, 1200, 0.005, (0.3, -0.1, 0.2)
+    XP, QP = rng.normal(size=(rows, 3)), rng.normal(size=(rows, 4))
+    UP, GP = rng.normal(size=(rows, 3)), rng.normal(size=(rows, 3))
+    x0, q0 = XP.copy(), QP.copy()
+    V.VPM.host_euler(XP, QP, UP, GP, n, dt, uinf)
+    ex = x0.copy()
+    ex[:n] = x0[:n] + (UP[:n] + np.array(uinf)) * dt
+    eq = q0.copy()
+    eq[:n, :3] = q0[:n, :3] - GP[:n] * dt
+    assert np.array_equal(XP, ex) and np.array_equal(QP, eq)
+    with pytest.raises(ValueError):
+        V.VPM.host_euler(XP, QP, UP, GP, rows + 1, dt)

@@ -40,7 +40,7 @@ EXPORTS = [
     "vpmg_read_particles_bin", "vpmg_write_particles_bin", "vpmg_write_solution", "vpmg_write_hist", "vpmg_set_output",
     "vpmg_dst_tiles", "vpmg_apply_poisson", "vpmg_adjoint_poisson", "vpmg_vjp_fields", "vpmg_vjp_remesh", "vpmg_adjoint_loss",
     "vpmg_adjoint_run", "vpmg_batch_create", "vpmg_batch_info", "vpmg_batch_step", "vpmg_batch_destroy",
-    "vpmg_batch_set_schedule", "vpmg_batch_get_schedule",
+    "vpmg_batch_set_schedule", "vpmg_batch_get_schedule", "vpmg_host_euler",
 ]
 
 
@@ -139,6 +139,7 @@ def load_library():
     L.vpmg_batch_step.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, _dp, C.POINTER(C.c_longlong),
                                   C.POINTER(C.c_longlong)]
     L.vpmg_batch_destroy.argtypes = [C.c_void_p]
+    L.vpmg_host_euler.argtypes = [_dp, _dp, _dp, _dp, C.c_int, C.c_double, _dp]
     L.vpmg_batch_set_schedule.argtypes = [C.c_void_p, C.c_int]
     L.vpmg_batch_get_schedule.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     L.vpmg_read_particles_bin.argtypes = [C.c_char_p, C.POINTER(C.c_int), _dp, _dp, _dp, C.c_int]
@@ -273,6 +274,18 @@ class VPM:
         n = C.c_int(XP.shape[0])
         self._chk(self._L.vpmg_remesh_particles_3d(self._h, iflag, _p(xb), _p(qb), C.byref(n), cap))
         return xb[:n.value].copy(), qb[:n.value].copy()
+
+    @staticmethod
+    def host_euler(XP, QP, UP, GP, n, dt, uinf=None):
+        """Forward Euler of the reference's time loop (test.f90:104-117) on
+        host arrays in one compiled pass: XP += (UP + uinf) dt, QP[:, :3] -= GP dt."""
+        for a, c in ((XP, 3), (QP, 4), (UP, 3), (GP, 3)):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape[1] != c or a.shape[0] < n:
+                raise ValueError("host_euler wants C-contiguous float64 (>= n, 3/4) arrays")
+        u = (C.c_double * 3)(*uinf) if uinf is not None else None
+        rc = load_library().vpmg_host_euler(_p(XP), _p(QP), _p(UP), _p(GP), int(n), float(dt), u)
+        if rc != 0:
+            raise ValueError("vpmg_host_euler: bad arguments")
 
     def remesh_in_place(self, XP, QP, n, iflag=1):
         """remesh_particles_3d(iflag) on caller-owned arrays of NVRM rows, as a

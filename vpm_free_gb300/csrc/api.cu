@@ -1234,6 +1234,25 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
   });
 }
 
+int vpmg_host_euler(double* xp, double* qp, const double* up, const double* gp, int n, double dt,
+                    const double uinf[3]) {
+  if (n < 0 || (n > 0 && (!xp || !qp || !up || !gp))) return VPMG_ERR_ARG;
+  const double u0 = uinf ? uinf[0] : 0.0, u1 = uinf ? uinf[1] : 0.0, u2 = uinf ? uinf[2] : 0.0;
+  for (int j = 0; j < n; ++j) {
+    double* x = xp + 3 * (size_t)j;
+    double* q = qp + 4 * (size_t)j;
+    const double* u = up + 3 * (size_t)j;
+    const double* g = gp + 3 * (size_t)j;
+    x[0] = x[0] + (u[0] + u0) * dt;
+    x[1] = x[1] + (u[1] + u1) * dt;
+    x[2] = x[2] + (u[2] + u2) * dt;
+    q[0] = q[0] - g[0] * dt;
+    q[1] = q[1] - g[1] * dt;
+    q[2] = q[2] - g[2] * dt;
+  }
+  return VPMG_OK;
+}
+
 int vpmg_remesh_device(vpmg_handle* h) {
   return guarded(h, [&] {
     VPMG_CHECK(h->prepared, VPMG_ERR_STATE, "define_sizes must come first");
