@@ -861,6 +861,7 @@ struct vpmg_batch {
     std::vector<double> ratio;
     std::vector<std::unique_ptr<GroupCorrection>> corr;  // per member (the leader's is empty)
     vpmg::DBuf<float2> gsrc;
+    vpmg::DBuf<double> part;  // the dense block's partial sums per problem
     cudaGraphExec_t exec = nullptr;
     long long launches = 0;
     double dt = 0.0;
@@ -941,7 +942,7 @@ void capture_group(vpmg_batch* b, vpmg_batch::Unit& u, double dt, int do_remesh)
       }
       {
         LaunchScope sc(L);
-        boundary_group_apply(L->bo_bl, u.gsrc.p, n, G, ls);
+        boundary_group_apply(L->bo_bl, u.gsrc.p, n, u.part.p, G, ls);
       }
       VPMG_CUDA(cudaEventRecord(ev[n], ls));
       for (int k = 1; k < n; ++k) VPMG_CUDA(cudaStreamWaitEvent(H[k]->stream, ev[n], 0));
@@ -1033,6 +1034,8 @@ int vpmg_batch_create(vpmg_handle* const* hs, int n, int flags, vpmg_batch** out
       }
       const BoundaryOp& L = hs[u->m[0]]->bo_bl;
       u->gsrc.ensure(4 * (size_t)L.ncell_total * u->m.size());
+      const size_t np = boundary_group_partial_count(L, (int)u->m.size());
+      if (np) u->part.ensure(np);
       VPMG_CUDA(cudaMemsetAsync(u->gsrc.p, 0, u->gsrc.bytes(), hs[u->m[0]]->stream));
       VPMG_CUDA(cudaStreamSynchronize(hs[u->m[0]]->stream));
     }

@@ -414,21 +414,85 @@ __device__ __forceinline__ void ff_mac3(FF& a0, FF& a1, FF& a2, float2 w, const 
   ff_mac(a2, w, make_float2(z.x, z.y));
 }
 
+// The dense block (coarsest level) of a shared operator against a group's
+// sources: a register-tiled product.  Lane = boundary node of a 32-node
+// chunk (its weights are one coalesced row), warp = a quad of problems
+// (4 problems x 3 components of float-float accumulators), CTA = 8 warps
+// over 8 / nquad chunks; a tile of kGroupTile cells of every problem's
+// sources is staged in shared memory and read as broadcasts.  Each weight
+// feeds twelve independent float-float chains.  blockIdx.y = segment of
+// the coarsest cells; partial sums go to part[segment][problem][comp][node].
+constexpr int kGroupTile = 64;
+__global__ void __launch_bounds__(256) k_group_dense(const float4* __restrict__ wtop, const float4* __restrict__ gsrc,
+                                                     int top0, int ntop, int ntop2, int ntarget, int nprob, int nquad,
+                                                     int cseg, double* __restrict__ part) {
+  extern __shared__ float4 gs[];  // [cell][problem][2]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int per = 8 / nquad;  // chunks per CTA
+  const int q = wid % nquad;  // problem quad
+  const int chunk = blockIdx.x * per + wid / nquad;
+  const bool active = chunk < (ntarget + 31) / 32 && wid < per * nquad;
+  const int p0 = 4 * q;
+  const int np = active ? max(0, min(4, nprob - p0)) : 0;
+  const int cb = blockIdx.y * cseg, ce = min(ntop, cb + cseg);
+  FF a[4][3];
+  for (int c0 = cb; c0 < ce; c0 += kGroupTile) {
+    const int nc = min(kGroupTile, ce - c0);
+    __syncthreads();
+    const float4* src = gsrc + 2 * (size_t)(top0 + c0) * nprob;
+    for (int i = threadIdx.x; i < 2 * nc * nprob; i += blockDim.x) gs[i] = __ldg(&src[i]);
+    __syncthreads();
+    if (!np) continue;
+    const float4* wp = wtop + ((size_t)chunk * ntop2 + (c0 >> 1)) * 32 + lane;
+    for (int c = 0; c < nc; c += 2) {
+      const float4 w = __ldg(&wp[(size_t)(c >> 1) * 32]);
+      const float2 wa = make_float2(w.x, w.y), wb = make_float2(w.z, w.w);
+      const bool two = c + 1 < nc;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (j < np) {
+          const float4* r = gs + 2 * ((size_t)c * nprob + p0 + j);
+          const float4 x = r[0], z = r[1];
+          ff_mac(a[j][0], wa, make_float2(x.x, x.y));
+          ff_mac(a[j][1], wa, make_float2(x.z, x.w));
+          ff_mac(a[j][2], wa, make_float2(z.x, z.y));
+          if (two) {
+            const float4* r2 = r + 2 * nprob;
+            const float4 x2 = r2[0], z2 = r2[1];
+            ff_mac(a[j][0], wb, make_float2(x2.x, x2.y));
+            ff_mac(a[j][1], wb, make_float2(x2.z, x2.w));
+            ff_mac(a[j][2], wb, make_float2(z2.x, z2.y));
+          }
+        }
+      }
+    }
+  }
+  const int t = chunk * 32 + lane;
+  if (!np || t >= ntarget) return;
+  double* out = part + (size_t)blockIdx.y * nprob * 3 * ntarget;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    if (j < np) {
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc)
+        out[((size_t)(p0 + j) * 3 + cc) * ntarget + t] = (double)a[j][cc].hi + (double)a[j][cc].lo;
+    }
+  }
+}
+
 // One recorded operator applied to the sources of up to kGroupMax problems
 // with the same index geometry (their weights differ by the factor of the
 // mesh spacing, folded into G.scale).  A warp per boundary node; lane
 // p + LG * grp serves problem p (LG = nprob lanes per problem set, NG =
 // 32 / LG sets) and every NG-th interaction from grp, so the weight and
 // cell id are read once for all problems and the problems' source records
-// of a cell are one contiguous load.  The dense block (coarsest level)
-// comes first, then the row of the finer levels; the NG partial sums are
-// added in set order.
-__global__ void __launch_bounds__(256) k_apply_group(const long long* __restrict__ rowptr,
-                                                        const int* __restrict__ col, const float2* __restrict__ wgt,
-                                                        const float2* __restrict__ wtop, int top0, int ntop, int ntop2,
-                                                        const float4* __restrict__ gsrc,
-                                                        const int* __restrict__ tgt_node, int ntarget, int nprob,
-                                                        GroupOut G) {
+// of a cell are one contiguous load.  The row holds the finer levels; the
+// NG partial sums are added in set order, then the dense block's partial
+// sums (k_group_dense) in segment order.
+__global__ void __launch_bounds__(256) k_apply_group(const long long* __restrict__ rowptr, const int* __restrict__ col,
+                                                     const float2* __restrict__ wgt, const float4* __restrict__ gsrc,
+                                                     const int* __restrict__ tgt_node, int ntarget, int nprob,
+                                                     const double* __restrict__ part, int nseg, GroupOut G) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
@@ -438,18 +502,6 @@ __global__ void __launch_bounds__(256) k_apply_group(const long long* __restrict
   const float4* sp = gsrc + 2 * (size_t)p;
   const size_t cstride = 2 * (size_t)LG;  // float4s per cell
   FF f0, f1, f2, g0, g1, g2;
-  if (wtop && act) {
-    const float2* wrow = wtop + (size_t)(warp >> 5) * ntop2 * 64 + (warp & 31) * 2;
-    int c = grp;
-    for (; c + NG < ntop; c += 2 * NG) {
-      const int c2 = c + NG;
-      const float2 wa = __ldg(&wrow[(size_t)(c >> 1) * 64 + (c & 1)]);
-      const float2 wb = __ldg(&wrow[(size_t)(c2 >> 1) * 64 + (c2 & 1)]);
-      ff_mac3(f0, f1, f2, wa, sp + (size_t)(top0 + c) * cstride);
-      ff_mac3(g0, g1, g2, wb, sp + (size_t)(top0 + c2) * cstride);
-    }
-    if (c < ntop) ff_mac3(f0, f1, f2, __ldg(&wrow[(size_t)(c >> 1) * 64 + (c & 1)]), sp + (size_t)(top0 + c) * cstride);
-  }
   const long long b = rowptr[warp], e = rowptr[warp + 1];
   if (act) {
     long long k = b + grp;
@@ -479,6 +531,13 @@ __global__ void __launch_bounds__(256) k_apply_group(const long long* __restrict
     a2 += __shfl_sync(0xffffffffu, b2, src);
   }
   if (grp == 0) {
+#pragma unroll 1
+    for (int q = 0; part && q < nseg; ++q) {  // the dense block's partial sums, in segment order
+      const double* d = part + ((size_t)q * nprob + p) * 3 * ntarget;
+      a0 += d[warp];
+      a1 += d[ntarget + warp];
+      a2 += d[2 * (size_t)ntarget + warp];
+    }
     const int node = tgt_node[warp];
     const double sc = G.scale[p];
     G.o[p][0][node] += a0 * sc;
@@ -1029,13 +1088,47 @@ void boundary_group_sources(BoundaryOp& B, float2* gsrc, int slot, int lanes, cu
   VPMG_LAUNCHED();
 }
 
-void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, const GroupOut& G, cudaStream_t s) {
+// Segments of the coarsest cells for k_group_dense: at least three waves of
+// CTAs (5 per SM), 64+ cells each; the same split at set-up and per step.
+static int group_dense_cseg(const BoundaryOp& L, int nprob) {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int nquad = nprob > 8 ? 4 : (nprob > 4 ? 2 : 1);
+  const long long ctas = ((L.ntarget + 31) / 32 + 8 / nquad - 1) / (8 / nquad);
+  int seg = 1;
+  while (seg < 8 && ctas * seg < 15LL * sms && L.ntopd / (2 * seg) >= 64) seg *= 2;
+  return (((L.ntopd + seg - 1) / seg) + 1) & ~1;
+}
+
+size_t boundary_group_partial_count(const BoundaryOp& L, int nprob) {
+  if (!L.dense) return 0;
+  const int cseg = group_dense_cseg(L, nprob);
+  const size_t nseg = (size_t)((L.ntopd + cseg - 1) / cseg);
+  return nseg * nprob * 3 * (size_t)L.ntarget;
+}
+
+void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, double* part, const GroupOut& G,
+                          cudaStream_t s) {
   VPMG_CHECK(L.precomputed && nprob >= 1 && nprob <= kGroupMax, VPMG_ERR_STATE,
              "group apply: operator not recorded or group too large");
+  int nseg = 0;
+  if (L.dense) {
+    VPMG_CHECK(part, VPMG_ERR_STATE, "group apply: no buffer for the dense block's partial sums");
+    const int nquad = nprob > 8 ? 4 : (nprob > 4 ? 2 : 1);
+    const int cseg = group_dense_cseg(L, nprob);
+    nseg = (L.ntopd + cseg - 1) / cseg;
+    const int per = 8 / nquad;
+    const dim3 grid((unsigned)(((L.ntarget + 31) / 32 + per - 1) / per), (unsigned)nseg);
+    const size_t smem = sizeof(float4) * 2 * kGroupTile * nprob;
+    k_group_dense<<<grid, 256, smem, s>>>(reinterpret_cast<const float4*>(L.wtop.p),
+                                          reinterpret_cast<const float4*>(gsrc), L.lev_off[L.levmax], L.ntopd,
+                                          (L.ntopd + 1) / 2, L.ntarget, nprob, nquad, cseg, part);
+    VPMG_LAUNCHED();
+  }
   const long long threads = (long long)L.ntarget * 32;
   k_apply_group<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
-      L.rowptr.p, L.col.p, L.w.p, L.dense ? L.wtop.p : nullptr, L.lev_off[L.levmax], L.ntopd, (L.ntopd + 1) / 2,
-      reinterpret_cast<const float4*>(gsrc), L.tgt_node.p, L.ntarget, nprob, G);
+      L.rowptr.p, L.col.p, L.w.p, reinterpret_cast<const float4*>(gsrc), L.tgt_node.p, L.ntarget, nprob, part, nseg,
+      G);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }

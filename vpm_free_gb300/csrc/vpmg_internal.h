@@ -206,7 +206,10 @@ void boundary_group_correct(const BoundaryOp& F, const GroupCorrection& C, doubl
 // Frees the recorded operator (and its transpose): applies walk the tree again.
 void boundary_release_recorded(BoundaryOp& B);
 void boundary_group_sources(BoundaryOp& B, float2* gsrc, int slot, int lanes, cudaStream_t s);
-void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, const GroupOut& G, cudaStream_t s);
+// doubles of the dense block's partial sums for a group of nprob problems
+size_t boundary_group_partial_count(const BoundaryOp& L, int nprob);
+void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, double* part, const GroupOut& G,
+                          cudaStream_t s);
 // Transposes (one component): boundary-value adjoint (grid node array) ->
 // cell adjoints -> panel adjoints -> accumulated into the sol0 adjoint.
 void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s);
