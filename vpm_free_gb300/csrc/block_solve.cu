@@ -54,21 +54,40 @@ __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W,
     tile[t] = v;
   }
   __syncthreads();
-  for (int o = threadIdx.x; o < kLines * nsel; o += blockDim.x) {
+  // R adjacent threads share one dot product (R = 128 / outputs, a power of
+  // two up to 8, when the CTA has fewer outputs than threads), each summing
+  // every R-th term; their partials meet in a fixed shuffle tree.
+  const int nout = kLines * nsel;
+  int R = 1;
+  while (R < 8 && nout * R * 2 <= (int)blockDim.x) R *= 2;
+  const int r = threadIdx.x % R;
+  for (int o0 = 0; o0 < nout; o0 += blockDim.x / R) {
+    const int o = o0 + threadIdx.x / R;
     const int li = o % kLines, i = o / kLines;
     const int l = l0 + li;
-    if (l >= nlines) continue;
-    const float2* a = tile + (size_t)li * m0;
-    const float2* b = Ss + (size_t)i * m0;
-    float2 a0 = make_float2(0.0f, 0.0f), a1 = a0;
-    int p = 0;
-    for (; p + 1 < m0; p += 2) {
-      a0 = ff::fma(a[p], b[p], a0);
-      a1 = ff::fma(a[p + 1], b[p + 1], a1);
+    const bool ok = o < nout && l < nlines;
+    float2 a0 = make_float2(0.0f, 0.0f), a1 = a0, a2 = a0, a3 = a0;
+    if (ok) {
+      const float2* a = tile + (size_t)li * m0;
+      const float2* b = Ss + (size_t)i * m0;
+      int p = r;
+      for (; p + 3 * R < m0; p += 4 * R) {
+        a0 = ff::fma(a[p], b[p], a0);
+        a1 = ff::fma(a[p + R], b[p + R], a1);
+        a2 = ff::fma(a[p + 2 * R], b[p + 2 * R], a2);
+        a3 = ff::fma(a[p + 3 * R], b[p + 3 * R], a3);
+      }
+      for (; p < m0; p += R) a0 = ff::fma(a[p], b[p], a0);
     }
-    if (p < m0) a0 = ff::fma(a[p], b[p], a0);
-    const int q = l % m1, kk = l / m1;
-    out[i + (size_t)nsel * (q + (size_t)m1 * kk)] = ff::to_double(ff::add(a0, a1));
+    float2 v = ff::add(ff::add(a0, a1), ff::add(a2, a3));
+    for (int m = 1; m < R; m <<= 1) {
+      const float2 w = make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+      v = (r & m) ? ff::add(w, v) : ff::add(v, w);
+    }
+    if (ok && r == 0) {
+      const int q = l % m1, kk = l / m1;
+      out[i + (size_t)nsel * (q + (size_t)m1 * kk)] = ff::to_double(v);
+    }
   }
 }
 
@@ -83,7 +102,7 @@ __global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W,
                                                    const int* __restrict__ klist, const float2* __restrict__ S,
                                                    int nsel, double* __restrict__ out, const float2* __restrict__ S2,
                                                    int nsel2, double* __restrict__ out2) {
-  extern __shared__ float2 tile[];  // [q][lane], m1 x kColTile
+  extern __shared__ float2 tile[];  // [q][lane], m1 x kColTile; then the partial sums [row][lane]
   const int p0 = blockIdx.x * kColTile;
   const int kk = blockIdx.y;
   const int k = klist ? klist[kk] : kk;
@@ -93,23 +112,44 @@ __global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W,
   for (int q = row; q < m1; q += rows)
     tile[q * kColTile + lane] = (p < m0) ? ff::split(plane[(size_t)m0 * q + p]) : make_float2(0.0f, 0.0f);
   __syncthreads();
-  if (p >= m0) return;
-  for (int jj = row; jj < nsel + nsel2; jj += rows) {
-    const bool second = jj >= nsel;
-    const int j = second ? jj - nsel : jj;
-    const float2* Sj = (second ? S2 : S) + (size_t)j * m1;
+  // R rows share one output row set when there are fewer outputs than rows
+  // (R a power of two), each summing every R-th q; the partials are added
+  // in row order through shared memory.
+  const int nout = nsel + nsel2;
+  int R = 1;
+  while (R < rows && nout * R * 2 <= rows) R *= 2;
+  const int r = row % R;
+  float2* partial = tile + (size_t)m1 * kColTile;
+  for (int j0 = 0; j0 < nout; j0 += rows / R) {
+    const int jj = j0 + row / R;
     float2 a0 = make_float2(0.0f, 0.0f), a1 = a0, a2 = a0, a3 = a0;
-    int q = 0;
-    for (; q + 3 < m1; q += 4) {
-      a0 = ff::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
-      a1 = ff::fma(__ldg(&Sj[q + 1]), tile[(q + 1) * kColTile + lane], a1);
-      a2 = ff::fma(__ldg(&Sj[q + 2]), tile[(q + 2) * kColTile + lane], a2);
-      a3 = ff::fma(__ldg(&Sj[q + 3]), tile[(q + 3) * kColTile + lane], a3);
+    if (jj < nout && p < m0) {
+      const bool second = jj >= nsel;
+      const int j = second ? jj - nsel : jj;
+      const float2* Sj = (second ? S2 : S) + (size_t)j * m1;
+      int q = r;
+      for (; q + 3 * R < m1; q += 4 * R) {
+        a0 = ff::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
+        a1 = ff::fma(__ldg(&Sj[q + R]), tile[(q + R) * kColTile + lane], a1);
+        a2 = ff::fma(__ldg(&Sj[q + 2 * R]), tile[(q + 2 * R) * kColTile + lane], a2);
+        a3 = ff::fma(__ldg(&Sj[q + 3 * R]), tile[(q + 3 * R) * kColTile + lane], a3);
+      }
+      for (; q < m1; q += R) a0 = ff::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
     }
-    for (; q < m1; ++q) a0 = ff::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
-    const double v = ff::to_double(ff::add(ff::add(a0, a1), ff::add(a2, a3)));
-    if (second) out2[(size_t)p + (size_t)m0 * (j + (size_t)nsel2 * kk)] = v;
-    else out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = v;
+    float2 v = ff::add(ff::add(a0, a1), ff::add(a2, a3));
+    if (R > 1) {
+      partial[row * kColTile + lane] = v;
+      __syncthreads();
+      if (r == 0)
+        for (int m = 1; m < R; ++m) v = ff::add(v, partial[(row + m) * kColTile + lane]);
+      __syncthreads();
+    }
+    if (r == 0 && jj < nout && p < m0) {
+      const bool second = jj >= nsel;
+      const int j = second ? jj - nsel : jj;
+      if (second) out2[(size_t)p + (size_t)m0 * (j + (size_t)nsel2 * kk)] = ff::to_double(v);
+      else out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = ff::to_double(v);
+    }
   }
 }
 
@@ -286,7 +326,7 @@ void partial_x(const double* W, int m0, int m1, int nk, const int* klist, const 
 size_t g_partial_y_smem = 0;  // dynamic shared memory granted to k_partial_y so far
 
 void partial_y_reserve(int m1) {
-  const size_t sm = sizeof(float2) * (size_t)m1 * kColTile;
+  const size_t sm = sizeof(float2) * ((size_t)m1 + 8) * kColTile;
   VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
   if (sm > g_partial_y_smem) {
     VPMG_CUDA(cudaFuncSetAttribute(k_partial_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -296,7 +336,7 @@ void partial_y_reserve(int m1) {
 
 void partial_y(const double* W, int m0, int m1, int nk, const int* klist, const float2* S, int nsel, double* out,
                cudaStream_t s, const float2* S2 = nullptr, int nsel2 = 0, double* out2 = nullptr) {
-  const size_t sm = sizeof(float2) * (size_t)m1 * kColTile;
+  const size_t sm = sizeof(float2) * ((size_t)m1 + 8) * kColTile;  // tile + partial sums of 8 rows
   VPMG_CHECK(sm <= g_partial_y_smem, VPMG_ERR_STATE, "k_partial_y shared memory not reserved");
   dim3 g((m0 + kColTile - 1) / kColTile, nk);
   k_partial_y<<<g, 256, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out, S2, nsel2, out2);
