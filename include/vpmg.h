@@ -5,7 +5,11 @@
  * `vpm(...)` driver call, pm.inp and particle arrays, and binds these entry
  * points through iso_c_binding (see vpm_free_gb300/fortran/).  Plain C
  * types only; every call returns an int status (0 = OK, < 0 = error, see
- * vpmg_status) and never aborts the process.  All arithmetic is FP64.
+ * vpmg_status) and never aborts the process.  Arrays are FP64; the heavy
+ * kernels (boundary operator, DST solves, projection weights, deposition,
+ * mesh-to-particle) compute in float-float arithmetic (about 48 significant
+ * bits) on the FP32 pipes, the rest in FP64; fields match an FP64 CPU
+ * restatement to relative L2 <= 1e-10.
  *
  * Array conventions follow the reference (Fortran column-major):
  *   XP(3,NVRM)  positions            -> double xp[ld*3], xp[3*p + d]
