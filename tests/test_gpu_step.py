@@ -211,6 +211,30 @@ def test_shared_operator_batch_equals_individual_runs(gpulib):
         h.close()
 
 
+@pytest.mark.parametrize("count", [6, 9])
+def test_large_batch_groups_equal_individual_runs(gpulib, count):
+    """Groups of 6 and 9 problems: two and three problem quads per warp set
+    in the dense-block kernel, 5 and 3 lane sets in the row kernel (2 and 5
+    idle lanes); every member reproduces its individual run."""
+    V = gpulib
+    names = ["ring32"] * count
+    solo = []
+    for h, _, _, w in _batch_problems(V, names):
+        h.run(2, 0.01)
+        solo.append(h.get_particles())
+        h.close()
+    hp = _batch_problems(V, names)
+    hs = [t[0] for t in hp]
+    with V.Batch(hs, release_shared=True) as b:
+        assert b.info() == (1, count)
+        b.run(2, 0.01)
+    for h, (x0, q0) in zip(hs, solo):
+        x1, q1 = h.get_particles()
+        assert x1.shape == x0.shape
+        assert rel_l2(x1, x0) <= 1e-12 and rel_l2(q1, q0) <= 1e-11
+        h.close()
+
+
 def test_shared_operator_batch_fields_match_oracle(gpulib, oracle):
     """One batched step of a two-problem group: the resident vector
     potential and velocity of each member against the oracle's step on the
