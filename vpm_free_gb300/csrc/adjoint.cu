@@ -776,8 +776,8 @@ void backward_step(vpmg_handle* h, double dt) {
   copy_ckpt(h, 1);
   forward_fields(h);
   {
-    const double* V[3] = {h->vel.p, h->vel.p + N, h->vel.p + 2 * N};
-    const double* G[3] = {h->def.p, h->def.p + N, h->def.p + 2 * N};
+    const float2* V[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
+    const float2* G[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
     const double u0[3] = {0.0, 0.0, 0.0};
     m2p(P, mg, h->bins, V, G, true, false, dt, u0, st);
   }
@@ -836,8 +836,8 @@ void step_masked(vpmg_handle* h, double dt, const int* mask) {
   const size_t N = h->gglob.count();
   Particles& P = h->parts;
   forward_fields(h);
-  const double* V[3] = {h->vel.p, h->vel.p + N, h->vel.p + 2 * N};
-  const double* G[3] = {h->def.p, h->def.p + N, h->def.p + 2 * N};
+  const float2* V[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
+  const float2* G[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
   const double u0[3] = {0.0, 0.0, 0.0};
   m2p(P, hx::mesh_dev(h->gglob, 4), h->bins, V, G, true, true, dt, u0, st);
   const Grid gr = hx::remesh_grid(h);

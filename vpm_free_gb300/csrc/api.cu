@@ -139,6 +139,9 @@ void prepare(vpmg_handle* h) {
   h->nblk = h->nb3[0] * h->nb3[1] * h->nb3[2];
   const size_t B = (size_t)h->nblk;
   h->rhs.ensure(3 * N); h->sol.ensure(3 * N); h->vel.ensure(3 * N); h->def.ensure(3 * N);
+  h->vel_ff.ensure(3 * N); h->def_ff.ensure(3 * N);
+  VPMG_CUDA(cudaMemsetAsync(h->vel_ff.p, 0, h->vel_ff.bytes(), h->stream));
+  VPMG_CUDA(cudaMemsetAsync(h->def_ff.p, 0, h->def_ff.bytes(), h->stream));
   h->rhs_bl.ensure(B * 3 * NB); h->sol_bl.ensure(B * 3 * NB); h->sol0.ensure(NB);
   h->samp.ensure(B * 3 * NC); h->crhs.ensure(3 * NC); h->csol.ensure(3 * NC); h->csol0.ensure(NC);
   h->sampsum.ensure(3 * NC);
@@ -364,7 +367,9 @@ void field_velocity(vpmg_handle* h) {
   // calc_velocity_serial_3d(1)
   double* V[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
   double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
-  velocity_and_stretching(s.nn, s.dpm, S, R, V, G, st);
+  float2* VF[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
+  float2* GF[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
+  velocity_and_stretching(s.nn, s.dpm, S, R, V, G, st, 3, VF, GF);
   ev_mark(h, 7);
 }
 
@@ -374,11 +379,13 @@ void field_step(vpmg_handle* h) {
   field_velocity(h);
 }
 
+// back_to_particles_3D(1) from the float-float copies of the velocity and
+// stretching (written with them by velocity_and_stretching).
 void m2p_step(vpmg_handle* h, bool write_up, bool euler, double dt, const double uinf[3]) {
   const size_t N = h->gglob.count();
   const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
-  const double* V[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
-  const double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
+  const float2* V[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
+  const float2* G[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
   m2p(h->parts, mg, h->bins, V, G, write_up, euler, dt, uinf, h->stream);
   ev_mark(h, 8);
 }
@@ -1378,12 +1385,14 @@ int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int
       double* Vv[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
       double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
       deposit(h->parts, mg, h->bins, R, h->stream);
+      float2* VF[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
+      float2* GF[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
       if (whattodo == 1) {
         poisson_part(h);
-        velocity_and_stretching(h->sz.nn, h->sz.dpm, S, R, Vv, G, h->stream, 1);
+        velocity_and_stretching(h->sz.nn, h->sz.dpm, S, R, Vv, G, h->stream, 1, VF, GF);
       } else {
         VPMG_CHECK(up && gp, VPMG_ERR_ARG, "UP or GP is null");
-        velocity_and_stretching(h->sz.nn, h->sz.dpm, S, R, Vv, G, h->stream, 2);
+        velocity_and_stretching(h->sz.nn, h->sz.dpm, S, R, Vv, G, h->stream, 2, VF, GF);
         const double u0[3] = {0.0, 0.0, 0.0};
         m2p_step(h, true, false, 0.0, u0);
         VPMG_CUDA(cudaMemcpyAsync(up, h->parts.up.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost,

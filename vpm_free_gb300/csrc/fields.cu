@@ -7,6 +7,7 @@
 //  * calc_velocity_serial_3d(1) (source/vpm_gcalc.f90:1-136): central-
 //    difference curl and the conservative stretching term.
 #include "fields.h"
+#include "ff.cuh"
 
 namespace vpmg {
 
@@ -73,9 +74,12 @@ __global__ void k_face_interp(const long long* __restrict__ node, const long lon
 }
 
 // u = curl psi on nodes 1..N-2 (0-based); other nodes keep zero.
+// With f0 (nullable), the velocity is also written as float-float pairs
+// f0/f1/f2 for the mesh-to-particle gather.
 __global__ void k_velocity(const double* __restrict__ p0, const double* __restrict__ p1, const double* __restrict__ p2,
                            int NX, int NY, int NZ, double i2x, double i2y, double i2z, double* __restrict__ u0,
-                           double* __restrict__ u1, double* __restrict__ u2) {
+                           double* __restrict__ u1, double* __restrict__ u2, float2* __restrict__ f0,
+                           float2* __restrict__ f1, float2* __restrict__ f2) {
   const int ex = NX - 2, ey = NY - 2, ez = NZ - 2;
   const size_t n = (size_t)ex * ey * ez;
   const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -86,16 +90,23 @@ __global__ void k_velocity(const double* __restrict__ p0, const double* __restri
   const double dx1 = (p1[id + 1] - p1[id - 1]) * i2x, dx2 = (p2[id + 1] - p2[id - 1]) * i2x;
   const double dy0 = (p0[id + sy] - p0[id - sy]) * i2y, dy2 = (p2[id + sy] - p2[id - sy]) * i2y;
   const double dz0 = (p0[id + sz] - p0[id - sz]) * i2z, dz1 = (p1[id + sz] - p1[id - sz]) * i2z;
-  u0[id] = dy2 - dz1;
-  u1[id] = -(dx2 - dz0);
-  u2[id] = dx1 - dy0;
+  const double v0 = dy2 - dz1, v1 = -(dx2 - dz0), v2 = dx1 - dy0;
+  u0[id] = v0;
+  u1[id] = v1;
+  u2[id] = v2;
+  if (f0) {
+    f0[id] = ff::split(v0);
+    f1[id] = ff::split(v1);
+    f2[id] = ff::split(v2);
+  }
 }
 
 // Stretching  SOL(m) = -sum_j d(RHS_j u_m)/dx_j  on nodes 2..N-3 (0-based).
 __global__ void k_deformation(const double* __restrict__ r0, const double* __restrict__ r1, const double* __restrict__ r2,
                               const double* __restrict__ u0, const double* __restrict__ u1,
                               const double* __restrict__ u2, int NX, int NY, int NZ, double i2x, double i2y, double i2z,
-                              double* __restrict__ g0, double* __restrict__ g1, double* __restrict__ g2) {
+                              double* __restrict__ g0, double* __restrict__ g1, double* __restrict__ g2,
+                              float2* __restrict__ f0, float2* __restrict__ f1, float2* __restrict__ f2) {
   const int ex = NX - 4, ey = NY - 4, ez = NZ - 4;
   const size_t n = (size_t)ex * ey * ez;
   const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -107,13 +118,16 @@ __global__ void k_deformation(const double* __restrict__ r0, const double* __res
                rzm = r2[id - sz];
   const double* U[3] = {u0, u1, u2};
   double* G[3] = {g0, g1, g2};
+  float2* F[3] = {f0, f1, f2};
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
     const double* u = U[m];
     const double a = -(rxp * u[id + 1] - rxm * u[id - 1]) * i2x;
     const double b = -(ryp * u[id + sy] - rym * u[id - sy]) * i2y;
     const double c = -(rzp * u[id + sz] - rzm * u[id - sz]) * i2z;
-    G[m][id] = (a + b) + c;
+    const double v = (a + b) + c;
+    G[m][id] = v;
+    if (f0) F[m][id] = ff::split(v);
   }
 }
 
@@ -232,18 +246,22 @@ void viscous_diffusion(const int dims[3], const int nn_bl[6], const double h[3],
 }
 
 void velocity_and_stretching(const int dims[3], const double h[3], const double* const psi[3], const double* const rhs[3],
-                             double* const vel[3], double* const def[3], cudaStream_t s, int parts) {
+                             double* const vel[3], double* const def[3], cudaStream_t s, int parts,
+                             float2* const vel_ff[3], float2* const def_ff[3]) {
   const int NX = dims[0], NY = dims[1], NZ = dims[2];
   const double i2x = 1.0 / (2 * h[0]), i2y = 1.0 / (2 * h[1]), i2z = 1.0 / (2 * h[2]);
   if ((parts & 1) && NX > 2 && NY > 2 && NZ > 2) {
     const size_t n = (size_t)(NX - 2) * (NY - 2) * (NZ - 2);
-    k_velocity<<<grid_for(n, 256), 256, 0, s>>>(psi[0], psi[1], psi[2], NX, NY, NZ, i2x, i2y, i2z, vel[0], vel[1], vel[2]);
+    k_velocity<<<grid_for(n, 256), 256, 0, s>>>(psi[0], psi[1], psi[2], NX, NY, NZ, i2x, i2y, i2z, vel[0], vel[1], vel[2],
+                                                vel_ff ? vel_ff[0] : nullptr, vel_ff ? vel_ff[1] : nullptr,
+                                                vel_ff ? vel_ff[2] : nullptr);
     VPMG_LAUNCHED();
   }
   if ((parts & 2) && NX > 4 && NY > 4 && NZ > 4) {
     const size_t n = (size_t)(NX - 4) * (NY - 4) * (NZ - 4);
     k_deformation<<<grid_for(n, 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], vel[0], vel[1], vel[2], NX, NY, NZ, i2x, i2y,
-                                                   i2z, def[0], def[1], def[2]);
+                                                   i2z, def[0], def[1], def[2], def_ff ? def_ff[0] : nullptr,
+                                                   def_ff ? def_ff[1] : nullptr, def_ff ? def_ff[2] : nullptr);
     VPMG_LAUNCHED();
   }
   VPMG_CUDA(cudaGetLastError());

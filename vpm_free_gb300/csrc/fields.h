@@ -26,7 +26,9 @@ void viscous_diffusion(const int dims[3], const int nn_bl[6], const double h[3],
                        double* const sol[3], cudaStream_t s);
 // calc_velocity_serial_3d: parts bit 0 = velocity (curl psi), bit 1 = stretching
 // (from rhs and the velocity in vel); idcalc 1 = both, 0 = velocity, -1 = stretching.
+// vel_ff / def_ff (nullable): the same values also as float-float pairs.
 void velocity_and_stretching(const int dims[3], const double h[3], const double* const psi[3], const double* const rhs[3],
-                             double* const vel[3], double* const def[3], cudaStream_t s, int parts = 3);
+                             double* const vel[3], double* const def[3], cudaStream_t s, int parts = 3,
+                             float2* const vel_ff[3] = nullptr, float2* const def_ff[3] = nullptr);
 
 }  // namespace vpmg

@@ -47,6 +47,7 @@ struct vpmg_handle {
   vpmg::Particles parts;
   vpmg::Binning bins;
   int np = 0;
+  vpmg::DBuf<float2> vel_ff, def_ff;  // velocity and stretching as float-float pairs (mesh-to-particle)
   vpmg::DBuf<double> stage;          // AoS staging for host copies
   vpmg::DBuf<double> bench_scratch;  // replay outputs of vpmg_bench_kernel
   // timing

@@ -184,12 +184,18 @@ __global__ void k_deposit(const int* __restrict__ starts, const float2* __restri
   r2[id] = ff::to_double(a2) * inv_dv;
 }
 
+// A field value as a float-float pair: split from FP64, or stored as one.
+__device__ __forceinline__ float2 field_ff(const double* __restrict__ f, size_t id) { return ff::split(f[id]); }
+__device__ __forceinline__ float2 field_ff(const float2* __restrict__ f, size_t id) { return f[id]; }
+
 // M2P over sorted slots: UP = sum W vel, GP = (sum W def) * vol; optionally
-// the forward Euler push.  Weight products and sums in float-float.
+// the forward Euler push.  Weight products and sums in float-float; the
+// fields are FP64 arrays or float-float pairs (T).
+template <typename T>
 __global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsorted_dev, const float2* __restrict__ rec,
                       MeshDev m,
-                      const double* __restrict__ v0, const double* __restrict__ v1, const double* __restrict__ v2,
-                      const double* __restrict__ g0, const double* __restrict__ g1, const double* __restrict__ g2,
+                      const T* __restrict__ v0, const T* __restrict__ v1, const T* __restrict__ v2,
+                      const T* __restrict__ g0, const T* __restrict__ g1, const T* __restrict__ g2,
                       double* __restrict__ up, double* __restrict__ gp, double* __restrict__ x, double* __restrict__ y,
                       double* __restrict__ z, double* __restrict__ q0, double* __restrict__ q1, double* __restrict__ q2,
                       const double* __restrict__ vol, int do_euler, double dt, double ux, double uy, double uz) {
@@ -215,12 +221,12 @@ __global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsor
       for (int a = 0; a < nw; ++a) {
         const float2 f = ff::mul(w[a], wyz);
         const size_t id = row + a;
-        u[0] = ff::fma(f, ff::split(v0[id]), u[0]);
-        u[1] = ff::fma(f, ff::split(v1[id]), u[1]);
-        u[2] = ff::fma(f, ff::split(v2[id]), u[2]);
-        gl[0] = ff::fma(f, ff::split(g0[id]), gl[0]);
-        gl[1] = ff::fma(f, ff::split(g1[id]), gl[1]);
-        gl[2] = ff::fma(f, ff::split(g2[id]), gl[2]);
+        u[0] = ff::fma(f, field_ff(v0, id), u[0]);
+        u[1] = ff::fma(f, field_ff(v1, id), u[1]);
+        u[2] = ff::fma(f, field_ff(v2, id), u[2]);
+        gl[0] = ff::fma(f, field_ff(g0, id), gl[0]);
+        gl[1] = ff::fma(f, field_ff(g1, id), gl[1]);
+        gl[2] = ff::fma(f, field_ff(g2, id), gl[2]);
       }
     }
   }
@@ -379,14 +385,25 @@ void deposit(const Particles& P, const MeshDev& m, const Binning& B, double* con
   VPMG_CUDA(cudaGetLastError());
 }
 
-void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const vel[3], const double* const def[3],
-         bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s) {
-  k_m2p<<<stride_grid(P.capacity, 128), 128, 0, s>>>(P.perm.p, B.nsorted_dev, P.rec.p, m, vel[0], vel[1], vel[2],
-                                                      def[0], def[1], def[2], write_up ? P.up.p : nullptr, P.gp.p,
-                                                      P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.vol.p,
-                                                      euler ? 1 : 0, dt, uinf[0], uinf[1], uinf[2]);
+template <typename T>
+static void m2p_launch(Particles& P, const MeshDev& m, const Binning& B, const T* const vel[3], const T* const def[3],
+                       bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s) {
+  k_m2p<T><<<stride_grid(P.capacity, 128), 128, 0, s>>>(P.perm.p, B.nsorted_dev, P.rec.p, m, vel[0], vel[1], vel[2],
+                                                         def[0], def[1], def[2], write_up ? P.up.p : nullptr, P.gp.p,
+                                                         P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.vol.p,
+                                                         euler ? 1 : 0, dt, uinf[0], uinf[1], uinf[2]);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
+}
+
+void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const vel[3], const double* const def[3],
+         bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s) {
+  m2p_launch(P, m, B, vel, def, write_up, euler, dt, uinf, s);
+}
+
+void m2p(Particles& P, const MeshDev& m, const Binning& B, const float2* const vel[3], const float2* const def[3],
+         bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s) {
+  m2p_launch(P, m, B, vel, def, write_up, euler, dt, uinf, s);
 }
 
 // Ordered compaction of the flagged nodes; the new count goes to P.d_np

@@ -47,6 +47,9 @@ void bin_particles(Particles& P, const MeshDev& m, Binning& B, cudaStream_t s);
 void deposit(const Particles& P, const MeshDev& m, const Binning& B, double* const rhs[3], cudaStream_t s);
 void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const vel[3], const double* const def[3],
          bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s);
+// the same with the fields as float-float pairs (no split per node visit)
+void m2p(Particles& P, const MeshDev& m, const Binning& B, const float2* const vel[3], const float2* const def[3],
+         bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s);
 void remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3],
                  const int hi[3], double thr, cudaStream_t s);
 // The emission mask alone: B.cursor = node flag, B.starts = emit slot (exclusive scan).
