@@ -131,6 +131,42 @@ __global__ void k_deformation(const double* __restrict__ r0, const double* __res
   }
 }
 
+// The stretching stencil in float-float arithmetic, writing both the FP64
+// field and its float-float pairs: the products and differences run on the
+// FP32 pipes, the only FP64 operation is the join of each output.  It reads
+// the velocity's float-float pairs.  (The velocity's curl stays FP64: it has
+// few operations per node and runs at the memory rate.)
+__global__ void k_deformation_ff(const double* __restrict__ r0, const double* __restrict__ r1,
+                                 const double* __restrict__ r2, const float2* __restrict__ u0,
+                                 const float2* __restrict__ u1, const float2* __restrict__ u2, int NX, int NY, int NZ,
+                                 double i2x, double i2y, double i2z, double* __restrict__ g0, double* __restrict__ g1,
+                                 double* __restrict__ g2, float2* __restrict__ f0, float2* __restrict__ f1,
+                                 float2* __restrict__ f2) {
+  const int ex = NX - 4, ey = NY - 4, ez = NZ - 4;
+  const size_t n = (size_t)ex * ey * ez;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = 2 + (int)(t % ex), j = 2 + (int)((t / ex) % ey), k = 2 + (int)(t / ((size_t)ex * ey));
+  const size_t sy = NX, sz = (size_t)NX * NY;
+  const size_t id = i + sy * j + sz * k;
+  const float2 IX = ff::split(i2x), IY = ff::split(i2y), IZ = ff::split(i2z);
+  const float2 rxp = ff::split(r0[id + 1]), rxm = ff::split(r0[id - 1]), ryp = ff::split(r1[id + sy]),
+               rym = ff::split(r1[id - sy]), rzp = ff::split(r2[id + sz]), rzm = ff::split(r2[id - sz]);
+  const float2* U[3] = {u0, u1, u2};
+  double* G[3] = {g0, g1, g2};
+  float2* F[3] = {f0, f1, f2};
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const float2* u = U[m];
+    const float2 a = ff::neg(ff::mul(ff::sub(ff::mul(rxp, u[id + 1]), ff::mul(rxm, u[id - 1])), IX));
+    const float2 b = ff::neg(ff::mul(ff::sub(ff::mul(ryp, u[id + sy]), ff::mul(rym, u[id - sy])), IY));
+    const float2 c = ff::neg(ff::mul(ff::sub(ff::mul(rzp, u[id + sz]), ff::mul(rzm, u[id - sz])), IZ));
+    const float2 v = ff::add(ff::add(a, b), c);
+    G[m][id] = ff::to_double(v);
+    F[m][id] = v;
+  }
+}
+
 // diffuse_vort_3d (source/vpm_gcalc.f90:138-210), neqpm = 3 (VIS = NI):
 // SOL(m) = -NI Lap_h RHS(m) on the nodes strictly inside [lo, hi] (0-based);
 // SOL is zero elsewhere (cleared by the caller).
@@ -259,9 +295,14 @@ void velocity_and_stretching(const int dims[3], const double h[3], const double*
   }
   if ((parts & 2) && NX > 4 && NY > 4 && NZ > 4) {
     const size_t n = (size_t)(NX - 4) * (NY - 4) * (NZ - 4);
-    k_deformation<<<grid_for(n, 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], vel[0], vel[1], vel[2], NX, NY, NZ, i2x, i2y,
-                                                   i2z, def[0], def[1], def[2], def_ff ? def_ff[0] : nullptr,
-                                                   def_ff ? def_ff[1] : nullptr, def_ff ? def_ff[2] : nullptr);
+    if (vel_ff && def_ff)  // the velocity's float-float pairs are current whenever vel_ff is passed
+      k_deformation_ff<<<grid_for(n, 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], vel_ff[0], vel_ff[1], vel_ff[2], NX, NY,
+                                                        NZ, i2x, i2y, i2z, def[0], def[1], def[2], def_ff[0],
+                                                        def_ff[1], def_ff[2]);
+    else
+      k_deformation<<<grid_for(n, 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], vel[0], vel[1], vel[2], NX, NY, NZ, i2x,
+                                                     i2y, i2z, def[0], def[1], def[2], def_ff ? def_ff[0] : nullptr,
+                                                     def_ff ? def_ff[1] : nullptr, def_ff ? def_ff[2] : nullptr);
     VPMG_LAUNCHED();
   }
   VPMG_CUDA(cudaGetLastError());
