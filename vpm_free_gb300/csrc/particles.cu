@@ -253,8 +253,13 @@ __global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsor
 }
 
 // Remesh: flag nodes inside [lo, hi] (0-based, per axis) with |w| >= thr.
+// flag = !(sqrt_rn(s) < thr) with s = (a*a + b*b) + c*c rounded as written.
+// A correctly rounded square root is monotonic, so sqrt_rn(s) < thr exactly
+// when s < tstar, the least double whose root is >= thr (found on the host):
+// no square root per node.  Nodes whose three values have biased exponents
+// <= emax have s < tstar / 2 and are decided from the exponent bits alone.
 __global__ void k_remesh_flags(const double* __restrict__ r0, const double* __restrict__ r1, const double* __restrict__ r2,
-                               MeshDev m, int lo0, int lo1, int lo2, int hi0, int hi1, int hi2, double thr,
+                               MeshDev m, int lo0, int lo1, int lo2, int hi0, int hi1, int hi2, double tstar, int emax,
                                int* __restrict__ flag) {
   const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
   const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -265,8 +270,12 @@ __global__ void k_remesh_flags(const double* __restrict__ r0, const double* __re
   int f = 0;
   if (i >= lo0 && i <= hi0 && j >= lo1 && j <= hi1 && k >= lo2 && k <= hi2) {
     const double a = r0[id], b = r1[id], c = r2[id];
-    const double wmag = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c)));
-    f = (wmag < thr) ? 0 : 1;
+    const int ea = (__double2hiint(a) >> 20) & 0x7FF, eb = (__double2hiint(b) >> 20) & 0x7FF,
+              ec = (__double2hiint(c) >> 20) & 0x7FF;
+    if (max(ea, max(eb, ec)) > emax) {
+      const double s2 = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+      f = (s2 < tstar) ? 0 : 1;
+    }
   }
   flag[id] = f;
 }
@@ -408,12 +417,33 @@ void m2p(Particles& P, const MeshDev& m, const Binning& B, const float2* const v
 
 // Ordered compaction of the flagged nodes; the new count goes to P.d_np
 // (clamped to the capacity, overflow flagged in B.err), on the stream.
+// tstar = least double t with sqrt_rn(t) >= thr (thr > 0): sqrt_rn(s) < thr
+// exactly when s < tstar.  emax = largest biased exponent e such that three
+// values below 2^(e - 1022) in magnitude give s < tstar / 2.
+static void remesh_threshold(double thr, double* tstar, int* emax) {
+  double t = thr * thr;
+  while (t > 0.0 && std::sqrt(std::nextafter(t, 0.0)) >= thr) t = std::nextafter(t, 0.0);
+  while (std::sqrt(t) < thr) t = std::nextafter(t, INFINITY);
+  *tstar = t;
+  int e = 0;
+  while (e < 2046) {
+    const double mx = std::ldexp(1.0, e + 1 - 1022);  // bound for exponent e + 1
+    if (3.0 * mx * mx >= 0.5 * t) break;
+    ++e;
+  }
+  *emax = e;
+}
+
 void remesh_mask(const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3], const int hi[3],
                  double thr, cudaStream_t s) {
   const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
   B.ensure(N);
+  VPMG_CHECK(thr > 0.0 && std::isfinite(thr), VPMG_ERR_ARG, "remesh threshold must be positive");
+  double tstar = 0.0;
+  int emax = 0;
+  remesh_threshold(thr, &tstar, &emax);
   k_remesh_flags<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], m, lo[0], lo[1], lo[2], hi[0], hi[1],
-                                                              hi[2], thr, B.cursor.p);
+                                                              hi[2], tstar, emax, B.cursor.p);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaMemsetAsync(B.sums.p, 0, sizeof(int) * B.sums.n, s));
   exclusive_scan_int(B.cursor.p, B.starts.p, N, B.sums.p, s);
