@@ -98,3 +98,22 @@ def test_host_euler_is_the_reference_update(gpulib):
     assert np.array_equal(XP, ex) and np.array_equal(QP, eq)
     with pytest.raises(ValueError):
         V.VPM.host_euler(XP, QP, UP, GP, rows + 1, dt)
+
+
+def test_batch_entry_points_reject_bad_arguments(gpulib):
+    """The batch object's C-ABI checks its arguments before any device work."""
+    L = gpulib.load_library()
+    out = C.c_void_p()
+    assert L.vpmg_batch_create(None, 1, 0, C.byref(out)) == -1
+    arr = (C.c_void_p * 1)(None)
+    assert L.vpmg_batch_create(arr, 1, 0, C.byref(out)) == -1
+    assert L.vpmg_batch_create(arr, 0, 0, C.byref(out)) == -1
+    u, s, r = C.c_int(0), C.c_int(0), C.c_longlong(0)
+    assert L.vpmg_batch_info(None, C.byref(u), C.byref(s), C.byref(r)) == -1
+    ms, sv, ps = C.c_double(0), C.c_longlong(0), C.c_longlong(0)
+    assert L.vpmg_batch_step(None, 1, 0.01, 1, C.byref(ms), C.byref(sv), C.byref(ps)) == -1
+    assert L.vpmg_batch_set_schedule(None, 0) == -1
+    assert L.vpmg_batch_get_schedule(None, None, None) == -1
+    assert L.vpmg_batch_destroy(None) == -1
+    assert L.vpmg_host_euler(None, None, None, None, 5, 0.1, None) == -1
+    assert L.vpmg_host_euler(None, None, None, None, 0, 0.1, None) == 0
