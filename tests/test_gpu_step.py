@@ -128,6 +128,23 @@ def _ring_handle(V, ncell, **kw):
     return h, w
 
 
+def test_zero_particles(gpulib):
+    """NVR = 0 on a sized handle: vpm(WhatToDo = 2) returns at once and
+    leaves the resident fields as they were (vpm.f90:171, `if (NVR.eq.0)
+    return`); remesh_particles_3d emits no particle.  No error either way."""
+    V = gpulib
+    h, _ = _ring_handle(V, 32)
+    before = {name: h.field(name).copy() for name in ("rhs", "sol", "vel", "def")}
+    xp, qp = np.zeros((0, 3)), np.zeros((0, 4))
+    up, gp = np.zeros((0, 3)), np.zeros((0, 3))
+    assert h.vpm(xp, qp, up, gp, 0, WhatToDo=2) == 0
+    for name, f in before.items():
+        assert np.array_equal(h.field(name), f), name
+    x2, q2 = h.remesh_particles_3d(1, xp, qp)
+    assert x2.shape[0] == 0 and q2.shape[0] == 0
+    h.close()
+
+
 def test_graph_replay_equals_uncaptured_steps(gpulib):
     """vpmg_run replays one captured step graph; it must reproduce the
     uncaptured vpmg_step loop bit for bit (deterministic kernels)."""
