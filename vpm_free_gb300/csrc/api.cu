@@ -888,6 +888,29 @@ struct vpmg_batch {
 };
 
 namespace {
+// CUDA events owned for the duration of one call (timed or not).
+struct EventSet {
+  std::vector<cudaEvent_t> e;
+  EventSet(size_t n, bool timing) : e(n, nullptr) {
+    try {
+      for (auto& x : e) VPMG_CUDA(timing ? cudaEventCreate(&x) : cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    } catch (...) {
+      release();  // a throwing constructor runs no destructor
+      throw;
+    }
+  }
+  ~EventSet() { release(); }
+  void release() {
+    for (auto& x : e)
+      if (x) {
+        cudaEventDestroy(x);
+        x = nullptr;
+      }
+  }
+  EventSet(const EventSet&) = delete;
+  EventSet& operator=(const EventSet&) = delete;
+};
+
 // a follower whose recorded operator differs from the leader's in more than
 // this fraction of the interactions keeps its own graph
 constexpr double kGroupMaxCorrected = 0.02;
@@ -916,8 +939,8 @@ void capture_group(vpmg_batch* b, vpmg_batch::Unit& u, double dt, int do_remesh)
     H[k]->hist.ensure(kHistCap);
     H[k]->hist_counter.ensure(1);
   }
-  std::vector<cudaEvent_t> ev(2 * n + 1, nullptr);
-  for (auto& e : ev) VPMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  EventSet evs(2 * (size_t)n + 1, false);
+  std::vector<cudaEvent_t>& ev = evs.e;
   std::vector<char> prof(n);
   std::vector<long long> l0(n);
   for (int k = 0; k < n; ++k) {
@@ -927,7 +950,6 @@ void capture_group(vpmg_batch* b, vpmg_batch::Unit& u, double dt, int do_remesh)
   }
   auto restore = [&] {
     for (int k = 0; k < n; ++k) H[k]->profile = prof[k];
-    for (auto e : ev) cudaEventDestroy(e);
   };
   const int lanes = n;
   cudaGraph_t g = nullptr;
@@ -1086,9 +1108,9 @@ int vpmg_batch_step(vpmg_batch* b, int nsteps, double dt, int do_remesh, double*
       VPMG_CUDA(cudaStreamSynchronize(h->stream));
     }
     const size_t nu = b->units.size();
-    std::vector<cudaEvent_t> mark((size_t)nsteps + 1, nullptr), done(nu, nullptr);
-    for (auto& e : mark) VPMG_CUDA(cudaEventCreate(&e));
-    for (auto& e : done) VPMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    EventSet marks((size_t)nsteps + 1, true), dones(nu, false);  // destroyed on every exit path
+    std::vector<cudaEvent_t>& mark = marks.e;
+    std::vector<cudaEvent_t>& done = dones.e;
     auto lead = [&](size_t i) { return b->hs[b->units[i]->m[0]]; };
     auto exec_of = [&](size_t i) {
       const auto& u = *b->units[i];
@@ -1143,8 +1165,6 @@ int vpmg_batch_step(vpmg_batch* b, int nsteps, double dt, int do_remesh, double*
     VPMG_CUDA(cudaEventSynchronize(mark[nsteps]));
     float t = 0.f;
     VPMG_CUDA(cudaEventElapsedTime(&t, mark[0], mark[nsteps]));
-    for (auto e : mark) cudaEventDestroy(e);
-    for (auto e : done) cudaEventDestroy(e);
     long long ps = 0;
     for (size_t i = 0; i < nu; ++i) {
       const auto& u = *b->units[i];
