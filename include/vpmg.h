@@ -5,11 +5,13 @@
  * `vpm(...)` driver call, pm.inp and particle arrays, and binds these entry
  * points through iso_c_binding (see vpm_free_gb300/fortran/).  Plain C
  * types only; every call returns an int status (0 = OK, < 0 = error, see
- * vpmg_status) and never aborts the process.  Arrays are FP64; the heavy
- * kernels (boundary operator, DST solves, projection weights, deposition,
- * mesh-to-particle) compute in float-float arithmetic (about 48 significant
- * bits) on the FP32 pipes, the rest in FP64; fields match an FP64 CPU
- * restatement to relative L2 <= 1e-10.
+ * vpmg_status) and never aborts the process.  Arrays are FP64, and by
+ * default every kernel computes in IEEE FP64, the reference's arithmetic.
+ * vpmg_set_arithmetic selects float-float instead for the heavy kernels
+ * (boundary operator, DST solves, projection weights, deposition,
+ * mesh-to-particle, stretching): about 48 significant bits and FP32's
+ * exponent range, on the FP32 pipes.  In either mode the fields match an
+ * FP64 CPU restatement to relative L2 <= 1e-10.
  *
  * Array conventions follow the reference (Fortran column-major):
  *   XP(3,NVRM)  positions            -> double xp[ld*3], xp[3*p + d]
@@ -84,6 +86,17 @@ int vpmg_read_pm_inp(const char* path, vpmg_config* cfg);
  * vpm_lib (source/vpm.f90:1-32) with an explicit handle.                   */
 int vpmg_create(const vpmg_config* cfg, int device, vpmg_handle** out);
 int vpmg_destroy(vpmg_handle* h);
+
+/* Arithmetic of the heavy kernels (no counterpart in the reference, which
+ * is REAL(8) throughout).  VPMG_ARITH_FP64 (default): IEEE FP64 everywhere.
+ * VPMG_ARITH_FF48: boundary operator, DST solves, projection weights,
+ * deposition, mesh-to-particle and stretching in float-float (hi + lo
+ * floats, about 48 significant bits; magnitudes between about 1e-38 and
+ * 3e38, smaller values flush to zero), the rest in FP64.  Changing it on a
+ * sized handle rebuilds the plans and the recorded boundary operator.    */
+enum { VPMG_ARITH_FP64 = 0, VPMG_ARITH_FF48 = 1 };
+int vpmg_set_arithmetic(vpmg_handle* h, int arith);
+int vpmg_get_arithmetic(const vpmg_handle* h, int* arith);
 const char* vpmg_last_error(const vpmg_handle* h);
 const char* vpmg_status_string(int status);
 
@@ -121,6 +134,12 @@ int vpmg_pmesh(vpmg_handle* h, double* const sol[3], const double* const rhs[3],
  * on the mesh of the last define_sizes: rhs[c] = sum_p W(x)W(y)W(z) QP(c,p) / DVpm. */
 int vpmg_project_particles_3d(vpmg_handle* h, const double* xp, const double* qp, int nvr,
                               double* const rhs[3]);
+
+/* projection_fun(itype, x) of module projlib (source/pmproject.f90:391-431):
+ * the 1-D projection kernels, 2 linear, 3 TSC, 4 M4', 5 and 6 the
+ * reference's two others, evaluated on |x| (0 for other itype).  Host
+ * code, no GPU; for host programs that `use projlib`.                    */
+double vpmg_projection_fun(int itype, double x);
 
 /* ---- allocation-free Dirichlet solve ----------------------------------
  * No counterpart in the reference: an extra entry point of this library.

@@ -20,12 +20,33 @@ def oracle():
     return O
 
 
-@pytest.fixture(scope="session")
-def gpulib():
+class _ArithLib:
+    """The package with VPM handles created in one arithmetic ('fp64', the
+    library default and the reference's, or 'ff48'); every other attribute
+    is the package's own."""
+
+    def __init__(self, mod, arith):
+        self._mod = mod
+        self.arith = arith
+
+        class VPM(mod.VPM):
+            def __init__(self, cfg, device=-1, arith=arith):
+                super().__init__(cfg, device, arith)
+
+        self.VPM = VPM
+
+    def __getattr__(self, name):
+        return getattr(self._mod, name)
+
+
+@pytest.fixture(scope="session", params=["fp64", "ff48"])
+def gpulib(request):
+    """The library, once per arithmetic of the heavy kernels: every test
+    that takes it runs in IEEE FP64 and in float-float."""
     import vpm_free_gb300 as V
     from vpm_free_gb300 import build
     build.build()
-    return V
+    return _ArithLib(V, request.param)
 
 TESTS = os.path.dirname(os.path.abspath(__file__))
 if TESTS not in sys.path:

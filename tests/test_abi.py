@@ -117,3 +117,39 @@ def test_batch_entry_points_reject_bad_arguments(gpulib):
     assert L.vpmg_batch_destroy(None) == -1
     assert L.vpmg_host_euler(None, None, None, None, 5, 0.1, None) == -1
     assert L.vpmg_host_euler(None, None, None, None, 0, 0.1, None) == 0
+
+
+def test_projection_fun_matches_oracle(gpulib, oracle):
+    """vpmg_projection_fun (projlib's projection_fun, pmproject.f90:391-431)
+    equals the oracle's restatement for every kernel type, both signs of x."""
+    L = gpulib.load_library()
+    O = oracle.lib()
+    xs = [i / 64.0 for i in range(-160, 161)] + [0.5, 1.0, 1.5, 2.0, 1e-9, 2.0000001]
+    for itype in (2, 3, 4, 5, 6):
+        for x in xs:
+            assert L.vpmg_projection_fun(itype, x) == O.vpmo_projection_fun(itype, x), (itype, x)
+    assert L.vpmg_projection_fun(7, 0.1) == 0.0
+
+
+def test_fortran_shim_declares_what_test_f90_uses():
+    """The Fortran binding declares, in modules that vpm_lib re-exports (as
+    the reference's vpm_lib re-exports vpm_vars and vpm_size, vpm.f90:42-44),
+    the names source/test.f90 takes from them: mrem (test.f90:47), st and et
+    (:54, :57), interf_iproj (:202), neqpm (:234), Dpm (:438); and a projlib
+    module with projection_fun (:187).  No Fortran compiler exists here, so
+    this reads the source."""
+    src = open(os.path.join(ROOT, "vpm_free_gb300", "fortran", "vpm_gb300.f90")).read().lower()
+
+    def module(name):
+        m = re.search(r"^module %s\b(.*?)^end module %s" % (name, name), src, flags=re.S | re.M)
+        assert m, name
+        return m.group(1)
+
+    lib = module("vpm_lib")
+    for used in ("vpm_vars", "vpm_size", "openmpth"):
+        assert re.search(r"^\s*use %s\b" % used, lib, flags=re.M), used
+    decl = module("vpm_vars") + module("vpm_size")
+    for name in ("mrem", "st", "et", "interf_iproj", "neqpm", "dpm", "nn_bl", "xbound"):
+        assert re.search(r"::[^\n]*\b%s\b" % name, decl), name
+    assert "function projection_fun" in module("projlib")
+    assert "velvrx_pm" in module("pmgrid")

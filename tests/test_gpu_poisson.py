@@ -98,7 +98,7 @@ def test_dst_tile_shape_does_not_change_results(gpulib):
         "    R = [rng.normal(size=(nz, ny, nx)) for _ in range(3)]\n"
         "    S = [np.zeros_like(R[0]) for _ in range(3)]\n"
         "    S[0][0] = 1.0\n"
-        "    with V.VPM(V.VPMConfig.make()) as h:\n"
+        f"    with V.VPM(V.VPMConfig.make(), arith='{gpulib.arith}') as h:\n"
         "        h.pmesh(S, R, [0, 0, 0, 1, 1, 1], [0.1, 0.11, 0.09], 0)\n"
         "    print(hashlib.sha256(b''.join(s.tobytes() for s in S)).hexdigest())\n")
     outs = []

@@ -14,9 +14,11 @@ the C-ABI of libvpmg.so (include/vpmg.h):
 
 Particle arrays use the reference's layout in C order: XP(3,NVR) is a
 (NVR, 3) float64 array, QP(4,NVR) a (NVR, 4) array with QP(:,1:3) =
--omega*vol and QP(:,4) = vol.  Everything computes in FP64 on the GPU;
-there is no CPU fallback: without the compiled library or a GPU every call
-raises.
+-omega*vol and QP(:,4) = vol.  By default everything computes in IEEE FP64
+on the GPU, as the reference does; ``VPM(cfg, arith="ff48")`` (or
+``set_arithmetic``) runs the heavy kernels in float-float instead (about
+48 significant bits, FP32's exponent range).  There is no CPU fallback:
+without the compiled library or a GPU every call raises.
 """
 import ctypes as C
 import os
@@ -24,12 +26,13 @@ import os
 import numpy as np
 
 __all__ = ["VPMConfig", "VPM", "VPMError", "read_pm_inp", "read_particles_bin", "write_particles_bin", "load_library",
-           "library_path", "FIELDS"]
+           "library_path", "FIELDS", "ARITH"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 
 FIELDS = {"rhs": 0, "sol": 1, "vel": 2, "def": 3, "bl_sol1": 4, "coarse_rhs": 5, "coarse_sol": 6, "bl_final": 7}
+ARITH = {"fp64": 0, "ff48": 1}  # VPMG_ARITH_FP64 (default), VPMG_ARITH_FF48
 
 EXPORTS = [
     "vpmg_read_pm_inp", "vpmg_create", "vpmg_destroy", "vpmg_last_error", "vpmg_status_string", "vpmg_vpm",
@@ -40,7 +43,8 @@ EXPORTS = [
     "vpmg_read_particles_bin", "vpmg_write_particles_bin", "vpmg_write_solution", "vpmg_write_hist", "vpmg_set_output",
     "vpmg_dst_tiles", "vpmg_apply_poisson", "vpmg_adjoint_poisson", "vpmg_vjp_fields", "vpmg_vjp_remesh", "vpmg_adjoint_loss",
     "vpmg_adjoint_run", "vpmg_batch_create", "vpmg_batch_info", "vpmg_batch_step", "vpmg_batch_destroy",
-    "vpmg_batch_set_schedule", "vpmg_batch_get_schedule", "vpmg_host_euler",
+    "vpmg_batch_set_schedule", "vpmg_batch_get_schedule", "vpmg_host_euler", "vpmg_set_arithmetic",
+    "vpmg_get_arithmetic", "vpmg_dirichlet_static", "vpmg_projection_fun",
 ]
 
 
@@ -154,6 +158,10 @@ def load_library():
     L.vpmg_vjp_remesh.argtypes = [C.c_void_p, _dp, _dp, C.c_int, _dp, C.c_int, _dp, _dp]
     L.vpmg_adjoint_loss.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, C.c_int, C.c_double, C.c_int, _dp]
     L.vpmg_adjoint_run.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp]
+    L.vpmg_projection_fun.argtypes = [C.c_int, C.c_double]
+    L.vpmg_projection_fun.restype = C.c_double
+    L.vpmg_set_arithmetic.argtypes = [C.c_void_p, C.c_int]
+    L.vpmg_get_arithmetic.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     _LIB = L
     return L
 
@@ -206,7 +214,7 @@ def write_particles_bin(path, XP, QP, vref):
 class VPM:
     """The vpm_lib module state (source/vpm.f90:1-32) on one GPU."""
 
-    def __init__(self, cfg, device=-1):
+    def __init__(self, cfg, device=-1, arith="fp64"):
         self._L = load_library()
         self.cfg = cfg
         h = C.c_void_p()
@@ -214,6 +222,20 @@ class VPM:
         if rc != 0:
             raise VPMError(rc, self._L.vpmg_status_string(rc).decode())
         self._h = h
+        if arith != "fp64":
+            self.set_arithmetic(arith)
+
+    def set_arithmetic(self, arith):
+        """'fp64' (default, the reference's arithmetic) or 'ff48' (float-float
+        heavy kernels).  On a sized handle the plans and the recorded
+        boundary operator are rebuilt."""
+        self._chk(self._L.vpmg_set_arithmetic(self._h, ARITH[arith] if isinstance(arith, str) else int(arith)))
+
+    @property
+    def arithmetic(self):
+        a = C.c_int(-1)
+        self._chk(self._L.vpmg_get_arithmetic(self._h, C.byref(a)))
+        return {v: k for k, v in ARITH.items()}[a.value]
 
     def close(self):
         if getattr(self, "_h", None):
@@ -239,8 +261,9 @@ class VPM:
 
     # ---- the reference's calls ------------------------------------------
     def vpm(self, XP, QP, UP, GP, NVR, neqpm=3, WhatToDo=2, NTIME=0, NI=0.0, NVRM=None):
-        """vpm(XP,QP,UP,GP,NVR,neqpm,WhatToDo,...,NTIME,NI,NVRM).  UP/GP are
-        overwritten (WhatToDo = 2).  Returns NVR."""
+        """vpm(XP,QP,UP,GP,NVR,neqpm,WhatToDo,...,NTIME,NI,NVRM).  WhatToDo 2
+        and 4 add the interpolated velocity to UP (the caller zeroes it, as
+        test.f90:90-91 does) and overwrite GP.  Returns NVR."""
         nvrm = XP.shape[0] if NVRM is None else NVRM
         for a, w in ((XP, 3), (QP, 4), (UP, 3), (GP, 3)):
             if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous or a.shape[1] != w):

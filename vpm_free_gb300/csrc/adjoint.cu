@@ -155,16 +155,22 @@ __global__ void k_particle_adj(MeshDev m, const int* __restrict__ np_dev, const 
   }
 }
 
-// Strength slots of the sorted records <- scale * w_p * v_p (w = QP(4) or 1).
-__global__ void k_records_set_q(float2* __restrict__ rec, const int* __restrict__ perm, const int* __restrict__ nsorted,
-                                const double* __restrict__ v, int cap, double scale, const double* __restrict__ w) {
+// Strength slots of the sorted records <- scale * w_p * v_p (w = QP(4) or 1),
+// as doubles (FP64 records) or float-float pairs (ff != 0).
+__global__ void k_records_set_q(float2* __restrict__ rec, int ff, const int* __restrict__ perm,
+                                const int* __restrict__ nsorted, const double* __restrict__ v, int cap, double scale,
+                                const double* __restrict__ w) {
   const int n = *nsorted;
+  double* rd = reinterpret_cast<double*>(rec);
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     const int p = perm[s];
     const double f = scale * (w ? w[p] : 1.0);
-    rec[(size_t)s * kRecLen + kRecQ] = ff::split(f * v[p]);
-    rec[(size_t)s * kRecLen + kRecQ + 1] = ff::split(f * v[cap + p]);
-    rec[(size_t)s * kRecLen + kRecQ + 2] = ff::split(f * v[2 * (size_t)cap + p]);
+    const double q[3] = {f * v[p], f * v[cap + p], f * v[2 * (size_t)cap + p]};
+    for (int c = 0; c < 3; ++c) {
+      const size_t slot = (size_t)s * kRecLen + kRecQ + c;
+      if (ff) rec[slot] = ff::split(q[c]);
+      else rd[slot] = q[c];
+    }
   }
 }
 
@@ -708,10 +714,11 @@ void fields_vjp(vpmg_handle* h, const double* upb, const double* gpb, double* xb
   double* U[3] = {S.ubar.p, S.ubar.p + N, S.ubar.p + 2 * N};
   double* G[3] = {S.gbar.p, S.gbar.p + N, S.gbar.p + 2 * N};
   // M2P^T: ubar = sum_p W upbar_p,  gbar = sum_p W vol_p gpbar_p  (the deposit divides by DV)
-  k_records_set_q<<<grid(cap), 256, 0, st>>>(P.rec.p, P.perm.p, h->bins.nsorted_dev, upb, cap, dvg, nullptr);
+  const int rff = P.arith == VPMG_ARITH_FF48 ? 1 : 0;
+  k_records_set_q<<<grid(cap), 256, 0, st>>>(P.rec.p, rff, P.perm.p, h->bins.nsorted_dev, upb, cap, dvg, nullptr);
   VPMG_LAUNCHED();
   deposit(P, mg, h->bins, U, st);
-  k_records_set_q<<<grid(cap), 256, 0, st>>>(P.rec.p, P.perm.p, h->bins.nsorted_dev, gpb, cap, dvg, P.vol.p);
+  k_records_set_q<<<grid(cap), 256, 0, st>>>(P.rec.p, rff, P.perm.p, h->bins.nsorted_dev, gpb, cap, dvg, P.vol.p);
   VPMG_LAUNCHED();
   deposit(P, mg, h->bins, G, st);
   // positions through the M2P weights
@@ -776,10 +783,8 @@ void backward_step(vpmg_handle* h, double dt) {
   copy_ckpt(h, 1);
   forward_fields(h);
   {
-    const float2* V[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
-    const float2* G[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
     const double u0[3] = {0.0, 0.0, 0.0};
-    m2p(P, mg, h->bins, V, G, true, false, dt, u0, st);
+    hx::m2p_fields(h, kUpSet, false, dt, u0);
   }
   k_after_euler<<<grid(cap), 256, 0, st>>>(P.d_np.p, P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.up.p, P.gp.p, dt,
                                           S.xq1.p, cap);
@@ -836,10 +841,8 @@ void step_masked(vpmg_handle* h, double dt, const int* mask) {
   const size_t N = h->gglob.count();
   Particles& P = h->parts;
   forward_fields(h);
-  const float2* V[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
-  const float2* G[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
   const double u0[3] = {0.0, 0.0, 0.0};
-  m2p(P, hx::mesh_dev(h->gglob, 4), h->bins, V, G, true, true, dt, u0, st);
+  hx::m2p_fields(h, kUpSet, true, dt, u0);
   const Grid gr = hx::remesh_grid(h);
   const MeshDev mr = hx::mesh_dev(gr, 4);
   bin_particles(P, mr, h->bins, st);

@@ -139,9 +139,13 @@ void prepare(vpmg_handle* h) {
   h->nblk = h->nb3[0] * h->nb3[1] * h->nb3[2];
   const size_t B = (size_t)h->nblk;
   h->rhs.ensure(3 * N); h->sol.ensure(3 * N); h->vel.ensure(3 * N); h->def.ensure(3 * N);
-  h->vel_ff.ensure(3 * N); h->def_ff.ensure(3 * N);
-  VPMG_CUDA(cudaMemsetAsync(h->vel_ff.p, 0, h->vel_ff.bytes(), h->stream));
-  VPMG_CUDA(cudaMemsetAsync(h->def_ff.p, 0, h->def_ff.bytes(), h->stream));
+  if (h->arith == VPMG_ARITH_FF48) {  // float-float copies of the velocity and stretching for the gather
+    h->vel_ff.ensure(3 * N); h->def_ff.ensure(3 * N);
+    VPMG_CUDA(cudaMemsetAsync(h->vel_ff.p, 0, h->vel_ff.bytes(), h->stream));
+    VPMG_CUDA(cudaMemsetAsync(h->def_ff.p, 0, h->def_ff.bytes(), h->stream));
+  } else {
+    h->vel_ff.release(); h->def_ff.release();
+  }
   h->rhs_bl.ensure(B * 3 * NB); h->sol_bl.ensure(B * 3 * NB); h->sol0.ensure(NB);
   h->samp.ensure(B * 3 * NC); h->crhs.ensure(3 * NC); h->csol.ensure(3 * NC); h->csol0.ensure(NC);
   h->sampsum.ensure(3 * NC);
@@ -153,9 +157,9 @@ void prepare(vpmg_handle* h) {
   const int bl_inner[6] = {s.nnbl_bl[0] - 1, s.nnbl_bl[1] - 1, s.nnbl_bl[2] - 1,
                            s.nnbl_bl[3] - 1, s.nnbl_bl[4] - 1, s.nnbl_bl[5] - 1};
   const int c_full[6] = {0, 0, 0, s.nn_coarse[0] - 1, s.nn_coarse[1] - 1, s.nn_coarse[2] - 1};
-  dirichlet_prepare(h->dp_bl, s.nnbl, bl_full, s.dpm, st);
-  dirichlet_prepare(h->dp_inner, s.nnbl, bl_inner, s.dpm, st);
-  dirichlet_prepare(h->dp_c, s.nn_coarse, c_full, s.dpm_coarse, st);
+  dirichlet_prepare(h->dp_bl, s.nnbl, bl_full, s.dpm, st, h->arith);
+  dirichlet_prepare(h->dp_inner, s.nnbl, bl_inner, s.dpm, st, h->arith);
+  dirichlet_prepare(h->dp_c, s.nn_coarse, c_full, s.dpm_coarse, st, h->arith);
   size_t wmax = 0;
   for (DirichletPlan* p : {&h->dp_bl, &h->dp_inner, &h->dp_c}) wmax = std::max(wmax, (size_t)p->m[0] * p->m[1] * p->m[2]);
   h->work.ensure(wmax);
@@ -166,9 +170,11 @@ void prepare(vpmg_handle* h) {
   }
   // boundary operators: fine block (levels ilevmax), coarse (ilevmax-1); iyntree = 0 -> untreed sum
   const bool tree = h->cfg.iyntree == 1;
-  boundary_prepare(h->bo_c, h->gco, tree ? std::max(s.ilevmax - 1, 0) : 0, h->op_budget, st, h->cfg.ibctyp, tree);
+  boundary_prepare(h->bo_c, h->gco, tree ? std::max(s.ilevmax - 1, 0) : 0, h->op_budget, st, h->cfg.ibctyp, tree,
+                   h->arith);
   if (h->nblk == 1) {
-    boundary_prepare(h->bo_bl, h->gbl, tree ? std::max(s.ilevmax, 0) : 0, h->op_budget, st, h->cfg.ibctyp, tree);
+    boundary_prepare(h->bo_bl, h->gbl, tree ? std::max(s.ilevmax, 0) : 0, h->op_budget, st, h->cfg.ibctyp, tree,
+                     h->arith);
     // YAPS maps
     YapsGeom Y;
     try {
@@ -194,12 +200,13 @@ void prepare(vpmg_handle* h) {
       h->g_blk[b] = make_grid(&Y.xbl[6 * (size_t)b], s.dpm, s.nnbl);
       h->bo_blk.push_back(std::make_unique<BoundaryOp>());
       boundary_prepare(*h->bo_blk[b], h->g_blk[b], tree ? std::max(s.ilevmax, 0) : 0, h->op_budget / h->nblk, st,
-                       h->cfg.ibctyp, tree);
+                       h->cfg.ibctyp, tree, h->arith);
     }
     h->ym.prepare(Y);
   }
   // particles: capacity for a full remesh of the global mesh
   h->parts.ensure((int)std::min<size_t>(N, (size_t)INT32_MAX / 16));
+  h->parts.arith = h->arith;
   h->bins.ensure(N);
   VPMG_CUDA(cudaStreamSynchronize(st));
   h->prepared = true;
@@ -357,6 +364,17 @@ void deposit_rhs(vpmg_handle* h) {
   deposit(h->parts, mg, h->bins, R, h->stream);
 }
 
+// The float-float copies of the velocity and stretching (float-float
+// arithmetic only; null pointers otherwise).
+void ff_fields(vpmg_handle* h, float2* VF[3], float2* GF[3]) {
+  const size_t N = h->gglob.count();
+  const bool ff = h->arith == VPMG_ARITH_FF48 && h->vel_ff.p && h->def_ff.p;
+  for (int c = 0; c < 3; ++c) {
+    VF[c] = ff ? h->vel_ff.p + c * N : nullptr;
+    GF[c] = ff ? h->def_ff.p + c * N : nullptr;
+  }
+}
+
 // calc_velocity_serial_3d(1) on h->sol and h->rhs
 void field_velocity(vpmg_handle* h) {
   cudaStream_t st = h->stream;
@@ -367,9 +385,9 @@ void field_velocity(vpmg_handle* h) {
   // calc_velocity_serial_3d(1)
   double* V[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
   double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
-  float2* VF[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
-  float2* GF[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
-  velocity_and_stretching(s.nn, s.dpm, S, R, V, G, st, 3, VF, GF);
+  float2* VF[3], * GF[3];
+  ff_fields(h, VF, GF);
+  velocity_and_stretching(s.nn, s.dpm, S, R, V, G, st, 3, VF[0] ? VF : nullptr, GF[0] ? GF : nullptr);
   ev_mark(h, 7);
 }
 
@@ -379,14 +397,24 @@ void field_step(vpmg_handle* h) {
   field_velocity(h);
 }
 
-// back_to_particles_3D(1) from the float-float copies of the velocity and
-// stretching (written with them by velocity_and_stretching).
-void m2p_step(vpmg_handle* h, bool write_up, bool euler, double dt, const double uinf[3]) {
+// back_to_particles_3D(1): FP64 from the velocity and stretching fields, or
+// float-float from their copies (written with them by
+// velocity_and_stretching).
+void m2p_fields(vpmg_handle* h, int up_mode, bool euler, double dt, const double uinf[3]) {
   const size_t N = h->gglob.count();
   const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
-  const float2* V[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
-  const float2* G[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
-  m2p(h->parts, mg, h->bins, V, G, write_up, euler, dt, uinf, h->stream);
+  if (h->arith == VPMG_ARITH_FF48) {
+    const float2* V[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
+    const float2* G[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
+    m2p(h->parts, mg, h->bins, V, G, up_mode, euler, dt, uinf, h->stream);
+  } else {
+    const double* V[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
+    const double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
+    m2p(h->parts, mg, h->bins, V, G, up_mode, euler, dt, uinf, h->stream);
+  }
+}
+void m2p_step(vpmg_handle* h, int up_mode, bool euler, double dt, const double uinf[3]) {
+  m2p_fields(h, up_mode, euler, dt, uinf);
   ev_mark(h, 8);
 }
 
@@ -464,6 +492,14 @@ void download_particles(vpmg_handle* h, double* xp, double* qp, int n) {
   VPMG_CUDA(cudaMemcpyAsync(xp, h->stage.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->stream));
   VPMG_CUDA(cudaMemcpyAsync(qp, h->stage.p + 3 * (size_t)n, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, h->stream));
   VPMG_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+// The caller's UP(3, n) into the device UP array, which back_to_particles
+// then adds to (source/vpm_time.f90:92-94).
+void upload_up(vpmg_handle* h, const double* up, int n) {
+  VPMG_CHECK(up, VPMG_ERR_ARG, "UP is null");
+  if (n > 0)
+    VPMG_CUDA(cudaMemcpyAsync(h->parts.up.p, up, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, h->stream));
 }
 
 void finish_phase_times(vpmg_handle* h) {
@@ -668,7 +704,7 @@ void step_head(vpmg_handle* h) {
 void step_tail(vpmg_handle* h, double dt, const double u0[3], int do_remesh) {
   poisson_tail(h);
   field_velocity(h);
-  m2p_step(h, true, true, dt, u0);
+  m2p_step(h, kUpSet, true, dt, u0);
   if (do_remesh) remesh(h);
   else ev_mark(h, 9);
 }
@@ -679,7 +715,7 @@ void one_step(vpmg_handle* h, double dt, const double uinf[3], int do_remesh) {
   ev_mark(h, 0);
   bin_particles(h->parts, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
   field_step(h);
-  m2p_step(h, true, true, dt, u0);
+  m2p_step(h, kUpSet, true, dt, u0);
   if (do_remesh) remesh(h);
   else ev_mark(h, 9);
 }
@@ -1264,6 +1300,31 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
   });
 }
 
+double vpmg_projection_fun(int itype, double x) {
+  // the projection kernels of pmproject.f90:391-431 on |x|, as the device
+  // kernels evaluate them
+  const double a = std::fabs(x);
+  switch (itype) {
+    case 2: return a > 1.0 ? 0.0 : 1.0 - a;
+    case 3:
+      if (a > 1.5) return 0.0;
+      if (a >= 0.5) return 0.5 * (-a + 1.5) * (-a + 1.5);
+      return 0.5 * (a + 1.5) * (a + 1.5) - 1.5 * (a + 0.5) * (a + 0.5);
+    case 4:
+      if (a > 2.0) return 0.0;
+      if (a >= 1.0) return 0.5 * ((2.0 - a) * (2.0 - a)) * (1.0 - a);
+      return 1.0 - 2.5 * (a * a) + 1.5 * (a * a * a);
+    case 5:
+    case 6: {
+      const double lim = itype == 5 ? 0.5 : 1.0;
+      if (a <= lim) return 1.0 - a * a;
+      if (a <= lim + 1.0) return 0.5 * (1.0 - a) * (2.0 - a);
+      return 0.0;
+    }
+    default: return 0.0;
+  }
+}
+
 int vpmg_host_euler(double* xp, double* qp, const double* up, const double* gp, int n, double dt,
                     const double uinf[3]) {
   if (n < 0 || (n > 0 && (!xp || !qp || !up || !gp))) return VPMG_ERR_ARG;
@@ -1405,16 +1466,19 @@ int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int
       double* Vv[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
       double* G[3] = {comp(h->def, N, 0), comp(h->def, N, 1), comp(h->def, N, 2)};
       deposit(h->parts, mg, h->bins, R, h->stream);
-      float2* VF[3] = {h->vel_ff.p, h->vel_ff.p + N, h->vel_ff.p + 2 * N};
-      float2* GF[3] = {h->def_ff.p, h->def_ff.p + N, h->def_ff.p + 2 * N};
+      float2* VF[3], * GF[3];
+      ff_fields(h, VF, GF);
+      float2* const* vf = VF[0] ? VF : nullptr;
+      float2* const* gf = GF[0] ? GF : nullptr;
       if (whattodo == 1) {
         poisson_part(h);
-        velocity_and_stretching(h->sz.nn, h->sz.dpm, S, R, Vv, G, h->stream, 1, VF, GF);
+        velocity_and_stretching(h->sz.nn, h->sz.dpm, S, R, Vv, G, h->stream, 1, vf, gf);
       } else {
         VPMG_CHECK(up && gp, VPMG_ERR_ARG, "UP or GP is null");
-        velocity_and_stretching(h->sz.nn, h->sz.dpm, S, R, Vv, G, h->stream, 2, VF, GF);
+        velocity_and_stretching(h->sz.nn, h->sz.dpm, S, R, Vv, G, h->stream, 2, vf, gf);
         const double u0[3] = {0.0, 0.0, 0.0};
-        m2p_step(h, true, false, 0.0, u0);
+        upload_up(h, up, *nvr);
+        m2p_step(h, kUpAdd, false, 0.0, u0);
         VPMG_CUDA(cudaMemcpyAsync(up, h->parts.up.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost,
                                   h->stream));
         VPMG_CUDA(cudaMemcpyAsync(gp, h->parts.gp.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost,
@@ -1439,7 +1503,7 @@ int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int
       const double* Vp[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
       const double* Sp[3] = {S[0], S[1], S[2]};
       const double u0[3] = {0, 0, 0};
-      m2p(h->parts, mg, h->bins, Vp, Sp, true, false, 0.0, u0, h->stream);  // GP = vol I(X) SOL; UP untouched
+      m2p(h->parts, mg, h->bins, Vp, Sp, kUpSet, false, 0.0, u0, h->stream);  // GP = vol I(X) SOL; UP untouched
       VPMG_CUDA(cudaMemcpyAsync(gp, h->parts.gp.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost,
                                 h->stream));
       VPMG_CUDA(cudaStreamSynchronize(h->stream));
@@ -1451,7 +1515,8 @@ int vpmg_vpm(vpmg_handle* h, double* xp, double* qp, double* up, double* gp, int
     bin_particles(h->parts, mesh_dev(h->gglob, h->cfg.interf_iproj), h->bins, h->stream);
     field_step(h);
     if (h->out_flags) step_writers(h, ntime);
-    m2p_step(h, true, false, 0.0, u0);
+    upload_up(h, up, *nvr);
+    m2p_step(h, kUpAdd, false, 0.0, u0);  // UP = UP + interpolated velocity, GP overwritten
     VPMG_CUDA(cudaMemcpyAsync(up, h->parts.up.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost, h->stream));
     VPMG_CUDA(cudaMemcpyAsync(gp, h->parts.gp.p, sizeof(double) * 3 * (size_t)*nvr, cudaMemcpyDeviceToHost, h->stream));
     VPMG_CUDA(cudaStreamSynchronize(h->stream));
@@ -1488,11 +1553,11 @@ int vpmg_pmesh(vpmg_handle* h, double* const sol[3], const double* const rhs[3],
     DirichletPlan dp;
     if (iynbc == 1) {
       const int full[6] = {0, 0, 0, nn[0] - 1, nn[1] - 1, nn[2] - 1};
-      dirichlet_prepare(dp, nn, full, dpm, h->stream);
+      dirichlet_prepare(dp, nn, full, dpm, h->stream, h->arith);
       w.ensure((size_t)dp.m[0] * dp.m[1] * dp.m[2]);
       fill_zero(s0.p, n, h->stream);
       BoundaryOp bo;
-      boundary_prepare(bo, g, itree == 1 ? levmax : 0, h->op_budget, h->stream, h->cfg.ibctyp, itree == 1);
+      boundary_prepare(bo, g, itree == 1 ? levmax : 0, h->op_budget, h->stream, h->cfg.ibctyp, itree == 1, h->arith);
       for (int c = 0; c < 3; ++c) {
         dirichlet_solve(dp, r.p + c * n, s0.p, true, w.p, h->stream);
         boundary_panels(bo, g, s0.p, c, h->stream);
@@ -1503,7 +1568,7 @@ int vpmg_pmesh(vpmg_handle* h, double* const sol[3], const double* const rhs[3],
       VPMG_CUDA(cudaStreamSynchronize(h->stream));
     } else {
       const int box[6] = {nn_bl[0] - 1, nn_bl[1] - 1, nn_bl[2] - 1, nn_bl[3] - 1, nn_bl[4] - 1, nn_bl[5] - 1};
-      dirichlet_prepare(dp, nn, box, dpm, h->stream);
+      dirichlet_prepare(dp, nn, box, dpm, h->stream, h->arith);
       w.ensure((size_t)dp.m[0] * dp.m[1] * dp.m[2]);
       for (int c = 0; c < 3; ++c) dirichlet_solve(dp, r.p + c * n, s.p + c * n, false, w.p, h->stream);
     }
@@ -1594,6 +1659,32 @@ int vpmg_dst_tiles(const vpmg_handle* h, int pairs[6]) {
   return VPMG_OK;
 }
 
+int vpmg_set_arithmetic(vpmg_handle* h, int arith) {
+  if (!h) return VPMG_ERR_ARG;
+  if (arith != VPMG_ARITH_FP64 && arith != VPMG_ARITH_FF48) return VPMG_ERR_ARG;
+  if (arith == h->arith) return VPMG_OK;
+  return guarded(h, [&] {
+    VPMG_CUDA(cudaStreamSynchronize(h->stream));
+    // captured graphs hold the other arithmetic's kernels and buffers
+    if (h->graph.exec) {
+      VPMG_CUDA(cudaGraphExecDestroy(h->graph.exec));
+      h->graph.exec = nullptr;
+    }
+    vpmg::hx::destroy_adjoint(h);
+    h->arith = arith;
+    if (h->sized) {
+      h->prepared = false;
+      prepare(h);  // plans, recorded operators and particle records in the new arithmetic
+    }
+  });
+}
+
+int vpmg_get_arithmetic(const vpmg_handle* h, int* arith) {
+  if (!h || !arith) return VPMG_ERR_ARG;
+  *arith = h->arith;
+  return VPMG_OK;
+}
+
 int vpmg_set_operator_budget(vpmg_handle* h, long long bytes) {
   if (!h) return VPMG_ERR_ARG;
   h->op_budget = bytes;
@@ -1617,6 +1708,9 @@ void sync_np(vpmg_handle* h) { ::sync_np(h); }
 void upload_particles(vpmg_handle* h, const double* xp, const double* qp, int n) { ::upload_particles(h, xp, qp, n); }
 void download_particles(vpmg_handle* h, double* xp, double* qp, int n) { ::download_particles(h, xp, qp, n); }
 void poisson_part(vpmg_handle* h) { ::poisson_part(h); }
+void m2p_fields(vpmg_handle* h, int up_mode, bool euler, double dt, const double uinf[3]) {
+  ::m2p_fields(h, up_mode, euler, dt, uinf);
+}
 void step_on_stream(vpmg_handle* h, double dt) {
   const double u0[3] = {0.0, 0.0, 0.0};
   if (h->keep_intermediates || h->no_graphs) {

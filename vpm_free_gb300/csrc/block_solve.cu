@@ -18,9 +18,10 @@
 // those of the full discrete solves (same linear algebra, different
 // rounding).
 #include <cmath>
+#include <cstring>
 
+#include "arith.cuh"
 #include "block_solve.h"
-#include "ff.cuh"
 
 namespace vpmg {
 
@@ -28,28 +29,35 @@ namespace {
 
 constexpr int kLines = 16;  // lines per CTA of the x dot-product kernel
 
-// The dot products below run in float-float arithmetic (ff.cuh): the
-// sine rows are stored as float-float pairs, W is split by bit operations
+__device__ __forceinline__ double shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ float2 shfl_xor(float2 v, int m) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+// The dot products below run in the policy's arithmetic (arith.cuh): the
+// sine rows are stored in it (doubles, or float-float pairs), W enters it
 // as it is staged, and each result is joined back into a double.
 
 // out[i + nsel*(q + m1*kk)] = sum_p S[i][p] * W[p + m0*(q + m1*k)],  k = klist ? klist[kk] : kk
+template <class A>
 __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W, int m0, int m1, int nk,
-                                                   const int* __restrict__ klist, const float2* __restrict__ S,
+                                                   const int* __restrict__ klist, const typename A::R* __restrict__ S,
                                                    int nsel, double* __restrict__ out) {
-  extern __shared__ float2 smf[];
-  float2* tile = smf;                     // kLines x m0
-  float2* Ss = smf + (size_t)kLines * m0;  // nsel x m0
+  using R = typename A::R;
+  extern __shared__ double smx[];
+  R* tile = reinterpret_cast<R*>(smx);       // kLines x m0
+  R* Ss = tile + (size_t)kLines * m0;         // nsel x m0
   const int nlines = m1 * nk;
   const int l0 = blockIdx.x * kLines;
   for (int t = threadIdx.x; t < nsel * m0; t += blockDim.x) Ss[t] = S[t];
   for (int t = threadIdx.x; t < kLines * m0; t += blockDim.x) {
     const int li = t / m0, p = t - li * m0;
     const int l = l0 + li;
-    float2 v = make_float2(0.0f, 0.0f);
+    R v = A::zero();
     if (l < nlines) {
       const int q = l % m1, kk = l / m1;
       const int k = klist ? klist[kk] : kk;
-      v = ff::split(W[(size_t)p + (size_t)m0 * (q + (size_t)m1 * k)]);
+      v = A::from(W[(size_t)p + (size_t)m0 * (q + (size_t)m1 * k)]);
     }
     tile[t] = v;
   }
@@ -58,35 +66,35 @@ __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W,
   // two up to 8, when the CTA has fewer outputs than threads), each summing
   // every R-th term; their partials meet in a fixed shuffle tree.
   const int nout = kLines * nsel;
-  int R = 1;
-  while (R < 8 && nout * R * 2 <= (int)blockDim.x) R *= 2;
-  const int r = threadIdx.x % R;
-  for (int o0 = 0; o0 < nout; o0 += blockDim.x / R) {
-    const int o = o0 + threadIdx.x / R;
+  int Rs = 1;
+  while (Rs < 8 && nout * Rs * 2 <= (int)blockDim.x) Rs *= 2;
+  const int r = threadIdx.x % Rs;
+  for (int o0 = 0; o0 < nout; o0 += blockDim.x / Rs) {
+    const int o = o0 + threadIdx.x / Rs;
     const int li = o % kLines, i = o / kLines;
     const int l = l0 + li;
     const bool ok = o < nout && l < nlines;
-    float2 a0 = make_float2(0.0f, 0.0f), a1 = a0, a2 = a0, a3 = a0;
+    R a0 = A::zero(), a1 = a0, a2 = a0, a3 = a0;
     if (ok) {
-      const float2* a = tile + (size_t)li * m0;
-      const float2* b = Ss + (size_t)i * m0;
+      const R* a = tile + (size_t)li * m0;
+      const R* b = Ss + (size_t)i * m0;
       int p = r;
-      for (; p + 3 * R < m0; p += 4 * R) {
-        a0 = ff::fma(a[p], b[p], a0);
-        a1 = ff::fma(a[p + R], b[p + R], a1);
-        a2 = ff::fma(a[p + 2 * R], b[p + 2 * R], a2);
-        a3 = ff::fma(a[p + 3 * R], b[p + 3 * R], a3);
+      for (; p + 3 * Rs < m0; p += 4 * Rs) {
+        a0 = A::fma(a[p], b[p], a0);
+        a1 = A::fma(a[p + Rs], b[p + Rs], a1);
+        a2 = A::fma(a[p + 2 * Rs], b[p + 2 * Rs], a2);
+        a3 = A::fma(a[p + 3 * Rs], b[p + 3 * Rs], a3);
       }
-      for (; p < m0; p += R) a0 = ff::fma(a[p], b[p], a0);
+      for (; p < m0; p += Rs) a0 = A::fma(a[p], b[p], a0);
     }
-    float2 v = ff::add(ff::add(a0, a1), ff::add(a2, a3));
-    for (int m = 1; m < R; m <<= 1) {
-      const float2 w = make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
-      v = (r & m) ? ff::add(w, v) : ff::add(v, w);
+    R v = A::add(A::add(a0, a1), A::add(a2, a3));
+    for (int m = 1; m < Rs; m <<= 1) {
+      const R w = shfl_xor(v, m);
+      v = (r & m) ? A::add(w, v) : A::add(v, w);
     }
     if (ok && r == 0) {
       const int q = l % m1, kk = l / m1;
-      out[i + (size_t)nsel * (q + (size_t)m1 * kk)] = ff::to_double(v);
+      out[i + (size_t)nsel * (q + (size_t)m1 * kk)] = A::to(v);
     }
   }
 }
@@ -98,11 +106,15 @@ __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W,
 constexpr int kColTile = 32;
 // A second row set (S2, nsel2 -> out2, same layout) is served from the
 // same staged tile when given, so two face sets cost one pass over W.
+template <class A>
 __global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W, int m0, int m1, int nk,
-                                                   const int* __restrict__ klist, const float2* __restrict__ S,
-                                                   int nsel, double* __restrict__ out, const float2* __restrict__ S2,
-                                                   int nsel2, double* __restrict__ out2) {
-  extern __shared__ float2 tile[];  // [q][lane], m1 x kColTile; then the partial sums [row][lane]
+                                                   const int* __restrict__ klist, const typename A::R* __restrict__ S,
+                                                   int nsel, double* __restrict__ out,
+                                                   const typename A::R* __restrict__ S2, int nsel2,
+                                                   double* __restrict__ out2) {
+  using R = typename A::R;
+  extern __shared__ double smy[];
+  R* tile = reinterpret_cast<R*>(smy);  // [q][lane], m1 x kColTile; then the partial sums [row][lane]
   const int p0 = blockIdx.x * kColTile;
   const int kk = blockIdx.y;
   const int k = klist ? klist[kk] : kk;
@@ -110,45 +122,45 @@ __global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W,
   const int lane = threadIdx.x % kColTile, row = threadIdx.x / kColTile, rows = blockDim.x / kColTile;
   const int p = p0 + lane;
   for (int q = row; q < m1; q += rows)
-    tile[q * kColTile + lane] = (p < m0) ? ff::split(plane[(size_t)m0 * q + p]) : make_float2(0.0f, 0.0f);
+    tile[q * kColTile + lane] = (p < m0) ? A::from(plane[(size_t)m0 * q + p]) : A::zero();
   __syncthreads();
   // R rows share one output row set when there are fewer outputs than rows
   // (R a power of two), each summing every R-th q; the partials are added
   // in row order through shared memory.
   const int nout = nsel + nsel2;
-  int R = 1;
-  while (R < rows && nout * R * 2 <= rows) R *= 2;
-  const int r = row % R;
-  float2* partial = tile + (size_t)m1 * kColTile;
-  for (int j0 = 0; j0 < nout; j0 += rows / R) {
-    const int jj = j0 + row / R;
-    float2 a0 = make_float2(0.0f, 0.0f), a1 = a0, a2 = a0, a3 = a0;
+  int Rs = 1;
+  while (Rs < rows && nout * Rs * 2 <= rows) Rs *= 2;
+  const int r = row % Rs;
+  R* partial = tile + (size_t)m1 * kColTile;
+  for (int j0 = 0; j0 < nout; j0 += rows / Rs) {
+    const int jj = j0 + row / Rs;
+    R a0 = A::zero(), a1 = a0, a2 = a0, a3 = a0;
     if (jj < nout && p < m0) {
       const bool second = jj >= nsel;
       const int j = second ? jj - nsel : jj;
-      const float2* Sj = (second ? S2 : S) + (size_t)j * m1;
+      const R* Sj = (second ? S2 : S) + (size_t)j * m1;
       int q = r;
-      for (; q + 3 * R < m1; q += 4 * R) {
-        a0 = ff::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
-        a1 = ff::fma(__ldg(&Sj[q + R]), tile[(q + R) * kColTile + lane], a1);
-        a2 = ff::fma(__ldg(&Sj[q + 2 * R]), tile[(q + 2 * R) * kColTile + lane], a2);
-        a3 = ff::fma(__ldg(&Sj[q + 3 * R]), tile[(q + 3 * R) * kColTile + lane], a3);
+      for (; q + 3 * Rs < m1; q += 4 * Rs) {
+        a0 = A::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
+        a1 = A::fma(__ldg(&Sj[q + Rs]), tile[(q + Rs) * kColTile + lane], a1);
+        a2 = A::fma(__ldg(&Sj[q + 2 * Rs]), tile[(q + 2 * Rs) * kColTile + lane], a2);
+        a3 = A::fma(__ldg(&Sj[q + 3 * Rs]), tile[(q + 3 * Rs) * kColTile + lane], a3);
       }
-      for (; q < m1; q += R) a0 = ff::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
+      for (; q < m1; q += Rs) a0 = A::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
     }
-    float2 v = ff::add(ff::add(a0, a1), ff::add(a2, a3));
-    if (R > 1) {
+    R v = A::add(A::add(a0, a1), A::add(a2, a3));
+    if (Rs > 1) {
       partial[row * kColTile + lane] = v;
       __syncthreads();
       if (r == 0)
-        for (int m = 1; m < R; ++m) v = ff::add(v, partial[(row + m) * kColTile + lane]);
+        for (int m = 1; m < Rs; ++m) v = A::add(v, partial[(row + m) * kColTile + lane]);
       __syncthreads();
     }
     if (r == 0 && jj < nout && p < m0) {
       const bool second = jj >= nsel;
       const int j = second ? jj - nsel : jj;
-      if (second) out2[(size_t)p + (size_t)m0 * (j + (size_t)nsel2 * kk)] = ff::to_double(v);
-      else out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = ff::to_double(v);
+      if (second) out2[(size_t)p + (size_t)m0 * (j + (size_t)nsel2 * kk)] = A::to(v);
+      else out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = A::to(v);
     }
   }
 }
@@ -276,15 +288,21 @@ __global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict_
   }
 }
 
-// sin(pi (i+1)(p+1)/N) of the selected rows, as float-float pairs
-std::vector<float2> sine_rows(const std::vector<int>& sel, int m) {
-  std::vector<float2> S(sel.size() * (size_t)m);
+// sin(pi (i+1)(p+1)/N) of the selected rows, one 8-byte word each: the
+// double (FP64) or its float-float pair (hi, lo) in the word's bytes.
+std::vector<double> sine_rows(const std::vector<int>& sel, int m, int arith) {
+  std::vector<double> S(sel.size() * (size_t)m);
   const double N = m + 1;
   for (size_t i = 0; i < sel.size(); ++i)
     for (int p = 0; p < m; ++p) {
       const double v = std::sin(kPI * (double)(sel[i] + 1) * (double)(p + 1) / N);
-      const float hi = (float)v;
-      S[i * m + p] = make_float2(hi, (float)(v - (double)hi));
+      if (arith == VPMG_ARITH_FF48) {
+        const float hi = (float)v;
+        const float2 f = make_float2(hi, (float)(v - (double)hi));
+        std::memcpy(&S[i * m + p], &f, sizeof(double));
+      } else {
+        S[i * m + p] = v;
+      }
     }
   return S;
 }
@@ -304,42 +322,52 @@ std::vector<int> plus1(const std::vector<int>& v) {
 size_t g_partial_smem = 0;  // dynamic shared memory granted to k_partial_x so far
 
 // Raises k_partial_x's shared-memory limit (called at set-up, outside any
-// stream capture).
+// stream capture).  Both arithmetics stage 8 bytes per value.
 void partial_x_reserve(int m0, int nsel) {
-  const size_t sm = sizeof(float2) * ((size_t)kLines * m0 + (size_t)nsel * m0);
+  const size_t sm = sizeof(double) * ((size_t)kLines * m0 + (size_t)nsel * m0);
   VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
   if (sm > g_partial_smem) {
-    VPMG_CUDA(cudaFuncSetAttribute(k_partial_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    VPMG_CUDA(cudaFuncSetAttribute(k_partial_x<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    VPMG_CUDA(cudaFuncSetAttribute(k_partial_x<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     g_partial_smem = sm;
   }
 }
 
-void partial_x(const double* W, int m0, int m1, int nk, const int* klist, const float2* S, int nsel, double* out,
-               cudaStream_t s) {
+void partial_x(int arith, const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel,
+               double* out, cudaStream_t s) {
   const int nlines = m1 * nk;
-  const size_t sm = sizeof(float2) * ((size_t)kLines * m0 + (size_t)nsel * m0);
+  const size_t sm = sizeof(double) * ((size_t)kLines * m0 + (size_t)nsel * m0);
   VPMG_CHECK(sm <= g_partial_smem, VPMG_ERR_STATE, "k_partial_x shared memory not reserved");
-  k_partial_x<<<(nlines + kLines - 1) / kLines, 128, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out);
+  const unsigned g = (nlines + kLines - 1) / kLines;
+  if (arith == VPMG_ARITH_FF48)
+    k_partial_x<FF><<<g, 128, sm, s>>>(W, m0, m1, nk, klist, reinterpret_cast<const float2*>(S), nsel, out);
+  else
+    k_partial_x<F64><<<g, 128, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out);
   VPMG_LAUNCHED();
 }
 
 size_t g_partial_y_smem = 0;  // dynamic shared memory granted to k_partial_y so far
 
 void partial_y_reserve(int m1) {
-  const size_t sm = sizeof(float2) * ((size_t)m1 + 8) * kColTile;
+  const size_t sm = sizeof(double) * ((size_t)m1 + 8) * kColTile;
   VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
   if (sm > g_partial_y_smem) {
-    VPMG_CUDA(cudaFuncSetAttribute(k_partial_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    VPMG_CUDA(cudaFuncSetAttribute(k_partial_y<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    VPMG_CUDA(cudaFuncSetAttribute(k_partial_y<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     g_partial_y_smem = sm;
   }
 }
 
-void partial_y(const double* W, int m0, int m1, int nk, const int* klist, const float2* S, int nsel, double* out,
-               cudaStream_t s, const float2* S2 = nullptr, int nsel2 = 0, double* out2 = nullptr) {
-  const size_t sm = sizeof(float2) * ((size_t)m1 + 8) * kColTile;  // tile + partial sums of 8 rows
+void partial_y(int arith, const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel,
+               double* out, cudaStream_t s, const double* S2 = nullptr, int nsel2 = 0, double* out2 = nullptr) {
+  const size_t sm = sizeof(double) * ((size_t)m1 + 8) * kColTile;  // tile + partial sums of 8 rows
   VPMG_CHECK(sm <= g_partial_y_smem, VPMG_ERR_STATE, "k_partial_y shared memory not reserved");
   dim3 g((m0 + kColTile - 1) / kColTile, nk);
-  k_partial_y<<<g, 256, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out, S2, nsel2, out2);
+  if (arith == VPMG_ARITH_FF48)
+    k_partial_y<FF><<<g, 256, sm, s>>>(W, m0, m1, nk, klist, reinterpret_cast<const float2*>(S), nsel, out,
+                                      reinterpret_cast<const float2*>(S2), nsel2, out2);
+  else
+    k_partial_y<F64><<<g, 256, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out, S2, nsel2, out2);
   VPMG_LAUNCHED();
 }
 
@@ -354,6 +382,7 @@ void scatter3(const double* src, int na, int nb, int nc, const int* ia, const in
 }  // namespace
 
 void BlockSolve::prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoarse) {
+  arith = P.arith;
   for (int d = 0; d < 3; ++d) { dims[d] = P.dims[d]; m[d] = P.m[d]; }
   VPMG_CHECK(m[0] >= 8 && m[1] >= 8 && m[2] >= 8, VPMG_ERR_UNSUPPORTED, "block too small for the partial solve");
   const size_t nint = (size_t)m[0] * m[1] * m[2];
@@ -362,9 +391,9 @@ void BlockSolve::prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoar
   // normal-derivative layers: interior indices 0..3 and m-4..m-1
   std::vector<int> fx = {0, 1, 2, 3, m[0] - 4, m[0] - 3, m[0] - 2, m[0] - 1};
   std::vector<int> fylo = {0, 1, 2, 3}, fyhi = {m[1] - 4, m[1] - 3, m[1] - 2, m[1] - 1};
-  up(S_fx, sine_rows(fx, m[0]));
-  up(S_fy_lo, sine_rows(fylo, m[1]));
-  up(S_fy_hi, sine_rows(fyhi, m[1]));
+  up(S_fx, sine_rows(fx, m[0], arith));
+  up(S_fy_lo, sine_rows(fylo, m[1], arith));
+  up(S_fy_hi, sine_rows(fyhi, m[1], arith));
   up(l_fx, plus1(fx));
   // inner-box faces: 1-based node nnbl_bl -> interior index nnbl_bl - 2
   for (int d = 0; d < 3; ++d) {
@@ -374,9 +403,9 @@ void BlockSolve::prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoar
                "inner block box outside the padded block");
   }
   std::vector<int> ix = {inner_lo[0], inner_hi[0]};
-  up(S_ix, sine_rows(ix, m[0]));
-  up(S_iy_lo, sine_rows({inner_lo[1]}, m[1]));
-  up(S_iy_hi, sine_rows({inner_hi[1]}, m[1]));
+  up(S_ix, sine_rows(ix, m[0], arith));
+  up(S_iy_lo, sine_rows({inner_lo[1]}, m[1], arith));
+  up(S_iy_hi, sine_rows({inner_hi[1]}, m[1], arith));
   up(l_ix, plus1(ix));
   // samples: 0-based nodes nc*t inside the block interior -> interior index nc*t - 1
   auto samples = [&](int d) {
@@ -386,8 +415,8 @@ void BlockSolve::prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoar
   };
   std::vector<int> sx = samples(0), sy = samples(1), sz = samples(2);
   nsx = (int)sx.size(); nsy = (int)sy.size(); nsz = (int)sz.size();
-  up(S_sx, sine_rows(sx, m[0]));
-  up(S_sy, sine_rows(sy, m[1]));
+  up(S_sx, sine_rows(sx, m[0], arith));
+  up(S_sy, sine_rows(sy, m[1], arith));
   up(l_sx, plus1(sx));
   up(l_sy, plus1(sy));
   up(l_sz, sz);  // plane list (interior index) for the y dots
@@ -425,13 +454,13 @@ void block_solve_zero_bc(BlockSolve& B, DirichletPlan& P, const double* rhs_c, i
   k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(g, B.W.p, P.rinvd.p, m0, m1, m2, 0, F);
   VPMG_LAUNCHED();
   // x faces: 8 layers by dot products along x, then inverse y
-  partial_x(B.W.p, m0, m1, m2, nullptr, B.S_fx.p, 8, B.X8.p, s);
+  partial_x(B.arith, B.W.p, m0, m1, m2, nullptr, B.S_fx.p, 8, B.X8.p, s);
   dst_lines_y(P.fy, B.X8.p, 8, m1, m2, s);
   scatter3(B.X8.p, 8, m1, m2, B.l_fx.p, nullptr, nullptr, 1, sol0, B.dims, s);
   // y faces: 4 + 4 rows by dot products along y, then inverse x
   const int my[3] = {m0, 4, m2};
   double* Y4b = B.Y4.p + (size_t)m0 * 4 * m2;
-  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_fy_lo.p, 4, B.Y4.p, s, B.S_fy_hi.p, 4, Y4b);
+  partial_y(B.arith, B.W.p, m0, m1, m2, nullptr, B.S_fy_lo.p, 4, B.Y4.p, s, B.S_fy_hi.p, 4, Y4b);
   const int olo[3] = {1, 1, 1};
   dst_x_inv_to_box(P.fx, B.Y4.p, sol0, B.dims, olo, my, s);
   const int ohi[3] = {1, 1 + m1 - 4, 1};
@@ -473,20 +502,20 @@ void block_solve_bc(BlockSolve& B, DirichletPlan& P, int c, double* sol_c, cudaS
   k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(g, B.W.p, P.rinvd.p, m0, m1, m2, 1, F);
   VPMG_LAUNCHED();
   // inner-box x faces
-  partial_x(B.W.p, m0, m1, m2, nullptr, B.S_ix.p, 2, B.X2.p, s);
+  partial_x(B.arith, B.W.p, m0, m1, m2, nullptr, B.S_ix.p, 2, B.X2.p, s);
   dst_lines_y(P.fy, B.X2.p, 2, m1, m2, s);
   scatter3(B.X2.p, 2, m1, m2, B.l_ix.p, nullptr, nullptr, 1, sol_c, B.dims, s);
   // inner-box y faces
   const int m1r[3] = {m0, 1, m2};
   double* Y1b = B.Y1.p + (size_t)m0 * m2;
-  partial_y(B.W.p, m0, m1, m2, nullptr, B.S_iy_lo.p, 1, B.Y1.p, s, B.S_iy_hi.p, 1, Y1b);
+  partial_y(B.arith, B.W.p, m0, m1, m2, nullptr, B.S_iy_lo.p, 1, B.Y1.p, s, B.S_iy_hi.p, 1, Y1b);
   const int oylo[3] = {1, B.inner_lo[1] + 1, 1};
   dst_x_inv_to_box(P.fx, B.Y1.p, sol_c, B.dims, oylo, m1r, s);
   const int oyhi[3] = {1, B.inner_hi[1] + 1, 1};
   dst_x_inv_to_box(P.fx, Y1b, sol_c, B.dims, oyhi, m1r, s);
   // interior samples: dots along y on the sampled planes, then along x
-  partial_y(B.W.p, m0, m1, B.nsz, B.l_sz.p, B.S_sy.p, B.nsy, B.Ys.p, s);
-  partial_x(B.Ys.p, m0, B.nsy, B.nsz, nullptr, B.S_sx.p, B.nsx, B.XS.p, s);
+  partial_y(B.arith, B.W.p, m0, m1, B.nsz, B.l_sz.p, B.S_sy.p, B.nsy, B.Ys.p, s);
+  partial_x(B.arith, B.Ys.p, m0, B.nsy, B.nsz, nullptr, B.S_sx.p, B.nsx, B.XS.p, s);
   scatter3(B.XS.p, B.nsx, B.nsy, B.nsz, B.l_sx.p, B.l_sy.p, B.l_idz.p, 0, sol_c, B.dims, s);
   // inner-box z faces: full inverse of the two planes (in place, after the dots)
   const int mz1[3] = {m0, m1, 1};

@@ -12,8 +12,10 @@ struct BlockSolve {
   int nsx = 0, nsy = 0, nsz = 0;
   DBuf<double> ghat;        // 3 * interior: forward transforms of the RHS
   DBuf<double> W;           // interior: Thomas output
-  // sine rows sin(pi (i+1)(p+1)/N) of the selected interior indices, float-float pairs
-  DBuf<float2> S_fx, S_fy_lo, S_fy_hi, S_ix, S_iy_lo, S_iy_hi, S_sx, S_sy;
+  int arith = VPMG_ARITH_FP64;  // the plan's arithmetic
+  // sine rows sin(pi (i+1)(p+1)/N) of the selected interior indices, one
+  // 8-byte word each: a double, or a float-float pair (arith)
+  DBuf<double> S_fx, S_fy_lo, S_fy_hi, S_ix, S_iy_lo, S_iy_hi, S_sx, S_sy;
   DBuf<double> e_x1, e_xN, e_y1, e_yN;  // sines of the first/last interior layer
   DBuf<int> l_fx, l_ix, l_sx, l_sy, l_sz, l_idy, l_idz;  // node lists for scatters / plane lists
   DBuf<double> X8, Y4, X2, Y1, Ys, XS;  // compact partial results

@@ -53,6 +53,7 @@ struct WalkDev {
   int bctype;     // 2 or 3
   int tree;       // 1: Bounds3d_lev walk; 0: untreed sum (levmax = 0)
   int dense;      // 1: the coarsest level goes to the dense block (count / fill)
+  int ff;         // 1: recorded weights as float-float pairs, 0: as doubles
   const int* tgt_frame;
   PanelFrame frame[6];
 };
@@ -185,14 +186,17 @@ __global__ void k_walk(WalkDev W, double* __restrict__ o0, double* __restrict__ 
       w = (r > 1e-05) ? __ddiv_rn(DS, r) : -2.0 * __dsqrt_rn(DS) * W.lg;
     }
     if (MODE == kFill) {
+      // the weight word: the double itself, or its float-float pair
       const float hi = __double2float_rn(w);
       const float2 wf = make_float2(hi, __double2float_rn(w - (double)hi));
+      const double word = W.ff ? *reinterpret_cast<const double*>(&wf) : w;
       if (W.dense && L == W.levmax) {
         const int cc2 = c - W.top0;  // [chunk][cell pair][lane][2]
-        wtop[(((size_t)(t >> 5) * ((W.ntop + 1) >> 1) + (cc2 >> 1)) * 32 + (t & 31)) * 2 + (cc2 & 1)] = wf;
+        reinterpret_cast<double*>(wtop)[(((size_t)(t >> 5) * ((W.ntop + 1) >> 1) + (cc2 >> 1)) * 32 + (t & 31)) * 2 +
+                                         (cc2 & 1)] = word;
       } else {
         col[out] = cc;
-        wgt[out] = wf;
+        reinterpret_cast<double*>(wgt)[out] = word;
         ++out;
       }
     } else if (MODE == kTranspose) {
@@ -233,19 +237,58 @@ __device__ __forceinline__ void ff_mac(FF& a, float2 w, float2 s) {
   a.hi = t;
 }
 
-// Sources to float-float pairs, once per apply, packed per cell as
+// Multiply-accumulate policies of the recorded operator's kernels.  A
+// weight is 8 bytes (W), a cell's packed sources (s0, s1, s2, 0) are 32
+// bytes read as two 16-byte halves (H), each holding two values (V).
+//   MacFF: float-float pairs, products and sums on the FP32 pipes;
+//   Mac64: IEEE FP64, one DFMA per product (the reference's arithmetic).
+struct MacFF {
+  using W = float2;
+  using V = float2;
+  using H = float4;
+  using W2 = float4;  // two weights (cells 2i, 2i+1 of the dense block)
+  using Acc = FF;
+  static constexpr bool kFF = true;
+  __device__ __forceinline__ static V v0(H h) { return make_float2(h.x, h.y); }
+  __device__ __forceinline__ static V v1(H h) { return make_float2(h.z, h.w); }
+  __device__ __forceinline__ static W wa(W2 w) { return make_float2(w.x, w.y); }
+  __device__ __forceinline__ static W wb(W2 w) { return make_float2(w.z, w.w); }
+  __device__ __forceinline__ static void mac(Acc& a, W w, V x) { ff_mac(a, w, x); }
+  __device__ __forceinline__ static double fin(const Acc& a) { return (double)a.hi + (double)a.lo; }
+  __device__ __forceinline__ static V vmake(double d) {  // rounded hi, then the rest
+    const float hi = __double2float_rn(d);
+    return make_float2(hi, __double2float_rn(d - (double)hi));
+  }
+  __device__ __forceinline__ static V vsplit(double d) { return ff::split(d); }
+};
+struct Acc64 {
+  double v = 0.0;
+};
+struct Mac64 {
+  using W = double;
+  using V = double;
+  using H = double2;
+  using W2 = double2;
+  using Acc = Acc64;
+  static constexpr bool kFF = false;
+  __device__ __forceinline__ static V v0(H h) { return h.x; }
+  __device__ __forceinline__ static V v1(H h) { return h.y; }
+  __device__ __forceinline__ static W wa(W2 w) { return w.x; }
+  __device__ __forceinline__ static W wb(W2 w) { return w.y; }
+  __device__ __forceinline__ static void mac(Acc& a, W w, V x) { a.v = fma(w, x, a.v); }
+  __device__ __forceinline__ static double fin(const Acc& a) { return a.v; }
+  __device__ __forceinline__ static V vmake(double d) { return d; }
+  __device__ __forceinline__ static V vsplit(double d) { return d; }
+};
+
+// Sources in the policy's arithmetic, once per apply, packed per cell as
 // (s0, s1, s2, 0): one 32-byte sector serves a gather of all components.
-__global__ void k_split(const double* __restrict__ x, int ncell, float2* __restrict__ out) {
+template <class M>
+__global__ void k_split(const double* __restrict__ x, int ncell, typename M::V* __restrict__ out) {
   const size_t n = 4 * (size_t)ncell;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const int cell = (int)(i >> 2), comp = (int)(i & 3);
-    float2 v = make_float2(0.0f, 0.0f);
-    if (comp < 3) {
-      const double d = x[(size_t)comp * ncell + cell];
-      const float hi = __double2float_rn(d);
-      v = make_float2(hi, __double2float_rn(d - (double)hi));
-    }
-    out[i] = v;
+    out[i] = M::vmake(comp < 3 ? x[(size_t)comp * ncell + cell] : 0.0);
   }
 }
 
@@ -257,119 +300,124 @@ __global__ void k_split(const double* __restrict__ x, int ncell, float2* __restr
 constexpr int kDenseTile = 512;  // cells per staged tile (16 KB of sources)
 // blockIdx.y = segment of cseg (even) cells; its partial sums go to
 // dsum[segment][component][node] (more, shorter warps: a fuller last wave).
-__global__ void __launch_bounds__(256) k_apply_dense(const float4* __restrict__ wtop, const float4* __restrict__ src,
-                                                     int top0, int ntop, int ntop2, int ntarget, int cseg,
-                                                     double* __restrict__ dsum) {
-  __shared__ float4 ss[2 * kDenseTile];
+template <class M>
+__global__ void __launch_bounds__(256) k_apply_dense(const typename M::W2* __restrict__ wtop,
+                                                     const typename M::H* __restrict__ src, int top0, int ntop,
+                                                     int ntop2, int ntarget, int cseg, double* __restrict__ dsum) {
+  using H = typename M::H;
+  using W2 = typename M::W2;
+  __shared__ H ss[2 * kDenseTile];
   const int lane = threadIdx.x & 31;
   const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const bool active = g < (ntarget + 31) / 32;
   const int cb = blockIdx.y * cseg, ce = min(ntop, cb + cseg);
   dsum += (size_t)blockIdx.y * 3 * ntarget;
-  FF f0, f1, f2, g0, g1, g2;
+  typename M::Acc f0, f1, f2, g0, g1, g2;
   for (int c0 = cb; c0 < ce; c0 += kDenseTile) {
     const int nc = min(kDenseTile, ce - c0);
     __syncthreads();
     for (int i = threadIdx.x; i < 2 * nc; i += blockDim.x) ss[i] = __ldg(&src[2 * (size_t)(top0 + c0) + i]);
     __syncthreads();
     if (!active) continue;
-    const float4* wp = wtop + ((size_t)g * ntop2 + (c0 >> 1)) * 32 + lane;
+    const W2* wp = wtop + ((size_t)g * ntop2 + (c0 >> 1)) * 32 + lane;
     int c = 0;
     for (; c + 7 < nc; c += 8) {
-      float4 w[4];
+      W2 w[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) w[u] = __ldg(&wp[(size_t)((c >> 1) + u) * 32]);
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const float4 a = ss[2 * (c + 2 * u)], z = ss[2 * (c + 2 * u) + 1];
-        const float4 a2 = ss[2 * (c + 2 * u + 1)], z2 = ss[2 * (c + 2 * u + 1) + 1];
-        const float2 wa = make_float2(w[u].x, w[u].y), wb = make_float2(w[u].z, w[u].w);
-        ff_mac(f0, wa, make_float2(a.x, a.y));
-        ff_mac(f1, wa, make_float2(a.z, a.w));
-        ff_mac(f2, wa, make_float2(z.x, z.y));
-        ff_mac(g0, wb, make_float2(a2.x, a2.y));
-        ff_mac(g1, wb, make_float2(a2.z, a2.w));
-        ff_mac(g2, wb, make_float2(z2.x, z2.y));
+        const H a = ss[2 * (c + 2 * u)], z = ss[2 * (c + 2 * u) + 1];
+        const H a2 = ss[2 * (c + 2 * u + 1)], z2 = ss[2 * (c + 2 * u + 1) + 1];
+        M::mac(f0, M::wa(w[u]), M::v0(a));
+        M::mac(f1, M::wa(w[u]), M::v1(a));
+        M::mac(f2, M::wa(w[u]), M::v0(z));
+        M::mac(g0, M::wb(w[u]), M::v0(a2));
+        M::mac(g1, M::wb(w[u]), M::v1(a2));
+        M::mac(g2, M::wb(w[u]), M::v0(z2));
       }
     }
     for (; c < nc; c += 2) {
-      const float4 w = __ldg(&wp[(size_t)(c >> 1) * 32]);
-      const float4 a = ss[2 * c], z = ss[2 * c + 1];
-      const float2 wa = make_float2(w.x, w.y);
-      ff_mac(f0, wa, make_float2(a.x, a.y));
-      ff_mac(f1, wa, make_float2(a.z, a.w));
-      ff_mac(f2, wa, make_float2(z.x, z.y));
+      const W2 w = __ldg(&wp[(size_t)(c >> 1) * 32]);
+      const H a = ss[2 * c], z = ss[2 * c + 1];
+      M::mac(f0, M::wa(w), M::v0(a));
+      M::mac(f1, M::wa(w), M::v1(a));
+      M::mac(f2, M::wa(w), M::v0(z));
       if (c + 1 < nc) {
-        const float4 a2 = ss[2 * (c + 1)], z2 = ss[2 * (c + 1) + 1];
-        const float2 wb = make_float2(w.z, w.w);
-        ff_mac(g0, wb, make_float2(a2.x, a2.y));
-        ff_mac(g1, wb, make_float2(a2.z, a2.w));
-        ff_mac(g2, wb, make_float2(z2.x, z2.y));
+        const H a2 = ss[2 * (c + 1)], z2 = ss[2 * (c + 1) + 1];
+        M::mac(g0, M::wb(w), M::v0(a2));
+        M::mac(g1, M::wb(w), M::v1(a2));
+        M::mac(g2, M::wb(w), M::v0(z2));
       }
     }
   }
   const int t = g * 32 + lane;
   if (active && t < ntarget) {
-    dsum[t] = ((double)f0.hi + (double)f0.lo) + ((double)g0.hi + (double)g0.lo);
-    dsum[ntarget + t] = ((double)f1.hi + (double)f1.lo) + ((double)g1.hi + (double)g1.lo);
-    dsum[2 * (size_t)ntarget + t] = ((double)f2.hi + (double)f2.lo) + ((double)g2.hi + (double)g2.lo);
+    dsum[t] = M::fin(f0) + M::fin(g0);
+    dsum[ntarget + t] = M::fin(f1) + M::fin(g1);
+    dsum[2 * (size_t)ntarget + t] = M::fin(f2) + M::fin(g2);
   }
 }
 
 // One warp per boundary node: lanes stride over the node's interaction
 // list (coalesced), fixed-shape shuffle reduction (deterministic); with
 // dsum, the dense block's partial sums join the warp's before the store.
+template <class M>
 __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__ rowptr, const int* __restrict__ col,
-                                                   const float2* __restrict__ wgt, const float4* __restrict__ src,
+                                                   const typename M::W* __restrict__ wgt,
+                                                   const typename M::H* __restrict__ src,
                                                    const int* __restrict__ tgt_node, int ntarget, double inv_pi4,
                                                    double* __restrict__ o0, double* __restrict__ o1,
                                                    double* __restrict__ o2, const double* __restrict__ dsum,
                                                    int nseg) {
+  using H = typename M::H;
+  using W = typename M::W;
+  using V = typename M::V;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
   const long long b = rowptr[warp], e = rowptr[warp + 1];
   // Four interactions per lane per trip: their ids and weights are loaded
   // before any gather so the loads overlap; two accumulator sets break the
-  // two-sum dependency chain.
-  FF f0, f1, f2, g0, g1, g2;
+  // dependency chain.
+  typename M::Acc f0, f1, f2, g0, g1, g2;
   long long k = b + lane;
   for (; k + 96 < e; k += 128) {
     int c[4];
-    float2 w[4];
+    W w[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) c[u] = __ldg(&col[k + 32 * u]);
 #pragma unroll
     for (int u = 0; u < 4; ++u) w[u] = __ldg(&wgt[k + 32 * u]);
-    float2 x0[4], x1[4], x2[4];
+    V x0[4], x1[4], x2[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const float4 a = __ldg(&src[2 * (size_t)c[u]]), z = __ldg(&src[2 * (size_t)c[u] + 1]);
-      x0[u] = make_float2(a.x, a.y);
-      x1[u] = make_float2(a.z, a.w);
-      x2[u] = make_float2(z.x, z.y);
+      const H a = __ldg(&src[2 * (size_t)c[u]]), z = __ldg(&src[2 * (size_t)c[u] + 1]);
+      x0[u] = M::v0(a);
+      x1[u] = M::v1(a);
+      x2[u] = M::v0(z);
     }
 #pragma unroll
     for (int u = 0; u < 4; u += 2) {
-      ff_mac(f0, w[u], x0[u]);
-      ff_mac(f1, w[u], x1[u]);
-      ff_mac(f2, w[u], x2[u]);
-      ff_mac(g0, w[u + 1], x0[u + 1]);
-      ff_mac(g1, w[u + 1], x1[u + 1]);
-      ff_mac(g2, w[u + 1], x2[u + 1]);
+      M::mac(f0, w[u], x0[u]);
+      M::mac(f1, w[u], x1[u]);
+      M::mac(f2, w[u], x2[u]);
+      M::mac(g0, w[u + 1], x0[u + 1]);
+      M::mac(g1, w[u + 1], x1[u + 1]);
+      M::mac(g2, w[u + 1], x2[u + 1]);
     }
   }
   for (; k < e; k += 32) {
     const int c = __ldg(&col[k]);
-    const float2 w = __ldg(&wgt[k]);
-    const float4 a = __ldg(&src[2 * (size_t)c]), z = __ldg(&src[2 * (size_t)c + 1]);
-    ff_mac(f0, w, make_float2(a.x, a.y));
-    ff_mac(f1, w, make_float2(a.z, a.w));
-    ff_mac(f2, w, make_float2(z.x, z.y));
+    const W w = __ldg(&wgt[k]);
+    const H a = __ldg(&src[2 * (size_t)c]), z = __ldg(&src[2 * (size_t)c + 1]);
+    M::mac(f0, w, M::v0(a));
+    M::mac(f1, w, M::v1(a));
+    M::mac(f2, w, M::v0(z));
   }
-  double a0 = ((double)f0.hi + (double)f0.lo) + ((double)g0.hi + (double)g0.lo);
-  double a1 = ((double)f1.hi + (double)f1.lo) + ((double)g1.hi + (double)g1.lo);
-  double a2 = ((double)f2.hi + (double)f2.lo) + ((double)g2.hi + (double)g2.lo);
+  double a0 = M::fin(f0) + M::fin(g0);
+  double a1 = M::fin(f1) + M::fin(g1);
+  double a2 = M::fin(f2) + M::fin(g2);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     a0 += __shfl_xor_sync(0xffffffffu, a0, o);
@@ -390,43 +438,46 @@ __global__ void __launch_bounds__(256) k_apply_csr(const long long* __restrict__
   }
 }
 
-// Group sources: problem `slot` of a group writes its float-float records
-// into slot `slot` of [cell][slot][s0 s1 s2 0], so that the problems'
-// records of one cell are adjacent (one coalesced load per warp).
-__global__ void k_split_slot(const double* __restrict__ x, int ncell, int slot, int lanes, float2* __restrict__ out) {
+// Group sources: problem `slot` of a group writes its records (policy
+// values) into slot `slot` of [cell][slot][s0 s1 s2 0], so that the
+// problems' records of one cell are adjacent (one coalesced load per warp).
+template <class M>
+__global__ void k_split_slot(const double* __restrict__ x, int ncell, int slot, int lanes,
+                             typename M::V* __restrict__ out) {
   const size_t n = 4 * (size_t)ncell;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const int cell = (int)(i >> 2), comp = (int)(i & 3);
-    float2 v = make_float2(0.0f, 0.0f);
-    if (comp < 3) {
-      const double d = x[(size_t)comp * ncell + cell];
-      const float hi = __double2float_rn(d);
-      v = make_float2(hi, __double2float_rn(d - (double)hi));
-    }
-    out[((size_t)cell * lanes + slot) * 4 + comp] = v;
+    out[((size_t)cell * lanes + slot) * 4 + comp] = M::vmake(comp < 3 ? x[(size_t)comp * ncell + cell] : 0.0);
   }
 }
 
-__device__ __forceinline__ void ff_mac3(FF& a0, FF& a1, FF& a2, float2 w, const float4* __restrict__ rec) {
-  const float4 a = __ldg(rec), z = __ldg(rec + 1);
-  ff_mac(a0, w, make_float2(a.x, a.y));
-  ff_mac(a1, w, make_float2(a.z, a.w));
-  ff_mac(a2, w, make_float2(z.x, z.y));
+template <class M>
+__device__ __forceinline__ void mac3(typename M::Acc& a0, typename M::Acc& a1, typename M::Acc& a2,
+                                     typename M::W w, const typename M::H* __restrict__ rec) {
+  const typename M::H a = __ldg(rec), z = __ldg(rec + 1);
+  M::mac(a0, w, M::v0(a));
+  M::mac(a1, w, M::v1(a));
+  M::mac(a2, w, M::v0(z));
 }
 
 // The dense block (coarsest level) of a shared operator against a group's
 // sources: a register-tiled product.  Lane = boundary node of a 32-node
 // chunk (its weights are one coalesced row), warp = a quad of problems
-// (4 problems x 3 components of float-float accumulators), CTA = 8 warps
-// over 8 / nquad chunks; a tile of kGroupTile cells of every problem's
-// sources is staged in shared memory and read as broadcasts.  Each weight
-// feeds twelve independent float-float chains.  blockIdx.y = segment of
-// the coarsest cells; partial sums go to part[segment][problem][comp][node].
+// (4 problems x 3 components of accumulators), CTA = 8 warps over
+// 8 / nquad chunks; a tile of kGroupTile cells of every problem's sources
+// is staged in shared memory and read as broadcasts.  Each weight feeds
+// twelve independent chains.  blockIdx.y = segment of the coarsest cells;
+// partial sums go to part[segment][problem][comp][node].
 constexpr int kGroupTile = 64;
-__global__ void __launch_bounds__(256) k_group_dense(const float4* __restrict__ wtop, const float4* __restrict__ gsrc,
-                                                     int top0, int ntop, int ntop2, int ntarget, int nprob, int nquad,
-                                                     int cseg, double* __restrict__ part) {
-  extern __shared__ float4 gs[];  // [cell][problem][2]
+template <class M>
+__global__ void __launch_bounds__(256) k_group_dense(const typename M::W2* __restrict__ wtop,
+                                                     const typename M::H* __restrict__ gsrc, int top0, int ntop,
+                                                     int ntop2, int ntarget, int nprob, int nquad, int cseg,
+                                                     double* __restrict__ part) {
+  using H = typename M::H;
+  using W2 = typename M::W2;
+  extern __shared__ double2 gsm[];
+  H* gs = reinterpret_cast<H*>(gsm);  // [cell][problem][2]
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int per = 8 / nquad;  // chunks per CTA
   const int q = wid % nquad;  // problem quad
@@ -435,33 +486,33 @@ __global__ void __launch_bounds__(256) k_group_dense(const float4* __restrict__ 
   const int p0 = 4 * q;
   const int np = active ? max(0, min(4, nprob - p0)) : 0;
   const int cb = blockIdx.y * cseg, ce = min(ntop, cb + cseg);
-  FF a[4][3];
+  typename M::Acc a[4][3];
   for (int c0 = cb; c0 < ce; c0 += kGroupTile) {
     const int nc = min(kGroupTile, ce - c0);
     __syncthreads();
-    const float4* src = gsrc + 2 * (size_t)(top0 + c0) * nprob;
+    const H* src = gsrc + 2 * (size_t)(top0 + c0) * nprob;
     for (int i = threadIdx.x; i < 2 * nc * nprob; i += blockDim.x) gs[i] = __ldg(&src[i]);
     __syncthreads();
     if (!np) continue;
-    const float4* wp = wtop + ((size_t)chunk * ntop2 + (c0 >> 1)) * 32 + lane;
+    const W2* wp = wtop + ((size_t)chunk * ntop2 + (c0 >> 1)) * 32 + lane;
     for (int c = 0; c < nc; c += 2) {
-      const float4 w = __ldg(&wp[(size_t)(c >> 1) * 32]);
-      const float2 wa = make_float2(w.x, w.y), wb = make_float2(w.z, w.w);
+      const W2 w = __ldg(&wp[(size_t)(c >> 1) * 32]);
+      const typename M::W wa = M::wa(w), wb = M::wb(w);
       const bool two = c + 1 < nc;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         if (j < np) {
-          const float4* r = gs + 2 * ((size_t)c * nprob + p0 + j);
-          const float4 x = r[0], z = r[1];
-          ff_mac(a[j][0], wa, make_float2(x.x, x.y));
-          ff_mac(a[j][1], wa, make_float2(x.z, x.w));
-          ff_mac(a[j][2], wa, make_float2(z.x, z.y));
+          const H* r = gs + 2 * ((size_t)c * nprob + p0 + j);
+          const H x = r[0], z = r[1];
+          M::mac(a[j][0], wa, M::v0(x));
+          M::mac(a[j][1], wa, M::v1(x));
+          M::mac(a[j][2], wa, M::v0(z));
           if (two) {
-            const float4* r2 = r + 2 * nprob;
-            const float4 x2 = r2[0], z2 = r2[1];
-            ff_mac(a[j][0], wb, make_float2(x2.x, x2.y));
-            ff_mac(a[j][1], wb, make_float2(x2.z, x2.w));
-            ff_mac(a[j][2], wb, make_float2(z2.x, z2.y));
+            const H* r2 = r + 2 * nprob;
+            const H x2 = r2[0], z2 = r2[1];
+            M::mac(a[j][0], wb, M::v0(x2));
+            M::mac(a[j][1], wb, M::v1(x2));
+            M::mac(a[j][2], wb, M::v0(z2));
           }
         }
       }
@@ -474,8 +525,7 @@ __global__ void __launch_bounds__(256) k_group_dense(const float4* __restrict__ 
   for (int j = 0; j < 4; ++j) {
     if (j < np) {
 #pragma unroll
-      for (int cc = 0; cc < 3; ++cc)
-        out[((size_t)(p0 + j) * 3 + cc) * ntarget + t] = (double)a[j][cc].hi + (double)a[j][cc].lo;
+      for (int cc = 0; cc < 3; ++cc) out[((size_t)(p0 + j) * 3 + cc) * ntarget + t] = M::fin(a[j][cc]);
     }
   }
 }
@@ -489,40 +539,44 @@ __global__ void __launch_bounds__(256) k_group_dense(const float4* __restrict__ 
 // of a cell are one contiguous load.  The row holds the finer levels; the
 // NG partial sums are added in set order, then the dense block's partial
 // sums (k_group_dense) in segment order.
+template <class M>
 __global__ void __launch_bounds__(256) k_apply_group(const long long* __restrict__ rowptr, const int* __restrict__ col,
-                                                     const float2* __restrict__ wgt, const float4* __restrict__ gsrc,
+                                                     const typename M::W* __restrict__ wgt,
+                                                     const typename M::H* __restrict__ gsrc,
                                                      const int* __restrict__ tgt_node, int ntarget, int nprob,
                                                      const double* __restrict__ part, int nseg, GroupOut G) {
+  using H = typename M::H;
+  using W = typename M::W;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
   const int LG = nprob, NG = 32 / nprob;
   const int p = lane % LG, grp = lane / LG;
   const bool act = grp < NG;
-  const float4* sp = gsrc + 2 * (size_t)p;
-  const size_t cstride = 2 * (size_t)LG;  // float4s per cell
-  FF f0, f1, f2, g0, g1, g2;
+  const H* sp = gsrc + 2 * (size_t)p;
+  const size_t cstride = 2 * (size_t)LG;  // halves per cell
+  typename M::Acc f0, f1, f2, g0, g1, g2;
   const long long b = rowptr[warp], e = rowptr[warp + 1];
   if (act) {
     long long k = b + grp;
     for (; k + 3 * NG < e; k += 4 * NG) {
       int c[4];
-      float2 w[4];
+      W w[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) c[u] = __ldg(&col[k + u * NG]);
 #pragma unroll
       for (int u = 0; u < 4; ++u) w[u] = __ldg(&wgt[k + u * NG]);
 #pragma unroll
       for (int u = 0; u < 4; u += 2) {
-        ff_mac3(f0, f1, f2, w[u], sp + (size_t)c[u] * cstride);
-        ff_mac3(g0, g1, g2, w[u + 1], sp + (size_t)c[u + 1] * cstride);
+        mac3<M>(f0, f1, f2, w[u], sp + (size_t)c[u] * cstride);
+        mac3<M>(g0, g1, g2, w[u + 1], sp + (size_t)c[u + 1] * cstride);
       }
     }
-    for (; k < e; k += NG) ff_mac3(f0, f1, f2, __ldg(&wgt[k]), sp + (size_t)__ldg(&col[k]) * cstride);
+    for (; k < e; k += NG) mac3<M>(f0, f1, f2, __ldg(&wgt[k]), sp + (size_t)__ldg(&col[k]) * cstride);
   }
-  double a0 = ((double)f0.hi + (double)f0.lo) + ((double)g0.hi + (double)g0.lo);
-  double a1 = ((double)f1.hi + (double)f1.lo) + ((double)g1.hi + (double)g1.lo);
-  double a2 = ((double)f2.hi + (double)f2.lo) + ((double)g2.hi + (double)g2.lo);
+  double a0 = M::fin(f0) + M::fin(g0);
+  double a1 = M::fin(f1) + M::fin(g1);
+  double a2 = M::fin(f2) + M::fin(g2);
   const double b0 = a0, b1 = a1, b2 = a2;
   for (int g = 1; g < NG; ++g) {
     const int src = min(p + g * LG, 31);
@@ -555,23 +609,28 @@ __global__ void __launch_bounds__(256) k_apply_group(const long long* __restrict
 // +wF) and L's missing from F (weight -ratio wL); for the dense block, the
 // coarsest cells accepted by one of them.  Shared cells must agree within
 // `tol` (relative), else *bad is set.
-__device__ __forceinline__ bool ff_close(float2 a, float2 b, double ratio, double tol) {
-  const double va = (double)a.x + (double)a.y, vb = (double)b.x + (double)b.y;
+// A recorded weight word as a double: an FP64 weight, or a float-float pair.
+__device__ __forceinline__ double wval(const double* w, size_t i, int ff) {
+  if (!ff) return w[i];
+  const float2 v = reinterpret_cast<const float2*>(w)[i];
+  return (double)v.x + (double)v.y;
+}
+__device__ __forceinline__ bool w_close(double va, double vb, double ratio, double tol) {
   if (va == 0.0 || vb == 0.0) return va == 0.0 && vb == 0.0;
   return fabs(vb - ratio * va) <= tol * fabs(vb);
 }
 __device__ __forceinline__ size_t dense_at(int t, int c, int ntop2) {
   return (((size_t)(t >> 5) * ntop2 + (c >> 1)) * 32 + (t & 31)) * 2 + (c & 1);
 }
-__device__ __forceinline__ double ffd(float2 v) { return (double)v.x + (double)v.y; }
 
 struct CorrArgs {
   const long long *Lr, *Fr;
   const int *Lc, *Fc;
-  const float2 *Lw, *Fw, *Ld, *Fd;
+  const double *Lw, *Fw, *Ld, *Fd;  // 8-byte weight words (ff: float-float pairs)
   const int* pre;
   int ntop, top0;
   double ratio, tol;
+  int ff;
 };
 
 template <bool FILL>
@@ -583,15 +642,15 @@ __device__ int corr_row(const CorrArgs& A, int t, int* __restrict__ ocol, double
     const int ca = (i < ie) ? A.Lc[i] : -1, cb = (j < je) ? A.Fc[j] : -1;
     const int pa = (ca >= 0) ? A.pre[ca] : 0x7fffffff, pb = (cb >= 0) ? A.pre[cb] : 0x7fffffff;
     if (pa == pb) {
-      ok &= ff_close(A.Lw[i], A.Fw[j], A.ratio, A.tol);
+      ok &= w_close(wval(A.Lw, i, A.ff), wval(A.Fw, j, A.ff), A.ratio, A.tol);
       ++i;
       ++j;
     } else if (pa < pb) {
-      if (FILL) { ocol[n] = ca; ow[n] = -A.ratio * ffd(A.Lw[i]); }
+      if (FILL) { ocol[n] = ca; ow[n] = -A.ratio * wval(A.Lw, i, A.ff); }
       ++n;
       ++i;
     } else {
-      if (FILL) { ocol[n] = cb; ow[n] = ffd(A.Fw[j]); }
+      if (FILL) { ocol[n] = cb; ow[n] = wval(A.Fw, j, A.ff); }
       ++n;
       ++j;
     }
@@ -599,13 +658,13 @@ __device__ int corr_row(const CorrArgs& A, int t, int* __restrict__ ocol, double
   if (A.Ld) {
     const int ntop2 = (A.ntop + 1) >> 1;
     for (int c = 0; c < A.ntop; ++c) {
-      const float2 a = A.Ld[dense_at(t, c, ntop2)], b = A.Fd[dense_at(t, c, ntop2)];
-      const bool za = ffd(a) == 0.0, zb = ffd(b) == 0.0;
+      const double a = wval(A.Ld, dense_at(t, c, ntop2), A.ff), b = wval(A.Fd, dense_at(t, c, ntop2), A.ff);
+      const bool za = a == 0.0, zb = b == 0.0;
       if (za != zb) {
-        if (FILL) { ocol[n] = A.top0 + c; ow[n] = ffd(b) - A.ratio * ffd(a); }
+        if (FILL) { ocol[n] = A.top0 + c; ow[n] = b - A.ratio * a; }
         ++n;
       } else if (!za) {
-        ok &= ff_close(a, b, A.ratio, A.tol);
+        ok &= w_close(a, b, A.ratio, A.tol);
       }
     }
   }
@@ -735,6 +794,7 @@ WalkDev walk_dev(const BoundaryOp& B) {
   W.tree = B.tree ? 1 : 0;
   W.tgt_frame = B.tgt_frame.p;
   W.dense = B.dense ? 1 : 0;
+  W.ff = B.arith == VPMG_ARITH_FF48 ? 1 : 0;
   for (int f = 0; f < 6; ++f) W.frame[f] = B.frame[f];
   return W;
 }
@@ -778,7 +838,9 @@ long long BoundaryOp::bytes() const {
 }
 
 void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s, int ibctyp,
-                      bool tree) {
+                      bool tree, int arith) {
+  VPMG_CHECK(arith == VPMG_ARITH_FP64 || arith == VPMG_ARITH_FF48, VPMG_ERR_ARG, "unknown arithmetic");
+  B.arith = arith;
   VPMG_CHECK(levmax >= 0 && levmax < kMaxLev - 1, VPMG_ERR_ARG, "levmax out of range");
   VPMG_CHECK(ibctyp == 2 || ibctyp == 3, VPMG_ERR_UNSUPPORTED, "ibctyp must be 2 or 3");
   VPMG_CHECK(tree || levmax == 0, VPMG_ERR_ARG, "the untreed sum has one level");
@@ -950,34 +1012,42 @@ static void aggregate_levels(BoundaryOp& B, cudaStream_t s) {
   }
 }
 
+template <class M>
+static void apply_recorded(BoundaryOp& B, double* const sol[3], cudaStream_t s) {
+  using H = typename M::H;
+  const size_t nc4 = 4 * (size_t)B.ncell_total;
+  VPMG_CHECK(B.csrc_ff.n >= nc4, VPMG_ERR_STATE, "boundary operator recorded without its source buffer");
+  typename M::V* src = reinterpret_cast<typename M::V*>(B.csrc_ff.p);
+  k_split<M><<<(unsigned)std::min<size_t>((nc4 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, B.ncell_total, src);
+  VPMG_LAUNCHED();
+  const H* src2 = reinterpret_cast<const H*>(src);
+  if (B.dense) {
+    const long long dthreads = (long long)((B.ntarget + 31) / 32) * 32;
+    const int cseg = dense_cseg(B);
+    const dim3 grid((unsigned)((dthreads + 255) / 256), (unsigned)dense_nseg(B));
+    k_apply_dense<M><<<grid, 256, 0, s>>>(reinterpret_cast<const typename M::W2*>(B.wtop.p), src2,
+                                          B.lev_off[B.levmax], B.ntopd, (B.ntopd + 1) / 2, B.ntarget, cseg,
+                                          B.dsum.p);
+    VPMG_LAUNCHED();
+  }
+  const long long threads = (long long)B.ntarget * 32;
+  k_apply_csr<M><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+      B.rowptr.p, B.col.p, reinterpret_cast<const typename M::W*>(B.w.p), src2, B.tgt_node.p, B.ntarget,
+      1.0 / (4.0 * kPI), sol[0], sol[1], sol[2], B.dense ? B.dsum.p : nullptr, B.dense ? dense_nseg(B) : 0);
+  VPMG_LAUNCHED();
+}
+
 void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStream_t s) {
   (void)g;
   aggregate_levels(B, s);
   if (B.precomputed) {
-    const size_t nc4 = 4 * (size_t)B.ncell_total;
-    VPMG_CHECK(B.csrc_ff.n >= nc4, VPMG_ERR_STATE, "boundary operator recorded without its source buffer");
-    k_split<<<(unsigned)std::min<size_t>((nc4 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, B.ncell_total,
-                                                                                    B.csrc_ff.p);
-    VPMG_LAUNCHED();
-    const float4* src4 = reinterpret_cast<const float4*>(B.csrc_ff.p);
-    if (B.dense) {
-      const long long dthreads = (long long)((B.ntarget + 31) / 32) * 32;
-      const int cseg = dense_cseg(B);
-      const dim3 grid((unsigned)((dthreads + 255) / 256), (unsigned)dense_nseg(B));
-      k_apply_dense<<<grid, 256, 0, s>>>(reinterpret_cast<const float4*>(B.wtop.p), src4, B.lev_off[B.levmax],
-                                         B.ntopd, (B.ntopd + 1) / 2, B.ntarget, cseg, B.dsum.p);
-      VPMG_LAUNCHED();
-    }
-    const long long threads = (long long)B.ntarget * 32;
-    k_apply_csr<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, src4, B.tgt_node.p,
-                                                                  B.ntarget, 1.0 / (4.0 * kPI), sol[0], sol[1],
-                                                                  sol[2], B.dense ? B.dsum.p : nullptr,
-                                                                  B.dense ? dense_nseg(B) : 0);
+    if (B.arith == VPMG_ARITH_FF48) apply_recorded<MacFF>(B, sol, s);
+    else apply_recorded<Mac64>(B, sol, s);
   } else {
     const WalkDev W = walk_dev(B);
     k_walk<kAccum><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, sol[0], sol[1], sol[2], nullptr, nullptr, nullptr, nullptr);
+    VPMG_LAUNCHED();
   }
-  VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
 
@@ -985,6 +1055,7 @@ void boundary_apply(BoundaryOp& B, const Grid& g, double* const sol[3], cudaStre
 bool boundary_group_match(const BoundaryOp& L, const Grid& gl, const BoundaryOp& F, const Grid& gf,
                           double max_frac, double* ratio, GroupCorrection& C, cudaStream_t s) {
   if (!L.precomputed || !F.precomputed || L.ibctyp != 2 || F.ibctyp != 2 || L.tree != F.tree) return false;
+  if (L.arith != F.arith) return false;
   if (L.ntarget != F.ntarget || L.ncell_total != F.ncell_total || L.levmax != F.levmax || L.dense != F.dense ||
       L.ntopd != F.ntopd || L.lev_off != F.lev_off || L.wtop.n != F.wtop.n)
     return false;
@@ -1026,8 +1097,10 @@ bool boundary_group_match(const BoundaryOp& L, const Grid& gl, const BoundaryOp&
   cnt.ensure((size_t)nt);
   bad.ensure(1);
   VPMG_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
-  CorrArgs A{L.rowptr.p, F.rowptr.p, L.col.p, F.col.p, L.w.p, F.w.p, L.dense ? L.wtop.p : nullptr,
-             F.dense ? F.wtop.p : nullptr, dpre.p, L.ntopd, L.lev_off[L.levmax], r, 1e-12};
+  auto words = [](const DBuf<float2>& b) { return reinterpret_cast<const double*>(b.p); };
+  CorrArgs A{L.rowptr.p, F.rowptr.p, L.col.p, F.col.p, words(L.w), words(F.w), L.dense ? words(L.wtop) : nullptr,
+             F.dense ? words(F.wtop) : nullptr, dpre.p, L.ntopd, L.lev_off[L.levmax], r, 1e-12,
+             L.arith == VPMG_ARITH_FF48 ? 1 : 0};
   k_corr_count<<<(nt + 127) / 128, 128, 0, s>>>(A, L.tgt_node.p, F.tgt_node.p, nt, cnt.p, bad.p);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
@@ -1083,8 +1156,11 @@ void boundary_group_correct(const BoundaryOp& F, const GroupCorrection& C, doubl
 void boundary_group_sources(BoundaryOp& B, float2* gsrc, int slot, int lanes, cudaStream_t s) {
   aggregate_levels(B, s);
   const size_t nc4 = 4 * (size_t)B.ncell_total;
-  k_split_slot<<<(unsigned)std::min<size_t>((nc4 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, B.ncell_total, slot,
-                                                                                        lanes, gsrc);
+  const unsigned g = (unsigned)std::min<size_t>((nc4 + 255) / 256, 152 * 16);
+  if (B.arith == VPMG_ARITH_FF48)
+    k_split_slot<MacFF><<<g, 256, 0, s>>>(B.csrc.p, B.ncell_total, slot, lanes, gsrc);
+  else
+    k_split_slot<Mac64><<<g, 256, 0, s>>>(B.csrc.p, B.ncell_total, slot, lanes, reinterpret_cast<double*>(gsrc));
   VPMG_LAUNCHED();
 }
 
@@ -1107,11 +1183,12 @@ size_t boundary_group_partial_count(const BoundaryOp& L, int nprob) {
   return nseg * nprob * 3 * (size_t)L.ntarget;
 }
 
-void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, double* part, const GroupOut& G,
+template <class M>
+static void group_apply_t(const BoundaryOp& L, const float2* gsrc, int nprob, double* part, const GroupOut& G,
                           cudaStream_t s) {
-  VPMG_CHECK(L.precomputed && nprob >= 1 && nprob <= kGroupMax, VPMG_ERR_STATE,
-             "group apply: operator not recorded or group too large");
+  using H = typename M::H;
   int nseg = 0;
+  const H* gs = reinterpret_cast<const H*>(gsrc);
   if (L.dense) {
     VPMG_CHECK(part, VPMG_ERR_STATE, "group apply: no buffer for the dense block's partial sums");
     const int nquad = nprob > 8 ? 4 : (nprob > 4 ? 2 : 1);
@@ -1119,17 +1196,25 @@ void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, do
     nseg = (L.ntopd + cseg - 1) / cseg;
     const int per = 8 / nquad;
     const dim3 grid((unsigned)(((L.ntarget + 31) / 32 + per - 1) / per), (unsigned)nseg);
-    const size_t smem = sizeof(float4) * 2 * kGroupTile * nprob;
-    k_group_dense<<<grid, 256, smem, s>>>(reinterpret_cast<const float4*>(L.wtop.p),
-                                          reinterpret_cast<const float4*>(gsrc), L.lev_off[L.levmax], L.ntopd,
-                                          (L.ntopd + 1) / 2, L.ntarget, nprob, nquad, cseg, part);
+    const size_t smem = sizeof(H) * 2 * kGroupTile * nprob;
+    k_group_dense<M><<<grid, 256, smem, s>>>(reinterpret_cast<const typename M::W2*>(L.wtop.p), gs,
+                                             L.lev_off[L.levmax], L.ntopd, (L.ntopd + 1) / 2, L.ntarget, nprob, nquad,
+                                             cseg, part);
     VPMG_LAUNCHED();
   }
   const long long threads = (long long)L.ntarget * 32;
-  k_apply_group<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
-      L.rowptr.p, L.col.p, L.w.p, reinterpret_cast<const float4*>(gsrc), L.tgt_node.p, L.ntarget, nprob, part, nseg,
-      G);
+  k_apply_group<M><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+      L.rowptr.p, L.col.p, reinterpret_cast<const typename M::W*>(L.w.p), gs, L.tgt_node.p, L.ntarget, nprob, part,
+      nseg, G);
   VPMG_LAUNCHED();
+}
+
+void boundary_group_apply(const BoundaryOp& L, const float2* gsrc, int nprob, double* part, const GroupOut& G,
+                          cudaStream_t s) {
+  VPMG_CHECK(L.precomputed && nprob >= 1 && nprob <= kGroupMax, VPMG_ERR_STATE,
+             "group apply: operator not recorded or group too large");
+  if (L.arith == VPMG_ARITH_FF48) group_apply_t<MacFF>(L, gsrc, nprob, part, G, s);
+  else group_apply_t<Mac64>(L, gsrc, nprob, part, G, s);
   VPMG_CUDA(cudaGetLastError());
 }
 
@@ -1143,7 +1228,7 @@ namespace vpmg {
 namespace {
 
 __global__ void __launch_bounds__(256) k_csr_T(const long long* __restrict__ rowptr, const int* __restrict__ col,
-                                               const float2* __restrict__ wgt, const int* __restrict__ tgt_node,
+                                               const double* __restrict__ wgt, int ff, const int* __restrict__ tgt_node,
                                                int ntarget, double scale, const double* __restrict__ bcbar,
                                                double* __restrict__ cellbar) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1152,7 +1237,7 @@ __global__ void __launch_bounds__(256) k_csr_T(const long long* __restrict__ row
   const double v = scale * bcbar[tgt_node[warp]];
   if (v == 0.0) return;
   for (long long k = rowptr[warp] + lane; k < rowptr[warp + 1]; k += 32)
-    atomicAdd(&cellbar[col[k]], ((double)wgt[k].x + (double)wgt[k].y) * v);
+    atomicAdd(&cellbar[col[k]], wval(wgt, k, ff) * v);
 }
 
 // Transposed interaction list: per-cell counts, then a fill through per-cell
@@ -1165,8 +1250,8 @@ __global__ void k_col_count(const long long* __restrict__ rowptr, const int* __r
   for (long long k = rowptr[warp] + lane; k < rowptr[warp + 1]; k += 32) atomicAdd(&cnt[col[k]], 1);
 }
 __global__ void k_col_fill(const long long* __restrict__ rowptr, const int* __restrict__ col,
-                           const float2* __restrict__ wgt, int ntarget, const long long* __restrict__ colptr,
-                           int* __restrict__ cursor, int* __restrict__ trow, float2* __restrict__ tw) {
+                           const double* __restrict__ wgt, int ntarget, const long long* __restrict__ colptr,
+                           int* __restrict__ cursor, int* __restrict__ trow, double* __restrict__ tw) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ntarget) return;
@@ -1174,27 +1259,31 @@ __global__ void k_col_fill(const long long* __restrict__ rowptr, const int* __re
     const int c = col[k];
     const long long slot = colptr[c] + atomicAdd(&cursor[c], 1);
     trow[slot] = warp;
-    tw[slot] = wgt[k];
+    tw[slot] = wgt[k];  // the 8-byte weight word, either arithmetic
   }
 }
-// The boundary-value adjoint of each target, split once per call.
+// The boundary-value adjoint of each target in the policy's arithmetic, once per call.
+template <class M>
 __global__ void k_split_bc(const double* __restrict__ bcbar, const int* __restrict__ tgt_node, int ntarget,
-                           float2* __restrict__ v) {
+                           typename M::V* __restrict__ v) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < ntarget) v[t] = ff::split(bcbar[tgt_node[t]]);
+  if (t < ntarget) v[t] = M::vsplit(bcbar[tgt_node[t]]);
 }
 
 // cellbar[c] = scale * sum over the cell's targets of w * bcbar(target node);
-// warp per cell, products and sums in float-float.
+// warp per cell, products and sums in the policy's arithmetic.
+template <class M>
 __global__ void __launch_bounds__(256) k_csc_T(const long long* __restrict__ colptr, const int* __restrict__ trow,
-                                               const float2* __restrict__ tw, const float2* __restrict__ v,
-                                               int ncell, double scale, double* __restrict__ cellbar) {
+                                               const typename M::W* __restrict__ tw,
+                                               const typename M::V* __restrict__ v, int ncell, double scale,
+                                               double* __restrict__ cellbar) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= ncell) return;
-  FF f;
-  for (long long k = colptr[warp] + lane; k < colptr[warp + 1]; k += 32) ff_mac(f, __ldg(&tw[k]), __ldg(&v[__ldg(&trow[k])]));
-  double a = (double)f.hi + (double)f.lo;
+  typename M::Acc f;
+  for (long long k = colptr[warp] + lane; k < colptr[warp + 1]; k += 32)
+    M::mac(f, __ldg(&tw[k]), __ldg(&v[__ldg(&trow[k])]));
+  double a = M::fin(f);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
   if (lane == 0) cellbar[warp] = scale * a;
@@ -1202,11 +1291,13 @@ __global__ void __launch_bounds__(256) k_csc_T(const long long* __restrict__ col
 
 // Transpose of the dense block: cellbar[top0 + c] += scale * sum_t w(t, c) bcbar(node t).
 // A warp per (cell, group of kDenseTGroup target chunks) forms a partial sum
-// (float-float; each chunk's 32 weights are one coalesced row), then
-// k_dense_T_sum adds a cell's groups in order (deterministic).
+// (each chunk's 32 weights are one coalesced row), then k_dense_T_sum adds
+// a cell's groups in order (deterministic).
 constexpr int kDenseTGroup = 64;
-__global__ void __launch_bounds__(256) k_dense_T(const float2* __restrict__ wtop, const float2* __restrict__ v, int ntop,
-                                                 int ntarget, double* __restrict__ part) {
+template <class M>
+__global__ void __launch_bounds__(256) k_dense_T(const typename M::W* __restrict__ wtop,
+                                                 const typename M::V* __restrict__ v, int ntop, int ntarget,
+                                                 double* __restrict__ part) {
   const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int nchunk = (ntarget + 31) / 32;
@@ -1214,14 +1305,14 @@ __global__ void __launch_bounds__(256) k_dense_T(const float2* __restrict__ wtop
   if (wid >= (long long)ntop * ngroup) return;
   const int c = (int)(wid % ntop), grp = (int)(wid / ntop);
   const int g1 = min(nchunk, (grp + 1) * kDenseTGroup);
-  FF f;
+  typename M::Acc f;
   for (int g = grp * kDenseTGroup; g < g1; ++g) {
     const int t = g * 32 + lane;
     if (t >= ntarget) continue;
-    const float2 w = __ldg(&wtop[(((size_t)g * ((ntop + 1) >> 1) + (c >> 1)) * 32 + lane) * 2 + (c & 1)]);
-    ff_mac(f, w, __ldg(&v[t]));
+    const typename M::W w = __ldg(&wtop[(((size_t)g * ((ntop + 1) >> 1) + (c >> 1)) * 32 + lane) * 2 + (c & 1)]);
+    M::mac(f, w, __ldg(&v[t]));
   }
-  double a = (double)f.hi + (double)f.lo;
+  double a = M::fin(f);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
   if (lane == 0) part[(size_t)grp * ntop + c] = a;
@@ -1306,18 +1397,23 @@ void boundary_transpose_prepare(BoundaryOp& B, cudaStream_t s) {
     return;
   }
   VPMG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int) * B.ncell_total, s));
-  k_col_fill<<<blocks, 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, B.ntarget, B.colptr.p, cnt.p, B.trow.p, B.tw.p);
+  k_col_fill<<<blocks, 256, 0, s>>>(B.rowptr.p, B.col.p, reinterpret_cast<const double*>(B.w.p), B.ntarget,
+                                    B.colptr.p, cnt.p, B.trow.p, reinterpret_cast<double*>(B.tw.p));
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
   VPMG_CUDA(cudaStreamSynchronize(s));
   B.transposed = true;
 }
 
-void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s) {
+template <class M>
+static void apply_T_recorded(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s) {
+  using V = typename M::V;
+  using W = typename M::W;
   const double scale = -1.0 / (4.0 * kPI);
+  V* vv = reinterpret_cast<V*>(B.vff.p);
   if (B.transposed || B.dense) {
     VPMG_CHECK(B.vff.n >= (size_t)B.ntarget, VPMG_ERR_STATE, "boundary transpose not prepared");
-    k_split_bc<<<(B.ntarget + 255) / 256, 256, 0, s>>>(bcbar, B.tgt_node.p, B.ntarget, B.vff.p);
+    k_split_bc<M><<<(B.ntarget + 255) / 256, 256, 0, s>>>(bcbar, B.tgt_node.p, B.ntarget, vv);
     VPMG_LAUNCHED();
   }
   auto dense_T = [&] {
@@ -1325,7 +1421,8 @@ void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaS
     const int ngroup = ((B.ntarget + 31) / 32 + kDenseTGroup - 1) / kDenseTGroup;
     VPMG_CHECK(B.dpart.n >= (size_t)ngroup * B.ntopd, VPMG_ERR_STATE, "boundary transpose not prepared");
     const long long threads = (long long)B.ntopd * ngroup * 32;
-    k_dense_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.wtop.p, B.vff.p, B.ntopd, B.ntarget, B.dpart.p);
+    k_dense_T<M><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(reinterpret_cast<const W*>(B.wtop.p), vv, B.ntopd,
+                                                                  B.ntarget, B.dpart.p);
     VPMG_LAUNCHED();
     k_dense_T_sum<<<(B.ntopd + 255) / 256, 256, 0, s>>>(B.dpart.p, B.ntopd, ngroup, B.lev_off[B.levmax], scale,
                                                          cellbar);
@@ -1333,21 +1430,29 @@ void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaS
   };
   if (B.transposed) {
     const long long threads = (long long)B.ncell_total * 32;
-    k_csc_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.colptr.p, B.trow.p, B.tw.p, B.vff.p, B.ncell_total,
-                                                              scale, cellbar);
+    k_csc_T<M><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.colptr.p, B.trow.p,
+                                                                 reinterpret_cast<const W*>(B.tw.p), vv,
+                                                                 B.ncell_total, scale, cellbar);
     VPMG_LAUNCHED();
     dense_T();
-    VPMG_CUDA(cudaGetLastError());
     return;
   }
   VPMG_CUDA(cudaMemsetAsync(cellbar, 0, sizeof(double) * B.ncell_total, s));
+  const long long threads = (long long)B.ntarget * 32;
+  k_csr_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p,
+                                                            reinterpret_cast<const double*>(B.w.p),
+                                                            M::kFF ? 1 : 0, B.tgt_node.p, B.ntarget, scale, bcbar,
+                                                            cellbar);
+  VPMG_LAUNCHED();
+  dense_T();
+}
+
+void boundary_apply_T(BoundaryOp& B, const double* bcbar, double* cellbar, cudaStream_t s) {
   if (B.precomputed) {
-    const long long threads = (long long)B.ntarget * 32;
-    k_csr_T<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(B.rowptr.p, B.col.p, B.w.p, B.tgt_node.p, B.ntarget,
-                                                              scale, bcbar, cellbar);
-    VPMG_LAUNCHED();
-    dense_T();
+    if (B.arith == VPMG_ARITH_FF48) apply_T_recorded<MacFF>(B, bcbar, cellbar, s);
+    else apply_T_recorded<Mac64>(B, bcbar, cellbar, s);
   } else {
+    VPMG_CUDA(cudaMemsetAsync(cellbar, 0, sizeof(double) * B.ncell_total, s));
     const WalkDev W = walk_dev(B);
     k_walk<kTranspose><<<(B.ntarget + 127) / 128, 128, 0, s>>>(W, cellbar, const_cast<double*>(bcbar), nullptr,
                                                                nullptr, nullptr, nullptr, nullptr);

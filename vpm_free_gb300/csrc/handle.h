@@ -23,6 +23,7 @@ struct vpmg_handle {
   vpmg_sizes sz{};
   bool sized = false, prepared = false;
   long long op_budget = 100LL << 30;
+  int arith = VPMG_ARITH_FP64;  // arithmetic of the heavy kernels (vpmg_set_arithmetic)
   // grids
   vpmg::Grid gglob{}, gbl{}, gco{};
   int inner_lo[3] = {0, 0, 0}, inner_ext[3] = {0, 0, 0};  // block inner box (0-based) and extent
@@ -47,7 +48,7 @@ struct vpmg_handle {
   vpmg::Particles parts;
   vpmg::Binning bins;
   int np = 0;
-  vpmg::DBuf<float2> vel_ff, def_ff;  // velocity and stretching as float-float pairs (mesh-to-particle)
+  vpmg::DBuf<float2> vel_ff, def_ff;  // velocity and stretching as float-float pairs (float-float arithmetic)
   vpmg::DBuf<double> stage;          // AoS staging for host copies
   vpmg::DBuf<double> bench_scratch;  // replay outputs of vpmg_bench_kernel
   // timing
@@ -101,6 +102,8 @@ MeshDev mesh_dev(const Grid& g, int itype);
 Grid remesh_grid(const vpmg_handle* h);       // global mesh with the remesh's recomputed spacing
 void field_step(vpmg_handle* h);              // deposit ... stretching on binned particles
 void poisson_part(vpmg_handle* h);            // h->rhs -> h->sol (rhsscat, yaps3d, solget)
+// back_to_particles_3D(1) (+ Euler) from the resident fields in the handle's arithmetic
+void m2p_fields(vpmg_handle* h, int up_mode, bool euler, double dt, const double uinf[3]);
 void remesh(vpmg_handle* h);                  // remesh_particles_3d(1), on the stream
 void step_on_stream(vpmg_handle* h, double dt);  // one full step (uinf = 0, remesh), graph replay when enabled
 void sync_np(vpmg_handle* h);

@@ -52,6 +52,29 @@ __device__ __forceinline__ float2 proj_fun_ff(int itype, float2 xa) {
   return zero;
 }
 
+// The same projection kernels in FP64, written as the reference writes them
+// (pmproject.f90:391-431), |x| given.
+__device__ __forceinline__ double proj_fun_f64(int itype, double xa) {
+  if (itype == 4) {
+    if (xa > 2.0) return 0.0;
+    if (xa >= 1.0) return 0.5 * ((2.0 - xa) * (2.0 - xa)) * (1.0 - xa);
+    return 1.0 - 2.5 * (xa * xa) + 1.5 * (xa * xa * xa);
+  }
+  if (itype == 3) {
+    if (xa > 1.5) return 0.0;
+    if (xa >= 0.5) return 0.5 * (-xa + 1.5) * (-xa + 1.5);
+    return 0.5 * (xa + 1.5) * (xa + 1.5) - 1.5 * (xa + 0.5) * (xa + 0.5);
+  }
+  if (itype == 2) return (xa > 1.0) ? 0.0 : 1.0 - xa;
+  if (itype == 5 || itype == 6) {
+    const double lim = (itype == 5) ? 0.5 : 1.0;
+    if (xa <= lim) return 1.0 - xa * xa;
+    if (xa <= lim + 1.0) return 0.5 * (1.0 - xa) * (2.0 - xa);
+    return 0.0;
+  }
+  return 0.0;
+}
+
 // Cell index exactly as int((x - XMIN)/DX) (IEEE division, truncation).
 __device__ __forceinline__ int cell_of(double x, double xmin, double d) { return (int)__ddiv_rn(__dsub_rn(x, xmin), d); }
 
@@ -184,6 +207,153 @@ __global__ void k_deposit(const int* __restrict__ starts, const float2* __restri
   r2[id] = ff::to_double(a2) * inv_dv;
 }
 
+// FP64 records, the same 24 slots as doubles: x weights (0..3), y-z weight
+// products (4 + 4b + c), strengths (20..22), and the base cell's x index in
+// the first four bytes of slot 23.  The stencil offsets follow the
+// reference: x_a = (XP - XMIN - (i_a - 1) DX) / DX, evaluated with the
+// reciprocal of DX.
+__global__ void k_records64(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
+                            const double* __restrict__ q0, const double* __restrict__ q1,
+                            const double* __restrict__ q2, const int* __restrict__ perm,
+                            const int* __restrict__ nsorted_dev, MeshDev m, double* __restrict__ rec) {
+  const int nsorted = *nsorted_dev;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
+    const int p = perm[s];
+    const double pos[3] = {x[p], y[p], z[p]};
+    double* r = rec + (size_t)s * kRecLen;
+    double wgt[3][4];
+    int cx = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int c0 = cell_of(pos[d], m.xmin[d], m.d[d]);
+      const int node0 = c0 - m.ips;  // 0-based node = (i-1) of the reference
+      const double off = pos[d] - m.xmin[d];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const double t = (off - (double)(node0 + a) * m.d[d]) * m.inv[d];
+        wgt[d][a] = (a <= m.ips + m.ipf) ? proj_fun_f64(m.itype, fabs(t)) : 0.0;
+      }
+      if (d == 0) cx = c0;
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) r[a] = wgt[0][a];
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) r[4 + 4 * b + c] = wgt[1][b] * wgt[2][c];
+    r[kRecQ] = q0[p];
+    r[kRecQ + 1] = q1[p];
+    r[kRecQ + 2] = q2[p];
+    r[23] = __hiloint2double(0, cx);
+  }
+}
+
+// FP64 deposition gather: one thread per node, the particles of the cells
+// whose stencil covers it in fixed cell and slot order (run-to-run
+// deterministic, no atomics); 1 DMUL + 3 DFMA per particle-node visit.
+__global__ void __launch_bounds__(256) k_deposit64(const int* __restrict__ starts, const double* __restrict__ rec,
+                                                   MeshDev m, double inv_dv, double* __restrict__ r0,
+                                                   double* __restrict__ r1, double* __restrict__ r2) {
+  const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
+  const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (id >= N) return;
+  const int i = (int)(id % m.n[0]);
+  const int j = (int)((id / m.n[0]) % m.n[1]);
+  const int k = (int)(id / ((size_t)m.n[0] * m.n[1]));
+  const int w = m.ips + m.ipf;
+  const int xlo = max(i - m.ipf, 0), xhi = min(i + m.ips, m.n[0] - 1);
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int ck = max(k - m.ipf, 0); ck <= min(k + m.ips, m.n[2] - 1); ++ck) {
+    const int iz = k - ck + m.ips;
+    for (int cj = max(j - m.ipf, 0); cj <= min(j + m.ips, m.n[1] - 1); ++cj) {
+      const int iy = j - cj + m.ips;
+      const size_t row = (size_t)m.n[0] * (cj + (size_t)m.n[1] * ck);
+      const int s = __ldg(&starts[row + xlo]), e = __ldg(&starts[row + xhi + 1]);
+      for (int t = s; t < e; ++t) {
+        const double* r = rec + (size_t)t * kRecLen;
+        const double2 q2c = __ldg(reinterpret_cast<const double2*>(r) + 11);  // q2, cell
+        const int ix = i - __double2loint(q2c.y) + m.ips;
+        if ((unsigned)ix > (unsigned)w) continue;  // only for a binning that does not match rec
+        const double2 q01 = __ldg(reinterpret_cast<const double2*>(r) + 10);
+        const double f = __ldg(&r[ix]) * __ldg(&r[4 + 4 * iy + iz]);
+        a0 = fma(f, q01.x, a0);
+        a1 = fma(f, q01.y, a1);
+        a2 = fma(f, q2c.x, a2);
+      }
+    }
+  }
+  r0[id] = a0 * inv_dv;
+  r1[id] = a1 * inv_dv;
+  r2[id] = a2 * inv_dv;
+}
+
+// FP64 mesh-to-particle over sorted slots: UP = sum W vel, GP = (sum W def)
+// * vol; optionally the forward Euler push.  6 DFMA per particle-node visit.
+__global__ void __launch_bounds__(128) k_m2p64(const int* __restrict__ perm, const int* __restrict__ nsorted_dev,
+                                               const double* __restrict__ rec, MeshDev m,
+                                               const double* __restrict__ v0, const double* __restrict__ v1,
+                                               const double* __restrict__ v2, const double* __restrict__ g0,
+                                               const double* __restrict__ g1, const double* __restrict__ g2,
+                                               double* __restrict__ up, double* __restrict__ gp, int up_add,
+                                               double* __restrict__ x, double* __restrict__ y,
+                                               double* __restrict__ z, double* __restrict__ q0,
+                                               double* __restrict__ q1, double* __restrict__ q2,
+                                               const double* __restrict__ vol, int do_euler, double dt, double ux,
+                                               double uy, double uz) {
+  const int nsorted = *nsorted_dev;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
+    const int p = perm[s];
+    const double* r = rec + (size_t)s * kRecLen;
+    double wx[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) wx[a] = r[a];
+    const int c0 = __double2loint(r[23]);
+    const int cj = cell_of(y[p], m.xmin[1], m.d[1]), ck = cell_of(z[p], m.xmin[2], m.d[2]);
+    const int nw = m.ips + m.ipf + 1;
+    double u[3] = {0.0, 0.0, 0.0}, gl[3] = {0.0, 0.0, 0.0};
+    for (int c = 0; c < nw; ++c) {
+      const int kk = ck - m.ips + c;
+      for (int b = 0; b < nw; ++b) {
+        const int jj = cj - m.ips + b;
+        const double wyz = r[4 + 4 * b + c];
+        const size_t row = (size_t)m.n[0] * (jj + (size_t)m.n[1] * kk) + (c0 - m.ips);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          if (a >= nw) break;
+          const double f = wx[a] * wyz;
+          const size_t id = row + a;
+          u[0] = fma(f, __ldg(&v0[id]), u[0]);
+          u[1] = fma(f, __ldg(&v1[id]), u[1]);
+          u[2] = fma(f, __ldg(&v2[id]), u[2]);
+          gl[0] = fma(f, __ldg(&g0[id]), gl[0]);
+          gl[1] = fma(f, __ldg(&g1[id]), gl[1]);
+          gl[2] = fma(f, __ldg(&g2[id]), gl[2]);
+        }
+      }
+    }
+    const double vp = vol[p];
+    const double gg0 = gl[0] * vp, gg1 = gl[1] * vp, gg2 = gl[2] * vp;
+    if (up) {  // UP = UP + sum W vel (vpm_time.f90:92-94) or UP = sum W vel
+      const double b0 = up_add ? up[3 * (size_t)p] : 0.0, b1 = up_add ? up[3 * (size_t)p + 1] : 0.0,
+                   b2 = up_add ? up[3 * (size_t)p + 2] : 0.0;
+      up[3 * (size_t)p] = b0 + u[0];
+      up[3 * (size_t)p + 1] = b1 + u[1];
+      up[3 * (size_t)p + 2] = b2 + u[2];
+      gp[3 * (size_t)p] = gg0;
+      gp[3 * (size_t)p + 1] = gg1;
+      gp[3 * (size_t)p + 2] = gg2;
+    }
+    if (do_euler) {
+      x[p] = x[p] + (u[0] + ux) * dt;
+      y[p] = y[p] + (u[1] + uy) * dt;
+      z[p] = z[p] + (u[2] + uz) * dt;
+      q0[p] = q0[p] - gg0 * dt;
+      q1[p] = q1[p] - gg1 * dt;
+      q2[p] = q2[p] - gg2 * dt;
+    }
+  }
+}
+
 // A field value as a float-float pair: split from FP64, or stored as one.
 __device__ __forceinline__ float2 field_ff(const double* __restrict__ f, size_t id) { return ff::split(f[id]); }
 __device__ __forceinline__ float2 field_ff(const float2* __restrict__ f, size_t id) { return f[id]; }
@@ -196,9 +366,10 @@ __global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsor
                       MeshDev m,
                       const T* __restrict__ v0, const T* __restrict__ v1, const T* __restrict__ v2,
                       const T* __restrict__ g0, const T* __restrict__ g1, const T* __restrict__ g2,
-                      double* __restrict__ up, double* __restrict__ gp, double* __restrict__ x, double* __restrict__ y,
-                      double* __restrict__ z, double* __restrict__ q0, double* __restrict__ q1, double* __restrict__ q2,
-                      const double* __restrict__ vol, int do_euler, double dt, double ux, double uy, double uz) {
+                      double* __restrict__ up, double* __restrict__ gp, int up_add, double* __restrict__ x,
+                      double* __restrict__ y, double* __restrict__ z, double* __restrict__ q0, double* __restrict__ q1,
+                      double* __restrict__ q2, const double* __restrict__ vol, int do_euler, double dt, double ux,
+                      double uy, double uz) {
   const int nsorted = *nsorted_dev;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
   const int p = perm[s];
@@ -233,10 +404,12 @@ __global__ void k_m2p(const int* __restrict__ perm, const int* __restrict__ nsor
   const double vp = vol[p];
   const double ud[3] = {ff::to_double(u[0]), ff::to_double(u[1]), ff::to_double(u[2])};
   const double gg0 = ff::to_double(gl[0]) * vp, gg1 = ff::to_double(gl[1]) * vp, gg2 = ff::to_double(gl[2]) * vp;
-  if (up) {
-    up[3 * (size_t)p] = ud[0];
-    up[3 * (size_t)p + 1] = ud[1];
-    up[3 * (size_t)p + 2] = ud[2];
+  if (up) {  // UP = UP + sum W vel (vpm_time.f90:92-94) or UP = sum W vel
+    const double b0 = up_add ? up[3 * (size_t)p] : 0.0, b1 = up_add ? up[3 * (size_t)p + 1] : 0.0,
+                 b2 = up_add ? up[3 * (size_t)p + 2] : 0.0;
+    up[3 * (size_t)p] = b0 + ud[0];
+    up[3 * (size_t)p + 1] = b1 + ud[1];
+    up[3 * (size_t)p + 2] = b2 + ud[2];
     gp[3 * (size_t)p] = gg0;
     gp[3 * (size_t)p + 1] = gg1;
     gp[3 * (size_t)p + 2] = gg2;
@@ -363,8 +536,12 @@ void bin_particles(Particles& P, const MeshDev& m, Binning& B, cudaStream_t s) {
   k_cell_order<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(B.starts.p, (int)N, P.perm.p);
   VPMG_LAUNCHED();
   B.nsorted_dev = B.starts.p + N;
-  k_records<<<stride_grid(P.capacity, 256), 256, 0, s>>>(P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.perm.p,
-                                                         B.nsorted_dev, m, P.rec.p);
+  if (P.arith == VPMG_ARITH_FF48)
+    k_records<<<stride_grid(P.capacity, 256), 256, 0, s>>>(P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.perm.p,
+                                                           B.nsorted_dev, m, P.rec.p);
+  else
+    k_records64<<<stride_grid(P.capacity, 256), 256, 0, s>>>(P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.perm.p,
+                                                             B.nsorted_dev, m, P.rec64());
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
@@ -389,30 +566,44 @@ int read_count(const int* d, cudaStream_t s) {
 void deposit(const Particles& P, const MeshDev& m, const Binning& B, double* const rhs[3], cudaStream_t s) {
   const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
   const double dv = m.d[0] * m.d[1] * m.d[2];
-  k_deposit<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(B.starts.p, P.rec.p, m, 1.0 / dv, rhs[0], rhs[1], rhs[2]);
+  if (P.arith == VPMG_ARITH_FF48)
+    k_deposit<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(B.starts.p, P.rec.p, m, 1.0 / dv, rhs[0], rhs[1], rhs[2]);
+  else
+    k_deposit64<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(B.starts.p, P.rec64(), m, 1.0 / dv, rhs[0], rhs[1],
+                                                            rhs[2]);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
 
 template <typename T>
 static void m2p_launch(Particles& P, const MeshDev& m, const Binning& B, const T* const vel[3], const T* const def[3],
-                       bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s) {
+                       int up_mode, bool euler, double dt, const double uinf[3], cudaStream_t s) {
   k_m2p<T><<<stride_grid(P.capacity, 128), 128, 0, s>>>(P.perm.p, B.nsorted_dev, P.rec.p, m, vel[0], vel[1], vel[2],
-                                                         def[0], def[1], def[2], write_up ? P.up.p : nullptr, P.gp.p,
-                                                         P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.vol.p,
+                                                         def[0], def[1], def[2], up_mode ? P.up.p : nullptr, P.gp.p,
+                                                         up_mode == 2 ? 1 : 0, P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.vol.p,
                                                          euler ? 1 : 0, dt, uinf[0], uinf[1], uinf[2]);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
 
 void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const vel[3], const double* const def[3],
-         bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s) {
-  m2p_launch(P, m, B, vel, def, write_up, euler, dt, uinf, s);
+         int up_mode, bool euler, double dt, const double uinf[3], cudaStream_t s) {
+  if (P.arith == VPMG_ARITH_FF48) {
+    m2p_launch(P, m, B, vel, def, up_mode, euler, dt, uinf, s);
+    return;
+  }
+  k_m2p64<<<stride_grid(P.capacity, 128), 128, 0, s>>>(P.perm.p, B.nsorted_dev, P.rec64(), m, vel[0], vel[1], vel[2],
+                                                       def[0], def[1], def[2], up_mode ? P.up.p : nullptr, P.gp.p,
+                                                       up_mode == 2 ? 1 : 0, P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.vol.p,
+                                                       euler ? 1 : 0, dt, uinf[0], uinf[1], uinf[2]);
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
 }
 
 void m2p(Particles& P, const MeshDev& m, const Binning& B, const float2* const vel[3], const float2* const def[3],
-         bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s) {
-  m2p_launch(P, m, B, vel, def, write_up, euler, dt, uinf, s);
+         int up_mode, bool euler, double dt, const double uinf[3], cudaStream_t s) {
+  VPMG_CHECK(P.arith == VPMG_ARITH_FF48, VPMG_ERR_STATE, "float-float fields with FP64 particle records");
+  m2p_launch(P, m, B, vel, def, up_mode, euler, dt, uinf, s);
 }
 
 // Ordered compaction of the flagged nodes; the new count goes to P.d_np

@@ -6,11 +6,13 @@
 
 namespace vpmg {
 
-// A sorted particle record: 24 float-float slots (ff.cuh), 192 bytes --
-// the 4 x stencil weights (0..3), the 16 products of the y and z weights
+// A sorted particle record: 24 slots of 8 bytes, 192 bytes -- the 4 x
+// stencil weights (0..3), the 16 products of the y and z weights
 // wy[b] wz[c] at 4 + 4b + c, the strengths (20..22) and the base cell's x
-// index as the bits of slot 23's high float.  A particle-node visit of the
-// deposition reads one x weight, one y-z product and two 16-byte loads.
+// index in the first four bytes of slot 23.  A slot is a double (FP64
+// arithmetic) or a float-float pair (float-float arithmetic).  A
+// particle-node visit of the deposition reads one x weight, one y-z product
+// and two 16-byte loads.
 constexpr int kRecLen = 24;
 constexpr int kRecQ = 20;  // first strength slot
 
@@ -30,8 +32,10 @@ struct Particles {
   DBuf<double> x, y, z, q0, q1, q2, vol;  // SoA, QP(1:3) and QP(4)
   DBuf<double> up, gp;                    // (3, cap) AoS like UP/GP
   DBuf<int> key, perm;
-  DBuf<float2> rec;                       // kRecLen float-float slots per sorted particle
+  DBuf<float2> rec;                       // kRecLen slots per sorted particle (8 bytes each)
   DBuf<int> d_np;                         // particle count, on the device
+  int arith = VPMG_ARITH_FP64;            // arithmetic of the records, deposition and gather
+  double* rec64() const { return reinterpret_cast<double*>(rec.p); }
   void ensure(int cap);
 };
 
@@ -45,11 +49,15 @@ struct Binning {
 // All of these only enqueue work on the stream (no host round trip).
 void bin_particles(Particles& P, const MeshDev& m, Binning& B, cudaStream_t s);
 void deposit(const Particles& P, const MeshDev& m, const Binning& B, double* const rhs[3], cudaStream_t s);
+// up_mode: 0 UP not written, 1 UP = sum W vel, 2 UP += sum W vel (the
+// reference's accumulation into the caller's UP, vpm_time.f90:92-94);
+// GP = vol * sum W def whenever UP is written.
+enum { kUpNone = 0, kUpSet = 1, kUpAdd = 2 };
 void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const vel[3], const double* const def[3],
-         bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s);
+         int up_mode, bool euler, double dt, const double uinf[3], cudaStream_t s);
 // the same with the fields as float-float pairs (no split per node visit)
 void m2p(Particles& P, const MeshDev& m, const Binning& B, const float2* const vel[3], const float2* const def[3],
-         bool write_up, bool euler, double dt, const double uinf[3], cudaStream_t s);
+         int up_mode, bool euler, double dt, const double uinf[3], cudaStream_t s);
 void remesh_emit(Particles& P, const MeshDev& m, Binning& B, const double* const rhs[3], const int lo[3],
                  const int hi[3], double thr, cudaStream_t s);
 // The emission mask alone: B.cursor = node flag, B.starts = emit slot (exclusive scan).

@@ -26,7 +26,7 @@
 #include <cmath>
 #include <cstdlib>
 
-#include "ff.cuh"
+#include "arith.cuh"
 #include "vpmg_internal.h"
 
 namespace vpmg {
@@ -39,137 +39,127 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kDefaultPairs = 4;
 constexpr int kMaxOddRadix = 17;  // largest odd prime radix (2*(cells) must factor into 2..17)
+constexpr int kRadixTab = (kMaxOddRadix + 1) * (kMaxOddRadix + 1);
 
-__constant__ float2 c_rcos_f[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];  // cos(2 pi i/R), float-float
-__constant__ float2 c_rsin_f[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
-bool g_tables_ready = false;
+// cos / sin (2 pi i / R) of the odd radices: FP64 and float-float copies
+__constant__ double c_rcos_d[kRadixTab];
+__constant__ double c_rsin_d[kRadixTab];
+__constant__ float2 c_rcos_f[kRadixTab];
+__constant__ float2 c_rsin_f[kRadixTab];
+
+template <class A>
+__device__ __forceinline__ typename A::R rcos(int i);
+template <class A>
+__device__ __forceinline__ typename A::R rsin(int i);
+template <>
+__device__ __forceinline__ double rcos<F64>(int i) { return c_rcos_d[i]; }
+template <>
+__device__ __forceinline__ double rsin<F64>(int i) { return c_rsin_d[i]; }
+template <>
+__device__ __forceinline__ float2 rcos<FF>(int i) { return c_rcos_f[i]; }
+template <>
+__device__ __forceinline__ float2 rsin<FF>(int i) { return c_rsin_f[i]; }
 
 struct FFTDev {
   int n, N, M, nst;
   int odd;    // 1 if a stage has an odd radix
   int rs;     // 1: real-symmetric DST-I (M = N), 0: odd extension (M = 2N)
   int pairs;  // line pairs per CTA
+  int arith;  // VPMG_ARITH_FP64 or VPMG_ARITH_FF48
   int radix[24];
-  const float4* tw;  // e^{-2 pi i t / M} as float-float (re.hi, re.lo, im.hi, im.lo)
-  const double* sn;  // sin(pi j / N) (rs only)
+  const double2* twd;  // e^{-2 pi i t / M}, FP64
+  const float4* twf;   // the same as float-float (re.hi, re.lo, im.hi, im.lo)
+  const double* sn;    // sin(pi j / N) (rs only)
 };
+template <class A>
+__device__ __forceinline__ const typename A::C* twiddles(const FFTDev& p);
+template <>
+__device__ __forceinline__ const double2* twiddles<F64>(const FFTDev& p) { return p.twd; }
+template <>
+__device__ __forceinline__ const float4* twiddles<FF>(const FFTDev& p) { return p.twf; }
 
-// ---- FFT stages in float-float arithmetic (ff.cuh) ----------------------
-// The stages are the FP64-heaviest part of the solve; on GB300 they run
-// about as fast again in float-float on the FP32 pipes (48-bit significand,
-// error-free sums and products), entered and left by bit operations.
-using ff::cadd;
-using ff::csub;
-using ff::cmul;
-
-template <int R>
+// ---- FFT stages in the policy's arithmetic (arith.cuh) -------------------
+// F64: IEEE double, the reference's arithmetic.  FF: float-float on the FP32
+// pipes (48-bit significand, error-free sums and products), entered and
+// left by bit operations.
+template <class A, int R>
 struct DFT;
 
-template <>
-struct DFT<2> {
-  __device__ __forceinline__ static void run(float4 (&v)[2]) {
-    const float4 a = v[0], b = v[1];
-    v[0] = cadd(a, b);
-    v[1] = csub(a, b);
+template <class A>
+struct DFT<A, 2> {
+  using C = typename A::C;
+  __device__ __forceinline__ static void run(C (&v)[2]) {
+    const C a = v[0], b = v[1];
+    v[0] = A::cadd(a, b);
+    v[1] = A::csub(a, b);
   }
 };
 
-__device__ __forceinline__ float4 mul_mi(float4 t) { return make_float4(t.z, t.w, -t.x, -t.y); }  // -i t
-__device__ __forceinline__ float4 mul_pi(float4 t) { return make_float4(-t.z, -t.w, t.x, t.y); }  // +i t
-
-__device__ __forceinline__ void dft4(float4& v0, float4& v1, float4& v2, float4& v3) {
-  const float4 t0 = cadd(v0, v2), t1 = csub(v0, v2), t2 = cadd(v1, v3), t3 = csub(v1, v3);
-  v0 = cadd(t0, t2);
-  v2 = csub(t0, t2);
-  v1 = cadd(t1, mul_mi(t3));  // t1 - i t3
-  v3 = cadd(t1, mul_pi(t3));  // t1 + i t3
+template <class A>
+__device__ __forceinline__ void dft4(typename A::C& v0, typename A::C& v1, typename A::C& v2, typename A::C& v3) {
+  using C = typename A::C;
+  const C t0 = A::cadd(v0, v2), t1 = A::csub(v0, v2), t2 = A::cadd(v1, v3), t3 = A::csub(v1, v3);
+  v0 = A::cadd(t0, t2);
+  v2 = A::csub(t0, t2);
+  v1 = A::cadd(t1, A::mul_mi(t3));  // t1 - i t3
+  v3 = A::cadd(t1, A::mul_pi(t3));  // t1 + i t3
 }
 
-template <>
-struct DFT<4> {
-  __device__ __forceinline__ static void run(float4 (&v)[4]) { dft4(v[0], v[1], v[2], v[3]); }
+template <class A>
+struct DFT<A, 4> {
+  using C = typename A::C;
+  __device__ __forceinline__ static void run(C (&v)[4]) { dft4<A>(v[0], v[1], v[2], v[3]); }
 };
 
-template <>
-struct DFT<8> {
-  __device__ __forceinline__ static void run(float4 (&v)[8]) {
-    float4 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
-    float4 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
-    dft4(e0, e1, e2, e3);
-    dft4(o0, o1, o2, o3);
-    const float2 r = make_float2(0.7071067690849304f, 1.2101617485882343e-08f);  // 1/sqrt(2) as hi + lo
+template <class A>
+struct DFT<A, 8> {
+  using C = typename A::C;
+  using R = typename A::R;
+  __device__ __forceinline__ static void run(C (&v)[8]) {
+    C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    C o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<A>(e0, e1, e2, e3);
+    dft4<A>(o0, o1, o2, o3);
+    const R r = A::rsqrt2();
     // W8^1 o1 = ((x+y) + i(y-x))/sqrt2 ; W8^2 o2 = -i o2 ; W8^3 o3 = ((y-x) - i(x+y))/sqrt2
-    const float2 s1 = ff::add(ff::re(o1), ff::im(o1)), d1 = ff::sub(ff::im(o1), ff::re(o1));
-    const float2 s3 = ff::add(ff::re(o3), ff::im(o3)), d3 = ff::sub(ff::im(o3), ff::re(o3));
-    const float4 w1 = ff::cplx(ff::mul(s1, r), ff::mul(d1, r));
-    const float4 w2 = mul_mi(o2);
-    const float4 w3 = ff::cplx(ff::mul(d3, r), ff::neg(ff::mul(s3, r)));
-    v[0] = cadd(e0, o0);
-    v[4] = csub(e0, o0);
-    v[1] = cadd(e1, w1);
-    v[5] = csub(e1, w1);
-    v[2] = cadd(e2, w2);
-    v[6] = csub(e2, w2);
-    v[3] = cadd(e3, w3);
-    v[7] = csub(e3, w3);
-  }
-};
-
-// Odd radix: X_k = x0 + sum_m [(v_m + v_{R-m}) cos(2 pi mk/R) - i (v_m - v_{R-m}) sin(2 pi mk/R)].
-template <int R>
-struct DFT {
-  __device__ __forceinline__ static void run(float4 (&v)[R]) {
-    constexpr int H = (R - 1) / 2;
-    float4 s[H], d[H];
-    const float4 x0 = v[0];
-    float4 sum = x0;
-#pragma unroll
-    for (int m = 1; m <= H; ++m) {
-      s[m - 1] = cadd(v[m], v[R - m]);
-      d[m - 1] = csub(v[m], v[R - m]);
-      sum = cadd(sum, s[m - 1]);
-    }
-    v[0] = sum;
-#pragma unroll
-    for (int k = 1; k <= H; ++k) {
-      float2 ar = ff::re(x0), ai = ff::im(x0), br = make_float2(0.0f, 0.0f), bi = make_float2(0.0f, 0.0f);
-#pragma unroll
-      for (int m = 1; m <= H; ++m) {
-        const int idx = (m * k) % R;
-        const float2 c = c_rcos_f[R * (kMaxOddRadix + 1) + idx];
-        const float2 sn = c_rsin_f[R * (kMaxOddRadix + 1) + idx];
-        ar = ff::fma(c, ff::re(s[m - 1]), ar);
-        ai = ff::fma(c, ff::im(s[m - 1]), ai);
-        br = ff::fma(sn, ff::re(d[m - 1]), br);
-        bi = ff::fma(sn, ff::im(d[m - 1]), bi);
-      }
-      v[k] = ff::cplx(ff::add(ar, bi), ff::sub(ai, br));
-      v[R - k] = ff::cplx(ff::sub(ar, bi), ff::add(ai, br));
-    }
+    const R s1 = A::add(A::re(o1), A::im(o1)), d1 = A::sub(A::im(o1), A::re(o1));
+    const R s3 = A::add(A::re(o3), A::im(o3)), d3 = A::sub(A::im(o3), A::re(o3));
+    const C w1 = A::cplx(A::mul(s1, r), A::mul(d1, r));
+    const C w2 = A::mul_mi(o2);
+    const C w3 = A::cplx(A::mul(d3, r), A::neg(A::mul(s3, r)));
+    v[0] = A::cadd(e0, o0);
+    v[4] = A::csub(e0, o0);
+    v[1] = A::cadd(e1, w1);
+    v[5] = A::csub(e1, w1);
+    v[2] = A::cadd(e2, w2);
+    v[6] = A::csub(e2, w2);
+    v[3] = A::cadd(e3, w3);
+    v[7] = A::csub(e3, w3);
   }
 };
 
 // One Stockham radix-R stage over npair transforms of length M held back
 // to back in shared memory.
-template <int R>
-__device__ __forceinline__ void stage(const float4* __restrict__ in, float4* __restrict__ out, int M, int Ns,
-                                      const float4* __restrict__ tw, int npair) {
+template <class A, int R>
+__device__ __forceinline__ void stage(const typename A::C* __restrict__ in, typename A::C* __restrict__ out, int M,
+                                      int Ns, const typename A::C* __restrict__ tw, int npair) {
+  using C = typename A::C;
   const int nbf = M / R;
   const int tws = M / (Ns * R);
   for (int t = threadIdx.x; t < npair * nbf; t += blockDim.x) {
     const int pr = t / nbf;
     const int j = t - pr * nbf;
-    const float4* src = in + pr * M;
-    float4* dst = out + pr * M;
-    float4 v[R];
+    const C* src = in + pr * M;
+    C* dst = out + pr * M;
+    C v[R];
 #pragma unroll
     for (int m = 0; m < R; ++m) v[m] = src[j + m * nbf];
     const int k = j % Ns;
     if (Ns > 1) {
 #pragma unroll
-      for (int m = 1; m < R; ++m) v[m] = cmul(v[m], __ldg(&tw[k * m * tws]));
+      for (int m = 1; m < R; ++m) v[m] = A::cmul(v[m], __ldg(&tw[k * m * tws]));
     }
-    DFT<R>::run(v);
+    DFT<A, R>::run(v);
     const int base = (j - k) * R + k;
 #pragma unroll
     for (int m = 0; m < R; ++m) dst[base + m * Ns] = v[m];
@@ -182,32 +172,34 @@ __device__ __forceinline__ void stage(const float4* __restrict__ in, float4* __r
 // s_m = v_m + v_{R-m} and d_m = v_m - v_{R-m}, in place in the stage's input
 // buffer (free after the stage), and writes X_0 = v_0 + sum s_m; (B) one
 // thread per output pair q = 1..H reads x0, s_m, d_m back from shared
-// memory and writes X_q and X_{R-q}.  The arithmetic and its order per
-// output are DFT<R>'s.
-template <int R>
-__device__ __forceinline__ void stage_odd(float4* __restrict__ in, float4* __restrict__ out, int M, int Ns,
-                                          const float4* __restrict__ tw, int npair) {
+// memory and writes X_q and X_{R-q}:
+//   X_q = x0 + sum_m [s_m cos(2 pi mq/R) - i d_m sin(2 pi mq/R)].
+template <class A, int R>
+__device__ __forceinline__ void stage_odd(typename A::C* __restrict__ in, typename A::C* __restrict__ out, int M,
+                                          int Ns, const typename A::C* __restrict__ tw, int npair) {
+  using C = typename A::C;
+  using Re = typename A::R;
   constexpr int H = (R - 1) / 2;
   const int nbf = M / R;
   const int tws = M / (Ns * R);
   for (int t = threadIdx.x; t < npair * nbf; t += blockDim.x) {
     const int pr = t / nbf;
     const int j = t - pr * nbf;
-    float4* src = in + pr * M;
+    C* src = in + pr * M;
     const int k = j % Ns;
     const int base = (j - k) * R + k;
-    float4 sum = src[j];
+    C sum = src[j];
 #pragma unroll
     for (int m = 1; m <= H; ++m) {
-      float4 a = src[j + m * nbf], b = src[j + (R - m) * nbf];
+      C a = src[j + m * nbf], b = src[j + (R - m) * nbf];
       if (Ns > 1) {
-        a = cmul(a, __ldg(&tw[k * m * tws]));
-        b = cmul(b, __ldg(&tw[k * (R - m) * tws]));
+        a = A::cmul(a, __ldg(&tw[k * m * tws]));
+        b = A::cmul(b, __ldg(&tw[k * (R - m) * tws]));
       }
-      const float4 sm = cadd(a, b);
+      const C sm = A::cadd(a, b);
       src[j + m * nbf] = sm;
-      src[j + (R - m) * nbf] = csub(a, b);
-      sum = cadd(sum, sm);
+      src[j + (R - m) * nbf] = A::csub(a, b);
+      sum = A::cadd(sum, sm);
     }
     out[pr * M + base] = sum;
   }
@@ -217,25 +209,25 @@ __device__ __forceinline__ void stage_odd(float4* __restrict__ in, float4* __res
     const int bf = t / H;
     const int pr = bf / nbf;
     const int j = bf - pr * nbf;
-    const float4* src = in + pr * M;
+    const C* src = in + pr * M;
     const int k = j % Ns;
     const int base = (j - k) * R + k;
-    const float4 x0 = src[j];
-    float2 ar = ff::re(x0), ai = ff::im(x0), br = make_float2(0.0f, 0.0f), bi = make_float2(0.0f, 0.0f);
+    const C x0 = src[j];
+    Re ar = A::re(x0), ai = A::im(x0), br = A::zero(), bi = A::zero();
 #pragma unroll
     for (int m = 1; m <= H; ++m) {
-      const float4 sm = src[j + m * nbf], dm = src[j + (R - m) * nbf];
+      const C sm = src[j + m * nbf], dm = src[j + (R - m) * nbf];
       const int idx = (m * q) % R;
-      const float2 c = c_rcos_f[R * (kMaxOddRadix + 1) + idx];
-      const float2 sn = c_rsin_f[R * (kMaxOddRadix + 1) + idx];
-      ar = ff::fma(c, ff::re(sm), ar);
-      ai = ff::fma(c, ff::im(sm), ai);
-      br = ff::fma(sn, ff::re(dm), br);
-      bi = ff::fma(sn, ff::im(dm), bi);
+      const Re c = rcos<A>(R * (kMaxOddRadix + 1) + idx);
+      const Re sn = rsin<A>(R * (kMaxOddRadix + 1) + idx);
+      ar = A::fma(c, A::re(sm), ar);
+      ai = A::fma(c, A::im(sm), ai);
+      br = A::fma(sn, A::re(dm), br);
+      bi = A::fma(sn, A::im(dm), bi);
     }
-    float4* dst = out + pr * M;
-    dst[base + q * Ns] = ff::cplx(ff::add(ar, bi), ff::sub(ai, br));
-    dst[base + (R - q) * Ns] = ff::cplx(ff::sub(ar, bi), ff::add(ai, br));
+    C* dst = out + pr * M;
+    dst[base + q * Ns] = A::cplx(A::add(ar, bi), A::sub(ai, br));
+    dst[base + (R - q) * Ns] = A::cplx(A::sub(ar, bi), A::add(ai, br));
   }
 }
 
@@ -243,24 +235,26 @@ __device__ __forceinline__ void stage_odd(float4* __restrict__ in, float4* __res
 // instantiates only the power-of-two radices, which keeps the register
 // count (and so the occupancy) of those kernels independent of the large
 // odd-radix butterflies.
-template <bool ODD>
-__device__ float4* fft_all(float4* A, float4* B, const FFTDev& p, int npair) {
+template <class A, bool ODD>
+__device__ typename A::C* fft_all(typename A::C* Abuf, typename A::C* Bbuf, const FFTDev& p, int npair) {
+  using C = typename A::C;
+  const C* tw = twiddles<A>(p);
   int Ns = 1;
   for (int s = 0; s < p.nst; ++s) {
     const int r = p.radix[s];
     switch (r) {
-      case 2: stage<2>(A, B, p.M, Ns, p.tw, npair); break;
-      case 4: stage<4>(A, B, p.M, Ns, p.tw, npair); break;
-      case 8: stage<8>(A, B, p.M, Ns, p.tw, npair); break;
+      case 2: stage<A, 2>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
+      case 4: stage<A, 4>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
+      case 8: stage<A, 8>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
       default:
         if constexpr (ODD) {
           switch (r) {
-            case 3: stage_odd<3>(A, B, p.M, Ns, p.tw, npair); break;
-            case 5: stage_odd<5>(A, B, p.M, Ns, p.tw, npair); break;
-            case 7: stage_odd<7>(A, B, p.M, Ns, p.tw, npair); break;
-            case 11: stage_odd<11>(A, B, p.M, Ns, p.tw, npair); break;
-            case 13: stage_odd<13>(A, B, p.M, Ns, p.tw, npair); break;
-            case 17: stage_odd<17>(A, B, p.M, Ns, p.tw, npair); break;
+            case 3: stage_odd<A, 3>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
+            case 5: stage_odd<A, 5>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
+            case 7: stage_odd<A, 7>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
+            case 11: stage_odd<A, 11>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
+            case 13: stage_odd<A, 13>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
+            case 17: stage_odd<A, 17>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
             default: break;
           }
         }
@@ -268,19 +262,22 @@ __device__ float4* fft_all(float4* A, float4* B, const FFTDev& p, int npair) {
     }
     __syncthreads();
     Ns *= r;
-    float4* t = A;
-    A = B;
-    B = t;
+    C* t = Abuf;
+    Abuf = Bbuf;
+    Bbuf = t;
   }
-  return A;
+  return Abuf;
 }
 
-// In place, the npair * M complex values of a buffer: FP64 -> float-float
-// (same 16 bytes per value).
-__device__ __forceinline__ void to_ff(double2* z, int n) {
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    const double2 v = z[t];
-    reinterpret_cast<float4*>(z)[t] = ff::from_double2(v);
+// In place, the npair * M complex values of a buffer: FP64 -> the policy's
+// complex type (same 16 bytes per value; nothing to do for F64).
+template <class A>
+__device__ __forceinline__ void to_arith(double2* z, int n) {
+  if constexpr (A::kFF) {
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+      const double2 v = z[t];
+      reinterpret_cast<typename A::C*>(z)[t] = A::from2(v);
+    }
   }
 }
 
@@ -301,17 +298,20 @@ __device__ __forceinline__ void odd_extend(double2* z, const FFTDev& p, int npai
 
 // Real-symmetric DST-I, input side: the pair's lines sit in L at 1..n;
 // Z_0 = 0, Z_j = s_j (L_j + L_{N-j}) + (L_j - L_{N-j}) / 2, s_j = sin(pi j / N).
-// The doubles are split into float-float here and Z is float-float.
-__device__ __forceinline__ void rs_pre(const double2* __restrict__ L, float4* __restrict__ Z, const FFTDev& p,
+// The doubles enter the policy's arithmetic here.
+template <class A>
+__device__ __forceinline__ void rs_pre(const double2* __restrict__ L, typename A::C* __restrict__ Z, const FFTDev& p,
                                        int npair) {
+  using C = typename A::C;
+  using R = typename A::R;
   for (int t = threadIdx.x; t < npair * p.N; t += blockDim.x) {
     const int pr = t / p.N, j = t - pr * p.N;
-    float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    C z = A::cplx(A::zero(), A::zero());
     if (j > 0) {
-      const float4 a = ff::from_double2(L[pr * p.M + j]), b = ff::from_double2(L[pr * p.M + p.N - j]);
-      const float2 sj = ff::split(__ldg(&p.sn[j]));
-      z = ff::cplx(ff::fma(sj, ff::add(ff::re(a), ff::re(b)), ff::scale(ff::sub(ff::re(a), ff::re(b)), 0.5f)),
-                   ff::fma(sj, ff::add(ff::im(a), ff::im(b)), ff::scale(ff::sub(ff::im(a), ff::im(b)), 0.5f)));
+      const C a = A::from2(L[pr * p.M + j]), b = A::from2(L[pr * p.M + p.N - j]);
+      const R sj = A::from(__ldg(&p.sn[j]));
+      z = A::cplx(A::fma(sj, A::add(A::re(a), A::re(b)), A::scale(A::sub(A::re(a), A::re(b)), 0.5f)),
+                  A::fma(sj, A::add(A::im(a), A::im(b)), A::scale(A::sub(A::im(a), A::im(b)), 0.5f)));
     }
     Z[pr * p.M + j] = z;
   }
@@ -321,59 +321,62 @@ __device__ __forceinline__ void rs_pre(const double2* __restrict__ L, float4* __
 // Z_{N-m} = c + id the two lines' spectra are F = ((a+c) + i(b-d))/2 and
 // G = ((b+d) - i(a-c))/2, so X_{2m} = (d-b)/2 and (a-c)/2, and the odd
 // outputs are the prefix sums of r_0 = Z_0 / 2, r_m = ((a+c)/2, (b+d)/2).
-// O[pair * M + k] receives X_k of both lines, k = 1..n, in float-float.
+// O[pair * M + k] receives X_k of both lines, k = 1..n.
 // The prefix sum runs over kScanSegs fixed segments of each line in a
 // fixed order, so the result does not depend on the tile shape; Z is its
 // scratch afterwards.
 constexpr int kScanSegs = 32;
-__device__ __forceinline__ void rs_post(float4* __restrict__ Z, float4* __restrict__ O, const FFTDev& p,
+template <class A>
+__device__ __forceinline__ void rs_post(typename A::C* __restrict__ Z, typename A::C* __restrict__ O, const FFTDev& p,
                                         int npair) {
+  using C = typename A::C;
+  using R = typename A::R;
   const int H = p.N >> 1;
   for (int t = threadIdx.x; t < npair * H; t += blockDim.x) {
     const int pr = t / H, m = t - pr * H;
-    const float4 u = Z[pr * p.M + m];
+    const C u = Z[pr * p.M + m];
     if (m == 0) {
-      O[pr * p.M + 1] = ff::cplx(ff::scale(ff::re(u), 0.5f), ff::scale(ff::im(u), 0.5f));
+      O[pr * p.M + 1] = A::cplx(A::scale(A::re(u), 0.5f), A::scale(A::im(u), 0.5f));
     } else {
-      const float4 v = Z[pr * p.M + p.N - m];
-      O[pr * p.M + 2 * m] = ff::cplx(ff::scale(ff::sub(ff::im(v), ff::im(u)), 0.5f),
-                                     ff::scale(ff::sub(ff::re(u), ff::re(v)), 0.5f));
-      O[pr * p.M + 2 * m + 1] = ff::cplx(ff::scale(ff::add(ff::re(u), ff::re(v)), 0.5f),
-                                         ff::scale(ff::add(ff::im(u), ff::im(v)), 0.5f));
+      const C v = Z[pr * p.M + p.N - m];
+      O[pr * p.M + 2 * m] = A::cplx(A::scale(A::sub(A::im(v), A::im(u)), 0.5f),
+                                    A::scale(A::sub(A::re(u), A::re(v)), 0.5f));
+      O[pr * p.M + 2 * m + 1] = A::cplx(A::scale(A::add(A::re(u), A::re(v)), 0.5f),
+                                        A::scale(A::add(A::im(u), A::im(v)), 0.5f));
     }
   }
   __syncthreads();
   // segments per line: min(kScanSegs, H) -- a function of N only; the
-  // scratch (2 npair S float-float values) fits in Z (npair M complex, M >= 2H >= 2S)
+  // scratch (2 npair S real values) fits in Z (npair M complex, M >= 2H >= 2S)
   const int S = min(kScanSegs, H);
-  float2* seg = reinterpret_cast<float2*>(Z);  // [line][S]
-  const int C = (H + S - 1) / S;
+  R* seg = reinterpret_cast<R*>(Z);  // [line][S]
+  const int Cn = (H + S - 1) / S;
   const int nls = 2 * npair * S;
   for (int t = threadIdx.x; t < nls; t += blockDim.x) {  // segment sums
     const int line = t / S, g = t - line * S;
-    const float2* o = reinterpret_cast<const float2*>(O + (line >> 1) * p.M) + (line & 1);  // X_k at o[2k]
-    const int m0 = min(H, g * C), m1 = min(H, m0 + C);
-    float2 sum = make_float2(0.0f, 0.0f);
-    for (int m = m0; m < m1; ++m) sum = ff::add(sum, o[2 * (2 * m + 1)]);
+    const R* o = reinterpret_cast<const R*>(O + (line >> 1) * p.M) + (line & 1);  // X_k at o[2k]
+    const int m0 = min(H, g * Cn), m1 = min(H, m0 + Cn);
+    R sum = A::zero();
+    for (int m = m0; m < m1; ++m) sum = A::add(sum, o[2 * (2 * m + 1)]);
     seg[t] = sum;
   }
   __syncthreads();
   for (int line = threadIdx.x; line < 2 * npair; line += blockDim.x) {  // exclusive scan of the segment sums
-    float2 run = make_float2(0.0f, 0.0f);
+    R run = A::zero();
     for (int g = 0; g < S; ++g) {
-      const float2 v = seg[line * S + g];
+      const R v = seg[line * S + g];
       seg[line * S + g] = run;
-      run = ff::add(run, v);
+      run = A::add(run, v);
     }
   }
   __syncthreads();
   for (int t = threadIdx.x; t < nls; t += blockDim.x) {  // inclusive values inside each segment
     const int line = t / S, g = t - line * S;
-    float2* o = reinterpret_cast<float2*>(O + (line >> 1) * p.M) + (line & 1);
-    const int m0 = min(H, g * C), m1 = min(H, m0 + C);
-    float2 run = seg[t];
+    R* o = reinterpret_cast<R*>(O + (line >> 1) * p.M) + (line & 1);
+    const int m0 = min(H, g * Cn), m1 = min(H, m0 + Cn);
+    R run = seg[t];
     for (int m = m0; m < m1; ++m) {
-      run = ff::add(run, o[2 * (2 * m + 1)]);
+      run = A::add(run, o[2 * (2 * m + 1)]);
       o[2 * (2 * m + 1)] = run;
     }
   }
@@ -383,33 +386,36 @@ __device__ __forceinline__ void rs_post(float4* __restrict__ Z, float4* __restri
 // of the plan's mode, see staging()): returns the buffer holding X_k of
 // line (pair, c) at index pair * M + k (k = 1..n) as component c (rs), or
 // the raw odd-extension spectrum (X_k = -W.y / 2 and W.x / 2).
-// The values in shared memory are float-float from the pre-twiddle (or the
-// odd extension) to the output; dst_out joins them back into doubles.
-template <bool ODD, int PAIRS>
-__device__ __forceinline__ float4* dst_pairs(double2* A, double2* B, const FFTDev& p) {
+// The values in shared memory are in the policy's arithmetic from the
+// pre-twiddle (or the odd extension) to the output; dst_out joins them
+// back into doubles.
+template <class A, bool ODD, int PAIRS>
+__device__ __forceinline__ typename A::C* dst_pairs(double2* Ab, double2* Bb, const FFTDev& p) {
+  using C = typename A::C;
   constexpr int npair = PAIRS;
-  float4* Af = reinterpret_cast<float4*>(A);
-  float4* Bf = reinterpret_cast<float4*>(B);
+  C* Af = reinterpret_cast<C*>(Ab);
+  C* Bf = reinterpret_cast<C*>(Bb);
   if (p.rs) {
-    rs_pre(B, Af, p, npair);
+    rs_pre<A>(Bb, Af, p, npair);
   } else {
-    odd_extend(A, p, npair);
+    odd_extend(Ab, p, npair);
     __syncthreads();
-    to_ff(A, npair * p.M);
+    to_arith<A>(Ab, npair * p.M);
   }
   __syncthreads();
-  float4* R = fft_all<ODD>(Af, Bf, p, npair);
+  C* R = fft_all<A, ODD>(Af, Bf, p, npair);
   if (!p.rs) return R;
-  float4* O = (R == Af) ? Bf : Af;
-  rs_post(R, O, p, npair);
+  C* O = (R == Af) ? Bf : Af;
+  rs_post<A>(R, O, p, npair);
   __syncthreads();
   return O;
 }
 __device__ __forceinline__ double2* staging(double2* A, double2* B, const FFTDev& p) { return p.rs ? B : A; }
-__device__ __forceinline__ double dst_out(const float4* O, const FFTDev& p, int li, int k) {
-  const float4 W = O[(li >> 1) * p.M + (k + 1)];
-  if (p.rs) return ff::to_double((li & 1) ? ff::im(W) : ff::re(W));
-  return ff::to_double((li & 1) ? ff::scale(ff::re(W), 0.5f) : ff::scale(ff::im(W), -0.5f));
+template <class A>
+__device__ __forceinline__ double dst_out(const typename A::C* O, const FFTDev& p, int li, int k) {
+  const typename A::C W = O[(li >> 1) * p.M + (k + 1)];
+  if (p.rs) return A::to((li & 1) ? A::im(W) : A::re(W));
+  return A::to((li & 1) ? A::scale(A::re(W), 0.5f) : A::scale(A::im(W), -0.5f));
 }
 
 // ------------------------------------------------------------ passes ----
@@ -420,7 +426,7 @@ struct Box {
 };
 
 // x pass, forward: rhs (+ folded boundary values) -> work, scaled.
-template <bool ODD, int PAIRS>
+template <class Ar, bool ODD, int PAIRS>
 __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict__ rhs, const double* __restrict__ sol,
                                                         int zero_bc, double* __restrict__ work, Box b, FFTDev p,
                                                         double ihx2, double ihy2, double ihz2, double scale) {
@@ -453,17 +459,17 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict
     zp[li & 1] = v;
   }
   __syncthreads();
-  const float4* R = dst_pairs<ODD, PAIRS>(A, B, p);
+  const typename Ar::C* R = dst_pairs<Ar, ODD, PAIRS>(A, B, p);
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
     const int l = l0 + li;
     if (l >= nlines) continue;
-    work[(size_t)l * n + k] = dst_out(R, p, li, k);
+    work[(size_t)l * n + k] = dst_out<Ar>(R, p, li, k);
   }
 }
 
 // y pass (forward or inverse): in place on work (m0 x m1 x m2, x fastest).
-template <bool ODD, int PAIRS>
+template <class Ar, bool ODD, int PAIRS>
 __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, int m0, int m1, int m2, FFTDev p) {
   extern __shared__ double2 smem[];
   double2* A = smem;
@@ -484,18 +490,18 @@ __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, i
     zp[li & 1] = v;
   }
   __syncthreads();
-  const float4* R = dst_pairs<ODD, PAIRS>(A, B, p);
+  const typename Ar::C* R = dst_pairs<Ar, ODD, PAIRS>(A, B, p);
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t % (2 * PAIRS), k = t / (2 * PAIRS);
     const int l = l0 + li;
     if (l >= nlines) continue;
     const int a = l % m0, c = l / m0;
-    work[(size_t)a + (size_t)m0 * k + plane * c] = dst_out(R, p, li, k);
+    work[(size_t)a + (size_t)m0 * k + plane * c] = dst_out<Ar>(R, p, li, k);
   }
 }
 
 // x pass, inverse: work -> interior of sol.
-template <bool ODD, int PAIRS>
+template <class Ar, bool ODD, int PAIRS>
 __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict__ work, double* __restrict__ sol, Box b,
                                                         FFTDev p) {
   extern __shared__ double2 smem[];
@@ -512,77 +518,79 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict
     zp[li & 1] = v;
   }
   __syncthreads();
-  const float4* R = dst_pairs<ODD, PAIRS>(A, B, p);
+  const typename Ar::C* R = dst_pairs<Ar, ODD, PAIRS>(A, B, p);
   const size_t sy = b.dims[0], sz = (size_t)b.dims[0] * b.dims[1];
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
     const int l = l0 + li;
     if (l >= nlines) continue;
     const int q = l % b.m[1], c = l / b.m[1];
-    sol[(size_t)(b.o[0] + k) + sy * (b.o[1] + q) + sz * (b.o[2] + c)] = dst_out(R, p, li, k);
+    sol[(size_t)(b.o[0] + k) + sy * (b.o[1] + q) + sz * (b.o[2] + c)] = dst_out<Ar>(R, p, li, k);
   }
 }
 
-// z pass: Thomas sweep per (p,q) with the reciprocal pivot table, in
-// float-float arithmetic (ff.cuh): the forward sweep leaves its values in
-// place as float-float pairs, the backward sweep writes the doubles.  The
-// column's loads are issued four planes ahead of the dependent chain (the
-// sweep is latency-bound otherwise).
-__global__ void k_thomas(double* __restrict__ g, const float2* __restrict__ rinv, int m0, int m1, int m2) {
+// z pass: Thomas sweep per (p,q) with the reciprocal pivot table (FP64:
+// rinvd, float-float: rinvf), in the policy's arithmetic: the forward
+// sweep leaves its values in place in that arithmetic, the backward sweep
+// writes the doubles.  The column's loads are issued four planes ahead of
+// the dependent chain (the sweep is latency-bound otherwise).
+template <class A>
+__global__ void k_thomas(double* __restrict__ g, const typename A::R* __restrict__ rinv, int m0, int m1, int m2) {
+  using R = typename A::R;
   const int pq = blockIdx.x * blockDim.x + threadIdx.x;
   if (pq >= m0 * m1) return;
   const size_t plane = (size_t)m0 * m1;
-  float2* gf = reinterpret_cast<float2*>(g);
-  float2 y = ff::split(g[pq]);
+  R* gf = reinterpret_cast<R*>(g);
+  R y = A::from(g[pq]);
   gf[pq] = y;
-  float2 ri = rinv[pq];
+  R ri = rinv[pq];
   int c = 1;
   for (; c + 3 < m2; c += 4) {
     const size_t id = pq + plane * c;
     const double g0 = g[id], g1 = g[id + plane], g2 = g[id + 2 * plane], g3 = g[id + 3 * plane];
-    const float2 r0 = rinv[id], r1 = rinv[id + plane], r2 = rinv[id + 2 * plane], r3 = rinv[id + 3 * plane];
-    y = ff::fma(y, ri, ff::split(g0));
+    const R r0 = rinv[id], r1 = rinv[id + plane], r2 = rinv[id + 2 * plane], r3 = rinv[id + 3 * plane];
+    y = A::fma(y, ri, A::from(g0));
     gf[id] = y;
-    y = ff::fma(y, r0, ff::split(g1));
+    y = A::fma(y, r0, A::from(g1));
     gf[id + plane] = y;
-    y = ff::fma(y, r1, ff::split(g2));
+    y = A::fma(y, r1, A::from(g2));
     gf[id + 2 * plane] = y;
-    y = ff::fma(y, r2, ff::split(g3));
+    y = A::fma(y, r2, A::from(g3));
     gf[id + 3 * plane] = y;
     ri = r3;
   }
   for (; c < m2; ++c) {
     const size_t id = pq + plane * c;
-    y = ff::fma(y, ri, ff::split(g[id]));
+    y = A::fma(y, ri, A::from(g[id]));
     gf[id] = y;
     ri = rinv[id];
   }
-  float2 u = ff::mul(y, ri);
-  g[pq + plane * (m2 - 1)] = ff::to_double(u);
+  R u = A::mul(y, ri);
+  g[pq + plane * (m2 - 1)] = A::to(u);
   c = m2 - 2;
   for (; c - 3 >= 0; c -= 4) {
     const size_t id = pq + plane * c;
-    const float2 g0 = gf[id], g1 = gf[id - plane], g2 = gf[id - 2 * plane], g3 = gf[id - 3 * plane];
-    const float2 r0 = rinv[id], r1 = rinv[id - plane], r2 = rinv[id - 2 * plane], r3 = rinv[id - 3 * plane];
-    u = ff::mul(ff::add(g0, u), r0);
-    g[id] = ff::to_double(u);
-    u = ff::mul(ff::add(g1, u), r1);
-    g[id - plane] = ff::to_double(u);
-    u = ff::mul(ff::add(g2, u), r2);
-    g[id - 2 * plane] = ff::to_double(u);
-    u = ff::mul(ff::add(g3, u), r3);
-    g[id - 3 * plane] = ff::to_double(u);
+    const R g0 = gf[id], g1 = gf[id - plane], g2 = gf[id - 2 * plane], g3 = gf[id - 3 * plane];
+    const R r0 = rinv[id], r1 = rinv[id - plane], r2 = rinv[id - 2 * plane], r3 = rinv[id - 3 * plane];
+    u = A::mul(A::add(g0, u), r0);
+    g[id] = A::to(u);
+    u = A::mul(A::add(g1, u), r1);
+    g[id - plane] = A::to(u);
+    u = A::mul(A::add(g2, u), r2);
+    g[id - 2 * plane] = A::to(u);
+    u = A::mul(A::add(g3, u), r3);
+    g[id - 3 * plane] = A::to(u);
   }
   for (; c >= 0; --c) {
     const size_t id = pq + plane * c;
-    u = ff::mul(ff::add(gf[id], u), rinv[id]);
-    g[id] = ff::to_double(u);
+    u = A::mul(A::add(gf[id], u), rinv[id]);
+    g[id] = A::to(u);
   }
 }
 
-// Reciprocal pivots 1/d, 1/(d - r), ... in FP64, stored as float-float
-// pairs (and as doubles when rinvd is given).
-__global__ void k_pivots(float2* __restrict__ rinv, double* __restrict__ rinvd, const double* __restrict__ mux,
+// Reciprocal pivots 1/d, 1/(d - r), ... in FP64, stored as doubles (rinvd)
+// and as float-float pairs (rinvf); either may be null.
+__global__ void k_pivots(float2* __restrict__ rinvf, double* __restrict__ rinvd, const double* __restrict__ mux,
                          const double* __restrict__ muy, int m0, int m1, int m2, double cx, double cy) {
   const int pq = blockIdx.x * blockDim.x + threadIdx.x;
   if (pq >= m0 * m1) return;
@@ -590,13 +598,21 @@ __global__ void k_pivots(float2* __restrict__ rinv, double* __restrict__ rinvd, 
   const double d = 2.0 + (mux[p] * cx + muy[q] * cy);
   const size_t plane = (size_t)m0 * m1;
   double r = 1.0 / d;
-  rinv[pq] = ff::split(r);
+  if (rinvf) rinvf[pq] = ff::split(r);
   if (rinvd) rinvd[pq] = r;
   for (int c = 1; c < m2; ++c) {
     r = 1.0 / (d - r);
-    rinv[pq + plane * c] = ff::split(r);
+    if (rinvf) rinvf[pq + plane * c] = ff::split(r);
     if (rinvd) rinvd[pq + plane * c] = r;
   }
+}
+
+void launch_thomas(cudaStream_t s, double* work, const DirichletPlan& P, int arith) {
+  const int nl = P.m[0] * P.m[1];
+  if (arith == VPMG_ARITH_FF48)
+    k_thomas<FF><<<(nl + 127) / 128, 128, 0, s>>>(work, P.rinv.p, P.m[0], P.m[1], P.m[2]);
+  else
+    k_thomas<F64><<<(nl + 127) / 128, 128, 0, s>>>(work, P.rinvd.p, P.m[0], P.m[1], P.m[2]);
 }
 
 __global__ void k_zero_box_faces(double* __restrict__ sol, Box b) {
@@ -630,57 +646,78 @@ __global__ void k_zero_box_faces(double* __restrict__ sol, Box b) {
 size_t tile_smem(const FFTDev& p) { return (size_t)2 * p.pairs * p.M * sizeof(double2); }
 unsigned tile_grid(int lines, const FFTDev& p) { return (unsigned)((lines + 2 * p.pairs - 1) / (2 * p.pairs)); }
 
-template <int PAIRS>
+template <class A, int PAIRS>
 void x_fwd_t(cudaStream_t s, const double* rhs, const double* sol, int zbc, double* work, Box b, FFTDev p,
              double ihx2, double ihy2, double ihz2, double scale) {
   const unsigned g = tile_grid(b.m[1] * b.m[2], p);
-  if (p.odd) k_dst_x_fwd<true, PAIRS><<<g, kThreads, tile_smem(p), s>>>(rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
-  else k_dst_x_fwd<false, PAIRS><<<g, kThreads, tile_smem(p), s>>>(rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+  if (p.odd)
+    k_dst_x_fwd<A, true, PAIRS><<<g, kThreads, tile_smem(p), s>>>(rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+  else
+    k_dst_x_fwd<A, false, PAIRS><<<g, kThreads, tile_smem(p), s>>>(rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
 }
-template <int PAIRS>
+template <class A, int PAIRS>
 void y_t(cudaStream_t s, double* work, int m0, int m1, int m2, FFTDev p) {
   const unsigned g = tile_grid(m0 * m2, p);
-  if (p.odd) k_dst_y<true, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, m0, m1, m2, p);
-  else k_dst_y<false, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, m0, m1, m2, p);
+  if (p.odd) k_dst_y<A, true, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, m0, m1, m2, p);
+  else k_dst_y<A, false, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, m0, m1, m2, p);
 }
-template <int PAIRS>
+template <class A, int PAIRS>
 void x_inv_t(cudaStream_t s, const double* work, double* sol, Box b, FFTDev p) {
   const unsigned g = tile_grid(b.m[1] * b.m[2], p);
-  if (p.odd) k_dst_x_inv<true, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, sol, b, p);
-  else k_dst_x_inv<false, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, sol, b, p);
+  if (p.odd) k_dst_x_inv<A, true, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, sol, b, p);
+  else k_dst_x_inv<A, false, PAIRS><<<g, kThreads, tile_smem(p), s>>>(work, sol, b, p);
+}
+template <class A>
+void launch_x_fwd_a(cudaStream_t s, const double* rhs, const double* sol, int zbc, double* work, Box b, FFTDev p,
+                    double ihx2, double ihy2, double ihz2, double scale) {
+  if (p.pairs == 2) x_fwd_t<A, 2>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+  else if (p.pairs == 8) x_fwd_t<A, 8>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+  else x_fwd_t<A, 4>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+}
+template <class A>
+void launch_y_a(cudaStream_t s, double* work, int m0, int m1, int m2, FFTDev p) {
+  if (p.pairs == 2) y_t<A, 2>(s, work, m0, m1, m2, p);
+  else if (p.pairs == 8) y_t<A, 8>(s, work, m0, m1, m2, p);
+  else y_t<A, 4>(s, work, m0, m1, m2, p);
+}
+template <class A>
+void launch_x_inv_a(cudaStream_t s, const double* work, double* sol, Box b, FFTDev p) {
+  if (p.pairs == 2) x_inv_t<A, 2>(s, work, sol, b, p);
+  else if (p.pairs == 8) x_inv_t<A, 8>(s, work, sol, b, p);
+  else x_inv_t<A, 4>(s, work, sol, b, p);
 }
 void launch_x_fwd(cudaStream_t s, const double* rhs, const double* sol, int zbc, double* work, Box b, FFTDev p,
                   double ihx2, double ihy2, double ihz2, double scale) {
-  if (p.pairs == 2) x_fwd_t<2>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
-  else if (p.pairs == 8) x_fwd_t<8>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
-  else x_fwd_t<4>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+  if (p.arith == VPMG_ARITH_FF48) launch_x_fwd_a<FF>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
+  else launch_x_fwd_a<F64>(s, rhs, sol, zbc, work, b, p, ihx2, ihy2, ihz2, scale);
 }
 void launch_y(cudaStream_t s, double* work, int m0, int m1, int m2, FFTDev p) {
-  if (p.pairs == 2) y_t<2>(s, work, m0, m1, m2, p);
-  else if (p.pairs == 8) y_t<8>(s, work, m0, m1, m2, p);
-  else y_t<4>(s, work, m0, m1, m2, p);
+  if (p.arith == VPMG_ARITH_FF48) launch_y_a<FF>(s, work, m0, m1, m2, p);
+  else launch_y_a<F64>(s, work, m0, m1, m2, p);
 }
 void launch_x_inv(cudaStream_t s, const double* work, double* sol, Box b, FFTDev p) {
-  if (p.pairs == 2) x_inv_t<2>(s, work, sol, b, p);
-  else if (p.pairs == 8) x_inv_t<8>(s, work, sol, b, p);
-  else x_inv_t<4>(s, work, sol, b, p);
+  if (p.arith == VPMG_ARITH_FF48) launch_x_inv_a<FF>(s, work, sol, b, p);
+  else launch_x_inv_a<F64>(s, work, sol, b, p);
 }
-template <int PAIRS>
+template <class A, int PAIRS>
 cudaError_t set_smem_t(int smax) {
   cudaError_t e = cudaSuccess;
   const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_fwd<true, PAIRS>, a, smax);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_fwd<false, PAIRS>, a, smax);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y<true, PAIRS>, a, smax);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y<false, PAIRS>, a, smax);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<true, PAIRS>, a, smax);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<false, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_fwd<A, true, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_fwd<A, false, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y<A, true, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y<A, false, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<A, true, PAIRS>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<A, false, PAIRS>, a, smax);
   return e;
 }
 cudaError_t set_dst_smem(int smax) {
-  cudaError_t e = set_smem_t<2>(smax);
-  if (e == cudaSuccess) e = set_smem_t<4>(smax);
-  if (e == cudaSuccess) e = set_smem_t<8>(smax);
+  cudaError_t e = set_smem_t<F64, 2>(smax);
+  if (e == cudaSuccess) e = set_smem_t<F64, 4>(smax);
+  if (e == cudaSuccess) e = set_smem_t<F64, 8>(smax);
+  if (e == cudaSuccess) e = set_smem_t<FF, 2>(smax);
+  if (e == cudaSuccess) e = set_smem_t<FF, 4>(smax);
+  if (e == cudaSuccess) e = set_smem_t<FF, 8>(smax);
   return e;
 }
 
@@ -689,13 +726,15 @@ FFTDev dev_plan(const FFTPlan& p) {
   d.n = p.n; d.N = p.N; d.M = p.M; d.nst = p.nst;
   d.rs = p.rs;
   d.pairs = p.pairs;
+  d.arith = p.arith;
   d.sn = p.sn.p;
   d.odd = 0;
   for (int i = 0; i < 24; ++i) {
     d.radix[i] = p.radix[i];
     if (i < p.nst && (p.radix[i] & 1)) d.odd = 1;
   }
-  d.tw = p.tw.p;
+  d.twd = p.twd.p;
+  d.twf = p.tw.p;
   return d;
 }
 
@@ -705,23 +744,43 @@ float2 host_split(double v) {
   return make_float2(hi, (float)(v - (double)hi));
 }
 
-// cos / sin (2 pi i / R) of the odd radices, float-float.
-void odd_radix_tables(float2* hc, float2* hs) {
+// cos / sin (2 pi i / R) of the odd radices, in FP64 and as float-float.
+void odd_radix_tables(double* dc, double* ds, float2* hc, float2* hs) {
   for (int R = 1; R <= kMaxOddRadix; ++R)
     for (int i = 0; i < R; ++i) {
-      hc[R * (kMaxOddRadix + 1) + i] = host_split(std::cos(2.0 * kPI * i / R));
-      hs[R * (kMaxOddRadix + 1) + i] = host_split(std::sin(2.0 * kPI * i / R));
+      const int k = R * (kMaxOddRadix + 1) + i;
+      dc[k] = std::cos(2.0 * kPI * i / R);
+      ds[k] = std::sin(2.0 * kPI * i / R);
+      hc[k] = host_split(dc[k]);
+      hs[k] = host_split(ds[k]);
     }
 }
 
-void ensure_tables() {
-  if (g_tables_ready) return;
-  static float2 hc[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)], hs[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
-  odd_radix_tables(hc, hs);
-  VPMG_CUDA(cudaMemcpyToSymbol(c_rcos_f, hc, sizeof(hc)));
-  VPMG_CUDA(cudaMemcpyToSymbol(c_rsin_f, hs, sizeof(hs)));
-  g_tables_ready = true;
+// The odd-radix constants live in __constant__ memory, held separately on
+// every device: uploaded once per device, with that device current, by the
+// plans and by the allocation-free entry point alike.  The copies come from
+// pageable host memory, so the device is synchronised before the tables
+// are marked ready: kernels on any stream then see the whole tables.
+constexpr int kMaxDevices = 64;
+bool g_tables_ready[kMaxDevices] = {false};
+cudaError_t ensure_tables_status() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  if (g_tables_ready[dev]) return cudaSuccess;
+  static double dc[kRadixTab], ds[kRadixTab];
+  static float2 hc[kRadixTab], hs[kRadixTab];
+  odd_radix_tables(dc, ds, hc, hs);
+  if ((e = cudaMemcpyToSymbol(c_rcos_d, dc, sizeof(dc))) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_rsin_d, ds, sizeof(ds))) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_rcos_f, hc, sizeof(hc))) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_rsin_f, hs, sizeof(hs))) != cudaSuccess) return e;
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
+  g_tables_ready[dev] = true;
+  return cudaSuccess;
 }
+void ensure_tables() { VPMG_CUDA(ensure_tables_status()); }
 
 size_t smem_bytes(const FFTPlan& p, int pairs) { return (size_t)2 * pairs * p.M * sizeof(double2); }
 constexpr size_t kMaxDstSmem = 227 * 1024;
@@ -729,7 +788,6 @@ constexpr size_t kMaxDstSmem = 227 * 1024;
 // The DST kernels' shared-memory limit is an attribute of each kernel on
 // each device, shared by every plan and by the allocation-free entry
 // point: it is only ever raised (set-up time, outside any stream capture).
-constexpr int kMaxDevices = 64;
 size_t g_dst_smem[kMaxDevices] = {0};
 cudaError_t raise_dst_smem_status(size_t need) {
   int dev = 0;
@@ -793,8 +851,9 @@ void tune_pairs(FFTPlan& p, int lines, int m0, int n, int m2, cudaStream_t s) {
 
 }  // namespace
 
-void make_fft_plan(FFTPlan& p, int n) {
+void make_fft_plan(FFTPlan& p, int n, int arith) {
   ensure_tables();
+  p.arith = arith;
   p.n = n;
   p.N = n + 1;
   p.pairs = kDefaultPairs;
@@ -828,6 +887,8 @@ void make_fft_plan(FFTPlan& p, int n) {
   }
   p.tw.ensure(p.M);
   VPMG_CUDA(cudaMemcpy(p.tw.p, hf.data(), sizeof(float4) * p.M, cudaMemcpyHostToDevice));
+  p.twd.ensure(p.M);
+  VPMG_CUDA(cudaMemcpy(p.twd.p, h.data(), sizeof(double2) * p.M, cudaMemcpyHostToDevice));
   if (p.rs) {
     std::vector<double> sn(p.N);
     for (int j = 0; j < p.N; ++j) sn[j] = std::sin(kPI * (double)j / (double)p.N);
@@ -836,19 +897,22 @@ void make_fft_plan(FFTPlan& p, int n) {
   }
 }
 
-void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], const double h[3], cudaStream_t s) {
-  bool same = P.ready;
+void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], const double h[3], cudaStream_t s,
+                       int arith) {
+  VPMG_CHECK(arith == VPMG_ARITH_FP64 || arith == VPMG_ARITH_FF48, VPMG_ERR_ARG, "unknown arithmetic");
+  bool same = P.ready && P.arith == arith;
   for (int d = 0; d < 3; ++d) same = same && P.dims[d] == dims[d] && P.h[d] == h[d];
   for (int d = 0; d < 6; ++d) same = same && P.box[d] == box[d];
   if (same) return;
   for (int d = 0; d < 3; ++d) { P.dims[d] = dims[d]; P.h[d] = h[d]; }
   for (int d = 0; d < 6; ++d) P.box[d] = box[d];
+  P.arith = arith;
   for (int d = 0; d < 3; ++d) {
     P.m[d] = box[d + 3] - box[d] - 1;
     VPMG_CHECK(P.m[d] >= 1, VPMG_ERR_ARG, "Dirichlet box without interior");
   }
-  make_fft_plan(P.fx, P.m[0]);
-  make_fft_plan(P.fy, P.m[1]);
+  make_fft_plan(P.fx, P.m[0], arith);
+  make_fft_plan(P.fy, P.m[1], arith);
   VPMG_CHECK(std::max(smem_bytes(P.fx, 2), smem_bytes(P.fy, 2)) <= kMaxDstSmem, VPMG_ERR_UNSUPPORTED,
              "mesh too large for the shared-memory DST");
   tune_pairs(P.fx, P.m[1] * P.m[2], 1, P.m[0], P.m[1] * P.m[2], s);  // rows along x
@@ -883,8 +947,7 @@ void dirichlet_solve(DirichletPlan& P, const double* rhs, double* sol, bool zero
   const double scale = -hz2 * 4.0 / ((double)(P.m[0] + 1) * (double)(P.m[1] + 1));
   launch_x_fwd(s, rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2, 1.0 / hz2, scale);
   launch_y(s, work, P.m[0], P.m[1], P.m[2], py);
-  const int nl = P.m[0] * P.m[1];
-  k_thomas<<<(nl + 127) / 128, 128, 0, s>>>(work, P.rinv.p, P.m[0], P.m[1], P.m[2]);
+  launch_thomas(s, work, P, P.arith);
   launch_y(s, work, P.m[0], P.m[1], P.m[2], py);
   launch_x_inv(s, work, sol, b, px);
   count_launch(5);
@@ -957,9 +1020,8 @@ __device__ __align__(256) double g_static_scratch[kStaticDoubles];
 
 constexpr int kStaticMaxDevices = 64;
 double* g_static_base[kStaticMaxDevices] = {nullptr};
-bool g_static_consts[kStaticMaxDevices] = {false};
 
-__global__ void k_static_tables(float4* __restrict__ twx, int mx, float4* __restrict__ twy, int my,
+__global__ void k_static_tables(double2* __restrict__ twx, int mx, double2* __restrict__ twy, int my,
                                 double* __restrict__ mux, int nx, double* __restrict__ muy, int ny,
                                 double* __restrict__ snx, int sx, double* __restrict__ sny, int sy) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -968,11 +1030,11 @@ __global__ void k_static_tables(float4* __restrict__ twx, int mx, float4* __rest
   if (t < sy) sny[t] = sinpi((double)t / sy);
   if (t < mx) {
     sincospi(-2.0 * t / mx, &sn, &cs);
-    twx[t] = ff::from_double2(make_double2(cs, sn));
+    twx[t] = make_double2(cs, sn);
   }
   if (t < my) {
     sincospi(-2.0 * t / my, &sn, &cs);
-    twy[t] = ff::from_double2(make_double2(cs, sn));
+    twy[t] = make_double2(cs, sn);
   }
   if (t < nx) {
     sn = sinpi((t + 1) / (2.0 * (nx + 1)));
@@ -986,12 +1048,14 @@ __global__ void k_static_tables(float4* __restrict__ twx, int mx, float4* __rest
 
 // Radix list of the DST-I of n points (no allocation), in the same form
 // as make_fft_plan (real-symmetric for even N).
-bool static_plan(int n, const float4* tw, const double* sn, FFTDev& d) {
+bool static_plan(int n, const double2* tw, const double* sn, FFTDev& d) {
   d.n = n;
   d.N = n + 1;
   d.rs = (d.N % 2 == 0) ? 1 : 0;
   d.M = d.rs ? d.N : 2 * d.N;
-  d.tw = tw;
+  d.arith = VPMG_ARITH_FP64;
+  d.twd = tw;
+  d.twf = nullptr;
   d.sn = sn;
   int m = d.M, twos = 0, odd[24], no = 0;
   while (m % 2 == 0) { m /= 2; ++twos; }
@@ -1041,21 +1105,16 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
     }
     g_static_base[dev] = static_cast<double*>(p);
   }
-  if (!g_static_consts[dev]) {
-    static float2 hc[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)], hs[(kMaxOddRadix + 1) * (kMaxOddRadix + 1)];
-    odd_radix_tables(hc, hs);
-    if (cudaMemcpyToSymbol(c_rcos_f, hc, sizeof(hc)) != cudaSuccess ||
-        cudaMemcpyToSymbol(c_rsin_f, hs, sizeof(hs)) != cudaSuccess) {
-      cudaGetLastError();
-      return VPMG_ERR_CUDA;
-    }
-    g_static_consts[dev] = true;
+  if (ensure_tables_status() != cudaSuccess) {
+    cudaGetLastError();
+    return VPMG_ERR_CUDA;
   }
+  // FP64 throughout, as the handle-based solves by default
   double* base = g_static_base[dev];
   double* work = base;
-  float2* rinv = reinterpret_cast<float2*>(base + kStaticMaxInterior);  // 8 bytes per pivot
-  float4* twx = reinterpret_cast<float4*>(base + 2 * kStaticMaxInterior);  // float-float twiddles, 16 B each
-  float4* twy = twx + kStaticTw;
+  double* rinv = base + kStaticMaxInterior;                                  // reciprocal pivots
+  double2* twx = reinterpret_cast<double2*>(base + 2 * kStaticMaxInterior);  // twiddles, 16 B each
+  double2* twy = twx + kStaticTw;
   double* mux = reinterpret_cast<double*>(twy + kStaticTw);
   double* muy = mux + kStaticMaxLine;
   double* snx = muy + kStaticMaxLine;
@@ -1077,13 +1136,13 @@ extern "C" int vpmg_dirichlet_static(const double* rhs, double* sol, const int d
                                                    px.rs ? px.N : 0, sny, py.rs ? py.N : 0);
   const double hz2 = h[2] * h[2], hx2 = h[0] * h[0], hy2 = h[1] * h[1];
   const int nl = m[0] * m[1];
-  k_pivots<<<(nl + 255) / 256, 256, 0, s>>>(rinv, nullptr, mux, muy, m[0], m[1], m[2], hz2 / hx2, hz2 / hy2);
+  k_pivots<<<(nl + 255) / 256, 256, 0, s>>>(nullptr, rinv, mux, muy, m[0], m[1], m[2], hz2 / hx2, hz2 / hy2);
   Box b;
   for (int d = 0; d < 3; ++d) { b.dims[d] = dims[d]; b.o[d] = box[d] + 1; b.m[d] = m[d]; }
   const double scale = -hz2 * 4.0 / ((double)(m[0] + 1) * (double)(m[1] + 1));
   launch_x_fwd(s, rhs, sol, zero_bc ? 1 : 0, work, b, px, 1.0 / hx2, 1.0 / hy2, 1.0 / hz2, scale);
   launch_y(s, work, m[0], m[1], m[2], py);
-  k_thomas<<<(nl + 127) / 128, 128, 0, s>>>(work, rinv, m[0], m[1], m[2]);
+  k_thomas<F64><<<(nl + 127) / 128, 128, 0, s>>>(work, rinv, m[0], m[1], m[2]);
   launch_y(s, work, m[0], m[1], m[2], py);
   launch_x_inv(s, work, sol, b, px);
   if (zero_bc) k_zero_box_faces<<<256, 256, 0, s>>>(sol, b);

@@ -81,12 +81,14 @@ struct FFTPlan {
   int n = 0, N = 0, M = 0;
   int rs = 0;
   int pairs = 4;     // line pairs per CTA of the DST kernels (tuned per plan)
+  int arith = VPMG_ARITH_FP64;  // arithmetic of the transforms
   int nst = 0;
   int radix[24];
-  DBuf<float4> tw;   // e^{-2 pi i t / M}, t = 0..M-1, float-float (re.hi, re.lo, im.hi, im.lo)
+  DBuf<double2> twd; // e^{-2 pi i t / M}, t = 0..M-1, FP64
+  DBuf<float4> tw;   // the same as float-float (re.hi, re.lo, im.hi, im.lo)
   DBuf<double> sn;   // sin(pi j / N), j = 0..N-1 (rs only)
 };
-void make_fft_plan(FFTPlan& p, int n);
+void make_fft_plan(FFTPlan& p, int n, int arith);
 
 // A Dirichlet box inside a node array of dims dims[3]: nodes box[0..2] to
 // box[3..5] (0-based, inclusive).  Interior m[d] = box[d+3]-box[d]-1.
@@ -95,12 +97,14 @@ struct DirichletPlan {
   int box[6] = {0, 0, 0, 0, 0, 0};
   int m[3] = {0, 0, 0};
   double h[3] = {0, 0, 0};
+  int arith = VPMG_ARITH_FP64;  // arithmetic of the transforms and sweeps
   FFTPlan fx, fy;
   DBuf<float2> rinv;  // reciprocal Thomas pivots, [k][q][p], float-float pairs
-  DBuf<double> rinvd; // the same in FP64, for the FP64 recurrence of the block solves
+  DBuf<double> rinvd; // the same in FP64
   bool ready = false;
 };
-void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], const double h[3], cudaStream_t s);
+void dirichlet_prepare(DirichletPlan& P, const int dims[3], const int box[6], const double h[3], cudaStream_t s,
+                       int arith);
 // Interior of sol <- solution of Lap_h u = rhs with the box faces of sol as
 // boundary values (zero_bc = false) or zero (true; then the box faces of
 // sol are zeroed).  work: >= m0*m1*m2 doubles.
@@ -126,6 +130,7 @@ struct BoundaryOp {
   // panels (level 0) and aggregated levels, device copies
   int nbound = 0, levmax = 0, ncell_total = 0, ntarget = 0;
   int ibctyp = 2;     // 2: point sources -dS/(4 pi r); 3: constant-source panels
+  int arith = VPMG_ARITH_FP64;  // recorded weights and their products: FP64 or float-float
   bool tree = true;   // Bounds3d_lev (tree) or the untreed Bounds3d
   PanelFrame frame[6];                  // ibctyp 3: one per target plane
   std::vector<int> lev_off;    // flat offset of each level's cells
@@ -138,7 +143,7 @@ struct BoundaryOp {
   DBuf<int> agg_istep;
   DBuf<int> anc;                        // [(lev-1)*nbound + leaf]: flat ancestor cell or -1
   DBuf<double> csrc;                    // 3 * ncell_total aggregated sources
-  DBuf<float2> csrc_ff;                 // the same as float-float pairs, [cell][s0 s1 s2 0] (recorded operator)
+  DBuf<float2> csrc_ff;                 // the same packed [cell][s0 s1 s2 0] in 8-byte words (doubles or float-float pairs)
   // panels: face geometry for the normal derivative
   DBuf<int> pan_face, pan_i, pan_j, pan_k;  // lower-corner node (0-based) of each panel
   // targets
@@ -150,9 +155,9 @@ struct BoundaryOp {
   long long nnz = 0;
   DBuf<long long> rowptr;
   DBuf<int> col;
-  DBuf<float2> w;                       // weights dS/r as float-float pairs (hi, lo), hi + lo = dS/r to 2^-48
+  DBuf<float2> w;                       // weights dS/r, 8-byte words: doubles, or float-float pairs (hi + lo = dS/r to 2^-48)
   // the coarsest level, which every target walks in full, as a dense block:
-  // [target / 32][cell][target % 32] float-float weights, zero where the
+  // [target / 32][cell][target % 32] weight words (as w), zero where the
   // cell was opened; the rows above then hold only the finer levels
   bool dense = false;
   int ntopd = 0;                        // cells of the coarsest level
@@ -165,13 +170,13 @@ struct BoundaryOp {
   bool transposed = false;
   DBuf<long long> colptr;
   DBuf<int> trow;
-  DBuf<float2> tw;                      // float-float weights of the transposed list
-  DBuf<float2> vff;                     // per target: the boundary-value adjoint, float-float
+  DBuf<float2> tw;                      // weight words of the transposed list
+  DBuf<float2> vff;                     // per target: the boundary-value adjoint in the operator's arithmetic
   DBuf<double> dpart;                   // dense transpose: partial sums [chunk group][cell]
   long long bytes() const;
 };
 void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s,
-                      int ibctyp = 2, bool tree = true);
+                      int ibctyp, bool tree, int arith);
 // Per component: normal-derivative panels from the zero-BC solution sol0,
 // aggregate, then add the boundary values into the faces of sol.
 void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp, cudaStream_t s);
