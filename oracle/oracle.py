@@ -72,6 +72,7 @@ def lib():
         L.vpmo_remesh.argtypes = [C.POINTER(Config), C.POINTER(Sizes), _dp, _dp, C.c_int, _dp, _dp, C.c_long, C.c_int]
         L.vpmo_remesh.restype = C.c_long
         L.vpmo_diffuse.argtypes = [C.POINTER(Config), C.POINTER(Sizes), _dp, _dp, C.c_double, _dp, C.c_int, C.c_int]
+        L.vpmo_whattodo4.argtypes = [C.POINTER(Config), C.POINTER(Sizes), _dp, _dp, _dp, _dp, C.c_int, C.c_int]
         L.vpmo_remesh_masked.argtypes = [C.POINTER(Config), C.POINTER(Sizes), _dp, _dp, C.c_int, _dp, _dp, C.c_long,
                                          C.c_int, C.POINTER(C.c_int), C.c_int]
         L.vpmo_remesh_masked.restype = C.c_long
@@ -191,6 +192,18 @@ def diffuse(cfg, sizes, xp, qp, ni, nthreads=0):
     if rc != 0:
         raise RuntimeError(f"vpmo_diffuse failed: {rc}")
     return gp
+
+
+def whattodo4(cfg, sizes, xp, qp, up, nthreads=0):
+    """vpm(WhatToDo = 4) after step_fields on the same mesh: returns (up + sum W vel, GP)."""
+    xp = np.ascontiguousarray(xp, dtype=np.float64)
+    qp = np.ascontiguousarray(qp, dtype=np.float64)
+    up = np.array(up, dtype=np.float64, order="C", copy=True)
+    gp = np.zeros((xp.shape[0], 3))
+    rc = lib().vpmo_whattodo4(C.byref(cfg), C.byref(sizes), xp, qp, up, gp, xp.shape[0], nthreads)
+    if rc != 0:
+        raise RuntimeError(f"vpmo_whattodo4 failed: {rc}")
+    return up, gp
 
 
 def get_field(which):

@@ -1351,6 +1351,62 @@ int vpmo_step_fields(const vpmo_config* cfg, const vpmo_sizes* s, const double* 
   return 0;
 }
 
+int vpmo_whattodo4(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, double* up,
+                   double* gp, int nvr, int nthreads) {
+  // vpm(WhatToDo = 4) (vpm.f90:316-343) after an earlier solve: deposition
+  // of these particles (vpm.f90:408-444), calc_velocity_serial_3d(-1)
+  // (vpm_gcalc.f90:1-136: SOL = 0, then the stretching from the new RHS and
+  // the velocity kept from the last solve), back_to_particles_3D(itype = 1)
+  // (vpm_time.f90:62-107: UP = UP + sum W vel, GP = vol sum W SOL).
+  Scratch& W = g_scr;
+  const int NX = s->nn[0], NY = s->nn[1], NZ = s->nn[2];
+  const size_t N = (size_t)NX * NY * NZ;
+  for (int c = 0; c < 3; ++c)
+    if (W.vel[c].size() != N) return -2;  // no resident velocity of this mesh
+  int e = vpmo_project_particles(s, cfg->interf_iproj, xp, qp, nvr, W.rhs[0].data(), W.rhs[1].data(),
+                                 W.rhs[2].data(), nthreads);
+  if (e) return e;
+  const double DX2 = 2 * s->dpm[0], DY2 = 2 * s->dpm[1], DZ2 = 2 * s->dpm[2];
+  const int* nb = s->nn_bl;
+  for (int c = 0; c < 3; ++c) W.def[c].assign(N, 0.0);
+  auto V = [&](int c, int i, int j, int k) { return W.vel[c][lin(NX, NY, i, j, k)]; };
+  auto RH = [&](int c, int i, int j, int k) { return W.rhs[c][lin(NX, NY, i, j, k)]; };
+  for (int k = nb[2] + 2; k <= nb[5] - 2; ++k)
+    for (int j = nb[1] + 2; j <= nb[4] - 2; ++j)
+      for (int i = nb[0] + 2; i <= nb[3] - 2; ++i) {
+        const size_t id = lin(NX, NY, i, j, k);
+        for (int m = 0; m < 3; ++m) {
+          const double wdudx = -(RH(0, i + 1, j, k) * V(m, i + 1, j, k) - RH(0, i - 1, j, k) * V(m, i - 1, j, k)) / DX2;
+          const double wdvdy = -(RH(1, i, j + 1, k) * V(m, i, j + 1, k) - RH(1, i, j - 1, k) * V(m, i, j - 1, k)) / DY2;
+          const double wdwdz = -(RH(2, i, j, k + 1) * V(m, i, j, k + 1) - RH(2, i, j, k - 1) * V(m, i, j, k - 1)) / DZ2;
+          W.def[m][id] = wdudx + wdvdy + wdwdz;
+        }
+      }
+  const int itype = cfg->interf_iproj;
+  const int ips = (itype == 2) ? 0 : 1, ipf = (itype == 2) ? 1 : 2;
+  const double XMIN = s->xbound[0], YMIN = s->xbound[1], ZMIN = s->xbound[2];
+  const double DX = s->dpm[0], DY = s->dpm[1], DZ = s->dpm[2];
+  for (int nv = 0; nv < nvr; ++nv) {
+    const double px = xp[3 * (size_t)nv], py = xp[3 * (size_t)nv + 1], pz = xp[3 * (size_t)nv + 2];
+    const int inode = (int)((px - XMIN) / DX) + 1, jnode = (int)((py - YMIN) / DY) + 1, knode = (int)((pz - ZMIN) / DZ) + 1;
+    double* u = up + 3 * (size_t)nv;
+    double gl[3] = {0, 0, 0};
+    for (int k = knode - ips; k <= knode + ipf; ++k)
+      for (int j = jnode - ips; j <= jnode + ipf; ++j)
+        for (int i = inode - ips; i <= inode + ipf; ++i) {
+          const double fx = projection_fun(itype, (px - XMIN - (double)(i - 1) * DX) / DX);
+          const double fy = projection_fun(itype, (py - YMIN - (double)(j - 1) * DY) / DY);
+          const double fz = projection_fun(itype, (pz - ZMIN - (double)(k - 1) * DZ) / DZ);
+          const double f = fx * fy * fz;
+          if (i < 1 || i > NX || j < 1 || j > NY || k < 1 || k > NZ) return -1;
+          const size_t id = lin(NX, NY, i, j, k);
+          for (int c = 0; c < 3; ++c) { u[c] = u[c] + f * W.vel[c][id]; gl[c] = gl[c] + f * W.def[c][id]; }
+        }
+    for (int c = 0; c < 3; ++c) gp[3 * (size_t)nv + c] = gl[c] * qp[4 * (size_t)nv + 3];
+  }
+  return 0;
+}
+
 int vpmo_diffuse(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, double ni, double* gp,
                  int nvr, int nthreads) {
   // vpm(WhatToDo = 5) (vpm.f90:345-372): deposition, diffuse_vort_3d

@@ -133,6 +133,10 @@ long vpmo_get_field(int which, double* out, long capacity);
 /* vpm(WhatToDo = 5): deposition, diffuse_vort_3d (SOL = -NI Lap_h RHS on the
  * block interior) and back_to_particles_3D(itype = 2): GP = vol sum W SOL.
  * The fields are kept for vpmo_get_field (RHS, SOL). */
+// vpm(WhatToDo = 4) after vpmo_step_fields: stretching from these particles'
+// deposition and the kept velocity; UP is added to, GP overwritten.
+int vpmo_whattodo4(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, double* up,
+                   double* gp, int nvr, int nthreads);
 int vpmo_diffuse(const vpmo_config* cfg, const vpmo_sizes* s, const double* xp, const double* qp, double ni, double* gp,
                  int nvr, int nthreads);
 
