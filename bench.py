@@ -10,7 +10,11 @@ step, dt = 0.005.  One step = field step (vpm WhatToDo = 2) + forward Euler
 particle-step = particles at the start of a step x 1 step.
 
   value : device-resident steps timed with CUDA events on the library's
-          stream (vpmg_run), inputs resident in HBM.
+          stream (vpmg_run), inputs resident in HBM, every kernel in IEEE
+          FP64 (--arith fp64, the default and the reference's arithmetic).
+  ff48  : the same loop with the heavy kernels in float-float (about 48
+          significant bits), reported beside the FP64 figures, never as the
+          headline.
   e2e   : the same loop through the reference-facing C-ABI calls with host
           arrays (vpm(...,2,...), host Euler, vpm(...,0,...),
           remesh_particles_3d(1)), host<->device copies inside, host clock.
@@ -400,6 +404,75 @@ def run_dirichlet(args, local):
     return 0
 
 
+KERNELS = (  # vpmg_bench_kernel ids: (id, name, launches per step)
+    (0, "k_apply_dense+k_apply_csr (boundary operator, fine block)", 1),
+    (1, "inner-box Dirichlet solve (k_dst_x_fwd, k_dst_y x2, k_thomas, k_dst_x_inv)", 3),
+    (6, "padded-block zero-BC solve where read (k_dst_x_fwd, k_dst_y, k_thomas_faces, k_partial_x/y, "
+        "partial inverses)", 3),
+    (2, "k_deposit (M4' gather deposition; field step and remesh)", 2),
+    (5, "k_m2p (mesh-to-particle gather + Euler)", 1),
+    (4, "k_deformation (stretching)", 1),
+    (3, "k_velocity (curl)", 1),
+    (7, "k_remesh_flags + scan", 1),
+)
+
+
+def kernel_rooflines(h, fp64_tflops, hbm_gbs, traffic):
+    """Per-kernel figures replayed on the resident state: the algorithmic
+    FP64 flops (FMA = 2) and HBM bytes per launch against the measured FP64
+    peak and HBM bandwidth; the bound is the resource whose time at peak is
+    longer, and frac = that time / the measured time."""
+    out = []
+    for which, name, per_step in KERNELS:
+        try:
+            kms, fl, by = h.bench_kernel(which, reps=3)
+        except Exception as e:  # not available on this handle (several YAPS blocks)
+            out.append({"kernel": name, "error": str(e)})
+            continue
+        t = kms * 1e-3
+        tf, gbs = fl / t / 1e12, by / t / 1e9
+        t_fp, t_hbm = fl / (fp64_tflops * 1e12), by / (hbm_gbs * 1e9)
+        if t_fp >= t_hbm:
+            r = {"bound": "fp64", "achieved": tf, "peak": fp64_tflops, "unit": "TFLOP/s", "frac": t_fp / t}
+        else:
+            r = {"bound": "hbm", "achieved": gbs, "peak": hbm_gbs, "unit": "GB/s", "frac": t_hbm / t}
+        r.update({"kernel": name, "ms_per_launch": kms, "launches_per_step": per_step,
+                  "ms_per_step": kms * per_step, "fp64_tflops": tf, "fp64_frac": t_fp / t, "hbm_gbs": gbs,
+                  "hbm_frac": t_hbm / t, "flops": fl, "bytes": by,
+                  "traffic": traffic.get(name.split(" ")[0])})
+        out.append(r)
+    return out
+
+
+def device_resident(V, cfg, xp, qp, w, args, local, dist, arith, clocks=None):
+    """Set-up (sizes, plans, recorded operator, first remesh) and the timed
+    device-resident loop in one arithmetic."""
+    import torch
+    torch.cuda.set_device(local)
+    free0 = torch.cuda.mem_get_info(local)[0]
+    t0 = time.perf_counter()
+    h = V.VPM(cfg, device=local, arith=arith)
+    if args.operator_budget >= 0:
+        h.set_operator_budget(args.operator_budget)
+    h.define_sizes(xp)
+    xr, qr = h.remesh_particles_3d(1, xp, qp)
+    h.set_particles(xr, qr)
+    setup_s = time.perf_counter() - t0
+    hbm_bytes = free0 - torch.cuda.mem_get_info(local)[0]
+    dt = w["dt"]
+    if args.warmup:
+        h.run(args.warmup, dt)
+    dist.barrier()
+    if clocks:
+        clocks.start()
+    l0 = h.kernel_launches()
+    ms, ps = h.run(args.steps, dt)
+    launches = h.kernel_launches() - l0
+    clk = clocks.stop() if clocks else {}
+    dist.barrier()
+    return h, xr, ms, ps, launches, clk, setup_s, hbm_bytes
+
+
 def run_ours(args, dist):
     import vpm_free_gb300 as V
     from vpm_free_gb300 import build as B
@@ -410,78 +483,39 @@ def run_ours(args, dist):
     xp, qp, w = _workload(args.workload)
     blocks = tuple(int(v) for v in args.blocks.split(","))
     cfg = V.VPMConfig.make(dpm=w["dpm"], box=w["box"], nb=blocks)
-    h = V.VPM(cfg, device=local)
-    if args.operator_budget >= 0:
-        h.set_operator_budget(args.operator_budget)
-    h.define_sizes(xp)
-    xr, qr = h.remesh_particles_3d(1, xp, qp)
-    h.set_particles(xr, qr)
+    h, xr, ms, ps, launches, clk, setup_s, hbm_bytes = device_resident(
+        V, cfg, xp, qp, w, args, local, dist, args.arith, Clocks(local) if rank == 0 else None)
     dt = w["dt"]
-    # warm-up (untimed)
-    if args.warmup:
-        h.run(args.warmup, dt)
-    dist.barrier()
-    clocks = Clocks(local)
-    if rank == 0:
-        clocks.start()
-    l0 = h.kernel_launches()
-    ms, ps = h.run(args.steps, dt)
-    launches = h.kernel_launches() - l0
-    clk = clocks.stop() if rank == 0 else {}
-    dist.barrier()
     t_max = dist.reduce(ms, "max")
     ps_all = dist.reduce(ps, "sum")
     value = ps_all / (t_max * 1e-3)
     # ---- per-kernel roofline figures (replays on the resident state) -------
     fp64 = h.fp64_peak()
     peaks = _measured_peaks()
-    kernels = []
-    for which, name, per_step in ((0, "k_apply_dense+k_apply_csr (boundary operator, fine block)", 1),
-                                  (1, "inner-box Dirichlet solve (k_dst_x_fwd, k_dst_y x2, k_thomas, k_dst_x_inv)", 3),
-                                  (2, "k_deposit (M4' gather deposition)", 2)):
-        kms, fl, by = h.bench_kernel(which, reps=3)
-        kernels.append({"kernel": name, "ms_per_launch": kms, "launches_per_step": per_step,
-                        "share_ms_per_step": kms * per_step, "flops": fl, "bytes": by})
-    dom = max(kernels, key=lambda k: k["share_ms_per_step"])
-    traffic = _traffic_table()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
-    roofs = []
-    for k in kernels:
-        tf = k["flops"] / (k["ms_per_launch"] * 1e-3) / 1e12
-        gbs = k["bytes"] / (k["ms_per_launch"] * 1e-3) / 1e9
-        if k["kernel"].startswith("k_apply"):
-            # float-float product on the FP32 pipes: bound by streaming the
-            # recorded operator (12 bytes per row entry: cell id + weight
-            # pair; 8 bytes per dense-block slot)
-            r = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
-                 "fp64_equivalent_tflops": tf}
-        elif k["kernel"].startswith("k_deposit"):
-            # the gather computes in float-float on the FP32 pipes: its figure
-            # is the 8 FP64 flops x 64 nodes per particle it replaces, as a
-            # fraction of the FP64 DFMA peak; the HBM fraction of the
-            # algorithmic bytes is kept beside it
-            r = {"bound": "fp64-equivalent", "achieved": tf, "peak": fp64, "unit": "TFLOP/s", "frac": tf / fp64,
-                 "arithmetic": "float-float on the FP32 pipes", "hbm_achieved_gbs": gbs, "hbm_frac": gbs / hbm}
-        else:
-            # computed in float-float on the FP32 pipes; the fraction is of the
-            # FP64 DFMA peak, counting the algorithmic FP64 flops it replaces
-            r = {"bound": "fp64-equivalent", "achieved": tf, "peak": fp64, "unit": "TFLOP/s", "frac": tf / fp64,
-                 "arithmetic": "float-float on the FP32 pipes"}
-        r["kernel"] = k["kernel"]
-        r["ms_per_launch"] = k["ms_per_launch"]
-        r["traffic"] = traffic.get(k["kernel"].split(" ")[0])
-        roofs.append(r)
-    roof = dict(roofs[kernels.index(dom)])
-    roof["peak_source"] = ("HBM: MEASURED_PEAKS.json hbm_gbs (of measured); FP64: DFMA-loop TFLOP/s measured in "
-                           "this run (no FP64 entry in MEASURED_PEAKS.json)")
+    roofs = kernel_rooflines(h, fp64, hbm, _traffic_table())
+    timed = [r for r in roofs if "error" not in r]
+    dom = max(timed, key=lambda r: r["ms_per_step"])
+    roof = {k: dom[k] for k in ("bound", "achieved", "peak", "unit", "frac", "kernel", "ms_per_launch", "traffic")}
+    roof["peak_source"] = ("FP64: DFMA-loop TFLOP/s measured in this run (MEASURED_PEAKS.json has no FP64 entry); "
+                           "HBM: MEASURED_PEAKS.json hbm_gbs (of measured)")
+    roof["hbm_frac"] = dom["hbm_frac"]
     tree = h.tree_stats()
     tiles = h.dst_tiles()
     sizes_bl = list(h.sizes().nnbl)
     sizes_nn = list(h.sizes().nn)
     np_end = h.num_particles()
+    phases = None
+    if args.workload == "leapfrog256":
+        h.set_profiling(1)
+        h.step(dt)
+        phases = dict(zip(["deposit", "fine_zero_bc", "boundary", "fine_bc", "coarse", "final", "fd", "m2p+euler",
+                           "remesh"], [round(v, 3) for v in h.phase_times()]))
+        h.set_profiling(0)
+    h.close()
     # ---- end to end through the reference-facing calls, host arrays -------
     ke = max(1, min(args.steps, args.e2e_steps))
-    he = V.VPM(cfg, device=local)
+    he = V.VPM(cfg, device=local, arith=args.arith)
     if args.operator_budget >= 0:
         he.set_operator_budget(args.operator_budget)
     he.vpm(xp, qp, None, None, xp.shape[0], WhatToDo=0, NTIME=0)
@@ -515,15 +549,35 @@ def run_ours(args, dist):
         he.vpm(XP[:n], QP[:n], None, None, n, WhatToDo=0, NTIME=it + 1)
         n_old = n
         n = he.remesh_in_place(XP, QP, n)
-        h2d += n_old * 7 * 8 * 2
+        # vpm(2): XP, QP and UP in, UP and GP out; remesh: XP, QP in, the new set out
+        h2d += n_old * (3 + 4 + 3) * 8 + n_old * 7 * 8
         d2h += n_old * 6 * 8 + n * 7 * 8
     te = time.perf_counter() - t0
     te_max = dist.reduce(te, "max")
+    he.close()
     e2e = {"value": dist.reduce(eps, "sum") / te_max, "unit": UNIT, "h2d_bytes_per_step": h2d // ke,
            "d2h_bytes_per_step": d2h // ke, "steps": ke,
            "timing": "host clock around synchronous vpm()/remesh_particles_3d() C-ABI calls on pinned host arrays "
                      "of NVRM rows; between them the host zeroes UP/GP (memset) and runs the Euler update in one "
                      "compiled single-threaded pass (vpmg_host_euler), as the reference's test.f90 loop does"}
+    # ---- the float-float arithmetic, labelled separately --------------------
+    ff = None
+    if args.arith == "fp64" and not args.no_ff48 and ws == 1:
+        hf, _, ms_f, ps_f, _, clk_f, setup_f, hbm_f = device_resident(V, cfg, xp, qp, w, args, local, dist, "ff48",
+                                                                     Clocks(local))
+        roofs_f = kernel_rooflines(hf, fp64, hbm, {})
+        timed_f = [r for r in roofs_f if "error" not in r]
+        dom_f = max(timed_f, key=lambda r: r["ms_per_step"])
+        hf.close()
+        ff = {"dtype": "ff48", "value": ps_f / (ms_f * 1e-3), "unit": UNIT, "ms_per_step": ms_f / args.steps,
+              "steps": args.steps, "setup_s": setup_f, "hbm_bytes": hbm_f, "clocks": clk_f,
+              "arithmetic": ("float-float (hi + lo floats, about 48 significant bits, magnitudes 1e-38..3e38) in the "
+                             "boundary operator, DST solves, projection weights, deposition, stretching and "
+                             "mesh-to-particle kernels on the FP32 pipes; the rest FP64; parity with the FP64 oracle "
+                             "<= 1e-10 (fields), <= 1e-9 (particles)"),
+              "dominant_kernel": {k: dom_f[k] for k in ("kernel", "ms_per_launch", "fp64_tflops", "hbm_gbs",
+                                                        "hbm_frac")},
+              "kernels": [{k: r[k] for k in ("kernel", "ms_per_launch", "hbm_gbs", "hbm_frac")} for r in timed_f]}
     # ---- CPU baseline (rank 0, N = 1, bounded sample) -----------------------
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu and args.workload == "leapfrog256" and blocks == (1, 1, 1):
@@ -531,21 +585,19 @@ def run_ours(args, dist):
         v, t, _ = cpu_step_sample(xp, qp, w, 1, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"1 full step (field step + Euler + remesh) of this workload, {t:.1f} s on {threads} threads"}
-    h.close()
-    he.close()
     batched = None
     if not args.no_batched and args.workload == "leapfrog256":
         batched = run_batched(args, local)
     adjoint = None
     if not args.no_adjoint and args.workload == "leapfrog256":
         adjoint = run_adjoint(args, local)
+    arith_text = ("IEEE FP64 in every kernel (the reference's REAL(8)); no tensor cores: no step is a dense "
+                  "contraction" if args.arith == "fp64" else ff["arithmetic"] if ff else "float-float heavy kernels")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded leapfrogging rings)",
-        "arithmetic": ("FP64 arrays and interface; the boundary operator, DST solves, projection weights, deposition, "
-                       "stretching and mesh-to-particle kernels compute in float-float (about 48 significant bits) "
-                       "on the FP32 pipes; parity with the FP64 oracle <= 1e-10 (fields), <= 1e-9 (particles)"),
+        "dtype": "f64" if args.arith == "fp64" else "ff48", "data": "synthetic (seeded leapfrogging rings)",
+        "arithmetic": arith_text,
         "config": {"workload": ("leapfrog256 (two coaxial rings, 256^3 mesh, M4', tree levels 3, ncoarse 8, remesh "
                                 "every step, dt 0.005)") if args.workload == "leapfrog256" else args.workload,
                    "mesh": [n - 1 for n in sizes_nn], "block": sizes_bl, "yaps_blocks": list(blocks),
@@ -554,8 +606,12 @@ def run_ours(args, dist):
                           f"{tree.get('bytes', 0) / 1e9:.1f} GB)"),
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "clocks": clk if rank == 0 else None,
-        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "roofline_kernels": roofs,
-        "tree": tree, "dst_tiles_autotuned": tiles, "cpu_baseline": cpu, "batched": batched, "adjoint": adjoint,
+        "setup_s": setup_s, "hbm_bytes": hbm_bytes,
+        "setup": "define_sizes (plans, DST tile autotuning, tree geometry, recorded boundary operator) and the "
+                 "initial remesh, host clock; hbm_bytes = device memory the handle holds after it",
+        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "roofline_kernels": roofs, "phase_ms": phases,
+        "tree": tree, "dst_tiles_autotuned": tiles, "cpu_baseline": cpu, "ff48": ff, "batched": batched,
+        "adjoint": adjoint,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -574,6 +630,9 @@ def main():
                     help="leapfrog256 is the benchmark; the rings are small profiling cases")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-problems measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint:forward measurement")
+    ap.add_argument("--arith", choices=["fp64", "ff48"], default="fp64",
+                    help="arithmetic of the headline run (fp64, the reference's, is the default)")
+    ap.add_argument("--no-ff48", action="store_true", help="skip the float-float run reported beside the FP64 one")
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--batch-operator-budget", type=int, default=12 << 30,
                     help="bytes of recorded boundary operator per batched problem")

@@ -270,12 +270,16 @@ int vpmg_batch_get_schedule(const vpmg_batch* b, int* schedule, float tuned_ms[2
 int vpmg_batch_destroy(vpmg_batch* b);
 /* Replays one kernel of the last step `reps` times between CUDA events on
  * the handle's stream (instrumentation for roofline figures).
- *   which = 0: boundary operator apply on the fine block (k_apply_csr or
- *              the tree walk), 1: one fine-block Dirichlet solve (5 kernels),
- *   2: deposition gather (k_deposit).
- * Outputs: mean device ms per replay, algorithmic FP64 flops and DRAM
- * bytes per replay (figures of the algorithm, not counters).  The replay
- * writes only scratch buffers.                                          */
+ *   which = 0: boundary operator apply on the fine block (recorded operator
+ *              or the tree walk), 1: one inner-box Dirichlet solve (5
+ *              kernels), 2: deposition gather, 3: velocity curl, 4:
+ *              stretching, 5: mesh-to-particle gather, 6: one component of
+ *              the padded block's zero-BC solve evaluated where it is read,
+ *              7: the remesh's |w| flags and their scan.
+ * Outputs: mean device ms per replay, algorithmic FP64 flops (an FMA
+ * counts 2) and DRAM bytes per replay (figures of the algorithm, not
+ * counters).  The replay writes only scratch buffers, the particles'
+ * UP/GP and the binning arrays, all rewritten by the next step.          */
 int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* flops, double* bytes);
 /* FP64 FMA throughput of this GPU (TFLOP/s, FMA = 2 flops) from a
  * register-resident DFMA loop: the roofline peak of the FP64-bound kernels. */

@@ -15,8 +15,10 @@ from helpers import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("shape", [(17, 13, 11), (33, 33, 33), (41, 29, 35)])
+@pytest.mark.parametrize("shape", [(17, 13, 11), (33, 33, 33), (41, 29, 35), (23, 59, 24)])
 def test_dirichlet_matches_oracle(gpulib, oracle, shape):
+    """(23, 59, 24): lines of 57 (N = 58 = 2 x 29) and 22 points (N = 23, odd
+    extension of length 46 = 2 x 23), primes above the specialised radices."""
     V = gpulib
     rng = np.random.default_rng(11)
     nz, ny, nx = shape

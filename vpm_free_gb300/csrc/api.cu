@@ -5,6 +5,7 @@
 // source/vpm.f90:1-32, source/main_pm.f90:2-45).  Fields stay resident in
 // HBM between calls; the Fortran-facing vpm() copies particles in and out.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1276,8 +1277,68 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
       f = [h, o, mg, st] { deposit(h->parts, mg, h->bins, o, st); };
       const double P = (double)read_count(h->bins.nsorted_dev, st);
       const int w = mg.ips + mg.ipf + 1;
-      fl = P * w * w * w * 8.0;
+      fl = P * w * w * w * 7.0;  // per particle-node visit: 1 multiply + 3 FMAs
       by = 56.0 * P + 24.0 * (double)N;
+    } else if (which == 3 || which == 4) {
+      // calc_velocity_serial_3d: 3 = the curl (velocity), 4 = the stretching
+      h->bench_scratch.ensure(6 * N);
+      double* V[3] = {h->bench_scratch.p, h->bench_scratch.p + N, h->bench_scratch.p + 2 * N};
+      double* G[3] = {h->bench_scratch.p + 3 * N, h->bench_scratch.p + 4 * N, h->bench_scratch.p + 5 * N};
+      double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
+      double* S[3] = {comp(h->sol, N, 0), comp(h->sol, N, 1), comp(h->sol, N, 2)};
+      double* Vr[3] = {comp(h->vel, N, 0), comp(h->vel, N, 1), comp(h->vel, N, 2)};
+      float2* VF[3], * GF[3];
+      ff_fields(h, VF, GF);
+      const vpmg_sizes s = h->sz;
+      if (which == 3) {
+        f = [s, S, R, V, G, st] { velocity_and_stretching(s.nn, s.dpm, S, R, V, G, st, 1); };
+        fl = 15.0 * (double)N;  // 6 differences, 6 scalings, 3 combinations per node
+        by = 48.0 * (double)N;  // psi read, u written
+      } else {
+        const bool ff = VF[0] != nullptr;
+        float2* vf[3] = {VF[0], VF[1], VF[2]};
+        float2* gf[3] = {GF[0], GF[1], GF[2]};
+        f = [s, S, R, Vr, G, st, ff, vf, gf] {
+          velocity_and_stretching(s.nn, s.dpm, S, R, const_cast<double* const*>(Vr), G, st, 2, ff ? vf : nullptr,
+                                  ff ? gf : nullptr);
+        };
+        fl = 42.0 * (double)N;  // 3 components x 3 directions x 4 flops + 2 sums
+        by = 72.0 * (double)N;  // RHS and u read, stretching written
+      }
+    } else if (which == 5) {
+      // back_to_particles_3D(1) on the binned particles (UP/GP rewritten in place)
+      const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
+      bin_particles(h->parts, mg, h->bins, st);
+      const double u0[3] = {0.0, 0.0, 0.0};
+      f = [h, u0] { m2p_fields(h, kUpSet, false, 0.0, u0); };
+      const double P = (double)read_count(h->bins.nsorted_dev, st);
+      const int w = mg.ips + mg.ipf + 1;
+      fl = P * w * w * w * 13.0;              // per visit: 1 multiply + 6 FMAs
+      by = 80.0 * P + 48.0 * (double)N;        // X, vol read, UP/GP written; 6 fields read once
+    } else if (which == 6) {
+      // one component of the padded block's zero-BC solve, evaluated where it is read
+      VPMG_CHECK(h->nblk == 1 && h->bsolve.ready, VPMG_ERR_UNSUPPORTED, "one-block handle needed");
+      h->bench_scratch.ensure(NB);
+      double* o = h->bench_scratch.p;
+      f = [h, o, NB, st] { block_solve_zero_bc(h->bsolve, h->dp_bl, h->rhs_bl.p, 0, o, st); };
+      const DirichletPlan& P = h->dp_bl;
+      const double nint = (double)P.m[0] * P.m[1] * P.m[2];
+      // forward x and y transforms, the Thomas sweep, 8 x-layer and 8 y-layer dot products
+      fl = nint * (2.5 * std::log2(2.0 * (P.m[0] + 1)) + 2.5 * std::log2(2.0 * (P.m[1] + 1)) + 4.0 + 32.0);
+      by = 8.0 * nint * 5.0;  // RHS read, transform written, sweep read + written, dots read
+    } else if (which == 7) {
+      // the remesh's |w| flags and their exclusive scan on the remesh grid
+      const Grid gr = hx::remesh_grid(h);
+      const MeshDev mr = mesh_dev(gr, h->cfg.interf_iproj);
+      const vpmg_sizes s = h->sz;
+      const int hh = h->cfg.interf_iproj / 2;
+      const int lo[3] = {s.nn_bl[0] - 1 + hh, s.nn_bl[1] - 1 + hh, s.nn_bl[2] - 1 + hh};
+      const int hi[3] = {s.nn_bl[3] - 1 - hh, s.nn_bl[4] - 1 - hh, s.nn_bl[5] - 1 - hh};
+      double* R[3] = {comp(h->rhs, N, 0), comp(h->rhs, N, 1), comp(h->rhs, N, 2)};
+      std::array<int, 3> l{lo[0], lo[1], lo[2]}, u{hi[0], hi[1], hi[2]};
+      f = [h, mr, R, l, u, st] { remesh_mask(mr, h->bins, R, l.data(), u.data(), (double)1e-09f, st); };
+      fl = 5.0 * (double)N;
+      by = 24.0 * (double)N + 4.0 * (double)N + 8.0 * (double)N;  // |w| read, flags written, scan
     } else {
       throw Error{VPMG_ERR_ARG, "unknown kernel id"};
     }

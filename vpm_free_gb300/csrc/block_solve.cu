@@ -453,26 +453,27 @@ void block_solve_zero_bc(BlockSolve& B, DirichletPlan& P, const double* rhs_c, i
   FaceTerms F{};
   k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(g, B.W.p, P.rinvd.p, m0, m1, m2, 0, F);
   VPMG_LAUNCHED();
-  // x faces: 8 layers by dot products along x, then inverse y
+  // x faces: 8 layers by dot products along x; y faces: 4 + 4 rows by dot products along y
   partial_x(B.arith, B.W.p, m0, m1, m2, nullptr, B.S_fx.p, 8, B.X8.p, s);
-  dst_lines_y(P.fy, B.X8.p, 8, m1, m2, s);
-  scatter3(B.X8.p, 8, m1, m2, B.l_fx.p, nullptr, nullptr, 1, sol0, B.dims, s);
-  // y faces: 4 + 4 rows by dot products along y, then inverse x
-  const int my[3] = {m0, 4, m2};
   double* Y4b = B.Y4.p + (size_t)m0 * 4 * m2;
   partial_y(B.arith, B.W.p, m0, m1, m2, nullptr, B.S_fy_lo.p, 4, B.Y4.p, s, B.S_fy_hi.p, 4, Y4b);
-  const int olo[3] = {1, 1, 1};
-  dst_x_inv_to_box(P.fx, B.Y4.p, sol0, B.dims, olo, my, s);
-  const int ohi[3] = {1, 1 + m1 - 4, 1};
-  dst_x_inv_to_box(P.fx, Y4b, sol0, B.dims, ohi, my, s);
-  // z faces: the first and last 4 planes, full inverse (in place on W, after the dots)
-  const int mz[3] = {m0, m1, 4};
-  dst_lines_y(P.fy, B.W.p, m0, m1, 4, s);
-  dst_x_inv_to_box(P.fx, B.W.p, sol0, B.dims, olo, mz, s);
+  // one launch of inverse y transforms: the x-face layers and the first and
+  // last 4 planes (z faces, in place on W after the dots) ...
   double* top = B.W.p + plane * (m2 - 4);
-  dst_lines_y(P.fy, top, m0, m1, 4, s);
-  const int oz[3] = {1, 1, 1 + m2 - 4};
-  dst_x_inv_to_box(P.fx, top, sol0, B.dims, oz, mz, s);
+  const DstYLines ys[3] = {{&P.fy, B.X8.p, 8, m1, m2}, {&P.fy, B.W.p, m0, m1, 4}, {&P.fy, top, m0, m1, 4}};
+  dst_lines_y_jobs(ys, 3, s);
+  scatter3(B.X8.p, 8, m1, m2, B.l_fx.p, nullptr, nullptr, 1, sol0, B.dims, s);
+  // ... then inverse x transforms into sol0: the y-face rows, then the z
+  // planes.  Jobs of one launch write disjoint nodes; where the rows and the
+  // planes meet (box edges) the planes' launch writes last, every run.
+  const DstXInvLines xr[2] = {
+      {&P.fx, B.Y4.p, sol0, {B.dims[0], B.dims[1], B.dims[2]}, {1, 1, 1}, {m0, 4, m2}},
+      {&P.fx, Y4b, sol0, {B.dims[0], B.dims[1], B.dims[2]}, {1, 1 + m1 - 4, 1}, {m0, 4, m2}}};
+  dst_x_inv_jobs(xr, 2, s);
+  const DstXInvLines xz[2] = {
+      {&P.fx, B.W.p, sol0, {B.dims[0], B.dims[1], B.dims[2]}, {1, 1, 1}, {m0, m1, 4}},
+      {&P.fx, top, sol0, {B.dims[0], B.dims[1], B.dims[2]}, {1, 1, 1 + m2 - 4}, {m0, m1, 4}}};
+  dst_x_inv_jobs(xz, 2, s);
   VPMG_CUDA(cudaGetLastError());
 }
 
@@ -483,14 +484,15 @@ void block_solve_bc(BlockSolve& B, DirichletPlan& P, int c, double* sol_c, cudaS
   k_extract_faces<<<256, 256, 0, s>>>(sol_c, B.dims[0], B.dims[1], B.dims[2], B.fx0.p, B.fxN.p, B.fy0.p, B.fyN.p,
                                       B.fz0.p, B.fzN.p);
   VPMG_LAUNCHED();
-  dst_lines_y(P.fy, B.fx0.p, 1, m1, m2, s);   // rows over j -> q
-  dst_lines_y(P.fy, B.fxN.p, 1, m1, m2, s);
-  dst_lines_y(P.fx, B.fy0.p, 1, m0, m2, s);   // rows over i -> p
-  dst_lines_y(P.fx, B.fyN.p, 1, m0, m2, s);
-  dst_lines_y(P.fx, B.fz0.p, 1, m0, m1, s);   // rows over i, then columns over j
-  dst_lines_y(P.fy, B.fz0.p, m0, m1, 1, s);
-  dst_lines_y(P.fx, B.fzN.p, 1, m0, m1, s);
-  dst_lines_y(P.fy, B.fzN.p, m0, m1, 1, s);
+  // transformed along the face's axes: rows over j -> q (x faces), over i ->
+  // p (y faces, and the z faces' rows), in one launch; then the z faces'
+  // columns over j
+  const DstYLines rows[6] = {{&P.fy, B.fx0.p, 1, m1, m2}, {&P.fy, B.fxN.p, 1, m1, m2},
+                             {&P.fx, B.fy0.p, 1, m0, m2}, {&P.fx, B.fyN.p, 1, m0, m2},
+                             {&P.fx, B.fz0.p, 1, m0, m1}, {&P.fx, B.fzN.p, 1, m0, m1}};
+  dst_lines_y_jobs(rows, 6, s);
+  const DstYLines cols[2] = {{&P.fy, B.fz0.p, m0, m1, 1}, {&P.fy, B.fzN.p, m0, m1, 1}};
+  dst_lines_y_jobs(cols, 2, s);
   const double scale = dirichlet_scale(P);
   FaceTerms F;
   F.fx0 = B.fx0.p; F.fxN = B.fxN.p; F.fy0 = B.fy0.p; F.fyN = B.fyN.p; F.fz0 = B.fz0.p; F.fzN = B.fzN.p;
@@ -501,31 +503,33 @@ void block_solve_bc(BlockSolve& B, DirichletPlan& P, int c, double* sol_c, cudaS
   const double* g = B.ghat.p + (size_t)c * nint;
   k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(g, B.W.p, P.rinvd.p, m0, m1, m2, 1, F);
   VPMG_LAUNCHED();
-  // inner-box x faces
+  // dot products: the inner-box x faces along x, its y faces along y, and
+  // the interior samples along y then x
   partial_x(B.arith, B.W.p, m0, m1, m2, nullptr, B.S_ix.p, 2, B.X2.p, s);
-  dst_lines_y(P.fy, B.X2.p, 2, m1, m2, s);
-  scatter3(B.X2.p, 2, m1, m2, B.l_ix.p, nullptr, nullptr, 1, sol_c, B.dims, s);
-  // inner-box y faces
-  const int m1r[3] = {m0, 1, m2};
   double* Y1b = B.Y1.p + (size_t)m0 * m2;
   partial_y(B.arith, B.W.p, m0, m1, m2, nullptr, B.S_iy_lo.p, 1, B.Y1.p, s, B.S_iy_hi.p, 1, Y1b);
-  const int oylo[3] = {1, B.inner_lo[1] + 1, 1};
-  dst_x_inv_to_box(P.fx, B.Y1.p, sol_c, B.dims, oylo, m1r, s);
-  const int oyhi[3] = {1, B.inner_hi[1] + 1, 1};
-  dst_x_inv_to_box(P.fx, Y1b, sol_c, B.dims, oyhi, m1r, s);
-  // interior samples: dots along y on the sampled planes, then along x
   partial_y(B.arith, B.W.p, m0, m1, B.nsz, B.l_sz.p, B.S_sy.p, B.nsy, B.Ys.p, s);
   partial_x(B.arith, B.Ys.p, m0, B.nsy, B.nsz, nullptr, B.S_sx.p, B.nsx, B.XS.p, s);
   scatter3(B.XS.p, B.nsx, B.nsy, B.nsz, B.l_sx.p, B.l_sy.p, B.l_idz.p, 0, sol_c, B.dims, s);
-  // inner-box z faces: full inverse of the two planes (in place, after the dots)
-  const int mz1[3] = {m0, m1, 1};
-  const int kz[2] = {B.inner_lo[2], B.inner_hi[2]};
-  for (int t = 0; t < 2; ++t) {
-    double* pl = B.W.p + plane * kz[t];
-    dst_lines_y(P.fy, pl, m0, m1, 1, s);
-    const int oz[3] = {1, 1, kz[t] + 1};
-    dst_x_inv_to_box(P.fx, pl, sol_c, B.dims, oz, mz1, s);
-  }
+  // one launch of inverse y transforms: the x-face layers and the inner-box
+  // z planes (in place on W, after the dots) ...
+  double* pl0 = B.W.p + plane * B.inner_lo[2];
+  double* pl1 = B.W.p + plane * B.inner_hi[2];
+  const DstYLines ys[3] = {{&P.fy, B.X2.p, 2, m1, m2}, {&P.fy, pl0, m0, m1, 1}, {&P.fy, pl1, m0, m1, 1}};
+  dst_lines_y_jobs(ys, 3, s);
+  scatter3(B.X2.p, 2, m1, m2, B.l_ix.p, nullptr, nullptr, 1, sol_c, B.dims, s);
+  // ... then inverse x transforms into sol_c: the y-face rows, then the z
+  // planes (jobs of one launch write disjoint nodes; at the box edges the
+  // planes' launch writes last, every run)
+  const int dm[3] = {B.dims[0], B.dims[1], B.dims[2]};
+  const DstXInvLines xr[2] = {
+      {&P.fx, B.Y1.p, sol_c, {dm[0], dm[1], dm[2]}, {1, B.inner_lo[1] + 1, 1}, {m0, 1, m2}},
+      {&P.fx, Y1b, sol_c, {dm[0], dm[1], dm[2]}, {1, B.inner_hi[1] + 1, 1}, {m0, 1, m2}}};
+  dst_x_inv_jobs(xr, 2, s);
+  const DstXInvLines xz[2] = {
+      {&P.fx, pl0, sol_c, {dm[0], dm[1], dm[2]}, {1, 1, B.inner_lo[2] + 1}, {m0, m1, 1}},
+      {&P.fx, pl1, sol_c, {dm[0], dm[1], dm[2]}, {1, 1, B.inner_hi[2] + 1}, {m0, m1, 1}}};
+  dst_x_inv_jobs(xz, 2, s);
   VPMG_CUDA(cudaGetLastError());
 }
 

@@ -208,32 +208,34 @@ __global__ void k_deposit(const int* __restrict__ starts, const float2* __restri
 }
 
 // FP64 records, the same 24 slots as doubles: x weights (0..3), y-z weight
-// products (4 + 4b + c), strengths (20..22), and the base cell's x index in
-// the first four bytes of slot 23.  The stencil offsets follow the
-// reference: x_a = (XP - XMIN - (i_a - 1) DX) / DX, evaluated with the
+// products (4 + 4b + c), strengths (20..22), and in slot 23 the base cell's
+// x index (low four bytes) and its linear index (high four bytes).  The
+// cell is the binning's (k_keys: the reference's int((x - XMIN)/DX) per
+// axis), so no division is repeated here; the stencil offsets follow the
+// reference, x_a = (XP - XMIN - (i_a - 1) DX) / DX, evaluated with the
 // reciprocal of DX.
 __global__ void k_records64(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
                             const double* __restrict__ q0, const double* __restrict__ q1,
                             const double* __restrict__ q2, const int* __restrict__ perm,
-                            const int* __restrict__ nsorted_dev, MeshDev m, double* __restrict__ rec) {
+                            const int* __restrict__ key, const int* __restrict__ nsorted_dev, MeshDev m,
+                            double* __restrict__ rec) {
   const int nsorted = *nsorted_dev;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
     const int p = perm[s];
+    const int kk = key[p];
+    const int cell[3] = {kk % m.n[0], (kk / m.n[0]) % m.n[1], kk / (m.n[0] * m.n[1])};
     const double pos[3] = {x[p], y[p], z[p]};
     double* r = rec + (size_t)s * kRecLen;
     double wgt[3][4];
-    int cx = 0;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const int c0 = cell_of(pos[d], m.xmin[d], m.d[d]);
-      const int node0 = c0 - m.ips;  // 0-based node = (i-1) of the reference
+      const int node0 = cell[d] - m.ips;  // 0-based node = (i-1) of the reference
       const double off = pos[d] - m.xmin[d];
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
         const double t = (off - (double)(node0 + a) * m.d[d]) * m.inv[d];
         wgt[d][a] = (a <= m.ips + m.ipf) ? proj_fun_f64(m.itype, fabs(t)) : 0.0;
       }
-      if (d == 0) cx = c0;
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) r[a] = wgt[0][a];
@@ -244,7 +246,7 @@ __global__ void k_records64(const double* __restrict__ x, const double* __restri
     r[kRecQ] = q0[p];
     r[kRecQ + 1] = q1[p];
     r[kRecQ + 2] = q2[p];
-    r[23] = __hiloint2double(0, cx);
+    r[23] = __hiloint2double(kk, cell[0]);
   }
 }
 
@@ -307,8 +309,8 @@ __global__ void __launch_bounds__(128) k_m2p64(const int* __restrict__ perm, con
     double wx[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a) wx[a] = r[a];
-    const int c0 = __double2loint(r[23]);
-    const int cj = cell_of(y[p], m.xmin[1], m.d[1]), ck = cell_of(z[p], m.xmin[2], m.d[2]);
+    const int c0 = __double2loint(r[23]), kk = __double2hiint(r[23]);  // the binning's cell
+    const int cj = (kk / m.n[0]) % m.n[1], ck = kk / (m.n[0] * m.n[1]);
     const int nw = m.ips + m.ipf + 1;
     double u[3] = {0.0, 0.0, 0.0}, gl[3] = {0.0, 0.0, 0.0};
     for (int c = 0; c < nw; ++c) {
@@ -541,7 +543,7 @@ void bin_particles(Particles& P, const MeshDev& m, Binning& B, cudaStream_t s) {
                                                            B.nsorted_dev, m, P.rec.p);
   else
     k_records64<<<stride_grid(P.capacity, 256), 256, 0, s>>>(P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.perm.p,
-                                                             B.nsorted_dev, m, P.rec64());
+                                                             P.key.p, B.nsorted_dev, m, P.rec64());
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }

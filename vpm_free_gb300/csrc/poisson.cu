@@ -38,7 +38,7 @@ namespace {
 // values computed do not depend on it.
 constexpr int kThreads = 128;
 constexpr int kDefaultPairs = 4;
-constexpr int kMaxOddRadix = 17;  // largest odd prime radix (2*(cells) must factor into 2..17)
+constexpr int kMaxOddRadix = 17;  // largest odd prime with a specialised stage (larger: stage_generic)
 constexpr int kRadixTab = (kMaxOddRadix + 1) * (kMaxOddRadix + 1);
 
 // cos / sin (2 pi i / R) of the odd radices: FP64 and float-float copies
@@ -231,6 +231,36 @@ __device__ __forceinline__ void stage_odd(typename A::C* __restrict__ in, typena
   }
 }
 
+// Radix-R stage for any odd prime R above kMaxOddRadix (the coarse grids
+// of some meshes, e.g. 58 = 2 x 29 points): one thread per output, the
+// direct DFT X_q = sum_m (w^{km} v_m) W_R^{mq}, its roots read from the
+// plan's twiddles (W_R^s = tw[s M / R]).  R^2 products per butterfly; used
+// only where no specialised stage exists.
+template <class A>
+__device__ __forceinline__ void stage_generic(const typename A::C* __restrict__ in, typename A::C* __restrict__ out,
+                                              int M, int Ns, int R, const typename A::C* __restrict__ tw,
+                                              int npair) {
+  using C = typename A::C;
+  const int nbf = M / R;
+  const int tws = M / (Ns * R);
+  const int rs = M / R;
+  for (int t = threadIdx.x; t < npair * nbf * R; t += blockDim.x) {
+    const int q = t % R;
+    const int bf = t / R;
+    const int pr = bf / nbf;
+    const int j = bf - pr * nbf;
+    const C* src = in + pr * M;
+    const int k = j % Ns;
+    C acc = src[j];
+    for (int m = 1; m < R; ++m) {
+      C v = src[j + m * nbf];
+      if (Ns > 1) v = A::cmul(v, __ldg(&tw[k * m * tws]));
+      acc = A::cadd(acc, A::cmul(v, __ldg(&tw[((m * q) % R) * rs])));
+    }
+    out[pr * M + (j - k) * R + k + q * Ns] = acc;
+  }
+}
+
 // Runs all stages; returns the buffer holding the result.  ODD = false
 // instantiates only the power-of-two radices, which keeps the register
 // count (and so the occupancy) of those kernels independent of the large
@@ -255,7 +285,7 @@ __device__ typename A::C* fft_all(typename A::C* Abuf, typename A::C* Bbuf, cons
             case 11: stage_odd<A, 11>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
             case 13: stage_odd<A, 13>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
             case 17: stage_odd<A, 17>(Abuf, Bbuf, p.M, Ns, tw, npair); break;
-            default: break;
+            default: stage_generic<A>(Abuf, Bbuf, p.M, Ns, r, tw, npair); break;
           }
         }
         break;
@@ -468,14 +498,16 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict
   }
 }
 
-// y pass (forward or inverse): in place on work (m0 x m1 x m2, x fastest).
+// y pass (forward or inverse): in place on work (m0 x m1 x m2, x fastest);
+// `tile` = which 2 * PAIRS lines.
 template <class Ar, bool ODD, int PAIRS>
-__global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, int m0, int m1, int m2, FFTDev p) {
+__device__ __forceinline__ void y_body(double* __restrict__ work, int m0, int m1, int m2, const FFTDev& p,
+                                       int tile) {
   extern __shared__ double2 smem[];
   double2* A = smem;
   double2* B = smem + PAIRS * p.M;
   const int nlines = m0 * m2;
-  const int l0 = blockIdx.x * (2 * PAIRS);
+  const int l0 = tile * (2 * PAIRS);
   const int n = p.n;  // == m1
   const size_t plane = (size_t)m0 * m1;
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
@@ -499,16 +531,20 @@ __global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, i
     work[(size_t)a + (size_t)m0 * k + plane * c] = dst_out<Ar>(R, p, li, k);
   }
 }
+template <class Ar, bool ODD, int PAIRS>
+__global__ void __launch_bounds__(kThreads) k_dst_y(double* __restrict__ work, int m0, int m1, int m2, FFTDev p) {
+  y_body<Ar, ODD, PAIRS>(work, m0, m1, m2, p, blockIdx.x);
+}
 
 // x pass, inverse: work -> interior of sol.
 template <class Ar, bool ODD, int PAIRS>
-__global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict__ work, double* __restrict__ sol, Box b,
-                                                        FFTDev p) {
+__device__ __forceinline__ void xinv_body(const double* __restrict__ work, double* __restrict__ sol, const Box& b,
+                                          const FFTDev& p, int tile) {
   extern __shared__ double2 smem[];
   double2* A = smem;
   double2* B = smem + PAIRS * p.M;
   const int nlines = b.m[1] * b.m[2];
-  const int l0 = blockIdx.x * (2 * PAIRS);
+  const int l0 = tile * (2 * PAIRS);
   const int n = p.n;
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, a = t - li * n;
@@ -527,6 +563,49 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict
     const int q = l % b.m[1], c = l / b.m[1];
     sol[(size_t)(b.o[0] + k) + sy * (b.o[1] + q) + sz * (b.o[2] + c)] = dst_out<Ar>(R, p, li, k);
   }
+}
+template <class Ar, bool ODD, int PAIRS>
+__global__ void __launch_bounds__(kThreads) k_dst_x_inv(const double* __restrict__ work, double* __restrict__ sol, Box b,
+                                                        FFTDev p) {
+  xinv_body<Ar, ODD, PAIRS>(work, sol, b, p, blockIdx.x);
+}
+
+// Several small transforms of one solve in one launch (the partially
+// evaluated block solves have many of a few hundred lines each, too few to
+// fill the GPU one launch at a time).  CTA blockIdx.x serves job j with
+// tile0[j] <= blockIdx.x < tile0[j + 1].  The transform of a line does not
+// depend on the launch it belongs to, so neither do the results.
+constexpr int kMaxJobs = 8;
+constexpr int kJobPairs = 2;
+struct YJobs {
+  int n;
+  int tile0[kMaxJobs + 1];
+  double* data[kMaxJobs];
+  int m0[kMaxJobs], m1[kMaxJobs], m2[kMaxJobs];
+  FFTDev p[kMaxJobs];
+};
+struct XJobs {
+  int n;
+  int tile0[kMaxJobs + 1];
+  const double* work[kMaxJobs];
+  double* sol[kMaxJobs];
+  Box b[kMaxJobs];
+  FFTDev p[kMaxJobs];
+};
+__device__ __forceinline__ int job_of(const int* tile0, int n) {
+  int j = 0;
+  while (j + 1 < n && (int)blockIdx.x >= tile0[j + 1]) ++j;
+  return j;
+}
+template <class Ar, bool ODD>
+__global__ void __launch_bounds__(kThreads) k_dst_y_jobs(const __grid_constant__ YJobs J) {
+  const int j = job_of(J.tile0, J.n);
+  y_body<Ar, ODD, kJobPairs>(J.data[j], J.m0[j], J.m1[j], J.m2[j], J.p[j], blockIdx.x - J.tile0[j]);
+}
+template <class Ar, bool ODD>
+__global__ void __launch_bounds__(kThreads) k_dst_x_inv_jobs(const __grid_constant__ XJobs J) {
+  const int j = job_of(J.tile0, J.n);
+  xinv_body<Ar, ODD, kJobPairs>(J.work[j], J.sol[j], J.b[j], J.p[j], blockIdx.x - J.tile0[j]);
 }
 
 // z pass: Thomas sweep per (p,q) with the reciprocal pivot table (FP64:
@@ -711,8 +790,20 @@ cudaError_t set_smem_t(int smax) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv<A, false, PAIRS>, a, smax);
   return e;
 }
+template <class A>
+cudaError_t set_jobs_smem(int smax) {
+  cudaError_t e = cudaSuccess;
+  const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y_jobs<A, true>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_y_jobs<A, false>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv_jobs<A, true>, a, smax);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dst_x_inv_jobs<A, false>, a, smax);
+  return e;
+}
 cudaError_t set_dst_smem(int smax) {
-  cudaError_t e = set_smem_t<F64, 2>(smax);
+  cudaError_t e = set_jobs_smem<F64>(smax);
+  if (e == cudaSuccess) e = set_jobs_smem<FF>(smax);
+  if (e == cudaSuccess) e = set_smem_t<F64, 2>(smax);
   if (e == cudaSuccess) e = set_smem_t<F64, 4>(smax);
   if (e == cudaSuccess) e = set_smem_t<F64, 8>(smax);
   if (e == cudaSuccess) e = set_smem_t<FF, 2>(smax);
@@ -867,10 +958,7 @@ void make_fft_plan(FFTPlan& p, int n, int arith) {
     while (m % f == 0) { odd.push_back(f); m /= f; }
   std::sort(odd.begin(), odd.end(), [](int a, int b) { return a > b; });
   p.nst = 0;
-  for (int f : odd) {
-    VPMG_CHECK(f <= kMaxOddRadix, VPMG_ERR_UNSUPPORTED, "mesh size has a prime factor > 17 in 2*(cells)");
-    p.radix[p.nst++] = f;
-  }
+  for (int f : odd) p.radix[p.nst++] = f;  // primes above 17 take the generic direct-DFT stage
   while (twos >= 3) { p.radix[p.nst++] = 8; twos -= 3; }
   if (twos == 2) p.radix[p.nst++] = 4;
   if (twos == 1) p.radix[p.nst++] = 2;
@@ -998,6 +1086,70 @@ void dst_x_inv_to_box(const FFTPlan& p, const double* data, double* sol, const i
   Box b;
   for (int d = 0; d < 3; ++d) { b.dims[d] = dims[d]; b.o[d] = o[d]; b.m[d] = m[d]; }
   launch_x_inv(s, data, sol, b, dev_plan(p));
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+// Job lists: several small transforms in one launch (tiles of kJobPairs line
+// pairs; all jobs in the plans' common arithmetic).
+void dst_lines_y_jobs(const DstYLines* jobs, int n, cudaStream_t s) {
+  VPMG_CHECK(n >= 1 && n <= kMaxJobs, VPMG_ERR_ARG, "dst_lines_y_jobs: 1..8 jobs");
+  YJobs J{};
+  J.n = n;
+  int tiles = 0, odd = 0, arith = jobs[0].plan->arith;
+  size_t smem = 0;
+  for (int j = 0; j < n; ++j) {
+    const DstYLines& q = jobs[j];
+    VPMG_CHECK(q.m1 == q.plan->n && q.plan->arith == arith, VPMG_ERR_ARG, "dst_lines_y_jobs: plan mismatch");
+    J.tile0[j] = tiles;
+    J.data[j] = q.data; J.m0[j] = q.m0; J.m1[j] = q.m1; J.m2[j] = q.m2;
+    J.p[j] = dev_plan(*q.plan);
+    J.p[j].pairs = kJobPairs;
+    odd |= J.p[j].odd;
+    tiles += (q.m0 * q.m2 + 2 * kJobPairs - 1) / (2 * kJobPairs);
+    smem = std::max(smem, (size_t)2 * kJobPairs * J.p[j].M * sizeof(double2));
+  }
+  J.tile0[n] = tiles;
+  if (tiles == 0) return;
+  if (arith == VPMG_ARITH_FF48) {
+    if (odd) k_dst_y_jobs<FF, true><<<tiles, kThreads, smem, s>>>(J);
+    else k_dst_y_jobs<FF, false><<<tiles, kThreads, smem, s>>>(J);
+  } else {
+    if (odd) k_dst_y_jobs<F64, true><<<tiles, kThreads, smem, s>>>(J);
+    else k_dst_y_jobs<F64, false><<<tiles, kThreads, smem, s>>>(J);
+  }
+  VPMG_LAUNCHED();
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void dst_x_inv_jobs(const DstXInvLines* jobs, int n, cudaStream_t s) {
+  VPMG_CHECK(n >= 1 && n <= kMaxJobs, VPMG_ERR_ARG, "dst_x_inv_jobs: 1..8 jobs");
+  XJobs J{};
+  J.n = n;
+  int tiles = 0, odd = 0, arith = jobs[0].plan->arith;
+  size_t smem = 0;
+  for (int j = 0; j < n; ++j) {
+    const DstXInvLines& q = jobs[j];
+    VPMG_CHECK(q.m[0] == q.plan->n && q.plan->arith == arith, VPMG_ERR_ARG, "dst_x_inv_jobs: plan mismatch");
+    J.tile0[j] = tiles;
+    J.work[j] = q.data;
+    J.sol[j] = q.sol;
+    for (int d = 0; d < 3; ++d) { J.b[j].dims[d] = q.dims[d]; J.b[j].o[d] = q.o[d]; J.b[j].m[d] = q.m[d]; }
+    J.p[j] = dev_plan(*q.plan);
+    J.p[j].pairs = kJobPairs;
+    odd |= J.p[j].odd;
+    tiles += (q.m[1] * q.m[2] + 2 * kJobPairs - 1) / (2 * kJobPairs);
+    smem = std::max(smem, (size_t)2 * kJobPairs * J.p[j].M * sizeof(double2));
+  }
+  J.tile0[n] = tiles;
+  if (tiles == 0) return;
+  if (arith == VPMG_ARITH_FF48) {
+    if (odd) k_dst_x_inv_jobs<FF, true><<<tiles, kThreads, smem, s>>>(J);
+    else k_dst_x_inv_jobs<FF, false><<<tiles, kThreads, smem, s>>>(J);
+  } else {
+    if (odd) k_dst_x_inv_jobs<F64, true><<<tiles, kThreads, smem, s>>>(J);
+    else k_dst_x_inv_jobs<F64, false><<<tiles, kThreads, smem, s>>>(J);
+  }
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }

@@ -116,6 +116,21 @@ void dst_forward_xy(DirichletPlan& P, const double* rhs, const double* sol, bool
 void dst_lines_y(const FFTPlan& p, double* data, int m0, int m1, int m2, cudaStream_t s);
 void dst_x_inv_to_box(const FFTPlan& p, const double* data, double* sol, const int dims[3], const int o[3],
                       const int m[3], cudaStream_t s);
+// Up to 8 of the above in one launch (each job with its own plan and arrays;
+// the plans share one arithmetic).  Results equal the single launches'.
+struct DstYLines {
+  const FFTPlan* plan;
+  double* data;
+  int m0, m1, m2;
+};
+void dst_lines_y_jobs(const DstYLines* jobs, int n, cudaStream_t s);
+struct DstXInvLines {
+  const FFTPlan* plan;
+  const double* data;
+  double* sol;
+  int dims[3], o[3], m[3];
+};
+void dst_x_inv_jobs(const DstXInvLines* jobs, int n, cudaStream_t s);
 
 // ------------------------------------------------- boundary operator ----
 struct TreeGeom;  // host-built quadtree of one grid (tree_host.cpp)
