@@ -585,6 +585,9 @@ def run_ours(args, dist):
         v, t, _ = cpu_step_sample(xp, qp, w, 1, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"1 full step (field step + Euler + remesh) of this workload, {t:.1f} s on {threads} threads"}
+        if args.cpu_1thread:  # the same step on one host thread (about 16x longer)
+            v1, t1, _ = cpu_step_sample(xp, qp, w, 1, 1)
+            cpu["one_thread"] = {"value": v1, "cores": 1, "sample": f"1 full step, {t1:.1f} s on 1 thread"}
     batched = None
     if not args.no_batched and args.workload == "leapfrog256":
         batched = run_batched(args, local)
@@ -626,6 +629,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-1thread", action="store_true",
+                    help="also time the CPU baseline step on one host thread (adds about two minutes)")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="leapfrog256",
                     help="leapfrog256 is the benchmark; the rings are small profiling cases")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-problems measurement")

@@ -155,9 +155,10 @@ __global__ void k_particle_adj(MeshDev m, const int* __restrict__ np_dev, const 
   }
 }
 
-// Strength slots of the sorted records <- scale * w_p * v_p (w = QP(4) or 1),
-// as doubles (FP64 records) or float-float pairs (ff != 0).
-__global__ void k_records_set_q(float2* __restrict__ rec, int ff, const int* __restrict__ perm,
+// Strength slots of the sorted records <- scale * w_p * v_p (w = QP(4) or 1):
+// FP64 records (ff == 0) are slot-major with stride cs, float-float records
+// (ff != 0) particle-major.
+__global__ void k_records_set_q(float2* __restrict__ rec, int ff, size_t cs, const int* __restrict__ perm,
                                 const int* __restrict__ nsorted, const double* __restrict__ v, int cap, double scale,
                                 const double* __restrict__ w) {
   const int n = *nsorted;
@@ -167,9 +168,8 @@ __global__ void k_records_set_q(float2* __restrict__ rec, int ff, const int* __r
     const double f = scale * (w ? w[p] : 1.0);
     const double q[3] = {f * v[p], f * v[cap + p], f * v[2 * (size_t)cap + p]};
     for (int c = 0; c < 3; ++c) {
-      const size_t slot = (size_t)s * kRecLen + kRecQ + c;
-      if (ff) rec[slot] = ff::split(q[c]);
-      else rd[slot] = q[c];
+      if (ff) rec[(size_t)s * kRecLen + kRecQ + c] = ff::split(q[c]);
+      else rd[(kRecQ + c) * cs + s] = q[c];
     }
   }
 }
@@ -715,10 +715,12 @@ void fields_vjp(vpmg_handle* h, const double* upb, const double* gpb, double* xb
   double* G[3] = {S.gbar.p, S.gbar.p + N, S.gbar.p + 2 * N};
   // M2P^T: ubar = sum_p W upbar_p,  gbar = sum_p W vol_p gpbar_p  (the deposit divides by DV)
   const int rff = P.arith == VPMG_ARITH_FF48 ? 1 : 0;
-  k_records_set_q<<<grid(cap), 256, 0, st>>>(P.rec.p, rff, P.perm.p, h->bins.nsorted_dev, upb, cap, dvg, nullptr);
+  k_records_set_q<<<grid(cap), 256, 0, st>>>(P.rec.p, rff, P.rec_stride(), P.perm.p, h->bins.nsorted_dev, upb, cap,
+                                             dvg, nullptr);
   VPMG_LAUNCHED();
   deposit(P, mg, h->bins, U, st);
-  k_records_set_q<<<grid(cap), 256, 0, st>>>(P.rec.p, rff, P.perm.p, h->bins.nsorted_dev, gpb, cap, dvg, P.vol.p);
+  k_records_set_q<<<grid(cap), 256, 0, st>>>(P.rec.p, rff, P.rec_stride(), P.perm.p, h->bins.nsorted_dev, gpb, cap,
+                                             dvg, P.vol.p);
   VPMG_LAUNCHED();
   deposit(P, mg, h->bins, G, st);
   // positions through the M2P weights

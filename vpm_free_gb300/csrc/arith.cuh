@@ -29,7 +29,22 @@ struct F64 {
   __device__ __forceinline__ static R mul(R a, R b) { return a * b; }
   __device__ __forceinline__ static R fma(R a, R b, R c) { return ::fma(a, b, c); }
   __device__ __forceinline__ static R neg(R a) { return -a; }
-  __device__ __forceinline__ static R scale(R a, float f) { return a * (double)f; }  // f a power of two
+  // a * f for f = +-0.5 (the transforms' only scalings) by integer
+  // operations on the bits, exactly the IEEE product and without an FP64
+  // pipe slot: the exponent field is decremented when the result stays
+  // normal; below that the significand (with its implicit bit) is halved,
+  // rounding half to even; inf and nan pass through.
+  __device__ __forceinline__ static R scale(R a, float f) {
+    if (f != 0.5f && f != -0.5f) return a * (double)f;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long sgn = (b & 0x8000000000000000ull) ^ (f < 0.0f ? 0x8000000000000000ull : 0ull);
+    const unsigned long long u = b & 0x7FFFFFFFFFFFFFFFull;
+    unsigned long long r;
+    if (u >= 0x7FF0000000000000ull) r = u;                           // inf, nan
+    else if (u >= 0x0020000000000000ull) r = u - 0x0010000000000000ull;  // biased exponent >= 2
+    else r = (u >> 1) + (u & (u >> 1) & 1ull);                         // subnormal result
+    return __longlong_as_double((long long)(sgn | r));
+  }
   __device__ __forceinline__ static R re(C v) { return v.x; }
   __device__ __forceinline__ static R im(C v) { return v.y; }
   __device__ __forceinline__ static C cplx(R r, R i) { return make_double2(r, i); }

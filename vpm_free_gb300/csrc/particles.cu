@@ -207,25 +207,27 @@ __global__ void k_deposit(const int* __restrict__ starts, const float2* __restri
   r2[id] = ff::to_double(a2) * inv_dv;
 }
 
-// FP64 records, the same 24 slots as doubles: x weights (0..3), y-z weight
-// products (4 + 4b + c), strengths (20..22), and in slot 23 the base cell's
-// x index (low four bytes) and its linear index (high four bytes).  The
-// cell is the binning's (k_keys: the reference's int((x - XMIN)/DX) per
-// axis), so no division is repeated here; the stencil offsets follow the
-// reference, x_a = (XP - XMIN - (i_a - 1) DX) / DX, evaluated with the
-// reciprocal of DX.
+// FP64 records, slot-major: slot k of sorted particle s at rec[k * cs + s]
+// (cs = the record stride, the particle capacity), so that a warp's lanes
+// read one slot of consecutive particles with coalesced loads.  Slots: x
+// weights (0..3), y-z weight products (4 + 4b + c), strengths (20..22), and
+// in slot 23 the base cell's x index (low four bytes) and its linear index
+// (high four bytes).  The cell is the binning's (k_keys: the reference's
+// int((x - XMIN)/DX) per axis), so no division is repeated here; the
+// stencil offsets follow the reference, x_a = (XP - XMIN - (i_a - 1) DX) / DX,
+// evaluated with the reciprocal of DX.
 __global__ void k_records64(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
                             const double* __restrict__ q0, const double* __restrict__ q1,
                             const double* __restrict__ q2, const int* __restrict__ perm,
                             const int* __restrict__ key, const int* __restrict__ nsorted_dev, MeshDev m,
-                            double* __restrict__ rec) {
+                            double* __restrict__ rec, size_t cs) {
   const int nsorted = *nsorted_dev;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
     const int p = perm[s];
     const int kk = key[p];
     const int cell[3] = {kk % m.n[0], (kk / m.n[0]) % m.n[1], kk / (m.n[0] * m.n[1])};
     const double pos[3] = {x[p], y[p], z[p]};
-    double* r = rec + (size_t)s * kRecLen;
+    double* r = rec + s;
     double wgt[3][4];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -238,61 +240,172 @@ __global__ void k_records64(const double* __restrict__ x, const double* __restri
       }
     }
 #pragma unroll
-    for (int a = 0; a < 4; ++a) r[a] = wgt[0][a];
+    for (int a = 0; a < 4; ++a) r[a * cs] = wgt[0][a];
 #pragma unroll
     for (int b = 0; b < 4; ++b)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) r[4 + 4 * b + c] = wgt[1][b] * wgt[2][c];
-    r[kRecQ] = q0[p];
-    r[kRecQ + 1] = q1[p];
-    r[kRecQ + 2] = q2[p];
-    r[23] = __hiloint2double(kk, cell[0]);
+      for (int c = 0; c < 4; ++c) r[(4 + 4 * b + c) * cs] = wgt[1][b] * wgt[2][c];
+    r[kRecQ * cs] = q0[p];
+    r[(kRecQ + 1) * cs] = q1[p];
+    r[(kRecQ + 2) * cs] = q2[p];
+    r[23 * cs] = __hiloint2double(kk, cell[0]);
   }
 }
 
-// FP64 deposition gather: one thread per node, the particles of the cells
-// whose stencil covers it in fixed cell and slot order (run-to-run
-// deterministic, no atomics); 1 DMUL + 3 DFMA per particle-node visit.
-__global__ void __launch_bounds__(256) k_deposit64(const int* __restrict__ starts, const double* __restrict__ rec,
-                                                   MeshDev m, double inv_dv, double* __restrict__ r0,
-                                                   double* __restrict__ r1, double* __restrict__ r2) {
-  const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
-  const size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (id >= N) return;
-  const int i = (int)(id % m.n[0]);
-  const int j = (int)((id / m.n[0]) % m.n[1]);
-  const int k = (int)(id / ((size_t)m.n[0] * m.n[1]));
-  const int w = m.ips + m.ipf;
-  const int xlo = max(i - m.ipf, 0), xhi = min(i + m.ips, m.n[0] - 1);
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-  for (int ck = max(k - m.ipf, 0); ck <= min(k + m.ips, m.n[2] - 1); ++ck) {
-    const int iz = k - ck + m.ips;
-    for (int cj = max(j - m.ipf, 0); cj <= min(j + m.ips, m.n[1] - 1); ++cj) {
-      const int iy = j - cj + m.ips;
-      const size_t row = (size_t)m.n[0] * (cj + (size_t)m.n[1] * ck);
-      const int s = __ldg(&starts[row + xlo]), e = __ldg(&starts[row + xhi + 1]);
-      for (int t = s; t < e; ++t) {
-        const double* r = rec + (size_t)t * kRecLen;
-        const double2 q2c = __ldg(reinterpret_cast<const double2*>(r) + 11);  // q2, cell
-        const int ix = i - __double2loint(q2c.y) + m.ips;
-        if ((unsigned)ix > (unsigned)w) continue;  // only for a binning that does not match rec
-        const double2 q01 = __ldg(reinterpret_cast<const double2*>(r) + 10);
-        const double f = __ldg(&r[ix]) * __ldg(&r[4 + 4 * iy + iz]);
-        a0 = fma(f, q01.x, a0);
-        a1 = fma(f, q01.y, a1);
-        a2 = fma(f, q2c.x, a2);
+// FP64 deposition gather, balanced over a warp's lanes.  A warp owns 32
+// consecutive x nodes of one (j, k) row.  Node n receives from the
+// particles of the (ips+ipf+1)^2 cell rows (cj, ck) covering it, in the
+// cell range [n - ipf, n + ips] of each row: its visits, enumerated in
+// (row, sorted slot) order.  The warp's visits (node by node) are split
+// into 32 equal chunks, one per lane, so every lane does a visit per trip
+// (1 DMUL + 3 DFMA) instead of idling while a neighbour with more particles
+// finishes.  A lane's running sums are flushed where its chunk leaves a
+// node: the first and last node it touches as pieces, nodes it covers
+// entirely as totals.  Each node then adds its pieces in lane order: a
+// fixed order, so the result is the same bits every run; no atomics.
+constexpr int kDepWarps = 8;
+__global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restrict__ starts,
+                                                             const double* __restrict__ rec, size_t cs, MeshDev m,
+                                                             double inv_dv, double* __restrict__ r0,
+                                                             double* __restrict__ r1, double* __restrict__ r2) {
+  __shared__ double pf[kDepWarps][32][3], pl[kDepWarps][32][3], tot[kDepWarps][32][3];
+  __shared__ int soff[kDepWarps][32], scnt[kDepWarps][32], snA[kDepWarps][32], snB[kDepWarps][32];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const int nseg = (m.n[0] + 31) / 32;
+  const long long wg = (long long)blockIdx.x * kDepWarps + wl;
+  if (wg >= (long long)nseg * m.n[1] * m.n[2]) return;  // whole warps only
+  const int seg = (int)(wg % nseg);
+  const long long jk = wg / nseg;
+  const int j = (int)(jk % m.n[1]), k = (int)(jk / m.n[1]);
+  const int i0 = seg * 32;
+  const int i = i0 + lane;
+  const bool valid = i < m.n[0];
+  // the cell rows covering this node row (the same for every lane)
+  const int cj0 = max(j - m.ipf, 0), cj1 = min(j + m.ips, m.n[1] - 1);
+  const int ck0 = max(k - m.ipf, 0), ck1 = min(k + m.ips, m.n[2] - 1);
+  const int ncj = cj1 - cj0 + 1, nrow = ncj * (ck1 - ck0 + 1);
+  const double* q0 = rec + kRecQ * cs;
+  const double* q1 = rec + (kRecQ + 1) * cs;
+  const double* q2 = rec + (kRecQ + 2) * cs;
+  const double* cellw = rec + 23 * cs;
+  // visits of this lane's node, and the warp's scan of them
+  int cnt = 0;
+  if (valid) {
+    const int xl = max(i - m.ipf, 0), xh = min(i + m.ips, m.n[0] - 1);
+    for (int r = 0; r < nrow; ++r) {
+      const size_t rb = (size_t)m.n[0] * ((cj0 + r % ncj) + (size_t)m.n[1] * (ck0 + r / ncj));
+      cnt += __ldg(&starts[rb + xh + 1]) - __ldg(&starts[rb + xl]);
+    }
+  }
+  int off = cnt;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(FULL, off, d);
+    if (lane >= d) off += v;
+  }
+  const int V = __shfl_sync(FULL, off, 31);
+  off -= cnt;  // exclusive
+  soff[wl][lane] = off;
+  scnt[wl][lane] = cnt;
+  if (V == 0) {
+    if (valid) {
+      const size_t id = (size_t)i + (size_t)m.n[0] * (j + (size_t)m.n[1] * k);
+      r0[id] = 0.0;
+      r1[id] = 0.0;
+      r2[id] = 0.0;
+    }
+    return;
+  }
+  const int C = (V + 31) / 32;
+  const int v0 = min(lane * C, V), v1 = min(v0 + C, V);
+  // first node of the chunk: the largest n with off_n <= v0 (it has visits)
+  int lo = 0, hi = 31;
+  const int vq = min(v0, V - 1);
+#pragma unroll
+  for (int it = 0; it < 5; ++it) {
+    const int mid = (lo + hi + 1) >> 1;
+    const int om = __shfl_sync(FULL, off, mid);
+    if (om <= vq) lo = mid;
+    else hi = mid - 1;
+  }
+  __syncwarp();
+  int nA = -1, n = lo;
+  if (v0 < v1) {
+    nA = n;
+    int ii = i0 + n;
+    int xl = max(ii - m.ipf, 0), xh = min(ii + m.ips, m.n[0] - 1);
+    // row and slot of visit v0 inside node n
+    int local = v0 - soff[wl][n];
+    int r = 0, tb = 0, te = 0;
+    for (;; ++r) {
+      const size_t rb = (size_t)m.n[0] * ((cj0 + r % ncj) + (size_t)m.n[1] * (ck0 + r / ncj));
+      tb = __ldg(&starts[rb + xl]);
+      te = __ldg(&starts[rb + xh + 1]);
+      if (local < te - tb) break;
+      local -= te - tb;
+    }
+    int t = tb + local;
+    int wyz_slot = 4 + 4 * (j - (cj0 + r % ncj) + m.ips) + (k - (ck0 + r / ncj) + m.ips);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int v = v0; v < v1; ++v) {
+      const int ix = ii - __double2loint(__ldg(&cellw[t])) + m.ips;
+      const double f = __ldg(&rec[ix * cs + t]) * __ldg(&rec[wyz_slot * cs + t]);
+      a0 = fma(f, __ldg(&q0[t]), a0);
+      a1 = fma(f, __ldg(&q1[t]), a1);
+      a2 = fma(f, __ldg(&q2[t]), a2);
+      if (++t < te || v + 1 == v1) continue;
+      // next nonempty row of node n, or the node is complete: flush it
+      for (;;) {
+        if (++r == nrow) {
+          double* dst = (n == nA) ? pf[wl][lane] : tot[wl][n];
+          dst[0] = a0; dst[1] = a1; dst[2] = a2;
+          a0 = a1 = a2 = 0.0;
+          do ++n; while (scnt[wl][n] == 0);
+          ii = i0 + n;
+          xl = max(ii - m.ipf, 0);
+          xh = min(ii + m.ips, m.n[0] - 1);
+          r = 0;
+        }
+        const size_t rb = (size_t)m.n[0] * ((cj0 + r % ncj) + (size_t)m.n[1] * (ck0 + r / ncj));
+        tb = __ldg(&starts[rb + xl]);
+        te = __ldg(&starts[rb + xh + 1]);
+        if (te > tb) break;
+      }
+      t = tb;
+      wyz_slot = 4 + 4 * (j - (cj0 + r % ncj) + m.ips) + (k - (ck0 + r / ncj) + m.ips);
+    }
+    double* dst = (n == nA) ? pf[wl][lane] : pl[wl][lane];  // the chunk's last node
+    dst[0] = a0; dst[1] = a1; dst[2] = a2;
+  }
+  snA[wl][lane] = nA;
+  snB[wl][lane] = (v0 < v1) ? n : -1;
+  __syncwarp();
+  if (!valid) return;
+  double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+  if (cnt > 0) {
+    const int L1 = off / C, L2 = (off + cnt - 1) / C;
+    if (L1 == L2 && snA[wl][L1] != lane && snB[wl][L1] != lane) {
+      b0 = tot[wl][lane][0]; b1 = tot[wl][lane][1]; b2 = tot[wl][lane][2];  // inside one chunk
+    } else {
+      for (int L = L1; L <= L2; ++L) {  // pieces in lane order
+        const double* src = (snA[wl][L] == lane) ? pf[wl][L] : pl[wl][L];
+        b0 += src[0];
+        b1 += src[1];
+        b2 += src[2];
       }
     }
   }
-  r0[id] = a0 * inv_dv;
-  r1[id] = a1 * inv_dv;
-  r2[id] = a2 * inv_dv;
+  const size_t id = (size_t)i + (size_t)m.n[0] * (j + (size_t)m.n[1] * k);
+  r0[id] = b0 * inv_dv;
+  r1[id] = b1 * inv_dv;
+  r2[id] = b2 * inv_dv;
 }
 
 // FP64 mesh-to-particle over sorted slots: UP = sum W vel, GP = (sum W def)
 // * vol; optionally the forward Euler push.  6 DFMA per particle-node visit.
 __global__ void __launch_bounds__(128) k_m2p64(const int* __restrict__ perm, const int* __restrict__ nsorted_dev,
-                                               const double* __restrict__ rec, MeshDev m,
+                                               const double* __restrict__ rec, size_t cs, MeshDev m,
                                                const double* __restrict__ v0, const double* __restrict__ v1,
                                                const double* __restrict__ v2, const double* __restrict__ g0,
                                                const double* __restrict__ g1, const double* __restrict__ g2,
@@ -305,11 +418,12 @@ __global__ void __launch_bounds__(128) k_m2p64(const int* __restrict__ perm, con
   const int nsorted = *nsorted_dev;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nsorted; s += gridDim.x * blockDim.x) {
     const int p = perm[s];
-    const double* r = rec + (size_t)s * kRecLen;
+    const double* r = rec + s;  // slot-major records (stride cs)
     double wx[4];
 #pragma unroll
-    for (int a = 0; a < 4; ++a) wx[a] = r[a];
-    const int c0 = __double2loint(r[23]), kk = __double2hiint(r[23]);  // the binning's cell
+    for (int a = 0; a < 4; ++a) wx[a] = r[a * cs];
+    const double cw = r[23 * cs];
+    const int c0 = __double2loint(cw), kk = __double2hiint(cw);  // the binning's cell
     const int cj = (kk / m.n[0]) % m.n[1], ck = kk / (m.n[0] * m.n[1]);
     const int nw = m.ips + m.ipf + 1;
     double u[3] = {0.0, 0.0, 0.0}, gl[3] = {0.0, 0.0, 0.0};
@@ -317,7 +431,7 @@ __global__ void __launch_bounds__(128) k_m2p64(const int* __restrict__ perm, con
       const int kk = ck - m.ips + c;
       for (int b = 0; b < nw; ++b) {
         const int jj = cj - m.ips + b;
-        const double wyz = r[4 + 4 * b + c];
+        const double wyz = r[(4 + 4 * b + c) * cs];
         const size_t row = (size_t)m.n[0] * (jj + (size_t)m.n[1] * kk) + (c0 - m.ips);
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
@@ -543,7 +657,7 @@ void bin_particles(Particles& P, const MeshDev& m, Binning& B, cudaStream_t s) {
                                                            B.nsorted_dev, m, P.rec.p);
   else
     k_records64<<<stride_grid(P.capacity, 256), 256, 0, s>>>(P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.perm.p,
-                                                             P.key.p, B.nsorted_dev, m, P.rec64());
+                                                             P.key.p, B.nsorted_dev, m, P.rec64(), P.rec_stride());
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
@@ -568,11 +682,13 @@ int read_count(const int* d, cudaStream_t s) {
 void deposit(const Particles& P, const MeshDev& m, const Binning& B, double* const rhs[3], cudaStream_t s) {
   const size_t N = (size_t)m.n[0] * m.n[1] * m.n[2];
   const double dv = m.d[0] * m.d[1] * m.d[2];
-  if (P.arith == VPMG_ARITH_FF48)
+  if (P.arith == VPMG_ARITH_FF48) {
     k_deposit<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(B.starts.p, P.rec.p, m, 1.0 / dv, rhs[0], rhs[1], rhs[2]);
-  else
-    k_deposit64<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(B.starts.p, P.rec64(), m, 1.0 / dv, rhs[0], rhs[1],
-                                                            rhs[2]);
+  } else {
+    const long long warps = (long long)((m.n[0] + 31) / 32) * m.n[1] * m.n[2];
+    k_deposit64<<<(unsigned)((warps + kDepWarps - 1) / kDepWarps), kDepWarps * 32, 0, s>>>(
+        B.starts.p, P.rec64(), P.rec_stride(), m, 1.0 / dv, rhs[0], rhs[1], rhs[2]);
+  }
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
@@ -594,7 +710,8 @@ void m2p(Particles& P, const MeshDev& m, const Binning& B, const double* const v
     m2p_launch(P, m, B, vel, def, up_mode, euler, dt, uinf, s);
     return;
   }
-  k_m2p64<<<stride_grid(P.capacity, 128), 128, 0, s>>>(P.perm.p, B.nsorted_dev, P.rec64(), m, vel[0], vel[1], vel[2],
+  k_m2p64<<<stride_grid(P.capacity, 128), 128, 0, s>>>(P.perm.p, B.nsorted_dev, P.rec64(), P.rec_stride(), m,
+                                                       vel[0], vel[1], vel[2],
                                                        def[0], def[1], def[2], up_mode ? P.up.p : nullptr, P.gp.p,
                                                        up_mode == 2 ? 1 : 0, P.x.p, P.y.p, P.z.p, P.q0.p, P.q1.p, P.q2.p, P.vol.p,
                                                        euler ? 1 : 0, dt, uinf[0], uinf[1], uinf[2]);

@@ -9,10 +9,11 @@ namespace vpmg {
 // A sorted particle record: 24 slots of 8 bytes, 192 bytes -- the 4 x
 // stencil weights (0..3), the 16 products of the y and z weights
 // wy[b] wz[c] at 4 + 4b + c, the strengths (20..22) and the base cell's x
-// index in the first four bytes of slot 23.  A slot is a double (FP64
-// arithmetic) or a float-float pair (float-float arithmetic).  A
-// particle-node visit of the deposition reads one x weight, one y-z product
-// and two 16-byte loads.
+// index in the first four bytes of slot 23.  FP64 arithmetic: each slot a
+// double, slot-major (slot k of sorted particle s at k * capacity + s; the
+// high four bytes of slot 23 hold the linear cell index).  Float-float
+// arithmetic: each slot a float-float pair, particle-major (24 slots per
+// particle back to back).
 constexpr int kRecLen = 24;
 constexpr int kRecQ = 20;  // first strength slot
 
@@ -36,6 +37,7 @@ struct Particles {
   DBuf<int> d_np;                         // particle count, on the device
   int arith = VPMG_ARITH_FP64;            // arithmetic of the records, deposition and gather
   double* rec64() const { return reinterpret_cast<double*>(rec.p); }
+  size_t rec_stride() const { return (size_t)capacity; }  // FP64 records: doubles between slots
   void ensure(int cap);
 };
 
