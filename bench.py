@@ -414,6 +414,7 @@ KERNELS = (  # vpmg_bench_kernel ids: (id, name, launches per step)
     (4, "k_deformation (stretching)", 1),
     (3, "k_velocity (curl)", 1),
     (7, "k_remesh_flags + scan", 1),
+    (8, "k_records64 + sort by cell (k_keys, scan, k_scatter, k_cell_order)", 2),
 )
 
 
@@ -638,7 +639,7 @@ def main():
     ap.add_argument("--arith", choices=["fp64", "ff48"], default="fp64",
                     help="arithmetic of the headline run (fp64, the reference's, is the default)")
     ap.add_argument("--no-ff48", action="store_true", help="skip the float-float run reported beside the FP64 one")
-    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--batch-steps", type=int, default=20, help="steps of the batched workload (20, its stated length)")
     ap.add_argument("--batch-operator-budget", type=int, default=12 << 30,
                     help="bytes of recorded boundary operator per batched problem")
     ap.add_argument("--dirichlet-nodes", type=int, default=273,

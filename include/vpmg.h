@@ -275,7 +275,8 @@ int vpmg_batch_destroy(vpmg_batch* b);
  *              kernels), 2: deposition gather, 3: velocity curl, 4:
  *              stretching, 5: mesh-to-particle gather, 6: one component of
  *              the padded block's zero-BC solve evaluated where it is read,
- *              7: the remesh's |w| flags and their scan.
+ *              7: the remesh's |w| flags and their scan, 8: the sort by
+ *              cell and the particle records on the global mesh.
  * Outputs: mean device ms per replay, algorithmic FP64 flops (an FMA
  * counts 2) and DRAM bytes per replay (figures of the algorithm, not
  * counters).  The replay writes only scratch buffers, the particles'

@@ -5,8 +5,8 @@ vpmg_adjoint_loss / vpmg_adjoint_run and the torch.autograd bridge.
   to rounding (single-level and two-level YAPS, quadtree with dummy cells);
 * the gradient of a 10-step loss (64^3 ring, 1024 probes in a shell around
   the ring plus a kinetic-energy term) matches central differences of the
-  GPU forward (h = 1e-6, 64 random directions) and, for a 3-step loss, of
-  the oracle's forward;
+  GPU forward and of the oracle's forward (h = 1e-6, 64 random directions
+  each);
 * the GPU loss equals the oracle's loss on the same particles.
 """
 import itertools
@@ -215,42 +215,74 @@ def test_adjoint_gradient_matches_gpu_central_differences(gpulib):
         assert rel_l2(g_adj, g_fd) <= FD_TOL, (g_adj[:4], g_fd[:4])
 
 
+_ORACLE_FD = {}  # the oracle's difference quotients, shared by both arithmetics' runs
+
+
+def _oracle_steps_loss(O, ocfg, s, x, q, masks, mode, nsteps, dt, probes, nthreads=0):
+    """The oracle's loss after nsteps steps; mode 1: the reference's remesh
+    cut, recording the masks; 2: replaying them."""
+    nn = list(s.nn)
+    x, q = x.copy(), q.copy()
+    for k in range(nsteps):
+        up, gp = O.step_fields(ocfg, s, x, q, nthreads=nthreads)
+        O.euler(x, q, up, gp, dt)
+        x, q = O.remesh_masked(ocfg, s, x, q, masks[k], mode, nthreads=nthreads)
+    O.step_fields(ocfg, s, x, q, nthreads=nthreads)
+    vel = O.get_field(O.F_VEL).reshape(3, nn[2], nn[1], nn[0])
+    return field_loss(vel, list(s.xbound)[:3], list(s.dpm), probes, KE)
+
+
+def _oracle_fd_worker(job):
+    """Central differences of the oracle's loss along some directions, in a
+    spawned process that loads the oracle itself."""
+    x0, q0, dirs, masks, nsteps, dt, probes, nthreads = job
+    from oracle import oracle as O
+    from vpm_free_gb300 import workloads as W
+    xp, _, w = W.ring64()
+    ocfg, _ = configs_for(w)
+    s = O.define_sizes(ocfg, xp)
+    out = []
+    for dx, dq in dirs:
+        lp = _oracle_steps_loss(O, ocfg, s, x0 + FD_H * dx, q0 + FD_H * dq, masks, 2, nsteps, dt, probes, nthreads)
+        lm = _oracle_steps_loss(O, ocfg, s, x0 - FD_H * dx, q0 - FD_H * dq, masks, 2, nsteps, dt, probes, nthreads)
+        out.append((lp - lm) / (2 * FD_H))
+    return out
+
+
 def test_adjoint_gradient_matches_oracle_central_differences(gpulib, oracle):
+    """The GPU gradient of the 10-step loss against central differences of
+    the oracle's forward (the C++ restatement of the reference's step) on
+    64 random directions: 128 oracle runs of 10 steps, computed once per
+    process, spread over a few spawned processes."""
+    import multiprocessing as mp
+    import os
     V, O = gpulib, oracle
     from vpm_free_gb300 import workloads as W
     xp, qp, w = W.ring64()
     ocfg, _ = configs_for(w)
     s = O.define_sizes(ocfg, xp)
     h, x0, q0, _ = _ring64_state(V)
-    probes = shell_probes(256, 1.2, 1.4, seed=12)
-    nsteps, dt = 3, w["dt"]
-    nn = list(s.nn)
-    xmin, d = list(s.xbound)[:3], list(s.dpm)
-
-    masks = [np.zeros(int(np.prod(nn)), dtype=np.int32) for _ in range(nsteps)]
-
-    def oracle_loss(x, q, mode):
-        """mode 1: the reference's remesh cut, recording the masks; 2: replaying them."""
-        x, q = x.copy(), q.copy()
-        for k in range(nsteps):
-            up, gp = O.step_fields(ocfg, s, x, q)
-            O.euler(x, q, up, gp, dt)
-            x, q = O.remesh_masked(ocfg, s, x, q, masks[k], mode)
-        O.step_fields(ocfg, s, x, q)
-        vel = O.get_field(O.F_VEL).reshape(3, nn[2], nn[1], nn[0])
-        return field_loss(vel, xmin, d, probes, KE)
-
+    probes = shell_probes(1024, 1.2, 1.4)
+    nsteps, dt = w["steps"], w["dt"]
+    masks = [np.zeros(int(np.prod(list(s.nn))), dtype=np.int32) for _ in range(nsteps)]
+    dirs = _directions(x0, q0, 64, seed=9)
     with h:
         h.set_particles(x0, q0)
         loss, xbar, qbar, _, _ = h.adjoint_run(nsteps, dt, probes, KE)
-        assert abs(loss - oracle_loss(x0, q0, 1)) <= 1e-10 * abs(loss)
-        g_adj, g_fd = [], []
-        for dx, dq in _directions(x0, q0, 6, seed=9):
-            lp = oracle_loss(x0 + FD_H * dx, q0 + FD_H * dq, 2)
-            lm = oracle_loss(x0 - FD_H * dx, q0 - FD_H * dq, 2)
-            g_fd.append((lp - lm) / (2 * FD_H))
-            g_adj.append(float(np.sum(xbar * dx) + np.sum(qbar * dq[:, :3])))
-        assert rel_l2(g_adj, g_fd) <= FD_TOL, (g_adj, g_fd)
+        assert abs(loss - _oracle_steps_loss(O, ocfg, s, x0, q0, masks, 1, nsteps, dt, probes)) <= 1e-10 * abs(loss)
+        if "fd" not in _ORACLE_FD:
+            nproc = max(1, min(4, (os.cpu_count() or 1) // 4))
+            threads = max(1, (os.cpu_count() or 1) // nproc)
+            jobs = [(x0, q0, dirs[i::nproc], masks, nsteps, dt, probes, threads) for i in range(nproc)]
+            with mp.get_context("spawn").Pool(nproc) as pool:
+                parts = pool.map(_oracle_fd_worker, jobs)
+            g = np.empty(len(dirs))
+            for i, part in enumerate(parts):
+                g[i::nproc] = part
+            _ORACLE_FD["fd"] = g
+        g_fd = _ORACLE_FD["fd"]
+        g_adj = np.array([float(np.sum(xbar * dx) + np.sum(qbar * dq[:, :3])) for dx, dq in dirs])
+        assert rel_l2(g_adj, g_fd) <= FD_TOL, (g_adj[:4], g_fd[:4])
 
 
 def test_torch_autograd_bridge(gpulib):

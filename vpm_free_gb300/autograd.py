@@ -6,7 +6,8 @@ remesh) from particles ``xp`` (NVR, 3) and ``qp`` (NVR, 4) -- the
 reference's XP / QP layout -- and back-propagates d loss / d xp and
 d loss / d qp[:, :3] computed by the library's exact transpose of every
 step (``vpmg_adjoint_run``).  QP(4) (the particle volume) is treated as a
-constant.  The library computes in FP64 on the GPU; the tensors may live
+constant.  The library computes on the GPU in the handle's arithmetic
+(IEEE FP64 unless the handle was set to float-float); the tensors may live
 on any device and are copied through host memory.
 """
 import numpy as np

@@ -1339,6 +1339,17 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
       f = [h, mr, R, l, u, st] { remesh_mask(mr, h->bins, R, l.data(), u.data(), (double)1e-09f, st); };
       fl = 5.0 * (double)N;
       by = 24.0 * (double)N + 4.0 * (double)N + 8.0 * (double)N;  // |w| read, flags written, scan
+    } else if (which == 8) {
+      // the sort by cell and the particle records on the global mesh
+      // (k_keys, scan, k_scatter, k_cell_order, k_records64)
+      const MeshDev mg = mesh_dev(h->gglob, h->cfg.interf_iproj);
+      f = [h, mg, st] { bin_particles(h->parts, mg, h->bins, st); };
+      f();
+      const double P = (double)read_count(h->bins.nsorted_dev, st);
+      fl = 112.0 * P;  // 12 projection weights (offset + M4' polynomial, 8 flops each) + 16 y-z products
+      // per particle: positions in, key and cursor, perm, strengths in, 24 record slots out; per node: counts,
+      // starts and their scan
+      by = 300.0 * P + 20.0 * (double)N;
     } else {
       throw Error{VPMG_ERR_ARG, "unknown kernel id"};
     }

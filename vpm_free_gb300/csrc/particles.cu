@@ -233,10 +233,23 @@ __global__ void k_records64(const double* __restrict__ x, const double* __restri
     for (int d = 0; d < 3; ++d) {
       const int node0 = cell[d] - m.ips;  // 0-based node = (i-1) of the reference
       const double off = pos[d] - m.xmin[d];
+      if (m.itype == 4) {
+        // M4' at the four distances 1+f, f, 1-f, 2-f from the offset f of
+        // the cell's own node (the branches of projection_fun resolved by
+        // the stencil's geometry): 16 FP64 operations instead of four
+        // offsets and four branchy polynomials
+        const double f = (off - (double)(node0 + 1) * m.d[d]) * m.inv[d];
+        const double g = 1.0 - f, f2 = f * f, g2 = g * g;
+        wgt[d][0] = -0.5 * (f * g2);
+        wgt[d][1] = fma(1.5 * f, f2, fma(-2.5, f2, 1.0));
+        wgt[d][2] = fma(1.5 * g, g2, fma(-2.5, g2, 1.0));
+        wgt[d][3] = -0.5 * (f2 * g);
+      } else {
 #pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        const double t = (off - (double)(node0 + a) * m.d[d]) * m.inv[d];
-        wgt[d][a] = (a <= m.ips + m.ipf) ? proj_fun_f64(m.itype, fabs(t)) : 0.0;
+        for (int a = 0; a < 4; ++a) {
+          const double t = (off - (double)(node0 + a) * m.d[d]) * m.inv[d];
+          wgt[d][a] = (a <= m.ips + m.ipf) ? proj_fun_f64(m.itype, fabs(t)) : 0.0;
+        }
       }
     }
 #pragma unroll
@@ -270,6 +283,8 @@ __global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restr
                                                              double* __restrict__ r1, double* __restrict__ r2) {
   __shared__ double pf[kDepWarps][32][3], pl[kDepWarps][32][3], tot[kDepWarps][32][3];
   __shared__ int soff[kDepWarps][32], scnt[kDepWarps][32], snA[kDepWarps][32], snB[kDepWarps][32];
+  __shared__ long long srow[kDepWarps][16];  // start of each covering cell row (linear cell index at x = 0)
+  __shared__ int swyz[kDepWarps][16];        // the y-z weight slot of that row for this node row
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int nseg = (m.n[0] + 31) / 32;
@@ -284,7 +299,13 @@ __global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restr
   // the cell rows covering this node row (the same for every lane)
   const int cj0 = max(j - m.ipf, 0), cj1 = min(j + m.ips, m.n[1] - 1);
   const int ck0 = max(k - m.ipf, 0), ck1 = min(k + m.ips, m.n[2] - 1);
-  const int ncj = cj1 - cj0 + 1, nrow = ncj * (ck1 - ck0 + 1);
+  const int ncj = cj1 - cj0 + 1, nrow = ncj * (ck1 - ck0 + 1);  // at most 4 x 4
+  if (lane < nrow) {
+    const int cj = cj0 + lane % ncj, ck = ck0 + lane / ncj;
+    srow[wl][lane] = (long long)m.n[0] * (cj + (long long)m.n[1] * ck);
+    swyz[wl][lane] = 4 + 4 * (j - cj + m.ips) + (k - ck + m.ips);
+  }
+  __syncwarp();
   const double* q0 = rec + kRecQ * cs;
   const double* q1 = rec + (kRecQ + 1) * cs;
   const double* q2 = rec + (kRecQ + 2) * cs;
@@ -294,7 +315,7 @@ __global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restr
   if (valid) {
     const int xl = max(i - m.ipf, 0), xh = min(i + m.ips, m.n[0] - 1);
     for (int r = 0; r < nrow; ++r) {
-      const size_t rb = (size_t)m.n[0] * ((cj0 + r % ncj) + (size_t)m.n[1] * (ck0 + r / ncj));
+      const long long rb = srow[wl][r];
       cnt += __ldg(&starts[rb + xh + 1]) - __ldg(&starts[rb + xl]);
     }
   }
@@ -339,14 +360,14 @@ __global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restr
     int local = v0 - soff[wl][n];
     int r = 0, tb = 0, te = 0;
     for (;; ++r) {
-      const size_t rb = (size_t)m.n[0] * ((cj0 + r % ncj) + (size_t)m.n[1] * (ck0 + r / ncj));
+      const long long rb = srow[wl][r];
       tb = __ldg(&starts[rb + xl]);
       te = __ldg(&starts[rb + xh + 1]);
       if (local < te - tb) break;
       local -= te - tb;
     }
     int t = tb + local;
-    int wyz_slot = 4 + 4 * (j - (cj0 + r % ncj) + m.ips) + (k - (ck0 + r / ncj) + m.ips);
+    int wyz_slot = swyz[wl][r];
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     for (int v = v0; v < v1; ++v) {
       const int ix = ii - __double2loint(__ldg(&cellw[t])) + m.ips;
@@ -367,13 +388,13 @@ __global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restr
           xh = min(ii + m.ips, m.n[0] - 1);
           r = 0;
         }
-        const size_t rb = (size_t)m.n[0] * ((cj0 + r % ncj) + (size_t)m.n[1] * (ck0 + r / ncj));
+        const long long rb = srow[wl][r];
         tb = __ldg(&starts[rb + xl]);
         te = __ldg(&starts[rb + xh + 1]);
         if (te > tb) break;
       }
       t = tb;
-      wyz_slot = 4 + 4 * (j - (cj0 + r % ncj) + m.ips) + (k - (ck0 + r / ncj) + m.ips);
+      wyz_slot = swyz[wl][r];
     }
     double* dst = (n == nA) ? pf[wl][lane] : pl[wl][lane];  // the chunk's last node
     dst[0] = a0; dst[1] = a1; dst[2] = a2;
