@@ -304,7 +304,7 @@ def run_batch_group(args, local):
     hs = []
     try:
         for xp, qp, w in probs:
-            h = V.VPM(V.VPMConfig.make(dpm=w["dpm"], box=w["box"]), device=local)
+            h = V.VPM(V.VPMConfig.make(dpm=w["dpm"], box=w["box"]), device=local, arith=args.arith)
             hs.append(h)
             h.define_sizes(xp)
             xr, qr = h.remesh_particles_3d(1, xp, qp)
@@ -316,7 +316,8 @@ def run_batch_group(args, local):
     finally:
         for h in hs:
             h.close()
-    print(json.dumps({"workload": f"batch group {name} x {len(probs)}", "steps": max(1, args.steps), "ms": ms,
+    print(json.dumps({"workload": f"batch group {name} x {len(probs)}", "arith": args.arith, "steps": max(1, args.steps),
+                      "ms": ms,
                       "solves_per_s": solves / (ms * 1e-3), "graphs_per_step": units,
                       "problems_sharing_an_operator": shared, "corrected_rows": rows}))
     return 0
@@ -393,13 +394,14 @@ def run_dirichlet(args, local):
     rng = np.random.default_rng(0)
     R = [rng.normal(size=(n, n, n)) for _ in range(3)]
     S = [np.zeros((n, n, n)) for _ in range(3)]
-    with V.VPM(V.VPMConfig.make(), device=local) as h:
+    with V.VPM(V.VPMConfig.make(), device=local, arith=args.arith) as h:
         t = []
         for _ in range(max(1, args.steps)):
             t0 = time.perf_counter()
             h.pmesh(S, R, [0.0, 0.0, 0.0, 1.0, 1.0, 1.0], [1.0 / (n - 1)] * 3, 0)
             t.append(time.perf_counter() - t0)
-    print(json.dumps({"workload": f"dirichlet{n}", "unit": "s per pmesh(iynbc=0) call, host clock incl. copies",
+    print(json.dumps({"workload": f"dirichlet{n}", "arith": args.arith,
+                      "unit": "s per pmesh(iynbc=0) call, host clock incl. copies",
                       "s": t}))
     return 0
 
