@@ -205,6 +205,13 @@ long long vpmg_kernel_launches(const vpmg_handle* h);
 int vpmg_phase_times(const vpmg_handle* h, double ms[9]);
 /* Boundary-operator statistics: interactions per fine solve, bytes held. */
 int vpmg_tree_stats(const vpmg_handle* h, long long* interactions, long long* bytes, int* precomputed);
+/* Whether the fine block's operator evaluates its coarsest tree level by
+ * FFT convolutions on the face lattices (FP64 handles whose coarsest cells
+ * form uniform lattices; VPMG_FARFIELD=0 at set-up keeps the dense block),
+ * its correction entries (the coarsest cells the walk opened) and the
+ * FP64 flops of one apply of the FFT part.  Instrumentation; no counterpart
+ * in the reference.                                                     */
+int vpmg_farfield_stats(const vpmg_handle* h, int* on, long long* corrections, double* flops);
 /* Per-phase event timing: 0 off (default), 1 on; 2 also keeps the
  * intermediate block fields readable by vpmg_get_field and evaluates the
  * block solves on the whole block (as the reference does) instead of only

@@ -44,7 +44,7 @@ EXPORTS = [
     "vpmg_dst_tiles", "vpmg_apply_poisson", "vpmg_adjoint_poisson", "vpmg_vjp_fields", "vpmg_vjp_remesh", "vpmg_adjoint_loss",
     "vpmg_adjoint_run", "vpmg_batch_create", "vpmg_batch_info", "vpmg_batch_step", "vpmg_batch_destroy",
     "vpmg_batch_set_schedule", "vpmg_batch_get_schedule", "vpmg_host_euler", "vpmg_set_arithmetic",
-    "vpmg_get_arithmetic", "vpmg_dirichlet_static", "vpmg_projection_fun",
+    "vpmg_get_arithmetic", "vpmg_dirichlet_static", "vpmg_projection_fun", "vpmg_farfield_stats",
 ]
 
 
@@ -131,6 +131,7 @@ def load_library():
     L.vpmg_kernel_launches.restype = C.c_longlong
     L.vpmg_phase_times.argtypes = [C.c_void_p, _dp]
     L.vpmg_tree_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]
+    L.vpmg_farfield_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_longlong), _dp]
     L.vpmg_set_profiling.argtypes = [C.c_void_p, C.c_int]
     L.vpmg_set_operator_budget.argtypes = [C.c_void_p, C.c_longlong]
     L.vpmg_run.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, C.c_int, _dp, C.POINTER(C.c_longlong)]
@@ -443,6 +444,14 @@ class VPM:
         a, b, c = C.c_longlong(0), C.c_longlong(0), C.c_int(0)
         self._chk(self._L.vpmg_tree_stats(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return {"interactions": a.value, "bytes": b.value, "precomputed": bool(c.value)}
+
+    def farfield_stats(self):
+        """{'on': the coarsest tree level goes by FFT convolutions, 'corrections':
+        opened coarsest cells subtracted as rows, 'flops': FP64 flops of one
+        apply of the FFT part}."""
+        a, b, c = C.c_int(0), C.c_longlong(0), C.c_double(0.0)
+        self._chk(self._L.vpmg_farfield_stats(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"on": bool(a.value), "corrections": b.value, "flops": c.value}
 
     def write_solution(self, ntime, directory=None):
         """NNNNNsolution.bin of the last field step (writesol, source/vpm.f90:662-709)."""

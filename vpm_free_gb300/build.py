@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvpmg.so")
 
-CU = ["api.cu", "poisson.cu", "particles.cu", "boundary.cu", "fields.cu", "util.cu", "block_solve.cu", "adjoint.cu", "yaps_multi.cu"]
+CU = ["api.cu", "poisson.cu", "particles.cu", "boundary.cu", "fields.cu", "util.cu", "block_solve.cu", "adjoint.cu", "yaps_multi.cu", "farfield.cu"]
 CPP = ["tree_host.cpp", "yaps_host.cpp", "io_files.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",

@@ -1259,6 +1259,16 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
       fl = 2.0 * 3.0 * nnz;  // three FMAs per interaction
       // streamed bytes: 12 per row entry (cell id + weight pair), 8 per slot of the dense block
       by = bo->precomputed ? (double)bo->nnz * (sizeof(int) + sizeof(float2)) + (double)bo->wtop.bytes() : 0.0;
+      if (bo->ff.on) {
+        // the coarsest level by FFT: the finer rows and the correction rows
+        // at three FMAs per entry, plus the transforms' flops; bytes: both
+        // row lists, the kernel spectra, and the transform arrays read and
+        // written once per pass
+        const FarField& F = bo->ff;
+        fl = 6.0 * ((double)bo->nnz + (double)F.ncorr) + F.flops;
+        by = 12.0 * ((double)bo->nnz + (double)F.ncorr) + (double)(F.kperp.bytes() + F.kpar.bytes()) +
+             4.0 * (double)(F.S2.bytes() + F.X.bytes() + F.Z.bytes() + F.Sw.bytes() + F.T.bytes());
+      }
     } else if (which == 1) {
       h->bench_scratch.ensure(NB);
       double* o = h->bench_scratch.p;
@@ -1705,6 +1715,15 @@ int vpmg_tree_stats(const vpmg_handle* h, long long* interactions, long long* by
   if (interactions) *interactions = bo.nnz + bo.ndense_acc;
   if (bytes) *bytes = bo.bytes();
   if (precomputed) *precomputed = bo.precomputed ? 1 : 0;
+  return VPMG_OK;
+}
+
+int vpmg_farfield_stats(const vpmg_handle* h, int* on, long long* corrections, double* flops) {
+  if (!h) return VPMG_ERR_ARG;
+  const BoundaryOp& bo = h->nblk > 1 && !h->bo_blk.empty() ? *h->bo_blk[0] : h->bo_bl;
+  if (on) *on = bo.ff.on ? 1 : 0;
+  if (corrections) *corrections = bo.ff.on ? bo.ff.ncorr : 0;
+  if (flops) *flops = bo.ff.on ? bo.ff.flops : 0.0;
   return VPMG_OK;
 }
 

@@ -834,7 +834,8 @@ PanelFrame make_frame(int iplane, const double d[3]) {
 
 long long BoundaryOp::bytes() const {
   return (long long)(rowptr.bytes() + col.bytes() + w.bytes() + colptr.bytes() + trow.bytes() + tw.bytes() +
-                     cx.bytes() * 5 + child.bytes() + csrc.bytes() + wtop.bytes() + dsum.bytes());
+                     cx.bytes() * 5 + child.bytes() + csrc.bytes() + wtop.bytes() + dsum.bytes()) +
+         ff.bytes();
 }
 
 void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s, int ibctyp,
@@ -982,6 +983,7 @@ void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget
     }
   }
   if (!B.precomputed) B.dense = false;  // the walk covers every level
+  farfield_prepare(B, g, s);
 }
 
 void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp, cudaStream_t s) {
@@ -1021,6 +1023,21 @@ static void apply_recorded(BoundaryOp& B, double* const sol[3], cudaStream_t s) 
   k_split<M><<<(unsigned)std::min<size_t>((nc4 + 255) / 256, 152 * 16), 256, 0, s>>>(B.csrc.p, B.ncell_total, src);
   VPMG_LAUNCHED();
   const H* src2 = reinterpret_cast<const H*>(src);
+  if (!M::kFF && B.ff.on) {
+    // the coarsest level by FFT over every cell into the partial sums, the
+    // finer rows on top, then the opened coarsest cells taken back out
+    farfield_apply(B, B.dsum.p, s);
+    const long long threads = (long long)B.ntarget * 32;
+    k_apply_csr<M><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+        B.rowptr.p, B.col.p, reinterpret_cast<const typename M::W*>(B.w.p), src2, B.tgt_node.p, B.ntarget,
+        1.0 / (4.0 * kPI), sol[0], sol[1], sol[2], B.dsum.p, 1);
+    VPMG_LAUNCHED();
+    k_apply_csr<M><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+        B.ff.crow.p, B.ff.ccol.p, reinterpret_cast<const typename M::W*>(B.ff.cw.p), src2, B.tgt_node.p, B.ntarget,
+        1.0 / (4.0 * kPI), sol[0], sol[1], sol[2], nullptr, 0);
+    VPMG_LAUNCHED();
+    return;
+  }
   if (B.dense) {
     const long long dthreads = (long long)((B.ntarget + 31) / 32) * 32;
     const int cseg = dense_cseg(B);
@@ -1138,6 +1155,7 @@ bool boundary_group_match(const BoundaryOp& L, const Grid& gl, const BoundaryOp&
 void boundary_release_recorded(BoundaryOp& B) {
   B.rowptr.release(); B.col.release(); B.w.release(); B.wtop.release(); B.dsum.release(); B.csrc_ff.release();
   B.colptr.release(); B.trow.release(); B.tw.release(); B.vff.release(); B.dpart.release();
+  farfield_release(B);
   B.precomputed = false;
   B.dense = false;
   B.transposed = false;

@@ -141,6 +141,38 @@ struct PanelFrame {
   double E1[3], E2[3], E3[3], S[4], T[4], D[4], diag, area;
 };
 
+// The coarsest tree level of a recorded operator evaluated as convolutions
+// on the face lattices (farfield.cu).  Every target sums every coarsest cell
+// (the opened ones included) by FFTs: between parallel faces a 2-D
+// convolution, between perpendicular faces a 1-D convolution along their
+// shared axis and a dense sum over the other two; the cells each target
+// opened are then subtracted as sparse correction rows.
+struct FarFieldAxis {    // complex FFT of length P = 2^a 3^b along one axis
+  int P = 0, nst = 0, npair = 1;
+  int radix[16];
+  DBuf<double2> tw;      // e^{-2 pi i t / P}
+};
+struct FarField {
+  bool on = false;
+  int istep = 0;                      // panels per coarsest cell side
+  int N[3] = {0, 0, 0};               // grid nodes per axis
+  double h[3] = {0, 0, 0};            // grid spacing per axis
+  double dS[6] = {0, 0, 0, 0, 0, 0};  // area of a coarsest cell of each face
+  int cell0[6] = {0, 0, 0, 0, 0, 0};  // first coarsest cell of each face (within the level)
+  FarFieldAxis ax[3];
+  long long kpar_off[3][2] = {{0, 0}, {0, 0}, {0, 0}};  // [normal axis][same face, opposite face]
+  long long kperp_off[24] = {};       // [target face * 4 + perpendicular source slot]
+  long long t_off[6][2] = {}, s2_off[6][2] = {}, sw_off[6][2] = {}, z_off[6][2] = {};
+  DBuf<double> kpar, kperp;           // kernel spectra (real), the inverse scalings folded in
+  DBuf<double2> T, S2, X, Sw, Z;      // transform work arrays
+  double flops = 0.0;                 // FP64 flops of one apply (FFTs 5 P log2 P per line, products, sums)
+  long long ncorr = 0;                // correction rows: the opened coarsest cells, weight -dS/r
+  DBuf<long long> crow;
+  DBuf<int> ccol;
+  DBuf<double> cw;
+  long long bytes() const;
+};
+
 struct BoundaryOp {
   // panels (level 0) and aggregated levels, device copies
   int nbound = 0, levmax = 0, ncell_total = 0, ntarget = 0;
@@ -188,10 +220,18 @@ struct BoundaryOp {
   DBuf<float2> tw;                      // weight words of the transposed list
   DBuf<float2> vff;                     // per target: the boundary-value adjoint in the operator's arithmetic
   DBuf<double> dpart;                   // dense transpose: partial sums [chunk group][cell]
+  FarField ff;                          // the dense block's sums by FFT (FP64, uniform coarsest lattices)
   long long bytes() const;
 };
 void boundary_prepare(BoundaryOp& B, const Grid& g, int levmax, long long budget_bytes, cudaStream_t s,
                       int ibctyp, bool tree, int arith);
+// Sets B.ff up when the recorded operator's coarsest level is a uniform
+// lattice on every face (FP64, ibctyp 2, tree, dense block recorded) and
+// VPMG_FARFIELD is not "0"; set-up time, outside stream capture.
+void farfield_prepare(BoundaryOp& B, const Grid& g, cudaStream_t s);
+// dsum[comp][target] = sum over every coarsest cell of dS/r times its source.
+void farfield_apply(BoundaryOp& B, double* dsum, cudaStream_t s);
+void farfield_release(BoundaryOp& B);
 // Per component: normal-derivative panels from the zero-BC solution sol0,
 // aggregate, then add the boundary values into the faces of sol.
 void boundary_panels(BoundaryOp& B, const Grid& g, const double* sol0, int comp, cudaStream_t s);
