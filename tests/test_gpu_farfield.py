@@ -106,3 +106,39 @@ def test_fft_far_field_declines_irregular_lattices(gpulib, oracle, monkeypatch):
     O.pmesh(ref, rhs, xb, d, iynbc=1, itree=1, levmax=levmax)
     for c in range(3):
         assert rel_l2(fast[c], ref[c]) <= FIELD_TOL, c
+
+
+def test_fft_operators_are_not_grouped(gpulib, monkeypatch):
+    """Problems whose coarsest level goes by FFT keep their own operators in
+    a batch (the group apply would use the dense block); with the dense
+    block (float-float, or VPMG_FARFIELD=0) the two ring32 problems share
+    one."""
+    from vpm_free_gb300 import workloads as W
+    V = gpulib
+    probs = [p for p in W.batched_rings(64) if p[2]["name"] == "ring32"][:2]
+
+    def handles():
+        out = []
+        for xp, qp, w in probs:
+            h = V.VPM(V.VPMConfig.make(dpm=w["dpm"], box=w["box"]))
+            h.define_sizes(xp)
+            xr, qr = h.remesh_particles_3d(1, xp, qp)
+            h.set_particles(xr, qr)
+            out.append(h)
+        return out
+    monkeypatch.delenv("VPMG_FARFIELD", raising=False)
+    hs = handles()
+    fft = hs[0].farfield_stats()["on"]
+    assert fft == (gpulib.arith == "fp64")
+    with V.Batch(hs) as b:
+        assert b.info() == ((2, 0) if fft else (1, 2))
+        b.run(1, 0.01)
+    for h in hs:
+        h.close()
+    monkeypatch.setenv("VPMG_FARFIELD", "0")
+    hs = handles()
+    assert not hs[0].farfield_stats()["on"]
+    with V.Batch(hs) as b:
+        assert b.info() == (1, 2)
+    for h in hs:
+        h.close()

@@ -198,12 +198,15 @@ def _batch_problems(V, names):
     return out
 
 
-def test_shared_operator_batch_equals_individual_runs(gpulib):
+def test_shared_operator_batch_equals_individual_runs(gpulib, monkeypatch):
     """Three 32^3 problems with different spacings share one recorded
     boundary operator (weights scaled by the spacing ratio, one apply for
     the group); a 48^3 problem runs its own graph.  Each must reproduce its
     individual run: the grouped ones to rounding (another summation order,
-    scaled weights), the single one bit for bit."""
+    scaled weights), the single one bit for bit.  The operators keep their
+    dense coarsest level (VPMG_FARFIELD=0): FFT-evaluated ones are not
+    grouped."""
+    monkeypatch.setenv("VPMG_FARFIELD", "0")
     V = gpulib
     names = ["ring32", "ring32", "ring32", "ring48"]
     solo = []
@@ -229,10 +232,11 @@ def test_shared_operator_batch_equals_individual_runs(gpulib):
 
 
 @pytest.mark.parametrize("count", [6, 9])
-def test_large_batch_groups_equal_individual_runs(gpulib, count):
+def test_large_batch_groups_equal_individual_runs(gpulib, count, monkeypatch):
     """Groups of 6 and 9 problems: two and three problem quads per warp set
     in the dense-block kernel, 5 and 3 lane sets in the row kernel (2 and 5
     idle lanes); every member reproduces its individual run."""
+    monkeypatch.setenv("VPMG_FARFIELD", "0")
     V = gpulib
     names = ["ring32"] * count
     solo = []
@@ -252,11 +256,12 @@ def test_large_batch_groups_equal_individual_runs(gpulib, count):
         h.close()
 
 
-def test_shared_operator_batch_fields_match_oracle(gpulib, oracle):
+def test_shared_operator_batch_fields_match_oracle(gpulib, oracle, monkeypatch):
     """One batched step of a two-problem group: the resident vector
     potential and velocity of each member against the oracle's step on the
     same particles.  The follower's own operator is released; afterwards it
     steps alone by walking the tree."""
+    monkeypatch.setenv("VPMG_FARFIELD", "0")
     V, O = gpulib, oracle
     hp = _batch_problems(V, ["ring32", "ring32"])
     with V.Batch([t[0] for t in hp], release_shared=True) as b:

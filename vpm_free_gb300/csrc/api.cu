@@ -164,7 +164,10 @@ void prepare(vpmg_handle* h) {
   size_t wmax = 0;
   for (DirichletPlan* p : {&h->dp_bl, &h->dp_inner, &h->dp_c}) wmax = std::max(wmax, (size_t)p->m[0] * p->m[1] * p->m[2]);
   h->work.ensure(wmax);
-  if (h->nblk == 1) h->bsolve.prepare(h->dp_bl, s.nnbl_bl, h->cfg.ncoarse);
+  if (h->nblk == 1) {
+    h->bsolve.prepare(h->dp_bl, s.nnbl_bl, h->cfg.ncoarse);
+    h->fsolve.prepare(h->dp_inner);
+  }
   for (int d = 0; d < 3; ++d) {
     h->inner_lo[d] = s.nnbl_bl[d] - 1;
     h->inner_ext[d] = s.nnbl_bl[d + 3] - s.nnbl_bl[d] + 1;
@@ -337,8 +340,15 @@ void poisson_tail(vpmg_handle* h) {
   infinite_domain(h, h->dp_c, h->bo_c, h->gco, h->crhs.p, h->csol.p, h->csol0.p, NC);
   yaps_face_interp(h->yaps, s.nn_coarse, CS, SM, SB, st);
   ev_mark(h, 5);
-  // (e): final Dirichlet solve on the inner block box
-  for (int c = 0; c < 3; ++c) dirichlet_solve(h->dp_inner, comp(h->rhs_bl, NB, c), SB[c], false, h->work.p, st);
+  // (e): final Dirichlet solve on the inner block box: the RHS (zero away
+  // from the vorticity) transformed alone, the faces' values in DST space
+  // (the block's transform scratch W is free by now)
+  for (int c = 0; c < 3; ++c) {
+    if (h->fsolve.ready && h->bsolve.ready)
+      dirichlet_solve_faces(h->dp_inner, h->fsolve, comp(h->rhs_bl, NB, c), SB[c], h->work.p, h->bsolve.W.p, st);
+    else
+      dirichlet_solve(h->dp_inner, comp(h->rhs_bl, NB, c), SB[c], false, h->work.p, st);
+  }
   // solget_3d
   double* S[3] = {comp(h->sol, N, 0), comp(h->sol, N, 1), comp(h->sol, N, 2)};
   for (int c = 0; c < 3; ++c) box_copy(SB[c], s.nnbl, h->inner_lo, S[c], s.nn, go, h->inner_ext, st);

@@ -203,6 +203,34 @@ __global__ void k_extract_faces(const double* __restrict__ s, int NX, int NY, in
   }
 }
 
+// The six faces of the box whose node (0,0,0) sits at (o0,o1,o2) of an
+// NX x NY x * array, interior m0 x m1 x m2: fx* [k][j], fy* [k][i], fz* [j][i].
+__global__ void k_extract_box_faces(const double* __restrict__ s, int NX, int NY, int o0, int o1, int o2, int m0,
+                                    int m1, int m2, double* __restrict__ fx0, double* __restrict__ fxN,
+                                    double* __restrict__ fy0, double* __restrict__ fyN, double* __restrict__ fz0,
+                                    double* __restrict__ fzN) {
+  const size_t sy = NX, sz = (size_t)NX * NY;
+  const long nx = (long)m1 * m2, ny = (long)m0 * m2, nz = (long)m0 * m1;
+  auto at = [&](int a, int b, int c) { return s[(size_t)(o0 + a) + sy * (o1 + b) + sz * (o2 + c)]; };
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nx + ny + nz; t += (long)gridDim.x * blockDim.x) {
+    if (t < nx) {
+      const int j = (int)(t % m1) + 1, k = (int)(t / m1) + 1;
+      fx0[t] = at(0, j, k);
+      fxN[t] = at(m0 + 1, j, k);
+    } else if (t < nx + ny) {
+      const long u = t - nx;
+      const int i = (int)(u % m0) + 1, k = (int)(u / m0) + 1;
+      fy0[u] = at(i, 0, k);
+      fyN[u] = at(i, m1 + 1, k);
+    } else {
+      const long u = t - nx - ny;
+      const int i = (int)(u % m0) + 1, j = (int)(u / m0) + 1;
+      fz0[u] = at(i, j, 0);
+      fzN[u] = at(i, j, m2 + 1);
+    }
+  }
+}
+
 struct FaceTerms {
   const double *fx0, *fxN, *fy0, *fyN, *fz0, *fzN;  // transforms: [k][q], [k][p], [q][p]
   const double *ex1, *exN, *ey1, *eyN;              // sin(pi (p+1)/N), sin(pi m (p+1)/N)
@@ -530,6 +558,61 @@ void block_solve_bc(BlockSolve& B, DirichletPlan& P, int c, double* sol_c, cudaS
       {&P.fx, pl0, sol_c, {dm[0], dm[1], dm[2]}, {1, 1, B.inner_lo[2] + 1}, {m0, m1, 1}},
       {&P.fx, pl1, sol_c, {dm[0], dm[1], dm[2]}, {1, 1, B.inner_hi[2] + 1}, {m0, m1, 1}}};
   dst_x_inv_jobs(xz, 2, s);
+  VPMG_CUDA(cudaGetLastError());
+}
+
+void FaceSolve::prepare(const DirichletPlan& P) {
+  const int m0 = P.m[0], m1 = P.m[1], m2 = P.m[2];
+  f.ensure(2 * ((size_t)m1 * m2 + (size_t)m0 * m2 + (size_t)m0 * m1));
+  std::vector<double> e(2 * (size_t)m0 + 2 * (size_t)m1);
+  for (int p = 0; p < m0; ++p) {
+    e[p] = std::sin(kPI * (double)(p + 1) / (double)(m0 + 1));
+    e[m0 + p] = std::sin(kPI * (double)m0 * (double)(p + 1) / (double)(m0 + 1));
+  }
+  for (int q = 0; q < m1; ++q) {
+    e[2 * m0 + q] = std::sin(kPI * (double)(q + 1) / (double)(m1 + 1));
+    e[2 * m0 + m1 + q] = std::sin(kPI * (double)m1 * (double)(q + 1) / (double)(m1 + 1));
+  }
+  this->e.ensure(e.size());
+  VPMG_CUDA(cudaMemcpy(this->e.p, e.data(), sizeof(double) * e.size(), cudaMemcpyHostToDevice));
+  ready = true;
+}
+
+void dirichlet_solve_faces(DirichletPlan& P, FaceSolve& FS, const double* rhs, double* sol, double* work,
+                           double* out, cudaStream_t s) {
+  VPMG_CHECK(FS.ready, VPMG_ERR_STATE, "face solve not prepared");
+  const int m0 = P.m[0], m1 = P.m[1], m2 = P.m[2];
+  const size_t plane = (size_t)m0 * m1;
+  // forward transforms of the RHS alone (zero tiles skip their FFTs)
+  dst_forward_xy(P, rhs, nullptr, true, work, s);
+  // the faces' values, transformed along their own axes
+  double* fx0 = FS.f.p;
+  double* fxN = fx0 + (size_t)m1 * m2;
+  double* fy0 = fxN + (size_t)m1 * m2;
+  double* fyN = fy0 + (size_t)m0 * m2;
+  double* fz0 = fyN + (size_t)m0 * m2;
+  double* fzN = fz0 + (size_t)m0 * m1;
+  k_extract_box_faces<<<256, 256, 0, s>>>(sol, P.dims[0], P.dims[1], P.box[0], P.box[1], P.box[2], m0, m1, m2, fx0,
+                                          fxN, fy0, fyN, fz0, fzN);
+  VPMG_LAUNCHED();
+  const DstYLines rows[6] = {{&P.fy, fx0, 1, m1, m2}, {&P.fy, fxN, 1, m1, m2}, {&P.fx, fy0, 1, m0, m2},
+                             {&P.fx, fyN, 1, m0, m2}, {&P.fx, fz0, 1, m0, m1}, {&P.fx, fzN, 1, m0, m1}};
+  dst_lines_y_jobs(rows, 6, s);
+  const DstYLines cols[2] = {{&P.fy, fz0, m0, m1, 1}, {&P.fy, fzN, m0, m1, 1}};
+  dst_lines_y_jobs(cols, 2, s);
+  // the sweep with the face terms, then the full inverse transforms
+  const double scale = dirichlet_scale(P);
+  FaceTerms F;
+  F.fx0 = fx0; F.fxN = fxN; F.fy0 = fy0; F.fyN = fyN; F.fz0 = fz0; F.fzN = fzN;
+  F.ex1 = FS.e.p; F.exN = FS.e.p + m0; F.ey1 = FS.e.p + 2 * m0; F.eyN = FS.e.p + 2 * m0 + m1;
+  F.cx = -scale / (P.h[0] * P.h[0]);
+  F.cy = -scale / (P.h[1] * P.h[1]);
+  F.cz = -scale / (P.h[2] * P.h[2]);
+  k_thomas_faces<<<(int)((plane + 127) / 128), 128, 0, s>>>(work, out, P.rinvd.p, m0, m1, m2, 1, F);
+  VPMG_LAUNCHED();
+  dst_lines_y(P.fy, out, m0, m1, m2, s);
+  const int o[3] = {P.box[0] + 1, P.box[1] + 1, P.box[2] + 1};
+  dst_x_inv_to_box(P.fx, out, sol, P.dims, o, P.m, s);
   VPMG_CUDA(cudaGetLastError());
 }
 

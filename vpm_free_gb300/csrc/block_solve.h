@@ -24,6 +24,20 @@ struct BlockSolve {
   void prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoarse);
 };
 
+// A whole box's Dirichlet solve with its face values entering in DST space
+// (as the block's BC solve does): forward x/y transforms of the RHS alone,
+// so vorticity-free tiles skip their FFTs; the faces of sol, transformed
+// along their own axes, join the Thomas sweep; full inverse transforms into
+// sol's interior.  work and out: interior-size scratch arrays.
+struct FaceSolve {
+  bool ready = false;
+  DBuf<double> f;   // the six faces' values, then their transforms
+  DBuf<double> e;   // sines of the first and last interior layer along x and y
+  void prepare(const DirichletPlan& P);
+};
+void dirichlet_solve_faces(DirichletPlan& P, FaceSolve& F, const double* rhs, double* sol, double* work,
+                           double* out, cudaStream_t s);
+
 // Zero-BC solve of component c: forward transform kept in ghat, u near the
 // six faces (4 interior layers) written into sol0.
 void block_solve_zero_bc(BlockSolve& B, DirichletPlan& P, const double* rhs_c, int c, double* sol0, cudaStream_t s);

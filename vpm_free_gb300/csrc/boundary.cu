@@ -1073,6 +1073,12 @@ bool boundary_group_match(const BoundaryOp& L, const Grid& gl, const BoundaryOp&
                           double max_frac, double* ratio, GroupCorrection& C, cudaStream_t s) {
   if (!L.precomputed || !F.precomputed || L.ibctyp != 2 || F.ibctyp != 2 || L.tree != F.tree) return false;
   if (L.arith != F.arith) return false;
+  // an operator whose coarsest level goes by FFT stays with its problem: the
+  // group would apply that level as the dense block, and in FP64 (the only
+  // arithmetic of the FFT path) sharing the weights saves memory traffic
+  // the step does not wait on, while the dense block costs five times the
+  // FFT path's operations
+  if (L.ff.on || F.ff.on) return false;
   if (L.ntarget != F.ntarget || L.ncell_total != F.ncell_total || L.levmax != F.levmax || L.dense != F.dense ||
       L.ntopd != F.ntopd || L.lev_off != F.lev_off || L.wtop.n != F.wtop.n)
     return false;

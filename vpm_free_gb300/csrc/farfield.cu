@@ -514,7 +514,7 @@ void farfield_prepare(BoundaryOp& B, const Grid& g, cudaStream_t s) {
     make_axis(F.ax[a], P);
   }
   F.istep = istep;
-  for (int f = 0; f < 7 && f < 6; ++f) F.cell0[f] = cell0[f];
+  for (int f = 0; f < 6; ++f) F.cell0[f] = cell0[f];
   // ---- buffers ------------------------------------------------------------
   long long tsz = 0, s2sz = 0, swsz = 0, zsz = 0;
   for (int f = 0; f < 6; ++f) {

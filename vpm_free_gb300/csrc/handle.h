@@ -33,6 +33,7 @@ struct vpmg_handle {
   vpmg::DBuf<double> samp, crhs, csol, csol0;
   vpmg::DirichletPlan dp_bl, dp_inner, dp_c;
   vpmg::BlockSolve bsolve;         // partially evaluated block solves
+  vpmg::FaceSolve fsolve;          // the inner box's solve with its faces in DST space
   bool full_block_solves = false;  // evaluate the block solves everywhere (parity / debugging)
   vpmg::BoundaryOp bo_bl, bo_c;
   vpmg::YapsDev yaps;

@@ -309,7 +309,6 @@ __global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restr
   const double* q0 = rec + kRecQ * cs;
   const double* q1 = rec + (kRecQ + 1) * cs;
   const double* q2 = rec + (kRecQ + 2) * cs;
-  const double* cellw = rec + 23 * cs;
   // visits of this lane's node, and the warp's scan of them
   int cnt = 0;
   if (valid) {
@@ -359,23 +358,39 @@ __global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restr
     // row and slot of visit v0 inside node n
     int local = v0 - soff[wl][n];
     int r = 0, tb = 0, te = 0;
-    for (;; ++r) {
-      const long long rb = srow[wl][r];
+    // the row's cell boundaries: cell xl + k holds slots [b_k, b_{k+1}),
+    // b_0 = tb; e1..e4 = b_1..b_4 clamped to the row's end te.  Knowing the
+    // slot's cell from them, a visit's loads do not wait on a load of it.
+    int e1 = 0, e2 = 0, e3 = 0, e4 = 0;
+    auto bounds = [&](long long rb) {
       tb = __ldg(&starts[rb + xl]);
+      e1 = __ldg(&starts[rb + min(xl + 1, xh + 1)]);
+      e2 = __ldg(&starts[rb + min(xl + 2, xh + 1)]);
+      e3 = __ldg(&starts[rb + min(xl + 3, xh + 1)]);
+      e4 = __ldg(&starts[rb + min(xl + 4, xh + 1)]);
       te = __ldg(&starts[rb + xh + 1]);
+    };
+    for (;; ++r) {
+      bounds(srow[wl][r]);
       if (local < te - tb) break;
       local -= te - tb;
     }
     int t = tb + local;
     int wyz_slot = swyz[wl][r];
+    int kc = 0, nb = e1;  // the slot's cell offset from xl and the next cell's first slot
+    while (t >= nb && kc < 3) { ++kc; nb = kc == 1 ? e2 : kc == 2 ? e3 : e4; }
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     for (int v = v0; v < v1; ++v) {
-      const int ix = ii - __double2loint(__ldg(&cellw[t])) + m.ips;
+      const int ix = ii - (xl + kc) + m.ips;
       const double f = __ldg(&rec[ix * cs + t]) * __ldg(&rec[wyz_slot * cs + t]);
       a0 = fma(f, __ldg(&q0[t]), a0);
       a1 = fma(f, __ldg(&q1[t]), a1);
       a2 = fma(f, __ldg(&q2[t]), a2);
-      if (++t < te || v + 1 == v1) continue;
+      if (++t < te) {
+        while (t >= nb && kc < 3) { ++kc; nb = kc == 1 ? e2 : kc == 2 ? e3 : e4; }
+        continue;
+      }
+      if (v + 1 == v1) continue;
       // next nonempty row of node n, or the node is complete: flush it
       for (;;) {
         if (++r == nrow) {
@@ -388,13 +403,14 @@ __global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restr
           xh = min(ii + m.ips, m.n[0] - 1);
           r = 0;
         }
-        const long long rb = srow[wl][r];
-        tb = __ldg(&starts[rb + xl]);
-        te = __ldg(&starts[rb + xh + 1]);
+        bounds(srow[wl][r]);
         if (te > tb) break;
       }
       t = tb;
       wyz_slot = swyz[wl][r];
+      kc = 0;
+      nb = e1;
+      while (t >= nb && kc < 3) { ++kc; nb = kc == 1 ? e2 : kc == 2 ? e3 : e4; }
     }
     double* dst = (n == nA) ? pf[wl][lane] : pl[wl][lane];  // the chunk's last node
     dst[0] = a0; dst[1] = a1; dst[2] = a2;

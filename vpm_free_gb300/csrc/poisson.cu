@@ -380,6 +380,7 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict
   const int l0 = blockIdx.x * (2 * PAIRS);
   const int n = p.n;
   const size_t sy = b.dims[0], sz = (size_t)b.dims[0] * b.dims[1];
+  int nz = 0;
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, a = t - li * n;
     const int l = l0 + li;
@@ -398,10 +399,19 @@ __global__ void __launch_bounds__(kThreads) k_dst_x_fwd(const double* __restrict
       }
       v *= scale;
     }
+    nz |= v != 0.0;
     double* zp = reinterpret_cast<double*>(staging(A, B, p) + (li >> 1) * p.M + (a + 1));
     zp[li & 1] = v;
   }
-  __syncthreads();
+  if (!__syncthreads_or(nz)) {
+    // a tile of zero lines (a vorticity-free part of the box): its
+    // transform is zero, no FFT needed
+    for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
+      const int l = l0 + t / n;
+      if (l < nlines) work[(size_t)l * n + (t - (t / n) * n)] = 0.0;
+    }
+    return;
+  }
   const typename Ar::C* R = dst_pairs<Ar, ODD, PAIRS>(A, B, p);
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t / n, k = t - li * n;
@@ -423,6 +433,7 @@ __device__ __forceinline__ void y_body(double* __restrict__ work, int m0, int m1
   const int l0 = tile * (2 * PAIRS);
   const int n = p.n;  // == m1
   const size_t plane = (size_t)m0 * m1;
+  int nz = 0;
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t % (2 * PAIRS), e = t / (2 * PAIRS);
     const int l = l0 + li;
@@ -431,10 +442,13 @@ __device__ __forceinline__ void y_body(double* __restrict__ work, int m0, int m1
       const int a = l % m0, c = l / m0;
       v = work[(size_t)a + (size_t)m0 * e + plane * c];
     }
+    nz |= v != 0.0;
     double* zp = reinterpret_cast<double*>(staging(A, B, p) + (li >> 1) * p.M + (e + 1));
     zp[li & 1] = v;
   }
-  __syncthreads();
+  // zero lines (planes of the box without vorticity) transform to zero,
+  // and the pass is in place: nothing to do
+  if (!__syncthreads_or(nz)) return;
   const typename Ar::C* R = dst_pairs<Ar, ODD, PAIRS>(A, B, p);
   for (int t = threadIdx.x; t < 2 * PAIRS * n; t += blockDim.x) {
     const int li = t % (2 * PAIRS), k = t / (2 * PAIRS);
