@@ -406,8 +406,9 @@ def run_dirichlet(args, local):
     return 0
 
 
-KERNELS = (  # vpmg_bench_kernel ids: (id, name, launches per step)
-    (0, "k_apply_dense+k_apply_csr (boundary operator, fine block)", 1),
+KERNELS = (  # vpmg_bench_kernel ids: (id, name, launches per step); the first word keys profiles/traffic.json
+    (0, "boundary (the fine block's operator: coarsest level by FFT k_ff_* or the dense block k_apply_dense, "
+        "finer levels and corrections k_apply_csr)", 1),
     (1, "inner-box Dirichlet solve (k_dst_x_fwd, k_dst_y x2, k_thomas, k_dst_x_inv)", 3),
     (6, "padded-block zero-BC solve where read (k_dst_x_fwd, k_dst_y, k_thomas_faces, k_partial_x/y, "
         "partial inverses)", 3),

@@ -1322,8 +1322,12 @@ int vpmg_bench_kernel(vpmg_handle* h, int which, int reps, double* ms, double* f
           velocity_and_stretching(s.nn, s.dpm, S, R, const_cast<double* const*>(Vr), G, st, 2, ff ? vf : nullptr,
                                   ff ? gf : nullptr);
         };
-        fl = 42.0 * (double)N;  // 3 components x 3 directions x 4 flops + 2 sums
-        by = 72.0 * (double)N;  // RHS and u read, stretching written
+        // 3 components x 3 directions x 4 flops + 2 sums where vorticity
+        // surrounds the node (elsewhere the FP64 kernel writes zeros): RHS
+        // read and stretching written everywhere, u read where computed
+        const double act = ff ? (double)N : (double)count_vortical_nodes(s.nn, R, st);
+        fl = 42.0 * act;
+        by = 48.0 * (double)N + 24.0 * act;
       }
     } else if (which == 5) {
       // back_to_particles_3D(1) on the binned particles (UP/GP rewritten in place)

@@ -17,6 +17,7 @@
 // axis, then a full inverse DST along the other.  The values produced are
 // those of the full discrete solves (same linear algebra, different
 // rounding).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -39,63 +40,99 @@ __device__ __forceinline__ float2 shfl_xor(float2 v, int m) {
 // as it is staged, and each result is joined back into a double.
 
 // out[i + nsel*(q + m1*kk)] = sum_p S[i][p] * W[p + m0*(q + m1*k)],  k = klist ? klist[kk] : kk
+// Persistent CTAs walk tiles of kLines lines.  In FP64 the next tile is
+// staged with asynchronous copies (cp.async, 8 bytes each) while the
+// current one is reduced, so the loads' latency hides behind the FMAs; the
+// sine rows are staged once per CTA.
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 template <class A>
-__global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W, int m0, int m1, int nk,
-                                                   const int* __restrict__ klist, const typename A::R* __restrict__ S,
-                                                   int nsel, double* __restrict__ out) {
-  using R = typename A::R;
-  extern __shared__ double smx[];
-  R* tile = reinterpret_cast<R*>(smx);       // kLines x m0
-  R* Ss = tile + (size_t)kLines * m0;         // nsel x m0
-  const int nlines = m1 * nk;
-  const int l0 = blockIdx.x * kLines;
-  for (int t = threadIdx.x; t < nsel * m0; t += blockDim.x) Ss[t] = S[t];
-  for (int t = threadIdx.x; t < kLines * m0; t += blockDim.x) {
+__device__ __forceinline__ void stage_x_tile(typename A::R* tile, const double* __restrict__ W, int m0, int m1,
+                                             int nlines, const int* __restrict__ klist, int l0, int lines) {
+  for (int t = threadIdx.x; t < lines * m0; t += blockDim.x) {
     const int li = t / m0, p = t - li * m0;
     const int l = l0 + li;
-    R v = A::zero();
     if (l < nlines) {
       const int q = l % m1, kk = l / m1;
       const int k = klist ? klist[kk] : kk;
-      v = A::from(W[(size_t)p + (size_t)m0 * (q + (size_t)m1 * k)]);
+      const double* src = W + (size_t)p + (size_t)m0 * (q + (size_t)m1 * k);
+      if constexpr (A::kFF) tile[t] = A::from(*src);
+      else cp_async8(&tile[t], src);
+    } else {
+      tile[t] = A::zero();
     }
-    tile[t] = v;
   }
-  __syncthreads();
+  if constexpr (!A::kFF) cp_async_commit();
+}
+
+template <class A>
+__global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W, int m0, int m1, int nk,
+                                                   const int* __restrict__ klist, const typename A::R* __restrict__ S,
+                                                   int nsel, double* __restrict__ out, int lines) {
+  using R = typename A::R;
+  extern __shared__ double smx[];
+  R* Ss = reinterpret_cast<R*>(smx);               // nsel x m0
+  R* const buf0 = Ss + (size_t)nsel * m0;           // two tiles of `lines` x m0 (lines <= kLines)
+  R* const buf1 = buf0 + (size_t)lines * m0;
+  const int nlines = m1 * nk;
+  const int ntiles = (nlines + lines - 1) / lines;
+  for (int t = threadIdx.x; t < nsel * m0; t += blockDim.x) Ss[t] = S[t];
+  int cur = 0;
+  if ((int)blockIdx.x < ntiles) stage_x_tile<A>(buf0, W, m0, m1, nlines, klist, blockIdx.x * lines, lines);
   // R adjacent threads share one dot product (R = 128 / outputs, a power of
   // two up to 8, when the CTA has fewer outputs than threads), each summing
   // every R-th term; their partials meet in a fixed shuffle tree.
-  const int nout = kLines * nsel;
+  const int nout = lines * nsel;
   int Rs = 1;
   while (Rs < 8 && nout * Rs * 2 <= (int)blockDim.x) Rs *= 2;
   const int r = threadIdx.x % Rs;
-  for (int o0 = 0; o0 < nout; o0 += blockDim.x / Rs) {
-    const int o = o0 + threadIdx.x / Rs;
-    const int li = o % kLines, i = o / kLines;
-    const int l = l0 + li;
-    const bool ok = o < nout && l < nlines;
-    R a0 = A::zero(), a1 = a0, a2 = a0, a3 = a0;
-    if (ok) {
-      const R* a = tile + (size_t)li * m0;
-      const R* b = Ss + (size_t)i * m0;
-      int p = r;
-      for (; p + 3 * Rs < m0; p += 4 * Rs) {
-        a0 = A::fma(a[p], b[p], a0);
-        a1 = A::fma(a[p + Rs], b[p + Rs], a1);
-        a2 = A::fma(a[p + 2 * Rs], b[p + 2 * Rs], a2);
-        a3 = A::fma(a[p + 3 * Rs], b[p + 3 * Rs], a3);
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int next = tile + gridDim.x;
+    if (next < ntiles) {
+      stage_x_tile<A>(cur ? buf0 : buf1, W, m0, m1, nlines, klist, next * lines, lines);
+      if constexpr (!A::kFF) cp_async_wait<1>();  // the current tile's copies are done
+    } else {
+      if constexpr (!A::kFF) cp_async_wait<0>();
+    }
+    __syncthreads();
+    const R* tl = cur ? buf1 : buf0;
+    const int l0 = tile * lines;
+    for (int o0 = 0; o0 < nout; o0 += blockDim.x / Rs) {
+      const int o = o0 + threadIdx.x / Rs;
+      const int li = o % lines, i = o / lines;
+      const int l = l0 + li;
+      const bool ok = o < nout && l < nlines;
+      R a0 = A::zero(), a1 = a0, a2 = a0, a3 = a0;
+      if (ok) {
+        const R* a = tl + (size_t)li * m0;
+        const R* b = Ss + (size_t)i * m0;
+        int p = r;
+        for (; p + 3 * Rs < m0; p += 4 * Rs) {
+          a0 = A::fma(a[p], b[p], a0);
+          a1 = A::fma(a[p + Rs], b[p + Rs], a1);
+          a2 = A::fma(a[p + 2 * Rs], b[p + 2 * Rs], a2);
+          a3 = A::fma(a[p + 3 * Rs], b[p + 3 * Rs], a3);
+        }
+        for (; p < m0; p += Rs) a0 = A::fma(a[p], b[p], a0);
       }
-      for (; p < m0; p += Rs) a0 = A::fma(a[p], b[p], a0);
+      R v = A::add(A::add(a0, a1), A::add(a2, a3));
+      for (int m = 1; m < Rs; m <<= 1) {
+        const R w = shfl_xor(v, m);
+        v = (r & m) ? A::add(w, v) : A::add(v, w);
+      }
+      if (ok && r == 0) {
+        const int q = l % m1, kk = l / m1;
+        out[i + (size_t)nsel * (q + (size_t)m1 * kk)] = A::to(v);
+      }
     }
-    R v = A::add(A::add(a0, a1), A::add(a2, a3));
-    for (int m = 1; m < Rs; m <<= 1) {
-      const R w = shfl_xor(v, m);
-      v = (r & m) ? A::add(w, v) : A::add(v, w);
-    }
-    if (ok && r == 0) {
-      const int q = l % m1, kk = l / m1;
-      out[i + (size_t)nsel * (q + (size_t)m1 * kk)] = A::to(v);
-    }
+    __syncthreads();  // the buffer is refilled two tiles on
+    cur ^= 1;
   }
 }
 
@@ -107,23 +144,39 @@ constexpr int kColTile = 32;
 // A second row set (S2, nsel2 -> out2, same layout) is served from the
 // same staged tile when given, so two face sets cost one pass over W.
 template <class A>
-__global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W, int m0, int m1, int nk,
-                                                   const int* __restrict__ klist, const typename A::R* __restrict__ S,
-                                                   int nsel, double* __restrict__ out,
-                                                   const typename A::R* __restrict__ S2, int nsel2,
-                                                   double* __restrict__ out2) {
-  using R = typename A::R;
-  extern __shared__ double smy[];
-  R* tile = reinterpret_cast<R*>(smy);  // [q][lane], m1 x kColTile; then the partial sums [row][lane]
-  const int p0 = blockIdx.x * kColTile;
-  const int kk = blockIdx.y;
+__device__ __forceinline__ void stage_y_tile(typename A::R* tile, const double* __restrict__ W, int m0, int m1,
+                                             const int* __restrict__ klist, int p0, int kk) {
   const int k = klist ? klist[kk] : kk;
   const double* plane = W + (size_t)m0 * m1 * k;
   const int lane = threadIdx.x % kColTile, row = threadIdx.x / kColTile, rows = blockDim.x / kColTile;
   const int p = p0 + lane;
-  for (int q = row; q < m1; q += rows)
-    tile[q * kColTile + lane] = (p < m0) ? A::from(plane[(size_t)m0 * q + p]) : A::zero();
-  __syncthreads();
+  for (int q = row; q < m1; q += rows) {
+    if (p < m0) {
+      if constexpr (A::kFF) tile[q * kColTile + lane] = A::from(plane[(size_t)m0 * q + p]);
+      else cp_async8(&tile[q * kColTile + lane], plane + (size_t)m0 * q + p);
+    } else {
+      tile[q * kColTile + lane] = A::zero();
+    }
+  }
+  if constexpr (!A::kFF) cp_async_commit();
+}
+
+// Persistent CTAs walk (column tile, plane) pairs; with dbl the next pair's
+// tile is staged asynchronously while the current one is reduced (FP64).
+template <class A>
+__global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W, int m0, int m1, int nk,
+                                                   const int* __restrict__ klist, const typename A::R* __restrict__ S,
+                                                   int nsel, double* __restrict__ out,
+                                                   const typename A::R* __restrict__ S2, int nsel2,
+                                                   double* __restrict__ out2, int dbl) {
+  using R = typename A::R;
+  extern __shared__ double smy[];
+  R* const buf0 = reinterpret_cast<R*>(smy);              // [q][lane], m1 x kColTile
+  R* const buf1 = buf0 + (size_t)m1 * kColTile;             // the second tile (dbl)
+  R* const partial = (dbl ? buf1 : buf0) + (size_t)m1 * kColTile;  // partial sums [row][lane]
+  const int nbx = (m0 + kColTile - 1) / kColTile;
+  const int ntiles = nbx * nk;
+  const int lane = threadIdx.x % kColTile, row = threadIdx.x / kColTile, rows = blockDim.x / kColTile;
   // R rows share one output row set when there are fewer outputs than rows
   // (R a power of two), each summing every R-th q; the partials are added
   // in row order through shared memory.
@@ -131,37 +184,59 @@ __global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W,
   int Rs = 1;
   while (Rs < rows && nout * Rs * 2 <= rows) Rs *= 2;
   const int r = row % Rs;
-  R* partial = tile + (size_t)m1 * kColTile;
-  for (int j0 = 0; j0 < nout; j0 += rows / Rs) {
-    const int jj = j0 + row / Rs;
-    R a0 = A::zero(), a1 = a0, a2 = a0, a3 = a0;
-    if (jj < nout && p < m0) {
-      const bool second = jj >= nsel;
-      const int j = second ? jj - nsel : jj;
-      const R* Sj = (second ? S2 : S) + (size_t)j * m1;
-      int q = r;
-      for (; q + 3 * Rs < m1; q += 4 * Rs) {
-        a0 = A::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
-        a1 = A::fma(__ldg(&Sj[q + Rs]), tile[(q + Rs) * kColTile + lane], a1);
-        a2 = A::fma(__ldg(&Sj[q + 2 * Rs]), tile[(q + 2 * Rs) * kColTile + lane], a2);
-        a3 = A::fma(__ldg(&Sj[q + 3 * Rs]), tile[(q + 3 * Rs) * kColTile + lane], a3);
+  int cur = 0;
+  if (dbl && (int)blockIdx.x < ntiles)
+    stage_y_tile<A>(buf0, W, m0, m1, klist, ((int)blockIdx.x % nbx) * kColTile, (int)blockIdx.x / nbx);
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int p0 = (tile % nbx) * kColTile, kk = tile / nbx;
+    const int next = tile + gridDim.x;
+    if (dbl) {
+      if (next < ntiles) {
+        stage_y_tile<A>(cur ? buf0 : buf1, W, m0, m1, klist, (next % nbx) * kColTile, next / nbx);
+        if constexpr (!A::kFF) cp_async_wait<1>();
+      } else {
+        if constexpr (!A::kFF) cp_async_wait<0>();
       }
-      for (; q < m1; q += Rs) a0 = A::fma(__ldg(&Sj[q]), tile[q * kColTile + lane], a0);
+    } else {
+      stage_y_tile<A>(buf0, W, m0, m1, klist, p0, kk);
+      if constexpr (!A::kFF) cp_async_wait<0>();
     }
-    R v = A::add(A::add(a0, a1), A::add(a2, a3));
-    if (Rs > 1) {
-      partial[row * kColTile + lane] = v;
-      __syncthreads();
-      if (r == 0)
-        for (int m = 1; m < Rs; ++m) v = A::add(v, partial[(row + m) * kColTile + lane]);
-      __syncthreads();
+    __syncthreads();
+    const R* tl = cur ? buf1 : buf0;
+    const int p = p0 + lane;
+    for (int j0 = 0; j0 < nout; j0 += rows / Rs) {
+      const int jj = j0 + row / Rs;
+      R a0 = A::zero(), a1 = a0, a2 = a0, a3 = a0;
+      if (jj < nout && p < m0) {
+        const bool second = jj >= nsel;
+        const int j = second ? jj - nsel : jj;
+        const R* Sj = (second ? S2 : S) + (size_t)j * m1;
+        int q = r;
+        for (; q + 3 * Rs < m1; q += 4 * Rs) {
+          a0 = A::fma(__ldg(&Sj[q]), tl[q * kColTile + lane], a0);
+          a1 = A::fma(__ldg(&Sj[q + Rs]), tl[(q + Rs) * kColTile + lane], a1);
+          a2 = A::fma(__ldg(&Sj[q + 2 * Rs]), tl[(q + 2 * Rs) * kColTile + lane], a2);
+          a3 = A::fma(__ldg(&Sj[q + 3 * Rs]), tl[(q + 3 * Rs) * kColTile + lane], a3);
+        }
+        for (; q < m1; q += Rs) a0 = A::fma(__ldg(&Sj[q]), tl[q * kColTile + lane], a0);
+      }
+      R v = A::add(A::add(a0, a1), A::add(a2, a3));
+      if (Rs > 1) {
+        partial[row * kColTile + lane] = v;
+        __syncthreads();
+        if (r == 0)
+          for (int m = 1; m < Rs; ++m) v = A::add(v, partial[(row + m) * kColTile + lane]);
+        __syncthreads();
+      }
+      if (r == 0 && jj < nout && p < m0) {
+        const bool second = jj >= nsel;
+        const int j = second ? jj - nsel : jj;
+        if (second) out2[(size_t)p + (size_t)m0 * (j + (size_t)nsel2 * kk)] = A::to(v);
+        else out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = A::to(v);
+      }
     }
-    if (r == 0 && jj < nout && p < m0) {
-      const bool second = jj >= nsel;
-      const int j = second ? jj - nsel : jj;
-      if (second) out2[(size_t)p + (size_t)m0 * (j + (size_t)nsel2 * kk)] = A::to(v);
-      else out[(size_t)p + (size_t)m0 * (j + (size_t)nsel * kk)] = A::to(v);
-    }
+    __syncthreads();  // the tile's buffer is refilled next
+    if (dbl) cur ^= 1;
   }
 }
 
@@ -265,10 +340,10 @@ __global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict_
     }
     return r;
   };
-  // loads eight planes ahead of the dependent chain (one thread per line
+  // loads twelve planes ahead of the dependent chain (one thread per line
   // leaves few warps per SM: the loads in flight set the speed); same
   // arithmetic order
-  constexpr int U = 8;
+  constexpr int U = 12;
   double y = rhs(0);
   out[pq] = y;
   double ri = rinv(pq);
@@ -351,33 +426,52 @@ size_t g_partial_smem = 0;  // dynamic shared memory granted to k_partial_x so f
 
 // Raises k_partial_x's shared-memory limit (called at set-up, outside any
 // stream capture).  Both arithmetics stage 8 bytes per value.
+// Tile height of k_partial_x: the most lines (up to kLines) whose two
+// staged tiles and the sine rows fit in a CTA's shared memory.
+int partial_x_lines(int m0, int nsel) {
+  int lines = kLines;
+  while (lines > 1 && sizeof(double) * (2 * (size_t)lines * m0 + (size_t)nsel * m0) > 227 * 1024) lines /= 2;
+  return lines;
+}
+
 void partial_x_reserve(int m0, int nsel) {
-  const size_t sm = sizeof(double) * ((size_t)kLines * m0 + (size_t)nsel * m0);
+  const size_t sm = sizeof(double) * (2 * (size_t)partial_x_lines(m0, nsel) * m0 + (size_t)nsel * m0);
   VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
-  if (sm > g_partial_smem) {
-    VPMG_CUDA(cudaFuncSetAttribute(k_partial_x<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    VPMG_CUDA(cudaFuncSetAttribute(k_partial_x<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    g_partial_smem = sm;
+  // the whole per-CTA maximum: every call's tile height keeps it within
+  const size_t cap = 227 * 1024;
+  if (cap > g_partial_smem) {
+    VPMG_CUDA(cudaFuncSetAttribute(k_partial_x<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+    VPMG_CUDA(cudaFuncSetAttribute(k_partial_x<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+    g_partial_smem = cap;
   }
 }
 
 void partial_x(int arith, const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel,
                double* out, cudaStream_t s) {
   const int nlines = m1 * nk;
-  const size_t sm = sizeof(double) * ((size_t)kLines * m0 + (size_t)nsel * m0);
+  const int lines = partial_x_lines(m0, nsel);
+  const size_t sm = sizeof(double) * (2 * (size_t)lines * m0 + (size_t)nsel * m0);
   VPMG_CHECK(sm <= g_partial_smem, VPMG_ERR_STATE, "k_partial_x shared memory not reserved");
-  const unsigned g = (nlines + kLines - 1) / kLines;
+  // persistent CTAs: as many as fit on the SMs at this shared-memory size
+  const unsigned ntiles = (nlines + lines - 1) / lines;
+  const unsigned per_sm = (unsigned)std::max<size_t>(1, std::min<size_t>(8, (227 * 1024) / (sm + 1024)));
+  const unsigned g = std::min(ntiles, 152u * per_sm);
   if (arith == VPMG_ARITH_FF48)
-    k_partial_x<FF><<<g, 128, sm, s>>>(W, m0, m1, nk, klist, reinterpret_cast<const float2*>(S), nsel, out);
+    k_partial_x<FF><<<g, 128, sm, s>>>(W, m0, m1, nk, klist, reinterpret_cast<const float2*>(S), nsel, out, lines);
   else
-    k_partial_x<F64><<<g, 128, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out);
+    k_partial_x<F64><<<g, 128, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out, lines);
   VPMG_LAUNCHED();
 }
 
 size_t g_partial_y_smem = 0;  // dynamic shared memory granted to k_partial_y so far
 
+// k_partial_y's shared memory: one or two column tiles and the partial sums
+// of 8 rows; two tiles (double buffering) when they fit.
+size_t partial_y_smem(int m1, bool dbl) { return sizeof(double) * ((dbl ? 2 : 1) * (size_t)m1 + 8) * kColTile; }
+bool partial_y_dbl(int m1) { return partial_y_smem(m1, true) <= 227 * 1024; }
+
 void partial_y_reserve(int m1) {
-  const size_t sm = sizeof(double) * ((size_t)m1 + 8) * kColTile;
+  const size_t sm = partial_y_smem(m1, partial_y_dbl(m1));
   VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
   if (sm > g_partial_y_smem) {
     VPMG_CUDA(cudaFuncSetAttribute(k_partial_y<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -388,14 +482,18 @@ void partial_y_reserve(int m1) {
 
 void partial_y(int arith, const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel,
                double* out, cudaStream_t s, const double* S2 = nullptr, int nsel2 = 0, double* out2 = nullptr) {
-  const size_t sm = sizeof(double) * ((size_t)m1 + 8) * kColTile;  // tile + partial sums of 8 rows
+  const int dbl = partial_y_dbl(m1) ? 1 : 0;
+  const size_t sm = partial_y_smem(m1, dbl);  // tiles + partial sums of 8 rows
   VPMG_CHECK(sm <= g_partial_y_smem, VPMG_ERR_STATE, "k_partial_y shared memory not reserved");
-  dim3 g((m0 + kColTile - 1) / kColTile, nk);
+  // persistent CTAs: as many as fit on the SMs at this shared-memory size
+  const unsigned ntiles = (unsigned)(((m0 + kColTile - 1) / kColTile) * nk);
+  const unsigned per_sm = (unsigned)std::max<size_t>(1, std::min<size_t>(8, (227 * 1024) / (sm + 1024)));
+  const unsigned g = std::min(ntiles, 152u * per_sm);
   if (arith == VPMG_ARITH_FF48)
     k_partial_y<FF><<<g, 256, sm, s>>>(W, m0, m1, nk, klist, reinterpret_cast<const float2*>(S), nsel, out,
-                                      reinterpret_cast<const float2*>(S2), nsel2, out2);
+                                      reinterpret_cast<const float2*>(S2), nsel2, out2, dbl);
   else
-    k_partial_y<F64><<<g, 256, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out, S2, nsel2, out2);
+    k_partial_y<F64><<<g, 256, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out, S2, nsel2, out2, dbl);
   VPMG_LAUNCHED();
 }
 

@@ -121,6 +121,15 @@ __global__ void k_deformation(const double* __restrict__ r0, const double* __res
   const double* U[3] = {u0, u1, u2};
   double* G[3] = {g0, g1, g2};
   float2* F[3] = {f0, f1, f2};
+  if (rxp == 0.0 && rxm == 0.0 && ryp == 0.0 && rym == 0.0 && rzp == 0.0 && rzm == 0.0) {
+    // no vorticity around the node (most of the mesh): the stretching is zero
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      G[m][id] = 0.0;
+      if (f0) F[m][id] = make_float2(0.0f, 0.0f);
+    }
+    return;
+  }
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
     // -sum_j (R_j u_m (+) - R_j u_m (-)) / (2 h_j): each difference one
@@ -283,6 +292,39 @@ void viscous_diffusion(const int dims[3], const int nn_bl[6], const double h[3],
       1.0 / (h[1] * h[1]), 1.0 / (h[2] * h[2]), ni, sol[0], sol[1], sol[2]);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
+}
+
+// Nodes where the FP64 stretching stencil has work: an interior node
+// (2..N-3) with a non-zero RHS among its six neighbours (instrumentation).
+__global__ void k_count_vortical(const double* __restrict__ r0, const double* __restrict__ r1,
+                                 const double* __restrict__ r2, int NX, int NY, int NZ,
+                                 unsigned long long* __restrict__ count) {
+  const int ex = NX - 4, ey = NY - 4, ez = NZ - 4;
+  const size_t n = (size_t)ex * ey * ez;
+  const size_t sy = NX, sz = (size_t)NX * NY;
+  unsigned long long c = 0;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(t % ex), j = 2 + (int)((t / ex) % ey), k = 2 + (int)(t / ((size_t)ex * ey));
+    const size_t id = i + sy * j + sz * k;
+    if (r0[id + 1] != 0.0 || r0[id - 1] != 0.0 || r1[id + sy] != 0.0 || r1[id - sy] != 0.0 || r2[id + sz] != 0.0 ||
+        r2[id - sz] != 0.0)
+      ++c;
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+long long count_vortical_nodes(const int dims[3], const double* const rhs[3], cudaStream_t s) {
+  if (dims[0] <= 4 || dims[1] <= 4 || dims[2] <= 4) return 0;
+  DBuf<unsigned long long> d;
+  d.ensure(1);
+  VPMG_CUDA(cudaMemsetAsync(d.p, 0, sizeof(unsigned long long), s));
+  k_count_vortical<<<152 * 8, 256, 0, s>>>(rhs[0], rhs[1], rhs[2], dims[0], dims[1], dims[2], d.p);
+  VPMG_LAUNCHED();
+  unsigned long long c = 0;
+  VPMG_CUDA(cudaMemcpyAsync(&c, d.p, sizeof(c), cudaMemcpyDeviceToHost, s));
+  VPMG_CUDA(cudaStreamSynchronize(s));
+  return (long long)c;
 }
 
 void velocity_and_stretching(const int dims[3], const double h[3], const double* const psi[3], const double* const rhs[3],

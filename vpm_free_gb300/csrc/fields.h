@@ -30,5 +30,8 @@ void viscous_diffusion(const int dims[3], const int nn_bl[6], const double h[3],
 void velocity_and_stretching(const int dims[3], const double h[3], const double* const psi[3], const double* const rhs[3],
                              double* const vel[3], double* const def[3], cudaStream_t s, int parts = 3,
                              float2* const vel_ff[3] = nullptr, float2* const def_ff[3] = nullptr);
+// Interior nodes (2..N-3) with a non-zero RHS among the stretching stencil's
+// six neighbours: where the FP64 stretching kernel computes (instrumentation).
+long long count_vortical_nodes(const int dims[3], const double* const rhs[3], cudaStream_t s);
 
 }  // namespace vpmg

@@ -380,17 +380,39 @@ __global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restr
     int kc = 0, nb = e1;  // the slot's cell offset from xl and the next cell's first slot
     while (t >= nb && kc < 3) { ++kc; nb = kc == 1 ? e2 : kc == 2 ? e3 : e4; }
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    for (int v = v0; v < v1; ++v) {
+    for (int v = v0; v < v1;) {
       const int ix = ii - (xl + kc) + m.ips;
-      const double f = __ldg(&rec[ix * cs + t]) * __ldg(&rec[wyz_slot * cs + t]);
-      a0 = fma(f, __ldg(&q0[t]), a0);
-      a1 = fma(f, __ldg(&q1[t]), a1);
-      a2 = fma(f, __ldg(&q2[t]), a2);
-      if (++t < te) {
+      if (v + 1 < v1 && t + 1 < te) {
+        // two visits of this row at once, their loads in flight together;
+        // the sums take them in the same order as one by one
+        int kc2 = kc, nb2 = nb;
+        while (t + 1 >= nb2 && kc2 < 3) { ++kc2; nb2 = kc2 == 1 ? e2 : kc2 == 2 ? e3 : e4; }
+        const int ix2 = ii - (xl + kc2) + m.ips;
+        const double wa = __ldg(&rec[ix * cs + t]), wb = __ldg(&rec[ix2 * cs + t + 1]);
+        const double ya = __ldg(&rec[wyz_slot * cs + t]), yb = __ldg(&rec[wyz_slot * cs + t + 1]);
+        const double qa0 = __ldg(&q0[t]), qa1 = __ldg(&q1[t]), qa2 = __ldg(&q2[t]);
+        const double qb0 = __ldg(&q0[t + 1]), qb1 = __ldg(&q1[t + 1]), qb2 = __ldg(&q2[t + 1]);
+        const double fa = wa * ya, fb = wb * yb;
+        a0 = fma(fb, qb0, fma(fa, qa0, a0));
+        a1 = fma(fb, qb1, fma(fa, qa1, a1));
+        a2 = fma(fb, qb2, fma(fa, qa2, a2));
+        t += 2;
+        v += 2;
+        kc = kc2;
+        nb = nb2;
+      } else {
+        const double f = __ldg(&rec[ix * cs + t]) * __ldg(&rec[wyz_slot * cs + t]);
+        a0 = fma(f, __ldg(&q0[t]), a0);
+        a1 = fma(f, __ldg(&q1[t]), a1);
+        a2 = fma(f, __ldg(&q2[t]), a2);
+        ++t;
+        ++v;
+      }
+      if (t < te) {
         while (t >= nb && kc < 3) { ++kc; nb = kc == 1 ? e2 : kc == 2 ? e3 : e4; }
         continue;
       }
-      if (v + 1 == v1) continue;
+      if (v == v1) continue;
       // next nonempty row of node n, or the node is complete: flush it
       for (;;) {
         if (++r == nrow) {
