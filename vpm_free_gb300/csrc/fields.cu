@@ -80,11 +80,9 @@ __global__ void k_velocity(const double* __restrict__ p0, const double* __restri
                            int NX, int NY, int NZ, double i2x, double i2y, double i2z, double* __restrict__ u0,
                            double* __restrict__ u1, double* __restrict__ u2, float2* __restrict__ f0,
                            float2* __restrict__ f1, float2* __restrict__ f2) {
-  const int ex = NX - 2, ey = NY - 2, ez = NZ - 2;
-  const size_t n = (size_t)ex * ey * ez;
-  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = 1 + (int)(t % ex), j = 1 + (int)((t / ex) % ey), k = 1 + (int)(t / ((size_t)ex * ey));
+  // grid: (x blocks, y, z) over the interior, no index divisions
+  const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y, k = 1 + blockIdx.z;
+  if (i > NX - 2) return;
   const size_t sy = NX, sz = (size_t)NX * NY;
   const size_t id = i + sy * j + sz * k;
   // central differences; each component's two scalings by 1/(2h) fused
@@ -109,11 +107,9 @@ __global__ void k_deformation(const double* __restrict__ r0, const double* __res
                               const double* __restrict__ u2, int NX, int NY, int NZ, double i2x, double i2y, double i2z,
                               double* __restrict__ g0, double* __restrict__ g1, double* __restrict__ g2,
                               float2* __restrict__ f0, float2* __restrict__ f1, float2* __restrict__ f2) {
-  const int ex = NX - 4, ey = NY - 4, ez = NZ - 4;
-  const size_t n = (size_t)ex * ey * ez;
-  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = 2 + (int)(t % ex), j = 2 + (int)((t / ex) % ey), k = 2 + (int)(t / ((size_t)ex * ey));
+  // grid: (x blocks, y, z) over nodes 2..N-3, no index divisions
+  const int i = 2 + blockIdx.x * blockDim.x + threadIdx.x, j = 2 + blockIdx.y, k = 2 + blockIdx.z;
+  if (i > NX - 3) return;
   const size_t sy = NX, sz = (size_t)NX * NY;
   const size_t id = i + sy * j + sz * k;
   const double rxp = r0[id + 1], rxm = r0[id - 1], ryp = r1[id + sy], rym = r1[id - sy], rzp = r2[id + sz],
@@ -333,8 +329,8 @@ void velocity_and_stretching(const int dims[3], const double h[3], const double*
   const int NX = dims[0], NY = dims[1], NZ = dims[2];
   const double i2x = 1.0 / (2 * h[0]), i2y = 1.0 / (2 * h[1]), i2z = 1.0 / (2 * h[2]);
   if ((parts & 1) && NX > 2 && NY > 2 && NZ > 2) {
-    const size_t n = (size_t)(NX - 2) * (NY - 2) * (NZ - 2);
-    k_velocity<<<grid_for(n, 256), 256, 0, s>>>(psi[0], psi[1], psi[2], NX, NY, NZ, i2x, i2y, i2z, vel[0], vel[1], vel[2],
+    const dim3 g((unsigned)((NX - 2 + 127) / 128), (unsigned)(NY - 2), (unsigned)(NZ - 2));
+    k_velocity<<<g, 128, 0, s>>>(psi[0], psi[1], psi[2], NX, NY, NZ, i2x, i2y, i2z, vel[0], vel[1], vel[2],
                                                 vel_ff ? vel_ff[0] : nullptr, vel_ff ? vel_ff[1] : nullptr,
                                                 vel_ff ? vel_ff[2] : nullptr);
     VPMG_LAUNCHED();
@@ -346,9 +342,9 @@ void velocity_and_stretching(const int dims[3], const double h[3], const double*
                                                         NZ, i2x, i2y, i2z, def[0], def[1], def[2], def_ff[0],
                                                         def_ff[1], def_ff[2]);
     else
-      k_deformation<<<grid_for(n, 256), 256, 0, s>>>(rhs[0], rhs[1], rhs[2], vel[0], vel[1], vel[2], NX, NY, NZ, i2x,
-                                                     i2y, i2z, def[0], def[1], def[2], def_ff ? def_ff[0] : nullptr,
-                                                     def_ff ? def_ff[1] : nullptr, def_ff ? def_ff[2] : nullptr);
+      k_deformation<<<dim3((unsigned)((NX - 4 + 127) / 128), (unsigned)(NY - 4), (unsigned)(NZ - 4)), 128, 0, s>>>(
+          rhs[0], rhs[1], rhs[2], vel[0], vel[1], vel[2], NX, NY, NZ, i2x, i2y, i2z, def[0], def[1], def[2],
+          def_ff ? def_ff[0] : nullptr, def_ff ? def_ff[1] : nullptr, def_ff ? def_ff[2] : nullptr);
     VPMG_LAUNCHED();
   }
   VPMG_CUDA(cudaGetLastError());
