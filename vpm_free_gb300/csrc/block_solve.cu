@@ -40,10 +40,12 @@ __device__ __forceinline__ float2 shfl_xor(float2 v, int m) {
 // as it is staged, and each result is joined back into a double.
 
 // out[i + nsel*(q + m1*kk)] = sum_p S[i][p] * W[p + m0*(q + m1*k)],  k = klist ? klist[kk] : kk
-// Persistent CTAs walk tiles of kLines lines.  In FP64 the next tile is
-// staged with asynchronous copies (cp.async, 8 bytes each) while the
-// current one is reduced, so the loads' latency hides behind the FMAs; the
-// sine rows are staged once per CTA.
+// Persistent CTAs walk tiles of up to kLines lines; the sine rows are
+// staged once per CTA.  In FP64 (dbl) the next tile is staged with
+// asynchronous copies (cp.async, 8 bytes each) while the current one is
+// reduced, so the loads' latency hides behind the FMAs.  Float-float
+// staging converts each value as it lands, which cannot run ahead: one
+// buffer, and the smaller footprint keeps more CTAs on an SM instead.
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
@@ -74,17 +76,18 @@ __device__ __forceinline__ void stage_x_tile(typename A::R* tile, const double* 
 template <class A>
 __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W, int m0, int m1, int nk,
                                                    const int* __restrict__ klist, const typename A::R* __restrict__ S,
-                                                   int nsel, double* __restrict__ out, int lines) {
+                                                   int nsel, double* __restrict__ out, int lines, int dbl) {
   using R = typename A::R;
   extern __shared__ double smx[];
   R* Ss = reinterpret_cast<R*>(smx);               // nsel x m0
-  R* const buf0 = Ss + (size_t)nsel * m0;           // two tiles of `lines` x m0 (lines <= kLines)
+  R* const buf0 = Ss + (size_t)nsel * m0;           // one or two (dbl) tiles of `lines` x m0 (lines <= kLines)
   R* const buf1 = buf0 + (size_t)lines * m0;
   const int nlines = m1 * nk;
   const int ntiles = (nlines + lines - 1) / lines;
   for (int t = threadIdx.x; t < nsel * m0; t += blockDim.x) Ss[t] = S[t];
   int cur = 0;
-  if ((int)blockIdx.x < ntiles) stage_x_tile<A>(buf0, W, m0, m1, nlines, klist, blockIdx.x * lines, lines);
+  if (dbl && (int)blockIdx.x < ntiles)
+    stage_x_tile<A>(buf0, W, m0, m1, nlines, klist, blockIdx.x * lines, lines);
   // R adjacent threads share one dot product (R = 128 / outputs, a power of
   // two up to 8, when the CTA has fewer outputs than threads), each summing
   // every R-th term; their partials meet in a fixed shuffle tree.
@@ -94,10 +97,15 @@ __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W,
   const int r = threadIdx.x % Rs;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int next = tile + gridDim.x;
-    if (next < ntiles) {
-      stage_x_tile<A>(cur ? buf0 : buf1, W, m0, m1, nlines, klist, next * lines, lines);
-      if constexpr (!A::kFF) cp_async_wait<1>();  // the current tile's copies are done
+    if (dbl) {
+      if (next < ntiles) {
+        stage_x_tile<A>(cur ? buf0 : buf1, W, m0, m1, nlines, klist, next * lines, lines);
+        if constexpr (!A::kFF) cp_async_wait<1>();  // the current tile's copies are done
+      } else {
+        if constexpr (!A::kFF) cp_async_wait<0>();
+      }
     } else {
+      stage_x_tile<A>(buf0, W, m0, m1, nlines, klist, tile * lines, lines);
       if constexpr (!A::kFF) cp_async_wait<0>();
     }
     __syncthreads();
@@ -131,8 +139,8 @@ __global__ void __launch_bounds__(128) k_partial_x(const double* __restrict__ W,
         out[i + (size_t)nsel * (q + (size_t)m1 * kk)] = A::to(v);
       }
     }
-    __syncthreads();  // the buffer is refilled two tiles on
-    cur ^= 1;
+    __syncthreads();  // the buffer is refilled next (one buffer) or two tiles on (dbl)
+    if (dbl) cur ^= 1;
   }
 }
 
@@ -161,8 +169,9 @@ __device__ __forceinline__ void stage_y_tile(typename A::R* tile, const double* 
   if constexpr (!A::kFF) cp_async_commit();
 }
 
-// Persistent CTAs walk (column tile, plane) pairs; with dbl the next pair's
-// tile is staged asynchronously while the current one is reduced (FP64).
+// Persistent CTAs walk (column tile, plane) pairs; with dbl (FP64, when two
+// tiles fit) the next pair's tile is staged asynchronously while the
+// current one is reduced.
 template <class A>
 __global__ void __launch_bounds__(256) k_partial_y(const double* __restrict__ W, int m0, int m1, int nk,
                                                    const int* __restrict__ klist, const typename A::R* __restrict__ S,
@@ -252,9 +261,17 @@ __global__ void k_scatter3(const double* __restrict__ src, int na, int nb, int n
   }
 }
 
-// Interior values of the six faces of the block: fx* [k][j], fy* [k][i], fz* [j][i].
-__global__ void k_extract_faces(const double* __restrict__ s, int NX, int NY, int NZ, double* __restrict__ fx0,
-                                double* __restrict__ fxN, double* __restrict__ fy0, double* __restrict__ fyN,
+// The first and last interior layers' sines along an axis of m nodes are
+// sin(pi (p+1)/(m+1)) and sin(pi m (p+1)/(m+1)) = (-1)^p sin(pi (p+1)/(m+1)),
+// so a pair of opposite faces enters mode p of the sweep as its sum (p
+// even) or its difference (p odd) times the first layer's sine.  The face
+// extractions below store the x and y pairs that way (the transforms along
+// the faces' own axes are linear): one FMA per axis and node in the sweep.
+//
+// Interior values of the six faces of the block: x pair (sum, difference)
+// [k][j], y pair [k][i], z faces [j][i].
+__global__ void k_extract_faces(const double* __restrict__ s, int NX, int NY, int NZ, double* __restrict__ fxs,
+                                double* __restrict__ fxd, double* __restrict__ fys, double* __restrict__ fyd,
                                 double* __restrict__ fz0, double* __restrict__ fzN) {
   const int m0 = NX - 2, m1 = NY - 2, m2 = NZ - 2;
   const size_t sy = NX, sz = (size_t)NX * NY;
@@ -262,13 +279,15 @@ __global__ void k_extract_faces(const double* __restrict__ s, int NX, int NY, in
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nx + ny + nz; t += (long)gridDim.x * blockDim.x) {
     if (t < nx) {
       const int j = (int)(t % m1) + 1, k = (int)(t / m1) + 1;
-      fx0[t] = s[sy * j + sz * k];
-      fxN[t] = s[(NX - 1) + sy * j + sz * k];
+      const double a = s[sy * j + sz * k], b = s[(NX - 1) + sy * j + sz * k];
+      fxs[t] = a + b;
+      fxd[t] = a - b;
     } else if (t < nx + ny) {
       const long u = t - nx;
       const int i = (int)(u % m0) + 1, k = (int)(u / m0) + 1;
-      fy0[u] = s[i + sz * k];
-      fyN[u] = s[i + sy * (NY - 1) + sz * k];
+      const double a = s[i + sz * k], b = s[i + sy * (NY - 1) + sz * k];
+      fys[u] = a + b;
+      fyd[u] = a - b;
     } else {
       const long u = t - nx - ny;
       const int i = (int)(u % m0) + 1, j = (int)(u / m0) + 1;
@@ -279,10 +298,11 @@ __global__ void k_extract_faces(const double* __restrict__ s, int NX, int NY, in
 }
 
 // The six faces of the box whose node (0,0,0) sits at (o0,o1,o2) of an
-// NX x NY x * array, interior m0 x m1 x m2: fx* [k][j], fy* [k][i], fz* [j][i].
+// NX x NY x * array, interior m0 x m1 x m2: x pair (sum, difference) [k][j],
+// y pair [k][i], z faces [j][i].
 __global__ void k_extract_box_faces(const double* __restrict__ s, int NX, int NY, int o0, int o1, int o2, int m0,
-                                    int m1, int m2, double* __restrict__ fx0, double* __restrict__ fxN,
-                                    double* __restrict__ fy0, double* __restrict__ fyN, double* __restrict__ fz0,
+                                    int m1, int m2, double* __restrict__ fxs, double* __restrict__ fxd,
+                                    double* __restrict__ fys, double* __restrict__ fyd, double* __restrict__ fz0,
                                     double* __restrict__ fzN) {
   const size_t sy = NX, sz = (size_t)NX * NY;
   const long nx = (long)m1 * m2, ny = (long)m0 * m2, nz = (long)m0 * m1;
@@ -290,13 +310,15 @@ __global__ void k_extract_box_faces(const double* __restrict__ s, int NX, int NY
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nx + ny + nz; t += (long)gridDim.x * blockDim.x) {
     if (t < nx) {
       const int j = (int)(t % m1) + 1, k = (int)(t / m1) + 1;
-      fx0[t] = at(0, j, k);
-      fxN[t] = at(m0 + 1, j, k);
+      const double a = at(0, j, k), b = at(m0 + 1, j, k);
+      fxs[t] = a + b;
+      fxd[t] = a - b;
     } else if (t < nx + ny) {
       const long u = t - nx;
       const int i = (int)(u % m0) + 1, k = (int)(u / m0) + 1;
-      fy0[u] = at(i, 0, k);
-      fyN[u] = at(i, m1 + 1, k);
+      const double a = at(i, 0, k), b = at(i, m1 + 1, k);
+      fys[u] = a + b;
+      fyd[u] = a - b;
     } else {
       const long u = t - nx - ny;
       const int i = (int)(u % m0) + 1, j = (int)(u / m0) + 1;
@@ -307,8 +329,8 @@ __global__ void k_extract_box_faces(const double* __restrict__ s, int NX, int NY
 }
 
 struct FaceTerms {
-  const double *fx0, *fxN, *fy0, *fyN, *fz0, *fzN;  // transforms: [k][q], [k][p], [q][p]
-  const double *ex1, *exN, *ey1, *eyN;              // sin(pi (p+1)/N), sin(pi m (p+1)/N)
+  const double *fxs, *fxd, *fys, *fyd, *fz0, *fzN;  // transforms: [k][q], [k][p], [q][p]
+  const double *ex1, *ey1;                          // sin(pi (p+1)/(m+1)) along x and y
   double cx, cy, cz;                                // -scale / h^2
 };
 
@@ -323,18 +345,18 @@ __global__ void k_thomas_faces(const double* __restrict__ g, double* __restrict_
   const int p = pq % m0, q = pq / m0;
   const size_t plane = (size_t)m0 * m1;
   auto rinv = [&](size_t id) { return rinvt[id]; };
-  double ax = 0.0, bx = 0.0, ay = 0.0, by = 0.0;
+  double ax = 0.0, ay = 0.0;
+  const double *fx = nullptr, *fy = nullptr;
   if (bc) {
     ax = F.cx * F.ex1[p];
-    bx = F.cx * F.exN[p];
     ay = F.cy * F.ey1[q];
-    by = F.cy * F.eyN[q];
+    fx = (p & 1) ? F.fxd : F.fxs;  // the x pair's sum (p even) or difference
+    fy = (q & 1) ? F.fyd : F.fys;
   }
   auto rhs = [&](int k) -> double {
     double r = g[pq + plane * k];
     if (bc) {
-      r += ax * F.fx0[(size_t)k * m1 + q] + bx * F.fxN[(size_t)k * m1 + q];
-      r += ay * F.fy0[(size_t)k * m0 + p] + by * F.fyN[(size_t)k * m0 + p];
+      r = fma(ay, fy[(size_t)k * m0 + p], fma(ax, fx[(size_t)k * m1 + q], r));
       if (k == 0) r += F.cz * F.fz0[pq];
       if (k == m2 - 1) r += F.cz * F.fzN[pq];
     }
@@ -426,16 +448,20 @@ size_t g_partial_smem = 0;  // dynamic shared memory granted to k_partial_x so f
 
 // Raises k_partial_x's shared-memory limit (called at set-up, outside any
 // stream capture).  Both arithmetics stage 8 bytes per value.
-// Tile height of k_partial_x: the most lines (up to kLines) whose two
-// staged tiles and the sine rows fit in a CTA's shared memory.
-int partial_x_lines(int m0, int nsel) {
+// k_partial_x's shared memory: the sine rows and one or two (dbl) tiles.
+size_t partial_x_smem(int m0, int nsel, int lines, bool dbl) {
+  return sizeof(double) * ((dbl ? 2 : 1) * (size_t)lines * m0 + (size_t)nsel * m0);
+}
+// Tile height of k_partial_x: the most lines (up to kLines) whose staged
+// tiles and the sine rows fit in a CTA's shared memory.
+int partial_x_lines(int m0, int nsel, bool dbl) {
   int lines = kLines;
-  while (lines > 1 && sizeof(double) * (2 * (size_t)lines * m0 + (size_t)nsel * m0) > 227 * 1024) lines /= 2;
+  while (lines > 1 && partial_x_smem(m0, nsel, lines, dbl) > 227 * 1024) lines /= 2;
   return lines;
 }
 
 void partial_x_reserve(int m0, int nsel) {
-  const size_t sm = sizeof(double) * (2 * (size_t)partial_x_lines(m0, nsel) * m0 + (size_t)nsel * m0);
+  const size_t sm = partial_x_smem(m0, nsel, partial_x_lines(m0, nsel, true), true);
   VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
   // the whole per-CTA maximum: every call's tile height keeps it within
   const size_t cap = 227 * 1024;
@@ -449,17 +475,18 @@ void partial_x_reserve(int m0, int nsel) {
 void partial_x(int arith, const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel,
                double* out, cudaStream_t s) {
   const int nlines = m1 * nk;
-  const int lines = partial_x_lines(m0, nsel);
-  const size_t sm = sizeof(double) * (2 * (size_t)lines * m0 + (size_t)nsel * m0);
+  const bool dbl = arith != VPMG_ARITH_FF48;
+  const int lines = partial_x_lines(m0, nsel, dbl);
+  const size_t sm = partial_x_smem(m0, nsel, lines, dbl);
   VPMG_CHECK(sm <= g_partial_smem, VPMG_ERR_STATE, "k_partial_x shared memory not reserved");
   // persistent CTAs: as many as fit on the SMs at this shared-memory size
   const unsigned ntiles = (nlines + lines - 1) / lines;
   const unsigned per_sm = (unsigned)std::max<size_t>(1, std::min<size_t>(8, (227 * 1024) / (sm + 1024)));
   const unsigned g = std::min(ntiles, 152u * per_sm);
   if (arith == VPMG_ARITH_FF48)
-    k_partial_x<FF><<<g, 128, sm, s>>>(W, m0, m1, nk, klist, reinterpret_cast<const float2*>(S), nsel, out, lines);
+    k_partial_x<FF><<<g, 128, sm, s>>>(W, m0, m1, nk, klist, reinterpret_cast<const float2*>(S), nsel, out, lines, 0);
   else
-    k_partial_x<F64><<<g, 128, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out, lines);
+    k_partial_x<F64><<<g, 128, sm, s>>>(W, m0, m1, nk, klist, S, nsel, out, lines, 1);
   VPMG_LAUNCHED();
 }
 
@@ -482,7 +509,7 @@ void partial_y_reserve(int m1) {
 
 void partial_y(int arith, const double* W, int m0, int m1, int nk, const int* klist, const double* S, int nsel,
                double* out, cudaStream_t s, const double* S2 = nullptr, int nsel2 = 0, double* out2 = nullptr) {
-  const int dbl = partial_y_dbl(m1) ? 1 : 0;
+  const int dbl = (arith != VPMG_ARITH_FF48 && partial_y_dbl(m1)) ? 1 : 0;
   const size_t sm = partial_y_smem(m1, dbl);  // tiles + partial sums of 8 rows
   VPMG_CHECK(sm <= g_partial_y_smem, VPMG_ERR_STATE, "k_partial_y shared memory not reserved");
   // persistent CTAs: as many as fit on the SMs at this shared-memory size
@@ -548,15 +575,15 @@ void BlockSolve::prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoar
   up(l_sz, sz);  // plane list (interior index) for the y dots
   std::vector<int> idz(sz);
   up(l_idz, plus1(idz));  // node list for the scatter
-  // first/last layer sines for the face terms
-  auto edge = [&](int mm, bool last) {
+  // first layer sines for the face terms
+  auto edge = [&](int mm) {
     std::vector<double> e(mm);
     const double N = mm + 1;
-    for (int p = 0; p < mm; ++p) e[p] = std::sin(kPI * (double)(last ? mm : 1) * (double)(p + 1) / N);
+    for (int p = 0; p < mm; ++p) e[p] = std::sin(kPI * (double)(p + 1) / N);
     return e;
   };
-  up(e_x1, edge(m[0], false)); up(e_xN, edge(m[0], true));
-  up(e_y1, edge(m[1], false)); up(e_yN, edge(m[1], true));
+  up(e_x1, edge(m[0]));
+  up(e_y1, edge(m[1]));
   partial_x_reserve(m[0], std::max(8, nsx));
   partial_y_reserve(m[1]);
   X8.ensure((size_t)8 * m[1] * m[2]);
@@ -565,8 +592,8 @@ void BlockSolve::prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoar
   Y1.ensure((size_t)m[0] * 2 * m[2]);
   Ys.ensure((size_t)m[0] * nsy * nsz);
   XS.ensure((size_t)nsx * nsy * nsz);
-  fx0.ensure((size_t)m[1] * m[2]); fxN.ensure((size_t)m[1] * m[2]);
-  fy0.ensure((size_t)m[0] * m[2]); fyN.ensure((size_t)m[0] * m[2]);
+  fxs.ensure((size_t)m[1] * m[2]); fxd.ensure((size_t)m[1] * m[2]);
+  fys.ensure((size_t)m[0] * m[2]); fyd.ensure((size_t)m[0] * m[2]);
   fz0.ensure((size_t)m[0] * m[1]); fzN.ensure((size_t)m[0] * m[1]);
   ready = true;
 }
@@ -607,22 +634,22 @@ void block_solve_bc(BlockSolve& B, DirichletPlan& P, int c, double* sol_c, cudaS
   const int m0 = B.m[0], m1 = B.m[1], m2 = B.m[2];
   const size_t nint = (size_t)m0 * m1 * m2, plane = (size_t)m0 * m1;
   // boundary values of the faces, transformed along the face's axes
-  k_extract_faces<<<256, 256, 0, s>>>(sol_c, B.dims[0], B.dims[1], B.dims[2], B.fx0.p, B.fxN.p, B.fy0.p, B.fyN.p,
+  k_extract_faces<<<256, 256, 0, s>>>(sol_c, B.dims[0], B.dims[1], B.dims[2], B.fxs.p, B.fxd.p, B.fys.p, B.fyd.p,
                                       B.fz0.p, B.fzN.p);
   VPMG_LAUNCHED();
   // transformed along the face's axes: rows over j -> q (x faces), over i ->
   // p (y faces, and the z faces' rows), in one launch; then the z faces'
   // columns over j
-  const DstYLines rows[6] = {{&P.fy, B.fx0.p, 1, m1, m2}, {&P.fy, B.fxN.p, 1, m1, m2},
-                             {&P.fx, B.fy0.p, 1, m0, m2}, {&P.fx, B.fyN.p, 1, m0, m2},
+  const DstYLines rows[6] = {{&P.fy, B.fxs.p, 1, m1, m2}, {&P.fy, B.fxd.p, 1, m1, m2},
+                             {&P.fx, B.fys.p, 1, m0, m2}, {&P.fx, B.fyd.p, 1, m0, m2},
                              {&P.fx, B.fz0.p, 1, m0, m1}, {&P.fx, B.fzN.p, 1, m0, m1}};
   dst_lines_y_jobs(rows, 6, s);
   const DstYLines cols[2] = {{&P.fy, B.fz0.p, m0, m1, 1}, {&P.fy, B.fzN.p, m0, m1, 1}};
   dst_lines_y_jobs(cols, 2, s);
   const double scale = dirichlet_scale(P);
   FaceTerms F;
-  F.fx0 = B.fx0.p; F.fxN = B.fxN.p; F.fy0 = B.fy0.p; F.fyN = B.fyN.p; F.fz0 = B.fz0.p; F.fzN = B.fzN.p;
-  F.ex1 = B.e_x1.p; F.exN = B.e_xN.p; F.ey1 = B.e_y1.p; F.eyN = B.e_yN.p;
+  F.fxs = B.fxs.p; F.fxd = B.fxd.p; F.fys = B.fys.p; F.fyd = B.fyd.p; F.fz0 = B.fz0.p; F.fzN = B.fzN.p;
+  F.ex1 = B.e_x1.p; F.ey1 = B.e_y1.p;
   F.cx = -scale / (P.h[0] * P.h[0]);
   F.cy = -scale / (P.h[1] * P.h[1]);
   F.cz = -scale / (P.h[2] * P.h[2]);
@@ -662,15 +689,9 @@ void block_solve_bc(BlockSolve& B, DirichletPlan& P, int c, double* sol_c, cudaS
 void FaceSolve::prepare(const DirichletPlan& P) {
   const int m0 = P.m[0], m1 = P.m[1], m2 = P.m[2];
   f.ensure(2 * ((size_t)m1 * m2 + (size_t)m0 * m2 + (size_t)m0 * m1));
-  std::vector<double> e(2 * (size_t)m0 + 2 * (size_t)m1);
-  for (int p = 0; p < m0; ++p) {
-    e[p] = std::sin(kPI * (double)(p + 1) / (double)(m0 + 1));
-    e[m0 + p] = std::sin(kPI * (double)m0 * (double)(p + 1) / (double)(m0 + 1));
-  }
-  for (int q = 0; q < m1; ++q) {
-    e[2 * m0 + q] = std::sin(kPI * (double)(q + 1) / (double)(m1 + 1));
-    e[2 * m0 + m1 + q] = std::sin(kPI * (double)m1 * (double)(q + 1) / (double)(m1 + 1));
-  }
+  std::vector<double> e((size_t)m0 + (size_t)m1);
+  for (int p = 0; p < m0; ++p) e[p] = std::sin(kPI * (double)(p + 1) / (double)(m0 + 1));
+  for (int q = 0; q < m1; ++q) e[m0 + q] = std::sin(kPI * (double)(q + 1) / (double)(m1 + 1));
   this->e.ensure(e.size());
   VPMG_CUDA(cudaMemcpy(this->e.p, e.data(), sizeof(double) * e.size(), cudaMemcpyHostToDevice));
   ready = true;
@@ -684,25 +705,25 @@ void dirichlet_solve_faces(DirichletPlan& P, FaceSolve& FS, const double* rhs, d
   // forward transforms of the RHS alone (zero tiles skip their FFTs)
   dst_forward_xy(P, rhs, nullptr, true, work, s);
   // the faces' values, transformed along their own axes
-  double* fx0 = FS.f.p;
-  double* fxN = fx0 + (size_t)m1 * m2;
-  double* fy0 = fxN + (size_t)m1 * m2;
-  double* fyN = fy0 + (size_t)m0 * m2;
-  double* fz0 = fyN + (size_t)m0 * m2;
+  double* fxs = FS.f.p;
+  double* fxd = fxs + (size_t)m1 * m2;
+  double* fys = fxd + (size_t)m1 * m2;
+  double* fyd = fys + (size_t)m0 * m2;
+  double* fz0 = fyd + (size_t)m0 * m2;
   double* fzN = fz0 + (size_t)m0 * m1;
-  k_extract_box_faces<<<256, 256, 0, s>>>(sol, P.dims[0], P.dims[1], P.box[0], P.box[1], P.box[2], m0, m1, m2, fx0,
-                                          fxN, fy0, fyN, fz0, fzN);
+  k_extract_box_faces<<<256, 256, 0, s>>>(sol, P.dims[0], P.dims[1], P.box[0], P.box[1], P.box[2], m0, m1, m2, fxs,
+                                          fxd, fys, fyd, fz0, fzN);
   VPMG_LAUNCHED();
-  const DstYLines rows[6] = {{&P.fy, fx0, 1, m1, m2}, {&P.fy, fxN, 1, m1, m2}, {&P.fx, fy0, 1, m0, m2},
-                             {&P.fx, fyN, 1, m0, m2}, {&P.fx, fz0, 1, m0, m1}, {&P.fx, fzN, 1, m0, m1}};
+  const DstYLines rows[6] = {{&P.fy, fxs, 1, m1, m2}, {&P.fy, fxd, 1, m1, m2}, {&P.fx, fys, 1, m0, m2},
+                             {&P.fx, fyd, 1, m0, m2}, {&P.fx, fz0, 1, m0, m1}, {&P.fx, fzN, 1, m0, m1}};
   dst_lines_y_jobs(rows, 6, s);
   const DstYLines cols[2] = {{&P.fy, fz0, m0, m1, 1}, {&P.fy, fzN, m0, m1, 1}};
   dst_lines_y_jobs(cols, 2, s);
   // the sweep with the face terms, then the full inverse transforms
   const double scale = dirichlet_scale(P);
   FaceTerms F;
-  F.fx0 = fx0; F.fxN = fxN; F.fy0 = fy0; F.fyN = fyN; F.fz0 = fz0; F.fzN = fzN;
-  F.ex1 = FS.e.p; F.exN = FS.e.p + m0; F.ey1 = FS.e.p + 2 * m0; F.eyN = FS.e.p + 2 * m0 + m1;
+  F.fxs = fxs; F.fxd = fxd; F.fys = fys; F.fyd = fyd; F.fz0 = fz0; F.fzN = fzN;
+  F.ex1 = FS.e.p; F.ey1 = FS.e.p + m0;
   F.cx = -scale / (P.h[0] * P.h[0]);
   F.cy = -scale / (P.h[1] * P.h[1]);
   F.cz = -scale / (P.h[2] * P.h[2]);

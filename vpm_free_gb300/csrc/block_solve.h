@@ -16,10 +16,12 @@ struct BlockSolve {
   // sine rows sin(pi (i+1)(p+1)/N) of the selected interior indices, one
   // 8-byte word each: a double, or a float-float pair (arith)
   DBuf<double> S_fx, S_fy_lo, S_fy_hi, S_ix, S_iy_lo, S_iy_hi, S_sx, S_sy;
-  DBuf<double> e_x1, e_xN, e_y1, e_yN;  // sines of the first/last interior layer
+  DBuf<double> e_x1, e_y1;  // sines of the first interior layer along x and y
   DBuf<int> l_fx, l_ix, l_sx, l_sy, l_sz, l_idy, l_idz;  // node lists for scatters / plane lists
   DBuf<double> X8, Y4, X2, Y1, Ys, XS;  // compact partial results
-  DBuf<double> fx0, fxN, fy0, fyN, fz0, fzN;  // Dirichlet face values -> their transforms
+  // Dirichlet face values -> their transforms: the x and y pairs as (sum,
+  // difference), the z faces as they are
+  DBuf<double> fxs, fxd, fys, fyd, fz0, fzN;
   int inner_lo[3] = {0, 0, 0}, inner_hi[3] = {0, 0, 0};  // interior indices of the inner-box faces
   void prepare(const DirichletPlan& P, const int nnbl_bl[6], int ncoarse);
 };
@@ -32,7 +34,7 @@ struct BlockSolve {
 struct FaceSolve {
   bool ready = false;
   DBuf<double> f;   // the six faces' values, then their transforms
-  DBuf<double> e;   // sines of the first and last interior layer along x and y
+  DBuf<double> e;   // sines of the first interior layer along x and y
   void prepare(const DirichletPlan& P);
 };
 void dirichlet_solve_faces(DirichletPlan& P, FaceSolve& F, const double* rhs, double* sol, double* work,
