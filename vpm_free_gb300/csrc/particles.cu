@@ -270,8 +270,8 @@ __global__ void k_records64(const double* __restrict__ x, const double* __restri
 // particles of the (ips+ipf+1)^2 cell rows (cj, ck) covering it, in the
 // cell range [n - ipf, n + ips] of each row: its visits, enumerated in
 // (row, sorted slot) order.  The warp's visits (node by node) are split
-// into 32 equal chunks, one per lane, so every lane does a visit per trip
-// (1 DMUL + 3 DFMA) instead of idling while a neighbour with more particles
+// into 32 equal chunks, one per lane, so every lane does two visits per trip
+// (2 DMUL + 6 DFMA) instead of idling while a neighbour with more particles
 // finishes.  A lane's running sums are flushed where its chunk leaves a
 // node: the first and last node it touches as pieces, nodes it covers
 // entirely as totals.  Each node then adds its pieces in lane order: a
@@ -381,33 +381,30 @@ __global__ void __launch_bounds__(kDepWarps * 32) k_deposit64(const int* __restr
     while (t >= nb && kc < 3) { ++kc; nb = kc == 1 ? e2 : kc == 2 ? e3 : e4; }
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     for (int v = v0; v < v1;) {
+      // two visits of this row per trip, their loads in flight together.
+      // Where the row or the chunk has one visit left, the second is the
+      // same slot with a zero weight: every lane runs the same FP64
+      // instructions (a partly masked one costs the pipe a full issue), and
+      // fma(0, q, a) = a keeps the sums those of the visits one by one.
       const int ix = ii - (xl + kc) + m.ips;
-      if (v + 1 < v1 && t + 1 < te) {
-        // two visits of this row at once, their loads in flight together;
-        // the sums take them in the same order as one by one
-        int kc2 = kc, nb2 = nb;
-        while (t + 1 >= nb2 && kc2 < 3) { ++kc2; nb2 = kc2 == 1 ? e2 : kc2 == 2 ? e3 : e4; }
-        const int ix2 = ii - (xl + kc2) + m.ips;
-        const double wa = __ldg(&rec[ix * cs + t]), wb = __ldg(&rec[ix2 * cs + t + 1]);
-        const double ya = __ldg(&rec[wyz_slot * cs + t]), yb = __ldg(&rec[wyz_slot * cs + t + 1]);
-        const double qa0 = __ldg(&q0[t]), qa1 = __ldg(&q1[t]), qa2 = __ldg(&q2[t]);
-        const double qb0 = __ldg(&q0[t + 1]), qb1 = __ldg(&q1[t + 1]), qb2 = __ldg(&q2[t + 1]);
-        const double fa = wa * ya, fb = wb * yb;
-        a0 = fma(fb, qb0, fma(fa, qa0, a0));
-        a1 = fma(fb, qb1, fma(fa, qa1, a1));
-        a2 = fma(fb, qb2, fma(fa, qa2, a2));
-        t += 2;
-        v += 2;
-        kc = kc2;
-        nb = nb2;
-      } else {
-        const double f = __ldg(&rec[ix * cs + t]) * __ldg(&rec[wyz_slot * cs + t]);
-        a0 = fma(f, __ldg(&q0[t]), a0);
-        a1 = fma(f, __ldg(&q1[t]), a1);
-        a2 = fma(f, __ldg(&q2[t]), a2);
-        ++t;
-        ++v;
-      }
+      const bool two = v + 1 < v1 && t + 1 < te;
+      const int t2 = two ? t + 1 : t;
+      int kc2 = kc, nb2 = nb;
+      while (t2 >= nb2 && kc2 < 3) { ++kc2; nb2 = kc2 == 1 ? e2 : kc2 == 2 ? e3 : e4; }
+      const int ix2 = ii - (xl + kc2) + m.ips;
+      const double wa = __ldg(&rec[ix * cs + t]), wb = __ldg(&rec[ix2 * cs + t2]);
+      const double ya = __ldg(&rec[wyz_slot * cs + t]), yb = __ldg(&rec[wyz_slot * cs + t2]);
+      const double qa0 = __ldg(&q0[t]), qa1 = __ldg(&q1[t]), qa2 = __ldg(&q2[t]);
+      const double qb0 = __ldg(&q0[t2]), qb1 = __ldg(&q1[t2]), qb2 = __ldg(&q2[t2]);
+      const double fa = wa * ya, fb = two ? wb * yb : 0.0;
+      a0 = fma(fb, qb0, fma(fa, qa0, a0));
+      a1 = fma(fb, qb1, fma(fa, qa1, a1));
+      a2 = fma(fb, qb2, fma(fa, qa2, a2));
+      const int step = two ? 2 : 1;
+      t += step;
+      v += step;
+      kc = kc2;
+      nb = nb2;
       if (t < te) {
         while (t >= nb && kc < 3) { ++kc; nb = kc == 1 ? e2 : kc == 2 ? e3 : e4; }
         continue;
