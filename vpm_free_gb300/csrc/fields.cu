@@ -13,16 +13,16 @@ namespace vpmg {
 
 namespace {
 
+// One node per thread; blockIdx.y is the plane k, and the threads of a
+// plane run over its e0 x e1 nodes without gaps (one 32-bit division per
+// node, no partly filled CTA per row).
 __global__ void k_box_copy(const double* __restrict__ src, int sx, int sy, int so0, int so1, int so2,
-                           double* __restrict__ dst, int dx, int dy, int do0, int do1, int do2, int e0, int e1, int e2) {
-  const size_t n = (size_t)e0 * e1 * e2;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(t % e0);
-    const int j = (int)((t / e0) % e1);
-    const int k = (int)(t / ((size_t)e0 * e1));
-    dst[(size_t)(do0 + i) + (size_t)dx * ((do1 + j) + (size_t)dy * (do2 + k))] =
-        src[(size_t)(so0 + i) + (size_t)sx * ((so1 + j) + (size_t)sy * (so2 + k))];
-  }
+                           double* __restrict__ dst, int dx, int dy, int do0, int do1, int do2, int e0, int e1) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= e0 * e1) return;
+  const int j = t / e0, i = t - j * e0, k = blockIdx.y;
+  dst[(size_t)(do0 + i) + (size_t)dx * ((do1 + j) + (size_t)dy * (do2 + k))] =
+      src[(size_t)(so0 + i) + (size_t)sx * ((so1 + j) + (size_t)sy * (so2 + k))];
 }
 
 __global__ void k_sample(const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
@@ -216,8 +216,11 @@ void box_copy(const double* src, const int sdims[3], const int so[3], double* ds
               const int ext[3], cudaStream_t s) {
   const size_t n = (size_t)ext[0] * ext[1] * ext[2];
   if (!n) return;
-  k_box_copy<<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 32), 256, 0, s>>>(
-      src, sdims[0], sdims[1], so[0], so[1], so[2], dst, ddims[0], ddims[1], dof[0], dof[1], dof[2], ext[0], ext[1], ext[2]);
+  VPMG_CHECK(ext[2] <= 65535 && (size_t)ext[0] * ext[1] <= (size_t)INT32_MAX, VPMG_ERR_UNSUPPORTED,
+             "box copy extent above the grid limit");
+  const dim3 grid((unsigned)(((size_t)ext[0] * ext[1] + 255) / 256), (unsigned)ext[2]);
+  k_box_copy<<<grid, 256, 0, s>>>(src, sdims[0], sdims[1], so[0], so[1], so[2], dst, ddims[0], ddims[1], dof[0], dof[1],
+                                  dof[2], ext[0], ext[1]);
   VPMG_LAUNCHED();
   VPMG_CUDA(cudaGetLastError());
 }
