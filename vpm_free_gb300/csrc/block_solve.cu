@@ -444,11 +444,22 @@ std::vector<int> plus1(const std::vector<int>& v) {
   return r;
 }
 
-size_t g_partial_smem = 0;  // dynamic shared memory granted to k_partial_x so far
+// Dynamic shared memory granted to k_partial_x and k_partial_y so far, per
+// device: the limit is an attribute of each kernel on each device, and one
+// process may hold handles on several devices.  Raised at set-up only
+// (outside any stream capture), never lowered.
+constexpr int kMaxDev = 64;
+size_t g_partial_smem[kMaxDev] = {0};
+size_t g_partial_y_smem[kMaxDev] = {0};
+size_t& granted(size_t* table) {
+  int dev = 0;
+  VPMG_CUDA(cudaGetDevice(&dev));
+  VPMG_CHECK(dev >= 0 && dev < kMaxDev, VPMG_ERR_UNSUPPORTED, "device index beyond the per-device tables");
+  return table[dev];
+}
 
-// Raises k_partial_x's shared-memory limit (called at set-up, outside any
-// stream capture).  Both arithmetics stage 8 bytes per value.
-// k_partial_x's shared memory: the sine rows and one or two (dbl) tiles.
+// k_partial_x's shared memory: the sine rows and one or two (dbl) tiles,
+// 8 bytes per value in both arithmetics.
 size_t partial_x_smem(int m0, int nsel, int lines, bool dbl) {
   return sizeof(double) * ((dbl ? 2 : 1) * (size_t)lines * m0 + (size_t)nsel * m0);
 }
@@ -465,10 +476,11 @@ void partial_x_reserve(int m0, int nsel) {
   VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
   // the whole per-CTA maximum: every call's tile height keeps it within
   const size_t cap = 227 * 1024;
-  if (cap > g_partial_smem) {
+  size_t& have = granted(g_partial_smem);
+  if (cap > have) {
     VPMG_CUDA(cudaFuncSetAttribute(k_partial_x<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
     VPMG_CUDA(cudaFuncSetAttribute(k_partial_x<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
-    g_partial_smem = cap;
+    have = cap;
   }
 }
 
@@ -478,7 +490,7 @@ void partial_x(int arith, const double* W, int m0, int m1, int nk, const int* kl
   const bool dbl = arith != VPMG_ARITH_FF48;
   const int lines = partial_x_lines(m0, nsel, dbl);
   const size_t sm = partial_x_smem(m0, nsel, lines, dbl);
-  VPMG_CHECK(sm <= g_partial_smem, VPMG_ERR_STATE, "k_partial_x shared memory not reserved");
+  VPMG_CHECK(sm <= granted(g_partial_smem), VPMG_ERR_STATE, "k_partial_x shared memory not reserved");
   // persistent CTAs: as many as fit on the SMs at this shared-memory size
   const unsigned ntiles = (nlines + lines - 1) / lines;
   const unsigned per_sm = (unsigned)std::max<size_t>(1, std::min<size_t>(8, (227 * 1024) / (sm + 1024)));
@@ -490,8 +502,6 @@ void partial_x(int arith, const double* W, int m0, int m1, int nk, const int* kl
   VPMG_LAUNCHED();
 }
 
-size_t g_partial_y_smem = 0;  // dynamic shared memory granted to k_partial_y so far
-
 // k_partial_y's shared memory: one or two column tiles and the partial sums
 // of 8 rows; two tiles (double buffering) when they fit.
 size_t partial_y_smem(int m1, bool dbl) { return sizeof(double) * ((dbl ? 2 : 1) * (size_t)m1 + 8) * kColTile; }
@@ -500,10 +510,11 @@ bool partial_y_dbl(int m1) { return partial_y_smem(m1, true) <= 227 * 1024; }
 void partial_y_reserve(int m1) {
   const size_t sm = partial_y_smem(m1, partial_y_dbl(m1));
   VPMG_CHECK(sm <= 227 * 1024, VPMG_ERR_UNSUPPORTED, "partial transform tile too large");
-  if (sm > g_partial_y_smem) {
+  size_t& have = granted(g_partial_y_smem);
+  if (sm > have) {
     VPMG_CUDA(cudaFuncSetAttribute(k_partial_y<F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     VPMG_CUDA(cudaFuncSetAttribute(k_partial_y<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    g_partial_y_smem = sm;
+    have = sm;
   }
 }
 
@@ -511,7 +522,7 @@ void partial_y(int arith, const double* W, int m0, int m1, int nk, const int* kl
                double* out, cudaStream_t s, const double* S2 = nullptr, int nsel2 = 0, double* out2 = nullptr) {
   const int dbl = (arith != VPMG_ARITH_FF48 && partial_y_dbl(m1)) ? 1 : 0;
   const size_t sm = partial_y_smem(m1, dbl);  // tiles + partial sums of 8 rows
-  VPMG_CHECK(sm <= g_partial_y_smem, VPMG_ERR_STATE, "k_partial_y shared memory not reserved");
+  VPMG_CHECK(sm <= granted(g_partial_y_smem), VPMG_ERR_STATE, "k_partial_y shared memory not reserved");
   // persistent CTAs: as many as fit on the SMs at this shared-memory size
   const unsigned ntiles = (unsigned)(((m0 + kColTile - 1) / kColTile) * nk);
   const unsigned per_sm = (unsigned)std::max<size_t>(1, std::min<size_t>(8, (227 * 1024) / (sm + 1024)));
