@@ -151,6 +151,17 @@ def _workload(name="leapfrog256"):
     return W.leapfrog256()
 
 
+def workload_config(name, nn, nnbl, blocks):
+    """The `config` object both arms print: the workload and its sizes
+    (define_sizes' mesh and padded block), nothing about how it runs."""
+    desc = ("leapfrog256 (two coaxial rings, 256^3 mesh, M4', tree levels 3, ncoarse 8, remesh every step, "
+            "dt 0.005)") if name == "leapfrog256" else name
+    field_mb = float(np.prod(nn)) * 8 / 1e6
+    return {"workload": desc, "mesh": [int(n) - 1 for n in nn], "block": [int(n) for n in nnbl],
+            "yaps_blocks": [int(b) for b in blocks],
+            "l2": f"inputs larger than L2 (each field component {field_mb:.0f} MB, and the recorded boundary operator)"}
+
+
 def _measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -370,13 +381,16 @@ def run_reference(args, dist):
     if warm:
         cpu_step_sample(xp, qp, w, warm, threads)
     v, t, ps = cpu_step_sample(xp, qp, w, steps, threads)
+    from oracle import oracle as O
+    sz = O.define_sizes(O.make_config(dpm=w["dpm"], box=w["box"], ompthreads=threads), xp)
     sample = (f"{steps} full steps (field step + Euler + remesh) of the 256^3 leapfrog workload after {warm} warm-up "
               f"step(s); oracle = C++ restatement of the reference's CPU path (Fortran/MPI/MKL original not buildable)")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
         "warmup": warm, "ms_per_step": 1e3 * t / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded leapfrogging rings)",
-        "config": {"workload": "leapfrog256", "mesh": [256, 256, 256], "parallelism": "host threads"},
+        "config": workload_config("leapfrog256", list(sz.nn), list(sz.nnbl), (1, 1, 1)),
+        "parallelism": "host threads",
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -605,13 +619,9 @@ def run_ours(args, dist):
         "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.arith == "fp64" else "ff48", "data": "synthetic (seeded leapfrogging rings)",
         "arithmetic": arith_text,
-        "config": {"workload": ("leapfrog256 (two coaxial rings, 256^3 mesh, M4', tree levels 3, ncoarse 8, remesh "
-                                "every step, dt 0.005)") if args.workload == "leapfrog256" else args.workload,
-                   "mesh": [n - 1 for n in sizes_nn], "block": sizes_bl, "yaps_blocks": list(blocks),
-                   "particles_start": int(xr.shape[0]), "particles_end": np_end,
-                   "l2": ("inputs larger than L2 (each field component 135 MB, recorded boundary operator "
-                          f"{tree.get('bytes', 0) / 1e9:.1f} GB)"),
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "config": workload_config(args.workload, sizes_nn, sizes_bl, blocks),
+        "parallelism": "replicas" if ws > 1 else "single GPU",
+        "particles": {"start": int(xr.shape[0]), "end": np_end},
         "clocks": clk if rank == 0 else None,
         "setup_s": setup_s, "hbm_bytes": hbm_bytes,
         "setup": "define_sizes (plans, DST tile autotuning, tree geometry, recorded boundary operator) and the "
