@@ -50,7 +50,7 @@ def build(verbose=False, force=False):
     """Compiles every translation unit (parallel) and links libvpmg.so."""
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(HERE, "..", "include", "vpmg.h"))
     jobs = []
     for f in CU:
